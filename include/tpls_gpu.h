@@ -1,0 +1,271 @@
+/*
+ * tpls_gpu.h -- C ABI of the GB300 implementation of the TPLS per-timestep
+ * hot path (level-set advection, redistancing, CSF, momentum operator with
+ * Jacobi / red-black SOR Crank-Nicolson sweeps, pressure Poisson solve,
+ * projection).
+ *
+ * Conventions (chosen so a Fortran driver can bind every entry with
+ * ISO_C_BINDING without wrappers):
+ *   - every array is the reference's explicit-shape, column-major array of a
+ *     single rank: p-grid (0:nx+1,0:ny+1,0:nz+1), u/v (0:nx+1,0:ny+1,0:nz-1),
+ *     w (0:nx+1,0:ny+1,0:nz), viscosity_aug (-1:nx+2,-1:ny+2,0:nz+1);
+ *   - scalars are passed by reference, in the reference's argument order;
+ *     index bounds (sx, ex, ...) are checked against the context and must be
+ *     the single-rank values; MPI-only arguments (neighbours, communicator,
+ *     derived-datatype handles) are accepted and ignored;
+ *   - every entry returns an int status: 0 = OK, >0 = error (TPLS_ERR_* or a
+ *     CUDA error code + TPLS_ERR_CUDA_BASE), <0 = KSP-style divergence of the
+ *     pressure solve (-3 DIVERGED_ITS, -9 DIVERGED_NAN);
+ *   - calls on one context are single-threaded and stream-ordered; separate
+ *     contexts may be driven from separate host threads.
+ * The per-routine entries take HOST arrays (copied in and out around the
+ * kernels); tpls_step() runs whole timesteps on device-resident state.
+ */
+#ifndef TPLS_GPU_H
+#define TPLS_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TPLS_OK 0
+#define TPLS_ERR_ARG 1         /* bad argument / bounds mismatch */
+#define TPLS_ERR_ALLOC 2       /* device allocation failed */
+#define TPLS_ERR_STATE 3       /* call sequence error */
+#define TPLS_ERR_NOT_BUILT 4   /* feature not available in this build */
+#define TPLS_ERR_CUDA_BASE 1000 /* + cudaError_t */
+#define TPLS_KSP_CONVERGED_RTOL 2
+#define TPLS_KSP_CONVERGED_ATOL 3
+#define TPLS_KSP_DIVERGED_ITS (-3)
+#define TPLS_KSP_DIVERGED_NAN (-9)
+
+#define TPLS_PREC_FP64 0      /* plain FP64 everywhere */
+#define TPLS_PREC_FP32_MIXED 1 /* FP32 stencils/sweeps/smoothing, FP64 state,
+                                  dots, residuals, volume integral, coarse solve */
+
+/* Physical and solver parameters.  Names follow the reference's .opt keys
+ * (option_names.F90) and main_ns_hybrid.F90 variables. */
+typedef struct tpls_params {
+  double dx, dy, dz, dt;          /* dx,dy,dz,dt */
+  double re, mu_plus, mu_minus;   /* re, mu_plus (upper), mu_minus (lower) */
+  double height, scap, smooth_width;
+  int mom_u, mom_v, mom_w;        /* max_iteration_mom_{u,v,w} (outer its = /2) */
+  int levelset;                   /* max_iteration_levelset */
+  double p_rtol;                  /* pressure solve: ||r||_2 <= rtol*||b||_2 */
+  int p_maxits;                   /* pressure solve iteration cap */
+  int precision;                  /* TPLS_PREC_* */
+  int reserved[6];
+} tpls_params;
+
+/* Per-step diagnostics, the quantities the reference logs each timestep
+ * (main_ns_hybrid.F90:601-605, 803-808, 840-845, 882-887, 903-911). */
+typedef struct tpls_stats {
+  double err_phi;   /* last redistancing sum (phi_reinit - updated)^2 */
+  double err_u, err_v, err_w; /* get_difference(u3, u3_old) etc. */
+  double p_rnorm;   /* final ||r||_2 of the pressure solve */
+  double p_bnorm;   /* ||b||_2 of the (projected) pressure right-hand side */
+  int p_its;        /* pressure iterations */
+  int p_reason;     /* KSP-style converged/diverged reason */
+  long steps_done;
+  double liquid_volume; /* sum over cells of (1-H(phi)) dV after the step */
+} tpls_stats;
+
+/* Field identifiers for tpls_set_field / tpls_get_field and the oracle.
+ * Kind P = p-grid, UV = u/v grid, W = w grid (see shapes above). */
+enum tpls_field {
+  TPLS_F_PHI2 = 0,      /* P  */
+  TPLS_F_U2, TPLS_F_V2, /* UV */
+  TPLS_F_W2,            /* W  */
+  TPLS_F_PRES,          /* P  */
+  TPLS_F_PRES_OLD,      /* P  */
+  TPLS_F_CONV0_U, TPLS_F_CONV1_U, TPLS_F_CONV0_V, TPLS_F_CONV1_V, /* UV */
+  TPLS_F_CONV0_W, TPLS_F_CONV1_W,                                 /* W */
+  TPLS_F_CSF_U0, TPLS_F_CSF_U1, TPLS_F_CSF_V0, TPLS_F_CSF_V1,     /* UV */
+  TPLS_F_CSF_W0, TPLS_F_CSF_W1,                                   /* W */
+  TPLS_F_CONV0_PHI, TPLS_F_CONV1_PHI,                             /* P */
+  /* intermediates of the last step (read-only) */
+  TPLS_F_CONV2_PHI,     /* P  */
+  TPLS_F_PHI3,          /* P  */
+  TPLS_F_RHS_P,         /* P  */
+  TPLS_F_U3, TPLS_F_V3, /* UV (before projection) */
+  TPLS_F_W3,            /* W  */
+  TPLS_F_COUNT
+};
+
+typedef struct tpls_ctx tpls_ctx;
+
+/* ---- context ---------------------------------------------------------- */
+/* Replaces the allocation / set-up of main_ns_hybrid.F90:216-549 and
+ * setup_MPI (configure_mpi_petsc.F90:61-212) for one channel on one GPU.
+ * u_inlet has nz entries (u_inlet(0:maxn-2)). */
+int tpls_gpu_create(int nx, int ny, int nz, const tpls_params *prm,
+                    const double *u_inlet, tpls_ctx **out);
+int tpls_gpu_destroy(tpls_ctx *ctx);
+int tpls_set_field(tpls_ctx *ctx, int field, const double *host);
+int tpls_get_field(tpls_ctx *ctx, int field, double *host);
+/* Device-resident fast path: nsteps full timesteps of main_ns_hybrid.F90:
+ * 583-918 followed by the history rotation :2480-2509. */
+int tpls_step(tpls_ctx *ctx, int nsteps);
+int tpls_get_stats(tpls_ctx *ctx, tpls_stats *out);
+int tpls_sync(tpls_ctx *ctx);
+const char *tpls_status_string(int status);
+/* Number of kernels the library has launched on this context (counted on
+ * the host at every launch site). */
+long tpls_kernel_launches(const tpls_ctx *ctx);
+
+/* Reference initial-condition tool restated for the harness:
+ * twophase_initialisation_wave.F90:79-122 base profile (Gauss-Seidel,
+ * 10000 sweeps) -- writes u_oned(0:nz-1). */
+int tpls_base_profile(int nz, double dz, double re, double dpdl,
+                      double mu_minus, double mu_plus, double height,
+                      double smooth_width, double *u_oned);
+
+/* ---- per-routine drop-in entries (host arrays) ------------------------ */
+
+/* advect_phi.f90:19-27  do_advect_phi (incl. weno.f90:18 WENOAppoxConvection) */
+int tpls_do_advect_phi(tpls_ctx *ctx, const double *phi2, double *u2,
+                       double *v2, double *w2, double *conv2_phi,
+                       const int *sx, const int *ex, const int *sy,
+                       const int *ey, const int *sz_p, const int *ez_p,
+                       const int *sz_uv, const int *sz_w, const int *ez_uv,
+                       const int *ez_w, const int *maxl, const int *maxn,
+                       const int *ex_max, const int *neighbours,
+                       const int *comm2d_quasiperiodic, const double *dx,
+                       const double *dy, const double *dz,
+                       const int *stride_p_augaug1_xz,
+                       const int *stride_p_augaug1_yz,
+                       const int *stride_p_augaug2_xz,
+                       const int *stride_p_augaug2_yz,
+                       const int *stride_p_augaug3_xz,
+                       const int *stride_p_augaug3_yz,
+                       const int *stride_uv_xz, const int *stride_uv_yz,
+                       const int *stride_w_xz, const int *stride_w_yz);
+
+/* two_phase_levelset.f90:20-25  do_tpls (AB3 update + redistancing) */
+int tpls_do_tpls(tpls_ctx *ctx, double *phi2, double *phi3,
+                 double *conv0_phi, double *conv1_phi, double *conv2_phi,
+                 const int *sx, const int *ex, const int *sy, const int *ey,
+                 const int *sz_p, const int *ez_p, const int *maxn,
+                 const int *ex_max, const int *stride_p_xz,
+                 const int *stride_p_yz, const int *max_iteration_levelset,
+                 const int *neighbours, const int *comm2d_quasiperiodic,
+                 const double *height, double *err2, const double *dx,
+                 const double *dz, const double *dt);
+
+/* levelset.f90:241-242  get_csf */
+int tpls_get_csf(tpls_ctx *ctx, double *fx_csf, double *fy_csf,
+                 double *fz_csf, const double *fi, const int *sx,
+                 const int *ex, const int *sy, const int *ey, const int *n,
+                 const int *ex_max, const double *dx, const double *dy,
+                 const double *dz, const double *scap,
+                 const double *smooth_width);
+
+/* momentum_allflux.f90:474  get_viscosity, plus the augmented-viscosity
+ * assembly of main_ns_hybrid.F90:646-724 (x ghost planes from phi2 and the
+ * 2-row periodic-y wrap).  viscosity_aug is (-1:nx+2,-1:ny+2,0:nz+1). */
+int tpls_get_viscosity(tpls_ctx *ctx, double *viscosity_aug,
+                       const double *phi, const int *ex, const int *ey,
+                       const int *sx, const int *sy, const int *maxn,
+                       const double *smooth_width, const double *re,
+                       const double *mu_minus, const double *mu_plus);
+
+/* momentum_allflux.f90:224-225  get_conv_all */
+int tpls_get_conv_all(tpls_ctx *ctx, double *conv_u2, double *conv_v2,
+                      double *conv_w2, const double *viscosity_aug,
+                      const double *u2, const double *v2, const double *w2,
+                      const int *sx, const int *sy, const int *ex,
+                      const int *ey, const int *maxn, const int *ex_max,
+                      const double *dx, const double *dy, const double *dz);
+
+/* momentum_allflux.f90:22-23  get_diffusion_all */
+int tpls_get_diffusion_all(tpls_ctx *ctx, double *diff_u, double *diff_v,
+                           double *diff_w, const double *viscosity,
+                           const double *u2, const double *v2,
+                           const double *w2, const int *sx, const int *sy,
+                           const int *ex, const int *ey, const int *maxn,
+                           const int *ex_max, const double *dx,
+                           const double *dy, const double *dz);
+
+/* jacobi_iteration_allflux.f90:21-22, 102-103, 195-196  do_jacobi_{u,v,w} */
+int tpls_do_jacobi_u(tpls_ctx *ctx, double *u3, const double *u3_old,
+                     const double *rhs, const double *viscosity,
+                     const double *dx, const double *dy, const double *dz,
+                     const double *dt, const int *ex, const int *ey,
+                     const int *sx, const int *sy, const int *maxn,
+                     const int *ex_max);
+int tpls_do_jacobi_v(tpls_ctx *ctx, double *v3, const double *v3_old,
+                     const double *rhs, const double *viscosity,
+                     const double *dx, const double *dy, const double *dz,
+                     const double *dt, const int *ex, const int *ey,
+                     const int *sx, const int *sy, const int *maxn,
+                     const int *ex_max);
+int tpls_do_jacobi_w(tpls_ctx *ctx, double *w3, const double *w3_old,
+                     const double *rhs, const double *viscosity,
+                     const double *dx, const double *dy, const double *dz,
+                     const double *dt, const int *ex, const int *ey,
+                     const int *sx, const int *sy, const int *maxn,
+                     const int *ex_max);
+
+/* sor_iteration_allflux.f90:19-20, 152-153, 280-281  do_sor_{u,v,w} */
+int tpls_do_sor_u(tpls_ctx *ctx, double *u3, const double *rhs,
+                  const double *viscosity, const double *dx,
+                  const double *dy, const double *dz, const double *dt,
+                  const int *ex, const int *ey, const int *sx, const int *sy,
+                  const int *maxn, const int *ex_max, const int *flg,
+                  const int *iteration_time);
+int tpls_do_sor_v(tpls_ctx *ctx, double *v3, const double *rhs,
+                  const double *viscosity, const double *dx,
+                  const double *dy, const double *dz, const double *dt,
+                  const int *ex, const int *ey, const int *sx, const int *sy,
+                  const int *maxn, const int *flg, const int *iteration_time);
+int tpls_do_sor_w(tpls_ctx *ctx, double *w3, const double *rhs,
+                  const double *viscosity, const double *dx,
+                  const double *dy, const double *dz, const double *dt,
+                  const int *ex, const int *ey, const int *sx, const int *sy,
+                  const int *maxn, const int *flg, const int *iteration_time);
+
+/* jacobi_iteration_allflux.f90:285  get_difference (z range sz:ez) */
+int tpls_get_difference(tpls_ctx *ctx, const double *ua, const double *ub,
+                        const int *ex, const int *ey, const int *ez,
+                        const int *sx, const int *sy, const int *sz,
+                        double *diff);
+
+/* pressure.f90:16  get_source_pres */
+int tpls_get_source_pres(tpls_ctx *ctx, double *rhs, const double *u3,
+                         const double *v3, const double *w3, const int *ex,
+                         const int *ey, const int *sx, const int *sy,
+                         const int *maxn, const double *dx, const double *dy,
+                         const double *dz, const double *dt);
+
+/* pressure.f90:59  get_uvw_pres */
+int tpls_get_uvw_pres(tpls_ctx *ctx, double *u3, double *v3, double *w3,
+                      const double *p, const int *ex, const int *ey,
+                      const int *sx, const int *sy, const int *maxn,
+                      const int *ex_max, const double *dx, const double *dy,
+                      const double *dz, const double *dt,
+                      const double *u_inlet);
+
+/* main_ns_hybrid.F90:896-913 `pres=pres_old; KSPSolve(ksp);
+ * copy_pressure_out_of_petsc` with the callbacks of pressure_solver.F90:
+ * 205-486 (initial guess, RHS incl. inlet rows, 7-point matrix with Neumann
+ * ghost rows, constant null space).  Solved by geometric-multigrid
+ * preconditioned CG on the symmetric reduced system.  pres is the full
+ * p-grid array (ghost planes and periodic-y rows written). rtol<=0 takes
+ * the context's p_rtol; maxits<=0 takes p_maxits. */
+int tpls_pressure_solve(tpls_ctx *ctx, double *pres, const double *pres_old,
+                        const double *rhs_p, const double *u3,
+                        const double *u_inlet, const double *dx,
+                        const double *dy, const double *dz, const double *dt,
+                        const double *rtol, const int *maxits, int *its,
+                        double *rnorm, int *reason);
+
+/* mpi.f90:110  exchange2d on one rank = periodic-y ghost rows over the full
+ * x span, for an array (0:nx+1,0:ny+1,sz:ez). */
+int tpls_exchange2d(tpls_ctx *ctx, double *uu, const int *ex, const int *ey,
+                    const int *ez, const int *sx, const int *sy,
+                    const int *sz);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TPLS_GPU_H */

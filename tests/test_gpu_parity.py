@@ -1,0 +1,214 @@
+"""GPU parity: every entry of the C ABI against the CPU oracle on the same
+seeded inputs (tolerance: 1e-11 relative max-norm for the FP64 form).
+
+Sizes: the 64x32x48 workload, a small even grid and an odd grid
+(37x19x23: odd ny exercises the unfused ghost-row path of the sweeps)."""
+import numpy as np
+import pytest
+
+from oracle.oracle import Oracle
+from tpls_gb300.api import TplsGpu
+from tpls_gb300.channel import make_case
+
+from _util import relmax
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-11
+SIZES = {"A": (64, 32, 48), "even": (32, 16, 24), "odd": (37, 19, 23)}
+
+
+def _case(size, steps=1, **kw):
+    nx, ny, nz = SIZES[size]
+    params, uin, st = make_case("A", nx=nx, ny=ny, nz=nz, **kw)
+    o = Oracle(nx, ny, nz, params, uin)
+    o.set_state(st)
+    if steps:
+        o.step(steps)  # realistic fields and non-zero histories
+    return params, uin, o
+
+
+@pytest.fixture(scope="module", params=list(SIZES))
+def setup(request):
+    params, uin, o = _case(request.param)
+    g = TplsGpu(o.nx, o.ny, o.nz, params, uin)
+    yield params, uin, o, g
+    g.close()
+
+
+def _rows(o):
+    return (slice(None), slice(1, o.ny + 1), slice(None))
+
+
+def test_advect(setup):
+    p, uin, o, g = setup
+    s = o.get_state()
+    args = [np.array(s[k], order="F") for k in ("PHI2", "U2", "V2", "W2")]
+    args_g = [np.array(a, order="F") for a in args]
+    co = o.do_advect_phi(*args, p.dx, p.dy, p.dz)
+    cg = g.do_advect_phi(*args_g, p.dx, p.dy, p.dz)
+    assert relmax(cg, co) < TOL
+    for a, b in zip(args_g[1:], args[1:]):
+        assert relmax(a, b) < TOL  # halo rows exchanged in place
+
+
+def test_do_tpls(setup):
+    p, uin, o, g = setup
+    s = o.get_state()
+    c2 = o.get_field("CONV2_PHI")
+    res_o = o.do_tpls(s["PHI2"], s["CONV0_PHI"], s["CONV1_PHI"], c2, p.levelset, p.height, p.dx, p.dz, p.dt)
+    res_g = g.do_tpls(s["PHI2"], s["CONV0_PHI"], s["CONV1_PHI"], c2, p.levelset, p.height, p.dx, p.dz, p.dt)
+    assert relmax(res_g[0], res_o[0], _rows(o)) < TOL
+    assert abs(res_g[1] - res_o[1]) <= 1e-9 * abs(res_o[1])
+
+
+def test_get_csf(setup):
+    p, uin, o, g = setup
+    phi = o.get_field("PHI2")
+    fo = o.get_csf(phi, p.dx, p.dy, p.dz, p.scap, p.smooth_width)
+    fg = g.get_csf(phi, p.dx, p.dy, p.dz, p.scap, p.smooth_width)
+    for a, b in zip(fg, fo):
+        assert relmax(a, b, _rows(o)) < TOL
+
+
+def test_get_viscosity(setup):
+    p, uin, o, g = setup
+    phi = o.get_field("PHI2")
+    vo = o.get_viscosity(phi, p.smooth_width, p.re, p.mu_minus, p.mu_plus)
+    vg = g.get_viscosity(phi, p.smooth_width, p.re, p.mu_minus, p.mu_plus)
+    r = (slice(1, o.nx + 3), slice(None), slice(None))  # x 0..nx+1 (x -1, nx+2 are undefined)
+    assert relmax(vg, vo, r) < TOL
+
+
+@pytest.mark.parametrize("which", ["conv", "diff"])
+def test_conv_diff(setup, which):
+    p, uin, o, g = setup
+    s = o.get_state()
+    va = o.get_viscosity(s["PHI2"], p.smooth_width, p.re, p.mu_minus, p.mu_plus)
+    fo = o.get_conv_all if which == "conv" else o.get_diffusion_all
+    fg = g.get_conv_all if which == "conv" else g.get_diffusion_all
+    ro = fo(va, s["U2"], s["V2"], s["W2"], p.dx, p.dy, p.dz)
+    rg = fg(va, s["U2"], s["V2"], s["W2"], p.dx, p.dy, p.dz)
+    for a, b in zip(rg, ro):
+        assert relmax(a, b) < TOL
+
+
+def _sweep_inputs(o, comp, seed):
+    kind = "w" if comp == 2 else "uv"
+    rng = np.random.default_rng(seed)
+    x = np.asfortranarray(rng.normal(size=o.shape(kind)))
+    xo = np.asfortranarray(rng.normal(size=o.shape(kind)))
+    rhs = np.asfortranarray(rng.normal(size=o.shape(kind)))
+    o.exchange2d(x)
+    o.exchange2d(xo)
+    return x, xo, rhs
+
+
+@pytest.mark.parametrize("comp", [0, 1, 2])
+def test_jacobi(setup, comp):
+    p, uin, o, g = setup
+    va = o.get_viscosity(o.get_field("PHI2"), p.smooth_width, p.re, p.mu_minus, p.mu_plus)
+    x, xo, rhs = _sweep_inputs(o, comp, 10 + comp)
+    xg = np.array(x, order="F")
+    fo = [o.do_jacobi_u, o.do_jacobi_v, o.do_jacobi_w][comp]
+    fg = [g.do_jacobi_u, g.do_jacobi_v, g.do_jacobi_w][comp]
+    fo(x, xo, rhs, va, p.dx, p.dy, p.dz, p.dt)
+    fg(xg, xo, rhs, va, p.dx, p.dy, p.dz, p.dt)
+    assert relmax(xg, x) < TOL
+
+
+@pytest.mark.parametrize("comp", [0, 1, 2])
+@pytest.mark.parametrize("flg", [0, 1])
+@pytest.mark.parametrize("iteration_time", [1, 2])
+def test_sor(setup, comp, flg, iteration_time):
+    p, uin, o, g = setup
+    va = o.get_viscosity(o.get_field("PHI2"), p.smooth_width, p.re, p.mu_minus, p.mu_plus)
+    x, _, rhs = _sweep_inputs(o, comp, 20 + comp)
+    xg = np.array(x, order="F")
+    fo = [o.do_sor_u, o.do_sor_v, o.do_sor_w][comp]
+    fg = [g.do_sor_u, g.do_sor_v, g.do_sor_w][comp]
+    fo(x, rhs, va, p.dx, p.dy, p.dz, p.dt, flg, iteration_time)
+    fg(xg, rhs, va, p.dx, p.dy, p.dz, p.dt, flg, iteration_time)
+    assert relmax(xg, x) < TOL
+
+
+def test_source_and_projection(setup):
+    p, uin, o, g = setup
+    u3, v3, w3 = (o.get_field(k) for k in ("U3", "V3", "W3"))
+    ro = o.get_source_pres(u3, v3, w3, p.dx, p.dy, p.dz, p.dt)
+    rg = g.get_source_pres(u3, v3, w3, p.dx, p.dy, p.dz, p.dt)
+    assert relmax(rg, ro) < TOL
+    pres = o.get_field("PRES")
+    uo, vo, wo = (np.array(a, order="F") for a in (u3, v3, w3))
+    ug, vg, wg = (np.array(a, order="F") for a in (u3, v3, w3))
+    o.get_uvw_pres(uo, vo, wo, pres, p.dx, p.dy, p.dz, p.dt, uin)
+    g.get_uvw_pres(ug, vg, wg, pres, p.dx, p.dy, p.dz, p.dt, uin)
+    for a, b in zip((ug, vg, wg), (uo, vo, wo)):
+        assert relmax(a, b) < TOL
+
+
+def test_difference(setup):
+    p, uin, o, g = setup
+    a = o.get_field("U3")
+    b = o.get_field("U2")
+    assert abs(g.get_difference(a, b) - o.get_difference(a, b)) <= 1e-12 * o.get_difference(a, b)
+
+
+def test_pressure_solve_tight(setup):
+    p, uin, o, g = setup
+    rhs, u3, pold = o.get_field("RHS_P"), o.get_field("U3"), o.get_field("PRES_OLD")
+    po, *_ = o.pressure_solve(pold, rhs, u3, uin, p.dx, p.dy, p.dz, p.dt)
+    pg, its, rn, reason = g.pressure_solve(pold, rhs, u3, uin, p.dx, p.dy, p.dz, p.dt, rtol=1e-13, maxits=200)
+    assert reason == 2 and its < 60
+    assert relmax(pg, po) < 1e-10
+
+
+def test_pressure_solve_reference_rtol(setup):
+    """At PETSc's default rtol = 1e-5 the pressure matches the exact solve to
+    within that tolerance (measured on the solution, relative max-norm)."""
+    p, uin, o, g = setup
+    rhs, u3, pold = o.get_field("RHS_P"), o.get_field("U3"), o.get_field("PRES_OLD")
+    po, *_ = o.pressure_solve(pold, rhs, u3, uin, p.dx, p.dy, p.dz, p.dt)
+    pg, its, rn, reason = g.pressure_solve(pold, rhs, u3, uin, p.dx, p.dy, p.dz, p.dt, rtol=1e-5, maxits=200)
+    assert reason == 2
+    d = pg - po
+    d -= d[1:-1, 1:-1, 1:-1].mean()
+    assert np.max(np.abs(d)) <= 1e-5 * np.max(np.abs(po - po[1:-1, 1:-1, 1:-1].mean()))
+
+
+@pytest.mark.parametrize("size", list(SIZES))
+def test_full_steps_match_oracle(size):
+    """Whole timesteps on device-resident state, compared after every step;
+    the pressure solve runs to 1e-13 so u, v, w can match to 1e-11."""
+    nx, ny, nz = SIZES[size]
+    params, uin, st = make_case("A", nx=nx, ny=ny, nz=nz, p_rtol=1e-13, p_maxits=200)
+    o = Oracle(nx, ny, nz, params, uin)
+    o.set_state(st)
+    g = TplsGpu(nx, ny, nz, params, uin)
+    g.set_state(st)
+    rows = (slice(None), slice(1, ny + 1), slice(None))
+    for step in range(3):
+        o.step(1)
+        g.step(1)
+        for k in ("PHI2", "U2", "V2", "W2"):
+            e = relmax(g.get_field(k), o.get_field(k), rows)
+            assert e < TOL, (step, k, e)
+        dp = g.get_field("PRES") - o.get_field("PRES")
+        assert np.max(np.abs(dp)) <= 1e-9 * np.max(np.abs(o.get_field("PRES"))), step
+    so, sg = o.stats(), g.stats()
+    assert abs(sg["liquid_volume"] - so["liquid_volume"]) <= 1e-12 * abs(so["liquid_volume"])
+    assert sg["p_reason"] == 2
+    g.close()
+
+
+def test_step_is_deterministic():
+    params, uin, st = make_case("A", nx=32, ny=16, nz=24)
+    outs = []
+    for _ in range(2):
+        g = TplsGpu(32, 16, 24, params, uin)
+        g.set_state(st)
+        g.step(2)
+        outs.append(g.get_state())
+        g.close()
+    for k in outs[0]:
+        np.testing.assert_array_equal(outs[0][k], outs[1][k])

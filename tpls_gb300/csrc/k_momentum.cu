@@ -1,0 +1,543 @@
+// k_momentum.cu -- momentum operator and Crank-Nicolson sweeps
+// (momentum_allflux.f90:22-471, jacobi_iteration_allflux.f90:21-311,
+// sor_iteration_allflux.f90:19-377, main_ns_hybrid.F90:629-641,743-887).
+//
+// Velocity components are addressed in the reference's staggered index
+// space: u(i,j,k) sits between p-cells (i,j+1,k+1) and (i+1,j+1,k+1),
+// v(i,j,k) between (i,j,k+1) and (i,j+1,k+1), w(i,j,k) between (i,j+1,k)
+// and (i,j+1,k+1); the viscosity field mu is on the p-grid with two
+// periodic ghost rows, so every face viscosity of the reference is read
+// directly.
+//
+// Red-black SOR: for an even iteration_time the colouring is the 3-D
+// checkerboard mod(k+j+flg,2), every point of a colour is independent and
+// one thread updates one point.  For an odd iteration_time the colouring is
+// mod(j+flg,2) in every plane, so the reference's sequential loop lets a
+// point see the already-relaxed point below it: one thread marches each
+// (i,j) column upward, carrying the relaxed value in a register.
+// Periodic ghost rows are written by the thread that writes the row they
+// copy (legal for even ny: no point of the colour being relaxed reads a
+// ghost row written in the same half-sweep); for odd ny the caller runs a
+// separate exchange after each half-sweep instead.
+#include "tpls_kernels.h"
+
+namespace tpls {
+
+struct Fc {
+  double px, mx, py, my, pz, mz;
+};
+
+// face viscosities, momentum_allflux.f90:91-98 (u), :145-152 (v), :187-194 (w)
+__device__ __forceinline__ Fc faces(int comp, const Geo &g, const double *__restrict__ mu, int i,
+                                    int j, int k) {
+  const int sy = g.sy, sz = g.szm;
+  Fc f;
+  if (comp == 0) {
+    const double *m = mu + TPLS_IDXM(g, i, j + 1, k + 1);
+    const double a = m[0], b = m[1];
+    f.px = b;
+    f.mx = a;
+    f.py = (a + b + m[sy] + m[1 + sy]) * 0.25;
+    f.my = (a + b + m[-sy] + m[1 - sy]) * 0.25;
+    f.pz = (a + b + m[sz] + m[1 + sz]) * 0.25;
+    f.mz = (a + b + m[-sz] + m[1 - sz]) * 0.25;
+  } else if (comp == 1) {
+    const double *m = mu + TPLS_IDXM(g, i, j + 1, k + 1);
+    const double a = m[0], b = m[-sy];
+    f.px = (a + b + m[1] + m[1 - sy]) * 0.25;
+    f.mx = (a + b + m[-1] + m[-1 - sy]) * 0.25;
+    f.py = a;
+    f.my = b;
+    f.pz = (a + b + m[sz] + m[sz - sy]) * 0.25;
+    f.mz = (a + b + m[-sz] + m[-sz - sy]) * 0.25;
+  } else {
+    const double *m = mu + TPLS_IDXM(g, i, j + 1, k);
+    const double a = m[0], b = m[sz];
+    f.px = (a + b + m[1] + m[1 + sz]) * 0.25;
+    f.mx = (a + b + m[-1] + m[-1 + sz]) * 0.25;
+    f.py = (a + b + m[sy] + m[sy + sz]) * 0.25;
+    f.my = (a + b + m[-sy] + m[-sy + sz]) * 0.25;
+    f.pz = b;
+    f.mz = a;
+  }
+  return f;
+}
+
+struct Helm {
+  double ax2, ay2, az2;  // dt/(2 d^2)
+  double dtdx;           // dt/dx (u outlet condition)
+};
+
+// jacobi_iteration_allflux.f90:84-90 (same form in every Jacobi/SOR routine)
+__device__ __forceinline__ double helm(const Fc &f, const Helm &h, double xp, double xm,
+                                       double yp, double ym, double zp, double zm,
+                                       double rhs) {
+  const double diag =
+      1.0 + h.ax2 * (f.px + f.mx) + h.ay2 * (f.py + f.my) + h.az2 * (f.pz + f.mz);
+  return (h.ax2 * (f.px * xp + f.mx * xm) + h.ay2 * (f.py * yp + f.my * ym) +
+          h.az2 * (f.pz * zp + f.mz * zm) + rhs) /
+         diag;
+}
+
+// ---------------------------------------------------------------------------
+// get_conv_all / get_diffusion_all point forms.
+struct CD {
+  double conv, diff;
+};
+
+__device__ __forceinline__ CD conv_diff(int comp, const Geo &g, double rdx, double rdy,
+                                        double rdz, const double *__restrict__ U,
+                                        const double *__restrict__ V,
+                                        const double *__restrict__ W,
+                                        const double *__restrict__ mu, int i, int j, int k) {
+  const int sy = g.sy, sz = g.sz, nzu = g.nz;  // u/v have planes 0..nz-1
+  const int c = TPLS_IDX(g, i, j, k);
+  const Fc f = faces(comp, g, mu, i, j, k);
+  CD r;
+  if (comp == 0) {
+    const double x = U[c];
+    const double tempv = (V[c] + V[c + 1] + V[c + sy] + V[c + 1 + sy]) * 0.25;
+    const double tempw = (W[c] + W[c + 1] + W[c + sz] + W[c + 1 + sz]) * 0.25;
+    const double Xc = 0.5 * (U[c + 1] - U[c - 1]) * rdx * x;
+    const double Yc = 0.5 * (U[c + sy] - U[c - sy]) * rdy * tempv;
+    double dz_;
+    if (k == 0) dz_ = (x + U[c + sz]) * (0.5 * rdz);
+    else if (k == nzu - 1) dz_ = -(x + U[c - sz]) * (0.5 * rdz);
+    else dz_ = 0.5 * (U[c + sz] - U[c - sz]) * rdz;
+    const double t1 = Xc + Yc + dz_ * tempw;
+    const double E = f.px * (U[c + 1] - x) * rdx, Wt = f.mx * (x - U[c - 1]) * rdx;
+    const double N = f.py * (V[c + 1 + sy] - V[c + sy]) * rdx, S = f.my * (V[c + 1] - V[c]) * rdx;
+    const double O = f.pz * (W[c + 1 + sz] - W[c + sz]) * rdx, I = f.mz * (W[c + 1] - W[c]) * rdx;
+    r.conv = t1 - ((E - Wt) * rdx + (N - S) * rdy + (O - I) * rdz);
+    const double umz = (k == 0) ? -2.0 * x + U[c + sz] * (1.0 / 3.0) : U[c - sz];
+    const double upz = (k == nzu - 1) ? -2.0 * x + U[c - sz] * (1.0 / 3.0) : U[c + sz];
+    r.diff = (f.px * (U[c + 1] - x) - f.mx * (x - U[c - 1])) * (rdx * rdx) +
+             (f.py * (U[c + sy] - x) - f.my * (x - U[c - sy])) * (rdy * rdy) +
+             (f.pz * (upz - x) - f.mz * (x - umz)) * (rdz * rdz);
+  } else if (comp == 1) {
+    const double x = V[c];
+    const double tempu = (U[c - 1 - sy] + U[c - 1] + U[c - sy] + U[c]) * 0.25;
+    const double tempw = (W[c - sy] + W[c] + W[c - sy + sz] + W[c + sz]) * 0.25;
+    const double Yc = 0.5 * (V[c + sy] - V[c - sy]) * rdy * x;
+    const double Xc = 0.5 * (V[c + 1] - V[c - 1]) * rdx * tempu;
+    double dz_;
+    if (k == 0) dz_ = (x + V[c + sz]) * (0.5 * rdz);
+    else if (k == nzu - 1) dz_ = -(x + V[c - sz]) * (0.5 * rdz);
+    else dz_ = 0.5 * (V[c + sz] - V[c - sz]) * rdz;
+    const double t1 = Xc + Yc + dz_ * tempw;
+    const double E = f.px * (U[c] - U[c - sy]) * rdy, Wt = f.mx * (U[c - 1] - U[c - 1 - sy]) * rdy;
+    const double N = f.py * (V[c + sy] - x) * rdy, S = f.my * (x - V[c - sy]) * rdy;
+    const double O = f.pz * (W[c + sz] - W[c - sy + sz]) * rdy, I = f.mz * (W[c] - W[c - sy]) * rdy;
+    r.conv = t1 - ((E - Wt) * rdx + (N - S) * rdy + (O - I) * rdz);
+    const double vmz = (k == 0) ? -2.0 * x + V[c + sz] * (1.0 / 3.0) : V[c - sz];
+    const double vpz = (k == nzu - 1) ? -2.0 * x + V[c - sz] * (1.0 / 3.0) : V[c + sz];
+    r.diff = (f.px * (V[c + 1] - x) - f.mx * (x - V[c - 1])) * (rdx * rdx) +
+             (f.py * (V[c + sy] - x) - f.my * (x - V[c - sy])) * (rdy * rdy) +
+             (f.pz * (vpz - x) - f.mz * (x - vmz)) * (rdz * rdz);
+  } else {
+    const double x = W[c];
+    const double tempu = (U[c - 1 - sz] + U[c - 1] + U[c - sz] + U[c]) * 0.25;
+    const double tempv = (V[c - sz] + V[c] + V[c + sy - sz] + V[c + sy]) * 0.25;
+    const double Zc = 0.5 * (W[c + sz] - W[c - sz]) * rdz * x;
+    const double Xc = 0.5 * (W[c + 1] - W[c - 1]) * rdx * tempu;
+    const double Yc = 0.5 * (W[c + sy] - W[c - sy]) * rdy * tempv;
+    const double t1 = Xc + Yc + Zc;
+    const double E = f.px * (U[c] - U[c - sz]) * rdz, Wt = f.mx * (U[c - 1] - U[c - 1 - sz]) * rdz;
+    const double N = f.py * (V[c + sy] - V[c + sy - sz]) * rdz, S = f.my * (V[c] - V[c - sz]) * rdz;
+    const double O = f.pz * (W[c + sz] - x) * rdz, I = f.mz * (x - W[c - sz]) * rdz;
+    r.conv = t1 - ((E - Wt) * rdx + (N - S) * rdy + (O - I) * rdz);
+    r.diff = (f.px * (W[c + 1] - x) - f.mx * (x - W[c - 1])) * (rdx * rdx) +
+             (f.py * (W[c + sy] - x) - f.my * (x - W[c - sy])) * (rdy * rdy) +
+             (f.pz * (W[c + sz] - x) - f.mz * (x - W[c - sz])) * (rdz * rdz);
+  }
+  return r;
+}
+
+constexpr int MB_X = 32, MB_Y = 4;
+
+// Domain of a component's conv/diff (get_conv_all ranges) and of the
+// right-hand side kernel (whole face range the history arrays carry).
+__device__ __forceinline__ bool cd_valid(int comp, const Geo &g, int i, int k) {
+  if (comp == 0) return i <= g.nx - 1;
+  if (comp == 2) return k >= 1 && k <= g.nz - 1;
+  return true;
+}
+
+__global__ void __launch_bounds__(MB_X *MB_Y)
+    k_mom_rhs(int comp, Geo g, Phys ph, const double *__restrict__ U,
+              const double *__restrict__ V, const double *__restrict__ W,
+              const double *__restrict__ mu, const double *__restrict__ fc,
+              const double *__restrict__ c1, const double *__restrict__ c0,
+              const double *__restrict__ s1, const double *__restrict__ s0,
+              double *__restrict__ conv2, double *__restrict__ csf2, double *__restrict__ rhs,
+              double *__restrict__ diff_out) {
+  const int i = blockIdx.x * MB_X + threadIdx.x + 1, j = blockIdx.y * MB_Y + threadIdx.y + 1;
+  const int k = blockIdx.z;
+  if (i > g.nx || j > g.ny) return;
+  const int c = TPLS_IDX(g, i, j, k);
+  CD cd = {0.0, 0.0};
+  if (cd_valid(comp, g, i, k)) cd = conv_diff(comp, g, 1.0 / ph.dx, 1.0 / ph.dy, 1.0 / ph.dz, U, V, W, mu, i, j, k);
+  // main_ns_hybrid.F90:629-641 face averages of the CSF force
+  double s2;
+  if (comp == 0) s2 = (fc[TPLS_IDX(g, i + 1, j + 1, k + 1)] + fc[TPLS_IDX(g, i, j + 1, k + 1)]) * 0.5;
+  else if (comp == 1) s2 = (fc[TPLS_IDX(g, i, j + 1, k + 1)] + fc[TPLS_IDX(g, i, j, k + 1)]) * 0.5;
+  else s2 = (fc[TPLS_IDX(g, i, j + 1, k + 1)] + fc[TPLS_IDX(g, i, j + 1, k)]) * 0.5;
+  const double X = (comp == 0) ? U[c] : (comp == 1) ? V[c] : W[c];
+  const double dt = ph.dt;
+  // main_ns_hybrid.F90:743-751 (AB3 convection and CSF, CN diffusion)
+  const double r = X - dt * ((23.0 / 12.0) * cd.conv - (4.0 / 3.0) * c1[c] + (5.0 / 12.0) * c0[c]) +
+                   (dt / 2.0) * cd.diff +
+                   dt * ((23.0 / 12.0) * s2 - (4.0 / 3.0) * s1[c] + (5.0 / 12.0) * s0[c]);
+  conv2[c] = cd.conv;
+  csf2[c] = s2;
+  rhs[c] = r;
+  if (diff_out) diff_out[c] = cd.diff;
+}
+
+cudaError_t launch_mom_rhs(int comp, const Geo &g, const Phys &ph,
+                           const double *u2, const double *v2,
+                           const double *w2, const double *mu,
+                           const double *fcsf, const double *c1,
+                           const double *c0, const double *s1,
+                           const double *s0, double *conv2, double *csf2,
+                           double *rhs, double *diff_out, cudaStream_t st) {
+  const int nk = (comp == 2) ? g.nz + 1 : g.nz;
+  dim3 grd((g.nx + MB_X - 1) / MB_X, (g.ny + MB_Y - 1) / MB_Y, nk);
+  k_mom_rhs<<<grd, dim3(MB_X, MB_Y), 0, st>>>(comp, g, ph, u2, v2, w2, mu, fcsf, c1, c0, s1, s0,
+                                              conv2, csf2, rhs, diff_out);
+  return cudaGetLastError();
+}
+
+// standalone get_conv_all / get_diffusion_all: out = conv or diff on the
+// component's domain (other entries are left untouched; the caller zeroes).
+__global__ void k_conv_diff(int comp, int want_conv, Geo g, Phys ph, const double *__restrict__ U,
+                            const double *__restrict__ V, const double *__restrict__ W,
+                            const double *__restrict__ mu, double *__restrict__ out) {
+  const int i = blockIdx.x * MB_X + threadIdx.x + 1, j = blockIdx.y * MB_Y + threadIdx.y + 1;
+  const int k = blockIdx.z;
+  if (i > g.nx || j > g.ny || !cd_valid(comp, g, i, k)) return;
+  CD cd = conv_diff(comp, g, 1.0 / ph.dx, 1.0 / ph.dy, 1.0 / ph.dz, U, V, W, mu, i, j, k);
+  out[TPLS_IDX(g, i, j, k)] = want_conv ? cd.conv : cd.diff;
+}
+
+cudaError_t launch_conv_diff(int comp, int want_conv, const Geo &g,
+                             const Phys &ph, const double *u2,
+                             const double *v2, const double *w2,
+                             const double *mu, double *out, cudaStream_t st) {
+  const int nk = (comp == 2) ? g.nz + 1 : g.nz;
+  dim3 grd((g.nx + MB_X - 1) / MB_X, (g.ny + MB_Y - 1) / MB_Y, nk);
+  k_conv_diff<<<grd, dim3(MB_X, MB_Y), 0, st>>>(comp, want_conv, g, ph, u2, v2, w2, mu, out);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Writers with the fused periodic ghost copy.
+__device__ __forceinline__ void put(const Geo &g, double *x, int i, int j, int k, double v,
+                                    int fuse) {
+  x[TPLS_IDX(g, i, j, k)] = v;
+  if (fuse) {
+    if (j == g.ny) x[TPLS_IDX(g, i, 0, k)] = v;
+    if (j == 1) x[TPLS_IDX(g, i, g.ny + 1, k)] = v;
+  }
+}
+
+// u outlet, main_ns_hybrid.F90:768-776 (note the pressure row index is the
+// u row index j, as written in the reference)
+__device__ __forceinline__ double u_outlet(const Geo &g, const Helm &h, const double *P,
+                                           double unm1, int j, int k) {
+  const int nx = g.nx;
+  return unm1 + h.dtdx * (P[TPLS_IDX(g, nx + 1, j, k + 1)] + P[TPLS_IDX(g, nx - 1, j, k + 1)] -
+                          2.0 * P[TPLS_IDX(g, nx, j, k + 1)]);
+}
+
+// z neighbours for u/v with the wall ghost rule `-2*x(0)+x(1)/3`
+// (jacobi_iteration_allflux.f90:63-73)
+__device__ __forceinline__ double zm_uv(const double *x, int c, int k, int sz) {
+  return (k == 0) ? -2.0 * x[c] + x[c + sz] * (1.0 / 3.0) : x[c - sz];
+}
+__device__ __forceinline__ double zp_uv(const double *x, int c, int k, int nzu, int sz) {
+  return (k == nzu - 1) ? -2.0 * x[c] + x[c - sz] * (1.0 / 3.0) : x[c + sz];
+}
+
+// jacobi_iteration_allflux.f90:21-282 with the routine's own boundary rows
+// (v, w) and, for bc=1, the driver's u boundary rows (:762-776).
+__global__ void __launch_bounds__(MB_X *MB_Y)
+    k_jacobi(int comp, Geo g, Helm h, const double *__restrict__ xo,
+             const double *__restrict__ rhs, const double *__restrict__ mu,
+             const double *__restrict__ P, double *__restrict__ x, int bc, int fuse) {
+  const int i = blockIdx.x * MB_X + threadIdx.x + 1, j = blockIdx.y * MB_Y + threadIdx.y + 1;
+  const int k = blockIdx.z + (comp == 2 ? 1 : 0);
+  const int iend = (comp == 0) ? g.nx - 1 : g.nx;
+  if (i > iend || j > g.ny) return;
+  const int c = TPLS_IDX(g, i, j, k), sy = g.sy, sz = g.sz;
+  const Fc f = faces(comp, g, mu, i, j, k);
+  double zp, zm;
+  if (comp == 2) {
+    zp = xo[c + sz];
+    zm = xo[c - sz];
+  } else {
+    zp = zp_uv(xo, c, k, g.nz, sz);
+    zm = zm_uv(xo, c, k, sz);
+  }
+  const double v = helm(f, h, xo[c + 1], xo[c - 1], xo[c + sy], xo[c - sy], zp, zm, rhs[c]);
+  put(g, x, i, j, k, v, fuse);
+  if (comp == 0) {
+    if (bc) {
+      if (i == 1) put(g, x, 0, j, k, v, fuse);
+      if (i == g.nx - 1) {
+        put(g, x, g.nx, j, k, u_outlet(g, h, P, v, j, k), fuse);
+        put(g, x, g.nx + 1, j, k, 0.0, fuse);
+      }
+    }
+  } else if (comp == 1) {  // jacobi_iteration_allflux.f90:178-189
+    if (i == 1) put(g, x, 0, j, k, v, fuse);
+    if (i == g.nx) put(g, x, g.nx + 1, j, k, v, fuse);
+  } else {  // jacobi_iteration_allflux.f90:257-279
+    const int nz = g.nz;
+    if (k == 1) put(g, x, i, j, 0, 0.0, fuse);
+    if (k == nz - 1) put(g, x, i, j, nz, 0.0, fuse);
+    if (i == 1) {
+      put(g, x, 0, j, k, v, fuse);
+      if (k == 1) put(g, x, 0, j, 0, 0.0, fuse);
+      if (k == nz - 1) put(g, x, 0, j, nz, 0.0, fuse);
+    }
+    if (i == g.nx) {
+      put(g, x, g.nx + 1, j, k, v, fuse);
+      if (k == 1) put(g, x, g.nx + 1, j, 0, 0.0, fuse);
+      if (k == nz - 1) put(g, x, g.nx + 1, j, nz, 0.0, fuse);
+    }
+  }
+}
+
+cudaError_t launch_jacobi(int comp, const Geo &g, const Phys &ph,
+                          const double *xo, const double *rhs,
+                          const double *mu, const double *pres, double *x,
+                          int bc, int fuse_ghosts, cudaStream_t st) {
+  Helm h;
+  h.ax2 = (ph.dt / (ph.dx * ph.dx)) / 2.0;
+  h.ay2 = (ph.dt / (ph.dy * ph.dy)) / 2.0;
+  h.az2 = (ph.dt / (ph.dz * ph.dz)) / 2.0;
+  h.dtdx = ph.dt / ph.dx;
+  const int nk = (comp == 2) ? g.nz - 1 : g.nz;
+  const int iend = (comp == 0) ? g.nx - 1 : g.nx;
+  dim3 grd((iend + MB_X - 1) / MB_X, (g.ny + MB_Y - 1) / MB_Y, nk);
+  k_jacobi<<<grd, dim3(MB_X, MB_Y), 0, st>>>(comp, g, h, xo, rhs, mu, pres, x, bc, fuse_ghosts);
+  return cudaGetLastError();
+}
+
+// Post-sweep boundary rows (main_ns_hybrid.F90:784-799 u, :826-836 v,
+// :860-879 w), written by the thread that owns the first / last x pair.
+__device__ __forceinline__ void sor_bc(int comp, const Geo &g, const Helm &h, double *x,
+                                       const double *P, int i2, int i, int iend, double v, int j,
+                                       int k, int fuse) {
+  if (i2 == 0) {
+    const double v1 = (i == 1) ? v : x[TPLS_IDX(g, 1, j, k)];
+    put(g, x, 0, j, k, v1, fuse);
+  }
+  if (i2 == (iend - 1) / 2) {
+    const double ve = (i == iend) ? v : x[TPLS_IDX(g, iend, j, k)];
+    if (comp == 0) {
+      put(g, x, g.nx, j, k, u_outlet(g, h, P, ve, j, k), fuse);
+      put(g, x, g.nx + 1, j, k, 0.0, fuse);
+    } else {
+      put(g, x, g.nx + 1, j, k, ve, fuse);
+    }
+  }
+}
+
+// sor_iteration_allflux.f90:54-99 (and v, w): 3-D checkerboard half-sweep.
+__global__ void __launch_bounds__(MB_X *MB_Y)
+    k_sor_even(int comp, Geo g, Helm h, double *__restrict__ x, const double *__restrict__ rhs,
+               const double *__restrict__ mu, const double *__restrict__ P, int flg, int bc,
+               int fuse) {
+  const int i2 = blockIdx.x * MB_X + threadIdx.x, j = blockIdx.y * MB_Y + threadIdx.y + 1;
+  const int k = blockIdx.z + (comp == 2 ? 1 : 0);
+  const int iend = (comp == 0) ? g.nx - 1 : g.nx;
+  if (i2 > (iend - 1) / 2 || j > g.ny) return;
+  const int i = 2 * i2 + 1 + ((k + j + flg) & 1);
+  double v = 0.0;
+  if (i <= iend) {
+    const int c = TPLS_IDX(g, i, j, k), sy = g.sy, sz = g.sz;
+    const Fc f = faces(comp, g, mu, i, j, k);
+    double zp, zm;
+    if (comp == 2) {
+      zp = x[c + sz];
+      zm = x[c - sz];
+    } else {
+      zp = zp_uv(x, c, k, g.nz, sz);
+      zm = zm_uv(x, c, k, sz);
+    }
+    const double xc = x[c];
+    const double res = helm(f, h, x[c + 1], x[c - 1], x[c + sy], x[c - sy], zp, zm, rhs[c]);
+    v = xc + 1.2 * (res - xc);
+    put(g, x, i, j, k, v, fuse);
+  }
+  if (bc) sor_bc(comp, g, h, x, P, i2, i, iend, v, j, k, fuse);
+}
+
+// sor_iteration_allflux.f90:100-146 (and v, w): 2-D colouring, sequential
+// in k within each column.
+__global__ void __launch_bounds__(MB_X *MB_Y)
+    k_sor_odd(int comp, Geo g, Helm h, double *__restrict__ x, const double *__restrict__ rhs,
+              const double *__restrict__ mu, const double *__restrict__ P, int flg, int bc,
+              int fuse) {
+  const int i2 = blockIdx.x * MB_X + threadIdx.x, j = blockIdx.y * MB_Y + threadIdx.y + 1;
+  const int iend = (comp == 0) ? g.nx - 1 : g.nx;
+  if (i2 > (iend - 1) / 2 || j > g.ny) return;
+  const int i = 2 * i2 + 1 + ((j + flg) & 1);
+  const bool act = (i <= iend);
+  const int sy = g.sy, sz = g.sz, nz = g.nz;
+  const int k0 = (comp == 2) ? 1 : 0, k1 = nz - 1;
+  double prev = 0.0;  // relaxed value at k-1 in this column
+  for (int k = k0; k <= k1; k++) {
+    double v = 0.0;
+    if (act) {
+      const int c = TPLS_IDX(g, i, j, k);
+      const Fc f = faces(comp, g, mu, i, j, k);
+      const double xc = x[c];
+      double zp, zm;
+      if (comp == 2) {
+        zm = (k == k0) ? x[c - sz] : prev;
+        zp = x[c + sz];
+      } else {
+        zm = (k == 0) ? -2.0 * xc + x[c + sz] * (1.0 / 3.0) : prev;
+        zp = (k == nz - 1) ? -2.0 * xc + prev * (1.0 / 3.0) : x[c + sz];
+      }
+      const double res = helm(f, h, x[c + 1], x[c - 1], x[c + sy], x[c - sy], zp, zm, rhs[c]);
+      v = xc + 1.2 * (res - xc);
+      put(g, x, i, j, k, v, fuse);
+      prev = v;
+    }
+    if (bc) sor_bc(comp, g, h, x, P, i2, i, iend, v, j, k, fuse);
+  }
+}
+
+cudaError_t launch_sor(int comp, const Geo &g, const Phys &ph, double *x,
+                       const double *rhs, const double *mu,
+                       const double *pres, int flg, int iteration_time,
+                       int bc, int fuse_ghosts, cudaStream_t st) {
+  Helm h;
+  h.ax2 = (ph.dt / (ph.dx * ph.dx)) / 2.0;
+  h.ay2 = (ph.dt / (ph.dy * ph.dy)) / 2.0;
+  h.az2 = (ph.dt / (ph.dz * ph.dz)) / 2.0;
+  h.dtdx = ph.dt / ph.dx;
+  const int iend = (comp == 0) ? g.nx - 1 : g.nx;
+  const int npairs = (iend + 1) / 2;
+  if (iteration_time % 2 == 0) {
+    const int nk = (comp == 2) ? g.nz - 1 : g.nz;
+    dim3 grd((npairs + MB_X - 1) / MB_X, (g.ny + MB_Y - 1) / MB_Y, nk);
+    k_sor_even<<<grd, dim3(MB_X, MB_Y), 0, st>>>(comp, g, h, x, rhs, mu, pres, flg, bc, fuse_ghosts);
+  } else {
+    dim3 grd((npairs + MB_X - 1) / MB_X, (g.ny + MB_Y - 1) / MB_Y, 1);
+    k_sor_odd<<<grd, dim3(MB_X, MB_Y), 0, st>>>(comp, g, h, x, rhs, mu, pres, flg, bc, fuse_ghosts);
+  }
+  return cudaGetLastError();
+}
+
+// get_difference: per-block partials of sum (a-b)^2 over i 1..nx, j 1..ny,
+// planes 0..nzp-1.
+__global__ void k_diff2(Geo g, const double *__restrict__ a, const double *__restrict__ b,
+                        double *__restrict__ part) {
+  const int i = blockIdx.x * MB_X + threadIdx.x + 1, j = blockIdx.y * MB_Y + threadIdx.y + 1;
+  const int k = blockIdx.z;
+  double e = 0.0;
+  if (i <= g.nx && j <= g.ny) {
+    const int c = TPLS_IDX(g, i, j, k);
+    const double d = a[c] - b[c];
+    e = d * d;
+  }
+  __shared__ double s[MB_X * MB_Y / 32];
+  for (int o = 16; o > 0; o >>= 1) e += __shfl_down_sync(0xffffffffu, e, o);
+  const int t = threadIdx.y * MB_X + threadIdx.x;
+  if ((t & 31) == 0) s[t >> 5] = e;
+  __syncthreads();
+  if (t == 0) {
+    double acc = 0.0;
+    for (int q = 0; q < MB_X * MB_Y / 32; q++) acc += s[q];
+    part[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)] = acc;
+  }
+}
+
+int diff2_blocks(const Geo &g, int nzp) {
+  return ((g.nx + MB_X - 1) / MB_X) * ((g.ny + MB_Y - 1) / MB_Y) * nzp;
+}
+
+cudaError_t launch_diff2(const Geo &g, const double *a, const double *b,
+                         int nzp, double *part, cudaStream_t st) {
+  dim3 grd((g.nx + MB_X - 1) / MB_X, (g.ny + MB_Y - 1) / MB_Y, nzp);
+  k_diff2<<<grd, dim3(MB_X, MB_Y), 0, st>>>(g, a, b, part);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// pressure.f90:16-56 get_source_pres on the full p-grid (zero outside the
+// interior; y ghost rows as periodic copies).
+__global__ void k_source(Geo g, double rdx, double rdy, double rdz, double rdt,
+                         const double *__restrict__ U, const double *__restrict__ V,
+                         const double *__restrict__ W, double *__restrict__ rhs) {
+  const int i = blockIdx.x * MB_X + threadIdx.x, j = blockIdx.y * MB_Y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i > g.nx + 1 || j > g.ny + 1) return;
+  double r = 0.0;
+  if (i >= 1 && i <= g.nx && k >= 1 && k <= g.nz) {
+    const int jj = wrapy(j, g.ny), jm = (jj == 1) ? g.ny : jj - 1;
+    r = ((U[TPLS_IDX(g, i, jm, k - 1)] - U[TPLS_IDX(g, i - 1, jm, k - 1)]) * rdx +
+         (V[TPLS_IDX(g, i, jj, k - 1)] - V[TPLS_IDX(g, i, jm, k - 1)]) * rdy +
+         (W[TPLS_IDX(g, i, jm, k)] - W[TPLS_IDX(g, i, jm, k - 1)]) * rdz) *
+        rdt;
+  }
+  rhs[TPLS_IDX(g, i, j, k)] = r;
+}
+
+cudaError_t launch_source(const Geo &g, const Phys &ph, const double *u3,
+                          const double *v3, const double *w3, double *rhs_p,
+                          cudaStream_t st) {
+  dim3 grd((g.nx + 2 + MB_X - 1) / MB_X, (g.ny + 2 + MB_Y - 1) / MB_Y, g.nz + 2);
+  k_source<<<grd, dim3(MB_X, MB_Y), 0, st>>>(g, 1.0 / ph.dx, 1.0 / ph.dy, 1.0 / ph.dz, 1.0 / ph.dt,
+                                             u3, v3, w3, rhs_p);
+  return cudaGetLastError();
+}
+
+// pressure.f90:59-134 get_uvw_pres, written out of place into the next
+// state's velocity arrays over x 0..nx+1 and every row (ghost rows as
+// periodic copies).
+__global__ void k_project(Geo g, double dtdx, double dtdy, double dtdz,
+                          const double *__restrict__ U, const double *__restrict__ V,
+                          const double *__restrict__ W, const double *__restrict__ P,
+                          const double *__restrict__ uin, double *__restrict__ uo,
+                          double *__restrict__ vo, double *__restrict__ wo) {
+  const int i = blockIdx.x * MB_X + threadIdx.x, j = blockIdx.y * MB_Y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i > g.nx + 1 || j > g.ny + 1) return;
+  const int jj = wrapy(j, g.ny);
+  const int c = TPLS_IDX(g, i, j, k), cc = TPLS_IDX(g, i, jj, k);
+  const int sy = g.sy, sz = g.sz;
+  if (k <= g.nz - 1) {
+    double u;
+    if (i == 0) u = uin[k];
+    else if (i == g.nx + 1) u = 0.0;
+    else u = U[cc] - dtdx * (P[cc + 1 + sy + sz] - P[cc + sy + sz]);
+    uo[c] = u;
+    vo[c] = V[cc] - dtdy * (P[cc + sy + sz] - P[cc + sz]);
+  }
+  wo[c] = W[cc] - dtdz * (P[cc + sy + sz] - P[cc + sy]);
+}
+
+cudaError_t launch_project(const Geo &g, const Phys &ph, const double *u3,
+                           const double *v3, const double *w3,
+                           const double *p, const double *u_inlet,
+                           double *u_out, double *v_out, double *w_out,
+                           cudaStream_t st) {
+  dim3 grd((g.nx + 2 + MB_X - 1) / MB_X, (g.ny + 2 + MB_Y - 1) / MB_Y, g.nz + 1);
+  k_project<<<grd, dim3(MB_X, MB_Y), 0, st>>>(g, ph.dt / ph.dx, ph.dt / ph.dy, ph.dt / ph.dz, u3, v3,
+                                              w3, p, u_inlet, u_out, v_out, w_out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bc(int comp, const Geo &g, const Phys &ph, double *x,
+                      const double *pres, cudaStream_t st) {
+  (void)comp; (void)g; (void)ph; (void)x; (void)pres; (void)st;
+  return cudaErrorNotSupported;
+}
+
+}  // namespace tpls

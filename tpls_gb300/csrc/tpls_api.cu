@@ -1,0 +1,886 @@
+// tpls_api.cu -- the C ABI (include/tpls_gpu.h): context, device-resident
+// state, the timestep driver and the per-routine drop-in entries.
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <vector>
+
+#include "tpls_pressure.h"
+
+using namespace tpls;
+
+namespace {
+
+constexpr int kMaxScratch = 8;
+
+}  // namespace
+
+struct tpls_ctx {
+  int nx, ny, nz;
+  tpls_params prm;
+  Geo g;
+  Phys ph;
+  int px;  // row pitch (elements)
+  cudaStream_t st = nullptr;
+  std::vector<void *> allocs;
+  // state
+  double *phi2, *u2, *v2, *w2, *pres, *pres_old;
+  double *conv_u[3], *conv_v[3], *conv_w[3], *conv_phi[3];
+  double *csf_u[3], *csf_v[3], *csf_w[3];
+  int phase = 0;  // conv0 = [phase%3], conv1 = [(phase+1)%3], conv2 = [(phase+2)%3]
+  // step work arrays
+  double *phiA, *phiB, *D;
+  signed char *flags;
+  double *mu, *fx, *fy, *fz;
+  double *rhs_u, *rhs_v, *rhs_w, *rhs_p;
+  double *x3[3][2];  // momentum ping-pong per component
+  int x3_final[3] = {0, 0, 0};
+  double *u_inlet;
+  double *part, *scal, *scal_host;
+  size_t part_len;
+  PoissonSolver *ps = nullptr;
+  tpls_stats stats;
+  long launches = 0;
+  bool need_exchange = true;
+  // scratch for the per-routine entries (allocated on first use)
+  double *scr[kMaxScratch] = {nullptr};
+  double *scr_mu = nullptr;
+  double *scr_uin = nullptr;
+  signed char *scr_flags = nullptr;
+};
+
+enum { SC_ERR_PHI = 0, SC_ERR_U, SC_ERR_V, SC_ERR_W, SC_VOL, SC_N };
+
+#define TCK(x)                                                           \
+  do {                                                                   \
+    cudaError_t e_ = (x);                                                \
+    if (e_ != cudaSuccess) return TPLS_ERR_CUDA_BASE + (int)e_;          \
+  } while (0)
+#define LCK(ctx, x)                                                      \
+  do {                                                                   \
+    cudaError_t e_ = (x);                                                \
+    (ctx)->launches++;                                                   \
+    if (e_ != cudaSuccess) return TPLS_ERR_CUDA_BASE + (int)e_;          \
+  } while (0)
+
+static int nz_planes(int kind, int nz) { return kind == 0 ? nz + 2 : (kind == 1 ? nz : nz + 1); }
+
+// device array in the pitched layout; returns the pointer to element (0,0,0)
+static cudaError_t alloc_field(tpls_ctx *c, int rows_before, int rows, int nzp, double **out) {
+  void *base = nullptr;
+  const size_t n = (size_t)c->px * rows * nzp + 8;
+  cudaError_t e = cudaMalloc(&base, n * sizeof(double));
+  if (e != cudaSuccess) return e;
+  c->allocs.push_back(base);
+  e = cudaMemset(base, 0, n * sizeof(double));
+  if (e != cudaSuccess) return e;
+  *out = (double *)base + XOFF + (size_t)c->px * rows_before;
+  return cudaSuccess;
+}
+static cudaError_t alloc_p(tpls_ctx *c, double **out) { return alloc_field(c, 0, c->ny + 2, c->nz + 2, out); }
+
+static int field_kind(int f) {
+  switch (f) {
+    case TPLS_F_U2: case TPLS_F_V2: case TPLS_F_CONV0_U: case TPLS_F_CONV1_U:
+    case TPLS_F_CONV0_V: case TPLS_F_CONV1_V: case TPLS_F_CSF_U0: case TPLS_F_CSF_U1:
+    case TPLS_F_CSF_V0: case TPLS_F_CSF_V1: case TPLS_F_U3: case TPLS_F_V3:
+      return 1;
+    case TPLS_F_W2: case TPLS_F_CONV0_W: case TPLS_F_CONV1_W: case TPLS_F_CSF_W0:
+    case TPLS_F_CSF_W1: case TPLS_F_W3:
+      return 2;
+    default:
+      return 0;
+  }
+}
+
+static double *field_ptr(tpls_ctx *c, int f) {
+  const int s0 = c->phase % 3, s1 = (c->phase + 1) % 3, s2 = (c->phase + 2) % 3;
+  switch (f) {
+    case TPLS_F_PHI2: return c->phi2;
+    case TPLS_F_U2: return c->u2;
+    case TPLS_F_V2: return c->v2;
+    case TPLS_F_W2: return c->w2;
+    case TPLS_F_PRES: return c->pres;
+    case TPLS_F_PRES_OLD: return c->pres_old;
+    case TPLS_F_CONV0_U: return c->conv_u[s0];
+    case TPLS_F_CONV1_U: return c->conv_u[s1];
+    case TPLS_F_CONV0_V: return c->conv_v[s0];
+    case TPLS_F_CONV1_V: return c->conv_v[s1];
+    case TPLS_F_CONV0_W: return c->conv_w[s0];
+    case TPLS_F_CONV1_W: return c->conv_w[s1];
+    case TPLS_F_CSF_U0: return c->csf_u[s0];
+    case TPLS_F_CSF_U1: return c->csf_u[s1];
+    case TPLS_F_CSF_V0: return c->csf_v[s0];
+    case TPLS_F_CSF_V1: return c->csf_v[s1];
+    case TPLS_F_CSF_W0: return c->csf_w[s0];
+    case TPLS_F_CSF_W1: return c->csf_w[s1];
+    case TPLS_F_CONV0_PHI: return c->conv_phi[s0];
+    case TPLS_F_CONV1_PHI: return c->conv_phi[s1];
+    // last step's intermediates: after the rotation the step's conv2 sits
+    // in the conv1 slot
+    case TPLS_F_CONV2_PHI: return c->conv_phi[s1];
+    case TPLS_F_PHI3: return c->phi2;
+    case TPLS_F_RHS_P: return c->rhs_p;
+    case TPLS_F_U3: return c->x3[0][c->x3_final[0]];
+    case TPLS_F_V3: return c->x3[1][c->x3_final[1]];
+    case TPLS_F_W3: return c->x3[2][c->x3_final[2]];
+    default: return nullptr;
+  }
+  (void)s2;
+}
+
+static cudaError_t h2d(tpls_ctx *c, double *dev0, const double *host, int nzp) {
+  const size_t w = sizeof(double) * (size_t)(c->nx + 2);
+  return cudaMemcpy2DAsync(dev0, sizeof(double) * c->px, host, w, w, (size_t)(c->ny + 2) * nzp,
+                           cudaMemcpyHostToDevice, c->st);
+}
+static cudaError_t d2h(tpls_ctx *c, double *host, const double *dev0, int nzp) {
+  const size_t w = sizeof(double) * (size_t)(c->nx + 2);
+  return cudaMemcpy2DAsync(host, w, dev0, sizeof(double) * c->px, w, (size_t)(c->ny + 2) * nzp,
+                           cudaMemcpyDeviceToHost, c->st);
+}
+// viscosity_aug (-1:nx+2,-1:ny+2,0:nz+1) <-> device mu (x 0..nx+1, y -1..ny+2)
+static cudaError_t h2d_mu(tpls_ctx *c, double *mu0, const double *host) {
+  const size_t w = sizeof(double) * (size_t)(c->nx + 2);
+  return cudaMemcpy2DAsync(mu0 - c->px, sizeof(double) * c->px, host + 1, sizeof(double) * (c->nx + 4), w,
+                           (size_t)(c->ny + 4) * (c->nz + 2), cudaMemcpyHostToDevice, c->st);
+}
+static cudaError_t d2h_mu(tpls_ctx *c, double *host, const double *mu0) {
+  const size_t w = sizeof(double) * (size_t)(c->nx + 2);
+  return cudaMemcpy2DAsync(host + 1, sizeof(double) * (c->nx + 4), mu0 - c->px, sizeof(double) * c->px, w,
+                           (size_t)(c->ny + 4) * (c->nz + 2), cudaMemcpyDeviceToHost, c->st);
+}
+
+static Phys phys_from(const tpls_params &p) {
+  Phys ph;
+  ph.dx = p.dx;
+  ph.dy = p.dy;
+  ph.dz = p.dz;
+  ph.dt = p.dt;
+  ph.re = p.re;
+  ph.mu_plus = p.mu_plus;
+  ph.mu_minus = p.mu_minus;
+  ph.height = p.height;
+  ph.scap = p.scap;
+  ph.sw = p.smooth_width;
+  return ph;
+}
+
+extern "C" {
+
+const char *tpls_status_string(int s) {
+  if (s == TPLS_OK) return "ok";
+  if (s == TPLS_ERR_ARG) return "bad argument or index bounds";
+  if (s == TPLS_ERR_ALLOC) return "device allocation failed";
+  if (s == TPLS_ERR_STATE) return "call sequence error";
+  if (s == TPLS_ERR_NOT_BUILT) return "not available in this build";
+  if (s == TPLS_KSP_DIVERGED_ITS) return "pressure solve: KSP_DIVERGED_ITS";
+  if (s == TPLS_KSP_DIVERGED_NAN) return "pressure solve: KSP_DIVERGED_NAN";
+  if (s >= TPLS_ERR_CUDA_BASE) return cudaGetErrorString((cudaError_t)(s - TPLS_ERR_CUDA_BASE));
+  return "unknown status";
+}
+
+int tpls_gpu_destroy(tpls_ctx *c) {
+  if (!c) return TPLS_OK;
+  if (c->st) cudaStreamSynchronize(c->st);
+  poisson_destroy(c->ps);
+  for (void *p : c->allocs) cudaFree(p);
+  if (c->scal_host) cudaFreeHost(c->scal_host);
+  if (c->st) cudaStreamDestroy(c->st);
+  delete c;
+  return TPLS_OK;
+}
+
+static int create_impl(int nx, int ny, int nz, const tpls_params *prm, const double *u_inlet,
+                       tpls_ctx *c) {
+  c->nx = nx;
+  c->ny = ny;
+  c->nz = nz;
+  c->prm = *prm;
+  c->ph = phys_from(*prm);
+  c->px = ((XOFF + nx + 2) + 3) / 4 * 4;
+  c->g.nx = nx;
+  c->g.ny = ny;
+  c->g.nz = nz;
+  c->g.sy = c->px;
+  c->g.sz = c->px * (ny + 2);
+  c->g.szm = c->px * (ny + 4);
+  TCK(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
+  double **pf[] = {&c->phi2, &c->pres, &c->pres_old, &c->conv_phi[0], &c->conv_phi[1], &c->conv_phi[2],
+                   &c->phiA, &c->phiB, &c->D, &c->fx, &c->fy, &c->fz, &c->rhs_p};
+  for (double **p : pf) TCK(alloc_p(c, p));
+  double **puv[] = {&c->u2, &c->v2, &c->conv_u[0], &c->conv_u[1], &c->conv_u[2], &c->conv_v[0],
+                    &c->conv_v[1], &c->conv_v[2], &c->csf_u[0], &c->csf_u[1], &c->csf_u[2],
+                    &c->csf_v[0], &c->csf_v[1], &c->csf_v[2], &c->rhs_u, &c->rhs_v,
+                    &c->x3[0][0], &c->x3[0][1], &c->x3[1][0], &c->x3[1][1]};
+  for (double **p : puv) TCK(alloc_field(c, 0, ny + 2, nz, p));
+  double **pw[] = {&c->w2, &c->conv_w[0], &c->conv_w[1], &c->conv_w[2], &c->csf_w[0], &c->csf_w[1],
+                   &c->csf_w[2], &c->rhs_w, &c->x3[2][0], &c->x3[2][1]};
+  for (double **p : pw) TCK(alloc_field(c, 0, ny + 2, nz + 1, p));
+  TCK(alloc_field(c, 1, ny + 4, nz + 2, &c->mu));
+  {
+    void *b = nullptr;
+    const size_t n = (size_t)c->px * (ny + 2) * (nz + 2) + 64;
+    TCK(cudaMalloc(&b, n));
+    c->allocs.push_back(b);
+    TCK(cudaMemset(b, 0, n));
+    c->flags = (signed char *)b + XOFF;
+  }
+  {
+    void *b = nullptr;
+    TCK(cudaMalloc(&b, sizeof(double) * nz));
+    c->allocs.push_back(b);
+    c->u_inlet = (double *)b;
+    TCK(cudaMemcpy(c->u_inlet, u_inlet, sizeof(double) * nz, cudaMemcpyHostToDevice));
+  }
+  c->part_len = (size_t)ls_iter_blocks(c->g);
+  size_t d2 = (size_t)diff2_blocks(c->g, nz + 1);
+  if (d2 > c->part_len) c->part_len = d2;
+  {
+    void *b = nullptr;
+    TCK(cudaMalloc(&b, sizeof(double) * c->part_len));
+    c->allocs.push_back(b);
+    c->part = (double *)b;
+    TCK(cudaMalloc(&b, sizeof(double) * SC_N));
+    c->allocs.push_back(b);
+    c->scal = (double *)b;
+    TCK(cudaMemset(c->scal, 0, sizeof(double) * SC_N));
+    TCK(cudaMallocHost(&b, sizeof(double) * SC_N));
+    c->scal_host = (double *)b;
+  }
+  TCK(poisson_create(c->g, 1.0 / (prm->dy * prm->dy), 1.0 / (prm->dx * prm->dx), 1.0 / (prm->dz * prm->dz),
+                     &c->ps));
+  memset(&c->stats, 0, sizeof(c->stats));
+  TCK(cudaDeviceSynchronize());
+  return TPLS_OK;
+}
+
+int tpls_gpu_create(int nx, int ny, int nz, const tpls_params *prm, const double *u_inlet,
+                    tpls_ctx **out) {
+  if (!out || !prm || !u_inlet) return TPLS_ERR_ARG;
+  *out = nullptr;
+  if (nx < 4 || ny < 3 || nz < 4) return TPLS_ERR_ARG;
+  const double cells = (double)(nx + 8) * (ny + 4) * (nz + 2);
+  if (cells >= 2.0e9) return TPLS_ERR_ARG;  // 32-bit element offsets
+  if (!(prm->dx > 0 && prm->dy > 0 && prm->dz > 0 && prm->dt > 0 && prm->re > 0 &&
+        prm->smooth_width > 0))
+    return TPLS_ERR_ARG;
+  if (prm->precision != TPLS_PREC_FP64) return TPLS_ERR_NOT_BUILT;
+  tpls_ctx *c = new tpls_ctx();
+  int s = create_impl(nx, ny, nz, prm, u_inlet, c);
+  if (s != TPLS_OK) {
+    tpls_gpu_destroy(c);
+    return s;
+  }
+  *out = c;
+  return TPLS_OK;
+}
+
+int tpls_set_field(tpls_ctx *c, int f, const double *host) {
+  if (!c || !host || f < 0 || f >= TPLS_F_COUNT) return TPLS_ERR_ARG;
+  double *d = field_ptr(c, f);
+  if (!d) return TPLS_ERR_ARG;
+  TCK(h2d(c, d, host, nz_planes(field_kind(f), c->nz)));
+  TCK(cudaStreamSynchronize(c->st));
+  c->need_exchange = true;
+  return TPLS_OK;
+}
+
+int tpls_get_field(tpls_ctx *c, int f, double *host) {
+  if (!c || !host || f < 0 || f >= TPLS_F_COUNT) return TPLS_ERR_ARG;
+  const double *d = field_ptr(c, f);
+  if (!d) return TPLS_ERR_ARG;
+  TCK(d2h(c, host, d, nz_planes(field_kind(f), c->nz)));
+  TCK(cudaStreamSynchronize(c->st));
+  return TPLS_OK;
+}
+
+int tpls_sync(tpls_ctx *c) {
+  if (!c) return TPLS_ERR_ARG;
+  TCK(cudaStreamSynchronize(c->st));
+  return TPLS_OK;
+}
+
+long tpls_kernel_launches(const tpls_ctx *c) { return c ? c->launches : -1; }
+
+// One velocity component's Crank-Nicolson solve (main_ns_hybrid.F90:756-887).
+static int momentum(tpls_ctx *c, int comp, const double *rhs, int max_iteration) {
+  const Geo &g = c->g;
+  const int nzp = nz_planes(comp == 2 ? 2 : 1, c->nz);
+  const int fuse = (g.ny % 2 == 0);
+  double **X = c->x3[comp];
+  TCK(cudaMemsetAsync(X[0] - XOFF, 0, sizeof(double) * ((size_t)c->px * (c->ny + 2) * nzp + 8), c->st));
+  const int N = max_iteration / 2;
+  for (int it = 1; it <= N; it++) {
+    double *src = X[(it - 1) % 2], *dst = X[it % 2];
+    LCK(c, launch_jacobi(comp, g, c->ph, src, rhs, c->mu, c->pres, dst, 1, fuse, c->st));
+    if (!fuse) LCK(c, launch_exchange(g, dst, nzp, c->st));
+    LCK(c, launch_sor(comp, g, c->ph, dst, rhs, c->mu, c->pres, 0, it, 0, fuse, c->st));
+    if (!fuse) LCK(c, launch_exchange(g, dst, nzp, c->st));
+    LCK(c, launch_sor(comp, g, c->ph, dst, rhs, c->mu, c->pres, 1, it, 1, fuse, c->st));
+    if (!fuse) LCK(c, launch_exchange(g, dst, nzp, c->st));
+  }
+  c->x3_final[comp] = N % 2;
+  const int nb = diff2_blocks(g, nzp);
+  if (N >= 1) {
+    LCK(c, launch_diff2(g, X[N % 2], X[(N - 1) % 2], nzp, c->part, c->st));
+    LCK(c, finish_sum(c->part, nb, c->scal + SC_ERR_U + comp, 1, c->st));
+  } else {
+    TCK(cudaMemsetAsync(c->scal + SC_ERR_U + comp, 0, sizeof(double), c->st));
+  }
+  return TPLS_OK;
+}
+
+static int step_once(tpls_ctx *c) {
+  const Geo &g = c->g;
+  const Phys &ph = c->ph;
+  cudaStream_t st = c->st;
+  const int s0 = c->phase % 3, s1 = (c->phase + 1) % 3, s2 = (c->phase + 2) % 3;
+  if (c->need_exchange) {  // advect_phi.f90:317-322 / main_ns_hybrid.F90:728-733
+    LCK(c, launch_exchange(g, c->u2, c->nz, st));
+    LCK(c, launch_exchange(g, c->v2, c->nz, st));
+    LCK(c, launch_exchange(g, c->w2, c->nz + 1, st));
+    c->need_exchange = false;
+  }
+  // viscosity from the pre-advection level set (main_ns_hybrid.F90:646-724)
+  LCK(c, launch_visc(g, ph, c->phi2, c->mu, st));
+  // advection (:585) and level-set update + redistancing (:596)
+  LCK(c, launch_advect(g, ph, c->phi2, c->u2, c->v2, c->w2, c->conv_phi[s2], st));
+  LCK(c, launch_ls_ab3(g, ph, c->phi2, c->conv_phi[s0], c->conv_phi[s1], c->conv_phi[s2], c->phiA, st));
+  LCK(c, launch_ls_status(g, ph, c->phiA, c->D, c->flags, st));
+  const int L = c->prm.levelset;
+  if (L <= 0) {
+    TCK(cudaMemcpyAsync(c->phi2 - XOFF, c->phiA - XOFF, sizeof(double) * ((size_t)c->px * (c->ny + 2) * (c->nz + 2)),
+                        cudaMemcpyDeviceToDevice, st));
+    TCK(cudaMemsetAsync(c->scal + SC_ERR_PHI, 0, sizeof(double), st));
+  }
+  for (int it = 1; it <= L; it++) {
+    const double *src = (it == 1) ? c->phiA : ((it % 2 == 0) ? c->phiB : c->phiA);
+    double *dst = (it == L) ? c->phi2 : ((it % 2 == 1) ? c->phiB : c->phiA);
+    LCK(c, launch_ls_iter(g, ph, src, c->D, c->flags, dst, (it == L) ? c->part : nullptr, st));
+  }
+  if (L > 0) LCK(c, finish_sum(c->part, ls_iter_blocks(g), c->scal + SC_ERR_PHI, 1, st));
+  // CSF from the redistanced phi3 (:618-641)
+  LCK(c, launch_csf(g, ph, c->phi2, c->fx, c->fy, c->fz, st));
+  // convective / diffusive terms and AB3 + CN right-hand sides (:728-751)
+  LCK(c, launch_mom_rhs(0, g, ph, c->u2, c->v2, c->w2, c->mu, c->fx, c->conv_u[s1], c->conv_u[s0],
+                        c->csf_u[s1], c->csf_u[s0], c->conv_u[s2], c->csf_u[s2], c->rhs_u, nullptr, st));
+  LCK(c, launch_mom_rhs(1, g, ph, c->u2, c->v2, c->w2, c->mu, c->fy, c->conv_v[s1], c->conv_v[s0],
+                        c->csf_v[s1], c->csf_v[s0], c->conv_v[s2], c->csf_v[s2], c->rhs_v, nullptr, st));
+  LCK(c, launch_mom_rhs(2, g, ph, c->u2, c->v2, c->w2, c->mu, c->fz, c->conv_w[s1], c->conv_w[s0],
+                        c->csf_w[s1], c->csf_w[s0], c->conv_w[s2], c->csf_w[s2], c->rhs_w, nullptr, st));
+  // momentum sweeps (:756-887)
+  int s;
+  if ((s = momentum(c, 0, c->rhs_u, c->prm.mom_u))) return s;
+  if ((s = momentum(c, 1, c->rhs_v, c->prm.mom_v))) return s;
+  if ((s = momentum(c, 2, c->rhs_w, c->prm.mom_w))) return s;
+  double *u3 = c->x3[0][c->x3_final[0]], *v3 = c->x3[1][c->x3_final[1]], *w3 = c->x3[2][c->x3_final[2]];
+  // pressure source (:892) and solve (:897-913)
+  LCK(c, launch_source(g, ph, u3, v3, w3, c->rhs_p, st));
+  int its = 0, reason = 0;
+  double rn = 0.0, bn = 0.0;
+  TCK(poisson_solve(c->ps, g, ph, c->rhs_p, u3, c->u_inlet, c->pres_old, c->pres, c->prm.p_rtol,
+                    c->prm.p_maxits, &its, &rn, &bn, &reason, st, &c->launches));
+  // projection into the next state's velocity arrays (:918)
+  LCK(c, launch_project(g, ph, u3, v3, w3, c->pres, c->u_inlet, c->u2, c->v2, c->w2, st));
+  // history rotation (:2480-2509)
+  TCK(cudaMemcpyAsync(c->pres_old - XOFF, c->pres - XOFF, sizeof(double) * ((size_t)c->px * (c->ny + 2) * (c->nz + 2)),
+                      cudaMemcpyDeviceToDevice, st));
+  c->phase = (c->phase + 1) % 3;
+  c->stats.p_its = its;
+  c->stats.p_rnorm = rn;
+  c->stats.p_bnorm = bn;
+  c->stats.p_reason = reason;
+  c->stats.steps_done++;
+  if (reason < 0) return reason;
+  return TPLS_OK;
+}
+
+int tpls_step(tpls_ctx *c, int nsteps) {
+  if (!c || nsteps < 0) return TPLS_ERR_ARG;
+  for (int n = 0; n < nsteps; n++) {
+    int s = step_once(c);
+    if (s != TPLS_OK) return s;
+  }
+  return TPLS_OK;
+}
+
+// liquid volume sum over cells of (1 - H(phi)) dV (FP64)
+__global__ void k_volume(Geo g, Phys ph, const double *__restrict__ phi, double *part) {
+  const int i = blockIdx.x * 32 + threadIdx.x + 1, j = blockIdx.y * 4 + threadIdx.y + 1,
+            k = blockIdx.z + 1;
+  double e = 0.0;
+  if (i <= g.nx && j <= g.ny) {
+    const double p = phi[TPLS_IDX(g, i, j, k)];
+    double hv;
+    if (p < -ph.sw) hv = 0.0;
+    else if (p > ph.sw) hv = 1.0;
+    else hv = 0.5 + (p / (2.0 * ph.sw)) + (1.0 / (2.0 * TPLS_PI_SP)) * sin(TPLS_PI_SP * p / ph.sw);
+    e = 1.0 - hv;
+  }
+  for (int o = 16; o > 0; o >>= 1) e += __shfl_down_sync(0xffffffffu, e, o);
+  __shared__ double s[4];
+  const int t = threadIdx.y * 32 + threadIdx.x;
+  if ((t & 31) == 0) s[t >> 5] = e;
+  __syncthreads();
+  if (t == 0) part[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)] = s[0] + s[1] + s[2] + s[3];
+}
+
+int tpls_get_stats(tpls_ctx *c, tpls_stats *out) {
+  if (!c || !out) return TPLS_ERR_ARG;
+  const Geo &g = c->g;
+  dim3 grd((g.nx + 31) / 32, (g.ny + 3) / 4, g.nz);
+  k_volume<<<grd, dim3(32, 4), 0, c->st>>>(g, c->ph, c->phi2, c->part);
+  LCK(c, cudaGetLastError());
+  LCK(c, finish_sum(c->part, (int)(grd.x * grd.y * grd.z), c->scal + SC_VOL, 1, c->st));
+  TCK(cudaMemcpyAsync(c->scal_host, c->scal, sizeof(double) * SC_N, cudaMemcpyDeviceToHost, c->st));
+  TCK(cudaStreamSynchronize(c->st));
+  c->stats.err_phi = c->scal_host[SC_ERR_PHI];
+  c->stats.err_u = c->scal_host[SC_ERR_U];
+  c->stats.err_v = c->scal_host[SC_ERR_V];
+  c->stats.err_w = c->scal_host[SC_ERR_W];
+  c->stats.liquid_volume = c->scal_host[SC_VOL] * c->prm.dx * c->prm.dy * c->prm.dz;
+  *out = c->stats;
+  return TPLS_OK;
+}
+
+// twophase_initialisation_wave.F90:79-122: viscosity profile of the flat
+// interface and 10000 in-place sweeps of the 1-D base-state iteration.
+int tpls_base_profile(int nz, double dz, double re, double dpdl, double mu_minus, double mu_plus,
+                      double height, double smooth_width, double *u_oned) {
+  if (nz < 3 || !u_oned) return TPLS_ERR_ARG;
+  const double pi = (double)3.14159265359f;
+  const int n = nz + 1;
+  std::vector<double> visc(n + 1);
+  for (int k = 0; k <= n; k++) {
+    const double z_val = dz * k - (dz / 2.0);
+    const double phi_val = z_val - height;
+    double hv;
+    if (phi_val < -smooth_width) hv = 0.0;
+    else if (phi_val > smooth_width) hv = 1.0;
+    else hv = 0.5 + (phi_val / (2.0 * smooth_width)) + (1.0 / (2.0 * pi)) * sin(pi * phi_val / smooth_width);
+    const double temp = mu_plus * hv + mu_minus * (1.0 - hv);
+    visc[k] = temp / re;
+  }
+  std::vector<double> u(n - 1, 0.0);
+  for (int it = 0; it < 10000; it++) {
+    for (int k = 0; k <= n - 2; k++) {
+      const double umz = (k == 0) ? -2.0 * u[0] + u[1] / 3.0 : u[k - 1];
+      const double upz = (k == n - 2) ? -2.0 * u[n - 2] + u[n - 3] / 3.0 : u[k + 1];
+      const double mm = (visc[k] + visc[k + 1]) / 2.0;
+      const double mp = (visc[k + 2] + visc[k + 1]) / 2.0;
+      const double diag = (mp + mm) / (dz * dz);
+      u[k] = (1.0 / diag) * (((mp * upz + mm * umz) / (dz * dz)) - dpdl);
+    }
+  }
+  for (int k = 0; k < nz; k++) u_oned[k] = u[k];
+  return TPLS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// per-routine drop-in entries (host arrays)
+
+static int check_bounds(const tpls_ctx *c, const int *sx, const int *ex, const int *sy, const int *ey) {
+  if ((sx && *sx != 1) || (ex && *ex != c->nx) || (sy && *sy != 1) || (ey && *ey != c->ny)) return TPLS_ERR_ARG;
+  return TPLS_OK;
+}
+#define CHECKB(c, a, b, d, e)                  \
+  do {                                         \
+    if (!(c)) return TPLS_ERR_ARG;             \
+    int s_ = check_bounds((c), a, b, d, e);    \
+    if (s_) return s_;                         \
+  } while (0)
+#define REQ(cond)                        \
+  do {                                   \
+    if (!(cond)) return TPLS_ERR_ARG;    \
+  } while (0)
+
+static int scratch(tpls_ctx *c) {
+  if (c->scr[0]) return TPLS_OK;
+  for (int q = 0; q < kMaxScratch; q++) TCK(alloc_p(c, &c->scr[q]));
+  TCK(alloc_field(c, 1, c->ny + 4, c->nz + 2, &c->scr_mu));
+  void *b = nullptr;
+  TCK(cudaMalloc(&b, sizeof(double) * c->nz));
+  c->allocs.push_back(b);
+  c->scr_uin = (double *)b;
+  TCK(cudaMalloc(&b, (size_t)c->px * (c->ny + 2) * (c->nz + 2) + 64));
+  c->allocs.push_back(b);
+  c->scr_flags = (signed char *)b + XOFF;
+  return TPLS_OK;
+}
+
+static Phys phys_with(const tpls_ctx *c, const double *dx, const double *dy, const double *dz,
+                      const double *dt) {
+  Phys ph = c->ph;
+  if (dx) ph.dx = *dx;
+  if (dy) ph.dy = *dy;
+  if (dz) ph.dz = *dz;
+  if (dt) ph.dt = *dt;
+  return ph;
+}
+
+int tpls_exchange2d(tpls_ctx *c, double *uu, const int *ex, const int *ey, const int *ez, const int *sx,
+                    const int *sy, const int *sz) {
+  CHECKB(c, sx, ex, sy, ey);
+  REQ(uu && ez && sz && *sz == 0 && *ez >= 0 && *ez <= c->nz + 1);
+  int s;
+  if ((s = scratch(c))) return s;
+  const int nzp = *ez + 1;
+  TCK(h2d(c, c->scr[0], uu, nzp));
+  LCK(c, launch_exchange(c->g, c->scr[0], nzp, c->st));
+  TCK(d2h(c, uu, c->scr[0], nzp));
+  TCK(cudaStreamSynchronize(c->st));
+  return TPLS_OK;
+}
+
+int tpls_do_advect_phi(tpls_ctx *c, const double *phi2, double *u2, double *v2, double *w2, double *conv2_phi,
+                       const int *sx, const int *ex, const int *sy, const int *ey, const int *sz_p,
+                       const int *ez_p, const int *sz_uv, const int *sz_w, const int *ez_uv, const int *ez_w,
+                       const int *maxl, const int *maxn, const int *ex_max, const int *neighbours,
+                       const int *comm2d_quasiperiodic, const double *dx, const double *dy, const double *dz,
+                       const int *, const int *, const int *, const int *, const int *, const int *,
+                       const int *, const int *, const int *, const int *) {
+  CHECKB(c, sx, ex, sy, ey);
+  const int nz = c->nz;
+  REQ(phi2 && u2 && v2 && w2 && conv2_phi && dx && dy && dz);
+  REQ(!sz_p || *sz_p == 0);
+  REQ(!ez_p || *ez_p == nz + 1);
+  REQ(!sz_uv || *sz_uv == 0);
+  REQ(!sz_w || *sz_w == 0);
+  REQ(!ez_uv || *ez_uv == nz - 1);
+  REQ(!ez_w || *ez_w == nz);
+  REQ(!maxl || *maxl == c->nx + 1);
+  REQ(!maxn || *maxn == nz + 1);
+  REQ(!ex_max || *ex_max == c->nx);
+  (void)neighbours;
+  (void)comm2d_quasiperiodic;
+  int s;
+  if ((s = scratch(c))) return s;
+  const Phys ph = phys_with(c, dx, dy, dz, nullptr);
+  double *P = c->scr[0], *U = c->scr[1], *V = c->scr[2], *W = c->scr[3], *C = c->scr[4];
+  TCK(h2d(c, P, phi2, nz + 2));
+  TCK(h2d(c, U, u2, nz));
+  TCK(h2d(c, V, v2, nz));
+  TCK(h2d(c, W, w2, nz + 1));
+  TCK(cudaMemsetAsync(C - XOFF, 0, sizeof(double) * ((size_t)c->px * (c->ny + 2) * (nz + 2)), c->st));
+  LCK(c, launch_advect(c->g, ph, P, U, V, W, C, c->st));
+  LCK(c, launch_exchange(c->g, U, nz, c->st));
+  LCK(c, launch_exchange(c->g, V, nz, c->st));
+  LCK(c, launch_exchange(c->g, W, nz + 1, c->st));
+  TCK(d2h(c, conv2_phi, C, nz + 2));
+  TCK(d2h(c, u2, U, nz));
+  TCK(d2h(c, v2, V, nz));
+  TCK(d2h(c, w2, W, nz + 1));
+  TCK(cudaStreamSynchronize(c->st));
+  return TPLS_OK;
+}
+
+int tpls_do_tpls(tpls_ctx *c, double *phi2, double *phi3, double *conv0_phi, double *conv1_phi,
+                 double *conv2_phi, const int *sx, const int *ex, const int *sy, const int *ey,
+                 const int *sz_p, const int *ez_p, const int *maxn, const int *ex_max, const int *,
+                 const int *, const int *max_iteration_levelset, const int *, const int *,
+                 const double *height, double *err2, const double *dx, const double *dz, const double *dt) {
+  CHECKB(c, sx, ex, sy, ey);
+  const int nz = c->nz;
+  REQ(phi2 && phi3 && conv0_phi && conv1_phi && conv2_phi && max_iteration_levelset && height && err2 && dx &&
+      dz && dt);
+  REQ(!sz_p || *sz_p == 0);
+  REQ(!ez_p || *ez_p == nz + 1);
+  REQ(!maxn || *maxn == nz + 1);
+  REQ(!ex_max || *ex_max == c->nx);
+  int s;
+  if ((s = scratch(c))) return s;
+  Phys ph = phys_with(c, dx, nullptr, dz, dt);
+  ph.height = *height;
+  double *P2 = c->scr[0], *C0 = c->scr[1], *C1 = c->scr[2], *C2 = c->scr[3], *A = c->scr[4], *B = c->scr[5],
+         *OUT = c->scr[6], *Dd = c->scr[7];
+  TCK(h2d(c, P2, phi2, nz + 2));
+  TCK(h2d(c, C0, conv0_phi, nz + 2));
+  TCK(h2d(c, C1, conv1_phi, nz + 2));
+  TCK(h2d(c, C2, conv2_phi, nz + 2));
+  LCK(c, launch_ls_ab3(c->g, ph, P2, C0, C1, C2, A, c->st));
+  LCK(c, launch_ls_status(c->g, ph, A, Dd, c->scr_flags, c->st));
+  const int L = *max_iteration_levelset;
+  const double *src = A;
+  if (L <= 0) {
+    TCK(cudaMemsetAsync(c->scal + SC_ERR_PHI, 0, sizeof(double), c->st));
+  }
+  for (int it = 1; it <= L; it++) {
+    double *dst = (it == L) ? OUT : ((it % 2 == 1) ? B : A);
+    if (it == 1 && L > 1) dst = B;
+    LCK(c, launch_ls_iter(c->g, ph, src, Dd, c->scr_flags, dst, (it == L) ? c->part : nullptr, c->st));
+    src = dst;
+  }
+  if (L > 0) LCK(c, finish_sum(c->part, ls_iter_blocks(c->g), c->scal + SC_ERR_PHI, 1, c->st));
+  TCK(d2h(c, phi3, src, nz + 2));
+  TCK(cudaMemcpyAsync(c->scal_host, c->scal, sizeof(double) * SC_N, cudaMemcpyDeviceToHost, c->st));
+  TCK(cudaStreamSynchronize(c->st));
+  *err2 = c->scal_host[SC_ERR_PHI];
+  return TPLS_OK;
+}
+
+int tpls_get_csf(tpls_ctx *c, double *fx_csf, double *fy_csf, double *fz_csf, const double *fi, const int *sx,
+                 const int *ex, const int *sy, const int *ey, const int *n, const int *ex_max, const double *dx,
+                 const double *dy, const double *dz, const double *scap, const double *smooth_width) {
+  CHECKB(c, sx, ex, sy, ey);
+  REQ(fx_csf && fy_csf && fz_csf && fi && dx && dy && dz && scap && smooth_width);
+  REQ(!n || *n == c->nz + 1);
+  REQ(!ex_max || *ex_max == c->nx);
+  int s;
+  if ((s = scratch(c))) return s;
+  Phys ph = phys_with(c, dx, dy, dz, nullptr);
+  ph.scap = *scap;
+  ph.sw = *smooth_width;
+  const int nz = c->nz;
+  TCK(h2d(c, c->scr[0], fi, nz + 2));
+  LCK(c, launch_csf(c->g, ph, c->scr[0], c->scr[1], c->scr[2], c->scr[3], c->st));
+  TCK(d2h(c, fx_csf, c->scr[1], nz + 2));
+  TCK(d2h(c, fy_csf, c->scr[2], nz + 2));
+  TCK(d2h(c, fz_csf, c->scr[3], nz + 2));
+  TCK(cudaStreamSynchronize(c->st));
+  return TPLS_OK;
+}
+
+int tpls_get_viscosity(tpls_ctx *c, double *viscosity_aug, const double *phi, const int *ex, const int *ey,
+                       const int *sx, const int *sy, const int *maxn, const double *smooth_width,
+                       const double *re, const double *mu_minus, const double *mu_plus) {
+  CHECKB(c, sx, ex, sy, ey);
+  REQ(viscosity_aug && phi && smooth_width && re && mu_minus && mu_plus);
+  REQ(!maxn || *maxn == c->nz + 1);
+  int s;
+  if ((s = scratch(c))) return s;
+  Phys ph = c->ph;
+  ph.sw = *smooth_width;
+  ph.re = *re;
+  ph.mu_minus = *mu_minus;
+  ph.mu_plus = *mu_plus;
+  TCK(h2d(c, c->scr[0], phi, c->nz + 2));
+  LCK(c, launch_visc(c->g, ph, c->scr[0], c->scr_mu, c->st));
+  TCK(d2h_mu(c, viscosity_aug, c->scr_mu));
+  TCK(cudaStreamSynchronize(c->st));
+  return TPLS_OK;
+}
+
+static int conv_diff_entry(tpls_ctx *c, int want_conv, double *o_u, double *o_v, double *o_w,
+                           const double *va, const double *u2, const double *v2, const double *w2,
+                           const double *dx, const double *dy, const double *dz) {
+  REQ(o_u && o_v && o_w && va && u2 && v2 && w2 && dx && dy && dz);
+  int s;
+  if ((s = scratch(c))) return s;
+  const Phys ph = phys_with(c, dx, dy, dz, nullptr);
+  const int nz = c->nz;
+  double *U = c->scr[0], *V = c->scr[1], *W = c->scr[2], *OU = c->scr[3], *OV = c->scr[4], *OW = c->scr[5];
+  TCK(h2d(c, U, u2, nz));
+  TCK(h2d(c, V, v2, nz));
+  TCK(h2d(c, W, w2, nz + 1));
+  TCK(h2d_mu(c, c->scr_mu, va));
+  const size_t bytes = sizeof(double) * ((size_t)c->px * (c->ny + 2) * (nz + 2));
+  TCK(cudaMemsetAsync(OU - XOFF, 0, bytes, c->st));
+  TCK(cudaMemsetAsync(OV - XOFF, 0, bytes, c->st));
+  TCK(cudaMemsetAsync(OW - XOFF, 0, bytes, c->st));
+  LCK(c, launch_conv_diff(0, want_conv, c->g, ph, U, V, W, c->scr_mu, OU, c->st));
+  LCK(c, launch_conv_diff(1, want_conv, c->g, ph, U, V, W, c->scr_mu, OV, c->st));
+  LCK(c, launch_conv_diff(2, want_conv, c->g, ph, U, V, W, c->scr_mu, OW, c->st));
+  TCK(d2h(c, o_u, OU, nz));
+  TCK(d2h(c, o_v, OV, nz));
+  TCK(d2h(c, o_w, OW, nz + 1));
+  TCK(cudaStreamSynchronize(c->st));
+  return TPLS_OK;
+}
+
+int tpls_get_conv_all(tpls_ctx *c, double *conv_u2, double *conv_v2, double *conv_w2, const double *va,
+                      const double *u2, const double *v2, const double *w2, const int *sx, const int *sy,
+                      const int *ex, const int *ey, const int *maxn, const int *ex_max, const double *dx,
+                      const double *dy, const double *dz) {
+  CHECKB(c, sx, ex, sy, ey);
+  REQ(!maxn || *maxn == c->nz + 1);
+  REQ(!ex_max || *ex_max == c->nx);
+  return conv_diff_entry(c, 1, conv_u2, conv_v2, conv_w2, va, u2, v2, w2, dx, dy, dz);
+}
+
+int tpls_get_diffusion_all(tpls_ctx *c, double *diff_u, double *diff_v, double *diff_w, const double *va,
+                           const double *u2, const double *v2, const double *w2, const int *sx, const int *sy,
+                           const int *ex, const int *ey, const int *maxn, const int *ex_max, const double *dx,
+                           const double *dy, const double *dz) {
+  CHECKB(c, sx, ex, sy, ey);
+  REQ(!maxn || *maxn == c->nz + 1);
+  REQ(!ex_max || *ex_max == c->nx);
+  return conv_diff_entry(c, 0, diff_u, diff_v, diff_w, va, u2, v2, w2, dx, dy, dz);
+}
+
+static int jacobi_entry(tpls_ctx *c, int comp, double *x3, const double *x3_old, const double *rhs,
+                        const double *va, const double *dx, const double *dy, const double *dz,
+                        const double *dt) {
+  REQ(x3 && x3_old && rhs && va && dx && dy && dz && dt);
+  int s;
+  if ((s = scratch(c))) return s;
+  const Phys ph = phys_with(c, dx, dy, dz, dt);
+  const int nzp = nz_planes(comp == 2 ? 2 : 1, c->nz);
+  double *X = c->scr[0], *XO = c->scr[1], *R = c->scr[2];
+  TCK(h2d(c, X, x3, nzp));
+  TCK(h2d(c, XO, x3_old, nzp));
+  TCK(h2d(c, R, rhs, nzp));
+  TCK(h2d_mu(c, c->scr_mu, va));
+  LCK(c, launch_jacobi(comp, c->g, ph, XO, R, c->scr_mu, nullptr, X, 0, 0, c->st));
+  TCK(d2h(c, x3, X, nzp));
+  TCK(cudaStreamSynchronize(c->st));
+  return TPLS_OK;
+}
+
+#define JAC_ENTRY(NAME, COMP)                                                                                   \
+  int NAME(tpls_ctx *c, double *x3, const double *x3_old, const double *rhs, const double *viscosity,          \
+           const double *dx, const double *dy, const double *dz, const double *dt, const int *ex, const int *ey, \
+           const int *sx, const int *sy, const int *maxn, const int *ex_max) {                                  \
+    CHECKB(c, sx, ex, sy, ey);                                                                                  \
+    REQ(!maxn || *maxn == c->nz + 1);                                                                           \
+    REQ(!ex_max || *ex_max == c->nx);                                                                           \
+    return jacobi_entry(c, COMP, x3, x3_old, rhs, viscosity, dx, dy, dz, dt);                                   \
+  }
+JAC_ENTRY(tpls_do_jacobi_u, 0)
+JAC_ENTRY(tpls_do_jacobi_v, 1)
+JAC_ENTRY(tpls_do_jacobi_w, 2)
+
+static int sor_entry(tpls_ctx *c, int comp, double *x3, const double *rhs, const double *va, const double *dx,
+                     const double *dy, const double *dz, const double *dt, const int *flg,
+                     const int *iteration_time) {
+  REQ(x3 && rhs && va && dx && dy && dz && dt && flg && iteration_time);
+  REQ(*flg == 0 || *flg == 1);
+  int s;
+  if ((s = scratch(c))) return s;
+  const Phys ph = phys_with(c, dx, dy, dz, dt);
+  const int nzp = nz_planes(comp == 2 ? 2 : 1, c->nz);
+  double *X = c->scr[0], *R = c->scr[1];
+  TCK(h2d(c, X, x3, nzp));
+  TCK(h2d(c, R, rhs, nzp));
+  TCK(h2d_mu(c, c->scr_mu, va));
+  LCK(c, launch_sor(comp, c->g, ph, X, R, c->scr_mu, nullptr, *flg, *iteration_time, 0, 0, c->st));
+  TCK(d2h(c, x3, X, nzp));
+  TCK(cudaStreamSynchronize(c->st));
+  return TPLS_OK;
+}
+
+int tpls_do_sor_u(tpls_ctx *c, double *u3, const double *rhs, const double *viscosity, const double *dx,
+                  const double *dy, const double *dz, const double *dt, const int *ex, const int *ey,
+                  const int *sx, const int *sy, const int *maxn, const int *ex_max, const int *flg,
+                  const int *iteration_time) {
+  CHECKB(c, sx, ex, sy, ey);
+  REQ(!maxn || *maxn == c->nz + 1);
+  REQ(!ex_max || *ex_max == c->nx);
+  return sor_entry(c, 0, u3, rhs, viscosity, dx, dy, dz, dt, flg, iteration_time);
+}
+int tpls_do_sor_v(tpls_ctx *c, double *v3, const double *rhs, const double *viscosity, const double *dx,
+                  const double *dy, const double *dz, const double *dt, const int *ex, const int *ey,
+                  const int *sx, const int *sy, const int *maxn, const int *flg, const int *iteration_time) {
+  CHECKB(c, sx, ex, sy, ey);
+  REQ(!maxn || *maxn == c->nz + 1);
+  return sor_entry(c, 1, v3, rhs, viscosity, dx, dy, dz, dt, flg, iteration_time);
+}
+int tpls_do_sor_w(tpls_ctx *c, double *w3, const double *rhs, const double *viscosity, const double *dx,
+                  const double *dy, const double *dz, const double *dt, const int *ex, const int *ey,
+                  const int *sx, const int *sy, const int *maxn, const int *flg, const int *iteration_time) {
+  CHECKB(c, sx, ex, sy, ey);
+  REQ(!maxn || *maxn == c->nz + 1);
+  return sor_entry(c, 2, w3, rhs, viscosity, dx, dy, dz, dt, flg, iteration_time);
+}
+
+int tpls_get_difference(tpls_ctx *c, const double *ua, const double *ub, const int *ex, const int *ey,
+                        const int *ez, const int *sx, const int *sy, const int *sz, double *diff) {
+  CHECKB(c, sx, ex, sy, ey);
+  REQ(ua && ub && ez && sz && diff && *sz == 0 && *ez >= 0 && *ez <= c->nz + 1);
+  int s;
+  if ((s = scratch(c))) return s;
+  const int nzp = *ez + 1;
+  TCK(h2d(c, c->scr[0], ua, nzp));
+  TCK(h2d(c, c->scr[1], ub, nzp));
+  LCK(c, launch_diff2(c->g, c->scr[0], c->scr[1], nzp, c->part, c->st));
+  LCK(c, finish_sum(c->part, diff2_blocks(c->g, nzp), c->scal + SC_ERR_U, 1, c->st));
+  TCK(cudaMemcpyAsync(c->scal_host, c->scal, sizeof(double) * SC_N, cudaMemcpyDeviceToHost, c->st));
+  TCK(cudaStreamSynchronize(c->st));
+  *diff = c->scal_host[SC_ERR_U];
+  return TPLS_OK;
+}
+
+int tpls_get_source_pres(tpls_ctx *c, double *rhs, const double *u3, const double *v3, const double *w3,
+                         const int *ex, const int *ey, const int *sx, const int *sy, const int *maxn,
+                         const double *dx, const double *dy, const double *dz, const double *dt) {
+  CHECKB(c, sx, ex, sy, ey);
+  REQ(rhs && u3 && v3 && w3 && dx && dy && dz && dt);
+  REQ(!maxn || *maxn == c->nz + 1);
+  int s;
+  if ((s = scratch(c))) return s;
+  const Phys ph = phys_with(c, dx, dy, dz, dt);
+  const int nz = c->nz;
+  TCK(h2d(c, c->scr[0], u3, nz));
+  TCK(h2d(c, c->scr[1], v3, nz));
+  TCK(h2d(c, c->scr[2], w3, nz + 1));
+  LCK(c, launch_source(c->g, ph, c->scr[0], c->scr[1], c->scr[2], c->scr[3], c->st));
+  TCK(d2h(c, rhs, c->scr[3], nz + 2));
+  TCK(cudaStreamSynchronize(c->st));
+  return TPLS_OK;
+}
+
+int tpls_get_uvw_pres(tpls_ctx *c, double *u3, double *v3, double *w3, const double *p, const int *ex,
+                      const int *ey, const int *sx, const int *sy, const int *maxn, const int *ex_max,
+                      const double *dx, const double *dy, const double *dz, const double *dt,
+                      const double *u_inlet) {
+  CHECKB(c, sx, ex, sy, ey);
+  REQ(u3 && v3 && w3 && p && dx && dy && dz && dt && u_inlet);
+  REQ(!maxn || *maxn == c->nz + 1);
+  REQ(!ex_max || *ex_max == c->nx);
+  int s;
+  if ((s = scratch(c))) return s;
+  const Phys ph = phys_with(c, dx, dy, dz, dt);
+  const int nz = c->nz;
+  double *U = c->scr[0], *V = c->scr[1], *W = c->scr[2], *P = c->scr[3], *UO = c->scr[4], *VO = c->scr[5],
+         *WO = c->scr[6];
+  TCK(h2d(c, U, u3, nz));
+  TCK(h2d(c, V, v3, nz));
+  TCK(h2d(c, W, w3, nz + 1));
+  TCK(h2d(c, P, p, nz + 2));
+  TCK(cudaMemcpyAsync(c->scr_uin, u_inlet, sizeof(double) * nz, cudaMemcpyHostToDevice, c->st));
+  LCK(c, launch_project(c->g, ph, U, V, W, P, c->scr_uin, UO, VO, WO, c->st));
+  // the reference updates rows 1..ny only; its ghost rows keep their values
+  const size_t w = sizeof(double) * (size_t)(c->nx + 2);
+  for (int k = 0; k <= nz; k++) {
+    double *dsts[3] = {u3, v3, w3};
+    double *srcs[3] = {UO, VO, WO};
+    for (int q = 0; q < 3; q++) {
+      if (q < 2 && k == nz) continue;
+      TCK(cudaMemcpy2DAsync(dsts[q] + (size_t)(c->nx + 2) * ((size_t)(c->ny + 2) * k + 1), w,
+                            srcs[q] + (size_t)c->g.sz * k + c->g.sy, sizeof(double) * c->px, w, c->ny,
+                            cudaMemcpyDeviceToHost, c->st));
+    }
+  }
+  TCK(cudaStreamSynchronize(c->st));
+  return TPLS_OK;
+}
+
+int tpls_pressure_solve(tpls_ctx *c, double *pres, const double *pres_old, const double *rhs_p, const double *u3,
+                        const double *u_inlet, const double *dx, const double *dy, const double *dz,
+                        const double *dt, const double *rtol, const int *maxits, int *its, double *rnorm,
+                        int *reason) {
+  if (!c) return TPLS_ERR_ARG;
+  REQ(pres && pres_old && rhs_p && u3 && u_inlet && dx && dy && dz && dt && its && rnorm && reason);
+  REQ(*dx == c->prm.dx && *dy == c->prm.dy && *dz == c->prm.dz);  // operator is set up at create
+  int s;
+  if ((s = scratch(c))) return s;
+  const Phys ph = phys_with(c, dx, dy, dz, dt);
+  const int nz = c->nz;
+  double *P = c->scr[0], *PO = c->scr[1], *R = c->scr[2], *U = c->scr[3];
+  TCK(h2d(c, PO, pres_old, nz + 2));
+  TCK(h2d(c, R, rhs_p, nz + 2));
+  TCK(h2d(c, U, u3, nz));
+  TCK(cudaMemcpyAsync(c->scr_uin, u_inlet, sizeof(double) * nz, cudaMemcpyHostToDevice, c->st));
+  const double rt = (rtol && *rtol > 0) ? *rtol : c->prm.p_rtol;
+  const int mi = (maxits && *maxits > 0) ? *maxits : c->prm.p_maxits;
+  double bn = 0.0;
+  TCK(poisson_solve(c->ps, c->g, ph, R, U, c->scr_uin, PO, P, rt, mi, its, rnorm, &bn, reason, c->st,
+                    &c->launches));
+  TCK(d2h(c, pres, P, nz + 2));
+  TCK(cudaStreamSynchronize(c->st));
+  return (*reason < 0) ? *reason : TPLS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,87 @@
+// tpls_kernels.h -- host-side launchers of the TPLS kernels (internal).
+// Every launcher enqueues on `st` and returns the cudaError_t of the launch.
+#pragma once
+#include "tpls_common.cuh"
+
+namespace tpls {
+
+// Scalar parameters passed by value to kernels.
+struct Phys {
+  double dx, dy, dz, dt;
+  double re, mu_plus, mu_minus, height, scap, sw;
+};
+
+// Deterministic block-partial reduction buffer: kernels write one partial
+// per block into part[], finish_sum() adds them in a fixed order.
+cudaError_t finish_sum(const double *part, int nparts, double *out, int nout,
+                       cudaStream_t st);
+
+// advect_phi.f90 / weno.f90: conv2_phi from phi2, u2, v2, w2.
+cudaError_t launch_advect(const Geo &g, const Phys &ph, const double *phi2,
+                          const double *u2, const double *v2,
+                          const double *w2, double *conv2_phi,
+                          cudaStream_t st);
+// exchange2d (mpi.f90:110) on one GPU: periodic copy of rows 0 and ny+1,
+// x = 0..nx+1, nzp planes.
+cudaError_t launch_exchange(const Geo &g, double *a, int nzp, cudaStream_t st);
+
+// two_phase_levelset.f90 / levelset.f90
+cudaError_t launch_ls_ab3(const Geo &g, const Phys &ph, const double *phi2,
+                          const double *c0, const double *c1, const double *c2,
+                          double *phi3, cudaStream_t st);
+cudaError_t launch_ls_status(const Geo &g, const Phys &ph, const double *phi3,
+                             double *D, signed char *flags, cudaStream_t st);
+cudaError_t launch_ls_iter(const Geo &g, const Phys &ph, const double *pr,
+                           const double *D, const signed char *flags,
+                           double *pr_new, double *err_part, cudaStream_t st);
+int ls_iter_blocks(const Geo &g);
+cudaError_t launch_csf(const Geo &g, const Phys &ph, const double *phi3,
+                       double *fx, double *fy, double *fz, cudaStream_t st);
+cudaError_t launch_visc(const Geo &g, const Phys &ph, const double *phi2,
+                        double *mu, cudaStream_t st);
+
+// momentum_allflux.f90 + main_ns_hybrid.F90:629-641,743-751: per component
+// conv2, csf2 (history) and the AB3/CN right-hand side.
+cudaError_t launch_mom_rhs(int comp, const Geo &g, const Phys &ph,
+                           const double *u2, const double *v2,
+                           const double *w2, const double *mu,
+                           const double *fcsf, const double *c1,
+                           const double *c0, const double *s1,
+                           const double *s0, double *conv2, double *csf2,
+                           double *rhs, double *diff_out, cudaStream_t st);
+// Standalone get_conv_all / get_diffusion_all (per-routine entries).
+cudaError_t launch_conv_diff(int comp, int want_conv, const Geo &g,
+                             const Phys &ph, const double *u2,
+                             const double *v2, const double *w2,
+                             const double *mu, double *out, cudaStream_t st);
+// jacobi_iteration_allflux.f90 / sor_iteration_allflux.f90 with the
+// boundary conditions of main_ns_hybrid.F90:756-887 fused in.
+//   bc: 0 = plain reference routine (only the routine's own BCs),
+//       1 = also the driver's post-sweep BCs (u: inlet copy, pressure outlet,
+//           fictitious point; v: inlet/outlet copies; w: walls, inlet,
+//           outlet).
+cudaError_t launch_jacobi(int comp, const Geo &g, const Phys &ph,
+                          const double *xo, const double *rhs,
+                          const double *mu, const double *pres, double *x,
+                          int bc, int fuse_ghosts, cudaStream_t st);
+cudaError_t launch_sor(int comp, const Geo &g, const Phys &ph, double *x,
+                       const double *rhs, const double *mu,
+                       const double *pres, int flg, int iteration_time,
+                       int bc, int fuse_ghosts, cudaStream_t st);
+cudaError_t launch_bc(int comp, const Geo &g, const Phys &ph, double *x,
+                      const double *pres, cudaStream_t st);
+cudaError_t launch_diff2(const Geo &g, const double *a, const double *b,
+                         int nzp, double *part, cudaStream_t st);
+int diff2_blocks(const Geo &g, int nzp);
+
+// pressure.f90
+cudaError_t launch_source(const Geo &g, const Phys &ph, const double *u3,
+                          const double *v3, const double *w3, double *rhs_p,
+                          cudaStream_t st);
+cudaError_t launch_project(const Geo &g, const Phys &ph, const double *u3,
+                           const double *v3, const double *w3,
+                           const double *p, const double *u_inlet,
+                           double *u_out, double *v_out, double *w_out,
+                           cudaStream_t st);
+
+}  // namespace tpls
