@@ -113,6 +113,21 @@ const char *tpls_status_string(int status);
  * the host at every launch site). */
 long tpls_kernel_launches(const tpls_ctx *ctx);
 
+/* Device timing by phase, with CUDA events recorded on the context's stream
+ * around every launch of a phase (kernels of the momentum sweeps are timed
+ * one launch at a time).  tpls_timing_read accumulates since the last reset
+ * (reset=1 clears after reading).  ms and launches have TPLS_T_COUNT
+ * entries. */
+enum tpls_timer {
+  TPLS_T_ADVECT = 0, TPLS_T_LEVELSET, TPLS_T_CSF, TPLS_T_VISC, TPLS_T_MOM_RHS,
+  TPLS_T_JACOBI, TPLS_T_SOR, TPLS_T_PRESSURE, TPLS_T_PROJECT, TPLS_T_OTHER,
+  TPLS_T_COUNT
+};
+int tpls_timing_enable(tpls_ctx *ctx, int on);
+int tpls_timing_read(tpls_ctx *ctx, double *ms, long *launches, int reset);
+/* The cudaStream_t every kernel of this context is launched on. */
+void *tpls_stream(tpls_ctx *ctx);
+
 /* Reference initial-condition tool restated for the harness:
  * twophase_initialisation_wave.F90:79-122 base profile (Gauss-Seidel,
  * 10000 sweeps) -- writes u_oned(0:nz-1). */

@@ -32,6 +32,8 @@ TPLS_PREC_FP64 = 0
 TPLS_PREC_FP32_MIXED = 1
 
 # field ids (enum tpls_field)
+TIMERS = ["advect", "levelset", "csf", "visc", "mom_rhs", "jacobi", "sor", "pressure", "project", "other"]
+
 F = dict(PHI2=0, U2=1, V2=2, W2=3, PRES=4, PRES_OLD=5, CONV0_U=6, CONV1_U=7, CONV0_V=8,
          CONV1_V=9, CONV0_W=10, CONV1_W=11, CSF_U0=12, CSF_U1=13, CSF_V0=14, CSF_V1=15,
          CSF_W0=16, CSF_W1=17, CONV0_PHI=18, CONV1_PHI=19, CONV2_PHI=20, PHI3=21, RHS_P=22,
@@ -127,6 +129,10 @@ def load_library(path: Path | None = None) -> C.CDLL:
     lib.tpls_kernel_launches.restype = C.c_long
     lib.tpls_base_profile.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
                                       C.c_double, C.c_double, C.c_double, _DP]
+    lib.tpls_timing_enable.argtypes = [C.c_void_p, C.c_int]
+    lib.tpls_timing_read.argtypes = [C.c_void_p, _DP, C.POINTER(C.c_long), C.c_int]
+    lib.tpls_stream.argtypes = [C.c_void_p]
+    lib.tpls_stream.restype = C.c_void_p
     if path is None:
         _lib = lib
     return lib
@@ -228,6 +234,14 @@ class TplsGpu:
         self._check(self.lib.tpls_get_field(self.ctx, F[name], _ptr(out)))
         return out
 
+    def get_field_into(self, name: str, out: np.ndarray) -> np.ndarray:
+        """Download a field into an existing Fortran-ordered array (e.g. one
+        in pinned host memory)."""
+        if out.shape != self.shape(FIELD_KIND[name]):
+            raise ValueError(f"{name}: shape {out.shape} != {self.shape(FIELD_KIND[name])}")
+        self._check(self.lib.tpls_get_field(self.ctx, F[name], _ptr(out)))
+        return out
+
     def set_state(self, state: dict) -> None:
         for k, v in state.items():
             self.set_field(k, v)
@@ -250,6 +264,21 @@ class TplsGpu:
 
     def kernel_launches(self) -> int:
         return int(self.lib.tpls_kernel_launches(self.ctx))
+
+    def stream_ptr(self) -> int:
+        """cudaStream_t (as an integer) all kernels of this context run on."""
+        return int(self.lib.tpls_stream(self.ctx) or 0)
+
+    def timing_enable(self, on: bool = True) -> None:
+        self._check(self.lib.tpls_timing_enable(self.ctx, 1 if on else 0))
+
+    def timing_read(self, reset: bool = False) -> dict:
+        """{phase: (device ms, kernel launches)} accumulated since the last
+        reset, measured with CUDA events on the context stream."""
+        ms = (C.c_double * len(TIMERS))()
+        n = (C.c_long * len(TIMERS))()
+        self._check(self.lib.tpls_timing_read(self.ctx, ms, n, 1 if reset else 0))
+        return {k: (ms[i], n[i]) for i, k in enumerate(TIMERS)}
 
     # -- per-routine drop-in entries ----------------------------------------
     def do_advect_phi(self, phi2, u2, v2, w2, dx, dy, dz):

@@ -471,7 +471,7 @@ cudaError_t launch_diff2(const Geo &g, const double *a, const double *b,
 
 // ---------------------------------------------------------------------------
 // pressure.f90:16-56 get_source_pres on the full p-grid (zero outside the
-// interior; y ghost rows as periodic copies).
+// interior, ghost rows included, as the routine itself leaves them).
 __global__ void k_source(Geo g, double rdx, double rdy, double rdz, double rdt,
                          const double *__restrict__ U, const double *__restrict__ V,
                          const double *__restrict__ W, double *__restrict__ rhs) {
@@ -479,8 +479,8 @@ __global__ void k_source(Geo g, double rdx, double rdy, double rdz, double rdt,
   const int k = blockIdx.z;
   if (i > g.nx + 1 || j > g.ny + 1) return;
   double r = 0.0;
-  if (i >= 1 && i <= g.nx && k >= 1 && k <= g.nz) {
-    const int jj = wrapy(j, g.ny), jm = (jj == 1) ? g.ny : jj - 1;
+  if (i >= 1 && i <= g.nx && j >= 1 && j <= g.ny && k >= 1 && k <= g.nz) {
+    const int jj = j, jm = (jj == 1) ? g.ny : jj - 1;
     r = ((U[TPLS_IDX(g, i, jm, k - 1)] - U[TPLS_IDX(g, i - 1, jm, k - 1)]) * rdx +
          (V[TPLS_IDX(g, i, jj, k - 1)] - V[TPLS_IDX(g, i, jm, k - 1)]) * rdy +
          (W[TPLS_IDX(g, i, jm, k)] - W[TPLS_IDX(g, i, jm, k - 1)]) * rdz) *

@@ -44,6 +44,17 @@ struct tpls_ctx {
   tpls_stats stats;
   long launches = 0;
   bool need_exchange = true;
+  // phase timing (tpls_timing_*)
+  bool timing = false;
+  int cur_slot = TPLS_T_OTHER;
+  std::vector<cudaEvent_t> ev_pool;
+  struct TRec {
+    int slot;
+    cudaEvent_t a, b;
+  };
+  std::vector<TRec> pending;
+  double t_ms[TPLS_T_COUNT] = {0};
+  long t_n[TPLS_T_COUNT] = {0};
   // scratch for the per-routine entries (allocated on first use)
   double *scr[kMaxScratch] = {nullptr};
   double *scr_mu = nullptr;
@@ -62,8 +73,21 @@ enum { SC_ERR_PHI = 0, SC_ERR_U, SC_ERR_V, SC_ERR_W, SC_VOL, SC_N };
   do {                                                                   \
     cudaError_t e_ = (x);                                                \
     (ctx)->launches++;                                                   \
+    (ctx)->t_n[(ctx)->cur_slot]++;                                       \
     if (e_ != cudaSuccess) return TPLS_ERR_CUDA_BASE + (int)e_;          \
   } while (0)
+
+// Phase scope: when timing is on, CUDA events on the context stream bracket
+// everything enqueued while the scope is alive.
+static cudaEvent_t ev_get(tpls_ctx *c);
+struct PhaseScope {
+  tpls_ctx *c;
+  int prev;
+  cudaEvent_t a = nullptr;
+  int slot;
+  PhaseScope(tpls_ctx *c_, int slot_);
+  ~PhaseScope();
+};
 
 static int nz_planes(int kind, int nz) { return kind == 0 ? nz + 2 : (kind == 1 ? nz : nz + 1); }
 
@@ -168,6 +192,48 @@ static Phys phys_from(const tpls_params &p) {
   return ph;
 }
 
+static cudaEvent_t ev_get(tpls_ctx *c) {
+  if (!c->ev_pool.empty()) {
+    cudaEvent_t e = c->ev_pool.back();
+    c->ev_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+  return e;
+}
+
+PhaseScope::PhaseScope(tpls_ctx *c_, int slot_) : c(c_), prev(c_->cur_slot), slot(slot_) {
+  c->cur_slot = slot;
+  if (c->timing) {
+    a = ev_get(c);
+    if (a) cudaEventRecord(a, c->st);
+  }
+}
+PhaseScope::~PhaseScope() {
+  if (c->timing && a) {
+    cudaEvent_t b = ev_get(c);
+    if (b) {
+      cudaEventRecord(b, c->st);
+      c->pending.push_back({slot, a, b});
+    } else {
+      c->ev_pool.push_back(a);
+    }
+  }
+  c->cur_slot = prev;
+}
+
+static void timing_flush(tpls_ctx *c) {
+  for (auto &r : c->pending) {
+    float ms = 0.f;
+    if (cudaEventSynchronize(r.b) == cudaSuccess && cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess)
+      c->t_ms[r.slot] += ms;
+    c->ev_pool.push_back(r.a);
+    c->ev_pool.push_back(r.b);
+  }
+  c->pending.clear();
+}
+
 extern "C" {
 
 const char *tpls_status_string(int s) {
@@ -185,6 +251,8 @@ const char *tpls_status_string(int s) {
 int tpls_gpu_destroy(tpls_ctx *c) {
   if (!c) return TPLS_OK;
   if (c->st) cudaStreamSynchronize(c->st);
+  timing_flush(c);
+  for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
   poisson_destroy(c->ps);
   for (void *p : c->allocs) cudaFree(p);
   if (c->scal_host) cudaFreeHost(c->scal_host);
@@ -315,11 +383,20 @@ static int momentum(tpls_ctx *c, int comp, const double *rhs, int max_iteration)
   const int N = max_iteration / 2;
   for (int it = 1; it <= N; it++) {
     double *src = X[(it - 1) % 2], *dst = X[it % 2];
-    LCK(c, launch_jacobi(comp, g, c->ph, src, rhs, c->mu, c->pres, dst, 1, fuse, c->st));
+    {
+      PhaseScope ps(c, TPLS_T_JACOBI);
+      LCK(c, launch_jacobi(comp, g, c->ph, src, rhs, c->mu, c->pres, dst, 1, fuse, c->st));
+    }
     if (!fuse) LCK(c, launch_exchange(g, dst, nzp, c->st));
-    LCK(c, launch_sor(comp, g, c->ph, dst, rhs, c->mu, c->pres, 0, it, 0, fuse, c->st));
+    {
+      PhaseScope ps(c, TPLS_T_SOR);
+      LCK(c, launch_sor(comp, g, c->ph, dst, rhs, c->mu, c->pres, 0, it, 0, fuse, c->st));
+    }
     if (!fuse) LCK(c, launch_exchange(g, dst, nzp, c->st));
-    LCK(c, launch_sor(comp, g, c->ph, dst, rhs, c->mu, c->pres, 1, it, 1, fuse, c->st));
+    {
+      PhaseScope ps(c, TPLS_T_SOR);
+      LCK(c, launch_sor(comp, g, c->ph, dst, rhs, c->mu, c->pres, 1, it, 1, fuse, c->st));
+    }
     if (!fuse) LCK(c, launch_exchange(g, dst, nzp, c->st));
   }
   c->x3_final[comp] = N % 2;
@@ -345,9 +422,16 @@ static int step_once(tpls_ctx *c) {
     c->need_exchange = false;
   }
   // viscosity from the pre-advection level set (main_ns_hybrid.F90:646-724)
-  LCK(c, launch_visc(g, ph, c->phi2, c->mu, st));
+  {
+    PhaseScope ps(c, TPLS_T_VISC);
+    LCK(c, launch_visc(g, ph, c->phi2, c->mu, st));
+  }
   // advection (:585) and level-set update + redistancing (:596)
-  LCK(c, launch_advect(g, ph, c->phi2, c->u2, c->v2, c->w2, c->conv_phi[s2], st));
+  {
+    PhaseScope ps(c, TPLS_T_ADVECT);
+    LCK(c, launch_advect(g, ph, c->phi2, c->u2, c->v2, c->w2, c->conv_phi[s2], st));
+  }
+  PhaseScope *ls_scope = new PhaseScope(c, TPLS_T_LEVELSET);
   LCK(c, launch_ls_ab3(g, ph, c->phi2, c->conv_phi[s0], c->conv_phi[s1], c->conv_phi[s2], c->phiA, st));
   LCK(c, launch_ls_status(g, ph, c->phiA, c->D, c->flags, st));
   const int L = c->prm.levelset;
@@ -362,8 +446,13 @@ static int step_once(tpls_ctx *c) {
     LCK(c, launch_ls_iter(g, ph, src, c->D, c->flags, dst, (it == L) ? c->part : nullptr, st));
   }
   if (L > 0) LCK(c, finish_sum(c->part, ls_iter_blocks(g), c->scal + SC_ERR_PHI, 1, st));
+  delete ls_scope;
   // CSF from the redistanced phi3 (:618-641)
-  LCK(c, launch_csf(g, ph, c->phi2, c->fx, c->fy, c->fz, st));
+  {
+    PhaseScope ps(c, TPLS_T_CSF);
+    LCK(c, launch_csf(g, ph, c->phi2, c->fx, c->fy, c->fz, st));
+  }
+  PhaseScope *rhs_scope = new PhaseScope(c, TPLS_T_MOM_RHS);
   // convective / diffusive terms and AB3 + CN right-hand sides (:728-751)
   LCK(c, launch_mom_rhs(0, g, ph, c->u2, c->v2, c->w2, c->mu, c->fx, c->conv_u[s1], c->conv_u[s0],
                         c->csf_u[s1], c->csf_u[s0], c->conv_u[s2], c->csf_u[s2], c->rhs_u, nullptr, st));
@@ -371,6 +460,7 @@ static int step_once(tpls_ctx *c) {
                         c->csf_v[s1], c->csf_v[s0], c->conv_v[s2], c->csf_v[s2], c->rhs_v, nullptr, st));
   LCK(c, launch_mom_rhs(2, g, ph, c->u2, c->v2, c->w2, c->mu, c->fz, c->conv_w[s1], c->conv_w[s0],
                         c->csf_w[s1], c->csf_w[s0], c->conv_w[s2], c->csf_w[s2], c->rhs_w, nullptr, st));
+  delete rhs_scope;
   // momentum sweeps (:756-887)
   int s;
   if ((s = momentum(c, 0, c->rhs_u, c->prm.mom_u))) return s;
@@ -378,16 +468,25 @@ static int step_once(tpls_ctx *c) {
   if ((s = momentum(c, 2, c->rhs_w, c->prm.mom_w))) return s;
   double *u3 = c->x3[0][c->x3_final[0]], *v3 = c->x3[1][c->x3_final[1]], *w3 = c->x3[2][c->x3_final[2]];
   // pressure source (:892) and solve (:897-913)
-  LCK(c, launch_source(g, ph, u3, v3, w3, c->rhs_p, st));
   int its = 0, reason = 0;
   double rn = 0.0, bn = 0.0;
-  TCK(poisson_solve(c->ps, g, ph, c->rhs_p, u3, c->u_inlet, c->pres_old, c->pres, c->prm.p_rtol,
-                    c->prm.p_maxits, &its, &rn, &bn, &reason, st, &c->launches));
+  {
+    PhaseScope ps(c, TPLS_T_PRESSURE);
+    LCK(c, launch_source(g, ph, u3, v3, w3, c->rhs_p, st));
+    const long l0 = c->launches;
+    TCK(poisson_solve(c->ps, g, ph, c->rhs_p, u3, c->u_inlet, c->pres_old, c->pres, c->prm.p_rtol,
+                      c->prm.p_maxits, &its, &rn, &bn, &reason, st, &c->launches));
+    c->t_n[TPLS_T_PRESSURE] += c->launches - l0;
+  }
   // projection into the next state's velocity arrays (:918)
-  LCK(c, launch_project(g, ph, u3, v3, w3, c->pres, c->u_inlet, c->u2, c->v2, c->w2, st));
-  // history rotation (:2480-2509)
-  TCK(cudaMemcpyAsync(c->pres_old - XOFF, c->pres - XOFF, sizeof(double) * ((size_t)c->px * (c->ny + 2) * (c->nz + 2)),
-                      cudaMemcpyDeviceToDevice, st));
+  {
+    PhaseScope ps(c, TPLS_T_PROJECT);
+    LCK(c, launch_project(g, ph, u3, v3, w3, c->pres, c->u_inlet, c->u2, c->v2, c->w2, st));
+    // history rotation (:2480-2509)
+    TCK(cudaMemcpyAsync(c->pres_old - XOFF, c->pres - XOFF,
+                        sizeof(double) * ((size_t)c->px * (c->ny + 2) * (c->nz + 2)), cudaMemcpyDeviceToDevice, st));
+  }
+  if (c->timing) timing_flush(c);
   c->phase = (c->phase + 1) % 3;
   c->stats.p_its = its;
   c->stats.p_rnorm = rn;
@@ -427,6 +526,31 @@ __global__ void k_volume(Geo g, Phys ph, const double *__restrict__ phi, double 
   __syncthreads();
   if (t == 0) part[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)] = s[0] + s[1] + s[2] + s[3];
 }
+
+int tpls_timing_enable(tpls_ctx *c, int on) {
+  if (!c) return TPLS_ERR_ARG;
+  TCK(cudaStreamSynchronize(c->st));
+  timing_flush(c);
+  c->timing = (on != 0);
+  return TPLS_OK;
+}
+
+int tpls_timing_read(tpls_ctx *c, double *ms, long *launches, int reset) {
+  if (!c) return TPLS_ERR_ARG;
+  TCK(cudaStreamSynchronize(c->st));
+  timing_flush(c);
+  for (int q = 0; q < TPLS_T_COUNT; q++) {
+    if (ms) ms[q] = c->t_ms[q];
+    if (launches) launches[q] = c->t_n[q];
+    if (reset) {
+      c->t_ms[q] = 0.0;
+      c->t_n[q] = 0;
+    }
+  }
+  return TPLS_OK;
+}
+
+void *tpls_stream(tpls_ctx *c) { return c ? (void *)c->st : nullptr; }
 
 int tpls_get_stats(tpls_ctx *c, tpls_stats *out) {
   if (!c || !out) return TPLS_ERR_ARG;
