@@ -274,6 +274,25 @@ int tpls_pressure_solve(tpls_ctx *ctx, double *pres, const double *pres_old,
                         const double *rtol, const int *maxits, int *its,
                         double *rnorm, int *reason);
 
+/* ---- no-allocation entry ------------------------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory: a time-step loop that cannot wait for cudaMalloc/cudaFree (they
+ * may block until the device is idle), or a program whose device memory is
+ * owned by another runtime's pool or by a fixed HBM budget.  Same sum as
+ * tpls_get_difference, on DEVICE arrays ua, ub in the reference layout
+ * (0:nx+1, 0:ny+1, 0:nzp-1), result written to the device address diff,
+ * enqueued on `stream` (a cudaStream_t; NULL = default stream).  It allocates
+ * nothing: its scratch is a fixed 512 KB array inside the library (one
+ * partial per row), so ny*nzp may not exceed TPLS_NOALLOC_MAX_ROWS (larger
+ * calls return TPLS_ERR_NOALLOC_LIMIT and launch nothing).  The first call
+ * on a device looks up that array's device address (make it before any
+ * stream capture).  All calls share the array: calls that overlap on the GPU
+ * race and must be serialised by the caller. */
+#define TPLS_NOALLOC_MAX_ROWS 65536
+#define TPLS_ERR_NOALLOC_LIMIT 5
+int tpls_get_difference_noalloc(const double *ua, const double *ub, int nx,
+                                int ny, int nzp, double *diff, void *stream);
+
 /* mpi.f90:110  exchange2d on one rank = periodic-y ghost rows over the full
  * x span, for an array (0:nx+1,0:ny+1,sz:ez). */
 int tpls_exchange2d(tpls_ctx *ctx, double *uu, const int *ex, const int *ey,
