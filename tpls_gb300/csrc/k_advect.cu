@@ -1,7 +1,8 @@
 // k_advect.cu -- level-set advection: WENO5 face values and the
 // conservative flux divergence (advect_phi.f90:19-119, weno.f90:18-215).
 //
-// One thread per (i,j) column of p-cells, marching k = 1..nz.  Each face
+// One thread per (i,j) column of p-cells, marching a chunk of 16 z levels
+// (one z-face below the chunk is computed at its start).  Each face
 // value is computed once: the x-face below a thread comes from its lower
 // lane by warp shuffle (lane 0 computes it), the y-face below from the row
 // below through shared memory (row 0 of the block computes it), and the
@@ -87,6 +88,7 @@ __device__ __forceinline__ double zface(const Geo &g, const double *__restrict__
 }
 
 constexpr int ADV_BX = 32, ADV_BY = 8;
+constexpr int ADV_KC = 16;  // z levels per thread (column chunk)
 
 __global__ void __launch_bounds__(ADV_BX *ADV_BY)
     k_advect(Geo g, double rdx, double rdy, double rdz, const double *__restrict__ phi,
@@ -96,11 +98,12 @@ __global__ void __launch_bounds__(ADV_BX *ADV_BY)
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int i = blockIdx.x * ADV_BX + tx + 1;
   const int j = blockIdx.y * ADV_BY + ty + 1;
+  const int k0 = blockIdx.z * ADV_KC + 1, k1 = min(k0 + ADV_KC - 1, g.nz);
   const bool act = (i <= g.nx) && (j <= g.ny);
   const int ic = act ? i : 1, jc = act ? j : 1;  // clamped for inactive lanes
   const int jm = (jc == 1) ? g.ny : jc - 1;      // u/v/w row index j-1 (wrapped)
-  double zlo = zface(g, phi, w, ic, jc, 0);
-  for (int k = 1; k <= g.nz; k++) {
+  double zlo = zface(g, phi, w, ic, jc, k0 - 1);
+  for (int k = k0; k <= k1; k++) {
     const double xo = xface(g, phi, u, ic, jc, k);
     double xl = __shfl_up_sync(0xffffffffu, xo, 1);
     if (tx == 0) xl = xface(g, phi, u, ic - 1, jc, k);
@@ -127,7 +130,8 @@ cudaError_t launch_advect(const Geo &g, const Phys &ph, const double *phi2,
                           const double *u2, const double *v2,
                           const double *w2, double *conv2_phi,
                           cudaStream_t st) {
-  dim3 blk(ADV_BX, ADV_BY), grd((g.nx + ADV_BX - 1) / ADV_BX, (g.ny + ADV_BY - 1) / ADV_BY);
+  dim3 blk(ADV_BX, ADV_BY),
+      grd((g.nx + ADV_BX - 1) / ADV_BX, (g.ny + ADV_BY - 1) / ADV_BY, (g.nz + ADV_KC - 1) / ADV_KC);
   k_advect<<<grd, blk, 0, st>>>(g, 1.0 / ph.dx, 1.0 / ph.dy, 1.0 / ph.dz, phi2, u2, v2, w2,
                                 conv2_phi);
   return cudaGetLastError();

@@ -115,16 +115,20 @@ __device__ __forceinline__ double rs_update(const Geo &g, double h, double ktau,
   if (f & 1) {
     dc = sg * fabs(p) - D[c];
   } else if (sg > 0.0) {
-    const double aP = fmax(p - pr[c - 1], 0.0), bM = fmin(pr[c + 1] - p, 0.0);
-    const double cP = fmax(p - pr[c - g.sy], 0.0), dM = fmin(pr[c + g.sy] - p, 0.0);
-    const double eP = fmax(p - pr[c - g.sz], 0.0), fM = fmin(pr[c + g.sz] - p, 0.0);
-    dc = sg * (sqrt(fmax(aP * aP, bM * bM) + fmax(cP * cP, dM * dM) + fmax(eP * eP, fM * fM)) - h);
+    // max(aP^2, bM^2) with aP = max(p - p[i-1], 0), bM = min(p[i+1] - p, 0)
+    // equals max(p - min(p[i-1], p[i+1]), 0)^2 bit for bit (rounding of a
+    // difference and of a square are monotone), likewise in y and z.
+    const double ax = fmax(p - fmin(pr[c - 1], pr[c + 1]), 0.0);
+    const double ay = fmax(p - fmin(pr[c - g.sy], pr[c + g.sy]), 0.0);
+    const double az = fmax(p - fmin(pr[c - g.sz], pr[c + g.sz]), 0.0);
+    dc = sg * (sqrt(ax * ax + ay * ay + az * az) - h);
   } else if (sg < 0.0) {
-    const double bP = fmax(pr[c + 1] - p, 0.0), aM = fmin(p - pr[c - 1], 0.0);
-    const double dP = fmax(pr[c + g.sy] - p, 0.0), cM = fmin(p - pr[c - g.sy], 0.0);
-    const double fP = fmax(pr[c + g.sz] - p, 0.0), eM = fmin(p - pr[c - g.sz], 0.0);
+    // max(bP^2, aM^2) = max(max(p[i-1], p[i+1]) - p, 0)^2, likewise y, z
+    const double ax = fmax(fmax(pr[c - 1], pr[c + 1]) - p, 0.0);
+    const double ay = fmax(fmax(pr[c - g.sy], pr[c + g.sy]) - p, 0.0);
+    const double az = fmax(fmax(pr[c - g.sz], pr[c + g.sz]) - p, 0.0);
     // levelset.f90:274-275 sums x, then z, then y
-    dc = sg * (sqrt(fmax(bP * bP, aM * aM) + fmax(fP * fP, eM * eM) + fmax(dP * dP, cM * cM)) - h);
+    dc = sg * (sqrt(ax * ax + az * az + ay * ay) - h);
   } else {
     dc = 0.0;
   }

@@ -27,6 +27,11 @@ struct Fc {
   double px, mx, py, my, pz, mz;
 };
 
+struct Helm {
+  double ax2, ay2, az2;  // dt/(2 d^2)
+  double dtdx;           // dt/dx (u outlet condition)
+};
+
 // face viscosities, momentum_allflux.f90:91-98 (u), :145-152 (v), :187-194 (w)
 __device__ __forceinline__ Fc faces(int comp, const Geo &g, const double *__restrict__ mu, int i,
                                     int j, int k) {
@@ -63,11 +68,6 @@ __device__ __forceinline__ Fc faces(int comp, const Geo &g, const double *__rest
   return f;
 }
 
-struct Helm {
-  double ax2, ay2, az2;  // dt/(2 d^2)
-  double dtdx;           // dt/dx (u outlet condition)
-};
-
 // jacobi_iteration_allflux.f90:84-90 (same form in every Jacobi/SOR routine)
 __device__ __forceinline__ double helm(const Fc &f, const Helm &h, double xp, double xm,
                                        double yp, double ym, double zp, double zm,
@@ -88,11 +88,10 @@ struct CD {
 __device__ __forceinline__ CD conv_diff(int comp, const Geo &g, double rdx, double rdy,
                                         double rdz, const double *__restrict__ U,
                                         const double *__restrict__ V,
-                                        const double *__restrict__ W,
-                                        const double *__restrict__ mu, int i, int j, int k) {
+                                        const double *__restrict__ W, const Fc &f, int i,
+                                        int j, int k) {
   const int sy = g.sy, sz = g.sz, nzu = g.nz;  // u/v have planes 0..nz-1
   const int c = TPLS_IDX(g, i, j, k);
-  const Fc f = faces(comp, g, mu, i, j, k);
   CD r;
   if (comp == 0) {
     const double x = U[c];
@@ -163,20 +162,54 @@ __device__ __forceinline__ bool cd_valid(int comp, const Geo &g, int i, int k) {
   return true;
 }
 
+// The sweep coefficients of one point, divided by the Helmholtz diagonal
+// (jacobi_iteration_allflux.f90:84-90): x_new = cxp x[i+1] + cxm x[i-1] +
+// cyp x[j+1] + cym x[j-1] + czp x[k+1] + czm x[k-1] + rhs/diag.  For u and v
+// the wall ghost rule `-2 x(0) + x(1)/3` (and its top mirror) is folded in:
+// at k = 0 the czm slot multiplies the point itself and czp absorbs czm/3;
+// at k = nz-1 the czp slot multiplies the point itself and czm absorbs
+// czp/3.  One 64-byte record per point: (cxp, cxm, cyp, cym, czp, czm, b, 0).
+__device__ __forceinline__ void write_coef(int comp, const Geo &g, const Helm &h, const Fc &f,
+                                           double rhs, int k, double *__restrict__ rec) {
+  const double diag =
+      1.0 + h.ax2 * (f.px + f.mx) + h.ay2 * (f.py + f.my) + h.az2 * (f.pz + f.mz);
+  const double r = 1.0 / diag;
+  double czp = h.az2 * f.pz * r, czm = h.az2 * f.mz * r;
+  if (comp != 2) {
+    if (k == 0) {
+      czp += czm * (1.0 / 3.0);
+      czm = -2.0 * czm;
+    } else if (k == g.nz - 1) {
+      czm += czp * (1.0 / 3.0);
+      czp = -2.0 * czp;
+    }
+  }
+  double2 *o = reinterpret_cast<double2 *>(rec);
+  o[0] = make_double2(h.ax2 * f.px * r, h.ax2 * f.mx * r);
+  o[1] = make_double2(h.ay2 * f.py * r, h.ay2 * f.my * r);
+  o[2] = make_double2(czp, czm);
+  o[3] = make_double2(rhs * r, 0.0);
+}
+
 __global__ void __launch_bounds__(MB_X *MB_Y)
-    k_mom_rhs(int comp, Geo g, Phys ph, const double *__restrict__ U,
+    k_mom_rhs(int comp, Geo g, Phys ph, Helm hm, const double *__restrict__ U,
               const double *__restrict__ V, const double *__restrict__ W,
               const double *__restrict__ mu, const double *__restrict__ fc,
               const double *__restrict__ c1, const double *__restrict__ c0,
               const double *__restrict__ s1, const double *__restrict__ s0,
               double *__restrict__ conv2, double *__restrict__ csf2, double *__restrict__ rhs,
-              double *__restrict__ diff_out) {
+              double *__restrict__ diff_out, double *__restrict__ coef) {
   const int i = blockIdx.x * MB_X + threadIdx.x + 1, j = blockIdx.y * MB_Y + threadIdx.y + 1;
   const int k = blockIdx.z;
   if (i > g.nx || j > g.ny) return;
   const int c = TPLS_IDX(g, i, j, k);
   CD cd = {0.0, 0.0};
-  if (cd_valid(comp, g, i, k)) cd = conv_diff(comp, g, 1.0 / ph.dx, 1.0 / ph.dy, 1.0 / ph.dz, U, V, W, mu, i, j, k);
+  const bool valid = cd_valid(comp, g, i, k);
+  Fc f;
+  if (valid) {
+    f = faces(comp, g, mu, i, j, k);
+    cd = conv_diff(comp, g, 1.0 / ph.dx, 1.0 / ph.dy, 1.0 / ph.dz, U, V, W, f, i, j, k);
+  }
   // main_ns_hybrid.F90:629-641 face averages of the CSF force
   double s2;
   if (comp == 0) s2 = (fc[TPLS_IDX(g, i + 1, j + 1, k + 1)] + fc[TPLS_IDX(g, i, j + 1, k + 1)]) * 0.5;
@@ -190,8 +223,9 @@ __global__ void __launch_bounds__(MB_X *MB_Y)
                    dt * ((23.0 / 12.0) * s2 - (4.0 / 3.0) * s1[c] + (5.0 / 12.0) * s0[c]);
   conv2[c] = cd.conv;
   csf2[c] = s2;
-  rhs[c] = r;
+  if (rhs) rhs[c] = r;
   if (diff_out) diff_out[c] = cd.diff;
+  if (coef && valid) write_coef(comp, g, hm, f, r, k, coef + 8 * (size_t)c);
 }
 
 cudaError_t launch_mom_rhs(int comp, const Geo &g, const Phys &ph,
@@ -200,11 +234,16 @@ cudaError_t launch_mom_rhs(int comp, const Geo &g, const Phys &ph,
                            const double *fcsf, const double *c1,
                            const double *c0, const double *s1,
                            const double *s0, double *conv2, double *csf2,
-                           double *rhs, double *diff_out, cudaStream_t st) {
+                           double *rhs, double *diff_out, double *coef, cudaStream_t st) {
   const int nk = (comp == 2) ? g.nz + 1 : g.nz;
+  Helm hm;
+  hm.ax2 = (ph.dt / (ph.dx * ph.dx)) / 2.0;
+  hm.ay2 = (ph.dt / (ph.dy * ph.dy)) / 2.0;
+  hm.az2 = (ph.dt / (ph.dz * ph.dz)) / 2.0;
+  hm.dtdx = ph.dt / ph.dx;
   dim3 grd((g.nx + MB_X - 1) / MB_X, (g.ny + MB_Y - 1) / MB_Y, nk);
-  k_mom_rhs<<<grd, dim3(MB_X, MB_Y), 0, st>>>(comp, g, ph, u2, v2, w2, mu, fcsf, c1, c0, s1, s0,
-                                              conv2, csf2, rhs, diff_out);
+  k_mom_rhs<<<grd, dim3(MB_X, MB_Y), 0, st>>>(comp, g, ph, hm, u2, v2, w2, mu, fcsf, c1, c0, s1, s0,
+                                              conv2, csf2, rhs, diff_out, coef);
   return cudaGetLastError();
 }
 
@@ -216,7 +255,8 @@ __global__ void k_conv_diff(int comp, int want_conv, Geo g, Phys ph, const doubl
   const int i = blockIdx.x * MB_X + threadIdx.x + 1, j = blockIdx.y * MB_Y + threadIdx.y + 1;
   const int k = blockIdx.z;
   if (i > g.nx || j > g.ny || !cd_valid(comp, g, i, k)) return;
-  CD cd = conv_diff(comp, g, 1.0 / ph.dx, 1.0 / ph.dy, 1.0 / ph.dz, U, V, W, mu, i, j, k);
+  const Fc f = faces(comp, g, mu, i, j, k);
+  CD cd = conv_diff(comp, g, 1.0 / ph.dx, 1.0 / ph.dy, 1.0 / ph.dz, U, V, W, f, i, j, k);
   out[TPLS_IDX(g, i, j, k)] = want_conv ? cd.conv : cd.diff;
 }
 
@@ -531,6 +571,249 @@ cudaError_t launch_project(const Geo &g, const Phys &ph, const double *u3,
   dim3 grd((g.nx + 2 + MB_X - 1) / MB_X, (g.ny + 2 + MB_Y - 1) / MB_Y, g.nz + 1);
   k_project<<<grd, dim3(MB_X, MB_Y), 0, st>>>(g, ph.dt / ph.dx, ph.dt / ph.dy, ph.dt / ph.dz, u3, v3,
                                               w3, p, u_inlet, u_out, v_out, w_out);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Sweeps on precomputed coefficient records (see write_coef): the same
+// Jacobi / red-black SOR updates as above with the face viscosities, the
+// diagonal and its reciprocal computed once per timestep instead of once per
+// sweep.  Boundary rows and ghost copies as in the kernels above.
+struct Rec {
+  double2 x, y, z, b;  // (cxp,cxm) (cyp,cym) (czp,czm) (b,-)
+};
+__device__ __forceinline__ Rec load_rec(const double *__restrict__ coef, int c) {
+  const double2 *r = reinterpret_cast<const double2 *>(coef + 8 * (size_t)c);
+  Rec q;
+  q.x = __ldg(r);
+  q.y = __ldg(r + 1);
+  q.z = __ldg(r + 2);
+  q.b = __ldg(r + 3);
+  return q;
+}
+__device__ __forceinline__ double rec_apply(const Rec &q, double xp, double xm, double yp, double ym,
+                                            double zp, double zm) {
+  double v = fma(q.x.x, xp, q.b.x);
+  v = fma(q.x.y, xm, v);
+  v = fma(q.y.x, yp, v);
+  v = fma(q.y.y, ym, v);
+  v = fma(q.z.x, zp, v);
+  return fma(q.z.y, zm, v);
+}
+
+__global__ void __launch_bounds__(MB_X *MB_Y)
+    k_jacobi_c(int comp, Geo g, Helm h, const double *__restrict__ xo,
+               const double *__restrict__ coef, const double *__restrict__ P,
+               double *__restrict__ x, int fuse) {
+  const int i = blockIdx.x * MB_X + threadIdx.x + 1, j = blockIdx.y * MB_Y + threadIdx.y + 1;
+  const int k = blockIdx.z + (comp == 2 ? 1 : 0);
+  const int iend = (comp == 0) ? g.nx - 1 : g.nx;
+  if (i > iend || j > g.ny) return;
+  const int c = TPLS_IDX(g, i, j, k), sy = g.sy, sz = g.sz;
+  const Rec q = load_rec(coef, c);
+  const double xc = xo[c];
+  double zp, zm;
+  if (comp == 2) {
+    zp = xo[c + sz];
+    zm = xo[c - sz];
+  } else {  // walls folded into the record: the z slot multiplies the point itself
+    zp = (k == g.nz - 1) ? xc : xo[c + sz];
+    zm = (k == 0) ? xc : xo[c - sz];
+  }
+  const double v = rec_apply(q, xo[c + 1], xo[c - 1], xo[c + sy], xo[c - sy], zp, zm);
+  put(g, x, i, j, k, v, fuse);
+  if (comp == 0) {
+    if (i == 1) put(g, x, 0, j, k, v, fuse);
+    if (i == g.nx - 1) {
+      put(g, x, g.nx, j, k, u_outlet(g, h, P, v, j, k), fuse);
+      put(g, x, g.nx + 1, j, k, 0.0, fuse);
+    }
+  } else if (comp == 1) {
+    if (i == 1) put(g, x, 0, j, k, v, fuse);
+    if (i == g.nx) put(g, x, g.nx + 1, j, k, v, fuse);
+  } else {
+    const int nz = g.nz;
+    if (k == 1) put(g, x, i, j, 0, 0.0, fuse);
+    if (k == nz - 1) put(g, x, i, j, nz, 0.0, fuse);
+    if (i == 1) {
+      put(g, x, 0, j, k, v, fuse);
+      if (k == 1) put(g, x, 0, j, 0, 0.0, fuse);
+      if (k == nz - 1) put(g, x, 0, j, nz, 0.0, fuse);
+    }
+    if (i == g.nx) {
+      put(g, x, g.nx + 1, j, k, v, fuse);
+      if (k == 1) put(g, x, g.nx + 1, j, 0, 0.0, fuse);
+      if (k == nz - 1) put(g, x, g.nx + 1, j, nz, 0.0, fuse);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(MB_X *MB_Y)
+    k_sor_even_c(int comp, Geo g, Helm h, double *__restrict__ x, const double *__restrict__ coef,
+                 const double *__restrict__ P, int flg, int bc, int fuse) {
+  const int i2 = blockIdx.x * MB_X + threadIdx.x, j = blockIdx.y * MB_Y + threadIdx.y + 1;
+  const int k = blockIdx.z + (comp == 2 ? 1 : 0);
+  const int iend = (comp == 0) ? g.nx - 1 : g.nx;
+  if (i2 > (iend - 1) / 2 || j > g.ny) return;
+  const int i = 2 * i2 + 1 + ((k + j + flg) & 1);
+  double v = 0.0;
+  if (i <= iend) {
+    const int c = TPLS_IDX(g, i, j, k), sy = g.sy, sz = g.sz;
+    const Rec q = load_rec(coef, c);
+    const double xc = x[c];
+    double zp, zm;
+    if (comp == 2) {
+      zp = x[c + sz];
+      zm = x[c - sz];
+    } else {
+      zp = (k == g.nz - 1) ? xc : x[c + sz];
+      zm = (k == 0) ? xc : x[c - sz];
+    }
+    const double res = rec_apply(q, x[c + 1], x[c - 1], x[c + sy], x[c - sy], zp, zm);
+    v = xc + 1.2 * (res - xc);
+    put(g, x, i, j, k, v, fuse);
+  }
+  if (bc) sor_bc(comp, g, h, x, P, i2, i, iend, v, j, k, fuse);
+}
+
+__global__ void __launch_bounds__(64)
+    k_sor_odd_c(int comp, Geo g, Helm h, double *__restrict__ x, const double *__restrict__ coef,
+                const double *__restrict__ P, int flg, int bc, int fuse) {
+  const int i2 = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 2 + threadIdx.y + 1;
+  const int iend = (comp == 0) ? g.nx - 1 : g.nx;
+  if (i2 > (iend - 1) / 2 || j > g.ny) return;
+  const int i = 2 * i2 + 1 + ((j + flg) & 1);
+  const bool act = (i <= iend);
+  const int sy = g.sy, sz = g.sz, nz = g.nz;
+  const int k0 = (comp == 2) ? 1 : 0, k1 = nz - 1;
+  double prev = 0.0;  // relaxed value at k-1 in this column
+  for (int k = k0; k <= k1; k++) {
+    double v = 0.0;
+    if (act) {
+      const int c = TPLS_IDX(g, i, j, k);
+      const Rec q = load_rec(coef, c);
+      const double xc = x[c];
+      double zp, zm;
+      if (comp == 2) {
+        zm = (k == k0) ? x[c - sz] : prev;
+        zp = x[c + sz];
+      } else {  // k = nz-1: the czm slot (folded) multiplies the relaxed point below
+        zm = (k == 0) ? xc : prev;
+        zp = (k == nz - 1) ? xc : x[c + sz];
+      }
+      const double res = rec_apply(q, x[c + 1], x[c - 1], x[c + sy], x[c - sy], zp, zm);
+      v = xc + 1.2 * (res - xc);
+      put(g, x, i, j, k, v, fuse);
+      prev = v;
+    }
+    if (bc) sor_bc(comp, g, h, x, P, i2, i, iend, v, j, k, fuse);
+  }
+}
+
+// Odd-iteration half-sweep in two phases.  Within such a half-sweep every
+// value a point reads is the pre-sweep value except the relaxed point below
+// it in its own column, so the update is the recurrence
+//   x_new(k) = A(k) + B(k) x_new(k-1),
+//   A = x + 1.2 (partial - x),  B = 1.2 czm   (partial = all terms but czm),
+// with A and B known before the sweep.  A block owns 32 columns of one row
+// (one per x pair); for each chunk of SO_KZ levels all its threads compute
+// A, B into shared memory in parallel, then one warp runs the recurrence.
+constexpr int SO_KZ = 32, SO_T = 256;
+
+__global__ void __launch_bounds__(SO_T)
+    k_sor_odd_c2(int comp, Geo g, Helm h, double *__restrict__ x, const double *__restrict__ coef,
+                 const double *__restrict__ P, int flg, int bc, int fuse) {
+  __shared__ double sA[SO_KZ][32], sB[SO_KZ][32];
+  const int j = blockIdx.y + 1;
+  const int iend = (comp == 0) ? g.nx - 1 : g.nx;
+  const int npair = (iend + 1) / 2;
+  const int par = (j + flg) & 1;
+  const int sy = g.sy, sz = g.sz, nz = g.nz;
+  const int k0 = (comp == 2) ? 1 : 0, k1 = nz - 1;
+  double prev = 0.0;  // owned by the recurrence warp
+  for (int kc = k0; kc <= k1; kc += SO_KZ) {
+    const int kn = min(SO_KZ, k1 - kc + 1);
+    for (int t = threadIdx.x; t < kn * 32; t += SO_T) {
+      const int lk = t >> 5, col = t & 31;
+      const int i2 = blockIdx.x * 32 + col, i = 2 * i2 + 1 + par, k = kc + lk;
+      double A = 0.0, B = 0.0;
+      if (i2 < npair && i <= iend) {
+        const int c = TPLS_IDX(g, i, j, k);
+        const Rec q = load_rec(coef, c);
+        const double xc = x[c];
+        double zp;
+        if (comp == 2) zp = x[c + sz];
+        else zp = (k == nz - 1) ? xc : x[c + sz];
+        double part = fma(q.x.x, x[c + 1], q.b.x);
+        part = fma(q.x.y, x[c - 1], part);
+        part = fma(q.y.x, x[c + sy], part);
+        part = fma(q.y.y, x[c - sy], part);
+        part = fma(q.z.x, zp, part);
+        if (k == k0) {  // the point below is a wall value (w) or the point itself (u, v)
+          const double zm = (comp == 2) ? x[c - sz] : xc;
+          A = xc + 1.2 * (fma(q.z.y, zm, part) - xc);
+        } else {
+          A = xc + 1.2 * (part - xc);
+          B = 1.2 * q.z.y;
+        }
+      }
+      sA[lk][col] = A;
+      sB[lk][col] = B;
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      const int col = threadIdx.x;
+      const int i2 = blockIdx.x * 32 + col, i = 2 * i2 + 1 + par;
+      if (i2 < npair) {
+        for (int lk = 0; lk < kn; lk++) {
+          const int k = kc + lk;
+          double v = 0.0;
+          if (i <= iend) {
+            v = fma(sB[lk][col], prev, sA[lk][col]);
+            put(g, x, i, j, k, v, fuse);
+            prev = v;
+          }
+          if (bc) sor_bc(comp, g, h, x, P, i2, i, iend, v, j, k, fuse);
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+static Helm helm_of(const Phys &ph) {
+  Helm h;
+  h.ax2 = (ph.dt / (ph.dx * ph.dx)) / 2.0;
+  h.ay2 = (ph.dt / (ph.dy * ph.dy)) / 2.0;
+  h.az2 = (ph.dt / (ph.dz * ph.dz)) / 2.0;
+  h.dtdx = ph.dt / ph.dx;
+  return h;
+}
+
+cudaError_t launch_jacobi_c(int comp, const Geo &g, const Phys &ph, const double *xo,
+                            const double *coef, const double *pres, double *x, int fuse_ghosts,
+                            cudaStream_t st) {
+  const int nk = (comp == 2) ? g.nz - 1 : g.nz;
+  const int iend = (comp == 0) ? g.nx - 1 : g.nx;
+  dim3 grd((iend + MB_X - 1) / MB_X, (g.ny + MB_Y - 1) / MB_Y, nk);
+  k_jacobi_c<<<grd, dim3(MB_X, MB_Y), 0, st>>>(comp, g, helm_of(ph), xo, coef, pres, x, fuse_ghosts);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sor_c(int comp, const Geo &g, const Phys &ph, double *x, const double *coef,
+                         const double *pres, int flg, int iteration_time, int bc, int fuse_ghosts,
+                         cudaStream_t st) {
+  const int iend = (comp == 0) ? g.nx - 1 : g.nx;
+  const int npairs = (iend + 1) / 2;
+  if (iteration_time % 2 == 0) {
+    const int nk = (comp == 2) ? g.nz - 1 : g.nz;
+    dim3 grd((npairs + MB_X - 1) / MB_X, (g.ny + MB_Y - 1) / MB_Y, nk);
+    k_sor_even_c<<<grd, dim3(MB_X, MB_Y), 0, st>>>(comp, g, helm_of(ph), x, coef, pres, flg, bc,
+                                                   fuse_ghosts);
+  } else {
+    dim3 grd((npairs + 31) / 32, g.ny, 1);
+    k_sor_odd_c2<<<grd, SO_T, 0, st>>>(comp, g, helm_of(ph), x, coef, pres, flg, bc, fuse_ghosts);
+  }
   return cudaGetLastError();
 }
 

@@ -52,34 +52,66 @@ struct PoissonSolver {
   double *cinv = nullptr;  // coarsest pseudo-inverse (nc x nc), or null
   int coarse_sweeps = 0;
   double *x = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr, *bvec = nullptr;
-  double *bin = nullptr;    // inlet ghost-row data (ny*nz)
-  double *part = nullptr;   // reduction partials
-  double *s = nullptr;      // device scalars
-  double *s_host = nullptr; // pinned mirror
-  int nblk;
+  double *bin = nullptr;     // inlet ghost-row data (ny*nz)
+  double *part = nullptr;    // reduction partials (3 * rblk)
+  unsigned *counter = nullptr;  // last-block ticket of the reductions
+  double *s = nullptr;       // device scalars
+  double *s_host = nullptr;  // pinned mirror
+  int rblk;                  // blocks of the grid-stride reduction kernels
   double omega = 0.8;
 };
 
-enum { S_SUMB = 0, S_SUMX0, S_BB, S_RZ, S_PQ, S_RR, S_SUMZ, S_SUMR, S_RZNEW, S_SUMX, S_COUNT };
+// device scalars of the CG iteration
+enum { S_SUMB = 0, S_SUMX0, S_BB, S_RR, S_RZ, S_ZMEAN, S_BETA, S_ALPHA, S_SUMX, S_COUNT };
 
 static inline int nblocks(int n) { return (n + PB - 1) / PB; }
 
 // ---------------------------------------------------------------------------
-// block partial sums of up to 3 quantities
+// Reductions: a fixed grid of rblk blocks, each thread accumulating a fixed
+// strided subset, one partial per block, and the last block to finish (by
+// an atomic ticket) summing the partials in a fixed order.  The result does
+// not depend on scheduling.  Returns true in the last block, with the sums
+// in tot[] of thread 0.
 template <int NQ>
-__device__ __forceinline__ void block_partials(double (&v)[NQ], double *part, int nblk) {
+__device__ __forceinline__ bool reduce_last(double (&v)[NQ], double *part, unsigned *counter,
+                                            double (&tot)[NQ]) {
   __shared__ double sh[NQ][PB / 32];
+  __shared__ bool last;
+  const int nblk = gridDim.x;
   for (int q = 0; q < NQ; q++) {
     double a = v[q];
     for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
     if ((threadIdx.x & 31) == 0) sh[q][threadIdx.x >> 5] = a;
   }
   __syncthreads();
-  if (threadIdx.x < NQ) {
-    double a = 0.0;
-    for (int w = 0; w < PB / 32; w++) a += sh[threadIdx.x][w];
-    part[(size_t)threadIdx.x * nblk + blockIdx.x] = a;
+  if (threadIdx.x == 0) {
+    for (int q = 0; q < NQ; q++) {
+      double a = 0.0;
+      for (int w = 0; w < PB / 32; w++) a += sh[q][w];
+      part[(size_t)q * nblk + blockIdx.x] = a;
+    }
+    __threadfence();
+    last = (atomicAdd(counter, 1u) == (unsigned)(nblk - 1));
   }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+  for (int q = 0; q < NQ; q++) {
+    double a = 0.0;
+    for (int b = threadIdx.x; b < nblk; b += PB) a += __ldcg(part + (size_t)q * nblk + b);
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+    if ((threadIdx.x & 31) == 0) sh[q][threadIdx.x >> 5] = a;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int q = 0; q < NQ; q++) {
+      double a = 0.0;
+      for (int w = 0; w < PB / 32; w++) a += sh[q][w];
+      tot[q] = a;
+    }
+    *counter = 0u;
+  }
+  return true;
 }
 
 __device__ __forceinline__ double applyA(const double *__restrict__ e, int i, int j, int k, int nx,
@@ -93,22 +125,24 @@ __device__ __forceinline__ double applyA(const double *__restrict__ e, int i, in
   return cx * (2.0 * v - xm - xp) + cy * (2.0 * v - ym - yp) + cz * (2.0 * v - zm - zp);
 }
 
-// b (compact interior) = -RHS_p + inlet contribution; x0 = p_old interior.
-__global__ void k_build_b(Geo g, double dxdt_over_dy, double rdy, const double *__restrict__ rhs_p,
-                          const double *__restrict__ u3, const double *__restrict__ uin,
-                          const double *__restrict__ pold, double *__restrict__ b,
-                          double *__restrict__ x0, double *__restrict__ bin,
-                          double *__restrict__ part, int nblk) {
+#define GRID_STRIDE(c, N) for (int c = blockIdx.x * PB + threadIdx.x; c < (N); c += gridDim.x * PB)
+
+// b (compact interior) = -RHS_p + inlet contribution; x0 = p_old interior;
+// sums of b and x0.
+__global__ void __launch_bounds__(PB)
+    k_build_b(Geo g, double dxdt_over_dy, double rdy, const double *__restrict__ rhs_p,
+              const double *__restrict__ u3, const double *__restrict__ uin,
+              const double *__restrict__ pold, double *__restrict__ b, double *__restrict__ x0,
+              double *__restrict__ bin, double *part, unsigned *counter, double *s) {
   const int nx = g.nx, ny = g.ny, nz = g.nz, N = nx * ny * nz;
-  const int c = blockIdx.x * PB + threadIdx.x;
   double v[2] = {0.0, 0.0};
-  if (c < N) {
+  GRID_STRIDE(c, N) {
     const int i = c % nx, j = (c / nx) % ny, k = c / (nx * ny);
     const int pc = TPLS_IDX(g, i + 1, j + 1, k + 1);
     double bb = -rhs_p[pc];
     if (i == 0) {
       // pressure_solver.F90:280-286: b(i,0,k) = (dx/dt)(u_inlet(k-1)-u3(0,i,k-1))/dy
-      const int ju = (j == 0) ? ny : j;  // u row (j+1)-1, row 0 is the copy of row ny
+      const int ju = (j == 0) ? ny : j;  // u row (j+1)-1; row 0 is the copy of row ny
       const double bi = dxdt_over_dy * (uin[k] - u3[TPLS_IDX(g, 0, ju, k)]);
       bin[j + ny * k] = bi;
       bb += bi * rdy;
@@ -116,101 +150,118 @@ __global__ void k_build_b(Geo g, double dxdt_over_dy, double rdy, const double *
     b[c] = bb;
     const double p0 = pold[pc];
     x0[c] = p0;
-    v[0] = bb;
-    v[1] = p0;
+    v[0] += bb;
+    v[1] += p0;
   }
-  block_partials<2>(v, part, nblk);
+  double tot[2];
+  if (reduce_last<2>(v, part, counter, tot) && threadIdx.x == 0) {
+    s[S_SUMB] = tot[0];
+    s[S_SUMX0] = tot[1];
+  }
 }
 
-// b -= mean(b); r = b - A x; partial ||b||^2, ||r||^2
-__global__ void k_init_r(int nx, int ny, int nz, double cx, double cy, double cz,
-                         const double *__restrict__ s, double *__restrict__ b,
-                         const double *__restrict__ x, double *__restrict__ r,
-                         double *__restrict__ part, int nblk) {
-  const int N = nx * ny * nz, c = blockIdx.x * PB + threadIdx.x;
+// b -= mean(b); r = b - A x; ||b||^2, ||r||^2
+__global__ void __launch_bounds__(PB)
+    k_init_r(int nx, int ny, int nz, double cx, double cy, double cz, double invN, double *s,
+             double *__restrict__ b, const double *__restrict__ x, double *__restrict__ r, double *part,
+             unsigned *counter) {
+  const int N = nx * ny * nz;
+  const double mb = s[S_SUMB] * invN;
   double v[2] = {0.0, 0.0};
-  if (c < N) {
+  GRID_STRIDE(c, N) {
     const int i = c % nx, j = (c / nx) % ny, k = c / (nx * ny);
-    const double bb = b[c] - s[S_SUMB] / (double)N;
+    const double bb = b[c] - mb;
     b[c] = bb;
     const double rr = bb - applyA(x, i, j, k, nx, ny, nz, cx, cy, cz);
     r[c] = rr;
-    v[0] = bb * bb;
-    v[1] = rr * rr;
+    v[0] += bb * bb;
+    v[1] += rr * rr;
   }
-  block_partials<2>(v, part, nblk);
+  double tot[2];
+  if (reduce_last<2>(v, part, counter, tot) && threadIdx.x == 0) {
+    s[S_BB] = tot[0];
+    s[S_RR] = tot[1];
+  }
 }
 
-// q = A p; partial p.q
-__global__ void k_apply_dot(int nx, int ny, int nz, double cx, double cy, double cz,
-                            const double *__restrict__ p, double *__restrict__ q,
-                            double *__restrict__ part, int nblk) {
-  const int N = nx * ny * nz, c = blockIdx.x * PB + threadIdx.x;
+// sum z, sum r, r.z -> mean(z), rz_new = r.(z - mean z), beta = rz_new/rz
+__global__ void __launch_bounds__(PB)
+    k_zdot(int N, double invN, int first, const double *__restrict__ r, const double *__restrict__ z,
+           double *part, unsigned *counter, double *s) {
+  double v[3] = {0.0, 0.0, 0.0};
+  GRID_STRIDE(c, N) {
+    const double zz = z[c], rr = r[c];
+    v[0] += zz;
+    v[1] += rr;
+    v[2] += rr * zz;
+  }
+  double tot[3];
+  if (reduce_last<3>(v, part, counter, tot) && threadIdx.x == 0) {
+    const double zm = tot[0] * invN;
+    const double rzn = tot[2] - zm * tot[1];
+    s[S_BETA] = first ? 0.0 : rzn / s[S_RZ];
+    s[S_ZMEAN] = zm;
+    s[S_RZ] = rzn;
+  }
+}
+
+// p = (z - mean z) + beta p
+__global__ void __launch_bounds__(PB)
+    k_pupdate(int N, const double *__restrict__ s, const double *__restrict__ z, double *__restrict__ p) {
+  const double zm = s[S_ZMEAN], beta = s[S_BETA];
+  const int c = blockIdx.x * PB + threadIdx.x;
+  if (c < N) p[c] = (z[c] - zm) + beta * p[c];
+}
+
+// q = A p; p.q -> alpha = rz / p.q
+__global__ void __launch_bounds__(PB)
+    k_apply_dot(int nx, int ny, int nz, double cx, double cy, double cz, const double *__restrict__ p,
+                double *__restrict__ q, double *part, unsigned *counter, double *s) {
+  const int N = nx * ny * nz;
   double v[1] = {0.0};
-  if (c < N) {
+  GRID_STRIDE(c, N) {
     const int i = c % nx, j = (c / nx) % ny, k = c / (nx * ny);
     const double a = applyA(p, i, j, k, nx, ny, nz, cx, cy, cz);
     q[c] = a;
-    v[0] = p[c] * a;
+    v[0] += p[c] * a;
   }
-  block_partials<1>(v, part, nblk);
+  double tot[1];
+  if (reduce_last<1>(v, part, counter, tot) && threadIdx.x == 0) s[S_ALPHA] = s[S_RZ] / tot[0];
 }
 
-// x += alpha p; r -= alpha q; partial r.r   (alpha = rz/pq from device)
-__global__ void k_axpy(int N, const double *__restrict__ s, const double *__restrict__ p,
-                       const double *__restrict__ q, double *__restrict__ x,
-                       double *__restrict__ r, double *__restrict__ part, int nblk) {
-  const int c = blockIdx.x * PB + threadIdx.x;
-  const double alpha = s[S_RZ] / s[S_PQ];
+// x += alpha p; r -= alpha q; ||r||^2
+__global__ void __launch_bounds__(PB)
+    k_axpy(int N, double *s, const double *__restrict__ p, const double *__restrict__ q,
+           double *__restrict__ x, double *__restrict__ r, double *part, unsigned *counter) {
+  const double alpha = s[S_ALPHA];
   double v[1] = {0.0};
-  if (c < N) {
+  GRID_STRIDE(c, N) {
     x[c] += alpha * p[c];
     const double rr = r[c] - alpha * q[c];
     r[c] = rr;
-    v[0] = rr * rr;
+    v[0] += rr * rr;
   }
-  block_partials<1>(v, part, nblk);
+  double tot[1];
+  if (reduce_last<1>(v, part, counter, tot) && threadIdx.x == 0) s[S_RR] = tot[0];
 }
 
-// partials of sum z, sum r, r.z
-__global__ void k_zdots(int N, const double *__restrict__ r, const double *__restrict__ z,
-                        double *__restrict__ part, int nblk) {
-  const int c = blockIdx.x * PB + threadIdx.x;
-  double v[3] = {0.0, 0.0, 0.0};
-  if (c < N) {
-    v[0] = z[c];
-    v[1] = r[c];
-    v[2] = r[c] * z[c];
-  }
-  block_partials<3>(v, part, nblk);
-}
-
-// rz_new = r.(z - mean z); beta = rz_new/rz (first: beta = 0); p = z - mean z + beta p;
-// the scalar bookkeeping (rz <- rz_new) is done by thread 0 of block 0 after
-// every block has read rz: a separate tiny kernel below.
-__global__ void k_pupdate(int N, int first, const double *__restrict__ s,
-                          const double *__restrict__ z, double *__restrict__ p) {
-  const int c = blockIdx.x * PB + threadIdx.x;
-  if (c >= N) return;
-  const double zm = s[S_SUMZ] / (double)N;
-  const double rznew = s[S_RZNEW] - zm * s[S_SUMR];
-  const double beta = first ? 0.0 : rznew / s[S_RZ];
-  p[c] = (z[c] - zm) + beta * p[c];
-}
-__global__ void k_rz_roll(double *s, int N) {
-  const double zm = s[S_SUMZ] / (double)N;
-  s[S_RZ] = s[S_RZNEW] - zm * s[S_SUMR];
+__global__ void __launch_bounds__(PB)
+    k_sumx(int N, const double *__restrict__ x, double *part, unsigned *counter, double *s) {
+  double v[1] = {0.0};
+  GRID_STRIDE(c, N) v[0] += x[c];
+  double tot[1];
+  if (reduce_last<1>(v, part, counter, tot) && threadIdx.x == 0) s[S_SUMX] = tot[0];
 }
 
 // write the solution back into the full p-grid array with every ghost
 // value rebuilt from its 2-point row, and the constant fixed.
-__global__ void k_writeback(Geo g, double dy, const double *__restrict__ s,
+__global__ void k_writeback(Geo g, double dy, double invN, const double *__restrict__ s,
                             const double *__restrict__ x, const double *__restrict__ bin,
                             double *__restrict__ pres) {
   const int i = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 4 + threadIdx.y, k = blockIdx.z;
   const int nx = g.nx, ny = g.ny, nz = g.nz;
   if (i > nx + 1 || j > ny + 1) return;
-  const double shift = (s[S_SUMX0] - s[S_SUMX]) / (double)(nx * ny * nz);
+  const double shift = (s[S_SUMX0] - s[S_SUMX]) * invN;
   const int jj = wrapy(j, ny) - 1;
   const int kk = (k == 0) ? 0 : ((k == nz + 1) ? nz - 1 : k - 1);  // z ghost planes copy
   double v;
@@ -232,10 +283,13 @@ struct LevArgs {
 
 // one damped z-line Jacobi sweep: eo = (1-w) ei + w Dline^{-1}(b - N ei);
 // zero_init: ei == 0.
-__global__ void k_line_jacobi(LevArgs L, double omega, int zero_init, const double *__restrict__ thomas,
-                              const double *__restrict__ b, const double *__restrict__ ei,
-                              double *__restrict__ t, double *__restrict__ eo) {
-  const int col = blockIdx.x * PB + threadIdx.x;
+constexpr int LJB = 64;  // threads per block of the line smoother (one column each)
+
+__global__ void __launch_bounds__(LJB)
+    k_line_jacobi(LevArgs L, double omega, double one_m_omega, int zero_init,
+                  const double *__restrict__ thomas, const double *__restrict__ b,
+                  const double *__restrict__ ei, double *__restrict__ t, double *__restrict__ eo) {
+  const int col = blockIdx.x * LJB + threadIdx.x;
   const int nx = L.nx, ny = L.ny, nz = L.nz;
   if (col >= nx * ny) return;
   const int i = col % nx, j = col / nx;
@@ -260,7 +314,66 @@ __global__ void k_line_jacobi(LevArgs L, double omega, int zero_init, const doub
   for (int k = nz - 1; k >= 0; k--) {
     const int c = col + plane * k;
     xn = t[c] - ((k < nz - 1) ? th[2 * k] * xn : 0.0);
-    eo[c] = zero_init ? omega * xn : (1.0 - omega) * ei[c] + omega * xn;
+    eo[c] = zero_init ? omega * xn : one_m_omega * ei[c] + omega * xn;
+  }
+}
+
+// The same sweep for 32 columns per block in three phases: all threads
+// assemble the line right-hand sides into shared memory, one warp runs the
+// Thomas forward/backward substitution in shared memory, all threads write
+// the damped result.  Dynamic shared memory: nz * 32 doubles.
+constexpr int LJ2_T = 256;
+
+__global__ void __launch_bounds__(LJ2_T)
+    k_line_jacobi2(LevArgs L, double omega, double one_m_omega, int zero_init,
+                   const double *__restrict__ thomas, const double *__restrict__ b,
+                   const double *__restrict__ ei, double *__restrict__ eo) {
+  extern __shared__ double buf[];  // [nz][32]
+  const int nx = L.nx, ny = L.ny, nz = L.nz, ncol = nx * ny, plane = nx * ny;
+  const int col0 = blockIdx.x * 32;
+  for (int t = threadIdx.x; t < nz * 32; t += LJ2_T) {
+    const int k = t >> 5, cl = t & 31, col = col0 + cl;
+    double rhs = 0.0;
+    if (col < ncol) {
+      const int c = col + plane * k;
+      rhs = b[c];
+      if (!zero_init) {
+        const int i = col % nx, j = col / nx;
+        const int jm = (j > 0) ? -nx : nx * (ny - 1), jp = (j < ny - 1) ? nx : -nx * (ny - 1);
+        double nb = L.cy * (ei[c + jm] + ei[c + jp]);
+        if (i > 0) nb += L.cx * ei[c - 1];
+        if (i < nx - 1) nb += L.cx * ei[c + 1];
+        rhs += nb;
+      }
+    }
+    buf[t] = rhs;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const int col = col0 + threadIdx.x;
+    if (col < ncol) {
+      const int i = col % nx;
+      const int cls = (nx == 1) ? 1 : ((i == 0) ? 0 : ((i == nx - 1) ? 2 : 1));
+      const double *th = thomas + (size_t)cls * nz * 2;
+      double y = 0.0;
+      for (int k = 0; k < nz; k++) {
+        y = (buf[k * 32 + threadIdx.x] + L.cz * y) * th[2 * k + 1];
+        buf[k * 32 + threadIdx.x] = y;
+      }
+      double xn = y;
+      for (int k = nz - 2; k >= 0; k--) {
+        xn = buf[k * 32 + threadIdx.x] - th[2 * k] * xn;
+        buf[k * 32 + threadIdx.x] = xn;
+      }
+    }
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < nz * 32; t += LJ2_T) {
+    const int k = t >> 5, col = col0 + (t & 31);
+    if (col < ncol) {
+      const int c = col + plane * k;
+      eo[c] = zero_init ? omega * buf[t] : one_m_omega * ei[c] + omega * buf[t];
+    }
   }
 }
 
@@ -294,7 +407,7 @@ __device__ __forceinline__ int rstencil(int c, int nc, int coarsened, int period
   return m;
 }
 
-__global__ void k_restrict(LevArgs F, LevArgs C, int cxs, int cys, int czs,
+__global__ void k_restrict(LevArgs F, LevArgs C, int cxs, int cys, int czs, double scale,
                            const double *__restrict__ rf, double *__restrict__ bc) {
   const int c = blockIdx.x * PB + threadIdx.x;
   if (c >= C.nx * C.ny * C.nz) return;
@@ -313,7 +426,6 @@ __global__ void k_restrict(LevArgs F, LevArgs C, int cxs, int cys, int czs,
       for (int q = 0; q < mx; q++) sx += wx[q] * row[fx[q]];
       acc += wzy * sx;
     }
-  const double scale = 1.0 / (double)((cxs ? 2 : 1) * (cys ? 2 : 1) * (czs ? 2 : 1));
   bc[c] = acc * scale;
 }
 
@@ -514,6 +626,7 @@ cudaError_t poisson_create(const Geo &g, double cx, double cy, double cz,
     PCK(cudaMalloc(&L.thomas, th.size() * sizeof(double)));
     PCK(cudaMemcpy(L.thomas, th.data(), th.size() * sizeof(double), cudaMemcpyHostToDevice));
   }
+  PCK(cudaFuncSetAttribute(k_line_jacobi2, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
   const PLevel &C = S->lv.back();
   if (C.n <= 512) {
     std::vector<double> M = coarse_pinv(C);
@@ -530,8 +643,10 @@ cudaError_t poisson_create(const Geo &g, double cx, double cy, double cz,
   PCK(cudaMalloc(&S->q, nb));
   PCK(cudaMalloc(&S->bvec, nb));
   PCK(cudaMalloc(&S->bin, sizeof(double) * (size_t)g.ny * g.nz));
-  S->nblk = nblocks(S->N);
-  PCK(cudaMalloc(&S->part, sizeof(double) * (size_t)S->nblk * 3));
+  S->rblk = nblocks(S->N) < 1216 ? nblocks(S->N) : 1216;  // 8 blocks per SM on 152 SMs
+  PCK(cudaMalloc(&S->part, sizeof(double) * (size_t)S->rblk * 3));
+  PCK(cudaMalloc(&S->counter, sizeof(unsigned)));
+  PCK(cudaMemset(S->counter, 0, sizeof(unsigned)));
   PCK(cudaMalloc(&S->s, sizeof(double) * S_COUNT));
   PCK(cudaMemset(S->s, 0, sizeof(double) * S_COUNT));
   PCK(cudaMallocHost(&S->s_host, sizeof(double) * S_COUNT));
@@ -558,6 +673,7 @@ void poisson_destroy(PoissonSolver *S) {
   cudaFree(S->bvec);
   cudaFree(S->bin);
   cudaFree(S->part);
+  cudaFree(S->counter);
   cudaFree(S->s);
   cudaFreeHost(S->s_host);
   delete S;
@@ -576,42 +692,54 @@ static LevArgs largs(const PLevel &L) {
   return a;
 }
 
-// one symmetric V-cycle: e_0 = M b_0 (b_0 = level-0 rhs pointer)
-static cudaError_t vcycle(PoissonSolver *S, const double *b0, double *e0, cudaStream_t st,
-                          long *nl) {
+static void line_sweep(const PLevel &L, const LevArgs &A, double w, double w1, int zero_init,
+                       const double *b, const double *ei, double *eo, cudaStream_t st) {
+  const size_t smem = sizeof(double) * 32 * (size_t)L.nz;
+  if (smem <= 200 * 1024) {
+    k_line_jacobi2<<<(L.nx * L.ny + 31) / 32, LJ2_T, smem, st>>>(A, w, w1, zero_init, L.thomas, b, ei, eo);
+  } else {
+    k_line_jacobi<<<(L.nx * L.ny + LJB - 1) / LJB, LJB, 0, st>>>(A, w, w1, zero_init, L.thomas, b, ei, L.t,
+                                                                 eo);
+  }
+}
+
+// one symmetric V-cycle: out = M b0.  Every level pre-smooths into its
+// scratch e2 (one damped line-Jacobi sweep from zero), restricts the
+// residual, adds the prolonged coarse correction into e2 and post-smooths
+// from e2 into its result buffer (out on the finest level, e elsewhere).
+static cudaError_t vcycle(PoissonSolver *S, const double *b0, double *out, cudaStream_t st, long *nl) {
   const int nlev = (int)S->lv.size();
+  const double w = S->omega, w1 = 1.0 - S->omega;
   for (int l = 0; l < nlev; l++) {
     PLevel &L = S->lv[l];
     const double *b = (l == 0) ? b0 : L.b;
-    double *e = (l == 0) ? e0 : L.e;
+    double *res = (l == 0) ? out : L.e;
     const LevArgs A = largs(L);
     if (l == nlev - 1) {
       if (S->cinv) {
-        k_coarse_solve<<<1, 256, 0, st>>>(L.n, S->cinv, b, e);
+        k_coarse_solve<<<1, 256, 0, st>>>(L.n, S->cinv, b, res);
         (*nl)++;
       } else {
-        double *cur = e, *oth = L.e2;
-        k_line_jacobi<<<nblocks(L.nx * L.ny), PB, 0, st>>>(A, S->omega, 1, L.thomas, b, nullptr, L.t, cur);
+        double *cur = L.e2, *oth = res;
+        line_sweep(L, A, w, w1, 1, b, nullptr, cur, st);
         (*nl)++;
-        for (int s = 1; s < S->coarse_sweeps; s++) {
-          k_line_jacobi<<<nblocks(L.nx * L.ny), PB, 0, st>>>(A, S->omega, 0, L.thomas, b, cur, L.t, oth);
+        for (int sw = 1; sw < S->coarse_sweeps; sw++) {
+          line_sweep(L, A, w, w1, 0, b, cur, oth, st);
           (*nl)++;
           double *tmp = cur;
           cur = oth;
           oth = tmp;
         }
-        if (cur != e) {
-          PCK(cudaMemcpyAsync(e, cur, sizeof(double) * L.n, cudaMemcpyDeviceToDevice, st));
-        }
+        if (cur != res) PCK(cudaMemcpyAsync(res, cur, sizeof(double) * L.n, cudaMemcpyDeviceToDevice, st));
       }
       PCK(cudaGetLastError());
       break;
     }
-    // pre-smoothing (one sweep from zero) and residual, then restrict
-    k_line_jacobi<<<nblocks(L.nx * L.ny), PB, 0, st>>>(A, S->omega, 1, L.thomas, b, nullptr, L.t, e);
-    k_residual<<<nblocks(L.n), PB, 0, st>>>(A, b, e, L.r);
+    line_sweep(L, A, w, w1, 1, b, nullptr, L.e2, st);
+    k_residual<<<nblocks(L.n), PB, 0, st>>>(A, b, L.e2, L.r);
     const PLevel &C = S->lv[l + 1];
-    k_restrict<<<nblocks(C.n), PB, 0, st>>>(A, largs(C), C.cxs, C.cys, C.czs, L.r, C.b);
+    const double scale = 1.0 / (double)((C.cxs ? 2 : 1) * (C.cys ? 2 : 1) * (C.czs ? 2 : 1));
+    k_restrict<<<nblocks(C.n), PB, 0, st>>>(A, largs(C), C.cxs, C.cys, C.czs, scale, L.r, C.b);
     *nl += 3;
     PCK(cudaGetLastError());
   }
@@ -619,12 +747,10 @@ static cudaError_t vcycle(PoissonSolver *S, const double *b0, double *e0, cudaSt
     PLevel &L = S->lv[l];
     const PLevel &C = S->lv[l + 1];
     const double *b = (l == 0) ? b0 : L.b;
-    double *e = (l == 0) ? e0 : L.e;
+    double *res = (l == 0) ? out : L.e;
     const LevArgs A = largs(L);
-    k_prolong_add<<<nblocks(L.n), PB, 0, st>>>(A, largs(C), C.cxs, C.cys, C.czs, C.e, e);
-    // post-smoothing (same damped line Jacobi: the cycle is symmetric)
-    k_line_jacobi<<<nblocks(L.nx * L.ny), PB, 0, st>>>(A, S->omega, 0, L.thomas, b, e, L.t, L.e2);
-    PCK(cudaMemcpyAsync(e, L.e2, sizeof(double) * L.n, cudaMemcpyDeviceToDevice, st));
+    k_prolong_add<<<nblocks(L.n), PB, 0, st>>>(A, largs(C), C.cxs, C.cys, C.czs, C.e, L.e2);
+    line_sweep(L, A, w, w1, 0, b, L.e2, res, st);
     *nl += 2;
     PCK(cudaGetLastError());
   }
@@ -637,15 +763,14 @@ cudaError_t poisson_solve(PoissonSolver *S, const Geo &g, const Phys &ph,
                           double *pres, double rtol, int maxits, int *its,
                           double *rnorm, double *bnorm, int *reason,
                           cudaStream_t st, long *nl) {
-  const int N = S->N, nb = S->nblk;
+  const int N = S->N, rb = S->rblk;
+  const double invN = 1.0 / (double)N;
   const PLevel &F = S->lv[0];
-  k_build_b<<<nb, PB, 0, st>>>(g, (ph.dx / ph.dt) / ph.dy, 1.0 / ph.dy, rhs_p, u3, u_inlet, pres_old,
-                               S->bvec, S->x, S->bin, S->part, nb);
-  PCK(finish_sum(S->part, nb, S->s + S_SUMB, 2, st));  // S_SUMB, S_SUMX0
-  k_init_r<<<nb, PB, 0, st>>>(F.nx, F.ny, F.nz, F.cx, F.cy, F.cz, S->s, S->bvec, S->x, S->r, S->part, nb);
-  PCK(finish_sum(S->part, nb, S->s + S_BB, 1, st));
-  PCK(finish_sum(S->part + nb, nb, S->s + S_RR, 1, st));
-  *nl += 5;
+  k_build_b<<<rb, PB, 0, st>>>(g, (ph.dx / ph.dt) / ph.dy, 1.0 / ph.dy, rhs_p, u3, u_inlet, pres_old,
+                               S->bvec, S->x, S->bin, S->part, S->counter, S->s);
+  k_init_r<<<rb, PB, 0, st>>>(F.nx, F.ny, F.nz, F.cx, F.cy, F.cz, invN, S->s, S->bvec, S->x, S->r, S->part,
+                              S->counter);
+  *nl += 2;
   PCK(cudaGetLastError());
   PCK(cudaMemcpyAsync(S->s_host, S->s, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, st));
   PCK(cudaStreamSynchronize(st));
@@ -656,38 +781,28 @@ cudaError_t poisson_solve(PoissonSolver *S, const Geo &g, const Phys &ph,
   const double target = rtol * bb;
   if (!(rr == rr)) rsn = TPLS_KSP_DIVERGED_NAN;
   else if (rr <= target || bb == 0.0) rsn = TPLS_KSP_CONVERGED_RTOL;
+  const int nb = nblocks(N);
   while (rsn == 0) {
     PCK(vcycle(S, S->r, S->z, st, nl));
-    k_zdots<<<nb, PB, 0, st>>>(N, S->r, S->z, S->part, nb);
-    PCK(finish_sum(S->part, nb, S->s + S_SUMZ, 2, st));  // S_SUMZ, S_SUMR
-    PCK(finish_sum(S->part + 2 * (size_t)nb, nb, S->s + S_RZNEW, 1, st));
-    k_pupdate<<<nb, PB, 0, st>>>(N, it == 0, S->s, S->z, S->p);
-    k_rz_roll<<<1, 1, 0, st>>>(S->s, N);
-    k_apply_dot<<<nb, PB, 0, st>>>(F.nx, F.ny, F.nz, F.cx, F.cy, F.cz, S->p, S->q, S->part, nb);
-    PCK(finish_sum(S->part, nb, S->s + S_PQ, 1, st));
-    k_axpy<<<nb, PB, 0, st>>>(N, S->s, S->p, S->q, S->x, S->r, S->part, nb);
-    PCK(finish_sum(S->part, nb, S->s + S_RR, 1, st));
-    *nl += 10;
+    k_zdot<<<rb, PB, 0, st>>>(N, invN, it == 0, S->r, S->z, S->part, S->counter, S->s);
+    k_pupdate<<<nb, PB, 0, st>>>(N, S->s, S->z, S->p);
+    k_apply_dot<<<rb, PB, 0, st>>>(F.nx, F.ny, F.nz, F.cx, F.cy, F.cz, S->p, S->q, S->part, S->counter, S->s);
+    k_axpy<<<rb, PB, 0, st>>>(N, S->s, S->p, S->q, S->x, S->r, S->part, S->counter);
+    *nl += 4;
     PCK(cudaGetLastError());
     it++;
-    PCK(cudaMemcpyAsync(S->s_host, S->s, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, st));
+    PCK(cudaMemcpyAsync(S->s_host + S_RR, S->s + S_RR, sizeof(double), cudaMemcpyDeviceToHost, st));
     PCK(cudaStreamSynchronize(st));
     rr = sqrt(S->s_host[S_RR]);
     if (!(rr == rr)) rsn = TPLS_KSP_DIVERGED_NAN;
     else if (rr <= target) rsn = TPLS_KSP_CONVERGED_RTOL;
     else if (it >= maxits) rsn = TPLS_KSP_DIVERGED_ITS;
   }
-  // sum x for the constant, then write back
-  {
-    double *dummy = S->z;  // r.z partials not needed: reuse k_zdots on (x, x)
-    (void)dummy;
-    k_zdots<<<nb, PB, 0, st>>>(N, S->x, S->x, S->part, nb);  // part[0] = sum x
-    PCK(finish_sum(S->part, nb, S->s + S_SUMX, 1, st));
-    dim3 grd((g.nx + 2 + 31) / 32, (g.ny + 2 + 3) / 4, g.nz + 2);
-    k_writeback<<<grd, dim3(32, 4), 0, st>>>(g, ph.dy, S->s, S->x, S->bin, pres);
-    *nl += 3;
-    PCK(cudaGetLastError());
-  }
+  k_sumx<<<rb, PB, 0, st>>>(N, S->x, S->part, S->counter, S->s);
+  dim3 grd((g.nx + 2 + 31) / 32, (g.ny + 2 + 3) / 4, g.nz + 2);
+  k_writeback<<<grd, dim3(32, 4), 0, st>>>(g, ph.dy, invN, S->s, S->x, S->bin, pres);
+  *nl += 2;
+  PCK(cudaGetLastError());
   *its = it;
   *rnorm = rr;
   *reason = rsn;

@@ -34,7 +34,8 @@ struct tpls_ctx {
   double *phiA, *phiB, *D;
   signed char *flags;
   double *mu, *fx, *fy, *fz;
-  double *rhs_u, *rhs_v, *rhs_w, *rhs_p;
+  double *rhs_p;
+  double *coef[3];  // per-component sweep records (8 doubles per point)
   double *x3[3][2];  // momentum ping-pong per component
   int x3_final[3] = {0, 0, 0};
   double *u_inlet;
@@ -281,12 +282,20 @@ static int create_impl(int nx, int ny, int nz, const tpls_params *prm, const dou
   for (double **p : pf) TCK(alloc_p(c, p));
   double **puv[] = {&c->u2, &c->v2, &c->conv_u[0], &c->conv_u[1], &c->conv_u[2], &c->conv_v[0],
                     &c->conv_v[1], &c->conv_v[2], &c->csf_u[0], &c->csf_u[1], &c->csf_u[2],
-                    &c->csf_v[0], &c->csf_v[1], &c->csf_v[2], &c->rhs_u, &c->rhs_v,
+                    &c->csf_v[0], &c->csf_v[1], &c->csf_v[2],
                     &c->x3[0][0], &c->x3[0][1], &c->x3[1][0], &c->x3[1][1]};
   for (double **p : puv) TCK(alloc_field(c, 0, ny + 2, nz, p));
   double **pw[] = {&c->w2, &c->conv_w[0], &c->conv_w[1], &c->conv_w[2], &c->csf_w[0], &c->csf_w[1],
-                   &c->csf_w[2], &c->rhs_w, &c->x3[2][0], &c->x3[2][1]};
+                   &c->csf_w[2], &c->x3[2][0], &c->x3[2][1]};
   for (double **p : pw) TCK(alloc_field(c, 0, ny + 2, nz + 1, p));
+  for (int q = 0; q < 3; q++) {  // one 64-byte record per point of each component
+    void *b = nullptr;
+    const size_t n = (size_t)8 * c->px * (ny + 2) * (q == 2 ? nz + 1 : nz);
+    TCK(cudaMalloc(&b, n * sizeof(double)));
+    c->allocs.push_back(b);
+    TCK(cudaMemset(b, 0, n * sizeof(double)));
+    c->coef[q] = (double *)b;
+  }
   TCK(alloc_field(c, 1, ny + 4, nz + 2, &c->mu));
   {
     void *b = nullptr;
@@ -374,7 +383,7 @@ int tpls_sync(tpls_ctx *c) {
 long tpls_kernel_launches(const tpls_ctx *c) { return c ? c->launches : -1; }
 
 // One velocity component's Crank-Nicolson solve (main_ns_hybrid.F90:756-887).
-static int momentum(tpls_ctx *c, int comp, const double *rhs, int max_iteration) {
+static int momentum(tpls_ctx *c, int comp, const double *coef, int max_iteration) {
   const Geo &g = c->g;
   const int nzp = nz_planes(comp == 2 ? 2 : 1, c->nz);
   const int fuse = (g.ny % 2 == 0);
@@ -385,17 +394,17 @@ static int momentum(tpls_ctx *c, int comp, const double *rhs, int max_iteration)
     double *src = X[(it - 1) % 2], *dst = X[it % 2];
     {
       PhaseScope ps(c, TPLS_T_JACOBI);
-      LCK(c, launch_jacobi(comp, g, c->ph, src, rhs, c->mu, c->pres, dst, 1, fuse, c->st));
+      LCK(c, launch_jacobi_c(comp, g, c->ph, src, coef, c->pres, dst, fuse, c->st));
     }
     if (!fuse) LCK(c, launch_exchange(g, dst, nzp, c->st));
     {
       PhaseScope ps(c, TPLS_T_SOR);
-      LCK(c, launch_sor(comp, g, c->ph, dst, rhs, c->mu, c->pres, 0, it, 0, fuse, c->st));
+      LCK(c, launch_sor_c(comp, g, c->ph, dst, coef, c->pres, 0, it, 0, fuse, c->st));
     }
     if (!fuse) LCK(c, launch_exchange(g, dst, nzp, c->st));
     {
       PhaseScope ps(c, TPLS_T_SOR);
-      LCK(c, launch_sor(comp, g, c->ph, dst, rhs, c->mu, c->pres, 1, it, 1, fuse, c->st));
+      LCK(c, launch_sor_c(comp, g, c->ph, dst, coef, c->pres, 1, it, 1, fuse, c->st));
     }
     if (!fuse) LCK(c, launch_exchange(g, dst, nzp, c->st));
   }
@@ -455,17 +464,20 @@ static int step_once(tpls_ctx *c) {
   PhaseScope *rhs_scope = new PhaseScope(c, TPLS_T_MOM_RHS);
   // convective / diffusive terms and AB3 + CN right-hand sides (:728-751)
   LCK(c, launch_mom_rhs(0, g, ph, c->u2, c->v2, c->w2, c->mu, c->fx, c->conv_u[s1], c->conv_u[s0],
-                        c->csf_u[s1], c->csf_u[s0], c->conv_u[s2], c->csf_u[s2], c->rhs_u, nullptr, st));
+                        c->csf_u[s1], c->csf_u[s0], c->conv_u[s2], c->csf_u[s2], nullptr, nullptr, c->coef[0],
+                        st));
   LCK(c, launch_mom_rhs(1, g, ph, c->u2, c->v2, c->w2, c->mu, c->fy, c->conv_v[s1], c->conv_v[s0],
-                        c->csf_v[s1], c->csf_v[s0], c->conv_v[s2], c->csf_v[s2], c->rhs_v, nullptr, st));
+                        c->csf_v[s1], c->csf_v[s0], c->conv_v[s2], c->csf_v[s2], nullptr, nullptr, c->coef[1],
+                        st));
   LCK(c, launch_mom_rhs(2, g, ph, c->u2, c->v2, c->w2, c->mu, c->fz, c->conv_w[s1], c->conv_w[s0],
-                        c->csf_w[s1], c->csf_w[s0], c->conv_w[s2], c->csf_w[s2], c->rhs_w, nullptr, st));
+                        c->csf_w[s1], c->csf_w[s0], c->conv_w[s2], c->csf_w[s2], nullptr, nullptr, c->coef[2],
+                        st));
   delete rhs_scope;
   // momentum sweeps (:756-887)
   int s;
-  if ((s = momentum(c, 0, c->rhs_u, c->prm.mom_u))) return s;
-  if ((s = momentum(c, 1, c->rhs_v, c->prm.mom_v))) return s;
-  if ((s = momentum(c, 2, c->rhs_w, c->prm.mom_w))) return s;
+  if ((s = momentum(c, 0, c->coef[0], c->prm.mom_u))) return s;
+  if ((s = momentum(c, 1, c->coef[1], c->prm.mom_v))) return s;
+  if ((s = momentum(c, 2, c->coef[2], c->prm.mom_w))) return s;
   double *u3 = c->x3[0][c->x3_final[0]], *v3 = c->x3[1][c->x3_final[1]], *w3 = c->x3[2][c->x3_final[2]];
   // pressure source (:892) and solve (:897-913)
   int its = 0, reason = 0;

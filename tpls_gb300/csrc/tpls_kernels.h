@@ -48,7 +48,8 @@ cudaError_t launch_mom_rhs(int comp, const Geo &g, const Phys &ph,
                            const double *fcsf, const double *c1,
                            const double *c0, const double *s1,
                            const double *s0, double *conv2, double *csf2,
-                           double *rhs, double *diff_out, cudaStream_t st);
+                           double *rhs, double *diff_out, double *coef,
+                           cudaStream_t st);
 // Standalone get_conv_all / get_diffusion_all (per-routine entries).
 cudaError_t launch_conv_diff(int comp, int want_conv, const Geo &g,
                              const Phys &ph, const double *u2,
@@ -68,6 +69,17 @@ cudaError_t launch_sor(int comp, const Geo &g, const Phys &ph, double *x,
                        const double *rhs, const double *mu,
                        const double *pres, int flg, int iteration_time,
                        int bc, int fuse_ghosts, cudaStream_t st);
+// Sweeps on the per-point coefficient records written by launch_mom_rhs
+// (coef != null there): same updates and boundary rows as launch_jacobi /
+// launch_sor with bc = 1.
+cudaError_t launch_jacobi_c(int comp, const Geo &g, const Phys &ph,
+                            const double *xo, const double *coef,
+                            const double *pres, double *x, int fuse_ghosts,
+                            cudaStream_t st);
+cudaError_t launch_sor_c(int comp, const Geo &g, const Phys &ph, double *x,
+                         const double *coef, const double *pres, int flg,
+                         int iteration_time, int bc, int fuse_ghosts,
+                         cudaStream_t st);
 cudaError_t launch_bc(int comp, const Geo &g, const Phys &ph, double *x,
                       const double *pres, cudaStream_t st);
 cudaError_t launch_diff2(const Geo &g, const double *a, const double *b,
