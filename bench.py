@@ -131,8 +131,10 @@ def run_gpu(args, ws, rank, local) -> dict | None:
     cells = nx * ny * nz
     g = TplsGpu(nx, ny, nz, params, uin)
     g.set_state(st)
-    g.step(args.warmup)
+    rc = g.step(args.warmup)
     g.sync()
+    if rc != 0:
+        raise SystemExit(f"tpls_step returned {rc} during warm-up")
     ext = torch.cuda.ExternalStream(g.stream_ptr())
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     g.timing_enable(True)
@@ -143,9 +145,11 @@ def run_gpu(args, ws, rank, local) -> dict | None:
         dist.barrier()
     torch.cuda.synchronize()
     ev0.record(ext)
-    g.step(args.steps)
+    rc = g.step(args.steps)
     ev1.record(ext)
     torch.cuda.synchronize()
+    if rc != 0:
+        raise SystemExit(f"tpls_step returned {rc} in the timed region: the run is not a valid measurement")
     if dist:
         dist.barrier()
     clocks = sampler.stop() if sampler else None
@@ -178,7 +182,8 @@ def run_gpu(args, ws, rank, local) -> dict | None:
     for _ in range(ke):
         for k in STATE_FIELDS:
             g.set_field(k, host[k])
-        g.step(1)
+        if g.step(1) != 0:
+            raise SystemExit("tpls_step failed in the end-to-end region")
         for k in STATE_FIELDS:
             g.get_field_into(k, host[k])
     e1.record(ext)
@@ -199,15 +204,12 @@ def run_gpu(args, ws, rank, local) -> dict | None:
     peaks = _peaks()
     hbm = float(peaks.get("hbm_gbs", 6800.0))
     jac_b, sor_b, jac_n, sor_n = _algorithmic_bytes(nx, ny, nz, params.mom_u)
-    jac_ms, jac_l = phases["jacobi"]
-    sor_ms, sor_l = phases["sor"]
-    dominant = "sor" if sor_ms >= jac_ms else "jacobi"
-    if dominant == "sor":
-        per_launch_b = sor_b / sor_n
-        avg_ms = sor_ms / max(sor_l, 1)
-    else:
-        per_launch_b = jac_b / jac_n
-        avg_ms = jac_ms / max(jac_l, 1)
+    # dominant kernel of the step: the odd-iteration red-black half-sweep
+    # (k_sor_odd_c2), timed launch by launch on the library's stream
+    sor_ms, sor_l = phases["sor_odd"]
+    dominant = "sor_odd_c2"
+    per_launch_b = sor_b / sor_n
+    avg_ms = sor_ms / max(sor_l, 1)
     achieved = per_launch_b / (avg_ms / 1e3) / 1e9
     traffic = None
     tf = ROOT / "profiles" / "traffic_per_launch.json"
@@ -240,7 +242,8 @@ def run_gpu(args, ws, rank, local) -> dict | None:
         "e2e": {"value": e2e, "unit": "cell-steps/s", "h2d_bytes_per_step": bi, "d2h_bytes_per_step": bi,
                 "steps": ke, "path": "tpls_set_field x20 -> tpls_step(1) -> tpls_get_field x20 per step"},
         "gpu_launches": launches,
-        "roofline": {"bound": "hbm", "kernel": f"k_{dominant}" if dominant == "jacobi" else "k_sor_even/k_sor_odd",
+        "roofline": {"bound": "hbm", "kernel": f"k_{dominant}", "bytes_per_launch": per_launch_b,
+                     "avg_launch_ms": avg_ms,
                      "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": traffic, "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback",
                      "note": "FP64 kernels on GB300 are FP64-pipe bound (1.01 TFLOP/s measured), not HBM bound"},

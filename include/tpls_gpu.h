@@ -68,6 +68,9 @@ typedef struct tpls_stats {
   int p_reason;     /* KSP-style converged/diverged reason */
   long steps_done;
   double liquid_volume; /* sum over cells of (1-H(phi)) dV after the step */
+  int p_worst;      /* lowest reason of the solves since the previous
+                       tpls_get_stats (0 when none diverged) */
+  int reserved_i[3];
 } tpls_stats;
 
 /* Field identifiers for tpls_set_field / tpls_get_field and the oracle.
@@ -104,14 +107,28 @@ int tpls_gpu_destroy(tpls_ctx *ctx);
 int tpls_set_field(tpls_ctx *ctx, int field, const double *host);
 int tpls_get_field(tpls_ctx *ctx, int field, double *host);
 /* Device-resident fast path: nsteps full timesteps of main_ns_hybrid.F90:
- * 583-918 followed by the history rotation :2480-2509. */
+ * 583-918 followed by the history rotation :2480-2509.  Returns TPLS_OK;
+ * TPLS_KSP_DIVERGED_ITS if any pressure solve hit p_maxits (the remaining
+ * steps still run, as in the reference's loop); TPLS_KSP_DIVERGED_NAN, an
+ * argument or a CUDA error at the failing step, which ends the call. */
 int tpls_step(tpls_ctx *ctx, int nsteps);
+/* The same steps enqueued without waiting: with graphs enabled (the
+ * default) each step is one CUDA-graph launch on the context's stream whose
+ * pressure iterations run under a device-side WHILE node, so no host round
+ * trip happens inside a step.  Returns TPLS_OK or a launch/capture error;
+ * the solves' outcome is read by tpls_get_stats (p_worst) or tpls_step.
+ * With graphs disabled or timing enabled it runs tpls_step. */
+int tpls_step_async(tpls_ctx *ctx, int nsteps);
+/* Graph mode on (1, default) or off (0: every step launched kernel by
+ * kernel, the pressure iterations driven by the host).  Both give
+ * bit-identical results. */
+int tpls_graphs_enable(tpls_ctx *ctx, int on);
 int tpls_get_stats(tpls_ctx *ctx, tpls_stats *out);
 int tpls_sync(tpls_ctx *ctx);
 const char *tpls_status_string(int status);
 /* Number of kernels the library has launched on this context (counted on
  * the host at every launch site). */
-long tpls_kernel_launches(const tpls_ctx *ctx);
+long tpls_kernel_launches(tpls_ctx *ctx);
 
 /* Device timing by phase, with CUDA events recorded on the context's stream
  * around every launch of a phase (kernels of the momentum sweeps are timed
@@ -120,7 +137,8 @@ long tpls_kernel_launches(const tpls_ctx *ctx);
  * entries. */
 enum tpls_timer {
   TPLS_T_ADVECT = 0, TPLS_T_LEVELSET, TPLS_T_CSF, TPLS_T_VISC, TPLS_T_MOM_RHS,
-  TPLS_T_JACOBI, TPLS_T_SOR, TPLS_T_PRESSURE, TPLS_T_PROJECT, TPLS_T_OTHER,
+  TPLS_T_JACOBI, TPLS_T_SOR, TPLS_T_SOR_ODD, TPLS_T_PRESSURE, TPLS_T_PROJECT,
+  TPLS_T_OTHER,
   TPLS_T_COUNT
 };
 int tpls_timing_enable(tpls_ctx *ctx, int on);

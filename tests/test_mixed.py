@@ -1,0 +1,73 @@
+"""FP32-mixed form (TPLS_PREC_FP32_MIXED) against the FP64 GPU form.
+
+The mixed form runs WENO5, redistancing, CSF, the momentum stencils and
+sweeps and the multigrid smoothing in FP32 on rounded copies of the FP64
+state; the state, the AB3 updates, the right-hand sides, the CG recurrences
+and dot products, the coarsest solve, the projection and the volume
+integral stay FP64.  Tolerances (relative max-norm over the field):
+phi and u 1e-5 after one step and after 20 steps; v and w (whose scale is
+the +-1e-3 noise and the interface-driven secondary flow) 1e-4 after one
+step; p 1e-3 after one step: u3 is the FP32 iterate, so its rounding
+(~6e-8 |u|) enters RHS_p = div(u3)/dt and moves p by ~1e-4 of its scale,
+while the projection removes that divergent noise from the velocity;
+liquid volume equal to 1e-8 relative after 20 steps."""
+import numpy as np
+import pytest
+
+from tpls_gb300.api import STATE_FIELDS, TplsGpu
+from tpls_gb300.channel import make_case
+
+from _util import relmax
+
+pytestmark = pytest.mark.gpu
+
+NX, NY, NZ = 64, 32, 48
+ROWS = (slice(None), slice(1, NY + 1), slice(None))
+
+
+def _ctx(precision, **kw):
+    params, uin, st = make_case("A", nx=NX, ny=NY, nz=NZ, precision=precision, **kw)
+    g = TplsGpu(NX, NY, NZ, params, uin)
+    g.set_state(st)
+    return g
+
+
+def test_mixed_one_step_from_fp64_state():
+    ref = _ctx(0, p_rtol=1e-12, p_maxits=400)
+    ref.step(5)
+    s5 = ref.get_state()
+    mix = _ctx(1, p_rtol=1e-12, p_maxits=400)
+    mix.set_state(s5)
+    ref2 = _ctx(0, p_rtol=1e-12, p_maxits=400)
+    ref2.set_state(s5)
+    assert ref2.step(1) == 0 and mix.step(1) == 0
+    e = {k: relmax(mix.get_field(k), ref2.get_field(k), ROWS) for k in ("PHI2", "U2", "V2", "W2", "PRES")}
+    assert e["PHI2"] < 1e-5 and e["U2"] < 1e-5, e
+    assert e["V2"] < 1e-4 and e["W2"] < 1e-4, e
+    assert e["PRES"] < 1e-3, e
+    for g in (ref, ref2, mix):
+        g.close()
+
+
+def test_mixed_twenty_steps_and_volume():
+    ref, mix = _ctx(0), _ctx(1)
+    assert ref.step(20) == 0 and mix.step(20) == 0
+    assert relmax(mix.get_field("PHI2"), ref.get_field("PHI2"), ROWS) < 1e-5
+    assert relmax(mix.get_field("U2"), ref.get_field("U2"), ROWS) < 1e-5
+    vr, vm = ref.stats()["liquid_volume"], mix.stats()["liquid_volume"]
+    assert abs(vm - vr) <= 1e-8 * abs(vr)
+    ref.close()
+    mix.close()
+
+
+def test_mixed_deterministic_and_u3_view():
+    a, b = _ctx(1), _ctx(1)
+    a.step(4)
+    b.step(4)
+    sa, sb = a.get_state(), b.get_state()
+    assert all(np.array_equal(sa[k], sb[k]) for k in STATE_FIELDS)
+    u3 = a.get_field("U3")  # the FP32 iterate widened to FP64
+    assert np.array_equal(u3, u3.astype(np.float32).astype(np.float64))
+    assert np.abs(u3[1:NX, 1:NY + 1, :]).max() > 1.0
+    a.close()
+    b.close()

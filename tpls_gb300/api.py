@@ -32,7 +32,8 @@ TPLS_PREC_FP64 = 0
 TPLS_PREC_FP32_MIXED = 1
 
 # field ids (enum tpls_field)
-TIMERS = ["advect", "levelset", "csf", "visc", "mom_rhs", "jacobi", "sor", "pressure", "project", "other"]
+TIMERS = ["advect", "levelset", "csf", "visc", "mom_rhs", "jacobi", "sor_even", "sor_odd", "pressure", "project",
+          "other"]
 
 F = dict(PHI2=0, U2=1, V2=2, W2=3, PRES=4, PRES_OLD=5, CONV0_U=6, CONV1_U=7, CONV0_V=8,
          CONV1_V=9, CONV0_W=10, CONV1_W=11, CSF_U0=12, CSF_U1=13, CSF_V0=14, CSF_V1=15,
@@ -60,10 +61,10 @@ class TplsStats(C.Structure):
     _fields_ = [("err_phi", C.c_double), ("err_u", C.c_double), ("err_v", C.c_double),
                 ("err_w", C.c_double), ("p_rnorm", C.c_double), ("p_bnorm", C.c_double),
                 ("p_its", C.c_int), ("p_reason", C.c_int), ("steps_done", C.c_long),
-                ("liquid_volume", C.c_double)]
+                ("liquid_volume", C.c_double), ("p_worst", C.c_int), ("reserved_i", C.c_int * 3)]
 
     def as_dict(self) -> dict:
-        return {k: getattr(self, k) for k, _ in self._fields_}
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved_i"}
 
 
 @dataclass
@@ -123,6 +124,8 @@ def load_library(path: Path | None = None) -> C.CDLL:
     lib.tpls_set_field.argtypes = [C.c_void_p, C.c_int, _DP]
     lib.tpls_get_field.argtypes = [C.c_void_p, C.c_int, _DP]
     lib.tpls_step.argtypes = [C.c_void_p, C.c_int]
+    lib.tpls_step_async.argtypes = [C.c_void_p, C.c_int]
+    lib.tpls_graphs_enable.argtypes = [C.c_void_p, C.c_int]
     lib.tpls_get_stats.argtypes = [C.c_void_p, C.POINTER(TplsStats)]
     lib.tpls_sync.argtypes = [C.c_void_p]
     lib.tpls_kernel_launches.argtypes = [C.c_void_p]
@@ -253,6 +256,14 @@ class TplsGpu:
         """nsteps timesteps on device-resident state; returns the status
         (0, or a negative KSP-style reason of the last pressure solve)."""
         return self._check(self.lib.tpls_step(self.ctx, nsteps))
+
+    def step_async(self, nsteps: int = 1) -> None:
+        """Enqueue nsteps graph-launched steps without waiting; the solves'
+        outcome is in stats()["p_worst"]."""
+        self._check(self.lib.tpls_step_async(self.ctx, nsteps))
+
+    def graphs_enable(self, on: bool = True) -> None:
+        self._check(self.lib.tpls_graphs_enable(self.ctx, 1 if on else 0))
 
     def stats(self) -> dict:
         st = TplsStats()

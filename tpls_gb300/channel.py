@@ -2,10 +2,18 @@
 benchmark configurations) built with the reference's own initial-condition
 routine for the base flow.
 
-Channel: Lx = 2*pi, Ly = pi, Lz = 1, uniform spacing dx = Lx/nx, dy = Ly/ny,
-dz = 1/nz; inlet/outlet in x, periodic y, no-slip walls in z (the
-reference's boundary conditions).  Two layers: mu_minus = m below the
-interface (phi < 0), mu_plus = 1 above; viscosity (mu)/Re.
+Channel: cubic cells dx = dy = dz = 1/nz, Lz = 1, Lx = nx dz, Ly = ny dz
+(the grid of twophase_initialisation_wave.F90:66-75); inlet/outlet in x,
+periodic y, no-slip walls in z (the reference's boundary conditions).  Two
+layers: mu_minus = m below the interface (phi < 0), mu_plus = 1 above;
+viscosity (mu)/Re.
+
+Cubic cells are required by the reference's redistancing: levelset.f90
+uses one spacing h = dx for every direction (the Godunov gradient and the
+inlet row z = k h - h/2, levelset.f90:168-177), so on a 2*pi x pi x 1 box
+(dx = 4.7 dz at 256x128x192) it drives phi towards a distance function
+stretched 4.7 times in z; the interface band collapses and the reference's
+algorithm diverges (NaN near step 85 at 256x128x192).
 
 * phi = z - h(x, y) on every p-grid point including ghosts, with cell
   centres x_i = (i-1/2)dx, y_j = (j-1/2)dy, z_k = (k-1/2)dz;
@@ -71,11 +79,15 @@ WORKLOADS = {
                   200, SEED0 + 1),
     "C": Workload("C: 512x256x256 FP32-mixed, m=20, Re=500, 4-mode interface", 512, 256, 256, 20.0, 500.0, 10.0,
                   0.08, 4, 500, SEED0 + 2),
+    # profiling case: the physics of B on a grid whose sweep working set
+    # (~200 MB of coefficient records) exceeds the 129 MB L2 while the whole
+    # channel stays near 1.5 GB on the device
+    "M": Workload("M: 192x96x144 FP64 profiling case, m=2, Re=200, 4-mode interface", 192, 96, 144, 2.0, 200.0,
+                  1.0, 0.05, 4, 200, SEED0 + 5),
 }
 
 
-def interface_height(w: Workload, x: np.ndarray, y: np.ndarray) -> np.ndarray:
-    Lx, Ly = 2.0 * np.pi, np.pi
+def interface_height(w: Workload, x: np.ndarray, y: np.ndarray, Lx: float, Ly: float) -> np.ndarray:
     if w.modes == 0:
         return 0.5 + w.amp_max * np.sin(2.0 * np.pi * x / Lx) * np.cos(2.0 * np.pi * y / Ly)
     rng = np.random.default_rng(w.seed)
@@ -101,8 +113,9 @@ def make_case(w: Workload | str, *, nx: int | None = None, ny: int | None = None
     nx = nx or w.nx
     ny = ny or w.ny
     nz = nz or w.nz
-    Lx, Ly = 2.0 * np.pi, np.pi
-    dx, dy, dz = Lx / nx, Ly / ny, 1.0 / nz
+    dz = 1.0 / nz
+    dx = dy = dz
+    Lx, Ly = nx * dx, ny * dy
     sw = 1.5 * dx
     mu_minus, mu_plus = w.m, 1.0
     uz = base_profile(nz, dz, w.re, -1.0, mu_minus, mu_plus, 0.5, sw)
@@ -114,7 +127,7 @@ def make_case(w: Workload | str, *, nx: int | None = None, ny: int | None = None
     xi = (np.arange(nx + 2) - 0.5) * dx
     yj = (np.arange(ny + 2) - 0.5) * dy
     zk = (np.arange(nz + 2) - 0.5) * dz
-    h = interface_height(w, xi[:, None], yj[None, :])
+    h = interface_height(w, xi[:, None], yj[None, :], Lx, Ly)
     phi = np.asfortranarray(zk[None, None, :] - h[:, :, None])
     u = np.asfortranarray(np.broadcast_to(uz[None, None, :], (nx + 2, ny + 2, nz)).copy())
     v = np.zeros((nx + 2, ny + 2, nz), order="F")

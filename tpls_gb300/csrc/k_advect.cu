@@ -16,85 +16,89 @@ namespace tpls {
 // weno.f90:175-215 (Jiang-Shu WENO5).  The three nonlinear weights
 // a_i/(a1+a2+a3) with a_i = c_i/q_i are formed with one division:
 // w_i = c_i*prod_{j!=i} q_j / sum_m c_m*prod_{j!=m} q_j.
-__device__ __forceinline__ double weno5(double v1, double v2, double v3,
-                                        double v4, double v5) {
-  const double eps = TPLS_WENO_EPS;
-  double t1 = v1 - 2.0 * v2 + v3, t2 = v1 - 4.0 * v2 + 3.0 * v3;
-  double q1 = eps + ((13.0 / 12.0) * t1 * t1 + 0.25 * t2 * t2);
-  t1 = v2 - 2.0 * v3 + v4;
+template <typename T>
+__device__ __forceinline__ T weno5(T v1, T v2, T v3, T v4, T v5) {
+  const T eps = (T)TPLS_WENO_EPS, two = (T)2, three = (T)3, four = (T)4;
+  const T c13 = (T)(13.0 / 12.0), c14 = (T)0.25;
+  T t1 = v1 - two * v2 + v3, t2 = v1 - four * v2 + three * v3;
+  T q1 = eps + (c13 * t1 * t1 + c14 * t2 * t2);
+  t1 = v2 - two * v3 + v4;
   t2 = v2 - v4;
-  double q2 = eps + ((13.0 / 12.0) * t1 * t1 + 0.25 * t2 * t2);
-  t1 = v3 - 2.0 * v4 + v5;
-  t2 = 3.0 * v3 - 4.0 * v4 + v5;
-  double q3 = eps + ((13.0 / 12.0) * t1 * t1 + 0.25 * t2 * t2);
+  T q2 = eps + (c13 * t1 * t1 + c14 * t2 * t2);
+  t1 = v3 - two * v4 + v5;
+  t2 = three * v3 - four * v4 + v5;
+  T q3 = eps + (c13 * t1 * t1 + c14 * t2 * t2);
   q1 *= q1;
   q2 *= q2;
   q3 *= q3;
-  const double n1 = 0.1 * (q2 * q3), n2 = 0.6 * (q1 * q3), n3 = 0.3 * (q1 * q2);
-  const double p1 = v1 * (1.0 / 3.0) - v2 * (7.0 / 6.0) + v3 * (11.0 / 6.0);
-  const double p2 = -v2 * (1.0 / 6.0) + v3 * (5.0 / 6.0) + v4 * (1.0 / 3.0);
-  const double p3 = v3 * (1.0 / 3.0) + v4 * (5.0 / 6.0) - v5 * (1.0 / 6.0);
+  const T n1 = (T)0.1 * (q2 * q3), n2 = (T)0.6 * (q1 * q3), n3 = (T)0.3 * (q1 * q2);
+  const T p1 = v1 * (T)(1.0 / 3.0) - v2 * (T)(7.0 / 6.0) + v3 * (T)(11.0 / 6.0);
+  const T p2 = -v2 * (T)(1.0 / 6.0) + v3 * (T)(5.0 / 6.0) + v4 * (T)(1.0 / 3.0);
+  const T p3 = v3 * (T)(1.0 / 3.0) + v4 * (T)(5.0 / 6.0) - v5 * (T)(1.0 / 6.0);
   return (n1 * p1 + n2 * p2 + n3 * p3) / (n1 + n2 + n3);
 }
 
 // dfx at u-index (iu, jp-1, kp-1): phi along x at p-row jp, level kp.
 // WENO for 3 <= iu <= nx-2, first-order upwind otherwise (weno.f90:45-100).
-__device__ __forceinline__ double xface(const Geo &g, const double *__restrict__ phi,
-                                        const double *__restrict__ u, int iu, int jp,
+template <typename T>
+__device__ __forceinline__ T xface(const Geo &g, const T *__restrict__ phi,
+                                        const T *__restrict__ u, int iu, int jp,
                                         int kp) {
   const int ju = (jp - 1 == 0) ? g.ny : jp - 1;
-  const double vel = u[TPLS_IDX(g, iu, ju, kp - 1)];
-  const double *row = phi + TPLS_IDX(g, 0, jp, kp);
+  const T vel = u[TPLS_IDX(g, iu, ju, kp - 1)];
+  const T *row = phi + TPLS_IDX(g, 0, jp, kp);
   if (iu >= 3 && iu <= g.nx - 2) {
-    if (vel >= 0.0) return weno5(row[iu - 2], row[iu - 1], row[iu], row[iu + 1], row[iu + 2]);
+    if (vel >= (T)0) return weno5(row[iu - 2], row[iu - 1], row[iu], row[iu + 1], row[iu + 2]);
     return weno5(row[iu + 3], row[iu + 2], row[iu + 1], row[iu], row[iu - 1]);
   }
-  return (vel >= 0.0) ? row[iu] : row[iu + 1];
+  return (vel >= (T)0) ? row[iu] : row[iu + 1];
 }
 
 // dfy at v-index (ip, jv, kp-1): phi along y at x=ip, level kp, periodic
 // rows (weno.f90:105-132; row 0 is the exchanged copy of row ny).
-__device__ __forceinline__ double yface(const Geo &g, const double *__restrict__ phi,
-                                        const double *__restrict__ v, int ip, int jv,
+template <typename T>
+__device__ __forceinline__ T yface(const Geo &g, const T *__restrict__ phi,
+                                        const T *__restrict__ v, int ip, int jv,
                                         int kp) {
   const int ny = g.ny;
   if (jv == 0) jv = ny;
-  const double vel = v[TPLS_IDX(g, ip, jv, kp - 1)];
-  const double *col = phi + TPLS_IDX(g, ip, 0, kp);
+  const T vel = v[TPLS_IDX(g, ip, jv, kp - 1)];
+  const T *col = phi + TPLS_IDX(g, ip, 0, kp);
   const int sy = g.sy;
 #define PY(jj) col[sy * wrapy((jj), ny)]
-  if (vel >= 0.0) return weno5(PY(jv - 2), PY(jv - 1), PY(jv), PY(jv + 1), PY(jv + 2));
+  if (vel >= (T)0) return weno5(PY(jv - 2), PY(jv - 1), PY(jv), PY(jv + 1), PY(jv + 2));
   return weno5(PY(jv + 3), PY(jv + 2), PY(jv + 1), PY(jv), PY(jv - 1));
 #undef PY
 }
 
 // dfz at w-index (ip, jp-1, kw): phi along z at x=ip, row jp.  WENO for
 // 3 <= kw <= nz-2, arithmetic mean otherwise (weno.f90:136-166).
-__device__ __forceinline__ double zface(const Geo &g, const double *__restrict__ phi,
-                                        const double *__restrict__ w, int ip, int jp,
+template <typename T>
+__device__ __forceinline__ T zface(const Geo &g, const T *__restrict__ phi,
+                                        const T *__restrict__ w, int ip, int jp,
                                         int kw) {
   const int ju = (jp - 1 == 0) ? g.ny : jp - 1;
-  const double *col = phi + TPLS_IDX(g, ip, jp, 0);
+  const T *col = phi + TPLS_IDX(g, ip, jp, 0);
   const int sz = g.sz;
   if (kw >= 3 && kw <= g.nz - 2) {
-    const double vel = w[TPLS_IDX(g, ip, ju, kw)];
-    if (vel >= 0.0)
+    const T vel = w[TPLS_IDX(g, ip, ju, kw)];
+    if (vel >= (T)0)
       return weno5(col[sz * (kw - 2)], col[sz * (kw - 1)], col[sz * kw], col[sz * (kw + 1)],
                    col[sz * (kw + 2)]);
     return weno5(col[sz * (kw + 3)], col[sz * (kw + 2)], col[sz * (kw + 1)], col[sz * kw],
                  col[sz * (kw - 1)]);
   }
-  return (col[sz * kw] + col[sz * (kw + 1)]) / 2.0;
+  return (col[sz * kw] + col[sz * (kw + 1)]) / (T)2;
 }
 
 constexpr int ADV_BX = 32, ADV_BY = 8;
 constexpr int ADV_KC = 16;  // z levels per thread (column chunk)
 
+template <typename T>
 __global__ void __launch_bounds__(ADV_BX *ADV_BY)
-    k_advect(Geo g, double rdx, double rdy, double rdz, const double *__restrict__ phi,
-             const double *__restrict__ u, const double *__restrict__ v,
-             const double *__restrict__ w, double *__restrict__ conv) {
-  __shared__ double yf_s[ADV_BY][ADV_BX];
+    k_advect(Geo g, T rdx, T rdy, T rdz, const T *__restrict__ phi, const T *__restrict__ u,
+             const T *__restrict__ v, const T *__restrict__ w, double *__restrict__ conv) {
+  __shared__ T yf_s[ADV_BY][ADV_BX];
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int i = blockIdx.x * ADV_BX + tx + 1;
   const int j = blockIdx.y * ADV_BY + ty + 1;
@@ -102,24 +106,24 @@ __global__ void __launch_bounds__(ADV_BX *ADV_BY)
   const bool act = (i <= g.nx) && (j <= g.ny);
   const int ic = act ? i : 1, jc = act ? j : 1;  // clamped for inactive lanes
   const int jm = (jc == 1) ? g.ny : jc - 1;      // u/v/w row index j-1 (wrapped)
-  double zlo = zface(g, phi, w, ic, jc, k0 - 1);
+  T zlo = zface(g, phi, w, ic, jc, k0 - 1);
   for (int k = k0; k <= k1; k++) {
-    const double xo = xface(g, phi, u, ic, jc, k);
-    double xl = __shfl_up_sync(0xffffffffu, xo, 1);
+    const T xo = xface(g, phi, u, ic, jc, k);
+    T xl = __shfl_up_sync(0xffffffffu, xo, 1);
     if (tx == 0) xl = xface(g, phi, u, ic - 1, jc, k);
-    const double yo = yface(g, phi, v, ic, jc, k);
+    const T yo = yface(g, phi, v, ic, jc, k);
     yf_s[ty][tx] = yo;
     __syncthreads();
-    const double yl = (ty > 0) ? yf_s[ty - 1][tx] : yface(g, phi, v, ic, jc - 1, k);
-    const double zo = zface(g, phi, w, ic, jc, k);
+    const T yl = (ty > 0) ? yf_s[ty - 1][tx] : yface(g, phi, v, ic, jc - 1, k);
+    const T zo = zface(g, phi, w, ic, jc, k);
     if (act) {
-      const double fxp = u[TPLS_IDX(g, i, jm, k - 1)] * xo;
-      const double fxm = u[TPLS_IDX(g, i - 1, jm, k - 1)] * xl;
-      const double fyp = v[TPLS_IDX(g, i, j, k - 1)] * yo;
-      const double fym = v[TPLS_IDX(g, i, jm, k - 1)] * yl;
-      const double fzp = w[TPLS_IDX(g, i, jm, k)] * zo;
-      const double fzm = w[TPLS_IDX(g, i, jm, k - 1)] * zlo;
-      conv[TPLS_IDX(g, i, j, k)] = (fxp - fxm) * rdx + (fyp - fym) * rdy + (fzp - fzm) * rdz;
+      const T fxp = u[TPLS_IDX(g, i, jm, k - 1)] * xo;
+      const T fxm = u[TPLS_IDX(g, i - 1, jm, k - 1)] * xl;
+      const T fyp = v[TPLS_IDX(g, i, j, k - 1)] * yo;
+      const T fym = v[TPLS_IDX(g, i, jm, k - 1)] * yl;
+      const T fzp = w[TPLS_IDX(g, i, jm, k)] * zo;
+      const T fzm = w[TPLS_IDX(g, i, jm, k - 1)] * zlo;
+      conv[TPLS_IDX(g, i, j, k)] = (double)((fxp - fxm) * rdx + (fyp - fym) * rdy + (fzp - fzm) * rdz);
     }
     zlo = zo;
     __syncthreads();
@@ -132,13 +136,42 @@ cudaError_t launch_advect(const Geo &g, const Phys &ph, const double *phi2,
                           cudaStream_t st) {
   dim3 blk(ADV_BX, ADV_BY),
       grd((g.nx + ADV_BX - 1) / ADV_BX, (g.ny + ADV_BY - 1) / ADV_BY, (g.nz + ADV_KC - 1) / ADV_KC);
-  k_advect<<<grd, blk, 0, st>>>(g, 1.0 / ph.dx, 1.0 / ph.dy, 1.0 / ph.dz, phi2, u2, v2, w2,
-                                conv2_phi);
+  k_advect<double><<<grd, blk, 0, st>>>(g, 1.0 / ph.dx, 1.0 / ph.dy, 1.0 / ph.dz, phi2, u2, v2, w2,
+                                        conv2_phi);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_advect(const Geo &g, const Phys &ph, const float *phi2, const float *u2, const float *v2,
+                          const float *w2, double *conv2_phi, cudaStream_t st) {
+  dim3 blk(ADV_BX, ADV_BY),
+      grd((g.nx + ADV_BX - 1) / ADV_BX, (g.ny + ADV_BY - 1) / ADV_BY, (g.nz + ADV_KC - 1) / ADV_KC);
+  k_advect<float><<<grd, blk, 0, st>>>(g, (float)(1.0 / ph.dx), (float)(1.0 / ph.dy), (float)(1.0 / ph.dz), phi2,
+                                       u2, v2, w2, conv2_phi);
+  return cudaGetLastError();
+}
+
+// elementwise FP64 -> FP32 copy over n elements (the FP32 shadows of the
+// FP64 state used by the FP32-mixed form)
+__global__ void k_to_float(const double *__restrict__ a, float *__restrict__ b, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+__global__ void k_to_double(const float *__restrict__ a, double *__restrict__ b, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    b[i] = (double)a[i];
+}
+cudaError_t launch_to_float(const double *a, float *b, size_t n, cudaStream_t st) {
+  k_to_float<<<1216, 256, 0, st>>>(a, b, n);
+  return cudaGetLastError();
+}
+cudaError_t launch_to_double(const float *a, double *b, size_t n, cudaStream_t st) {
+  k_to_double<<<1216, 256, 0, st>>>(a, b, n);
   return cudaGetLastError();
 }
 
 // exchange2d on one GPU: rows 0 <- ny, ny+1 <- 1 over x = 0..nx+1.
-__global__ void k_exchange(Geo g, double *a, int nzp) {
+template <typename T>
+__global__ void k_exchange(Geo g, T *a, int nzp) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int k = blockIdx.y;
   if (i > g.nx + 1 || k >= nzp) return;
@@ -148,7 +181,12 @@ __global__ void k_exchange(Geo g, double *a, int nzp) {
 
 cudaError_t launch_exchange(const Geo &g, double *a, int nzp, cudaStream_t st) {
   dim3 blk(128), grd((g.nx + 2 + 127) / 128, nzp);
-  k_exchange<<<grd, blk, 0, st>>>(g, a, nzp);
+  k_exchange<double><<<grd, blk, 0, st>>>(g, a, nzp);
+  return cudaGetLastError();
+}
+cudaError_t launch_exchange(const Geo &g, float *a, int nzp, cudaStream_t st) {
+  dim3 blk(128), grd((g.nx + 2 + 127) / 128, nzp);
+  k_exchange<float><<<grd, blk, 0, st>>>(g, a, nzp);
   return cudaGetLastError();
 }
 

@@ -61,28 +61,29 @@ cudaError_t launch_ls_ab3(const Geo &g, const Phys &ph, const double *phi2,
 // levelset.f90:17-94 get_levelset_status with h = dx.  flags packs the
 // indicator istatus (bit 0) and sign(phi)+1 (bits 1-2); D and flags are 0
 // outside the interior.
-__global__ void k_ls_status(Geo g, double h, const double *__restrict__ phi,
-                            double *__restrict__ D, signed char *__restrict__ flags) {
+template <typename T>
+__global__ void k_ls_status(Geo g, T h, const double *__restrict__ phi, T *__restrict__ D,
+                            signed char *__restrict__ flags) {
   const int i = blockIdx.x * LS_BX + threadIdx.x, j = blockIdx.y * LS_BY + threadIdx.y;
   const int k = blockIdx.z;
   if (i > g.nx + 1 || j > g.ny + 1) return;
   const int c = TPLS_IDX(g, i, j, k);
   if (i < 1 || i > g.nx || j < 1 || j > g.ny || k < 1 || k > g.nz) {
-    D[c] = 0.0;
+    D[c] = (T)0;
     flags[c] = 0;
     return;
   }
-  const double p = phi[c];
-  const double pxp = phi[c + 1], pxm = phi[c - 1], pyp = phi[c + g.sy], pym = phi[c - g.sy];
-  const double pzp = phi[c + g.sz], pzm = phi[c - g.sz];
-  const int sgn = (p < 0.0) ? -1 : ((p > 0.0) ? 1 : 0);
-  const double mn = fmin(fmin(fmin(p * pxp, p * pxm), fmin(p * pyp, p * pym)), fmin(p * pzp, p * pzm));
-  const int st = (mn <= 0.0) ? 1 : 0;
-  double d = 0.0;
+  const T p = (T)phi[c];
+  const T pxp = (T)phi[c + 1], pxm = (T)phi[c - 1], pyp = (T)phi[c + g.sy], pym = (T)phi[c - g.sy];
+  const T pzp = (T)phi[c + g.sz], pzm = (T)phi[c - g.sz];
+  const int sgn = (p < (T)0) ? -1 : ((p > (T)0) ? 1 : 0);
+  const T mn = fmin(fmin(fmin(p * pxp, p * pxm), fmin(p * pyp, p * pym)), fmin(p * pzp, p * pzm));
+  const int st = (mn <= (T)0) ? 1 : 0;
+  T d = (T)0;
   if (st) {
-    const double gx = pxp - pxm, gy = pyp - pym, gz = pzp - pzm;
-    const double b1 = sqrt(gx * gx + gy * gy + gz * gz) * 0.5;
-    double mx = fmax(fmax(fabs(pxp - p), fabs(pxm - p)), fmax(fabs(pyp - p), fabs(pym - p)));
+    const T gx = pxp - pxm, gy = pyp - pym, gz = pzp - pzm;
+    const T b1 = sqrt(gx * gx + gy * gy + gz * gz) * (T)0.5;
+    T mx = fmax(fmax(fabs(pxp - p), fabs(pxm - p)), fmax(fabs(pyp - p), fabs(pym - p)));
     mx = fmax(fmax(mx, fmax(fabs(pzp - p), fabs(pzm - p))), fmax(b1, h));
     d = h * p / mx;
   }
@@ -92,7 +93,12 @@ __global__ void k_ls_status(Geo g, double h, const double *__restrict__ phi,
 
 cudaError_t launch_ls_status(const Geo &g, const Phys &ph, const double *phi3,
                              double *D, signed char *flags, cudaStream_t st) {
-  k_ls_status<<<full_grid(g, g.nz + 2), dim3(LS_BX, LS_BY), 0, st>>>(g, ph.dx, phi3, D, flags);
+  k_ls_status<double><<<full_grid(g, g.nz + 2), dim3(LS_BX, LS_BY), 0, st>>>(g, ph.dx, phi3, D, flags);
+  return cudaGetLastError();
+}
+cudaError_t launch_ls_status(const Geo &g, const Phys &ph, const double *phi3, float *D, signed char *flags,
+                             cudaStream_t st) {
+  k_ls_status<float><<<full_grid(g, g.nz + 2), dim3(LS_BX, LS_BY), 0, st>>>(g, (float)ph.dx, phi3, D, flags);
   return cudaGetLastError();
 }
 
@@ -102,70 +108,77 @@ cudaError_t launch_ls_status(const Geo &g, const Phys &ph, const double *phi3,
 // copy, linear z extrapolation, periodic y.  err_part (optional) receives
 // one partial of sum((pr - pr_new)^2) per block over i 1..nx, j 1..ny,
 // k 0..nz+1.
-__device__ __forceinline__ double rs_update(const Geo &g, double h, double ktau,
-                                            const double *__restrict__ pr,
-                                            const double *__restrict__ D,
-                                            const signed char *__restrict__ flags, int i, int j,
-                                            int k) {
+template <typename TC, typename TI>
+__device__ __forceinline__ TC rs_update(const Geo &g, TC h, TC ktau, const TI *__restrict__ pr0,
+                                        const TC *__restrict__ D, const signed char *__restrict__ flags,
+                                        int i, int j, int k) {
   const int c = TPLS_IDX(g, i, j, k);
   const int f = flags[c];
-  const double p = pr[c];
-  const double sg = (double)(((f >> 1) & 3) - 1);
-  double dc;
+  struct Ld {
+    const TI *p;
+    __device__ TC operator[](int q) const { return (TC)p[q]; }
+  } pr{pr0};
+  const TC p = pr[c];
+  const TC sg = (TC)(((f >> 1) & 3) - 1);
+  const TC zero = (TC)0;
+  TC dc;
   if (f & 1) {
     dc = sg * fabs(p) - D[c];
-  } else if (sg > 0.0) {
+  } else if (sg > zero) {
     // max(aP^2, bM^2) with aP = max(p - p[i-1], 0), bM = min(p[i+1] - p, 0)
     // equals max(p - min(p[i-1], p[i+1]), 0)^2 bit for bit (rounding of a
     // difference and of a square are monotone), likewise in y and z.
-    const double ax = fmax(p - fmin(pr[c - 1], pr[c + 1]), 0.0);
-    const double ay = fmax(p - fmin(pr[c - g.sy], pr[c + g.sy]), 0.0);
-    const double az = fmax(p - fmin(pr[c - g.sz], pr[c + g.sz]), 0.0);
+    const TC ax = fmax(p - fmin(pr[c - 1], pr[c + 1]), zero);
+    const TC ay = fmax(p - fmin(pr[c - g.sy], pr[c + g.sy]), zero);
+    const TC az = fmax(p - fmin(pr[c - g.sz], pr[c + g.sz]), zero);
     dc = sg * (sqrt(ax * ax + ay * ay + az * az) - h);
-  } else if (sg < 0.0) {
+  } else if (sg < zero) {
     // max(bP^2, aM^2) = max(max(p[i-1], p[i+1]) - p, 0)^2, likewise y, z
-    const double ax = fmax(fmax(pr[c - 1], pr[c + 1]) - p, 0.0);
-    const double ay = fmax(fmax(pr[c - g.sy], pr[c + g.sy]) - p, 0.0);
-    const double az = fmax(fmax(pr[c - g.sz], pr[c + g.sz]) - p, 0.0);
+    const TC ax = fmax(fmax(pr[c - 1], pr[c + 1]) - p, zero);
+    const TC ay = fmax(fmax(pr[c - g.sy], pr[c + g.sy]) - p, zero);
+    const TC az = fmax(fmax(pr[c - g.sz], pr[c + g.sz]) - p, zero);
     // levelset.f90:274-275 sums x, then z, then y
     dc = sg * (sqrt(ax * ax + az * az + ay * ay) - h);
   } else {
-    dc = 0.0;
+    dc = zero;
   }
   return p - ktau * dc;
 }
 
-__device__ __forceinline__ double rs_val(const Geo &g, const Phys &ph, double h, double ktau,
-                                         const double *pr, const double *D,
-                                         const signed char *flags, int i, int j, int k) {
-  if (i == 0) return (k * h - 0.5 * h) - ph.height;
-  return rs_update(g, h, ktau, pr, D, flags, (i == g.nx + 1) ? g.nx : i, j, k);
+template <typename TC, typename TI>
+__device__ __forceinline__ TC rs_val(const Geo &g, const Phys &ph, TC h, TC ktau, const TI *pr, const TC *D,
+                                     const signed char *flags, int i, int j, int k) {
+  if (i == 0) return (TC)((k * (double)h - 0.5 * (double)h) - ph.height);
+  return rs_update<TC, TI>(g, h, ktau, pr, D, flags, (i == g.nx + 1) ? g.nx : i, j, k);
 }
 
+// TI/TO: storage of the input/output iterate; TC: arithmetic (double for
+// the FP64 form; float for the FP32-mixed form, whose first iteration reads
+// the FP64 phi3 and whose last writes the FP64 state).
+template <typename TC, typename TI, typename TO>
 __global__ void __launch_bounds__(LS_BX *LS_BY)
-    k_ls_iter(Geo g, Phys ph, double h, double ktau, const double *__restrict__ pr,
-              const double *__restrict__ D, const signed char *__restrict__ flags,
-              double *__restrict__ out, double *__restrict__ err_part) {
+    k_ls_iter(Geo g, Phys ph, TC h, TC ktau, const TI *__restrict__ pr, const TC *__restrict__ D,
+              const signed char *__restrict__ flags, TO *__restrict__ out, double *__restrict__ err_part) {
   const int i = blockIdx.x * LS_BX + threadIdx.x, j = blockIdx.y * LS_BY + threadIdx.y;
   const int k = blockIdx.z;
   double e = 0.0;
   if (i <= g.nx + 1 && j <= g.ny + 1) {
     const int jj = wrapy(j, g.ny);
-    double v;
+    TC v;
     if (k == 0)
-      v = 2.0 * rs_val(g, ph, h, ktau, pr, D, flags, i, jj, 1) -
-          rs_val(g, ph, h, ktau, pr, D, flags, i, jj, 2);
+      v = (TC)2 * rs_val<TC, TI>(g, ph, h, ktau, pr, D, flags, i, jj, 1) -
+          rs_val<TC, TI>(g, ph, h, ktau, pr, D, flags, i, jj, 2);
     else if (k == g.nz + 1)
-      v = 2.0 * rs_val(g, ph, h, ktau, pr, D, flags, i, jj, g.nz) -
-          rs_val(g, ph, h, ktau, pr, D, flags, i, jj, g.nz - 1);
+      v = (TC)2 * rs_val<TC, TI>(g, ph, h, ktau, pr, D, flags, i, jj, g.nz) -
+          rs_val<TC, TI>(g, ph, h, ktau, pr, D, flags, i, jj, g.nz - 1);
     else
-      v = rs_val(g, ph, h, ktau, pr, D, flags, i, jj, k);
+      v = rs_val<TC, TI>(g, ph, h, ktau, pr, D, flags, i, jj, k);
     const int c = TPLS_IDX(g, i, j, k);
     if (err_part && i >= 1 && i <= g.nx && j >= 1 && j <= g.ny) {
-      const double d = pr[c] - v;
+      const double d = (double)pr[c] - (double)v;
       e = d * d;
     }
-    out[c] = v;
+    out[c] = (TO)v;
   }
   if (err_part) {
     __shared__ double s[LS_BX * LS_BY / 32];
@@ -186,13 +199,25 @@ int ls_iter_blocks(const Geo &g) {
   return (int)(gr.x * gr.y * gr.z);
 }
 
-cudaError_t launch_ls_iter(const Geo &g, const Phys &ph, const double *pr,
-                           const double *D, const signed char *flags,
-                           double *pr_new, double *err_part, cudaStream_t st) {
+template <typename TC, typename TI, typename TO>
+static cudaError_t ls_iter(const Geo &g, const Phys &ph, const TI *pr, const TC *D, const signed char *flags,
+                           TO *pr_new, double *err_part, cudaStream_t st) {
   const double h = ph.dx, dtau = 0.3 * h;
-  k_ls_iter<<<full_grid(g, g.nz + 2), dim3(LS_BX, LS_BY), 0, st>>>(g, ph, h, dtau / h, pr, D, flags,
-                                                                   pr_new, err_part);
+  k_ls_iter<TC, TI, TO><<<full_grid(g, g.nz + 2), dim3(LS_BX, LS_BY), 0, st>>>(g, ph, (TC)h, (TC)(dtau / h), pr,
+                                                                              D, flags, pr_new, err_part);
   return cudaGetLastError();
+}
+cudaError_t launch_ls_iter(const Geo &g, const Phys &ph, const double *pr, const double *D,
+                           const signed char *flags, double *pr_new, double *err_part, cudaStream_t st) {
+  return ls_iter<double, double, double>(g, ph, pr, D, flags, pr_new, err_part, st);
+}
+cudaError_t launch_ls_iter32(const Geo &g, const Phys &ph, const double *pr64, const float *pr32,
+                             const float *D, const signed char *flags, double *out64, float *out32,
+                             double *err_part, cudaStream_t st) {
+  if (pr64 && out64) return ls_iter<float, double, double>(g, ph, pr64, D, flags, out64, err_part, st);
+  if (pr64) return ls_iter<float, double, float>(g, ph, pr64, D, flags, out32, err_part, st);
+  if (out64) return ls_iter<float, float, double>(g, ph, pr32, D, flags, out64, err_part, st);
+  return ls_iter<float, float, float>(g, ph, pr32, D, flags, out32, err_part, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -204,43 +229,48 @@ struct F3 {
   double x, y, z;
 };
 
+template <typename T>
 __device__ __forceinline__ F3 csf_point(const Geo &g, const Phys &ph, double max_kappa,
-                                        const double *__restrict__ fi, int i, int j, int k) {
+                                        const double *__restrict__ fi0, int i, int j, int k) {
   const int c = TPLS_IDX(g, i, j, k);
-  const double p = fi[c];
+  struct Ld {
+    const double *p;
+    __device__ T operator[](int q) const { return (T)p[q]; }
+  } fi{fi0};
+  const T p = fi[c];
   F3 r = {0.0, 0.0, 0.0};
-  if (p < -ph.sw || p > ph.sw) return r;
+  if ((double)p < -ph.sw || (double)p > ph.sw) return r;
   const int sy = g.sy, sz = g.sz;
-  const double rdx = 1.0 / ph.dx, rdy = 1.0 / ph.dy, rdz = 1.0 / ph.dz;
-  const double r2dx = 0.5 * rdx, r2dy = 0.5 * rdy, r2dz = 0.5 * rdz;
-  const double d2x = (fi[c + 1] - 2.0 * p + fi[c - 1]) * (rdx * rdx);
-  const double d2y = (fi[c + sy] - 2.0 * p + fi[c - sy]) * (rdy * rdy);
-  const double d2z = (fi[c + sz] - 2.0 * p + fi[c - sz]) * (rdz * rdz);
-  const double gx = (fi[c + 1] - fi[c - 1]) * r2dx;
-  const double gy = (fi[c + sy] - fi[c - sy]) * r2dy;
-  const double gz = (fi[c + sz] - fi[c - sz]) * r2dz;
-  const double d2xz = ((fi[c + 1 + sz] - fi[c - 1 + sz]) - (fi[c + 1 - sz] - fi[c - 1 - sz])) * (r2dx * r2dz);
-  const double d2yz = ((fi[c + sy + sz] - fi[c - sy + sz]) - (fi[c + sy - sz] - fi[c - sy - sz])) * (r2dy * r2dz);
-  const double d2xy = ((fi[c + 1 + sy] - fi[c - 1 + sy]) - (fi[c + 1 - sy] - fi[c - 1 - sy])) * (r2dx * r2dy);
-  const double nrm = gx * gx + gy * gy + gz * gz;
-  double kap;
-  if (nrm < 1e-10) {
-    kap = 0.0;
+  const T rdx = (T)(1.0 / ph.dx), rdy = (T)(1.0 / ph.dy), rdz = (T)(1.0 / ph.dz);
+  const T r2dx = (T)0.5 * rdx, r2dy = (T)0.5 * rdy, r2dz = (T)0.5 * rdz, two = (T)2;
+  const T d2x = (fi[c + 1] - two * p + fi[c - 1]) * (rdx * rdx);
+  const T d2y = (fi[c + sy] - two * p + fi[c - sy]) * (rdy * rdy);
+  const T d2z = (fi[c + sz] - two * p + fi[c - sz]) * (rdz * rdz);
+  const T gx = (fi[c + 1] - fi[c - 1]) * r2dx;
+  const T gy = (fi[c + sy] - fi[c - sy]) * r2dy;
+  const T gz = (fi[c + sz] - fi[c - sz]) * r2dz;
+  const T d2xz = ((fi[c + 1 + sz] - fi[c - 1 + sz]) - (fi[c + 1 - sz] - fi[c - 1 - sz])) * (r2dx * r2dz);
+  const T d2yz = ((fi[c + sy + sz] - fi[c - sy + sz]) - (fi[c + sy - sz] - fi[c - sy - sz])) * (r2dy * r2dz);
+  const T d2xy = ((fi[c + 1 + sy] - fi[c - 1 + sy]) - (fi[c + 1 - sy] - fi[c - 1 - sy])) * (r2dx * r2dy);
+  const T nrm = gx * gx + gy * gy + gz * gz;
+  T kap;
+  if (nrm < (T)1e-10) {
+    kap = (T)0;
   } else {
-    const double s = sqrt(nrm);            // nrm**0.5
-    const double inv15 = 1.0 / (nrm * s);  // nrm**(-1.5)
-    const double term1 = (d2x + d2y + d2z) / s;
-    const double term2 = (gx * gx * d2x + gy * gy * d2y + gz * gz * d2z) * inv15;
-    const double term3 = 2.0 * (gx * gy * d2xy + gx * gz * d2xz + gy * gz * d2yz) * inv15;
+    const T s = sqrt(nrm);             // nrm**0.5
+    const T inv15 = (T)1 / (nrm * s);  // nrm**(-1.5)
+    const T term1 = (d2x + d2y + d2z) / s;
+    const T term2 = (gx * gx * d2x + gy * gy * d2y + gz * gz * d2z) * inv15;
+    const T term3 = two * (gx * gy * d2xy + gx * gz * d2xz + gy * gz * d2yz) * inv15;
     kap = -(term1 - term2 - term3);
   }
-  if (kap > max_kappa) kap = max_kappa;
-  const double a = 1.0 / (2.0 * ph.sw);
-  const double dirac = a + a * cos(TPLS_PI_SP * p / ph.sw);
-  const double m = dirac * ph.scap * kap;
-  r.x = m * gx;
-  r.y = m * gy;
-  r.z = m * gz;
+  if (kap > (T)max_kappa) kap = (T)max_kappa;
+  const T a = (T)(1.0 / (2.0 * ph.sw));
+  const T dirac = a + a * cos((T)TPLS_PI_SP * p / (T)ph.sw);
+  const T m = dirac * (T)ph.scap * kap;
+  r.x = (double)(m * gx);
+  r.y = (double)(m * gy);
+  r.z = (double)(m * gz);
   return r;
 }
 
@@ -250,37 +280,47 @@ __device__ __forceinline__ F3 lin2(F3 a, F3 b) {  // 2a - b
 }
 
 // value on the i = 1..nx columns including the extrapolated z ghost planes
+template <typename T>
 __device__ __forceinline__ F3 csf_colval(const Geo &g, const Phys &ph, double mk,
                                          const double *fi, int i, int j, int k) {
-  if (k == 0) return lin2(csf_point(g, ph, mk, fi, i, j, 1), csf_point(g, ph, mk, fi, i, j, 2));
+  if (k == 0) return lin2(csf_point<T>(g, ph, mk, fi, i, j, 1), csf_point<T>(g, ph, mk, fi, i, j, 2));
   if (k == g.nz + 1)
-    return lin2(csf_point(g, ph, mk, fi, i, j, g.nz), csf_point(g, ph, mk, fi, i, j, g.nz - 1));
-  return csf_point(g, ph, mk, fi, i, j, k);
+    return lin2(csf_point<T>(g, ph, mk, fi, i, j, g.nz), csf_point<T>(g, ph, mk, fi, i, j, g.nz - 1));
+  return csf_point<T>(g, ph, mk, fi, i, j, k);
 }
 
+// T: arithmetic of the curvature (double, or float in the FP32-mixed form);
+// TO: storage of the force components.
+template <typename T, typename TO>
 __global__ void k_csf(Geo g, Phys ph, double mk, const double *__restrict__ fi,
-                      double *__restrict__ fx, double *__restrict__ fy, double *__restrict__ fz) {
+                      TO *__restrict__ fx, TO *__restrict__ fy, TO *__restrict__ fz) {
   const int i = blockIdx.x * LS_BX + threadIdx.x, j = blockIdx.y * LS_BY + threadIdx.y;
   const int k = blockIdx.z;
   if (i > g.nx + 1 || j > g.ny + 1) return;
   const int jj = wrapy(j, g.ny);
   F3 v;
   if (i == 0)
-    v = lin2(csf_colval(g, ph, mk, fi, 1, jj, k), csf_colval(g, ph, mk, fi, 2, jj, k));
+    v = lin2(csf_colval<T>(g, ph, mk, fi, 1, jj, k), csf_colval<T>(g, ph, mk, fi, 2, jj, k));
   else if (i == g.nx + 1)
-    v = lin2(csf_colval(g, ph, mk, fi, g.nx, jj, k), csf_colval(g, ph, mk, fi, g.nx - 1, jj, k));
+    v = lin2(csf_colval<T>(g, ph, mk, fi, g.nx, jj, k), csf_colval<T>(g, ph, mk, fi, g.nx - 1, jj, k));
   else
-    v = csf_colval(g, ph, mk, fi, i, jj, k);
+    v = csf_colval<T>(g, ph, mk, fi, i, jj, k);
   const int c = TPLS_IDX(g, i, j, k);
-  fx[c] = v.x;
-  fy[c] = v.y;
-  fz[c] = v.z;
+  fx[c] = (TO)v.x;
+  fy[c] = (TO)v.y;
+  fz[c] = (TO)v.z;
 }
 
 cudaError_t launch_csf(const Geo &g, const Phys &ph, const double *phi3,
                        double *fx, double *fy, double *fz, cudaStream_t st) {
   const double mk = 1.0 / fmin(fmin(ph.dx, ph.dy), ph.dz);
-  k_csf<<<full_grid(g, g.nz + 2), dim3(LS_BX, LS_BY), 0, st>>>(g, ph, mk, phi3, fx, fy, fz);
+  k_csf<double, double><<<full_grid(g, g.nz + 2), dim3(LS_BX, LS_BY), 0, st>>>(g, ph, mk, phi3, fx, fy, fz);
+  return cudaGetLastError();
+}
+cudaError_t launch_csf(const Geo &g, const Phys &ph, const double *phi3, float *fx, float *fy, float *fz,
+                       cudaStream_t st) {
+  const double mk = 1.0 / fmin(fmin(ph.dx, ph.dy), ph.dz);
+  k_csf<float, float><<<full_grid(g, g.nz + 2), dim3(LS_BX, LS_BY), 0, st>>>(g, ph, mk, phi3, fx, fy, fz);
   return cudaGetLastError();
 }
 
@@ -288,7 +328,8 @@ cudaError_t launch_csf(const Geo &g, const Phys &ph, const double *phi3,
 // momentum_allflux.f90:474-521 get_viscosity on x = 0..nx+1 (the ghost
 // planes of main_ns_hybrid.F90:653-710 use the same formula and the same
 // single-precision pi) and the 2-row periodic-y augmentation.
-__global__ void k_visc(Geo g, Phys ph, const double *__restrict__ phi, double *__restrict__ mu) {
+template <typename T>
+__global__ void k_visc(Geo g, Phys ph, const double *__restrict__ phi, T *__restrict__ mu) {
   const int i = blockIdx.x * LS_BX + threadIdx.x, j = blockIdx.y * LS_BY + threadIdx.y - 1;
   const int k = blockIdx.z;
   if (i > g.nx + 1 || j > g.ny + 2) return;
@@ -300,13 +341,18 @@ __global__ void k_visc(Geo g, Phys ph, const double *__restrict__ phi, double *_
     hv = 1.0;
   else
     hv = 0.5 + (p / (2.0 * ph.sw)) + (1.0 / (2.0 * TPLS_PI_SP)) * sin(TPLS_PI_SP * p / ph.sw);
-  mu[TPLS_IDXM(g, i, j, k)] = (ph.mu_plus * hv + ph.mu_minus * (1.0 - hv)) / ph.re;
+  mu[TPLS_IDXM(g, i, j, k)] = (T)((ph.mu_plus * hv + ph.mu_minus * (1.0 - hv)) / ph.re);
 }
 
 cudaError_t launch_visc(const Geo &g, const Phys &ph, const double *phi2,
                         double *mu, cudaStream_t st) {
   dim3 grd((g.nx + 2 + LS_BX - 1) / LS_BX, (g.ny + 4 + LS_BY - 1) / LS_BY, g.nz + 2);
-  k_visc<<<grd, dim3(LS_BX, LS_BY), 0, st>>>(g, ph, phi2, mu);
+  k_visc<double><<<grd, dim3(LS_BX, LS_BY), 0, st>>>(g, ph, phi2, mu);
+  return cudaGetLastError();
+}
+cudaError_t launch_visc(const Geo &g, const Phys &ph, const double *phi2, float *mu, cudaStream_t st) {
+  dim3 grd((g.nx + 2 + LS_BX - 1) / LS_BX, (g.ny + 4 + LS_BY - 1) / LS_BY, g.nz + 2);
+  k_visc<float><<<grd, dim3(LS_BX, LS_BY), 0, st>>>(g, ph, phi2, mu);
   return cudaGetLastError();
 }
 

@@ -19,49 +19,48 @@
 // copy (legal for even ny: no point of the colour being relaxed reads a
 // ghost row written in the same half-sweep); for odd ny the caller runs a
 // separate exchange after each half-sweep instead.
-#include "tpls_kernels.h"
+#include "tpls_sweep.cuh"
 
 namespace tpls {
 
-struct Fc {
-  double px, mx, py, my, pz, mz;
+template <typename T>
+struct FcT {
+  T px, mx, py, my, pz, mz;
 };
+using Fc = FcT<double>;
 
-struct Helm {
-  double ax2, ay2, az2;  // dt/(2 d^2)
-  double dtdx;           // dt/dx (u outlet condition)
-};
 
 // face viscosities, momentum_allflux.f90:91-98 (u), :145-152 (v), :187-194 (w)
-__device__ __forceinline__ Fc faces(int comp, const Geo &g, const double *__restrict__ mu, int i,
-                                    int j, int k) {
+template <typename T>
+__device__ __forceinline__ FcT<T> faces(int comp, const Geo &g, const T *__restrict__ mu, int i, int j,
+                                        int k) {
   const int sy = g.sy, sz = g.szm;
-  Fc f;
+  FcT<T> f;
   if (comp == 0) {
-    const double *m = mu + TPLS_IDXM(g, i, j + 1, k + 1);
-    const double a = m[0], b = m[1];
+    const T *m = mu + TPLS_IDXM(g, i, j + 1, k + 1);
+    const T a = m[0], b = m[1];
     f.px = b;
     f.mx = a;
-    f.py = (a + b + m[sy] + m[1 + sy]) * 0.25;
-    f.my = (a + b + m[-sy] + m[1 - sy]) * 0.25;
-    f.pz = (a + b + m[sz] + m[1 + sz]) * 0.25;
-    f.mz = (a + b + m[-sz] + m[1 - sz]) * 0.25;
+    f.py = (a + b + m[sy] + m[1 + sy]) * (T)0.25;
+    f.my = (a + b + m[-sy] + m[1 - sy]) * (T)0.25;
+    f.pz = (a + b + m[sz] + m[1 + sz]) * (T)0.25;
+    f.mz = (a + b + m[-sz] + m[1 - sz]) * (T)0.25;
   } else if (comp == 1) {
-    const double *m = mu + TPLS_IDXM(g, i, j + 1, k + 1);
-    const double a = m[0], b = m[-sy];
-    f.px = (a + b + m[1] + m[1 - sy]) * 0.25;
-    f.mx = (a + b + m[-1] + m[-1 - sy]) * 0.25;
+    const T *m = mu + TPLS_IDXM(g, i, j + 1, k + 1);
+    const T a = m[0], b = m[-sy];
+    f.px = (a + b + m[1] + m[1 - sy]) * (T)0.25;
+    f.mx = (a + b + m[-1] + m[-1 - sy]) * (T)0.25;
     f.py = a;
     f.my = b;
-    f.pz = (a + b + m[sz] + m[sz - sy]) * 0.25;
-    f.mz = (a + b + m[-sz] + m[-sz - sy]) * 0.25;
+    f.pz = (a + b + m[sz] + m[sz - sy]) * (T)0.25;
+    f.mz = (a + b + m[-sz] + m[-sz - sy]) * (T)0.25;
   } else {
-    const double *m = mu + TPLS_IDXM(g, i, j + 1, k);
-    const double a = m[0], b = m[sz];
-    f.px = (a + b + m[1] + m[1 + sz]) * 0.25;
-    f.mx = (a + b + m[-1] + m[-1 + sz]) * 0.25;
-    f.py = (a + b + m[sy] + m[sy + sz]) * 0.25;
-    f.my = (a + b + m[-sy] + m[-sy + sz]) * 0.25;
+    const T *m = mu + TPLS_IDXM(g, i, j + 1, k);
+    const T a = m[0], b = m[sz];
+    f.px = (a + b + m[1] + m[1 + sz]) * (T)0.25;
+    f.mx = (a + b + m[-1] + m[-1 + sz]) * (T)0.25;
+    f.py = (a + b + m[sy] + m[sy + sz]) * (T)0.25;
+    f.my = (a + b + m[-sy] + m[-sy + sz]) * (T)0.25;
     f.pz = b;
     f.mz = a;
   }
@@ -81,69 +80,71 @@ __device__ __forceinline__ double helm(const Fc &f, const Helm &h, double xp, do
 
 // ---------------------------------------------------------------------------
 // get_conv_all / get_diffusion_all point forms.
-struct CD {
-  double conv, diff;
+template <typename T>
+struct CDT {
+  T conv, diff;
 };
 
-__device__ __forceinline__ CD conv_diff(int comp, const Geo &g, double rdx, double rdy,
-                                        double rdz, const double *__restrict__ U,
-                                        const double *__restrict__ V,
-                                        const double *__restrict__ W, const Fc &f, int i,
-                                        int j, int k) {
+template <typename T>
+__device__ __forceinline__ CDT<T> conv_diff(int comp, const Geo &g, T rdx, T rdy, T rdz,
+                                            const T *__restrict__ U, const T *__restrict__ V,
+                                            const T *__restrict__ W, const FcT<T> &f, int i, int j,
+                                            int k) {
   const int sy = g.sy, sz = g.sz, nzu = g.nz;  // u/v have planes 0..nz-1
   const int c = TPLS_IDX(g, i, j, k);
-  CD r;
+  const T h = (T)0.5, two = (T)2, third = (T)(1.0 / 3.0);
+  CDT<T> r;
   if (comp == 0) {
-    const double x = U[c];
-    const double tempv = (V[c] + V[c + 1] + V[c + sy] + V[c + 1 + sy]) * 0.25;
-    const double tempw = (W[c] + W[c + 1] + W[c + sz] + W[c + 1 + sz]) * 0.25;
-    const double Xc = 0.5 * (U[c + 1] - U[c - 1]) * rdx * x;
-    const double Yc = 0.5 * (U[c + sy] - U[c - sy]) * rdy * tempv;
-    double dz_;
-    if (k == 0) dz_ = (x + U[c + sz]) * (0.5 * rdz);
-    else if (k == nzu - 1) dz_ = -(x + U[c - sz]) * (0.5 * rdz);
-    else dz_ = 0.5 * (U[c + sz] - U[c - sz]) * rdz;
-    const double t1 = Xc + Yc + dz_ * tempw;
-    const double E = f.px * (U[c + 1] - x) * rdx, Wt = f.mx * (x - U[c - 1]) * rdx;
-    const double N = f.py * (V[c + 1 + sy] - V[c + sy]) * rdx, S = f.my * (V[c + 1] - V[c]) * rdx;
-    const double O = f.pz * (W[c + 1 + sz] - W[c + sz]) * rdx, I = f.mz * (W[c + 1] - W[c]) * rdx;
+    const T x = U[c];
+    const T tempv = (V[c] + V[c + 1] + V[c + sy] + V[c + 1 + sy]) * (T)0.25;
+    const T tempw = (W[c] + W[c + 1] + W[c + sz] + W[c + 1 + sz]) * (T)0.25;
+    const T Xc = h * (U[c + 1] - U[c - 1]) * rdx * x;
+    const T Yc = h * (U[c + sy] - U[c - sy]) * rdy * tempv;
+    T dz_;
+    if (k == 0) dz_ = (x + U[c + sz]) * (h * rdz);
+    else if (k == nzu - 1) dz_ = -(x + U[c - sz]) * (h * rdz);
+    else dz_ = h * (U[c + sz] - U[c - sz]) * rdz;
+    const T t1 = Xc + Yc + dz_ * tempw;
+    const T E = f.px * (U[c + 1] - x) * rdx, Wt = f.mx * (x - U[c - 1]) * rdx;
+    const T N = f.py * (V[c + 1 + sy] - V[c + sy]) * rdx, S = f.my * (V[c + 1] - V[c]) * rdx;
+    const T O = f.pz * (W[c + 1 + sz] - W[c + sz]) * rdx, I = f.mz * (W[c + 1] - W[c]) * rdx;
     r.conv = t1 - ((E - Wt) * rdx + (N - S) * rdy + (O - I) * rdz);
-    const double umz = (k == 0) ? -2.0 * x + U[c + sz] * (1.0 / 3.0) : U[c - sz];
-    const double upz = (k == nzu - 1) ? -2.0 * x + U[c - sz] * (1.0 / 3.0) : U[c + sz];
+    const T umz = (k == 0) ? -two * x + U[c + sz] * third : U[c - sz];
+    const T upz = (k == nzu - 1) ? -two * x + U[c - sz] * third : U[c + sz];
     r.diff = (f.px * (U[c + 1] - x) - f.mx * (x - U[c - 1])) * (rdx * rdx) +
              (f.py * (U[c + sy] - x) - f.my * (x - U[c - sy])) * (rdy * rdy) +
              (f.pz * (upz - x) - f.mz * (x - umz)) * (rdz * rdz);
   } else if (comp == 1) {
-    const double x = V[c];
-    const double tempu = (U[c - 1 - sy] + U[c - 1] + U[c - sy] + U[c]) * 0.25;
-    const double tempw = (W[c - sy] + W[c] + W[c - sy + sz] + W[c + sz]) * 0.25;
-    const double Yc = 0.5 * (V[c + sy] - V[c - sy]) * rdy * x;
-    const double Xc = 0.5 * (V[c + 1] - V[c - 1]) * rdx * tempu;
-    double dz_;
-    if (k == 0) dz_ = (x + V[c + sz]) * (0.5 * rdz);
-    else if (k == nzu - 1) dz_ = -(x + V[c - sz]) * (0.5 * rdz);
-    else dz_ = 0.5 * (V[c + sz] - V[c - sz]) * rdz;
-    const double t1 = Xc + Yc + dz_ * tempw;
-    const double E = f.px * (U[c] - U[c - sy]) * rdy, Wt = f.mx * (U[c - 1] - U[c - 1 - sy]) * rdy;
-    const double N = f.py * (V[c + sy] - x) * rdy, S = f.my * (x - V[c - sy]) * rdy;
-    const double O = f.pz * (W[c + sz] - W[c - sy + sz]) * rdy, I = f.mz * (W[c] - W[c - sy]) * rdy;
+    const T x = V[c];
+    const T tempu = (U[c - 1 - sy] + U[c - 1] + U[c - sy] + U[c]) * (T)0.25;
+    const T tempw = (W[c - sy] + W[c] + W[c - sy + sz] + W[c + sz]) * (T)0.25;
+    const T Yc = h * (V[c + sy] - V[c - sy]) * rdy * x;
+    const T Xc = h * (V[c + 1] - V[c - 1]) * rdx * tempu;
+    T dz_;
+    if (k == 0) dz_ = (x + V[c + sz]) * (h * rdz);
+    else if (k == nzu - 1) dz_ = -(x + V[c - sz]) * (h * rdz);
+    else dz_ = h * (V[c + sz] - V[c - sz]) * rdz;
+    const T t1 = Xc + Yc + dz_ * tempw;
+    const T E = f.px * (U[c] - U[c - sy]) * rdy, Wt = f.mx * (U[c - 1] - U[c - 1 - sy]) * rdy;
+    const T N = f.py * (V[c + sy] - x) * rdy, S = f.my * (x - V[c - sy]) * rdy;
+    const T O = f.pz * (W[c + sz] - W[c - sy + sz]) * rdy, I = f.mz * (W[c] - W[c - sy]) * rdy;
     r.conv = t1 - ((E - Wt) * rdx + (N - S) * rdy + (O - I) * rdz);
-    const double vmz = (k == 0) ? -2.0 * x + V[c + sz] * (1.0 / 3.0) : V[c - sz];
-    const double vpz = (k == nzu - 1) ? -2.0 * x + V[c - sz] * (1.0 / 3.0) : V[c + sz];
+    const T vmz = (k == 0) ? -two * x + V[c + sz] * third : V[c - sz];
+    const T vpz = (k == nzu - 1) ? -two * x + V[c - sz] * third : V[c + sz];
     r.diff = (f.px * (V[c + 1] - x) - f.mx * (x - V[c - 1])) * (rdx * rdx) +
              (f.py * (V[c + sy] - x) - f.my * (x - V[c - sy])) * (rdy * rdy) +
              (f.pz * (vpz - x) - f.mz * (x - vmz)) * (rdz * rdz);
   } else {
-    const double x = W[c];
-    const double tempu = (U[c - 1 - sz] + U[c - 1] + U[c - sz] + U[c]) * 0.25;
-    const double tempv = (V[c - sz] + V[c] + V[c + sy - sz] + V[c + sy]) * 0.25;
-    const double Zc = 0.5 * (W[c + sz] - W[c - sz]) * rdz * x;
-    const double Xc = 0.5 * (W[c + 1] - W[c - 1]) * rdx * tempu;
-    const double Yc = 0.5 * (W[c + sy] - W[c - sy]) * rdy * tempv;
-    const double t1 = Xc + Yc + Zc;
-    const double E = f.px * (U[c] - U[c - sz]) * rdz, Wt = f.mx * (U[c - 1] - U[c - 1 - sz]) * rdz;
-    const double N = f.py * (V[c + sy] - V[c + sy - sz]) * rdz, S = f.my * (V[c] - V[c - sz]) * rdz;
-    const double O = f.pz * (W[c + sz] - x) * rdz, I = f.mz * (x - W[c - sz]) * rdz;
+    const T x = W[c];
+    const T tempu = (U[c - 1 - sz] + U[c - 1] + U[c - sz] + U[c]) * (T)0.25;
+    const T tempv = (V[c - sz] + V[c] + V[c + sy - sz] + V[c + sy]) * (T)0.25;
+    const T Zc = h * (W[c + sz] - W[c - sz]) * rdz * x;
+    const T Xc = h * (W[c + 1] - W[c - 1]) * rdx * tempu;
+    const T Yc = h * (W[c + sy] - W[c - sy]) * rdy * tempv;
+    const T t1 = Xc + Yc + Zc;
+    const T E = f.px * (U[c] - U[c - sz]) * rdz, Wt = f.mx * (U[c - 1] - U[c - 1 - sz]) * rdz;
+    const T N = f.py * (V[c + sy] - V[c + sy - sz]) * rdz, S = f.my * (V[c] - V[c - sz]) * rdz;
+    const T O = f.pz * (W[c + sz] - x) * rdz, I = f.mz * (x - W[c - sz]) * rdz;
     r.conv = t1 - ((E - Wt) * rdx + (N - S) * rdy + (O - I) * rdz);
     r.diff = (f.px * (W[c + 1] - x) - f.mx * (x - W[c - 1])) * (rdx * rdx) +
              (f.py * (W[c + sy] - x) - f.my * (x - W[c - sy])) * (rdy * rdy) +
@@ -169,63 +170,93 @@ __device__ __forceinline__ bool cd_valid(int comp, const Geo &g, int i, int k) {
 // at k = 0 the czm slot multiplies the point itself and czp absorbs czm/3;
 // at k = nz-1 the czp slot multiplies the point itself and czm absorbs
 // czp/3.  One 64-byte record per point: (cxp, cxm, cyp, cym, czp, czm, b, 0).
-__device__ __forceinline__ void write_coef(int comp, const Geo &g, const Helm &h, const Fc &f,
-                                           double rhs, int k, double *__restrict__ rec) {
-  const double diag =
-      1.0 + h.ax2 * (f.px + f.mx) + h.ay2 * (f.py + f.my) + h.az2 * (f.pz + f.mz);
-  const double r = 1.0 / diag;
-  double czp = h.az2 * f.pz * r, czm = h.az2 * f.mz * r;
-  if (comp != 2) {
-    if (k == 0) {
-      czp += czm * (1.0 / 3.0);
-      czm = -2.0 * czm;
-    } else if (k == g.nz - 1) {
-      czm += czp * (1.0 / 3.0);
-      czp = -2.0 * czp;
-    }
-  }
+template <typename T>
+__device__ __forceinline__ void store_rec(T *rec, T a0, T a1, T a2, T a3, T a4, T a5, T a6);
+template <>
+__device__ __forceinline__ void store_rec<double>(double *rec, double a0, double a1, double a2, double a3,
+                                                  double a4, double a5, double a6) {
   double2 *o = reinterpret_cast<double2 *>(rec);
-  o[0] = make_double2(h.ax2 * f.px * r, h.ax2 * f.mx * r);
-  o[1] = make_double2(h.ay2 * f.py * r, h.ay2 * f.my * r);
-  o[2] = make_double2(czp, czm);
-  o[3] = make_double2(rhs * r, 0.0);
+  o[0] = make_double2(a0, a1);
+  o[1] = make_double2(a2, a3);
+  o[2] = make_double2(a4, a5);
+  o[3] = make_double2(a6, 0.0);
+}
+template <>
+__device__ __forceinline__ void store_rec<float>(float *rec, float a0, float a1, float a2, float a3, float a4,
+                                                 float a5, float a6) {
+  float4 *o = reinterpret_cast<float4 *>(rec);
+  o[0] = make_float4(a0, a1, a2, a3);
+  o[1] = make_float4(a4, a5, a6, 0.f);
 }
 
+template <typename T>
+__device__ __forceinline__ void write_coef(int comp, const Geo &g, const Helm &h, const FcT<T> &f,
+                                           double rhs, int k, T *__restrict__ rec) {
+  const T ax2 = (T)h.ax2, ay2 = (T)h.ay2, az2 = (T)h.az2;
+  const T diag = (T)1 + ax2 * (f.px + f.mx) + ay2 * (f.py + f.my) + az2 * (f.pz + f.mz);
+  const T r = (T)1 / diag;
+  T czp = az2 * f.pz * r, czm = az2 * f.mz * r;
+  if (comp != 2) {
+    if (k == 0) {
+      czp += czm * (T)(1.0 / 3.0);
+      czm = (T)(-2) * czm;
+    } else if (k == g.nz - 1) {
+      czm += czp * (T)(1.0 / 3.0);
+      czp = (T)(-2) * czp;
+    }
+  }
+  store_rec<T>(rec, ax2 * f.px * r, ax2 * f.mx * r, ay2 * f.py * r, ay2 * f.my * r, czp, czm, (T)rhs * r);
+}
+
+// X64 is the component's FP64 state (u2, v2 or w2): the right-hand side is
+// assembled in FP64 even when the stencils run in FP32 (T = float).
+template <typename T>
 __global__ void __launch_bounds__(MB_X *MB_Y)
-    k_mom_rhs(int comp, Geo g, Phys ph, Helm hm, const double *__restrict__ U,
-              const double *__restrict__ V, const double *__restrict__ W,
-              const double *__restrict__ mu, const double *__restrict__ fc,
-              const double *__restrict__ c1, const double *__restrict__ c0,
-              const double *__restrict__ s1, const double *__restrict__ s0,
-              double *__restrict__ conv2, double *__restrict__ csf2, double *__restrict__ rhs,
-              double *__restrict__ diff_out, double *__restrict__ coef) {
+    k_mom_rhs(int comp, Geo g, Phys ph, Helm hm, const T *__restrict__ U, const T *__restrict__ V,
+              const T *__restrict__ W, const double *__restrict__ X64, const T *__restrict__ mu,
+              const T *__restrict__ fc, const double *__restrict__ c1, const double *__restrict__ c0,
+              const double *__restrict__ s1, const double *__restrict__ s0, double *__restrict__ conv2,
+              double *__restrict__ csf2, double *__restrict__ rhs, double *__restrict__ diff_out,
+              T *__restrict__ coef) {
   const int i = blockIdx.x * MB_X + threadIdx.x + 1, j = blockIdx.y * MB_Y + threadIdx.y + 1;
   const int k = blockIdx.z;
   if (i > g.nx || j > g.ny) return;
   const int c = TPLS_IDX(g, i, j, k);
-  CD cd = {0.0, 0.0};
+  CDT<T> cd = {(T)0, (T)0};
   const bool valid = cd_valid(comp, g, i, k);
-  Fc f;
+  FcT<T> f;
   if (valid) {
     f = faces(comp, g, mu, i, j, k);
-    cd = conv_diff(comp, g, 1.0 / ph.dx, 1.0 / ph.dy, 1.0 / ph.dz, U, V, W, f, i, j, k);
+    cd = conv_diff<T>(comp, g, (T)(1.0 / ph.dx), (T)(1.0 / ph.dy), (T)(1.0 / ph.dz), U, V, W, f, i, j, k);
   }
   // main_ns_hybrid.F90:629-641 face averages of the CSF force
   double s2;
-  if (comp == 0) s2 = (fc[TPLS_IDX(g, i + 1, j + 1, k + 1)] + fc[TPLS_IDX(g, i, j + 1, k + 1)]) * 0.5;
-  else if (comp == 1) s2 = (fc[TPLS_IDX(g, i, j + 1, k + 1)] + fc[TPLS_IDX(g, i, j, k + 1)]) * 0.5;
-  else s2 = (fc[TPLS_IDX(g, i, j + 1, k + 1)] + fc[TPLS_IDX(g, i, j + 1, k)]) * 0.5;
-  const double X = (comp == 0) ? U[c] : (comp == 1) ? V[c] : W[c];
-  const double dt = ph.dt;
+  if (comp == 0) s2 = ((double)fc[TPLS_IDX(g, i + 1, j + 1, k + 1)] + (double)fc[TPLS_IDX(g, i, j + 1, k + 1)]) * 0.5;
+  else if (comp == 1) s2 = ((double)fc[TPLS_IDX(g, i, j + 1, k + 1)] + (double)fc[TPLS_IDX(g, i, j, k + 1)]) * 0.5;
+  else s2 = ((double)fc[TPLS_IDX(g, i, j + 1, k + 1)] + (double)fc[TPLS_IDX(g, i, j + 1, k)]) * 0.5;
+  const double X = X64[c];
+  const double dt = ph.dt, conv = (double)cd.conv, diff = (double)cd.diff;
   // main_ns_hybrid.F90:743-751 (AB3 convection and CSF, CN diffusion)
-  const double r = X - dt * ((23.0 / 12.0) * cd.conv - (4.0 / 3.0) * c1[c] + (5.0 / 12.0) * c0[c]) +
-                   (dt / 2.0) * cd.diff +
+  const double r = X - dt * ((23.0 / 12.0) * conv - (4.0 / 3.0) * c1[c] + (5.0 / 12.0) * c0[c]) +
+                   (dt / 2.0) * diff +
                    dt * ((23.0 / 12.0) * s2 - (4.0 / 3.0) * s1[c] + (5.0 / 12.0) * s0[c]);
-  conv2[c] = cd.conv;
+  conv2[c] = conv;
   csf2[c] = s2;
   if (rhs) rhs[c] = r;
-  if (diff_out) diff_out[c] = cd.diff;
+  if (diff_out) diff_out[c] = diff;
   if (coef && valid) write_coef(comp, g, hm, f, r, k, coef + 8 * (size_t)c);
+}
+
+template <typename T>
+static cudaError_t mom_rhs(int comp, const Geo &g, const Phys &ph, const T *u2, const T *v2, const T *w2,
+                           const double *x64, const T *mu, const T *fcsf, const double *c1, const double *c0,
+                           const double *s1, const double *s0, double *conv2, double *csf2, double *rhs,
+                           double *diff_out, T *coef, cudaStream_t st) {
+  const int nk = (comp == 2) ? g.nz + 1 : g.nz;
+  dim3 grd((g.nx + MB_X - 1) / MB_X, (g.ny + MB_Y - 1) / MB_Y, nk);
+  k_mom_rhs<T><<<grd, dim3(MB_X, MB_Y), 0, st>>>(comp, g, ph, helm_of(ph), u2, v2, w2, x64, mu, fcsf, c1, c0,
+                                                 s1, s0, conv2, csf2, rhs, diff_out, coef);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_mom_rhs(int comp, const Geo &g, const Phys &ph,
@@ -235,16 +266,17 @@ cudaError_t launch_mom_rhs(int comp, const Geo &g, const Phys &ph,
                            const double *c0, const double *s1,
                            const double *s0, double *conv2, double *csf2,
                            double *rhs, double *diff_out, double *coef, cudaStream_t st) {
-  const int nk = (comp == 2) ? g.nz + 1 : g.nz;
-  Helm hm;
-  hm.ax2 = (ph.dt / (ph.dx * ph.dx)) / 2.0;
-  hm.ay2 = (ph.dt / (ph.dy * ph.dy)) / 2.0;
-  hm.az2 = (ph.dt / (ph.dz * ph.dz)) / 2.0;
-  hm.dtdx = ph.dt / ph.dx;
-  dim3 grd((g.nx + MB_X - 1) / MB_X, (g.ny + MB_Y - 1) / MB_Y, nk);
-  k_mom_rhs<<<grd, dim3(MB_X, MB_Y), 0, st>>>(comp, g, ph, hm, u2, v2, w2, mu, fcsf, c1, c0, s1, s0,
-                                              conv2, csf2, rhs, diff_out, coef);
-  return cudaGetLastError();
+  const double *x64 = (comp == 0) ? u2 : (comp == 1) ? v2 : w2;
+  return mom_rhs<double>(comp, g, ph, u2, v2, w2, x64, mu, fcsf, c1, c0, s1, s0, conv2, csf2, rhs, diff_out,
+                         coef, st);
+}
+
+cudaError_t launch_mom_rhs32(int comp, const Geo &g, const Phys &ph, const float *u2, const float *v2,
+                             const float *w2, const double *x64, const float *mu, const float *fcsf,
+                             const double *c1, const double *c0, const double *s1, const double *s0,
+                             double *conv2, double *csf2, float *coef, cudaStream_t st) {
+  return mom_rhs<float>(comp, g, ph, u2, v2, w2, x64, mu, fcsf, c1, c0, s1, s0, conv2, csf2, nullptr, nullptr,
+                        coef, st);
 }
 
 // standalone get_conv_all / get_diffusion_all: out = conv or diff on the
@@ -256,7 +288,7 @@ __global__ void k_conv_diff(int comp, int want_conv, Geo g, Phys ph, const doubl
   const int k = blockIdx.z;
   if (i > g.nx || j > g.ny || !cd_valid(comp, g, i, k)) return;
   const Fc f = faces(comp, g, mu, i, j, k);
-  CD cd = conv_diff(comp, g, 1.0 / ph.dx, 1.0 / ph.dy, 1.0 / ph.dz, U, V, W, f, i, j, k);
+  CDT<double> cd = conv_diff<double>(comp, g, 1.0 / ph.dx, 1.0 / ph.dy, 1.0 / ph.dz, U, V, W, f, i, j, k);
   out[TPLS_IDX(g, i, j, k)] = want_conv ? cd.conv : cd.diff;
 }
 
@@ -268,26 +300,6 @@ cudaError_t launch_conv_diff(int comp, int want_conv, const Geo &g,
   dim3 grd((g.nx + MB_X - 1) / MB_X, (g.ny + MB_Y - 1) / MB_Y, nk);
   k_conv_diff<<<grd, dim3(MB_X, MB_Y), 0, st>>>(comp, want_conv, g, ph, u2, v2, w2, mu, out);
   return cudaGetLastError();
-}
-
-// ---------------------------------------------------------------------------
-// Writers with the fused periodic ghost copy.
-__device__ __forceinline__ void put(const Geo &g, double *x, int i, int j, int k, double v,
-                                    int fuse) {
-  x[TPLS_IDX(g, i, j, k)] = v;
-  if (fuse) {
-    if (j == g.ny) x[TPLS_IDX(g, i, 0, k)] = v;
-    if (j == 1) x[TPLS_IDX(g, i, g.ny + 1, k)] = v;
-  }
-}
-
-// u outlet, main_ns_hybrid.F90:768-776 (note the pressure row index is the
-// u row index j, as written in the reference)
-__device__ __forceinline__ double u_outlet(const Geo &g, const Helm &h, const double *P,
-                                           double unm1, int j, int k) {
-  const int nx = g.nx;
-  return unm1 + h.dtdx * (P[TPLS_IDX(g, nx + 1, j, k + 1)] + P[TPLS_IDX(g, nx - 1, j, k + 1)] -
-                          2.0 * P[TPLS_IDX(g, nx, j, k + 1)]);
 }
 
 // z neighbours for u/v with the wall ghost rule `-2*x(0)+x(1)/3`
@@ -363,26 +375,6 @@ cudaError_t launch_jacobi(int comp, const Geo &g, const Phys &ph,
   dim3 grd((iend + MB_X - 1) / MB_X, (g.ny + MB_Y - 1) / MB_Y, nk);
   k_jacobi<<<grd, dim3(MB_X, MB_Y), 0, st>>>(comp, g, h, xo, rhs, mu, pres, x, bc, fuse_ghosts);
   return cudaGetLastError();
-}
-
-// Post-sweep boundary rows (main_ns_hybrid.F90:784-799 u, :826-836 v,
-// :860-879 w), written by the thread that owns the first / last x pair.
-__device__ __forceinline__ void sor_bc(int comp, const Geo &g, const Helm &h, double *x,
-                                       const double *P, int i2, int i, int iend, double v, int j,
-                                       int k, int fuse) {
-  if (i2 == 0) {
-    const double v1 = (i == 1) ? v : x[TPLS_IDX(g, 1, j, k)];
-    put(g, x, 0, j, k, v1, fuse);
-  }
-  if (i2 == (iend - 1) / 2) {
-    const double ve = (i == iend) ? v : x[TPLS_IDX(g, iend, j, k)];
-    if (comp == 0) {
-      put(g, x, g.nx, j, k, u_outlet(g, h, P, ve, j, k), fuse);
-      put(g, x, g.nx + 1, j, k, 0.0, fuse);
-    } else {
-      put(g, x, g.nx + 1, j, k, ve, fuse);
-    }
-  }
 }
 
 // sor_iteration_allflux.f90:54-99 (and v, w): 3-D checkerboard half-sweep.
@@ -476,14 +468,14 @@ cudaError_t launch_sor(int comp, const Geo &g, const Phys &ph, double *x,
 
 // get_difference: per-block partials of sum (a-b)^2 over i 1..nx, j 1..ny,
 // planes 0..nzp-1.
-__global__ void k_diff2(Geo g, const double *__restrict__ a, const double *__restrict__ b,
-                        double *__restrict__ part) {
+template <typename T>
+__global__ void k_diff2(Geo g, const T *__restrict__ a, const T *__restrict__ b, double *__restrict__ part) {
   const int i = blockIdx.x * MB_X + threadIdx.x + 1, j = blockIdx.y * MB_Y + threadIdx.y + 1;
   const int k = blockIdx.z;
   double e = 0.0;
   if (i <= g.nx && j <= g.ny) {
     const int c = TPLS_IDX(g, i, j, k);
-    const double d = a[c] - b[c];
+    const double d = (double)a[c] - (double)b[c];
     e = d * d;
   }
   __shared__ double s[MB_X * MB_Y / 32];
@@ -502,48 +494,64 @@ int diff2_blocks(const Geo &g, int nzp) {
   return ((g.nx + MB_X - 1) / MB_X) * ((g.ny + MB_Y - 1) / MB_Y) * nzp;
 }
 
-cudaError_t launch_diff2(const Geo &g, const double *a, const double *b,
-                         int nzp, double *part, cudaStream_t st) {
+template <typename T>
+static cudaError_t diff2(const Geo &g, const T *a, const T *b, int nzp, double *part, cudaStream_t st) {
   dim3 grd((g.nx + MB_X - 1) / MB_X, (g.ny + MB_Y - 1) / MB_Y, nzp);
-  k_diff2<<<grd, dim3(MB_X, MB_Y), 0, st>>>(g, a, b, part);
+  k_diff2<T><<<grd, dim3(MB_X, MB_Y), 0, st>>>(g, a, b, part);
   return cudaGetLastError();
+}
+cudaError_t launch_diff2(const Geo &g, const double *a, const double *b, int nzp, double *part,
+                         cudaStream_t st) {
+  return diff2(g, a, b, nzp, part, st);
+}
+cudaError_t launch_diff2(const Geo &g, const float *a, const float *b, int nzp, double *part,
+                         cudaStream_t st) {
+  return diff2(g, a, b, nzp, part, st);
 }
 
 // ---------------------------------------------------------------------------
 // pressure.f90:16-56 get_source_pres on the full p-grid (zero outside the
 // interior, ghost rows included, as the routine itself leaves them).
-__global__ void k_source(Geo g, double rdx, double rdy, double rdz, double rdt,
-                         const double *__restrict__ U, const double *__restrict__ V,
-                         const double *__restrict__ W, double *__restrict__ rhs) {
+template <typename T>
+__global__ void k_source(Geo g, double rdx, double rdy, double rdz, double rdt, const T *__restrict__ U,
+                         const T *__restrict__ V, const T *__restrict__ W, double *__restrict__ rhs) {
   const int i = blockIdx.x * MB_X + threadIdx.x, j = blockIdx.y * MB_Y + threadIdx.y;
   const int k = blockIdx.z;
   if (i > g.nx + 1 || j > g.ny + 1) return;
   double r = 0.0;
   if (i >= 1 && i <= g.nx && j >= 1 && j <= g.ny && k >= 1 && k <= g.nz) {
     const int jj = j, jm = (jj == 1) ? g.ny : jj - 1;
-    r = ((U[TPLS_IDX(g, i, jm, k - 1)] - U[TPLS_IDX(g, i - 1, jm, k - 1)]) * rdx +
-         (V[TPLS_IDX(g, i, jj, k - 1)] - V[TPLS_IDX(g, i, jm, k - 1)]) * rdy +
-         (W[TPLS_IDX(g, i, jm, k)] - W[TPLS_IDX(g, i, jm, k - 1)]) * rdz) *
+    r = (((double)U[TPLS_IDX(g, i, jm, k - 1)] - (double)U[TPLS_IDX(g, i - 1, jm, k - 1)]) * rdx +
+         ((double)V[TPLS_IDX(g, i, jj, k - 1)] - (double)V[TPLS_IDX(g, i, jm, k - 1)]) * rdy +
+         ((double)W[TPLS_IDX(g, i, jm, k)] - (double)W[TPLS_IDX(g, i, jm, k - 1)]) * rdz) *
         rdt;
   }
   rhs[TPLS_IDX(g, i, j, k)] = r;
 }
 
-cudaError_t launch_source(const Geo &g, const Phys &ph, const double *u3,
-                          const double *v3, const double *w3, double *rhs_p,
+template <typename T>
+static cudaError_t source(const Geo &g, const Phys &ph, const T *u3, const T *v3, const T *w3, double *rhs_p,
                           cudaStream_t st) {
   dim3 grd((g.nx + 2 + MB_X - 1) / MB_X, (g.ny + 2 + MB_Y - 1) / MB_Y, g.nz + 2);
-  k_source<<<grd, dim3(MB_X, MB_Y), 0, st>>>(g, 1.0 / ph.dx, 1.0 / ph.dy, 1.0 / ph.dz, 1.0 / ph.dt,
-                                             u3, v3, w3, rhs_p);
+  k_source<T><<<grd, dim3(MB_X, MB_Y), 0, st>>>(g, 1.0 / ph.dx, 1.0 / ph.dy, 1.0 / ph.dz, 1.0 / ph.dt, u3, v3,
+                                                w3, rhs_p);
   return cudaGetLastError();
+}
+cudaError_t launch_source(const Geo &g, const Phys &ph, const double *u3, const double *v3, const double *w3,
+                          double *rhs_p, cudaStream_t st) {
+  return source(g, ph, u3, v3, w3, rhs_p, st);
+}
+cudaError_t launch_source(const Geo &g, const Phys &ph, const float *u3, const float *v3, const float *w3,
+                          double *rhs_p, cudaStream_t st) {
+  return source(g, ph, u3, v3, w3, rhs_p, st);
 }
 
 // pressure.f90:59-134 get_uvw_pres, written out of place into the next
 // state's velocity arrays over x 0..nx+1 and every row (ghost rows as
 // periodic copies).
-__global__ void k_project(Geo g, double dtdx, double dtdy, double dtdz,
-                          const double *__restrict__ U, const double *__restrict__ V,
-                          const double *__restrict__ W, const double *__restrict__ P,
+template <typename T>
+__global__ void k_project(Geo g, double dtdx, double dtdy, double dtdz, const T *__restrict__ U,
+                          const T *__restrict__ V, const T *__restrict__ W, const double *__restrict__ P,
                           const double *__restrict__ uin, double *__restrict__ uo,
                           double *__restrict__ vo, double *__restrict__ wo) {
   const int i = blockIdx.x * MB_X + threadIdx.x, j = blockIdx.y * MB_Y + threadIdx.y;
@@ -556,265 +564,30 @@ __global__ void k_project(Geo g, double dtdx, double dtdy, double dtdz,
     double u;
     if (i == 0) u = uin[k];
     else if (i == g.nx + 1) u = 0.0;
-    else u = U[cc] - dtdx * (P[cc + 1 + sy + sz] - P[cc + sy + sz]);
+    else u = (double)U[cc] - dtdx * (P[cc + 1 + sy + sz] - P[cc + sy + sz]);
     uo[c] = u;
-    vo[c] = V[cc] - dtdy * (P[cc + sy + sz] - P[cc + sz]);
+    vo[c] = (double)V[cc] - dtdy * (P[cc + sy + sz] - P[cc + sz]);
   }
-  wo[c] = W[cc] - dtdz * (P[cc + sy + sz] - P[cc + sy]);
+  wo[c] = (double)W[cc] - dtdz * (P[cc + sy + sz] - P[cc + sy]);
 }
 
-cudaError_t launch_project(const Geo &g, const Phys &ph, const double *u3,
-                           const double *v3, const double *w3,
-                           const double *p, const double *u_inlet,
-                           double *u_out, double *v_out, double *w_out,
-                           cudaStream_t st) {
+template <typename T>
+static cudaError_t project(const Geo &g, const Phys &ph, const T *u3, const T *v3, const T *w3, const double *p,
+                           const double *u_inlet, double *u_out, double *v_out, double *w_out, cudaStream_t st) {
   dim3 grd((g.nx + 2 + MB_X - 1) / MB_X, (g.ny + 2 + MB_Y - 1) / MB_Y, g.nz + 1);
-  k_project<<<grd, dim3(MB_X, MB_Y), 0, st>>>(g, ph.dt / ph.dx, ph.dt / ph.dy, ph.dt / ph.dz, u3, v3,
-                                              w3, p, u_inlet, u_out, v_out, w_out);
+  k_project<T><<<grd, dim3(MB_X, MB_Y), 0, st>>>(g, ph.dt / ph.dx, ph.dt / ph.dy, ph.dt / ph.dz, u3, v3, w3, p,
+                                                 u_inlet, u_out, v_out, w_out);
   return cudaGetLastError();
 }
-
-// ---------------------------------------------------------------------------
-// Sweeps on precomputed coefficient records (see write_coef): the same
-// Jacobi / red-black SOR updates as above with the face viscosities, the
-// diagonal and its reciprocal computed once per timestep instead of once per
-// sweep.  Boundary rows and ghost copies as in the kernels above.
-struct Rec {
-  double2 x, y, z, b;  // (cxp,cxm) (cyp,cym) (czp,czm) (b,-)
-};
-__device__ __forceinline__ Rec load_rec(const double *__restrict__ coef, int c) {
-  const double2 *r = reinterpret_cast<const double2 *>(coef + 8 * (size_t)c);
-  Rec q;
-  q.x = __ldg(r);
-  q.y = __ldg(r + 1);
-  q.z = __ldg(r + 2);
-  q.b = __ldg(r + 3);
-  return q;
+cudaError_t launch_project(const Geo &g, const Phys &ph, const double *u3, const double *v3, const double *w3,
+                           const double *p, const double *u_inlet, double *u_out, double *v_out, double *w_out,
+                           cudaStream_t st) {
+  return project(g, ph, u3, v3, w3, p, u_inlet, u_out, v_out, w_out, st);
 }
-__device__ __forceinline__ double rec_apply(const Rec &q, double xp, double xm, double yp, double ym,
-                                            double zp, double zm) {
-  double v = fma(q.x.x, xp, q.b.x);
-  v = fma(q.x.y, xm, v);
-  v = fma(q.y.x, yp, v);
-  v = fma(q.y.y, ym, v);
-  v = fma(q.z.x, zp, v);
-  return fma(q.z.y, zm, v);
-}
-
-__global__ void __launch_bounds__(MB_X *MB_Y)
-    k_jacobi_c(int comp, Geo g, Helm h, const double *__restrict__ xo,
-               const double *__restrict__ coef, const double *__restrict__ P,
-               double *__restrict__ x, int fuse) {
-  const int i = blockIdx.x * MB_X + threadIdx.x + 1, j = blockIdx.y * MB_Y + threadIdx.y + 1;
-  const int k = blockIdx.z + (comp == 2 ? 1 : 0);
-  const int iend = (comp == 0) ? g.nx - 1 : g.nx;
-  if (i > iend || j > g.ny) return;
-  const int c = TPLS_IDX(g, i, j, k), sy = g.sy, sz = g.sz;
-  const Rec q = load_rec(coef, c);
-  const double xc = xo[c];
-  double zp, zm;
-  if (comp == 2) {
-    zp = xo[c + sz];
-    zm = xo[c - sz];
-  } else {  // walls folded into the record: the z slot multiplies the point itself
-    zp = (k == g.nz - 1) ? xc : xo[c + sz];
-    zm = (k == 0) ? xc : xo[c - sz];
-  }
-  const double v = rec_apply(q, xo[c + 1], xo[c - 1], xo[c + sy], xo[c - sy], zp, zm);
-  put(g, x, i, j, k, v, fuse);
-  if (comp == 0) {
-    if (i == 1) put(g, x, 0, j, k, v, fuse);
-    if (i == g.nx - 1) {
-      put(g, x, g.nx, j, k, u_outlet(g, h, P, v, j, k), fuse);
-      put(g, x, g.nx + 1, j, k, 0.0, fuse);
-    }
-  } else if (comp == 1) {
-    if (i == 1) put(g, x, 0, j, k, v, fuse);
-    if (i == g.nx) put(g, x, g.nx + 1, j, k, v, fuse);
-  } else {
-    const int nz = g.nz;
-    if (k == 1) put(g, x, i, j, 0, 0.0, fuse);
-    if (k == nz - 1) put(g, x, i, j, nz, 0.0, fuse);
-    if (i == 1) {
-      put(g, x, 0, j, k, v, fuse);
-      if (k == 1) put(g, x, 0, j, 0, 0.0, fuse);
-      if (k == nz - 1) put(g, x, 0, j, nz, 0.0, fuse);
-    }
-    if (i == g.nx) {
-      put(g, x, g.nx + 1, j, k, v, fuse);
-      if (k == 1) put(g, x, g.nx + 1, j, 0, 0.0, fuse);
-      if (k == nz - 1) put(g, x, g.nx + 1, j, nz, 0.0, fuse);
-    }
-  }
-}
-
-__global__ void __launch_bounds__(MB_X *MB_Y)
-    k_sor_even_c(int comp, Geo g, Helm h, double *__restrict__ x, const double *__restrict__ coef,
-                 const double *__restrict__ P, int flg, int bc, int fuse) {
-  const int i2 = blockIdx.x * MB_X + threadIdx.x, j = blockIdx.y * MB_Y + threadIdx.y + 1;
-  const int k = blockIdx.z + (comp == 2 ? 1 : 0);
-  const int iend = (comp == 0) ? g.nx - 1 : g.nx;
-  if (i2 > (iend - 1) / 2 || j > g.ny) return;
-  const int i = 2 * i2 + 1 + ((k + j + flg) & 1);
-  double v = 0.0;
-  if (i <= iend) {
-    const int c = TPLS_IDX(g, i, j, k), sy = g.sy, sz = g.sz;
-    const Rec q = load_rec(coef, c);
-    const double xc = x[c];
-    double zp, zm;
-    if (comp == 2) {
-      zp = x[c + sz];
-      zm = x[c - sz];
-    } else {
-      zp = (k == g.nz - 1) ? xc : x[c + sz];
-      zm = (k == 0) ? xc : x[c - sz];
-    }
-    const double res = rec_apply(q, x[c + 1], x[c - 1], x[c + sy], x[c - sy], zp, zm);
-    v = xc + 1.2 * (res - xc);
-    put(g, x, i, j, k, v, fuse);
-  }
-  if (bc) sor_bc(comp, g, h, x, P, i2, i, iend, v, j, k, fuse);
-}
-
-__global__ void __launch_bounds__(64)
-    k_sor_odd_c(int comp, Geo g, Helm h, double *__restrict__ x, const double *__restrict__ coef,
-                const double *__restrict__ P, int flg, int bc, int fuse) {
-  const int i2 = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 2 + threadIdx.y + 1;
-  const int iend = (comp == 0) ? g.nx - 1 : g.nx;
-  if (i2 > (iend - 1) / 2 || j > g.ny) return;
-  const int i = 2 * i2 + 1 + ((j + flg) & 1);
-  const bool act = (i <= iend);
-  const int sy = g.sy, sz = g.sz, nz = g.nz;
-  const int k0 = (comp == 2) ? 1 : 0, k1 = nz - 1;
-  double prev = 0.0;  // relaxed value at k-1 in this column
-  for (int k = k0; k <= k1; k++) {
-    double v = 0.0;
-    if (act) {
-      const int c = TPLS_IDX(g, i, j, k);
-      const Rec q = load_rec(coef, c);
-      const double xc = x[c];
-      double zp, zm;
-      if (comp == 2) {
-        zm = (k == k0) ? x[c - sz] : prev;
-        zp = x[c + sz];
-      } else {  // k = nz-1: the czm slot (folded) multiplies the relaxed point below
-        zm = (k == 0) ? xc : prev;
-        zp = (k == nz - 1) ? xc : x[c + sz];
-      }
-      const double res = rec_apply(q, x[c + 1], x[c - 1], x[c + sy], x[c - sy], zp, zm);
-      v = xc + 1.2 * (res - xc);
-      put(g, x, i, j, k, v, fuse);
-      prev = v;
-    }
-    if (bc) sor_bc(comp, g, h, x, P, i2, i, iend, v, j, k, fuse);
-  }
-}
-
-// Odd-iteration half-sweep in two phases.  Within such a half-sweep every
-// value a point reads is the pre-sweep value except the relaxed point below
-// it in its own column, so the update is the recurrence
-//   x_new(k) = A(k) + B(k) x_new(k-1),
-//   A = x + 1.2 (partial - x),  B = 1.2 czm   (partial = all terms but czm),
-// with A and B known before the sweep.  A block owns 32 columns of one row
-// (one per x pair); for each chunk of SO_KZ levels all its threads compute
-// A, B into shared memory in parallel, then one warp runs the recurrence.
-constexpr int SO_KZ = 32, SO_T = 256;
-
-__global__ void __launch_bounds__(SO_T)
-    k_sor_odd_c2(int comp, Geo g, Helm h, double *__restrict__ x, const double *__restrict__ coef,
-                 const double *__restrict__ P, int flg, int bc, int fuse) {
-  __shared__ double sA[SO_KZ][32], sB[SO_KZ][32];
-  const int j = blockIdx.y + 1;
-  const int iend = (comp == 0) ? g.nx - 1 : g.nx;
-  const int npair = (iend + 1) / 2;
-  const int par = (j + flg) & 1;
-  const int sy = g.sy, sz = g.sz, nz = g.nz;
-  const int k0 = (comp == 2) ? 1 : 0, k1 = nz - 1;
-  double prev = 0.0;  // owned by the recurrence warp
-  for (int kc = k0; kc <= k1; kc += SO_KZ) {
-    const int kn = min(SO_KZ, k1 - kc + 1);
-    for (int t = threadIdx.x; t < kn * 32; t += SO_T) {
-      const int lk = t >> 5, col = t & 31;
-      const int i2 = blockIdx.x * 32 + col, i = 2 * i2 + 1 + par, k = kc + lk;
-      double A = 0.0, B = 0.0;
-      if (i2 < npair && i <= iend) {
-        const int c = TPLS_IDX(g, i, j, k);
-        const Rec q = load_rec(coef, c);
-        const double xc = x[c];
-        double zp;
-        if (comp == 2) zp = x[c + sz];
-        else zp = (k == nz - 1) ? xc : x[c + sz];
-        double part = fma(q.x.x, x[c + 1], q.b.x);
-        part = fma(q.x.y, x[c - 1], part);
-        part = fma(q.y.x, x[c + sy], part);
-        part = fma(q.y.y, x[c - sy], part);
-        part = fma(q.z.x, zp, part);
-        if (k == k0) {  // the point below is a wall value (w) or the point itself (u, v)
-          const double zm = (comp == 2) ? x[c - sz] : xc;
-          A = xc + 1.2 * (fma(q.z.y, zm, part) - xc);
-        } else {
-          A = xc + 1.2 * (part - xc);
-          B = 1.2 * q.z.y;
-        }
-      }
-      sA[lk][col] = A;
-      sB[lk][col] = B;
-    }
-    __syncthreads();
-    if (threadIdx.x < 32) {
-      const int col = threadIdx.x;
-      const int i2 = blockIdx.x * 32 + col, i = 2 * i2 + 1 + par;
-      if (i2 < npair) {
-        for (int lk = 0; lk < kn; lk++) {
-          const int k = kc + lk;
-          double v = 0.0;
-          if (i <= iend) {
-            v = fma(sB[lk][col], prev, sA[lk][col]);
-            put(g, x, i, j, k, v, fuse);
-            prev = v;
-          }
-          if (bc) sor_bc(comp, g, h, x, P, i2, i, iend, v, j, k, fuse);
-        }
-      }
-    }
-    __syncthreads();
-  }
-}
-
-static Helm helm_of(const Phys &ph) {
-  Helm h;
-  h.ax2 = (ph.dt / (ph.dx * ph.dx)) / 2.0;
-  h.ay2 = (ph.dt / (ph.dy * ph.dy)) / 2.0;
-  h.az2 = (ph.dt / (ph.dz * ph.dz)) / 2.0;
-  h.dtdx = ph.dt / ph.dx;
-  return h;
-}
-
-cudaError_t launch_jacobi_c(int comp, const Geo &g, const Phys &ph, const double *xo,
-                            const double *coef, const double *pres, double *x, int fuse_ghosts,
-                            cudaStream_t st) {
-  const int nk = (comp == 2) ? g.nz - 1 : g.nz;
-  const int iend = (comp == 0) ? g.nx - 1 : g.nx;
-  dim3 grd((iend + MB_X - 1) / MB_X, (g.ny + MB_Y - 1) / MB_Y, nk);
-  k_jacobi_c<<<grd, dim3(MB_X, MB_Y), 0, st>>>(comp, g, helm_of(ph), xo, coef, pres, x, fuse_ghosts);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_sor_c(int comp, const Geo &g, const Phys &ph, double *x, const double *coef,
-                         const double *pres, int flg, int iteration_time, int bc, int fuse_ghosts,
-                         cudaStream_t st) {
-  const int iend = (comp == 0) ? g.nx - 1 : g.nx;
-  const int npairs = (iend + 1) / 2;
-  if (iteration_time % 2 == 0) {
-    const int nk = (comp == 2) ? g.nz - 1 : g.nz;
-    dim3 grd((npairs + MB_X - 1) / MB_X, (g.ny + MB_Y - 1) / MB_Y, nk);
-    k_sor_even_c<<<grd, dim3(MB_X, MB_Y), 0, st>>>(comp, g, helm_of(ph), x, coef, pres, flg, bc,
-                                                   fuse_ghosts);
-  } else {
-    dim3 grd((npairs + 31) / 32, g.ny, 1);
-    k_sor_odd_c2<<<grd, SO_T, 0, st>>>(comp, g, helm_of(ph), x, coef, pres, flg, bc, fuse_ghosts);
-  }
-  return cudaGetLastError();
+cudaError_t launch_project(const Geo &g, const Phys &ph, const float *u3, const float *v3, const float *w3,
+                           const double *p, const double *u_inlet, double *u_out, double *v_out, double *w_out,
+                           cudaStream_t st) {
+  return project(g, ph, u3, v3, w3, p, u_inlet, u_out, v_out, w_out, st);
 }
 
 cudaError_t launch_bc(int comp, const Geo &g, const Phys &ph, double *x,

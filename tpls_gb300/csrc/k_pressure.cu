@@ -38,12 +38,15 @@ namespace tpls {
 
 constexpr int PB = 256;  // threads per block for 1-D pressure kernels
 
+// Level vectors are stored in the level type of the solver (double, or
+// float for the FP32 preconditioner of the FP32-mixed form); void pointers
+// here, typed at each launch.
 struct PLevel {
   int nx, ny, nz, n;
   int cxs, cys, czs;     // this level was coarsened in x/y/z from the finer one
   double cx, cy, cz;
-  double *b = nullptr, *e = nullptr, *e2 = nullptr, *r = nullptr, *t = nullptr;
-  double *thomas = nullptr;  // [3 classes][nz][2] = (cprime, inv_den)
+  void *b = nullptr, *e = nullptr, *e2 = nullptr, *r = nullptr, *t = nullptr;
+  void *thomas = nullptr;  // [3 classes][nz][2] = (cprime, inv_den)
 };
 
 struct PoissonSolver {
@@ -59,10 +62,43 @@ struct PoissonSolver {
   double *s_host = nullptr;  // pinned mirror
   int rblk;                  // blocks of the grid-stride reduction kernels
   double omega = 0.8;
+  int fp32 = 0;              // multigrid levels in FP32 (CG stays FP64)
+  cudaStream_t side = nullptr;  // capture stream of the WHILE body
 };
 
 // device scalars of the CG iteration
-enum { S_SUMB = 0, S_SUMX0, S_BB, S_RR, S_RZ, S_ZMEAN, S_BETA, S_ALPHA, S_SUMX, S_COUNT };
+// S_IT: iterations of the current solve; S_REASON: its KSP-style reason (0
+// while iterating); S_WORST: lowest reason since the last stats read;
+// S_ITS_TOTAL: iterations since the solver was created.
+enum {
+  S_SUMB = 0, S_SUMX0, S_BB, S_RR, S_RZ, S_ZMEAN, S_BETA, S_ALPHA, S_SUMX,
+  S_TARGET, S_IT, S_REASON, S_WORST, S_ITS_TOTAL, S_COUNT
+};
+
+// Convergence test of pressure_solver.F90's KSP settings on the device, by
+// the last block of a reduction: NaN, ||r|| <= rtol ||b||, or maxits.  With a
+// graph, the WHILE node's condition is set here, so a captured solve needs
+// no host round trip.
+struct CgCtl {
+  int maxits;
+  int use_cond;
+  cudaGraphConditionalHandle cond;
+};
+
+__device__ __forceinline__ void cg_decide(double *s, double rr2, int it, const CgCtl &ctl, bool init) {
+  const double rr = sqrt(rr2);
+  int rsn = 0;
+  if (!(rr == rr)) rsn = TPLS_KSP_DIVERGED_NAN;
+  else if (rr <= s[S_TARGET] || (init && s[S_BB] == 0.0)) rsn = TPLS_KSP_CONVERGED_RTOL;
+  else if (!init && it >= ctl.maxits) rsn = TPLS_KSP_DIVERGED_ITS;
+  s[S_IT] = (double)it;
+  s[S_REASON] = (double)rsn;
+  if (rsn != 0) {
+    if ((double)rsn < s[S_WORST]) s[S_WORST] = (double)rsn;
+    s[S_ITS_TOTAL] += (double)it;
+  }
+  if (ctl.use_cond) cudaGraphSetConditional(ctl.cond, rsn == 0 ? 1u : 0u);
+}
 
 static inline int nblocks(int n) { return (n + PB - 1) / PB; }
 
@@ -114,24 +150,27 @@ __device__ __forceinline__ bool reduce_last(double (&v)[NQ], double *part, unsig
   return true;
 }
 
-__device__ __forceinline__ double applyA(const double *__restrict__ e, int i, int j, int k, int nx,
-                                         int ny, int nz, double cx, double cy, double cz) {
+template <typename R, typename TE>
+__device__ __forceinline__ R applyA(const TE *__restrict__ e, int i, int j, int k, int nx, int ny, int nz,
+                                    R cx, R cy, R cz) {
   const int c = i + nx * (j + ny * k);
-  const double v = e[c];
-  const double xm = (i > 0) ? e[c - 1] : v, xp = (i < nx - 1) ? e[c + 1] : v;
-  const double ym = e[c + nx * ((j > 0) ? -1 : ny - 1)];
-  const double yp = e[c + nx * ((j < ny - 1) ? 1 : 1 - ny)];
-  const double zm = (k > 0) ? e[c - nx * ny] : v, zp = (k < nz - 1) ? e[c + nx * ny] : v;
-  return cx * (2.0 * v - xm - xp) + cy * (2.0 * v - ym - yp) + cz * (2.0 * v - zm - zp);
+  const R v = (R)e[c];
+  const R xm = (i > 0) ? (R)e[c - 1] : v, xp = (i < nx - 1) ? (R)e[c + 1] : v;
+  const R ym = (R)e[c + nx * ((j > 0) ? -1 : ny - 1)];
+  const R yp = (R)e[c + nx * ((j < ny - 1) ? 1 : 1 - ny)];
+  const R zm = (k > 0) ? (R)e[c - nx * ny] : v, zp = (k < nz - 1) ? (R)e[c + nx * ny] : v;
+  const R two = (R)2;
+  return cx * (two * v - xm - xp) + cy * (two * v - ym - yp) + cz * (two * v - zm - zp);
 }
 
 #define GRID_STRIDE(c, N) for (int c = blockIdx.x * PB + threadIdx.x; c < (N); c += gridDim.x * PB)
 
 // b (compact interior) = -RHS_p + inlet contribution; x0 = p_old interior;
 // sums of b and x0.
+template <typename TU>
 __global__ void __launch_bounds__(PB)
     k_build_b(Geo g, double dxdt_over_dy, double rdy, const double *__restrict__ rhs_p,
-              const double *__restrict__ u3, const double *__restrict__ uin,
+              const TU *__restrict__ u3, const double *__restrict__ uin,
               const double *__restrict__ pold, double *__restrict__ b, double *__restrict__ x0,
               double *__restrict__ bin, double *part, unsigned *counter, double *s) {
   const int nx = g.nx, ny = g.ny, nz = g.nz, N = nx * ny * nz;
@@ -143,7 +182,7 @@ __global__ void __launch_bounds__(PB)
     if (i == 0) {
       // pressure_solver.F90:280-286: b(i,0,k) = (dx/dt)(u_inlet(k-1)-u3(0,i,k-1))/dy
       const int ju = (j == 0) ? ny : j;  // u row (j+1)-1; row 0 is the copy of row ny
-      const double bi = dxdt_over_dy * (uin[k] - u3[TPLS_IDX(g, 0, ju, k)]);
+      const double bi = dxdt_over_dy * (uin[k] - (double)u3[TPLS_IDX(g, 0, ju, k)]);
       bin[j + ny * k] = bi;
       bb += bi * rdy;
     }
@@ -162,8 +201,8 @@ __global__ void __launch_bounds__(PB)
 
 // b -= mean(b); r = b - A x; ||b||^2, ||r||^2
 __global__ void __launch_bounds__(PB)
-    k_init_r(int nx, int ny, int nz, double cx, double cy, double cz, double invN, double *s,
-             double *__restrict__ b, const double *__restrict__ x, double *__restrict__ r, double *part,
+    k_init_r(int nx, int ny, int nz, double cx, double cy, double cz, double invN, double rtol, CgCtl ctl,
+             double *s, double *__restrict__ b, const double *__restrict__ x, double *__restrict__ r, double *part,
              unsigned *counter) {
   const int N = nx * ny * nz;
   const double mb = s[S_SUMB] * invN;
@@ -172,7 +211,7 @@ __global__ void __launch_bounds__(PB)
     const int i = c % nx, j = (c / nx) % ny, k = c / (nx * ny);
     const double bb = b[c] - mb;
     b[c] = bb;
-    const double rr = bb - applyA(x, i, j, k, nx, ny, nz, cx, cy, cz);
+    const double rr = bb - applyA<double, double>(x, i, j, k, nx, ny, nz, cx, cy, cz);
     r[c] = rr;
     v[0] += bb * bb;
     v[1] += rr * rr;
@@ -181,13 +220,15 @@ __global__ void __launch_bounds__(PB)
   if (reduce_last<2>(v, part, counter, tot) && threadIdx.x == 0) {
     s[S_BB] = tot[0];
     s[S_RR] = tot[1];
+    s[S_TARGET] = rtol * sqrt(tot[0]);
+    cg_decide(s, tot[1], 0, ctl, true);
   }
 }
 
 // sum z, sum r, r.z -> mean(z), rz_new = r.(z - mean z), beta = rz_new/rz
 __global__ void __launch_bounds__(PB)
-    k_zdot(int N, double invN, int first, const double *__restrict__ r, const double *__restrict__ z,
-           double *part, unsigned *counter, double *s) {
+    k_zdot(int N, double invN, const double *__restrict__ r, const double *__restrict__ z, double *part,
+           unsigned *counter, double *s) {
   double v[3] = {0.0, 0.0, 0.0};
   GRID_STRIDE(c, N) {
     const double zz = z[c], rr = r[c];
@@ -199,7 +240,7 @@ __global__ void __launch_bounds__(PB)
   if (reduce_last<3>(v, part, counter, tot) && threadIdx.x == 0) {
     const double zm = tot[0] * invN;
     const double rzn = tot[2] - zm * tot[1];
-    s[S_BETA] = first ? 0.0 : rzn / s[S_RZ];
+    s[S_BETA] = (s[S_IT] == 0.0) ? 0.0 : rzn / s[S_RZ];
     s[S_ZMEAN] = zm;
     s[S_RZ] = rzn;
   }
@@ -221,7 +262,7 @@ __global__ void __launch_bounds__(PB)
   double v[1] = {0.0};
   GRID_STRIDE(c, N) {
     const int i = c % nx, j = (c / nx) % ny, k = c / (nx * ny);
-    const double a = applyA(p, i, j, k, nx, ny, nz, cx, cy, cz);
+    const double a = applyA<double, double>(p, i, j, k, nx, ny, nz, cx, cy, cz);
     q[c] = a;
     v[0] += p[c] * a;
   }
@@ -231,7 +272,7 @@ __global__ void __launch_bounds__(PB)
 
 // x += alpha p; r -= alpha q; ||r||^2
 __global__ void __launch_bounds__(PB)
-    k_axpy(int N, double *s, const double *__restrict__ p, const double *__restrict__ q,
+    k_axpy(int N, CgCtl ctl, double *s, const double *__restrict__ p, const double *__restrict__ q,
            double *__restrict__ x, double *__restrict__ r, double *part, unsigned *counter) {
   const double alpha = s[S_ALPHA];
   double v[1] = {0.0};
@@ -242,7 +283,10 @@ __global__ void __launch_bounds__(PB)
     v[0] += rr * rr;
   }
   double tot[1];
-  if (reduce_last<1>(v, part, counter, tot) && threadIdx.x == 0) s[S_RR] = tot[0];
+  if (reduce_last<1>(v, part, counter, tot) && threadIdx.x == 0) {
+    s[S_RR] = tot[0];
+    cg_decide(s, tot[0], (int)s[S_IT] + 1, ctl, false);
+  }
 }
 
 __global__ void __launch_bounds__(PB)
@@ -275,74 +319,80 @@ __global__ void k_writeback(Geo g, double dy, double invN, const double *__restr
 }
 
 // ---------------------------------------------------------------------------
-// multigrid kernels
+// multigrid kernels.  R is the arithmetic type of the level (double, or
+// float for the FP32 preconditioner); TB, TE, TO the storage types of the
+// right-hand side, the input iterate and the output (the finest level of
+// the FP32 preconditioner reads the FP64 CG residual and writes the FP64
+// preconditioned vector directly).
+template <typename R>
 struct LevArgs {
   int nx, ny, nz;
-  double cx, cy, cz;
+  R cx, cy, cz;
 };
 
 // one damped z-line Jacobi sweep: eo = (1-w) ei + w Dline^{-1}(b - N ei);
 // zero_init: ei == 0.
 constexpr int LJB = 64;  // threads per block of the line smoother (one column each)
 
+template <typename R, typename TB, typename TE, typename TO>
 __global__ void __launch_bounds__(LJB)
-    k_line_jacobi(LevArgs L, double omega, double one_m_omega, int zero_init,
-                  const double *__restrict__ thomas, const double *__restrict__ b,
-                  const double *__restrict__ ei, double *__restrict__ t, double *__restrict__ eo) {
+    k_line_jacobi(LevArgs<R> L, R omega, R one_m_omega, int zero_init, const R *__restrict__ thomas,
+                  const TB *__restrict__ b, const TE *__restrict__ ei, R *__restrict__ t, TO *__restrict__ eo) {
   const int col = blockIdx.x * LJB + threadIdx.x;
   const int nx = L.nx, ny = L.ny, nz = L.nz;
   if (col >= nx * ny) return;
   const int i = col % nx, j = col / nx;
   const int cls = (nx == 1) ? 1 : ((i == 0) ? 0 : ((i == nx - 1) ? 2 : 1));
-  const double *th = thomas + (size_t)cls * nz * 2;
+  const R *th = thomas + (size_t)cls * nz * 2;
   const int plane = nx * ny;
   const int jm = (j > 0) ? -nx : nx * (ny - 1), jp = (j < ny - 1) ? nx : -nx * (ny - 1);
-  double y = 0.0;
+  R y = (R)0;
   for (int k = 0; k < nz; k++) {
     const int c = col + plane * k;
-    double rhs = b[c];
+    R rhs = (R)b[c];
     if (!zero_init) {
-      double nb = L.cy * (ei[c + jm] + ei[c + jp]);
-      if (i > 0) nb += L.cx * ei[c - 1];
-      if (i < nx - 1) nb += L.cx * ei[c + 1];
+      R nb = L.cy * ((R)ei[c + jm] + (R)ei[c + jp]);
+      if (i > 0) nb += L.cx * (R)ei[c - 1];
+      if (i < nx - 1) nb += L.cx * (R)ei[c + 1];
       rhs += nb;
     }
     y = (rhs + L.cz * y) * th[2 * k + 1];
     t[c] = y;
   }
-  double xn = 0.0;
+  R xn = (R)0;
   for (int k = nz - 1; k >= 0; k--) {
     const int c = col + plane * k;
-    xn = t[c] - ((k < nz - 1) ? th[2 * k] * xn : 0.0);
-    eo[c] = zero_init ? omega * xn : one_m_omega * ei[c] + omega * xn;
+    xn = t[c] - ((k < nz - 1) ? th[2 * k] * xn : (R)0);
+    eo[c] = (TO)(zero_init ? omega * xn : one_m_omega * (R)ei[c] + omega * xn);
   }
 }
 
 // The same sweep for 32 columns per block in three phases: all threads
 // assemble the line right-hand sides into shared memory, one warp runs the
 // Thomas forward/backward substitution in shared memory, all threads write
-// the damped result.  Dynamic shared memory: nz * 32 doubles.
+// the damped result.  Dynamic shared memory: nz * 32 values of R.
 constexpr int LJ2_T = 256;
 
+template <typename R, typename TB, typename TE, typename TO>
 __global__ void __launch_bounds__(LJ2_T)
-    k_line_jacobi2(LevArgs L, double omega, double one_m_omega, int zero_init,
-                   const double *__restrict__ thomas, const double *__restrict__ b,
-                   const double *__restrict__ ei, double *__restrict__ eo) {
-  extern __shared__ double buf[];  // [nz][32]
+    k_line_jacobi2(LevArgs<R> L, R omega, R one_m_omega, int zero_init, const R *__restrict__ thomas,
+                   const TB *__restrict__ b, const TE *__restrict__ ei, TO *__restrict__ eo) {
+  extern __shared__ __align__(16) unsigned char lj2_raw[];
+  R *buf = reinterpret_cast<R *>(lj2_raw);  // [nz][32]
   const int nx = L.nx, ny = L.ny, nz = L.nz, ncol = nx * ny, plane = nx * ny;
   const int col0 = blockIdx.x * 32;
   for (int t = threadIdx.x; t < nz * 32; t += LJ2_T) {
     const int k = t >> 5, cl = t & 31, col = col0 + cl;
-    double rhs = 0.0;
+    R rhs = (R)0;
     if (col < ncol) {
       const int c = col + plane * k;
-      rhs = b[c];
+      rhs = (R)b[c];
       if (!zero_init) {
         const int i = col % nx, j = col / nx;
         const int jm = (j > 0) ? -nx : nx * (ny - 1), jp = (j < ny - 1) ? nx : -nx * (ny - 1);
-        double nb = L.cy * (ei[c + jm] + ei[c + jp]);
-        if (i > 0) nb += L.cx * ei[c - 1];
-        if (i < nx - 1) nb += L.cx * ei[c + 1];
+        R nb = L.cy * ((R)ei[c + jm] + (R)ei[c + jp]);
+        if (i > 0) nb += L.cx * (R)ei[c - 1];
+        if (i < nx - 1) nb += L.cx * (R)ei[c + 1];
         rhs += nb;
       }
     }
@@ -354,13 +404,13 @@ __global__ void __launch_bounds__(LJ2_T)
     if (col < ncol) {
       const int i = col % nx;
       const int cls = (nx == 1) ? 1 : ((i == 0) ? 0 : ((i == nx - 1) ? 2 : 1));
-      const double *th = thomas + (size_t)cls * nz * 2;
-      double y = 0.0;
+      const R *th = thomas + (size_t)cls * nz * 2;
+      R y = (R)0;
       for (int k = 0; k < nz; k++) {
         y = (buf[k * 32 + threadIdx.x] + L.cz * y) * th[2 * k + 1];
         buf[k * 32 + threadIdx.x] = y;
       }
-      double xn = y;
+      R xn = y;
       for (int k = nz - 2; k >= 0; k--) {
         xn = buf[k * 32 + threadIdx.x] - th[2 * k] * xn;
         buf[k * 32 + threadIdx.x] = xn;
@@ -372,57 +422,58 @@ __global__ void __launch_bounds__(LJ2_T)
     const int k = t >> 5, col = col0 + (t & 31);
     if (col < ncol) {
       const int c = col + plane * k;
-      eo[c] = zero_init ? omega * buf[t] : one_m_omega * ei[c] + omega * buf[t];
+      eo[c] = (TO)(zero_init ? omega * buf[t] : one_m_omega * (R)ei[c] + omega * buf[t]);
     }
   }
 }
 
-__global__ void k_residual(LevArgs L, const double *__restrict__ b, const double *__restrict__ e,
-                           double *__restrict__ r) {
+template <typename R, typename TB, typename TE>
+__global__ void k_residual(LevArgs<R> L, const TB *__restrict__ b, const TE *__restrict__ e, R *__restrict__ r) {
   const int c = blockIdx.x * PB + threadIdx.x;
   const int nx = L.nx, ny = L.ny, nz = L.nz;
   if (c >= nx * ny * nz) return;
   const int i = c % nx, j = (c / nx) % ny, k = c / (nx * ny);
-  r[c] = b[c] - applyA(e, i, j, k, nx, ny, nz, L.cx, L.cy, L.cz);
+  r[c] = (R)b[c] - applyA<R, TE>(e, i, j, k, nx, ny, nz, L.cx, L.cy, L.cz);
 }
 
 // 1-D restriction stencil: fine indices and weights contributing to coarse c
-__device__ __forceinline__ int rstencil(int c, int nc, int coarsened, int periodic, int *f,
-                                        double *w) {
+template <typename R>
+__device__ __forceinline__ int rstencil(int c, int nc, int coarsened, int periodic, int *f, R *w) {
   if (!coarsened) {
     f[0] = c;
-    w[0] = 1.0;
+    w[0] = (R)1;
     return 1;
   }
   const int nf = 2 * nc;
   int m = 0;
   f[m] = 2 * c;
-  w[m++] = (!periodic && c == 0) ? 1.0 : 0.75;
+  w[m++] = (!periodic && c == 0) ? (R)1 : (R)0.75;
   f[m] = 2 * c + 1;
-  w[m++] = (!periodic && c == nc - 1) ? 1.0 : 0.75;
-  if (c > 0) { f[m] = 2 * c - 1; w[m++] = 0.25; }
-  else if (periodic) { f[m] = nf - 1; w[m++] = 0.25; }
-  if (c < nc - 1) { f[m] = 2 * c + 2; w[m++] = 0.25; }
-  else if (periodic) { f[m] = 0; w[m++] = 0.25; }
+  w[m++] = (!periodic && c == nc - 1) ? (R)1 : (R)0.75;
+  if (c > 0) { f[m] = 2 * c - 1; w[m++] = (R)0.25; }
+  else if (periodic) { f[m] = nf - 1; w[m++] = (R)0.25; }
+  if (c < nc - 1) { f[m] = 2 * c + 2; w[m++] = (R)0.25; }
+  else if (periodic) { f[m] = 0; w[m++] = (R)0.25; }
   return m;
 }
 
-__global__ void k_restrict(LevArgs F, LevArgs C, int cxs, int cys, int czs, double scale,
-                           const double *__restrict__ rf, double *__restrict__ bc) {
+template <typename R>
+__global__ void k_restrict(LevArgs<R> F, LevArgs<R> C, int cxs, int cys, int czs, R scale,
+                           const R *__restrict__ rf, R *__restrict__ bc) {
   const int c = blockIdx.x * PB + threadIdx.x;
   if (c >= C.nx * C.ny * C.nz) return;
   const int I = c % C.nx, J = (c / C.nx) % C.ny, K = c / (C.nx * C.ny);
   int fx[4], fy[4], fz[4];
-  double wx[4], wy[4], wz[4];
-  const int mx = rstencil(I, C.nx, cxs, 0, fx, wx);
-  const int my = rstencil(J, C.ny, cys, 1, fy, wy);
-  const int mz = rstencil(K, C.nz, czs, 0, fz, wz);
-  double acc = 0.0;
+  R wx[4], wy[4], wz[4];
+  const int mx = rstencil<R>(I, C.nx, cxs, 0, fx, wx);
+  const int my = rstencil<R>(J, C.ny, cys, 1, fy, wy);
+  const int mz = rstencil<R>(K, C.nz, czs, 0, fz, wz);
+  R acc = (R)0;
   for (int a = 0; a < mz; a++)
     for (int bq = 0; bq < my; bq++) {
-      const double wzy = wz[a] * wy[bq];
-      const double *row = rf + F.nx * (fy[bq] + F.ny * fz[a]);
-      double sx = 0.0;
+      const R wzy = wz[a] * wy[bq];
+      const R *row = rf + F.nx * (fy[bq] + F.ny * fz[a]);
+      R sx = (R)0;
       for (int q = 0; q < mx; q++) sx += wx[q] * row[fx[q]];
       acc += wzy * sx;
     }
@@ -430,11 +481,11 @@ __global__ void k_restrict(LevArgs F, LevArgs C, int cxs, int cys, int czs, doub
 }
 
 // 1-D prolongation: coarse indices and weights for fine f
-__device__ __forceinline__ int pstencil(int f, int nc, int coarsened, int periodic, int *c,
-                                        double *w) {
+template <typename R>
+__device__ __forceinline__ int pstencil(int f, int nc, int coarsened, int periodic, int *c, R *w) {
   if (!coarsened) {
     c[0] = f;
-    w[0] = 1.0;
+    w[0] = (R)1;
     return 1;
   }
   const int c0 = f >> 1;
@@ -442,50 +493,52 @@ __device__ __forceinline__ int pstencil(int f, int nc, int coarsened, int period
   if (c1 < 0 || c1 >= nc) {
     if (!periodic) {
       c[0] = c0;
-      w[0] = 1.0;
+      w[0] = (R)1;
       return 1;
     }
     c1 = (c1 < 0) ? c1 + nc : c1 - nc;
   }
   c[0] = c0;
-  w[0] = 0.75;
+  w[0] = (R)0.75;
   c[1] = c1;
-  w[1] = 0.25;
+  w[1] = (R)0.25;
   return 2;
 }
 
-__global__ void k_prolong_add(LevArgs F, LevArgs C, int cxs, int cys, int czs,
-                              const double *__restrict__ ec, double *__restrict__ ef) {
+template <typename R>
+__global__ void k_prolong_add(LevArgs<R> F, LevArgs<R> C, int cxs, int cys, int czs, const R *__restrict__ ec,
+                              R *__restrict__ ef) {
   const int c = blockIdx.x * PB + threadIdx.x;
   if (c >= F.nx * F.ny * F.nz) return;
   const int i = c % F.nx, j = (c / F.nx) % F.ny, k = c / (F.nx * F.ny);
   int cx[2], cy[2], cz[2];
-  double wx[2], wy[2], wz[2];
-  const int mx = pstencil(i, C.nx, cxs, 0, cx, wx);
-  const int my = pstencil(j, C.ny, cys, 1, cy, wy);
-  const int mz = pstencil(k, C.nz, czs, 0, cz, wz);
-  double acc = 0.0;
+  R wx[2], wy[2], wz[2];
+  const int mx = pstencil<R>(i, C.nx, cxs, 0, cx, wx);
+  const int my = pstencil<R>(j, C.ny, cys, 1, cy, wy);
+  const int mz = pstencil<R>(k, C.nz, czs, 0, cz, wz);
+  R acc = (R)0;
   for (int a = 0; a < mz; a++)
     for (int bq = 0; bq < my; bq++) {
-      const double *row = ec + C.nx * (cy[bq] + C.ny * cz[a]);
-      double sx = 0.0;
+      const R *row = ec + C.nx * (cy[bq] + C.ny * cz[a]);
+      R sx = (R)0;
       for (int q = 0; q < mx; q++) sx += wx[q] * row[cx[q]];
       acc += wz[a] * wy[bq] * sx;
     }
   ef[c] += acc;
 }
 
-// coarsest grid: e = Cinv b (one block)
-__global__ void k_coarse_solve(int n, const double *__restrict__ cinv, const double *__restrict__ b,
-                               double *__restrict__ e) {
+// coarsest grid: e = Cinv b (one block; the pseudo-inverse and the
+// products stay FP64 in both forms)
+template <typename T>
+__global__ void k_coarse_solve(int n, const double *__restrict__ cinv, const T *__restrict__ b, T *__restrict__ e) {
   __shared__ double sb[512];
-  for (int a = threadIdx.x; a < n; a += blockDim.x) sb[a] = b[a];
+  for (int a = threadIdx.x; a < n; a += blockDim.x) sb[a] = (double)b[a];
   __syncthreads();
   for (int a = threadIdx.x; a < n; a += blockDim.x) {
     const double *row = cinv + (size_t)a * n;
     double acc = 0.0;
     for (int q = 0; q < n; q++) acc += row[q] * sb[q];
-    e[a] = acc;
+    e[a] = (T)acc;
   }
 }
 
@@ -580,9 +633,16 @@ static std::vector<double> thomas_factors(const PLevel &L) {
     if (e_ != cudaSuccess) return e_; \
   } while (0)
 
-cudaError_t poisson_create(const Geo &g, double cx, double cy, double cz,
+template <typename R, typename TB, typename TE, typename TO>
+static cudaError_t lj2_attr() {
+  return cudaFuncSetAttribute(k_line_jacobi2<R, TB, TE, TO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              200 * 1024);
+}
+
+cudaError_t poisson_create(const Geo &g, double cx, double cy, double cz, int fp32,
                            PoissonSolver **out) {
   PoissonSolver *S = new PoissonSolver();
+  S->fp32 = fp32 ? 1 : 0;
   S->nx = g.nx;
   S->ny = g.ny;
   S->nz = g.nz;
@@ -614,19 +674,32 @@ cudaError_t poisson_create(const Geo &g, double cx, double cy, double cz,
     c.cz = c.czs ? f.cz / 4.0 : f.cz;
     S->lv.push_back(c);
   }
+  const size_t esz = S->fp32 ? sizeof(float) : sizeof(double);
   for (size_t l = 0; l < S->lv.size(); l++) {
     PLevel &L = S->lv[l];
-    const size_t bytes = sizeof(double) * (size_t)L.n;
+    const size_t bytes = esz * (size_t)L.n;
     if (l > 0) PCK(cudaMalloc(&L.b, bytes));
     PCK(cudaMalloc(&L.e, bytes));
     PCK(cudaMalloc(&L.e2, bytes));
     PCK(cudaMalloc(&L.r, bytes));
     PCK(cudaMalloc(&L.t, bytes));
     std::vector<double> th = thomas_factors(L);
-    PCK(cudaMalloc(&L.thomas, th.size() * sizeof(double)));
-    PCK(cudaMemcpy(L.thomas, th.data(), th.size() * sizeof(double), cudaMemcpyHostToDevice));
+    if (S->fp32) {
+      std::vector<float> thf(th.begin(), th.end());
+      PCK(cudaMalloc(&L.thomas, thf.size() * sizeof(float)));
+      PCK(cudaMemcpy(L.thomas, thf.data(), thf.size() * sizeof(float), cudaMemcpyHostToDevice));
+    } else {
+      PCK(cudaMalloc(&L.thomas, th.size() * sizeof(double)));
+      PCK(cudaMemcpy(L.thomas, th.data(), th.size() * sizeof(double), cudaMemcpyHostToDevice));
+    }
   }
-  PCK(cudaFuncSetAttribute(k_line_jacobi2, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+  if (S->fp32) {
+    PCK((lj2_attr<float, double, float, float>()));
+    PCK((lj2_attr<float, double, float, double>()));
+    PCK((lj2_attr<float, float, float, float>()));
+  } else {
+    PCK((lj2_attr<double, double, double, double>()));
+  }
   const PLevel &C = S->lv.back();
   if (C.n <= 512) {
     std::vector<double> M = coarse_pinv(C);
@@ -676,30 +749,35 @@ void poisson_destroy(PoissonSolver *S) {
   cudaFree(S->counter);
   cudaFree(S->s);
   cudaFreeHost(S->s_host);
+  if (S->side) cudaStreamDestroy(S->side);
   delete S;
 }
 
 int poisson_levels(const PoissonSolver *S) { return (int)S->lv.size(); }
 
-static LevArgs largs(const PLevel &L) {
-  LevArgs a;
+template <typename R>
+static LevArgs<R> largs(const PLevel &L) {
+  LevArgs<R> a;
   a.nx = L.nx;
   a.ny = L.ny;
   a.nz = L.nz;
-  a.cx = L.cx;
-  a.cy = L.cy;
-  a.cz = L.cz;
+  a.cx = (R)L.cx;
+  a.cy = (R)L.cy;
+  a.cz = (R)L.cz;
   return a;
 }
 
-static void line_sweep(const PLevel &L, const LevArgs &A, double w, double w1, int zero_init,
-                       const double *b, const double *ei, double *eo, cudaStream_t st) {
-  const size_t smem = sizeof(double) * 32 * (size_t)L.nz;
+template <typename R, typename TB, typename TE, typename TO>
+static void line_sweep(const PLevel &L, R w, R w1, int zero_init, const TB *b, const TE *ei, TO *eo,
+                       cudaStream_t st) {
+  const LevArgs<R> A = largs<R>(L);
+  const R *th = static_cast<const R *>(L.thomas);
+  const size_t smem = sizeof(R) * 32 * (size_t)L.nz;
   if (smem <= 200 * 1024) {
-    k_line_jacobi2<<<(L.nx * L.ny + 31) / 32, LJ2_T, smem, st>>>(A, w, w1, zero_init, L.thomas, b, ei, eo);
+    k_line_jacobi2<R, TB, TE, TO><<<(L.nx * L.ny + 31) / 32, LJ2_T, smem, st>>>(A, w, w1, zero_init, th, b, ei, eo);
   } else {
-    k_line_jacobi<<<(L.nx * L.ny + LJB - 1) / LJB, LJB, 0, st>>>(A, w, w1, zero_init, L.thomas, b, ei, L.t,
-                                                                 eo);
+    k_line_jacobi<R, TB, TE, TO><<<(L.nx * L.ny + LJB - 1) / LJB, LJB, 0, st>>>(A, w, w1, zero_init, th, b, ei,
+                                                                                static_cast<R *>(L.t), eo);
   }
 }
 
@@ -707,106 +785,202 @@ static void line_sweep(const PLevel &L, const LevArgs &A, double w, double w1, i
 // scratch e2 (one damped line-Jacobi sweep from zero), restricts the
 // residual, adds the prolonged coarse correction into e2 and post-smooths
 // from e2 into its result buffer (out on the finest level, e elsewhere).
+// R: level type; the finest level reads b0 and writes out in FP64.
+template <typename R>
 static cudaError_t vcycle(PoissonSolver *S, const double *b0, double *out, cudaStream_t st, long *nl) {
   const int nlev = (int)S->lv.size();
-  const double w = S->omega, w1 = 1.0 - S->omega;
+  const R w = (R)S->omega, w1 = (R)(1.0 - S->omega);
+  auto lvp = [](void *p) { return static_cast<R *>(p); };
+  if (nlev == 1) {
+    PLevel &L = S->lv[0];
+    if (S->cinv) {
+      k_coarse_solve<double><<<1, 256, 0, st>>>(L.n, S->cinv, b0, out);
+      (*nl)++;
+      return cudaGetLastError();
+    }
+    // single level without a dense inverse: damped line-Jacobi sweeps
+    R *cur = lvp(L.e2), *oth = lvp(L.e);
+    line_sweep<R, double, R, R>(L, w, w1, 1, b0, nullptr, cur, st);
+    (*nl)++;
+    for (int sw = 1; sw < S->coarse_sweeps - 1; sw++) {
+      line_sweep<R, double, R, R>(L, w, w1, 0, b0, cur, oth, st);
+      (*nl)++;
+      R *tmp = cur;
+      cur = oth;
+      oth = tmp;
+    }
+    line_sweep<R, double, R, double>(L, w, w1, 0, b0, cur, out, st);
+    (*nl)++;
+    return cudaGetLastError();
+  }
   for (int l = 0; l < nlev; l++) {
     PLevel &L = S->lv[l];
-    const double *b = (l == 0) ? b0 : L.b;
-    double *res = (l == 0) ? out : L.e;
-    const LevArgs A = largs(L);
+    const R *b = lvp(L.b);
+    R *res = lvp(L.e);
     if (l == nlev - 1) {
       if (S->cinv) {
-        k_coarse_solve<<<1, 256, 0, st>>>(L.n, S->cinv, b, res);
+        k_coarse_solve<R><<<1, 256, 0, st>>>(L.n, S->cinv, b, res);
         (*nl)++;
       } else {
-        double *cur = L.e2, *oth = res;
-        line_sweep(L, A, w, w1, 1, b, nullptr, cur, st);
+        R *cur = lvp(L.e2), *oth = res;
+        line_sweep<R, R, R, R>(L, w, w1, 1, b, nullptr, cur, st);
         (*nl)++;
         for (int sw = 1; sw < S->coarse_sweeps; sw++) {
-          line_sweep(L, A, w, w1, 0, b, cur, oth, st);
+          line_sweep<R, R, R, R>(L, w, w1, 0, b, cur, oth, st);
           (*nl)++;
-          double *tmp = cur;
+          R *tmp = cur;
           cur = oth;
           oth = tmp;
         }
-        if (cur != res) PCK(cudaMemcpyAsync(res, cur, sizeof(double) * L.n, cudaMemcpyDeviceToDevice, st));
+        if (cur != res) PCK(cudaMemcpyAsync(res, cur, sizeof(R) * L.n, cudaMemcpyDeviceToDevice, st));
       }
       PCK(cudaGetLastError());
       break;
     }
-    line_sweep(L, A, w, w1, 1, b, nullptr, L.e2, st);
-    k_residual<<<nblocks(L.n), PB, 0, st>>>(A, b, L.e2, L.r);
+    const LevArgs<R> A = largs<R>(L);
+    if (l == 0) {
+      line_sweep<R, double, R, R>(L, w, w1, 1, b0, nullptr, lvp(L.e2), st);
+      k_residual<R, double, R><<<nblocks(L.n), PB, 0, st>>>(A, b0, lvp(L.e2), lvp(L.r));
+    } else {
+      line_sweep<R, R, R, R>(L, w, w1, 1, b, nullptr, lvp(L.e2), st);
+      k_residual<R, R, R><<<nblocks(L.n), PB, 0, st>>>(A, b, lvp(L.e2), lvp(L.r));
+    }
     const PLevel &C = S->lv[l + 1];
-    const double scale = 1.0 / (double)((C.cxs ? 2 : 1) * (C.cys ? 2 : 1) * (C.czs ? 2 : 1));
-    k_restrict<<<nblocks(C.n), PB, 0, st>>>(A, largs(C), C.cxs, C.cys, C.czs, scale, L.r, C.b);
+    const R scale = (R)(1.0 / (double)((C.cxs ? 2 : 1) * (C.cys ? 2 : 1) * (C.czs ? 2 : 1)));
+    k_restrict<R><<<nblocks(C.n), PB, 0, st>>>(A, largs<R>(C), C.cxs, C.cys, C.czs, scale, lvp(L.r), lvp(C.b));
     *nl += 3;
     PCK(cudaGetLastError());
   }
   for (int l = nlev - 2; l >= 0; l--) {
     PLevel &L = S->lv[l];
     const PLevel &C = S->lv[l + 1];
-    const double *b = (l == 0) ? b0 : L.b;
-    double *res = (l == 0) ? out : L.e;
-    const LevArgs A = largs(L);
-    k_prolong_add<<<nblocks(L.n), PB, 0, st>>>(A, largs(C), C.cxs, C.cys, C.czs, C.e, L.e2);
-    line_sweep(L, A, w, w1, 0, b, L.e2, res, st);
+    const LevArgs<R> A = largs<R>(L);
+    k_prolong_add<R><<<nblocks(L.n), PB, 0, st>>>(A, largs<R>(C), C.cxs, C.cys, C.czs, lvp(C.e), lvp(L.e2));
+    if (l == 0)
+      line_sweep<R, double, R, double>(L, w, w1, 0, b0, lvp(L.e2), out, st);
+    else
+      line_sweep<R, R, R, R>(L, w, w1, 0, lvp(L.b), lvp(L.e2), lvp(L.e), st);
     *nl += 2;
     PCK(cudaGetLastError());
   }
   return cudaSuccess;
 }
 
+// The solve in three parts: set-up (b, x0 = p_old, r0 and the first
+// convergence test), one PCG iteration (V-cycle, z.r, p update, A p, x and r
+// updates, convergence test), and the write-back of p with its ghosts.
+static cudaError_t solve_begin(PoissonSolver *S, const Geo &g, const Phys &ph, const double *rhs_p,
+                               const void *u3, int u3_fp32, const double *u_inlet, const double *pres_old,
+                               double rtol, const CgCtl &ctl, cudaStream_t st, long *nl) {
+  const int N = S->N, rb = S->rblk;
+  const PLevel &F = S->lv[0];
+  if (u3_fp32)
+    k_build_b<float><<<rb, PB, 0, st>>>(g, (ph.dx / ph.dt) / ph.dy, 1.0 / ph.dy, rhs_p,
+                                        static_cast<const float *>(u3), u_inlet, pres_old, S->bvec, S->x, S->bin,
+                                        S->part, S->counter, S->s);
+  else
+    k_build_b<double><<<rb, PB, 0, st>>>(g, (ph.dx / ph.dt) / ph.dy, 1.0 / ph.dy, rhs_p,
+                                         static_cast<const double *>(u3), u_inlet, pres_old, S->bvec, S->x, S->bin,
+                                         S->part, S->counter, S->s);
+  k_init_r<<<rb, PB, 0, st>>>(F.nx, F.ny, F.nz, F.cx, F.cy, F.cz, 1.0 / (double)N, rtol, ctl, S->s, S->bvec,
+                              S->x, S->r, S->part, S->counter);
+  *nl += 2;
+  return cudaGetLastError();
+}
+
+static cudaError_t solve_iteration(PoissonSolver *S, const CgCtl &ctl, cudaStream_t st, long *nl) {
+  const int N = S->N, rb = S->rblk;
+  const PLevel &F = S->lv[0];
+  PCK(S->fp32 ? vcycle<float>(S, S->r, S->z, st, nl) : vcycle<double>(S, S->r, S->z, st, nl));
+  k_zdot<<<rb, PB, 0, st>>>(N, 1.0 / (double)N, S->r, S->z, S->part, S->counter, S->s);
+  k_pupdate<<<nblocks(N), PB, 0, st>>>(N, S->s, S->z, S->p);
+  k_apply_dot<<<rb, PB, 0, st>>>(F.nx, F.ny, F.nz, F.cx, F.cy, F.cz, S->p, S->q, S->part, S->counter, S->s);
+  k_axpy<<<rb, PB, 0, st>>>(N, ctl, S->s, S->p, S->q, S->x, S->r, S->part, S->counter);
+  *nl += 4;
+  return cudaGetLastError();
+}
+
+static cudaError_t solve_end(PoissonSolver *S, const Geo &g, const Phys &ph, double *pres, cudaStream_t st,
+                             long *nl) {
+  k_sumx<<<S->rblk, PB, 0, st>>>(S->N, S->x, S->part, S->counter, S->s);
+  dim3 grd((g.nx + 2 + 31) / 32, (g.ny + 2 + 3) / 4, g.nz + 2);
+  k_writeback<<<grd, dim3(32, 4), 0, st>>>(g, ph.dy, 1.0 / (double)S->N, S->s, S->x, S->bin, pres);
+  *nl += 2;
+  return cudaGetLastError();
+}
+
 cudaError_t poisson_solve(PoissonSolver *S, const Geo &g, const Phys &ph,
-                          const double *rhs_p, const double *u3,
+                          const double *rhs_p, const void *u3, int u3_fp32,
                           const double *u_inlet, const double *pres_old,
                           double *pres, double rtol, int maxits, int *its,
                           double *rnorm, double *bnorm, int *reason,
                           cudaStream_t st, long *nl) {
-  const int N = S->N, rb = S->rblk;
-  const double invN = 1.0 / (double)N;
-  const PLevel &F = S->lv[0];
-  k_build_b<<<rb, PB, 0, st>>>(g, (ph.dx / ph.dt) / ph.dy, 1.0 / ph.dy, rhs_p, u3, u_inlet, pres_old,
-                               S->bvec, S->x, S->bin, S->part, S->counter, S->s);
-  k_init_r<<<rb, PB, 0, st>>>(F.nx, F.ny, F.nz, F.cx, F.cy, F.cz, invN, S->s, S->bvec, S->x, S->r, S->part,
-                              S->counter);
-  *nl += 2;
-  PCK(cudaGetLastError());
+  const CgCtl ctl = {maxits, 0, 0};
+  PCK(solve_begin(S, g, ph, rhs_p, u3, u3_fp32, u_inlet, pres_old, rtol, ctl, st, nl));
+  while (true) {
+    PCK(cudaMemcpyAsync(S->s_host, S->s, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, st));
+    PCK(cudaStreamSynchronize(st));
+    if (S->s_host[S_REASON] != 0.0) break;
+    PCK(solve_iteration(S, ctl, st, nl));
+  }
+  PCK(solve_end(S, g, ph, pres, st, nl));
+  *its = (int)S->s_host[S_IT];
+  *rnorm = sqrt(S->s_host[S_RR]);
+  *bnorm = sqrt(S->s_host[S_BB]);
+  *reason = (int)S->s_host[S_REASON];
+  return cudaSuccess;
+}
+
+cudaError_t poisson_solve_capture(PoissonSolver *S, const Geo &g, const Phys &ph,
+                                  const double *rhs_p, const void *u3, int u3_fp32,
+                                  const double *u_inlet, const double *pres_old,
+                                  double *pres, double rtol, int maxits,
+                                  cudaStream_t st, long *nl_static, long *nl_body) {
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t graph = nullptr;
+  PCK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &graph, nullptr, nullptr, nullptr));
+  if (cs != cudaStreamCaptureStatusActive || !graph) return cudaErrorStreamCaptureUnmatched;
+  CgCtl ctl = {maxits, 1, 0};
+  PCK(cudaGraphConditionalHandleCreate(&ctl.cond, graph, 0, 0));
+  PCK(solve_begin(S, g, ph, rhs_p, u3, u3_fp32, u_inlet, pres_old, rtol, ctl, st, nl_static));
+  const cudaGraphNode_t *deps = nullptr;
+  size_t ndeps = 0;
+  PCK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &graph, &deps, nullptr, &ndeps));
+  cudaGraphNodeParams cp = {};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = ctl.cond;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t node;
+  PCK(cudaGraphAddNode(&node, graph, deps, nullptr, ndeps, &cp));
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  if (!S->side) PCK(cudaStreamCreateWithFlags(&S->side, cudaStreamNonBlocking));
+  PCK(cudaStreamBeginCaptureToGraph(S->side, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  const cudaError_t eb = solve_iteration(S, ctl, S->side, nl_body);
+  cudaGraph_t out = nullptr;
+  const cudaError_t ee = cudaStreamEndCapture(S->side, &out);
+  PCK(eb);
+  PCK(ee);
+  PCK(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+  return solve_end(S, g, ph, pres, st, nl_static);
+}
+
+cudaError_t poisson_read(PoissonSolver *S, cudaStream_t st, int *its, double *rnorm, double *bnorm,
+                         int *reason, int *worst, double *its_total) {
   PCK(cudaMemcpyAsync(S->s_host, S->s, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, st));
   PCK(cudaStreamSynchronize(st));
-  const double bb = sqrt(S->s_host[S_BB]);
-  double rr = sqrt(S->s_host[S_RR]);
-  *bnorm = bb;
-  int it = 0, rsn = 0;
-  const double target = rtol * bb;
-  if (!(rr == rr)) rsn = TPLS_KSP_DIVERGED_NAN;
-  else if (rr <= target || bb == 0.0) rsn = TPLS_KSP_CONVERGED_RTOL;
-  const int nb = nblocks(N);
-  while (rsn == 0) {
-    PCK(vcycle(S, S->r, S->z, st, nl));
-    k_zdot<<<rb, PB, 0, st>>>(N, invN, it == 0, S->r, S->z, S->part, S->counter, S->s);
-    k_pupdate<<<nb, PB, 0, st>>>(N, S->s, S->z, S->p);
-    k_apply_dot<<<rb, PB, 0, st>>>(F.nx, F.ny, F.nz, F.cx, F.cy, F.cz, S->p, S->q, S->part, S->counter, S->s);
-    k_axpy<<<rb, PB, 0, st>>>(N, S->s, S->p, S->q, S->x, S->r, S->part, S->counter);
-    *nl += 4;
-    PCK(cudaGetLastError());
-    it++;
-    PCK(cudaMemcpyAsync(S->s_host + S_RR, S->s + S_RR, sizeof(double), cudaMemcpyDeviceToHost, st));
-    PCK(cudaStreamSynchronize(st));
-    rr = sqrt(S->s_host[S_RR]);
-    if (!(rr == rr)) rsn = TPLS_KSP_DIVERGED_NAN;
-    else if (rr <= target) rsn = TPLS_KSP_CONVERGED_RTOL;
-    else if (it >= maxits) rsn = TPLS_KSP_DIVERGED_ITS;
-  }
-  k_sumx<<<rb, PB, 0, st>>>(N, S->x, S->part, S->counter, S->s);
-  dim3 grd((g.nx + 2 + 31) / 32, (g.ny + 2 + 3) / 4, g.nz + 2);
-  k_writeback<<<grd, dim3(32, 4), 0, st>>>(g, ph.dy, invN, S->s, S->x, S->bin, pres);
-  *nl += 2;
-  PCK(cudaGetLastError());
-  *its = it;
-  *rnorm = rr;
-  *reason = rsn;
+  *its = (int)S->s_host[S_IT];
+  *rnorm = sqrt(S->s_host[S_RR]);
+  *bnorm = sqrt(S->s_host[S_BB]);
+  *reason = (int)S->s_host[S_REASON];
+  *worst = (int)S->s_host[S_WORST];
+  *its_total = S->s_host[S_ITS_TOTAL];
   return cudaSuccess;
+}
+
+cudaError_t poisson_reset_worst(PoissonSolver *S, cudaStream_t st) {
+  static const double zero = 0.0;
+  return cudaMemcpyAsync(S->s + S_WORST, &zero, sizeof(double), cudaMemcpyHostToDevice, st);
 }
 
 }  // namespace tpls

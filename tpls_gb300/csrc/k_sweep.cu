@@ -1,0 +1,266 @@
+// k_sweep.cu -- Jacobi and red-black SOR sweeps of the Crank-Nicolson
+// Helmholtz solve on precomputed per-point coefficient records
+// (jacobi_iteration_allflux.f90:21-282, sor_iteration_allflux.f90:19-377,
+// boundary rows of main_ns_hybrid.F90:756-887).
+//
+// k_mom_rhs writes, once per timestep, one record per point of a velocity
+// component: the six neighbour coefficients and rhs/diag, already divided
+// by the Helmholtz diagonal (see write_coef in k_momentum.cu).  A sweep
+// point is then x_new = sum(c_n x_n) + b: seven FMAs instead of the face
+// averages, diagonal and division of the reference's form, evaluated once
+// per step instead of once per sweep.  Templated on the storage/arithmetic
+// type: double for the FP64 form, float for the FP32-mixed form (records
+// of 8 floats, velocity in FP32 during the sweeps).
+#include "tpls_sweep.cuh"
+
+namespace tpls {
+
+constexpr int SW_X = 32, SW_Y = 4;
+
+template <typename T>
+struct Rec {
+  T xp, xm, yp, ym, zp, zm, b;
+};
+
+// record of point c (8 values per point; `stream` = evict-first loads)
+template <typename T>
+__device__ __forceinline__ Rec<T> load_rec(const T *__restrict__ coef, int c, bool stream);
+template <>
+__device__ __forceinline__ Rec<double> load_rec<double>(const double *__restrict__ coef, int c, bool stream) {
+  const double2 *r = reinterpret_cast<const double2 *>(coef + 8 * (size_t)c);
+  const double2 a = stream ? __ldcs(r) : __ldg(r), b = stream ? __ldcs(r + 1) : __ldg(r + 1);
+  const double2 d = stream ? __ldcs(r + 2) : __ldg(r + 2), e = stream ? __ldcs(r + 3) : __ldg(r + 3);
+  Rec<double> q = {a.x, a.y, b.x, b.y, d.x, d.y, e.x};
+  return q;
+}
+template <>
+__device__ __forceinline__ Rec<float> load_rec<float>(const float *__restrict__ coef, int c, bool stream) {
+  const float4 *r = reinterpret_cast<const float4 *>(coef + 8 * (size_t)c);
+  const float4 a = stream ? __ldcs(r) : __ldg(r), b = stream ? __ldcs(r + 1) : __ldg(r + 1);
+  Rec<float> q = {a.x, a.y, a.z, a.w, b.x, b.y, b.z};
+  return q;
+}
+
+template <typename T>
+__device__ __forceinline__ T rec_apply(const Rec<T> &q, T xp, T xm, T yp, T ym, T zp, T zm) {
+  T v = fma(q.xp, xp, q.b);
+  v = fma(q.xm, xm, v);
+  v = fma(q.yp, yp, v);
+  v = fma(q.ym, ym, v);
+  v = fma(q.zp, zp, v);
+  return fma(q.zm, zm, v);
+}
+
+// Jacobi: x = J(xo) on the component's interior with its boundary rows.
+template <typename T>
+__global__ void __launch_bounds__(SW_X *SW_Y)
+    k_jacobi_c(int comp, Geo g, Helm h, const T *__restrict__ xo, const T *__restrict__ coef,
+               const double *__restrict__ P, T *__restrict__ x, int fuse) {
+  const int i = blockIdx.x * SW_X + threadIdx.x + 1, j = blockIdx.y * SW_Y + threadIdx.y + 1;
+  const int k = blockIdx.z + (comp == 2 ? 1 : 0);
+  const int iend = (comp == 0) ? g.nx - 1 : g.nx;
+  if (i > iend || j > g.ny) return;
+  const int c = TPLS_IDX(g, i, j, k), sy = g.sy, sz = g.sz;
+  const Rec<T> q = load_rec(coef, c, false);
+  const T xc = xo[c];
+  T zp, zm;
+  if (comp == 2) {
+    zp = xo[c + sz];
+    zm = xo[c - sz];
+  } else {  // walls folded into the record: the z slot multiplies the point itself
+    zp = (k == g.nz - 1) ? xc : xo[c + sz];
+    zm = (k == 0) ? xc : xo[c - sz];
+  }
+  const T v = rec_apply(q, xo[c + 1], xo[c - 1], xo[c + sy], xo[c - sy], zp, zm);
+  put(g, x, i, j, k, v, fuse);
+  if (comp == 0) {
+    if (i == 1) put(g, x, 0, j, k, v, fuse);
+    if (i == g.nx - 1) {
+      put(g, x, g.nx, j, k, u_outlet(g, h, P, v, j, k), fuse);
+      put(g, x, g.nx + 1, j, k, (T)0, fuse);
+    }
+  } else if (comp == 1) {
+    if (i == 1) put(g, x, 0, j, k, v, fuse);
+    if (i == g.nx) put(g, x, g.nx + 1, j, k, v, fuse);
+  } else {
+    const int nz = g.nz;
+    if (k == 1) put(g, x, i, j, 0, (T)0, fuse);
+    if (k == nz - 1) put(g, x, i, j, nz, (T)0, fuse);
+    if (i == 1) {
+      put(g, x, 0, j, k, v, fuse);
+      if (k == 1) put(g, x, 0, j, 0, (T)0, fuse);
+      if (k == nz - 1) put(g, x, 0, j, nz, (T)0, fuse);
+    }
+    if (i == g.nx) {
+      put(g, x, g.nx + 1, j, k, v, fuse);
+      if (k == 1) put(g, x, g.nx + 1, j, 0, (T)0, fuse);
+      if (k == nz - 1) put(g, x, g.nx + 1, j, nz, (T)0, fuse);
+    }
+  }
+}
+
+// 3-D checkerboard half-sweep (even iteration_time), one thread per point
+// of the colour.
+template <typename T>
+__global__ void __launch_bounds__(SW_X *SW_Y)
+    k_sor_even_c(int comp, Geo g, Helm h, T *__restrict__ x, const T *__restrict__ coef,
+                 const double *__restrict__ P, int flg, int bc, int fuse) {
+  const int i2 = blockIdx.x * SW_X + threadIdx.x, j = blockIdx.y * SW_Y + threadIdx.y + 1;
+  const int k = blockIdx.z + (comp == 2 ? 1 : 0);
+  const int iend = (comp == 0) ? g.nx - 1 : g.nx;
+  if (i2 > (iend - 1) / 2 || j > g.ny) return;
+  const int i = 2 * i2 + 1 + ((k + j + flg) & 1);
+  T v = 0;
+  if (i <= iend) {
+    const int c = TPLS_IDX(g, i, j, k), sy = g.sy, sz = g.sz;
+    const Rec<T> q = load_rec(coef, c, false);
+    const T xc = x[c];
+    T zp, zm;
+    if (comp == 2) {
+      zp = x[c + sz];
+      zm = x[c - sz];
+    } else {
+      zp = (k == g.nz - 1) ? xc : x[c + sz];
+      zm = (k == 0) ? xc : x[c - sz];
+    }
+    const T res = rec_apply(q, x[c + 1], x[c - 1], x[c + sy], x[c - sy], zp, zm);
+    v = xc + (T)1.2 * (res - xc);
+    put(g, x, i, j, k, v, fuse);
+  }
+  if (bc) sor_bc(comp, g, h, x, P, i2, i, iend, v, j, k, fuse);
+}
+
+// Odd-iteration half-sweep (2-D colouring, sequential in k).  Within such a
+// half-sweep every value a point reads is the pre-sweep value except the
+// relaxed point below it in its own column, so the update is the recurrence
+//   x_new(k) = A(k) + B(k) x_new(k-1),
+//   A = x + 1.2 (partial - x),  B = 1.2 czm   (partial = all terms but czm),
+// with A and B known before the sweep.  A block owns 32 columns of one row
+// (one per x pair).  Warp 0 runs the recurrence of chunk c (SO_KZ levels)
+// while warps 1..7 compute A and B of chunk c+1 into the other half of a
+// double-buffered shared array, so the dependent FMA chain overlaps the
+// parallel work.  Coefficient records are streamed (evict-first) so the
+// x field stays resident in L2.
+constexpr int SO_KZ = 32, SO_T = 256;
+
+template <typename T>
+__device__ __forceinline__ void sor_odd_produce(int comp, const Geo &g, const T *__restrict__ x,
+                                                const T *__restrict__ coef, int j, int par, int npair,
+                                                int iend, int k0, int kc, int kn, T (*sA)[32],
+                                                T (*sB)[32], int t0, int nthr) {
+  const int sy = g.sy, sz = g.sz, nz = g.nz;
+  for (int t = t0; t < kn * 32; t += nthr) {
+    const int lk = t >> 5, col = t & 31;
+    const int i2 = blockIdx.x * 32 + col, i = 2 * i2 + 1 + par, k = kc + lk;
+    T A = 0, B = 0;
+    if (i2 < npair && i <= iend) {
+      const int c = TPLS_IDX(g, i, j, k);
+      const Rec<T> q = load_rec(coef, c, true);
+      const T xc = x[c];
+      T zp;
+      if (comp == 2) zp = x[c + sz];
+      else zp = (k == nz - 1) ? xc : x[c + sz];
+      T part = fma(q.xp, x[c + 1], q.b);
+      part = fma(q.xm, x[c - 1], part);
+      part = fma(q.yp, x[c + sy], part);
+      part = fma(q.ym, x[c - sy], part);
+      part = fma(q.zp, zp, part);
+      if (k == k0) {  // the point below is a wall value (w) or the point itself (u, v)
+        const T zm = (comp == 2) ? x[c - sz] : xc;
+        A = xc + (T)1.2 * (fma(q.zm, zm, part) - xc);
+      } else {
+        A = xc + (T)1.2 * (part - xc);
+        B = (T)1.2 * q.zm;
+      }
+    }
+    sA[lk][col] = A;
+    sB[lk][col] = B;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(SO_T)
+    k_sor_odd_c2(int comp, Geo g, Helm h, T *__restrict__ x, const T *__restrict__ coef,
+                 const double *__restrict__ P, int flg, int bc, int fuse) {
+  __shared__ T sA[2][SO_KZ][32], sB[2][SO_KZ][32];
+  const int j = blockIdx.y + 1;
+  const int iend = (comp == 0) ? g.nx - 1 : g.nx;
+  const int npair = (iend + 1) / 2;
+  const int par = (j + flg) & 1;
+  const int k0 = (comp == 2) ? 1 : 0, k1 = g.nz - 1;
+  const int nch = (k1 - k0 + SO_KZ) / SO_KZ;
+  const int warp = threadIdx.x >> 5;
+  sor_odd_produce(comp, g, x, coef, j, par, npair, iend, k0, k0, min(SO_KZ, k1 - k0 + 1), sA[0], sB[0],
+                  (int)threadIdx.x, SO_T);
+  __syncthreads();
+  T prev = 0;  // owned by warp 0
+  for (int ch = 0; ch < nch; ch++) {
+    const int kc = k0 + ch * SO_KZ, kn = min(SO_KZ, k1 - kc + 1), buf = ch & 1;
+    if (warp == 0) {
+      const int col = threadIdx.x;
+      const int i2 = blockIdx.x * 32 + col, i = 2 * i2 + 1 + par;
+      if (i2 < npair) {
+        for (int lk = 0; lk < kn; lk++) {
+          const int k = kc + lk;
+          T v = 0;
+          if (i <= iend) {
+            v = fma(sB[buf][lk][col], prev, sA[buf][lk][col]);
+            put(g, x, i, j, k, v, fuse);
+            prev = v;
+          }
+          if (bc) sor_bc(comp, g, h, x, P, i2, i, iend, v, j, k, fuse);
+        }
+      }
+    } else if (ch + 1 < nch) {
+      const int kc2 = kc + SO_KZ;
+      sor_odd_produce(comp, g, x, coef, j, par, npair, iend, k0, kc2, min(SO_KZ, k1 - kc2 + 1), sA[buf ^ 1],
+                      sB[buf ^ 1], (int)threadIdx.x - 32, SO_T - 32);
+    }
+    __syncthreads();
+  }
+}
+
+template <typename T>
+static cudaError_t jacobi_c(int comp, const Geo &g, const Phys &ph, const T *xo, const T *coef,
+                            const double *pres, T *x, int fuse, cudaStream_t st) {
+  const int nk = (comp == 2) ? g.nz - 1 : g.nz;
+  const int iend = (comp == 0) ? g.nx - 1 : g.nx;
+  dim3 grd((iend + SW_X - 1) / SW_X, (g.ny + SW_Y - 1) / SW_Y, nk);
+  k_jacobi_c<T><<<grd, dim3(SW_X, SW_Y), 0, st>>>(comp, g, helm_of(ph), xo, coef, pres, x, fuse);
+  return cudaGetLastError();
+}
+
+template <typename T>
+static cudaError_t sor_c(int comp, const Geo &g, const Phys &ph, T *x, const T *coef, const double *pres,
+                         int flg, int iteration_time, int bc, int fuse, cudaStream_t st) {
+  const int iend = (comp == 0) ? g.nx - 1 : g.nx;
+  const int npairs = (iend + 1) / 2;
+  if (iteration_time % 2 == 0) {
+    const int nk = (comp == 2) ? g.nz - 1 : g.nz;
+    dim3 grd((npairs + SW_X - 1) / SW_X, (g.ny + SW_Y - 1) / SW_Y, nk);
+    k_sor_even_c<T><<<grd, dim3(SW_X, SW_Y), 0, st>>>(comp, g, helm_of(ph), x, coef, pres, flg, bc, fuse);
+  } else {
+    dim3 grd((npairs + 31) / 32, g.ny, 1);
+    k_sor_odd_c2<T><<<grd, SO_T, 0, st>>>(comp, g, helm_of(ph), x, coef, pres, flg, bc, fuse);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_jacobi_c(int comp, const Geo &g, const Phys &ph, const double *xo, const double *coef,
+                            const double *pres, double *x, int fuse, cudaStream_t st) {
+  return jacobi_c(comp, g, ph, xo, coef, pres, x, fuse, st);
+}
+cudaError_t launch_jacobi_c(int comp, const Geo &g, const Phys &ph, const float *xo, const float *coef,
+                            const double *pres, float *x, int fuse, cudaStream_t st) {
+  return jacobi_c(comp, g, ph, xo, coef, pres, x, fuse, st);
+}
+cudaError_t launch_sor_c(int comp, const Geo &g, const Phys &ph, double *x, const double *coef,
+                         const double *pres, int flg, int iteration_time, int bc, int fuse, cudaStream_t st) {
+  return sor_c(comp, g, ph, x, coef, pres, flg, iteration_time, bc, fuse, st);
+}
+cudaError_t launch_sor_c(int comp, const Geo &g, const Phys &ph, float *x, const float *coef,
+                         const double *pres, int flg, int iteration_time, int bc, int fuse, cudaStream_t st) {
+  return sor_c(comp, g, ph, x, coef, pres, flg, iteration_time, bc, fuse, st);
+}
+
+}  // namespace tpls

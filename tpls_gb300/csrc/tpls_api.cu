@@ -39,12 +39,29 @@ struct tpls_ctx {
   double *x3[3][2];  // momentum ping-pong per component
   int x3_final[3] = {0, 0, 0};
   double *u_inlet;
+  // FP32-mixed form: FP32 copies of the step inputs and FP32 work arrays
+  // (the state above stays FP64)
+  int mixed = 0;
+  float *phi32, *u32, *v32, *w32, *mu32, *D32, *fx32, *fy32, *fz32, *prA32, *prB32;
+  float *coef32[3];
+  float *x3f[3][2];
+  double *x3d = nullptr;  // FP64 view of u3/v3/w3 for tpls_get_field / tpls_set_field
+  size_t n_p, n_uv, n_w;  // elements of each allocation (incl. pitch and padding)
   double *part, *scal, *scal_host;
   size_t part_len;
   PoissonSolver *ps = nullptr;
   tpls_stats stats;
   long launches = 0;
   bool need_exchange = true;
+  // CUDA-graph steps: one executable graph per history phase (the AB3 slot
+  // pointers differ), captured on first use
+  bool use_graphs = true;
+  bool capturing = false;
+  bool graph_pending = false;  // graph steps launched since the last stats read
+  cudaGraphExec_t gexec[3] = {nullptr, nullptr, nullptr};
+  long g_static[3] = {0, 0, 0};  // kernels per launch outside the CG loop body
+  long g_body = 0;               // kernels per CG iteration
+  double its_accounted = 0.0;    // pressure iterations already counted in `launches`
   // phase timing (tpls_timing_*)
   bool timing = false;
   int cur_slot = TPLS_T_OTHER;
@@ -93,18 +110,20 @@ struct PhaseScope {
 static int nz_planes(int kind, int nz) { return kind == 0 ? nz + 2 : (kind == 1 ? nz : nz + 1); }
 
 // device array in the pitched layout; returns the pointer to element (0,0,0)
-static cudaError_t alloc_field(tpls_ctx *c, int rows_before, int rows, int nzp, double **out) {
+template <typename T>
+static cudaError_t alloc_field(tpls_ctx *c, int rows_before, int rows, int nzp, T **out) {
   void *base = nullptr;
   const size_t n = (size_t)c->px * rows * nzp + 8;
-  cudaError_t e = cudaMalloc(&base, n * sizeof(double));
+  cudaError_t e = cudaMalloc(&base, n * sizeof(T));
   if (e != cudaSuccess) return e;
   c->allocs.push_back(base);
-  e = cudaMemset(base, 0, n * sizeof(double));
+  e = cudaMemset(base, 0, n * sizeof(T));
   if (e != cudaSuccess) return e;
-  *out = (double *)base + XOFF + (size_t)c->px * rows_before;
+  *out = (T *)base + XOFF + (size_t)c->px * rows_before;
   return cudaSuccess;
 }
-static cudaError_t alloc_p(tpls_ctx *c, double **out) { return alloc_field(c, 0, c->ny + 2, c->nz + 2, out); }
+template <typename T>
+static cudaError_t alloc_p(tpls_ctx *c, T **out) { return alloc_field(c, 0, c->ny + 2, c->nz + 2, out); }
 
 static int field_kind(int f) {
   switch (f) {
@@ -148,9 +167,9 @@ static double *field_ptr(tpls_ctx *c, int f) {
     case TPLS_F_CONV2_PHI: return c->conv_phi[s1];
     case TPLS_F_PHI3: return c->phi2;
     case TPLS_F_RHS_P: return c->rhs_p;
-    case TPLS_F_U3: return c->x3[0][c->x3_final[0]];
-    case TPLS_F_V3: return c->x3[1][c->x3_final[1]];
-    case TPLS_F_W3: return c->x3[2][c->x3_final[2]];
+    case TPLS_F_U3: return c->mixed ? c->x3d : c->x3[0][c->x3_final[0]];
+    case TPLS_F_V3: return c->mixed ? c->x3d : c->x3[1][c->x3_final[1]];
+    case TPLS_F_W3: return c->mixed ? c->x3d : c->x3[2][c->x3_final[2]];
     default: return nullptr;
   }
   (void)s2;
@@ -237,6 +256,8 @@ static void timing_flush(tpls_ctx *c) {
 
 extern "C" {
 
+static int refresh_graph_stats(tpls_ctx *c);
+
 const char *tpls_status_string(int s) {
   if (s == TPLS_OK) return "ok";
   if (s == TPLS_ERR_ARG) return "bad argument or index bounds";
@@ -254,6 +275,8 @@ int tpls_gpu_destroy(tpls_ctx *c) {
   if (c->st) cudaStreamSynchronize(c->st);
   timing_flush(c);
   for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
+  for (cudaGraphExec_t ge : c->gexec)
+    if (ge) cudaGraphExecDestroy(ge);
   poisson_destroy(c->ps);
   for (void *p : c->allocs) cudaFree(p);
   if (c->scal_host) cudaFreeHost(c->scal_host);
@@ -277,26 +300,55 @@ static int create_impl(int nx, int ny, int nz, const tpls_params *prm, const dou
   c->g.sz = c->px * (ny + 2);
   c->g.szm = c->px * (ny + 4);
   TCK(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
+  c->mixed = (prm->precision == TPLS_PREC_FP32_MIXED);
+  c->n_p = (size_t)c->px * (ny + 2) * (nz + 2) + 8;
+  c->n_uv = (size_t)c->px * (ny + 2) * nz + 8;
+  c->n_w = (size_t)c->px * (ny + 2) * (nz + 1) + 8;
   double **pf[] = {&c->phi2, &c->pres, &c->pres_old, &c->conv_phi[0], &c->conv_phi[1], &c->conv_phi[2],
-                   &c->phiA, &c->phiB, &c->D, &c->fx, &c->fy, &c->fz, &c->rhs_p};
+                   &c->phiA, &c->rhs_p};
   for (double **p : pf) TCK(alloc_p(c, p));
   double **puv[] = {&c->u2, &c->v2, &c->conv_u[0], &c->conv_u[1], &c->conv_u[2], &c->conv_v[0],
                     &c->conv_v[1], &c->conv_v[2], &c->csf_u[0], &c->csf_u[1], &c->csf_u[2],
-                    &c->csf_v[0], &c->csf_v[1], &c->csf_v[2],
-                    &c->x3[0][0], &c->x3[0][1], &c->x3[1][0], &c->x3[1][1]};
+                    &c->csf_v[0], &c->csf_v[1], &c->csf_v[2]};
   for (double **p : puv) TCK(alloc_field(c, 0, ny + 2, nz, p));
   double **pw[] = {&c->w2, &c->conv_w[0], &c->conv_w[1], &c->conv_w[2], &c->csf_w[0], &c->csf_w[1],
-                   &c->csf_w[2], &c->x3[2][0], &c->x3[2][1]};
+                   &c->csf_w[2]};
   for (double **p : pw) TCK(alloc_field(c, 0, ny + 2, nz + 1, p));
-  for (int q = 0; q < 3; q++) {  // one 64-byte record per point of each component
-    void *b = nullptr;
-    const size_t n = (size_t)8 * c->px * (ny + 2) * (q == 2 ? nz + 1 : nz);
-    TCK(cudaMalloc(&b, n * sizeof(double)));
-    c->allocs.push_back(b);
-    TCK(cudaMemset(b, 0, n * sizeof(double)));
-    c->coef[q] = (double *)b;
+  const int rec = 8;  // record entries per point: 64 B in FP64, 32 B in FP32
+  if (!c->mixed) {
+    double **pf2[] = {&c->phiB, &c->D, &c->fx, &c->fy, &c->fz};
+    for (double **p : pf2) TCK(alloc_p(c, p));
+    double **px3[] = {&c->x3[0][0], &c->x3[0][1], &c->x3[1][0], &c->x3[1][1]};
+    for (double **p : px3) TCK(alloc_field(c, 0, ny + 2, nz, p));
+    TCK(alloc_field(c, 0, ny + 2, nz + 1, &c->x3[2][0]));
+    TCK(alloc_field(c, 0, ny + 2, nz + 1, &c->x3[2][1]));
+    for (int q = 0; q < 3; q++) {
+      void *b = nullptr;
+      const size_t n = (size_t)rec * c->px * (ny + 2) * (q == 2 ? nz + 1 : nz);
+      TCK(cudaMalloc(&b, n * sizeof(double)));
+      c->allocs.push_back(b);
+      TCK(cudaMemset(b, 0, n * sizeof(double)));
+      c->coef[q] = (double *)b;
+    }
+    TCK(alloc_field(c, 1, ny + 4, nz + 2, &c->mu));
+  } else {
+    float **qf[] = {&c->phi32, &c->D32, &c->fx32, &c->fy32, &c->fz32, &c->prA32, &c->prB32};
+    for (float **p : qf) TCK(alloc_p(c, p));
+    float **quv[] = {&c->u32, &c->v32, &c->x3f[0][0], &c->x3f[0][1], &c->x3f[1][0], &c->x3f[1][1]};
+    for (float **p : quv) TCK(alloc_field(c, 0, ny + 2, nz, p));
+    float **qw[] = {&c->w32, &c->x3f[2][0], &c->x3f[2][1]};
+    for (float **p : qw) TCK(alloc_field(c, 0, ny + 2, nz + 1, p));
+    for (int q = 0; q < 3; q++) {
+      void *b = nullptr;
+      const size_t n = (size_t)rec * c->px * (ny + 2) * (q == 2 ? nz + 1 : nz);
+      TCK(cudaMalloc(&b, n * sizeof(float)));
+      c->allocs.push_back(b);
+      TCK(cudaMemset(b, 0, n * sizeof(float)));
+      c->coef32[q] = (float *)b;
+    }
+    TCK(alloc_field(c, 1, ny + 4, nz + 2, &c->mu32));
+    TCK(alloc_field(c, 0, ny + 2, nz + 1, &c->x3d));
   }
-  TCK(alloc_field(c, 1, ny + 4, nz + 2, &c->mu));
   {
     void *b = nullptr;
     const size_t n = (size_t)c->px * (ny + 2) * (nz + 2) + 64;
@@ -328,7 +380,7 @@ static int create_impl(int nx, int ny, int nz, const tpls_params *prm, const dou
     c->scal_host = (double *)b;
   }
   TCK(poisson_create(c->g, 1.0 / (prm->dy * prm->dy), 1.0 / (prm->dx * prm->dx), 1.0 / (prm->dz * prm->dz),
-                     &c->ps));
+                     c->mixed, &c->ps));
   memset(&c->stats, 0, sizeof(c->stats));
   TCK(cudaDeviceSynchronize());
   return TPLS_OK;
@@ -344,7 +396,7 @@ int tpls_gpu_create(int nx, int ny, int nz, const tpls_params *prm, const double
   if (!(prm->dx > 0 && prm->dy > 0 && prm->dz > 0 && prm->dt > 0 && prm->re > 0 &&
         prm->smooth_width > 0))
     return TPLS_ERR_ARG;
-  if (prm->precision != TPLS_PREC_FP64) return TPLS_ERR_NOT_BUILT;
+  if (prm->precision != TPLS_PREC_FP64 && prm->precision != TPLS_PREC_FP32_MIXED) return TPLS_ERR_ARG;
   tpls_ctx *c = new tpls_ctx();
   int s = create_impl(nx, ny, nz, prm, u_inlet, c);
   if (s != TPLS_OK) {
@@ -355,11 +407,24 @@ int tpls_gpu_create(int nx, int ny, int nz, const tpls_params *prm, const double
   return TPLS_OK;
 }
 
+// FP32 iterate behind U3/V3/W3 in the FP32-mixed form, and its element count
+static float *mixed_x3(tpls_ctx *c, int f, size_t *n) {
+  const int q = (f == TPLS_F_U3) ? 0 : ((f == TPLS_F_V3) ? 1 : 2);
+  *n = (q == 2) ? c->n_w : c->n_uv;
+  return c->x3f[q][c->x3_final[q]];
+}
+static bool is_x3(int f) { return f == TPLS_F_U3 || f == TPLS_F_V3 || f == TPLS_F_W3; }
+
 int tpls_set_field(tpls_ctx *c, int f, const double *host) {
   if (!c || !host || f < 0 || f >= TPLS_F_COUNT) return TPLS_ERR_ARG;
   double *d = field_ptr(c, f);
   if (!d) return TPLS_ERR_ARG;
   TCK(h2d(c, d, host, nz_planes(field_kind(f), c->nz)));
+  if (c->mixed && is_x3(f)) {
+    size_t n;
+    float *x = mixed_x3(c, f, &n);
+    TCK(launch_to_float(d - XOFF, x - XOFF, n, c->st));
+  }
   TCK(cudaStreamSynchronize(c->st));
   c->need_exchange = true;
   return TPLS_OK;
@@ -367,8 +432,13 @@ int tpls_set_field(tpls_ctx *c, int f, const double *host) {
 
 int tpls_get_field(tpls_ctx *c, int f, double *host) {
   if (!c || !host || f < 0 || f >= TPLS_F_COUNT) return TPLS_ERR_ARG;
-  const double *d = field_ptr(c, f);
+  double *d = field_ptr(c, f);
   if (!d) return TPLS_ERR_ARG;
+  if (c->mixed && is_x3(f)) {
+    size_t n;
+    const float *x = mixed_x3(c, f, &n);
+    TCK(launch_to_double(x - XOFF, d - XOFF, n, c->st));
+  }
   TCK(d2h(c, host, d, nz_planes(field_kind(f), c->nz)));
   TCK(cudaStreamSynchronize(c->st));
   return TPLS_OK;
@@ -380,30 +450,36 @@ int tpls_sync(tpls_ctx *c) {
   return TPLS_OK;
 }
 
-long tpls_kernel_launches(const tpls_ctx *c) { return c ? c->launches : -1; }
+long tpls_kernel_launches(tpls_ctx *c) {
+  if (!c) return -1;
+  if (refresh_graph_stats(c) != TPLS_OK) return -1;
+  return c->launches;
+}
 
-// One velocity component's Crank-Nicolson solve (main_ns_hybrid.F90:756-887).
-static int momentum(tpls_ctx *c, int comp, const double *coef, int max_iteration) {
+extern "C++" {
+// One velocity component's Crank-Nicolson solve (main_ns_hybrid.F90:756-887)
+// on the iterate pair X (FP64, or FP32 in the FP32-mixed form).
+template <typename T>
+static int momentum(tpls_ctx *c, int comp, const T *coef, T **X, int max_iteration) {
   const Geo &g = c->g;
   const int nzp = nz_planes(comp == 2 ? 2 : 1, c->nz);
   const int fuse = (g.ny % 2 == 0);
-  double **X = c->x3[comp];
-  TCK(cudaMemsetAsync(X[0] - XOFF, 0, sizeof(double) * ((size_t)c->px * (c->ny + 2) * nzp + 8), c->st));
+  TCK(cudaMemsetAsync(X[0] - XOFF, 0, sizeof(T) * ((size_t)c->px * (c->ny + 2) * nzp + 8), c->st));
   const int N = max_iteration / 2;
   for (int it = 1; it <= N; it++) {
-    double *src = X[(it - 1) % 2], *dst = X[it % 2];
+    T *src = X[(it - 1) % 2], *dst = X[it % 2];
     {
       PhaseScope ps(c, TPLS_T_JACOBI);
       LCK(c, launch_jacobi_c(comp, g, c->ph, src, coef, c->pres, dst, fuse, c->st));
     }
     if (!fuse) LCK(c, launch_exchange(g, dst, nzp, c->st));
     {
-      PhaseScope ps(c, TPLS_T_SOR);
+      PhaseScope ps(c, (it % 2) ? TPLS_T_SOR_ODD : TPLS_T_SOR);
       LCK(c, launch_sor_c(comp, g, c->ph, dst, coef, c->pres, 0, it, 0, fuse, c->st));
     }
     if (!fuse) LCK(c, launch_exchange(g, dst, nzp, c->st));
     {
-      PhaseScope ps(c, TPLS_T_SOR);
+      PhaseScope ps(c, (it % 2) ? TPLS_T_SOR_ODD : TPLS_T_SOR);
       LCK(c, launch_sor_c(comp, g, c->ph, dst, coef, c->pres, 1, it, 1, fuse, c->st));
     }
     if (!fuse) LCK(c, launch_exchange(g, dst, nzp, c->st));
@@ -418,18 +494,63 @@ static int momentum(tpls_ctx *c, int comp, const double *coef, int max_iteration
   }
   return TPLS_OK;
 }
+}  // extern "C++"
+
+// Periodic y rows of the velocity state after a host upload
+// (advect_phi.f90:317-322 / main_ns_hybrid.F90:728-733); later steps keep
+// them current in the kernels that write the state.
+static int prologue(tpls_ctx *c) {
+  if (c->need_exchange) {
+    LCK(c, launch_exchange(c->g, c->u2, c->nz, c->st));
+    LCK(c, launch_exchange(c->g, c->v2, c->nz, c->st));
+    LCK(c, launch_exchange(c->g, c->w2, c->nz + 1, c->st));
+    c->need_exchange = false;
+  }
+  return TPLS_OK;
+}
+
+// Pressure solve of the step (main_ns_hybrid.F90:897-913): host-driven
+// iterations when launching eagerly, a WHILE node when capturing.
+static int pressure_stage(tpls_ctx *c, const void *u3, int u3_fp32, int *its, double *rn, double *bn,
+                          int *reason) {
+  *its = 0;
+  *rn = *bn = 0.0;
+  *reason = 0;
+  if (c->capturing) {
+    long ns = 0, nb = 0;
+    TCK(poisson_solve_capture(c->ps, c->g, c->ph, c->rhs_p, u3, u3_fp32, c->u_inlet, c->pres_old, c->pres,
+                              c->prm.p_rtol, c->prm.p_maxits, c->st, &ns, &nb));
+    c->launches += ns;
+    c->g_body = nb;
+    return TPLS_OK;
+  }
+  const long l0 = c->launches;
+  TCK(poisson_solve(c->ps, c->g, c->ph, c->rhs_p, u3, u3_fp32, c->u_inlet, c->pres_old, c->pres, c->prm.p_rtol,
+                    c->prm.p_maxits, its, rn, bn, reason, c->st, &c->launches));
+  c->t_n[TPLS_T_PRESSURE] += c->launches - l0;
+  c->its_accounted += *its;
+  return TPLS_OK;
+}
+
+// Bookkeeping after an eagerly launched step.
+static int finish_eager(tpls_ctx *c, int its, double rn, double bn, int reason) {
+  if (c->timing) timing_flush(c);
+  c->phase = (c->phase + 1) % 3;
+  c->stats.p_its = its;
+  c->stats.p_rnorm = rn;
+  c->stats.p_bnorm = bn;
+  c->stats.p_reason = reason;
+  if (reason < c->stats.p_worst) c->stats.p_worst = reason;
+  c->stats.steps_done++;
+  if (reason < 0) return reason;
+  return TPLS_OK;
+}
 
 static int step_once(tpls_ctx *c) {
   const Geo &g = c->g;
   const Phys &ph = c->ph;
   cudaStream_t st = c->st;
   const int s0 = c->phase % 3, s1 = (c->phase + 1) % 3, s2 = (c->phase + 2) % 3;
-  if (c->need_exchange) {  // advect_phi.f90:317-322 / main_ns_hybrid.F90:728-733
-    LCK(c, launch_exchange(g, c->u2, c->nz, st));
-    LCK(c, launch_exchange(g, c->v2, c->nz, st));
-    LCK(c, launch_exchange(g, c->w2, c->nz + 1, st));
-    c->need_exchange = false;
-  }
   // viscosity from the pre-advection level set (main_ns_hybrid.F90:646-724)
   {
     PhaseScope ps(c, TPLS_T_VISC);
@@ -475,9 +596,9 @@ static int step_once(tpls_ctx *c) {
   delete rhs_scope;
   // momentum sweeps (:756-887)
   int s;
-  if ((s = momentum(c, 0, c->coef[0], c->prm.mom_u))) return s;
-  if ((s = momentum(c, 1, c->coef[1], c->prm.mom_v))) return s;
-  if ((s = momentum(c, 2, c->coef[2], c->prm.mom_w))) return s;
+  if ((s = momentum<double>(c, 0, c->coef[0], c->x3[0], c->prm.mom_u))) return s;
+  if ((s = momentum<double>(c, 1, c->coef[1], c->x3[1], c->prm.mom_v))) return s;
+  if ((s = momentum<double>(c, 2, c->coef[2], c->x3[2], c->prm.mom_w))) return s;
   double *u3 = c->x3[0][c->x3_final[0]], *v3 = c->x3[1][c->x3_final[1]], *w3 = c->x3[2][c->x3_final[2]];
   // pressure source (:892) and solve (:897-913)
   int its = 0, reason = 0;
@@ -485,10 +606,7 @@ static int step_once(tpls_ctx *c) {
   {
     PhaseScope ps(c, TPLS_T_PRESSURE);
     LCK(c, launch_source(g, ph, u3, v3, w3, c->rhs_p, st));
-    const long l0 = c->launches;
-    TCK(poisson_solve(c->ps, g, ph, c->rhs_p, u3, c->u_inlet, c->pres_old, c->pres, c->prm.p_rtol,
-                      c->prm.p_maxits, &its, &rn, &bn, &reason, st, &c->launches));
-    c->t_n[TPLS_T_PRESSURE] += c->launches - l0;
+    if ((s = pressure_stage(c, u3, 0, &its, &rn, &bn, &reason))) return s;
   }
   // projection into the next state's velocity arrays (:918)
   {
@@ -498,23 +616,193 @@ static int step_once(tpls_ctx *c) {
     TCK(cudaMemcpyAsync(c->pres_old - XOFF, c->pres - XOFF,
                         sizeof(double) * ((size_t)c->px * (c->ny + 2) * (c->nz + 2)), cudaMemcpyDeviceToDevice, st));
   }
-  if (c->timing) timing_flush(c);
-  c->phase = (c->phase + 1) % 3;
+  if (c->capturing) return TPLS_OK;
+  return finish_eager(c, its, rn, bn, reason);
+}
+
+// FP32-mixed timestep: the same sequence as step_once with the stencils,
+// the redistancing iterations, the momentum sweeps and the multigrid
+// preconditioner in FP32.  The state (phi, u, v, w, p, the AB3 histories),
+// the AB3 updates, the momentum right-hand sides, the CG recurrences and the
+// projection stay FP64; every FP32 array is a rounded copy or an
+// intermediate of one step.
+static int step_once_mixed(tpls_ctx *c) {
+  const Geo &g = c->g;
+  const Phys &ph = c->ph;
+  cudaStream_t st = c->st;
+  const int s0 = c->phase % 3, s1 = (c->phase + 1) % 3, s2 = (c->phase + 2) % 3;
+  {
+    PhaseScope ps(c, TPLS_T_VISC);
+    LCK(c, launch_visc(g, ph, c->phi2, c->mu32, st));
+  }
+  {
+    PhaseScope ps(c, TPLS_T_ADVECT);
+    LCK(c, launch_to_float(c->phi2 - XOFF, c->phi32 - XOFF, c->n_p, st));
+    LCK(c, launch_to_float(c->u2 - XOFF, c->u32 - XOFF, c->n_uv, st));
+    LCK(c, launch_to_float(c->v2 - XOFF, c->v32 - XOFF, c->n_uv, st));
+    LCK(c, launch_to_float(c->w2 - XOFF, c->w32 - XOFF, c->n_w, st));
+    LCK(c, launch_advect(g, ph, (const float *)c->phi32, c->u32, c->v32, c->w32, c->conv_phi[s2], st));
+  }
+  PhaseScope *ls_scope = new PhaseScope(c, TPLS_T_LEVELSET);
+  LCK(c, launch_ls_ab3(g, ph, c->phi2, c->conv_phi[s0], c->conv_phi[s1], c->conv_phi[s2], c->phiA, st));
+  LCK(c, launch_ls_status(g, ph, c->phiA, c->D32, c->flags, st));
+  const int L = c->prm.levelset;
+  if (L <= 0) {
+    TCK(cudaMemcpyAsync(c->phi2 - XOFF, c->phiA - XOFF, sizeof(double) * c->n_p, cudaMemcpyDeviceToDevice, st));
+    TCK(cudaMemsetAsync(c->scal + SC_ERR_PHI, 0, sizeof(double), st));
+  }
+  for (int it = 1; it <= L; it++) {
+    const double *src64 = (it == 1) ? c->phiA : nullptr;
+    const float *src32 = (it == 1) ? nullptr : ((it % 2 == 0) ? c->prB32 : c->prA32);
+    double *dst64 = (it == L) ? c->phi2 : nullptr;
+    float *dst32 = (it == L) ? nullptr : ((it % 2 == 1) ? c->prB32 : c->prA32);
+    LCK(c, launch_ls_iter32(g, ph, src64, src32, c->D32, c->flags, dst64, dst32, (it == L) ? c->part : nullptr,
+                            st));
+  }
+  if (L > 0) LCK(c, finish_sum(c->part, ls_iter_blocks(g), c->scal + SC_ERR_PHI, 1, st));
+  delete ls_scope;
+  {
+    PhaseScope ps(c, TPLS_T_CSF);
+    LCK(c, launch_csf(g, ph, c->phi2, c->fx32, c->fy32, c->fz32, st));
+  }
+  {
+    PhaseScope ps(c, TPLS_T_MOM_RHS);
+    LCK(c, launch_mom_rhs32(0, g, ph, c->u32, c->v32, c->w32, c->u2, c->mu32, c->fx32, c->conv_u[s1],
+                            c->conv_u[s0], c->csf_u[s1], c->csf_u[s0], c->conv_u[s2], c->csf_u[s2], c->coef32[0],
+                            st));
+    LCK(c, launch_mom_rhs32(1, g, ph, c->u32, c->v32, c->w32, c->v2, c->mu32, c->fy32, c->conv_v[s1],
+                            c->conv_v[s0], c->csf_v[s1], c->csf_v[s0], c->conv_v[s2], c->csf_v[s2], c->coef32[1],
+                            st));
+    LCK(c, launch_mom_rhs32(2, g, ph, c->u32, c->v32, c->w32, c->w2, c->mu32, c->fz32, c->conv_w[s1],
+                            c->conv_w[s0], c->csf_w[s1], c->csf_w[s0], c->conv_w[s2], c->csf_w[s2], c->coef32[2],
+                            st));
+  }
+  int s;
+  if ((s = momentum<float>(c, 0, c->coef32[0], c->x3f[0], c->prm.mom_u))) return s;
+  if ((s = momentum<float>(c, 1, c->coef32[1], c->x3f[1], c->prm.mom_v))) return s;
+  if ((s = momentum<float>(c, 2, c->coef32[2], c->x3f[2], c->prm.mom_w))) return s;
+  const float *u3 = c->x3f[0][c->x3_final[0]], *v3 = c->x3f[1][c->x3_final[1]], *w3 = c->x3f[2][c->x3_final[2]];
+  int its = 0, reason = 0;
+  double rn = 0.0, bn = 0.0;
+  {
+    PhaseScope ps(c, TPLS_T_PRESSURE);
+    LCK(c, launch_source(g, ph, u3, v3, w3, c->rhs_p, st));
+    if ((s = pressure_stage(c, u3, 1, &its, &rn, &bn, &reason))) return s;
+  }
+  {
+    PhaseScope ps(c, TPLS_T_PROJECT);
+    LCK(c, launch_project(g, ph, u3, v3, w3, c->pres, c->u_inlet, c->u2, c->v2, c->w2, st));
+    TCK(cudaMemcpyAsync(c->pres_old - XOFF, c->pres - XOFF, sizeof(double) * c->n_p, cudaMemcpyDeviceToDevice,
+                        st));
+  }
+  if (c->capturing) return TPLS_OK;
+  return finish_eager(c, its, rn, bn, reason);
+}
+
+// One step as a CUDA-graph launch; the graph of this history phase is
+// captured from the eager sequence on first use.
+static int step_graph(tpls_ctx *c) {
+  int s = prologue(c);
+  if (s) return s;
+  const int ph = c->phase;
+  if (!c->gexec[ph]) {
+    const long l0 = c->launches;
+    TCK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
+    c->capturing = true;
+    s = c->mixed ? step_once_mixed(c) : step_once(c);
+    c->capturing = false;
+    cudaGraph_t gr = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(c->st, &gr);
+    const long n = c->launches - l0;
+    c->launches = l0;
+    if (s != TPLS_OK || e != cudaSuccess) {
+      if (gr) cudaGraphDestroy(gr);
+      return s != TPLS_OK ? s : TPLS_ERR_CUDA_BASE + (int)e;
+    }
+    const cudaError_t ei = cudaGraphInstantiate(&c->gexec[ph], gr, 0);
+    cudaGraphDestroy(gr);
+    TCK(ei);
+    c->g_static[ph] = n;
+  }
+  TCK(cudaGraphLaunch(c->gexec[ph], c->st));
+  c->launches += c->g_static[ph];
+  c->phase = (ph + 1) % 3;
+  c->stats.steps_done++;
+  c->graph_pending = true;
+  return TPLS_OK;
+}
+
+// Reads the outcome of graph-launched solves (synchronises): last solve's
+// figures, the lowest reason since the previous read, and the CG-loop
+// kernels into the launch count.
+static int refresh_graph_stats(tpls_ctx *c) {
+  if (!c->graph_pending) return TPLS_OK;
+  int its, reason, worst;
+  double rn, bn, total;
+  TCK(poisson_read(c->ps, c->st, &its, &rn, &bn, &reason, &worst, &total));
+  TCK(poisson_reset_worst(c->ps, c->st));
   c->stats.p_its = its;
   c->stats.p_rnorm = rn;
   c->stats.p_bnorm = bn;
   c->stats.p_reason = reason;
-  c->stats.steps_done++;
-  if (reason < 0) return reason;
+  if (worst < c->stats.p_worst) c->stats.p_worst = worst;
+  c->launches += (long)(total - c->its_accounted) * c->g_body;
+  c->its_accounted = total;
+  c->graph_pending = false;
   return TPLS_OK;
 }
 
+static bool graph_path(const tpls_ctx *c) { return c->use_graphs && !c->timing; }
+
+// A pressure solve that reaches p_maxits (KSP_DIVERGED_ITS) does not stop
+// the run, as in the reference's time loop; the status of such a step is
+// returned after the remaining steps.  A NaN residual, an argument or a CUDA
+// error stops at the failing step (graph launches: at the end of the call).
 int tpls_step(tpls_ctx *c, int nsteps) {
   if (!c || nsteps < 0) return TPLS_ERR_ARG;
+  if (graph_path(c)) {
+    for (int n = 0; n < nsteps; n++) {
+      int s = step_graph(c);
+      if (s) return s;
+    }
+    TCK(cudaStreamSynchronize(c->st));
+    int s = refresh_graph_stats(c);
+    if (s) return s;
+    const int worst = c->stats.p_worst;
+    c->stats.p_worst = 0;
+    return worst < 0 ? worst : TPLS_OK;
+  }
+  int worst = TPLS_OK;
   for (int n = 0; n < nsteps; n++) {
-    int s = step_once(c);
+    int s = prologue(c);
+    if (s) return s;
+    s = c->mixed ? step_once_mixed(c) : step_once(c);
+    if (s == TPLS_KSP_DIVERGED_ITS) {
+      worst = s;
+      continue;
+    }
     if (s != TPLS_OK) return s;
   }
+  c->stats.p_worst = 0;
+  return worst;
+}
+
+int tpls_step_async(tpls_ctx *c, int nsteps) {
+  if (!c || nsteps < 0) return TPLS_ERR_ARG;
+  if (!graph_path(c)) return tpls_step(c, nsteps);
+  for (int n = 0; n < nsteps; n++) {
+    int s = step_graph(c);
+    if (s) return s;
+  }
+  return TPLS_OK;
+}
+
+int tpls_graphs_enable(tpls_ctx *c, int on) {
+  if (!c) return TPLS_ERR_ARG;
+  TCK(cudaStreamSynchronize(c->st));
+  int s = refresh_graph_stats(c);
+  if (s) return s;
+  c->use_graphs = (on != 0);
   return TPLS_OK;
 }
 
@@ -566,6 +854,10 @@ void *tpls_stream(tpls_ctx *c) { return c ? (void *)c->st : nullptr; }
 
 int tpls_get_stats(tpls_ctx *c, tpls_stats *out) {
   if (!c || !out) return TPLS_ERR_ARG;
+  {
+    int s = refresh_graph_stats(c);
+    if (s) return s;
+  }
   const Geo &g = c->g;
   dim3 grd((g.nx + 31) / 32, (g.ny + 3) / 4, g.nz);
   k_volume<<<grd, dim3(32, 4), 0, c->st>>>(g, c->ph, c->phi2, c->part);
@@ -579,6 +871,7 @@ int tpls_get_stats(tpls_ctx *c, tpls_stats *out) {
   c->stats.err_w = c->scal_host[SC_ERR_W];
   c->stats.liquid_volume = c->scal_host[SC_VOL] * c->prm.dx * c->prm.dy * c->prm.dz;
   *out = c->stats;
+  c->stats.p_worst = 0;
   return TPLS_OK;
 }
 
@@ -1012,8 +1305,9 @@ int tpls_pressure_solve(tpls_ctx *c, double *pres, const double *pres_old, const
   const double rt = (rtol && *rtol > 0) ? *rtol : c->prm.p_rtol;
   const int mi = (maxits && *maxits > 0) ? *maxits : c->prm.p_maxits;
   double bn = 0.0;
-  TCK(poisson_solve(c->ps, c->g, ph, R, U, c->scr_uin, PO, P, rt, mi, its, rnorm, &bn, reason, c->st,
+  TCK(poisson_solve(c->ps, c->g, ph, R, U, 0, c->scr_uin, PO, P, rt, mi, its, rnorm, &bn, reason, c->st,
                     &c->launches));
+  c->its_accounted += *its;
   TCK(d2h(c, pres, P, nz + 2));
   TCK(cudaStreamSynchronize(c->st));
   return (*reason < 0) ? *reason : TPLS_OK;

@@ -24,6 +24,14 @@ cudaError_t launch_advect(const Geo &g, const Phys &ph, const double *phi2,
 // exchange2d (mpi.f90:110) on one GPU: periodic copy of rows 0 and ny+1,
 // x = 0..nx+1, nzp planes.
 cudaError_t launch_exchange(const Geo &g, double *a, int nzp, cudaStream_t st);
+cudaError_t launch_exchange(const Geo &g, float *a, int nzp, cudaStream_t st);
+// FP32-mixed form: WENO5 faces and flux divergence in FP32 on FP32 copies
+// of phi, u, v, w; conv2_phi written in FP64.
+cudaError_t launch_advect(const Geo &g, const Phys &ph, const float *phi2,
+                          const float *u2, const float *v2, const float *w2,
+                          double *conv2_phi, cudaStream_t st);
+cudaError_t launch_to_float(const double *a, float *b, size_t n, cudaStream_t st);
+cudaError_t launch_to_double(const float *a, double *b, size_t n, cudaStream_t st);
 
 // two_phase_levelset.f90 / levelset.f90
 cudaError_t launch_ls_ab3(const Geo &g, const Phys &ph, const double *phi2,
@@ -39,6 +47,20 @@ cudaError_t launch_csf(const Geo &g, const Phys &ph, const double *phi3,
                        double *fx, double *fy, double *fz, cudaStream_t st);
 cudaError_t launch_visc(const Geo &g, const Phys &ph, const double *phi2,
                         double *mu, cudaStream_t st);
+// FP32-mixed form of the level-set kernels: status with D in FP32, the
+// redistancing iterations in FP32 (first reads the FP64 phi3 when pr64 is
+// given, last writes the FP64 state when out64 is given), CSF in FP32,
+// viscosity stored in FP32 (the Heaviside evaluated in FP64).
+cudaError_t launch_ls_status(const Geo &g, const Phys &ph, const double *phi3,
+                             float *D, signed char *flags, cudaStream_t st);
+cudaError_t launch_ls_iter32(const Geo &g, const Phys &ph, const double *pr64,
+                             const float *pr32, const float *D,
+                             const signed char *flags, double *out64,
+                             float *out32, double *err_part, cudaStream_t st);
+cudaError_t launch_csf(const Geo &g, const Phys &ph, const double *phi3,
+                       float *fx, float *fy, float *fz, cudaStream_t st);
+cudaError_t launch_visc(const Geo &g, const Phys &ph, const double *phi2,
+                        float *mu, cudaStream_t st);
 
 // momentum_allflux.f90 + main_ns_hybrid.F90:629-641,743-751: per component
 // conv2, csf2 (history) and the AB3/CN right-hand side.
@@ -50,6 +72,16 @@ cudaError_t launch_mom_rhs(int comp, const Geo &g, const Phys &ph,
                            const double *s0, double *conv2, double *csf2,
                            double *rhs, double *diff_out, double *coef,
                            cudaStream_t st);
+// FP32-mixed form: stencils on FP32 copies of u, v, w, mu and the CSF force,
+// right-hand side assembled in FP64 from the component's FP64 state x64,
+// coefficient records (8 floats per point) for the FP32 sweeps.
+cudaError_t launch_mom_rhs32(int comp, const Geo &g, const Phys &ph,
+                             const float *u2, const float *v2, const float *w2,
+                             const double *x64, const float *mu,
+                             const float *fcsf, const double *c1,
+                             const double *c0, const double *s1,
+                             const double *s0, double *conv2, double *csf2,
+                             float *coef, cudaStream_t st);
 // Standalone get_conv_all / get_diffusion_all (per-routine entries).
 cudaError_t launch_conv_diff(int comp, int want_conv, const Geo &g,
                              const Phys &ph, const double *u2,
@@ -80,9 +112,19 @@ cudaError_t launch_sor_c(int comp, const Geo &g, const Phys &ph, double *x,
                          const double *coef, const double *pres, int flg,
                          int iteration_time, int bc, int fuse_ghosts,
                          cudaStream_t st);
+cudaError_t launch_jacobi_c(int comp, const Geo &g, const Phys &ph,
+                            const float *xo, const float *coef,
+                            const double *pres, float *x, int fuse_ghosts,
+                            cudaStream_t st);
+cudaError_t launch_sor_c(int comp, const Geo &g, const Phys &ph, float *x,
+                         const float *coef, const double *pres, int flg,
+                         int iteration_time, int bc, int fuse_ghosts,
+                         cudaStream_t st);
 cudaError_t launch_bc(int comp, const Geo &g, const Phys &ph, double *x,
                       const double *pres, cudaStream_t st);
 cudaError_t launch_diff2(const Geo &g, const double *a, const double *b,
+                         int nzp, double *part, cudaStream_t st);
+cudaError_t launch_diff2(const Geo &g, const float *a, const float *b,
                          int nzp, double *part, cudaStream_t st);
 int diff2_blocks(const Geo &g, int nzp);
 
@@ -90,8 +132,16 @@ int diff2_blocks(const Geo &g, int nzp);
 cudaError_t launch_source(const Geo &g, const Phys &ph, const double *u3,
                           const double *v3, const double *w3, double *rhs_p,
                           cudaStream_t st);
+cudaError_t launch_source(const Geo &g, const Phys &ph, const float *u3,
+                          const float *v3, const float *w3, double *rhs_p,
+                          cudaStream_t st);
 cudaError_t launch_project(const Geo &g, const Phys &ph, const double *u3,
                            const double *v3, const double *w3,
+                           const double *p, const double *u_inlet,
+                           double *u_out, double *v_out, double *w_out,
+                           cudaStream_t st);
+cudaError_t launch_project(const Geo &g, const Phys &ph, const float *u3,
+                           const float *v3, const float *w3,
                            const double *p, const double *u_inlet,
                            double *u_out, double *v_out, double *w_out,
                            cudaStream_t st);

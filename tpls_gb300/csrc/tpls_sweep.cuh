@@ -1,0 +1,68 @@
+// tpls_sweep.cuh -- device helpers shared by the Crank-Nicolson sweep
+// kernels (boundary rows of main_ns_hybrid.F90:756-887 and the fused
+// periodic ghost-row copies), templated on the storage type of the
+// velocity being relaxed (double, or float in the FP32-mixed form).
+#pragma once
+#include "tpls_kernels.h"
+
+namespace tpls {
+
+struct Helm {
+  double ax2, ay2, az2;  // dt/(2 d^2)
+  double dtdx;           // dt/dx (u outlet condition)
+};
+
+// Write a value and, when ghost rows are fused (even ny), its periodic copy.
+template <typename T>
+__device__ __forceinline__ void put(const Geo &g, T *x, int i, int j, int k, T v, int fuse) {
+  x[TPLS_IDX(g, i, j, k)] = v;
+  if (fuse) {
+    if (j == g.ny) x[TPLS_IDX(g, i, 0, k)] = v;
+    if (j == 1) x[TPLS_IDX(g, i, g.ny + 1, k)] = v;
+  }
+}
+
+// u outlet, main_ns_hybrid.F90:768-776 (the pressure row index is the u row
+// index j, as written in the reference); evaluated in FP64.
+template <typename T>
+__device__ __forceinline__ T u_outlet(const Geo &g, const Helm &h, const double *P, T unm1, int j,
+                                      int k) {
+  const int nx = g.nx;
+  return (T)((double)unm1 + h.dtdx * (P[TPLS_IDX(g, nx + 1, j, k + 1)] +
+                                      P[TPLS_IDX(g, nx - 1, j, k + 1)] -
+                                      2.0 * P[TPLS_IDX(g, nx, j, k + 1)]));
+}
+
+// Post-sweep boundary rows (main_ns_hybrid.F90:784-799 u, :826-836 v,
+// :860-879 w), written by the thread that owns the first / last x pair:
+// the inlet copy x(0) = x(1), for u the pressure outlet x(nx) and the
+// fictitious point x(nx+1) = 0, for v and w the outlet copy.  A value of the
+// colour not relaxed in this half-sweep is read (it is final already).
+template <typename T>
+__device__ __forceinline__ void sor_bc(int comp, const Geo &g, const Helm &h, T *x, const double *P,
+                                       int i2, int i, int iend, T v, int j, int k, int fuse) {
+  if (i2 == 0) {
+    const T v1 = (i == 1) ? v : x[TPLS_IDX(g, 1, j, k)];
+    put(g, x, 0, j, k, v1, fuse);
+  }
+  if (i2 == (iend - 1) / 2) {
+    const T ve = (i == iend) ? v : x[TPLS_IDX(g, iend, j, k)];
+    if (comp == 0) {
+      put(g, x, g.nx, j, k, u_outlet(g, h, P, ve, j, k), fuse);
+      put(g, x, g.nx + 1, j, k, (T)0, fuse);
+    } else {
+      put(g, x, g.nx + 1, j, k, ve, fuse);
+    }
+  }
+}
+
+static inline Helm helm_of(const Phys &ph) {
+  Helm h;
+  h.ax2 = (ph.dt / (ph.dx * ph.dx)) / 2.0;
+  h.ay2 = (ph.dt / (ph.dy * ph.dy)) / 2.0;
+  h.az2 = (ph.dt / (ph.dz * ph.dz)) / 2.0;
+  h.dtdx = ph.dt / ph.dx;
+  return h;
+}
+
+}  // namespace tpls
