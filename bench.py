@@ -126,7 +126,8 @@ def run_gpu(args, ws, rank, local) -> dict | None:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     w = WORKLOADS[args.config]
-    params, uin, st = make_case(args.config, p_rtol=args.p_rtol)
+    precision = _precision(args)
+    params, uin, st = make_case(args.config, p_rtol=args.p_rtol, precision=precision)
     nx, ny, nz = w.nx, w.ny, w.nz
     cells = nx * ny * nz
     g = TplsGpu(nx, ny, nz, params, uin)
@@ -137,13 +138,12 @@ def run_gpu(args, ws, rank, local) -> dict | None:
         raise SystemExit(f"tpls_step returned {rc} during warm-up")
     ext = torch.cuda.ExternalStream(g.stream_ptr())
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    g.timing_enable(True)
-    g.timing_read(reset=True)
     l0 = g.kernel_launches()
     sampler = ClockSampler(local) if rank == 0 else None
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
+    # timed region: tpls_step, one CUDA-graph launch per step
     ev0.record(ext)
     rc = g.step(args.steps)
     ev1.record(ext)
@@ -155,9 +155,16 @@ def run_gpu(args, ws, rank, local) -> dict | None:
     clocks = sampler.stop() if sampler else None
     ms = ev0.elapsed_time(ev1)
     launches = g.kernel_launches() - l0
+    stats = g.stats()
+    # phase breakdown: a separate, shorter pass launched kernel by kernel
+    # with CUDA events between phases (not part of the timed region)
+    nph = max(1, min(args.steps, args.phase_steps))
+    g.timing_enable(True)
+    g.timing_read(reset=True)
+    if g.step(nph) != 0:
+        raise SystemExit("tpls_step failed in the phase-timing pass")
     phases = g.timing_read(reset=True)
     g.timing_enable(False)
-    stats = g.stats()
     if dist:
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -208,7 +215,8 @@ def run_gpu(args, ws, rank, local) -> dict | None:
     # (k_sor_odd_c2), timed launch by launch on the library's stream
     sor_ms, sor_l = phases["sor_odd"]
     dominant = "sor_odd_c2"
-    per_launch_b = sor_b / sor_n
+    esz = 4.0 if precision == 1 else 8.0
+    per_launch_b = sor_b / sor_n * (esz / 8.0)
     avg_ms = sor_ms / max(sor_l, 1)
     achieved = per_launch_b / (avg_ms / 1e3) / 1e9
     traffic = None
@@ -232,12 +240,15 @@ def run_gpu(args, ws, rank, local) -> dict | None:
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f64",
+        "dtype": "f64" if precision == 0 else "f32 stencils/sweeps/smoothing + f64 state/dots/coarse solve",
         "data": "synthetic: seeded two-layer channel (4-mode interface, +-1e-3 velocity noise), no dataset",
         "config": {"workload": w.name, "grid": [nx, ny, nz], "cells": cells, "m": w.m, "re": w.re,
                    "mom_uvw": params.mom_u, "levelset": params.levelset, "p_rtol": params.p_rtol,
-                   "precision": "fp64", "parallelism": f"{ws} independent replica(s), no sharding",
-                   "l2": "working set ~3 GB per step >> 129 MB L2 (no flush needed)",
+                   "precision": "fp64" if precision == 0 else "fp32-mixed",
+                   "parallelism": f"{ws} independent replica(s), no sharding",
+                   "l2": f"working set ~{cells * 500 / 1e9:.0f} GB per step >> 129 MB L2 (no flush needed)",
+                   "launch": "one CUDA graph per step (device-side WHILE node for the pressure CG)",
+                   "grid_geometry": "cubic cells dx=dy=dz=1/nz (the reference's initialisation grid)",
                    "baseline_metric": BASELINE_METRIC},
         "e2e": {"value": e2e, "unit": "cell-steps/s", "h2d_bytes_per_step": bi, "d2h_bytes_per_step": bi,
                 "steps": ke, "path": "tpls_set_field x20 -> tpls_step(1) -> tpls_get_field x20 per step"},
@@ -247,7 +258,8 @@ def run_gpu(args, ws, rank, local) -> dict | None:
                      "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": traffic, "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback",
                      "note": "FP64 kernels on GB300 are FP64-pipe bound (1.01 TFLOP/s measured), not HBM bound"},
-        "phases_ms_per_step": {k: v[0] / args.steps for k, v in phases.items()},
+        "phases_ms_per_step": {k: v[0] / nph for k, v in phases.items()},
+        "phases_note": f"eager pass of {nph} steps with events between phases",
         "pressure": {"its_last": stats["p_its"], "reason_last": stats["p_reason"]},
         "cpu_baseline": cpu,
         "clocks": clocks,
@@ -256,6 +268,167 @@ def run_gpu(args, ws, rank, local) -> dict | None:
         dist.destroy_process_group()
     g.close()
     return out
+
+
+def run_batch(args, ws, rank, local) -> dict | None:
+    """The batched workload: 48 seeded instances of uneven grids, FP32-mixed,
+    all advanced by one CUDA-graph launch per batch step; compared with the
+    same instances run one by one."""
+    import torch
+    from tpls_gb300.api import STATE_FIELDS
+    from tpls_gb300.batch import Batch, draw_instances, open_instance, run_one_by_one
+
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    precision = _precision(args)
+    insts = draw_instances(args.instances)
+    cells = sum(i.cells for i in insts)
+    # e2e: states uploaded from host, the batch run, states downloaded
+    hosts = []
+    members = []
+    for inst in insts:
+        g = open_instance(inst, precision)
+        hosts.append(g.get_state())
+        members.append(g)
+    b = Batch(members)
+    if b.step(args.warmup) != 0:
+        raise SystemExit("batch warm-up failed")
+    ext = torch.cuda.ExternalStream(members[0].stream_ptr())
+    sampler = ClockSampler(local) if rank == 0 else None
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    rc = b.step(args.steps)
+    torch.cuda.synchronize()
+    sec = time.perf_counter() - t0
+    if dist:
+        dist.barrier()
+    clocks = sampler.stop() if sampler else None
+    if rc != 0:
+        raise SystemExit(f"batch step returned {rc}: not a valid measurement")
+    launches = sum(m.kernel_launches() for m in members)
+    # e2e through the API: upload every member's state from host, run, download
+    bi = sum(sum(a.nbytes for a in h.values()) for h in hosts)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    for m, h in zip(members, hosts):
+        m.set_state(h)
+    if b.step(args.steps) != 0:
+        raise SystemExit("batch e2e run failed")
+    outs = [m.get_state() for m in members]
+    e2e_sec = time.perf_counter() - t1
+    del outs
+    b.close()
+    for m in members:
+        m.close()
+    del ext
+    solo = None
+    if not args.no_one_by_one:
+        solo = run_one_by_one(insts, args.steps, precision, warmup=args.warmup)
+    if dist:
+        t = torch.tensor([sec, e2e_sec], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        sec, e2e_sec = float(t[0]), float(t[1])
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return None
+    value = ws * cells * args.steps / sec
+    out = {
+        "metric": "cell-steps/s",
+        "value": value,
+        "unit": "cell-steps/s",
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": sec * 1e3 / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64" if precision == 0 else "f32 stencils/sweeps/smoothing + f64 state/dots/coarse solve",
+        "data": "synthetic: 48 seeded channel instances, no dataset",
+        "config": {"workload": f"D: {len(insts)} batched instances, uneven grids, "
+                               f"{'fp64' if precision == 0 else 'fp32-mixed'}",
+                   "instances": len(insts), "total_cells": cells,
+                   "grids": [[i.nx, i.ny, i.nz] for i in insts],
+                   "launch": "one CUDA graph per batch step (every member's step as a branch)",
+                   "timing": "host wall clock around synchronised batch steps",
+                   "l2": f"working set ~{cells * 300 / 1e9:.0f} GB per step >> 129 MB L2",
+                   "baseline_metric": BASELINE_METRIC},
+        "jobs_per_s": ws * len(insts) / sec,
+        "e2e": {"value": ws * cells * args.steps / e2e_sec, "unit": "cell-steps/s",
+                "h2d_bytes_per_step": bi / args.steps, "d2h_bytes_per_step": bi / args.steps,
+                "path": "tpls_set_field x20 per member -> tpls_batch_step(steps) -> tpls_get_field x20 per member"},
+        "gpu_launches": launches,
+        "one_by_one": None if solo is None else {
+            "seconds": solo["seconds"], "value": cells * args.steps / solo["seconds"],
+            "batched_speedup": solo["seconds"] / sec},
+        "roofline": None,
+        "cpu_baseline": None,
+        "clocks": clocks,
+    }
+    if dist:
+        dist.destroy_process_group()
+    return out
+
+
+def run_serve(args, ws, rank, local) -> dict | None:
+    """The served job stream: the first --jobs jobs of the seeded 2000-job
+    Poisson stream (arrival rate --rate jobs/s), admitted under a 160 GB
+    footprint budget, run once in the FP32-mixed form and once in FP64."""
+    import torch
+    from tpls_gb300.serve import GpuBackend, Server, draw_jobs, summarize
+    torch.cuda.set_device(local)
+    if rank != 0:
+        return None
+    forms = {}
+    clocks = None
+    for name, prec in (("fp32_mixed", 1), ("fp64", 0)):
+        jobs = draw_jobs(2000, rate=args.rate, precision=prec)[:args.jobs]
+        sampler = ClockSampler(local)
+        srv = Server(GpuBackend(), budget_bytes=160e9, max_active=64)
+        res = srv.run(jobs)
+        c = sampler.stop()
+        clocks = clocks or c
+        sm = summarize(res)
+        sm["peak_admitted_gb"] = srv.peak_bytes / 1e9
+        sm["peak_active_jobs"] = srv.peak_active
+        sm["clocks"] = c
+        forms[name] = sm
+    mx = forms["fp32_mixed"]
+    return {
+        "metric": "jobs/s",
+        "value": mx["jobs_per_s"],
+        "unit": "jobs/s",
+        "n_gpus": ws,
+        "steps": sum(j.steps for j in draw_jobs(2000, rate=args.rate)[:args.jobs]),
+        "warmup": 0,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "fp32-mixed (fp64 form alongside)",
+        "data": "synthetic: seeded Poisson job stream, no dataset",
+        "config": {"workload": f"E: first {args.jobs} jobs of the seeded 2000-job stream, Poisson arrivals at "
+                               f"{args.rate} jobs/s, grids up to 384x192x192, budgets 50-1000 steps, 160 GB "
+                               f"admission, snapshots every 50 steps",
+                   "timing": "host wall clock from the first arrival to the last completion",
+                   "baseline_metric": BASELINE_METRIC},
+        "serve": forms,
+        "p50_latency_s": mx["p50_latency_s"],
+        "p99_latency_s": mx["p99_latency_s"],
+        "cell_steps_per_s": mx["cell_steps_per_s"],
+        "clocks": clocks,
+    }
+
+
+def _precision(args) -> int:
+    if args.precision is not None:
+        return 0 if args.precision == "fp64" else 1
+    return 1 if args.config in ("C", "D") else 0
 
 
 def cpu_baseline(config: str, seconds: float) -> dict:
@@ -290,18 +463,24 @@ def run_reference(args, ws, rank) -> dict | None:
     from tpls_gb300.channel import WORKLOADS, make_case
     cores = os.cpu_count() or 1
     set_threads(cores)
-    w = WORKLOADS[args.config]
-    params, uin, st = make_case(args.config, p_rtol=args.p_rtol)
+    w = WORKLOADS[args.config if args.config in WORKLOADS else "B"]
+    params, uin, st = make_case(w, p_rtol=args.p_rtol)
     o = Oracle(w.nx, w.ny, w.nz, params, uin)
     o.set_state(st)
-    o.step(args.warmup)
+    o.step(min(args.warmup, 1))
+    # bounded sample: up to --steps steps or --ref-seconds of CPU time
+    n = 0
     t0 = time.perf_counter()
-    o.step(args.steps)
+    while n < args.steps:
+        o.step(1)
+        n += 1
+        if time.perf_counter() - t0 > args.ref_seconds:
+            break
     dt = time.perf_counter() - t0
     o.close()
-    v = w.nx * w.ny * w.nz * args.steps / dt
+    v = w.nx * w.ny * w.nz * n / dt
     return {"impl": "reference", "metric": "cell-steps/s", "value": v, "unit": "cell-steps/s", "n_gpus": ws,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps,
+            "steps": n, "warmup": min(args.warmup, 1), "ms_per_step": dt * 1e3 / n,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic: seeded two-layer channel (4-mode interface, +-1e-3 velocity noise), no dataset",
             "config": {"workload": w.name, "grid": [w.nx, w.ny, w.nz], "mom_uvw": params.mom_u,
@@ -309,7 +488,8 @@ def run_reference(args, ws, rank) -> dict | None:
                        "implementation": "C restatement of the reference's Fortran routines (oracle/), OpenMP; "
                                          "the Fortran/MPI/PETSc reference cannot be built here"},
             "cpu_baseline": {"value": v, "unit": "cell-steps/s", "cores": cores, "kind": "port",
-                             "sample": f"{args.steps} full timesteps after {args.warmup} warm-up"},
+                             "sample": f"{n} full timesteps (of {args.steps} requested, bounded to "
+                                       f"{args.ref_seconds:.0f} s) after {min(args.warmup, 1)} warm-up"},
             "e2e": {"value": v, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
@@ -324,12 +504,24 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default=None,
+                    help="default: fp64 for A/B/M, mixed for C/D")
+    ap.add_argument("--phase-steps", type=int, default=20)
+    ap.add_argument("--ref-seconds", type=float, default=120.0)
+    ap.add_argument("--instances", type=int, default=48)
+    ap.add_argument("--no-one-by-one", action="store_true")
+    ap.add_argument("--jobs", type=int, default=16)
+    ap.add_argument("--rate", type=float, default=1.0)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3  # timing rule: at least 3 warm-up steps
     ws, rank, local = _dist()
     if args.impl == "reference":
         out = run_reference(args, ws, rank)
+    elif args.config == "D":
+        out = run_batch(args, ws, rank, local)
+    elif args.config == "E":
+        out = run_serve(args, ws, rank, local)
     else:
         out = run_gpu(args, ws, rank, local)
     if out is not None:

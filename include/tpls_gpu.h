@@ -119,6 +119,39 @@ int tpls_step(tpls_ctx *ctx, int nsteps);
  * the solves' outcome is read by tpls_get_stats (p_worst) or tpls_step.
  * With graphs disabled or timing enabled it runs tpls_step. */
 int tpls_step_async(tpls_ctx *ctx, int nsteps);
+/* ---- job-serving helpers (no counterpart in the reference) ------------ */
+/* Device bytes tpls_gpu_create allocates for this grid and precision (each
+ * allocation rounded to the allocator's 2 MiB unit), or -1 for bad
+ * arguments.  Host-only: used for admission before anything is allocated. */
+long long tpls_footprint_bytes(int nx, int ny, int nz, int precision);
+/* 1 when every step enqueued on the context has finished, 0 while work is
+ * pending, or an error status.  Does not block. */
+int tpls_query(tpls_ctx *ctx);
+/* Interface height h(x, y) of the current phi: for each column (i, j),
+ * i = 1..nx, j = 1..ny, the lowest z where phi changes sign between
+ * consecutive cell centres, by linear interpolation (cell centres at
+ * z_k = (k - 1/2) dz); columns without a sign change get -1.  h_host holds
+ * nx*ny doubles, i fastest. */
+int tpls_interface_height(tpls_ctx *ctx, double *h_host);
+
+/* ---- batches (no counterpart in the reference, which runs one channel
+ * per MPI job) ------------------------------------------------------------
+ * n independent channels advanced in lockstep: each batch step is ONE
+ * CUDA-graph launch holding every member's step as a parallel branch (the
+ * members' pressure iterations as device-side WHILE nodes), so the
+ * instances' kernels share the GPU concurrently.  Members must be at the
+ * same history phase (created together, or stepped the same number of
+ * times) and must not be stepped on their own while in a batch.  The
+ * members keep their state, fields and stats; the batch only launches. */
+typedef struct tpls_batch tpls_batch;
+int tpls_batch_create(tpls_ctx *const *ctxs, int n, tpls_batch **out);
+int tpls_batch_destroy(tpls_batch *b);
+/* Enqueue nsteps batch steps (one graph launch each) without waiting. */
+int tpls_batch_step_async(tpls_batch *b, int nsteps);
+/* The same, then wait; returns the lowest pressure reason of any member
+ * (0 when every solve converged) or an error. */
+int tpls_batch_step(tpls_batch *b, int nsteps);
+
 /* Graph mode on (1, default) or off (0: every step launched kernel by
  * kernel, the pressure iterations driven by the host).  Both give
  * bit-identical results. */

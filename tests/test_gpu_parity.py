@@ -178,26 +178,52 @@ def test_pressure_solve_reference_rtol(setup):
 
 @pytest.mark.parametrize("size", list(SIZES))
 def test_full_steps_match_oracle(size):
-    """Whole timesteps on device-resident state, compared after every step;
-    the pressure solve runs to 1e-13 so u, v, w can match to 1e-11."""
+    """Whole timesteps on device-resident state, per step: before every step
+    the GPU context is loaded with the oracle's state, both take one step,
+    and phi, u, v, w must match to 1e-11 (pressure solved to 1e-14 so the
+    solve's own tolerance is not what is measured)."""
     nx, ny, nz = SIZES[size]
-    params, uin, st = make_case("A", nx=nx, ny=ny, nz=nz, p_rtol=1e-13, p_maxits=200)
+    params, uin, st = make_case("A", nx=nx, ny=ny, nz=nz, p_rtol=1e-14, p_maxits=400)
     o = Oracle(nx, ny, nz, params, uin)
     o.set_state(st)
     g = TplsGpu(nx, ny, nz, params, uin)
-    g.set_state(st)
     rows = (slice(None), slice(1, ny + 1), slice(None))
-    for step in range(3):
+    for step in range(4):
+        g.set_state(o.get_state())
         o.step(1)
         g.step(1)
         for k in ("PHI2", "U2", "V2", "W2"):
             e = relmax(g.get_field(k), o.get_field(k), rows)
             assert e < TOL, (step, k, e)
-        dp = g.get_field("PRES") - o.get_field("PRES")
-        assert np.max(np.abs(dp)) <= 1e-9 * np.max(np.abs(o.get_field("PRES"))), step
-    so, sg = o.stats(), g.stats()
-    assert abs(sg["liquid_volume"] - so["liquid_volume"]) <= 1e-12 * abs(so["liquid_volume"])
-    assert sg["p_reason"] == 2
+        dp = (g.get_field("PRES") - o.get_field("PRES"))[1:nx + 1, 1:ny + 1, 1:nz + 1]
+        assert np.max(np.abs(dp)) <= 1e-11 * np.max(np.abs(o.get_field("PRES"))), step
+        so, sg = o.stats(), g.stats()
+        assert abs(sg["liquid_volume"] - so["liquid_volume"]) <= 1e-12 * abs(so["liquid_volume"])
+        assert sg["p_reason"] == 2
+    g.close()
+
+
+@pytest.mark.parametrize("size", list(SIZES))
+def test_free_running_steps_track_oracle(size):
+    """Both sides stepping on their own state for 4 steps.  The reference's
+    step amplifies rounding-level differences: a 1e-15 relative perturbation
+    of the oracle's own input grows to ~3e-12 in v and ~4e-13 in w after one
+    step on the 64x32x48 channel, and the GPU and oracle pressure solves
+    differ at 1e-13, so the bound here is 1e-9 (the per-step parity above is
+    the 1e-11 check)."""
+    nx, ny, nz = SIZES[size]
+    params, uin, st = make_case("A", nx=nx, ny=ny, nz=nz, p_rtol=1e-14, p_maxits=400)
+    o = Oracle(nx, ny, nz, params, uin)
+    o.set_state(st)
+    g = TplsGpu(nx, ny, nz, params, uin)
+    g.set_state(st)
+    rows = (slice(None), slice(1, ny + 1), slice(None))
+    for step in range(4):
+        o.step(1)
+        g.step(1)
+        for k in ("PHI2", "U2", "V2", "W2"):
+            e = relmax(g.get_field(k), o.get_field(k), rows)
+            assert e < 1e-9, (step, k, e)
     g.close()
 
 

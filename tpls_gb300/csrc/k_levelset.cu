@@ -62,7 +62,7 @@ cudaError_t launch_ls_ab3(const Geo &g, const Phys &ph, const double *phi2,
 // indicator istatus (bit 0) and sign(phi)+1 (bits 1-2); D and flags are 0
 // outside the interior.
 template <typename T>
-__global__ void k_ls_status(Geo g, T h, const double *__restrict__ phi, T *__restrict__ D,
+__global__ void k_ls_status(Geo g, double h, const double *__restrict__ phi, T *__restrict__ D,
                             signed char *__restrict__ flags) {
   const int i = blockIdx.x * LS_BX + threadIdx.x, j = blockIdx.y * LS_BY + threadIdx.y;
   const int k = blockIdx.z;
@@ -73,21 +73,24 @@ __global__ void k_ls_status(Geo g, T h, const double *__restrict__ phi, T *__res
     flags[c] = 0;
     return;
   }
-  const T p = (T)phi[c];
-  const T pxp = (T)phi[c + 1], pxm = (T)phi[c - 1], pyp = (T)phi[c + g.sy], pym = (T)phi[c - g.sy];
-  const T pzp = (T)phi[c + g.sz], pzm = (T)phi[c - g.sz];
-  const int sgn = (p < (T)0) ? -1 : ((p > (T)0) ? 1 : 0);
-  const T mn = fmin(fmin(fmin(p * pxp, p * pxm), fmin(p * pyp, p * pym)), fmin(p * pzp, p * pzm));
-  const int st = (mn <= (T)0) ? 1 : 0;
-  T d = (T)0;
+  // FP64 in both forms: the status flags are discrete decisions, so the
+  // FP32-mixed form takes them from the same arithmetic as the FP64 form
+  // and only stores D in FP32.
+  const double p = phi[c];
+  const double pxp = phi[c + 1], pxm = phi[c - 1], pyp = phi[c + g.sy], pym = phi[c - g.sy];
+  const double pzp = phi[c + g.sz], pzm = phi[c - g.sz];
+  const int sgn = (p < 0.0) ? -1 : ((p > 0.0) ? 1 : 0);
+  const double mn = fmin(fmin(fmin(p * pxp, p * pxm), fmin(p * pyp, p * pym)), fmin(p * pzp, p * pzm));
+  const int st = (mn <= 0.0) ? 1 : 0;
+  double d = 0.0;
   if (st) {
-    const T gx = pxp - pxm, gy = pyp - pym, gz = pzp - pzm;
-    const T b1 = sqrt(gx * gx + gy * gy + gz * gz) * (T)0.5;
-    T mx = fmax(fmax(fabs(pxp - p), fabs(pxm - p)), fmax(fabs(pyp - p), fabs(pym - p)));
+    const double gx = pxp - pxm, gy = pyp - pym, gz = pzp - pzm;
+    const double b1 = sqrt(gx * gx + gy * gy + gz * gz) * 0.5;
+    double mx = fmax(fmax(fabs(pxp - p), fabs(pxm - p)), fmax(fabs(pyp - p), fabs(pym - p)));
     mx = fmax(fmax(mx, fmax(fabs(pzp - p), fabs(pzm - p))), fmax(b1, h));
     d = h * p / mx;
   }
-  D[c] = d;
+  D[c] = (T)d;
   flags[c] = (signed char)(st | ((sgn + 1) << 1));
 }
 
@@ -98,7 +101,7 @@ cudaError_t launch_ls_status(const Geo &g, const Phys &ph, const double *phi3,
 }
 cudaError_t launch_ls_status(const Geo &g, const Phys &ph, const double *phi3, float *D, signed char *flags,
                              cudaStream_t st) {
-  k_ls_status<float><<<full_grid(g, g.nz + 2), dim3(LS_BX, LS_BY), 0, st>>>(g, (float)ph.dx, phi3, D, flags);
+  k_ls_status<float><<<full_grid(g, g.nz + 2), dim3(LS_BX, LS_BY), 0, st>>>(g, ph.dx, phi3, D, flags);
   return cudaGetLastError();
 }
 
@@ -237,9 +240,10 @@ __device__ __forceinline__ F3 csf_point(const Geo &g, const Phys &ph, double max
     const double *p;
     __device__ T operator[](int q) const { return (T)p[q]; }
   } fi{fi0};
-  const T p = fi[c];
+  const double p64 = fi0[c];
   F3 r = {0.0, 0.0, 0.0};
-  if ((double)p < -ph.sw || (double)p > ph.sw) return r;
+  if (p64 < -ph.sw || p64 > ph.sw) return r;  // band decision in FP64 in both forms
+  const T p = (T)p64;
   const int sy = g.sy, sz = g.sz;
   const T rdx = (T)(1.0 / ph.dx), rdy = (T)(1.0 / ph.dy), rdz = (T)(1.0 / ph.dz);
   const T r2dx = (T)0.5 * rdx, r2dy = (T)0.5 * rdy, r2dz = (T)0.5 * rdz, two = (T)2;
@@ -320,7 +324,10 @@ cudaError_t launch_csf(const Geo &g, const Phys &ph, const double *phi3,
 cudaError_t launch_csf(const Geo &g, const Phys &ph, const double *phi3, float *fx, float *fy, float *fz,
                        cudaStream_t st) {
   const double mk = 1.0 / fmin(fmin(ph.dx, ph.dy), ph.dz);
-  k_csf<float, float><<<full_grid(g, g.nz + 2), dim3(LS_BX, LS_BY), 0, st>>>(g, ph, mk, phi3, fx, fy, fz);
+  // curvature stays FP64: its second differences of phi (~dx^2 |phi''|)
+  // would lose ~1e-3 of their value to FP32 cancellation, a coherent error
+  // in the surface-tension force at the interface; the force is stored FP32
+  k_csf<double, float><<<full_grid(g, g.nz + 2), dim3(LS_BX, LS_BY), 0, st>>>(g, ph, mk, phi3, fx, fy, fz);
   return cudaGetLastError();
 }
 

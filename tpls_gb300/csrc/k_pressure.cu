@@ -755,6 +755,31 @@ void poisson_destroy(PoissonSolver *S) {
 
 int poisson_levels(const PoissonSolver *S) { return (int)S->lv.size(); }
 
+size_t poisson_footprint(const Geo &g, int fp32, size_t (*rnd)(size_t)) {
+  // the level sizes poisson_create builds, without allocating
+  const size_t esz = fp32 ? sizeof(float) : sizeof(double);
+  size_t tot = 0;
+  int nx = g.nx, ny = g.ny, nz = g.nz, l = 0;
+  while (true) {
+    const size_t n = (size_t)nx * ny * nz;
+    tot += (l > 0 ? 5 : 4) * rnd(esz * n) + rnd(esz * 3 * nz * 2);
+    if (n <= 512) {
+      tot += rnd(sizeof(double) * n * n);
+      break;
+    }
+    const int cx = (nx % 2 == 0 && nx >= 4), cy = (ny % 2 == 0 && ny >= 4), cz = (nz % 2 == 0 && nz >= 4);
+    if (!cx && !cy && !cz) break;
+    nx = cx ? nx / 2 : nx;
+    ny = cy ? ny / 2 : ny;
+    nz = cz ? nz / 2 : nz;
+    l++;
+  }
+  const size_t N = (size_t)g.nx * g.ny * g.nz;
+  tot += 6 * rnd(sizeof(double) * N) + rnd(sizeof(double) * (size_t)g.ny * g.nz);
+  tot += rnd(sizeof(double) * 3 * 1216) + rnd(sizeof(unsigned)) + rnd(sizeof(double) * S_COUNT);
+  return tot;
+}
+
 template <typename R>
 static LevArgs<R> largs(const PLevel &L) {
   LevArgs<R> a;

@@ -46,6 +46,7 @@ struct tpls_ctx {
   float *coef32[3];
   float *x3f[3][2];
   double *x3d = nullptr;  // FP64 view of u3/v3/w3 for tpls_get_field / tpls_set_field
+  double *hbuf = nullptr; // interface height (nx*ny)
   size_t n_p, n_uv, n_w;  // elements of each allocation (incl. pitch and padding)
   double *part, *scal, *scal_host;
   size_t part_len;
@@ -364,6 +365,12 @@ static int create_impl(int nx, int ny, int nz, const tpls_params *prm, const dou
     c->u_inlet = (double *)b;
     TCK(cudaMemcpy(c->u_inlet, u_inlet, sizeof(double) * nz, cudaMemcpyHostToDevice));
   }
+  {
+    void *b = nullptr;
+    TCK(cudaMalloc(&b, sizeof(double) * (size_t)nx * ny));
+    c->allocs.push_back(b);
+    c->hbuf = (double *)b;
+  }
   c->part_len = (size_t)ls_iter_blocks(c->g);
   size_t d2 = (size_t)diff2_blocks(c->g, nz + 1);
   if (d2 > c->part_len) c->part_len = d2;
@@ -384,6 +391,52 @@ static int create_impl(int nx, int ny, int nz, const tpls_params *prm, const dou
   memset(&c->stats, 0, sizeof(c->stats));
   TCK(cudaDeviceSynchronize());
   return TPLS_OK;
+}
+
+static size_t round_alloc(size_t b) {  // device allocations come in 2 MiB units
+  const size_t u = (size_t)2 << 20;
+  return (b + u - 1) / u * u;
+}
+
+long long tpls_footprint_bytes(int nx, int ny, int nz, int precision) {
+  if (nx < 4 || ny < 3 || nz < 4) return -1;
+  if (precision != TPLS_PREC_FP64 && precision != TPLS_PREC_FP32_MIXED) return -1;
+  const size_t px = (size_t)((XOFF + nx + 2) + 3) / 4 * 4;
+  const size_t np = px * (ny + 2) * (nz + 2) + 8, nuv = px * (ny + 2) * nz + 8, nw = px * (ny + 2) * (nz + 1) + 8;
+  const size_t nmu = px * (ny + 4) * (nz + 2) + 8;
+  const size_t nrec = (size_t)8 * px * (ny + 2);
+  const size_t D = sizeof(double), F = sizeof(float);
+  size_t t = 8 * round_alloc(D * np) + 14 * round_alloc(D * nuv) + 7 * round_alloc(D * nw);
+  if (precision == TPLS_PREC_FP64) {
+    t += 5 * round_alloc(D * np) + 4 * round_alloc(D * nuv) + 2 * round_alloc(D * nw);
+    t += 2 * round_alloc(D * nrec * nz) + round_alloc(D * nrec * (nz + 1)) + round_alloc(D * nmu);
+  } else {
+    t += 7 * round_alloc(F * np) + 6 * round_alloc(F * nuv) + 3 * round_alloc(F * nw);
+    t += 2 * round_alloc(F * nrec * nz) + round_alloc(F * nrec * (nz + 1)) + round_alloc(F * nmu);
+    t += round_alloc(D * nw);
+  }
+  t += round_alloc(px * (ny + 2) * (nz + 2) + 64) + round_alloc(D * nz) + round_alloc(D * nx * ny);
+  Geo g;
+  g.nx = nx;
+  g.ny = ny;
+  g.nz = nz;
+  g.sy = (int)px;
+  g.sz = (int)(px * (ny + 2));
+  g.szm = (int)(px * (ny + 4));
+  size_t part = (size_t)ls_iter_blocks(g);
+  const size_t d2 = (size_t)diff2_blocks(g, nz + 1);
+  if (d2 > part) part = d2;
+  t += round_alloc(D * part) + round_alloc(D * SC_N);
+  t += poisson_footprint(g, precision == TPLS_PREC_FP32_MIXED, round_alloc);
+  return (long long)t;
+}
+
+int tpls_query(tpls_ctx *c) {
+  if (!c) return TPLS_ERR_ARG;
+  const cudaError_t e = cudaStreamQuery(c->st);
+  if (e == cudaSuccess) return 1;
+  if (e == cudaErrorNotReady) return 0;
+  return TPLS_ERR_CUDA_BASE + (int)e;
 }
 
 int tpls_gpu_create(int nx, int ny, int nz, const tpls_params *prm, const double *u_inlet,
@@ -803,6 +856,172 @@ int tpls_graphs_enable(tpls_ctx *c, int on) {
   int s = refresh_graph_stats(c);
   if (s) return s;
   c->use_graphs = (on != 0);
+  return TPLS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Batches: independent channels advanced in lockstep by one CUDA-graph launch
+// per step.  The batch graph is the fork of every member's step (captured
+// from each member's own stream, the members' pressure loops as WHILE
+// nodes) joined back into the batch stream, so the instances' kernels run
+// concurrently under one launch.  One graph per history phase.
+}  // extern "C"
+
+struct tpls_batch {
+  std::vector<tpls_ctx *> m;
+  cudaStream_t st = nullptr;
+  cudaEvent_t fork = nullptr, done = nullptr;
+  std::vector<cudaEvent_t> join;
+  cudaGraphExec_t gexec[3] = {nullptr, nullptr, nullptr};
+  std::vector<long> n_static[3];  // kernels per member outside the CG loop
+};
+
+extern "C" {
+
+int tpls_batch_destroy(tpls_batch *b) {
+  if (!b) return TPLS_OK;
+  if (b->st) cudaStreamSynchronize(b->st);
+  for (cudaGraphExec_t ge : b->gexec)
+    if (ge) cudaGraphExecDestroy(ge);
+  for (cudaEvent_t e : b->join) cudaEventDestroy(e);
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->done) cudaEventDestroy(b->done);
+  if (b->st) cudaStreamDestroy(b->st);
+  delete b;
+  return TPLS_OK;
+}
+
+int tpls_batch_create(tpls_ctx *const *ctxs, int n, tpls_batch **out) {
+  if (!ctxs || n <= 0 || !out) return TPLS_ERR_ARG;
+  *out = nullptr;
+  for (int q = 0; q < n; q++) {
+    if (!ctxs[q]) return TPLS_ERR_ARG;
+    for (int r = 0; r < q; r++)
+      if (ctxs[r] == ctxs[q]) return TPLS_ERR_ARG;
+  }
+  tpls_batch *b = new tpls_batch();
+  b->m.assign(ctxs, ctxs + n);
+  cudaError_t e = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
+  b->join.assign(n, nullptr);
+  for (int q = 0; q < n && e == cudaSuccess; q++) e = cudaEventCreateWithFlags(&b->join[q], cudaEventDisableTiming);
+  if (e != cudaSuccess) {
+    tpls_batch_destroy(b);
+    return TPLS_ERR_CUDA_BASE + (int)e;
+  }
+  *out = b;
+  return TPLS_OK;
+}
+
+static int batch_capture(tpls_batch *b, int ph) {
+  const int n = (int)b->m.size();
+  std::vector<long> l0(n);
+  for (int q = 0; q < n; q++) l0[q] = b->m[q]->launches;
+  TCK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
+  int s = TPLS_OK;
+  cudaError_t e = cudaEventRecord(b->fork, b->st);
+  for (int q = 0; q < n && s == TPLS_OK && e == cudaSuccess; q++) {
+    tpls_ctx *c = b->m[q];
+    e = cudaStreamWaitEvent(c->st, b->fork, 0);
+    if (e != cudaSuccess) break;
+    c->capturing = true;
+    s = c->mixed ? step_once_mixed(c) : step_once(c);
+    c->capturing = false;
+    if (s == TPLS_OK) e = cudaEventRecord(b->join[q], c->st);
+    if (s == TPLS_OK && e == cudaSuccess) e = cudaStreamWaitEvent(b->st, b->join[q], 0);
+  }
+  cudaGraph_t gr = nullptr;
+  const cudaError_t ee = cudaStreamEndCapture(b->st, &gr);
+  b->n_static[ph].assign(n, 0);
+  for (int q = 0; q < n; q++) {
+    b->n_static[ph][q] = b->m[q]->launches - l0[q];
+    b->m[q]->launches = l0[q];
+  }
+  if (s != TPLS_OK || e != cudaSuccess || ee != cudaSuccess) {
+    if (gr) cudaGraphDestroy(gr);
+    if (s != TPLS_OK) return s;
+    return TPLS_ERR_CUDA_BASE + (int)(e != cudaSuccess ? e : ee);
+  }
+  const cudaError_t ei = cudaGraphInstantiate(&b->gexec[ph], gr, 0);
+  cudaGraphDestroy(gr);
+  TCK(ei);
+  return TPLS_OK;
+}
+
+int tpls_batch_step_async(tpls_batch *b, int nsteps) {
+  if (!b || nsteps < 0) return TPLS_ERR_ARG;
+  const int n = (int)b->m.size();
+  for (int it = 0; it < nsteps; it++) {
+    const int ph = b->m[0]->phase;
+    for (tpls_ctx *c : b->m)
+      if (c->phase != ph || c->timing) return TPLS_ERR_STATE;
+    for (int q = 0; q < n; q++) {  // host uploads: ghost rows, then order the member streams before the batch
+      tpls_ctx *c = b->m[q];
+      int s = prologue(c);
+      if (s) return s;
+      TCK(cudaEventRecord(b->join[q], c->st));
+      TCK(cudaStreamWaitEvent(b->st, b->join[q], 0));
+    }
+    if (!b->gexec[ph]) {
+      int s = batch_capture(b, ph);
+      if (s) return s;
+    }
+    TCK(cudaGraphLaunch(b->gexec[ph], b->st));
+    TCK(cudaEventRecord(b->done, b->st));
+    for (int q = 0; q < n; q++) {
+      tpls_ctx *c = b->m[q];
+      TCK(cudaStreamWaitEvent(c->st, b->done, 0));  // later work on a member follows the batch step
+      c->launches += b->n_static[ph][q];
+      c->phase = (ph + 1) % 3;
+      c->stats.steps_done++;
+      c->graph_pending = true;
+    }
+  }
+  return TPLS_OK;
+}
+
+int tpls_batch_step(tpls_batch *b, int nsteps) {
+  int s = tpls_batch_step_async(b, nsteps);
+  if (s) return s;
+  TCK(cudaStreamSynchronize(b->st));
+  int worst = TPLS_OK;
+  for (tpls_ctx *c : b->m) {
+    TCK(cudaStreamSynchronize(c->st));
+    s = refresh_graph_stats(c);
+    if (s) return s;
+    if (c->stats.p_worst < worst) worst = c->stats.p_worst;
+    c->stats.p_worst = 0;
+  }
+  return worst;
+}
+
+// interface height per column: first sign change of phi between cell
+// centres k and k+1 (k = 1..nz-1), linear interpolation; -1 if none
+__global__ void k_iface_height(Geo g, double dz, const double *__restrict__ phi, double *__restrict__ h) {
+  const int i = blockIdx.x * 32 + threadIdx.x + 1, j = blockIdx.y * 4 + threadIdx.y + 1;
+  if (i > g.nx || j > g.ny) return;
+  double out = -1.0;
+  double p0 = phi[TPLS_IDX(g, i, j, 1)];
+  for (int k = 1; k < g.nz; k++) {
+    const double p1 = phi[TPLS_IDX(g, i, j, k + 1)];
+    if ((p0 < 0.0 && p1 >= 0.0) || (p0 >= 0.0 && p1 < 0.0)) {
+      out = (k - 0.5) * dz + dz * (p0 / (p0 - p1));
+      break;
+    }
+    p0 = p1;
+  }
+  h[(i - 1) + g.nx * (j - 1)] = out;
+}
+
+int tpls_interface_height(tpls_ctx *c, double *h_host) {
+  if (!c || !h_host) return TPLS_ERR_ARG;
+  const Geo &g = c->g;
+  dim3 grd((g.nx + 31) / 32, (g.ny + 3) / 4, 1);
+  k_iface_height<<<grd, dim3(32, 4), 0, c->st>>>(g, c->prm.dz, c->phi2, c->hbuf);
+  LCK(c, cudaGetLastError());
+  TCK(cudaMemcpyAsync(h_host, c->hbuf, sizeof(double) * (size_t)g.nx * g.ny, cudaMemcpyDeviceToHost, c->st));
+  TCK(cudaStreamSynchronize(c->st));
   return TPLS_OK;
 }
 

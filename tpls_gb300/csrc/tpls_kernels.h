@@ -47,10 +47,11 @@ cudaError_t launch_csf(const Geo &g, const Phys &ph, const double *phi3,
                        double *fx, double *fy, double *fz, cudaStream_t st);
 cudaError_t launch_visc(const Geo &g, const Phys &ph, const double *phi2,
                         double *mu, cudaStream_t st);
-// FP32-mixed form of the level-set kernels: status with D in FP32, the
-// redistancing iterations in FP32 (first reads the FP64 phi3 when pr64 is
-// given, last writes the FP64 state when out64 is given), CSF in FP32,
-// viscosity stored in FP32 (the Heaviside evaluated in FP64).
+// FP32-mixed form of the level-set kernels: status decided in FP64 with D
+// stored in FP32, the redistancing iterations in FP32 (first reads the FP64
+// phi3 when pr64 is given, last writes the FP64 state when out64 is given),
+// CSF evaluated in FP64 and stored in FP32, viscosity stored in FP32 (the
+// Heaviside evaluated in FP64).
 cudaError_t launch_ls_status(const Geo &g, const Phys &ph, const double *phi3,
                              float *D, signed char *flags, cudaStream_t st);
 cudaError_t launch_ls_iter32(const Geo &g, const Phys &ph, const double *pr64,

@@ -14,6 +14,9 @@ cudaError_t poisson_create(const Geo &g, double cx, double cy, double cz,
                            int fp32, PoissonSolver **out);
 void poisson_destroy(PoissonSolver *S);
 int poisson_levels(const PoissonSolver *S);
+// Device bytes poisson_create allocates for this grid, each allocation
+// rounded by rnd (the allocator's granularity).
+size_t poisson_footprint(const Geo &g, int fp32, size_t (*rnd)(size_t));
 // Solves for pres (full p-grid incl. ghosts) from RHS_p, u3's inlet column
 // (u3 is float when u3_fp32), u_inlet and the initial guess pres_old.
 // Synchronises the stream once per iteration to test convergence.
