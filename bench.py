@@ -104,15 +104,30 @@ def _dist():
 
 
 def _algorithmic_bytes(nx, ny, nz, mom):
-    """Compulsory bytes of the momentum-sweep launches (FP64): Jacobi reads
-    x_old, RHS, mu and writes x (32 B per point); a red-black half-sweep
-    reads x (all points, 8 B), RHS and mu of the relaxed colour (8 B) and
-    writes that colour (4 B): 20 B per point."""
+    """Compulsory bytes of the momentum-sweep launches (FP64, per point of
+    the component grid): Jacobi 32 B (x_old, RHS, mu read, x written), a
+    red-black half-sweep 28 B (x and mu read in full, RHS of the relaxed
+    colour, that colour written).  Returns (Jacobi bytes, odd half-sweep
+    bytes, Jacobi launches, odd half-sweep launches) of one step."""
     pts = [(nx - 1) * ny * nz, nx * ny * nz, nx * ny * (nz - 1)]
     outer = mom // 2
+    n_odd = (outer + 1) // 2  # outer iterations 1, 3, 5, ... use the odd sweep
     jac = sum(32.0 * p for p in pts) * outer
-    sor = sum(20.0 * p for p in pts) * 2 * outer
-    return jac, sor, 3 * outer, 6 * outer
+    sor_odd = sum(28.0 * p for p in pts) * 2 * n_odd
+    return jac, sor_odd, 3 * outer, 6 * n_odd
+
+
+def _profile_figure(tag: str, kernel: str, workload: str):
+    """A figure from the committed ncu summaries: lines
+    '<tag> <kernel> <workload>: <number> ...' (tag 'traffic' = DRAM bytes per
+    launch, 'fp64pipe' = FP64 pipe active % of peak)."""
+    import re
+    for f in sorted((ROOT / "profiles").glob("*.md")):
+        for line in f.read_text().splitlines():
+            m = re.match(r"(\S+) (\S+) (\S+): ([0-9.]+)", line.strip())
+            if m and m.group(1) == tag and m.group(2) == kernel and m.group(3) == workload:
+                return float(m.group(4))
+    return None
 
 
 def run_gpu(args, ws, rank, local) -> dict | None:
@@ -212,20 +227,17 @@ def run_gpu(args, ws, rank, local) -> dict | None:
     hbm = float(peaks.get("hbm_gbs", 6800.0))
     jac_b, sor_b, jac_n, sor_n = _algorithmic_bytes(nx, ny, nz, params.mom_u)
     # dominant kernel of the step: the odd-iteration red-black half-sweep
-    # (k_sor_odd_c2), timed launch by launch on the library's stream
+    # (k_sor_odd_c3), its launches timed with CUDA events on the library's
+    # stream in the phase pass
     sor_ms, sor_l = phases["sor_odd"]
-    dominant = "sor_odd_c2"
+    dominant = "k_sor_odd_c3"
     esz = 4.0 if precision == 1 else 8.0
     per_launch_b = sor_b / sor_n * (esz / 8.0)
     avg_ms = sor_ms / max(sor_l, 1)
     achieved = per_launch_b / (avg_ms / 1e3) / 1e9
-    traffic = None
-    tf = ROOT / "profiles" / "traffic_per_launch.json"
-    if tf.exists():
-        try:
-            traffic = json.loads(tf.read_text()).get(f"k_{dominant}")
-        except Exception:
-            traffic = None
+    wl = f"{nx}x{ny}x{nz}-{'fp64' if precision == 0 else 'mixed'}"
+    traffic = _profile_figure("traffic", dominant, wl)
+    fp64_pct = _profile_figure("fp64pipe", dominant, wl)
     cpu = None
     if ws == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(args.config, args.cpu_seconds)
@@ -253,11 +265,15 @@ def run_gpu(args, ws, rank, local) -> dict | None:
         "e2e": {"value": e2e, "unit": "cell-steps/s", "h2d_bytes_per_step": bi, "d2h_bytes_per_step": bi,
                 "steps": ke, "path": "tpls_set_field x20 -> tpls_step(1) -> tpls_get_field x20 per step"},
         "gpu_launches": launches,
-        "roofline": {"bound": "hbm", "kernel": f"k_{dominant}", "bytes_per_launch": per_launch_b,
+        "roofline": {"bound": "hbm", "kernel": dominant, "bytes_per_launch": per_launch_b,
                      "avg_launch_ms": avg_ms,
                      "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": traffic, "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback",
-                     "note": "FP64 kernels on GB300 are FP64-pipe bound (1.01 TFLOP/s measured), not HBM bound"},
+                     "note": "achieved = algorithmic bytes (28 B per component point per half-sweep) / "
+                             "event time; traffic = ncu DRAM bytes per launch (profiles/); the FP64 form's "
+                             "kernels are bound by GB300's FP64 pipe (1.01 TFLOP/s), see fp64_pipe"},
+        "fp64_pipe": {"kernel": dominant, "ncu_active_pct_of_peak": fp64_pct,
+                      "source": "ncu sm__pipe_fp64_cycles_active of the same kernel (profiles/)"},
         "phases_ms_per_step": {k: v[0] / nph for k, v in phases.items()},
         "phases_note": f"eager pass of {nph} steps with events between phases",
         "pressure": {"its_last": stats["p_its"], "reason_last": stats["p_reason"]},

@@ -12,8 +12,10 @@ The batched workload: 48 instances with seeded draws nx in {64..256 step
 32}, ny in {32..128 step 32}, nz in {32..128 step 16}, viscosity ratio m
 log-uniform in [1, 20], density ratio r uniform in [1, 10] (recorded only:
 the reference has no density ratio), Re uniform in [50, 500], interface
-amplitude uniform in [0.01, 0.1] (the bound of the 4 seeded modes), 200
-steps each in the FP32-mixed form.
+amplitude uniform in [0.01, 0.1] (the bound of the 4 seeded modes, whose
+wavelengths are kept >= 1, the channel height: with cubic cells a box can
+be as narrow as Ly = 32/128, where 4 spanwise modes of amplitude 0.1 would
+fold the interface), 200 steps each in the FP32-mixed form.
 """
 from __future__ import annotations
 
@@ -47,7 +49,8 @@ class Instance:
 
     def workload(self) -> Workload:
         return Workload(f"instance {self.idx}: {self.nx}x{self.ny}x{self.nz}, m={self.m:.3g}, Re={self.re:.3g}",
-                        self.nx, self.ny, self.nz, self.m, self.re, self.r, self.amp, 4, 200, self.seed)
+                        self.nx, self.ny, self.nz, self.m, self.re, self.r, self.amp, 4, 200, self.seed,
+                        min_wavelength=1.0)
 
 
 def draw_instances(n: int = 48, seed: int = BATCH_SEED, max_dims: tuple | None = None) -> list[Instance]:

@@ -22,7 +22,9 @@ algorithm diverges (NaN near step 85 at 256x128x192).
   and w points (w stays 0 on the walls); u_inlet(k) = u(z_k);
 * p = -x with x = i*dx - dx/2 (twophase_initialisation_wave.F90:145-154),
   p_old = 0 (main_ns_hybrid.F90:423);
-* smooth_width = 1.5 dx, scap = 1, height = 0.5, dt = 0.2 dx / max u.
+* smooth_width = 1.5 dx, scap = 1, height = 0.5,
+  dt = min(0.2 dx / max u, 0.5 sqrt(dx^3 / (2 pi))) (CFL 0.2; the capillary
+  bound is below it only for slow, low-Re instances).
 
 Noise comes from SplitMix64(seed) in Fortran order over u, then v, then w;
 interface modes from numpy's PCG64(seed).  There is no public dataset for
@@ -70,6 +72,10 @@ class Workload:
     modes: int        # 0 = the single-mode interface of the 64x32x48 case
     steps: int
     seed: int
+    # > 0: interface modes limited to wavelengths >= this length (kx, ky <=
+    # L / min_wavelength; ky = 0 when Ly is shorter), for the batched and
+    # served instances whose boxes can be narrow
+    min_wavelength: float = 0.0
 
 
 WORKLOADS = {
@@ -91,8 +97,14 @@ def interface_height(w: Workload, x: np.ndarray, y: np.ndarray, Lx: float, Ly: f
     if w.modes == 0:
         return 0.5 + w.amp_max * np.sin(2.0 * np.pi * x / Lx) * np.cos(2.0 * np.pi * y / Ly)
     rng = np.random.default_rng(w.seed)
-    kx = rng.integers(1, 5, size=w.modes)
-    ky = rng.integers(1, 5, size=w.modes)
+    if w.min_wavelength > 0.0:
+        kxm = max(1, min(4, int(Lx // w.min_wavelength)))
+        kym = min(4, int(Ly // w.min_wavelength))
+        kx = rng.integers(1, kxm + 1, size=w.modes)
+        ky = rng.integers(1, kym + 1, size=w.modes) if kym >= 1 else np.zeros(w.modes, dtype=np.int64)
+    else:
+        kx = rng.integers(1, 5, size=w.modes)
+        ky = rng.integers(1, 5, size=w.modes)
     amp = rng.uniform(0.0, w.amp_max, size=w.modes)
     th = rng.uniform(0.0, 2.0 * np.pi, size=w.modes)
     h = np.full(np.broadcast(x, y).shape, 0.5)
@@ -120,7 +132,10 @@ def make_case(w: Workload | str, *, nx: int | None = None, ny: int | None = None
     mu_minus, mu_plus = w.m, 1.0
     uz = base_profile(nz, dz, w.re, -1.0, mu_minus, mu_plus, 0.5, sw)
     umax = float(np.max(np.abs(uz)))
-    dt = 0.2 * dx / umax
+    # CFL 0.2 on the base flow, and half the capillary limit of the explicit
+    # surface-tension term, sqrt(rho dx^3 / (2 pi sigma)) with rho = 1 and
+    # sigma = scap = 1 (binding only for slow, low-Re instances)
+    dt = min(0.2 * dx / umax, 0.5 * np.sqrt(dx ** 3 / (2.0 * np.pi)))
     params = Params(dx=dx, dy=dy, dz=dz, dt=dt, re=w.re, mu_plus=mu_plus, mu_minus=mu_minus, height=0.5,
                     scap=1.0, smooth_width=sw, mom_u=mom, mom_v=mom, mom_w=mom, levelset=levelset,
                     p_rtol=p_rtol, p_maxits=p_maxits, precision=precision)

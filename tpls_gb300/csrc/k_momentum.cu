@@ -244,7 +244,7 @@ __global__ void __launch_bounds__(MB_X *MB_Y)
   csf2[c] = s2;
   if (rhs) rhs[c] = r;
   if (diff_out) diff_out[c] = diff;
-  if (coef && valid) write_coef(comp, g, hm, f, r, k, coef + 8 * (size_t)c);
+  if (coef && valid) write_coef(comp, g, hm, f, r, k, coef + 8 * (size_t)rec_slot(g, c, i));
 }
 
 template <typename T>

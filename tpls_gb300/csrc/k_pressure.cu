@@ -159,11 +159,22 @@ __device__ __forceinline__ R applyA(const TE *__restrict__ e, int i, int j, int 
   const R ym = (R)e[c + nx * ((j > 0) ? -1 : ny - 1)];
   const R yp = (R)e[c + nx * ((j < ny - 1) ? 1 : 1 - ny)];
   const R zm = (k > 0) ? (R)e[c - nx * ny] : v, zp = (k < nz - 1) ? (R)e[c + nx * ny] : v;
-  const R two = (R)2;
-  return cx * (two * v - xm - xp) + cy * (two * v - ym - yp) + cz * (two * v - zm - zp);
+  // (2cx + 2cy + 2cz) v - cx (xm + xp) - cy (ym + yp) - cz (zm + zp): seven
+  // FP64 operations (the FP64 pipe bounds these kernels on GB300)
+  const R d = (R)2 * (cx + cy + cz);
+  R a = d * v;
+  a = fma(-cx, xm + xp, a);
+  a = fma(-cy, ym + yp, a);
+  return fma(-cz, zm + zp, a);
 }
 
 #define GRID_STRIDE(c, N) for (int c = blockIdx.x * PB + threadIdx.x; c < (N); c += gridDim.x * PB)
+// rows (j, k) of the compact nx*ny*nz grid handed to warps in a fixed
+// order, lanes striding over i; row = j + ny k, c = i + nx row
+#define ROW_LOOP(nx, ny, nz)                                                                          \
+  for (int row = blockIdx.x * (PB / 32) + (int)(threadIdx.x >> 5); row < (ny) * (nz);                \
+       row += gridDim.x * (PB / 32))                                                                 \
+    for (int j = row % (ny), k = row / (ny), i = (int)(threadIdx.x & 31); i < (nx); i += 32)
 
 // b (compact interior) = -RHS_p + inlet contribution; x0 = p_old interior;
 // sums of b and x0.
@@ -173,10 +184,10 @@ __global__ void __launch_bounds__(PB)
               const TU *__restrict__ u3, const double *__restrict__ uin,
               const double *__restrict__ pold, double *__restrict__ b, double *__restrict__ x0,
               double *__restrict__ bin, double *part, unsigned *counter, double *s) {
-  const int nx = g.nx, ny = g.ny, nz = g.nz, N = nx * ny * nz;
+  const int nx = g.nx, ny = g.ny, nz = g.nz;
   double v[2] = {0.0, 0.0};
-  GRID_STRIDE(c, N) {
-    const int i = c % nx, j = (c / nx) % ny, k = c / (nx * ny);
+  ROW_LOOP(nx, ny, nz) {
+    const int c = i + nx * row;
     const int pc = TPLS_IDX(g, i + 1, j + 1, k + 1);
     double bb = -rhs_p[pc];
     if (i == 0) {
@@ -204,11 +215,10 @@ __global__ void __launch_bounds__(PB)
     k_init_r(int nx, int ny, int nz, double cx, double cy, double cz, double invN, double rtol, CgCtl ctl,
              double *s, double *__restrict__ b, const double *__restrict__ x, double *__restrict__ r, double *part,
              unsigned *counter) {
-  const int N = nx * ny * nz;
   const double mb = s[S_SUMB] * invN;
   double v[2] = {0.0, 0.0};
-  GRID_STRIDE(c, N) {
-    const int i = c % nx, j = (c / nx) % ny, k = c / (nx * ny);
+  ROW_LOOP(nx, ny, nz) {
+    const int c = i + nx * row;
     const double bb = b[c] - mb;
     b[c] = bb;
     const double rr = bb - applyA<double, double>(x, i, j, k, nx, ny, nz, cx, cy, cz);
@@ -258,10 +268,9 @@ __global__ void __launch_bounds__(PB)
 __global__ void __launch_bounds__(PB)
     k_apply_dot(int nx, int ny, int nz, double cx, double cy, double cz, const double *__restrict__ p,
                 double *__restrict__ q, double *part, unsigned *counter, double *s) {
-  const int N = nx * ny * nz;
   double v[1] = {0.0};
-  GRID_STRIDE(c, N) {
-    const int i = c % nx, j = (c / nx) % ny, k = c / (nx * ny);
+  ROW_LOOP(nx, ny, nz) {
+    const int c = i + nx * row;
     const double a = applyA<double, double>(p, i, j, k, nx, ny, nz, cx, cy, cz);
     q[c] = a;
     v[0] += p[c] * a;
@@ -381,18 +390,20 @@ __global__ void __launch_bounds__(LJ2_T)
   R *buf = reinterpret_cast<R *>(lj2_raw);  // [nz][32]
   const int nx = L.nx, ny = L.ny, nz = L.nz, ncol = nx * ny, plane = nx * ny;
   const int col0 = blockIdx.x * 32;
+  // every thread keeps one column (LJ2_T is a multiple of 32)
+  const int mycol = col0 + (threadIdx.x & 31);
+  const int ci = mycol % nx, cj = mycol / nx;
+  const int jm = (cj > 0) ? -nx : nx * (ny - 1), jp = (cj < ny - 1) ? nx : -nx * (ny - 1);
   for (int t = threadIdx.x; t < nz * 32; t += LJ2_T) {
-    const int k = t >> 5, cl = t & 31, col = col0 + cl;
+    const int k = t >> 5;
     R rhs = (R)0;
-    if (col < ncol) {
-      const int c = col + plane * k;
+    if (mycol < ncol) {
+      const int c = mycol + plane * k;
       rhs = (R)b[c];
       if (!zero_init) {
-        const int i = col % nx, j = col / nx;
-        const int jm = (j > 0) ? -nx : nx * (ny - 1), jp = (j < ny - 1) ? nx : -nx * (ny - 1);
         R nb = L.cy * ((R)ei[c + jm] + (R)ei[c + jp]);
-        if (i > 0) nb += L.cx * (R)ei[c - 1];
-        if (i < nx - 1) nb += L.cx * (R)ei[c + 1];
+        if (ci > 0) nb += L.cx * (R)ei[c - 1];
+        if (ci < nx - 1) nb += L.cx * (R)ei[c + 1];
         rhs += nb;
       }
     }
@@ -427,12 +438,19 @@ __global__ void __launch_bounds__(LJ2_T)
   }
 }
 
+// point kernels of the V-cycle run on 3-D grids of 32x8 blocks (x, y) and
+// one z plane per grid z index
+constexpr int MG_BX = 32, MG_BY = 8;
+static inline dim3 mg_grid(int nx, int ny, int nz) {
+  return dim3((nx + MG_BX - 1) / MG_BX, (ny + MG_BY - 1) / MG_BY, nz);
+}
+
 template <typename R, typename TB, typename TE>
 __global__ void k_residual(LevArgs<R> L, const TB *__restrict__ b, const TE *__restrict__ e, R *__restrict__ r) {
-  const int c = blockIdx.x * PB + threadIdx.x;
   const int nx = L.nx, ny = L.ny, nz = L.nz;
-  if (c >= nx * ny * nz) return;
-  const int i = c % nx, j = (c / nx) % ny, k = c / (nx * ny);
+  const int i = blockIdx.x * MG_BX + threadIdx.x, j = blockIdx.y * MG_BY + threadIdx.y, k = blockIdx.z;
+  if (i >= nx || j >= ny) return;
+  const int c = i + nx * (j + ny * k);
   r[c] = (R)b[c] - applyA<R, TE>(e, i, j, k, nx, ny, nz, L.cx, L.cy, L.cz);
 }
 
@@ -455,29 +473,6 @@ __device__ __forceinline__ int rstencil(int c, int nc, int coarsened, int period
   if (c < nc - 1) { f[m] = 2 * c + 2; w[m++] = (R)0.25; }
   else if (periodic) { f[m] = 0; w[m++] = (R)0.25; }
   return m;
-}
-
-template <typename R>
-__global__ void k_restrict(LevArgs<R> F, LevArgs<R> C, int cxs, int cys, int czs, R scale,
-                           const R *__restrict__ rf, R *__restrict__ bc) {
-  const int c = blockIdx.x * PB + threadIdx.x;
-  if (c >= C.nx * C.ny * C.nz) return;
-  const int I = c % C.nx, J = (c / C.nx) % C.ny, K = c / (C.nx * C.ny);
-  int fx[4], fy[4], fz[4];
-  R wx[4], wy[4], wz[4];
-  const int mx = rstencil<R>(I, C.nx, cxs, 0, fx, wx);
-  const int my = rstencil<R>(J, C.ny, cys, 1, fy, wy);
-  const int mz = rstencil<R>(K, C.nz, czs, 0, fz, wz);
-  R acc = (R)0;
-  for (int a = 0; a < mz; a++)
-    for (int bq = 0; bq < my; bq++) {
-      const R wzy = wz[a] * wy[bq];
-      const R *row = rf + F.nx * (fy[bq] + F.ny * fz[a]);
-      R sx = (R)0;
-      for (int q = 0; q < mx; q++) sx += wx[q] * row[fx[q]];
-      acc += wzy * sx;
-    }
-  bc[c] = acc * scale;
 }
 
 // 1-D prolongation: coarse indices and weights for fine f
@@ -505,26 +500,47 @@ __device__ __forceinline__ int pstencil(int f, int nc, int coarsened, int period
   return 2;
 }
 
+// Separable transfers: P = Px (x) Py (x) Pz and R = P^T / 2^d applied one
+// axis at a time through intermediate grids, 2 (P) or 4 (R) multiply-adds
+// per output point instead of the 8 (P) or 64 (R) of the direct 3-D
+// stencils.  (nx, ny, nz) are the output dimensions; the input has the same
+// dimensions except `nin` along axis `ax`.
 template <typename R>
-__global__ void k_prolong_add(LevArgs<R> F, LevArgs<R> C, int cxs, int cys, int czs, const R *__restrict__ ec,
-                              R *__restrict__ ef) {
-  const int c = blockIdx.x * PB + threadIdx.x;
-  if (c >= F.nx * F.ny * F.nz) return;
-  const int i = c % F.nx, j = (c / F.nx) % F.ny, k = c / (F.nx * F.ny);
-  int cx[2], cy[2], cz[2];
-  R wx[2], wy[2], wz[2];
-  const int mx = pstencil<R>(i, C.nx, cxs, 0, cx, wx);
-  const int my = pstencil<R>(j, C.ny, cys, 1, cy, wy);
-  const int mz = pstencil<R>(k, C.nz, czs, 0, cz, wz);
+__global__ void k_prolong_axis(int ax, int periodic, int nx, int ny, int nz, int nin, const R *__restrict__ in,
+                               R *__restrict__ out, int add) {
+  const int i = blockIdx.x * MG_BX + threadIdx.x, j = blockIdx.y * MG_BY + threadIdx.y, k = blockIdx.z;
+  if (i >= nx || j >= ny) return;
+  const int f = (ax == 0) ? i : ((ax == 1) ? j : k);
+  int cc[2];
+  R w[2];
+  const int m = pstencil<R>(f, nin, 1, periodic, cc, w);
+  const int inx = (ax == 0) ? nin : nx, iny = (ax == 1) ? nin : ny;
   R acc = (R)0;
-  for (int a = 0; a < mz; a++)
-    for (int bq = 0; bq < my; bq++) {
-      const R *row = ec + C.nx * (cy[bq] + C.ny * cz[a]);
-      R sx = (R)0;
-      for (int q = 0; q < mx; q++) sx += wx[q] * row[cx[q]];
-      acc += wz[a] * wy[bq] * sx;
-    }
-  ef[c] += acc;
+  for (int q = 0; q < m; q++) {
+    const int ii = (ax == 0) ? cc[q] : i, jj = (ax == 1) ? cc[q] : j, kk = (ax == 2) ? cc[q] : k;
+    acc = fma(w[q], in[ii + inx * (jj + iny * kk)], acc);
+  }
+  const int o = i + nx * (j + ny * k);
+  out[o] = add ? out[o] + acc : acc;
+}
+
+template <typename R>
+__global__ void k_restrict_axis(int ax, int periodic, int nx, int ny, int nz, int nin, R scale,
+                                const R *__restrict__ in, R *__restrict__ out) {
+  const int i = blockIdx.x * MG_BX + threadIdx.x, j = blockIdx.y * MG_BY + threadIdx.y, k = blockIdx.z;
+  if (i >= nx || j >= ny) return;
+  const int cidx = (ax == 0) ? i : ((ax == 1) ? j : k);
+  const int nco = (ax == 0) ? nx : ((ax == 1) ? ny : nz);
+  int ff[4];
+  R w[4];
+  const int m = rstencil<R>(cidx, nco, 1, periodic, ff, w);
+  const int inx = (ax == 0) ? nin : nx, iny = (ax == 1) ? nin : ny;
+  R acc = (R)0;
+  for (int q = 0; q < m; q++) {
+    const int ii = (ax == 0) ? ff[q] : i, jj = (ax == 1) ? ff[q] : j, kk = (ax == 2) ? ff[q] : k;
+    acc = fma(w[q], in[ii + inx * (jj + iny * kk)], acc);
+  }
+  out[i + nx * (j + ny * k)] = acc * scale;
 }
 
 // coarsest grid: e = Cinv b (one block; the pseudo-inverse and the
@@ -806,6 +822,62 @@ static void line_sweep(const PLevel &L, R w, R w1, int zero_init, const TB *b, c
   }
 }
 
+// R = P^T / 2^d over the coarsened axes in the order x, y, z; the
+// intermediate grids live in the fine level's scratch t (n values: the
+// first intermediate uses its first n/2, the second the next n/4).
+template <typename R>
+static cudaError_t restrict_chain(const PLevel &F, const PLevel &C, const R *rf, R *t, R *bc, cudaStream_t st,
+                                  long *nl) {
+  int d[3] = {F.nx, F.ny, F.nz};
+  const int cd[3] = {C.nx, C.ny, C.nz};
+  const int cs[3] = {C.cxs, C.cys, C.czs};
+  int last = -1, nax = 0;
+  for (int a = 0; a < 3; a++)
+    if (cs[a]) last = a, nax++;
+  const R scale = (R)(1.0 / (double)(1 << nax));
+  const R *src = rf;
+  R *bufs[2] = {t, t + (size_t)F.n / 2};
+  int b = 0;
+  for (int a = 0; a < 3; a++) {
+    if (!cs[a]) continue;
+    const int nin = d[a];
+    d[a] = cd[a];
+    R *dst = (a == last) ? bc : bufs[b++];
+    k_restrict_axis<R><<<mg_grid(d[0], d[1], d[2]), dim3(MG_BX, MG_BY), 0, st>>>(
+        a, a == 1, d[0], d[1], d[2], nin, (a == last) ? scale : (R)1, src, dst);
+    (*nl)++;
+    src = dst;
+  }
+  return cudaGetLastError();
+}
+
+// ef += P ec over the coarsened axes in the order z, y, x.
+template <typename R>
+static cudaError_t prolong_chain(const PLevel &F, const PLevel &C, const R *ec, R *t, R *ef, cudaStream_t st,
+                                 long *nl) {
+  int d[3] = {C.nx, C.ny, C.nz};
+  const int fd[3] = {F.nx, F.ny, F.nz};
+  const int cs[3] = {C.cxs, C.cys, C.czs};
+  int last = -1;
+  for (int a = 2; a >= 0; a--)
+    if (cs[a]) last = a;
+  const R *src = ec;
+  R *bufs[2] = {t + (size_t)F.n / 2, t};  // the smaller intermediate first
+  int b = 0;
+  for (int a = 2; a >= 0; a--) {
+    if (!cs[a]) continue;
+    const int nin = d[a];
+    d[a] = fd[a];
+    const bool fin = (a == last);
+    R *dst = fin ? ef : bufs[b++];
+    k_prolong_axis<R><<<mg_grid(d[0], d[1], d[2]), dim3(MG_BX, MG_BY), 0, st>>>(a, a == 1, d[0], d[1], d[2], nin,
+                                                                                src, dst, fin ? 1 : 0);
+    (*nl)++;
+    src = dst;
+  }
+  return cudaGetLastError();
+}
+
 // one symmetric V-cycle: out = M b0.  Every level pre-smooths into its
 // scratch e2 (one damped line-Jacobi sweep from zero), restricts the
 // residual, adds the prolonged coarse correction into e2 and post-smooths
@@ -865,27 +937,27 @@ static cudaError_t vcycle(PoissonSolver *S, const double *b0, double *out, cudaS
     const LevArgs<R> A = largs<R>(L);
     if (l == 0) {
       line_sweep<R, double, R, R>(L, w, w1, 1, b0, nullptr, lvp(L.e2), st);
-      k_residual<R, double, R><<<nblocks(L.n), PB, 0, st>>>(A, b0, lvp(L.e2), lvp(L.r));
+      k_residual<R, double, R><<<mg_grid(L.nx, L.ny, L.nz), dim3(MG_BX, MG_BY), 0, st>>>(A, b0, lvp(L.e2),
+                                                                                    lvp(L.r));
     } else {
       line_sweep<R, R, R, R>(L, w, w1, 1, b, nullptr, lvp(L.e2), st);
-      k_residual<R, R, R><<<nblocks(L.n), PB, 0, st>>>(A, b, lvp(L.e2), lvp(L.r));
+      k_residual<R, R, R><<<mg_grid(L.nx, L.ny, L.nz), dim3(MG_BX, MG_BY), 0, st>>>(A, b, lvp(L.e2), lvp(L.r));
     }
     const PLevel &C = S->lv[l + 1];
-    const R scale = (R)(1.0 / (double)((C.cxs ? 2 : 1) * (C.cys ? 2 : 1) * (C.czs ? 2 : 1)));
-    k_restrict<R><<<nblocks(C.n), PB, 0, st>>>(A, largs<R>(C), C.cxs, C.cys, C.czs, scale, lvp(L.r), lvp(C.b));
-    *nl += 3;
+    PCK(restrict_chain<R>(L, C, lvp(L.r), lvp(L.t), lvp(C.b), st, nl));
+    *nl += 2;
     PCK(cudaGetLastError());
   }
   for (int l = nlev - 2; l >= 0; l--) {
     PLevel &L = S->lv[l];
     const PLevel &C = S->lv[l + 1];
     const LevArgs<R> A = largs<R>(L);
-    k_prolong_add<R><<<nblocks(L.n), PB, 0, st>>>(A, largs<R>(C), C.cxs, C.cys, C.czs, lvp(C.e), lvp(L.e2));
+    PCK(prolong_chain<R>(L, C, lvp(C.e), lvp(L.t), lvp(L.e2), st, nl));
     if (l == 0)
       line_sweep<R, double, R, double>(L, w, w1, 0, b0, lvp(L.e2), out, st);
     else
       line_sweep<R, R, R, R>(L, w, w1, 0, lvp(L.b), lvp(L.e2), lvp(L.e), st);
-    *nl += 2;
+    *nl += 1;
     PCK(cudaGetLastError());
   }
   return cudaSuccess;

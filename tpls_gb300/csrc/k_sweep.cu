@@ -61,7 +61,7 @@ __global__ void __launch_bounds__(SW_X *SW_Y)
   const int iend = (comp == 0) ? g.nx - 1 : g.nx;
   if (i > iend || j > g.ny) return;
   const int c = TPLS_IDX(g, i, j, k), sy = g.sy, sz = g.sz;
-  const Rec<T> q = load_rec(coef, c, false);
+  const Rec<T> q = load_rec(coef, rec_slot(g, c, i), false);
   const T xc = xo[c];
   T zp, zm;
   if (comp == 2) {
@@ -113,7 +113,7 @@ __global__ void __launch_bounds__(SW_X *SW_Y)
   T v = 0;
   if (i <= iend) {
     const int c = TPLS_IDX(g, i, j, k), sy = g.sy, sz = g.sz;
-    const Rec<T> q = load_rec(coef, c, false);
+    const Rec<T> q = load_rec(coef, rec_slot(g, c, i), false);
     const T xc = x[c];
     T zp, zm;
     if (comp == 2) {
@@ -155,7 +155,7 @@ __device__ __forceinline__ void sor_odd_produce(int comp, const Geo &g, const T 
     T A = 0, B = 0;
     if (i2 < npair && i <= iend) {
       const int c = TPLS_IDX(g, i, j, k);
-      const Rec<T> q = load_rec(coef, c, true);
+      const Rec<T> q = load_rec(coef, rec_slot(g, c, i), true);
       const T xc = x[c];
       T zp;
       if (comp == 2) zp = x[c + sz];
@@ -220,6 +220,106 @@ __global__ void __launch_bounds__(SO_T)
   }
 }
 
+// The same half-sweep with the column recurrence split across warps.  A
+// block holds 32 columns (lanes) and SO3_W chunks of consecutive levels
+// (warps):
+//   1. every warp runs the recurrence over its chunk from a zero start,
+//      keeping y(k), the chunk-local solution, and P(k), the product of the
+//      B factors since the chunk start, in shared memory;
+//   2. each warp folds the ends of the chunks below it into x_in, the value
+//      entering its chunk;
+//   3. x(k) = y(k) + P(k) x_in for the chunk, written with the boundary rows.
+// The dependent chain per column becomes nz/SO3_W levels plus SO3_W folds;
+// the result differs from the level-by-level order only by rounding (P
+// decays like (1.2 czm)^m, so x_in's contribution is weighted by it).
+// Shared memory: 2 (nlev + W) 32 values of T; W = 8 or 16 warps.
+template <typename T, int SO3_W>
+__global__ void __launch_bounds__(SO3_W * 32)
+    k_sor_odd_c3(int comp, Geo g, Helm h, T *__restrict__ x, const T *__restrict__ coef,
+                 const double *__restrict__ P, int flg, int bc, int fuse) {
+  extern __shared__ __align__(16) unsigned char so3_raw[];
+  const int j = blockIdx.y + 1;
+  const int iend = (comp == 0) ? g.nx - 1 : g.nx;
+  const int npair = (iend + 1) / 2;
+  const int par = (j + flg) & 1;
+  const int k0 = (comp == 2) ? 1 : 0, k1 = g.nz - 1;
+  const int nlev = k1 - k0 + 1;
+  T *sy = reinterpret_cast<T *>(so3_raw);  // [nlev][32]
+  T *sp = sy + (size_t)nlev * 32;          // [nlev][32]
+  T *ey = sp + (size_t)nlev * 32;          // [SO3_W][32]
+  T *ep = ey + SO3_W * 32;                 // [SO3_W][32]
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int i2 = blockIdx.x * 32 + lane, i = 2 * i2 + 1 + par;
+  const bool act = (i2 < npair) && (i <= iend);
+  const int per = (nlev + SO3_W - 1) / SO3_W;
+  const int kb = k0 + w * per, ke = min(k1 + 1, kb + per);
+  const int sy_ = g.sy, sz = g.sz, nz = g.nz;
+  T yv = 0, pv = 1;
+  if (act) {
+#pragma unroll 2
+    for (int k = kb; k < ke; k++) {
+      const int c = TPLS_IDX(g, i, j, k);
+      const Rec<T> q = load_rec(coef, rec_slot(g, c, i), true);
+      const T xc = x[c];
+      T zp;
+      if (comp == 2) zp = x[c + sz];
+      else zp = (k == nz - 1) ? xc : x[c + sz];
+      T part = fma(q.xp, x[c + 1], q.b);
+      part = fma(q.xm, x[c - 1], part);
+      part = fma(q.yp, x[c + sy_], part);
+      part = fma(q.ym, x[c - sy_], part);
+      part = fma(q.zp, zp, part);
+      T A, B;
+      if (k == k0) {  // the point below is a wall value (w) or the point itself (u, v)
+        const T zm = (comp == 2) ? x[c - sz] : xc;
+        A = xc + (T)1.2 * (fma(q.zm, zm, part) - xc);
+        B = 0;
+      } else {
+        A = xc + (T)1.2 * (part - xc);
+        B = (T)1.2 * q.zm;
+      }
+      yv = fma(B, yv, A);
+      pv = B * pv;
+      sy[(k - k0) * 32 + lane] = yv;
+      sp[(k - k0) * 32 + lane] = pv;
+    }
+  }
+  ey[w * 32 + lane] = yv;  // an empty chunk passes x_in through (y 0, P 1)
+  ep[w * 32 + lane] = pv;
+  __syncthreads();
+  T xin = 0;
+  for (int v = 0; v < w; v++) xin = fma(ep[v * 32 + lane], xin, ey[v * 32 + lane]);
+  if (i2 < npair) {
+    for (int k = kb; k < ke; k++) {
+      T v = 0;
+      if (i <= iend) {
+        v = fma(sp[(k - k0) * 32 + lane], xin, sy[(k - k0) * 32 + lane]);
+        put(g, x, i, j, k, v, fuse);
+      }
+      if (bc) sor_bc(comp, g, h, x, P, i2, i, iend, v, j, k, fuse);
+    }
+  }
+}
+
+template <typename T>
+static size_t so3_smem(const Geo &g, int comp, int w) {
+  const int nlev = g.nz - (comp == 2 ? 1 : 0);
+  return sizeof(T) * 2 * ((size_t)nlev + w) * 32;
+}
+constexpr size_t SO3_SMEM_MAX = 200 * 1024;
+
+cudaError_t sweep_init() {
+  const int m = (int)SO3_SMEM_MAX;
+  cudaError_t e = cudaFuncSetAttribute(k_sor_odd_c3<double, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_sor_odd_c3<double, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_sor_odd_c3<float, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_sor_odd_c3<float, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+  return e;
+}
+
 template <typename T>
 static cudaError_t jacobi_c(int comp, const Geo &g, const Phys &ph, const T *xo, const T *coef,
                             const double *pres, T *x, int fuse, cudaStream_t st) {
@@ -241,7 +341,15 @@ static cudaError_t sor_c(int comp, const Geo &g, const Phys &ph, T *x, const T *
     k_sor_even_c<T><<<grd, dim3(SW_X, SW_Y), 0, st>>>(comp, g, helm_of(ph), x, coef, pres, flg, bc, fuse);
   } else {
     dim3 grd((npairs + 31) / 32, g.ny, 1);
-    k_sor_odd_c2<T><<<grd, SO_T, 0, st>>>(comp, g, helm_of(ph), x, coef, pres, flg, bc, fuse);
+    // 16 chunks once columns are long enough to give each warp >= 8 levels
+    const int w = (g.nz >= 128) ? 16 : 8;
+    const size_t sm = so3_smem<T>(g, comp, w);
+    if (sm <= SO3_SMEM_MAX && w == 16)
+      k_sor_odd_c3<T, 16><<<grd, 16 * 32, sm, st>>>(comp, g, helm_of(ph), x, coef, pres, flg, bc, fuse);
+    else if (sm <= SO3_SMEM_MAX)
+      k_sor_odd_c3<T, 8><<<grd, 8 * 32, sm, st>>>(comp, g, helm_of(ph), x, coef, pres, flg, bc, fuse);
+    else
+      k_sor_odd_c2<T><<<grd, SO_T, 0, st>>>(comp, g, helm_of(ph), x, coef, pres, flg, bc, fuse);
   }
   return cudaGetLastError();
 }

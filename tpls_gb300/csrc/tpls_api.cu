@@ -301,6 +301,7 @@ static int create_impl(int nx, int ny, int nz, const tpls_params *prm, const dou
   c->g.sz = c->px * (ny + 2);
   c->g.szm = c->px * (ny + 4);
   TCK(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
+  TCK(sweep_init());
   c->mixed = (prm->precision == TPLS_PREC_FP32_MIXED);
   c->n_p = (size_t)c->px * (ny + 2) * (nz + 2) + 8;
   c->n_uv = (size_t)c->px * (ny + 2) * nz + 8;

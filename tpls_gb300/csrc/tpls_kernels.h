@@ -121,6 +121,8 @@ cudaError_t launch_sor_c(int comp, const Geo &g, const Phys &ph, float *x,
                          const float *coef, const double *pres, int flg,
                          int iteration_time, int bc, int fuse_ghosts,
                          cudaStream_t st);
+// One-time kernel attributes of the sweeps (dynamic shared memory).
+cudaError_t sweep_init();
 cudaError_t launch_bc(int comp, const Geo &g, const Phys &ph, double *x,
                       const double *pres, cudaStream_t st);
 cudaError_t launch_diff2(const Geo &g, const double *a, const double *b,

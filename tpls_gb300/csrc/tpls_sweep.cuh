@@ -12,6 +12,15 @@ struct Helm {
   double dtdx;           // dt/dx (u outlet condition)
 };
 
+// Slot of point (i, j, k) (linear index c, 1 <= i <= nx) in the coefficient
+// record arrays.  Each (j, k) row keeps the records of odd i in its first
+// half and of even i in its second half (the row pitch sy is a multiple of
+// 4), so a red-black half-sweep, which relaxes one i parity per row, reads
+// one contiguous half-row of records instead of every other 64-byte record.
+__device__ __forceinline__ int rec_slot(const Geo &g, int c, int i) {
+  return c - i + ((i & 1) ? ((i - 1) >> 1) : ((g.sy >> 1) + (i >> 1) - 1));
+}
+
 // Write a value and, when ghost rows are fused (even ny), its periodic copy.
 template <typename T>
 __device__ __forceinline__ void put(const Geo &g, T *x, int i, int j, int k, T v, int fuse) {
