@@ -142,7 +142,8 @@ def run_gpu(args, ws, rank, local) -> dict | None:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     w = WORKLOADS[args.config]
     precision = _precision(args)
-    params, uin, st = make_case(args.config, p_rtol=args.p_rtol, precision=precision)
+    parts = args.fp64_parts if precision == 1 else 0
+    params, uin, st = make_case(args.config, p_rtol=args.p_rtol, precision=precision, fp64_parts=parts)
     nx, ny, nz = w.nx, w.ny, w.nz
     cells = nx * ny * nz
     g = TplsGpu(nx, ny, nz, params, uin)
@@ -257,6 +258,7 @@ def run_gpu(args, ws, rank, local) -> dict | None:
         "config": {"workload": w.name, "grid": [nx, ny, nz], "cells": cells, "m": w.m, "re": w.re,
                    "mom_uvw": params.mom_u, "levelset": params.levelset, "p_rtol": params.p_rtol,
                    "precision": "fp64" if precision == 0 else "fp32-mixed",
+                   "fp64_parts": parts,
                    "parallelism": f"{ws} independent replica(s), no sharding",
                    "l2": f"working set ~{cells * 500 / 1e9:.0f} GB per step >> 129 MB L2 (no flush needed)",
                    "launch": "one CUDA graph per step (device-side WHILE node for the pressure CG)",
@@ -523,6 +525,9 @@ def main():
     ap.add_argument("--precision", choices=["fp64", "mixed"], default=None,
                     help="default: fp64 for A/B/M, mixed for C/D")
     ap.add_argument("--phase-steps", type=int, default=20)
+    ap.add_argument("--fp64-parts", type=int, default=16,
+                    help="FP32-mixed form: TPLS_PART_* bits kept in FP64 (default 16: momentum stencils, "
+                         "the setting that holds phi/u within 1e-5 of the FP64 form)")
     ap.add_argument("--ref-seconds", type=float, default=120.0)
     ap.add_argument("--instances", type=int, default=48)
     ap.add_argument("--no-one-by-one", action="store_true")

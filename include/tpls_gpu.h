@@ -54,8 +54,18 @@ typedef struct tpls_params {
   double p_rtol;                  /* pressure solve: ||r||_2 <= rtol*||b||_2 */
   int p_maxits;                   /* pressure solve iteration cap */
   int precision;                  /* TPLS_PREC_* */
-  int reserved[6];
+  int fp64_parts;                 /* FP32-mixed form only: TPLS_PART_* bits of
+                                     the parts kept in FP64 (0 = all FP32) */
+  int reserved[5];
 } tpls_params;
+
+/* Parts of the FP32-mixed form that can be kept in FP64 (tpls_params.fp64_parts). */
+#define TPLS_PART_ADVECT 1    /* WENO5 advection */
+#define TPLS_PART_LEVELSET 2  /* redistancing iterations */
+#define TPLS_PART_MOMENTUM 4  /* momentum stencils, records and sweeps */
+#define TPLS_PART_MULTIGRID 8 /* multigrid preconditioner */
+#define TPLS_PART_MOM_STENCIL 16 /* momentum stencils and sweep records in FP64
+                                    (records stored FP32 for FP32 sweeps) */
 
 /* Per-step diagnostics, the quantities the reference logs each timestep
  * (main_ns_hybrid.F90:601-605, 803-808, 840-845, 882-887, 903-911). */

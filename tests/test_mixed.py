@@ -71,3 +71,18 @@ def test_mixed_deterministic_and_u3_view():
     assert np.abs(u3[1:NX, 1:NY + 1, :]).max() > 1.0
     a.close()
     b.close()
+
+
+def test_mixed_with_every_part_fp64_equals_fp64_form():
+    """fp64_parts = all four parts: the FP32-mixed driver then launches the
+    FP64 form's kernels in the same order, so the state is bit-identical."""
+    ref = _ctx(0)
+    params, uin, st = make_case("A", nx=NX, ny=NY, nz=NZ, precision=1, fp64_parts=15)
+    mix = TplsGpu(NX, NY, NZ, params, uin)
+    mix.set_state(st)
+    assert ref.step(3) == 0 and mix.step(3) == 0
+    a, b = ref.get_state(), mix.get_state()
+    assert all(np.array_equal(a[k], b[k]) for k in STATE_FIELDS)
+    assert np.array_equal(ref.get_field("U3"), mix.get_field("U3"))
+    ref.close()
+    mix.close()

@@ -30,6 +30,7 @@ LIB_PATH = _ROOT / "_lib" / "libtpls_gb300.so"
 
 TPLS_PREC_FP64 = 0
 TPLS_PREC_FP32_MIXED = 1
+PART_ADVECT, PART_LEVELSET, PART_MOMENTUM, PART_MULTIGRID, PART_MOM_STENCIL = 1, 2, 4, 8, 16
 
 # field ids (enum tpls_field)
 TIMERS = ["advect", "levelset", "csf", "visc", "mom_rhs", "jacobi", "sor_even", "sor_odd", "pressure", "project",
@@ -54,7 +55,7 @@ class TplsParams(C.Structure):
                 ("height", C.c_double), ("scap", C.c_double), ("smooth_width", C.c_double),
                 ("mom_u", C.c_int), ("mom_v", C.c_int), ("mom_w", C.c_int), ("levelset", C.c_int),
                 ("p_rtol", C.c_double), ("p_maxits", C.c_int), ("precision", C.c_int),
-                ("reserved", C.c_int * 6)]
+                ("fp64_parts", C.c_int), ("reserved", C.c_int * 5)]
 
 
 class TplsStats(C.Structure):
@@ -87,6 +88,7 @@ class Params:
     p_rtol: float = 1e-5
     p_maxits: int = 200
     precision: int = TPLS_PREC_FP64
+    fp64_parts: int = 0  # FP32-mixed form: PART_* bits kept in FP64
     extra: dict = field(default_factory=dict)
 
     def to_c(self) -> TplsParams:

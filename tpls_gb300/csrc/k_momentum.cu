@@ -189,9 +189,9 @@ __device__ __forceinline__ void store_rec<float>(float *rec, float a0, float a1,
   o[1] = make_float4(a4, a5, a6, 0.f);
 }
 
-template <typename T>
+template <typename T, typename TR>
 __device__ __forceinline__ void write_coef(int comp, const Geo &g, const Helm &h, const FcT<T> &f,
-                                           double rhs, int k, T *__restrict__ rec) {
+                                           double rhs, int k, TR *__restrict__ rec) {
   const T ax2 = (T)h.ax2, ay2 = (T)h.ay2, az2 = (T)h.az2;
   const T diag = (T)1 + ax2 * (f.px + f.mx) + ay2 * (f.py + f.my) + az2 * (f.pz + f.mz);
   const T r = (T)1 / diag;
@@ -205,19 +205,22 @@ __device__ __forceinline__ void write_coef(int comp, const Geo &g, const Helm &h
       czp = (T)(-2) * czp;
     }
   }
-  store_rec<T>(rec, ax2 * f.px * r, ax2 * f.mx * r, ay2 * f.py * r, ay2 * f.my * r, czp, czm, (T)rhs * r);
+  store_rec<TR>(rec, (TR)(ax2 * f.px * r), (TR)(ax2 * f.mx * r), (TR)(ay2 * f.py * r), (TR)(ay2 * f.my * r),
+                (TR)czp, (TR)czm, (TR)((T)rhs * r));
 }
 
 // X64 is the component's FP64 state (u2, v2 or w2): the right-hand side is
 // assembled in FP64 even when the stencils run in FP32 (T = float).
-template <typename T>
+// TR: storage of the sweep records (T, or float when FP64 stencils feed the
+// FP32 sweeps of the FP32-mixed form).
+template <typename T, typename TR>
 __global__ void __launch_bounds__(MB_X *MB_Y)
     k_mom_rhs(int comp, Geo g, Phys ph, Helm hm, const T *__restrict__ U, const T *__restrict__ V,
               const T *__restrict__ W, const double *__restrict__ X64, const T *__restrict__ mu,
               const T *__restrict__ fc, const double *__restrict__ c1, const double *__restrict__ c0,
               const double *__restrict__ s1, const double *__restrict__ s0, double *__restrict__ conv2,
               double *__restrict__ csf2, double *__restrict__ rhs, double *__restrict__ diff_out,
-              T *__restrict__ coef) {
+              TR *__restrict__ coef) {
   const int i = blockIdx.x * MB_X + threadIdx.x + 1, j = blockIdx.y * MB_Y + threadIdx.y + 1;
   const int k = blockIdx.z;
   if (i > g.nx || j > g.ny) return;
@@ -244,18 +247,18 @@ __global__ void __launch_bounds__(MB_X *MB_Y)
   csf2[c] = s2;
   if (rhs) rhs[c] = r;
   if (diff_out) diff_out[c] = diff;
-  if (coef && valid) write_coef(comp, g, hm, f, r, k, coef + 8 * (size_t)rec_slot(g, c, i));
+  if (coef && valid) write_coef<T, TR>(comp, g, hm, f, r, k, coef + 8 * (size_t)rec_slot(g, c, i));
 }
 
-template <typename T>
+template <typename T, typename TR = T>
 static cudaError_t mom_rhs(int comp, const Geo &g, const Phys &ph, const T *u2, const T *v2, const T *w2,
                            const double *x64, const T *mu, const T *fcsf, const double *c1, const double *c0,
                            const double *s1, const double *s0, double *conv2, double *csf2, double *rhs,
-                           double *diff_out, T *coef, cudaStream_t st) {
+                           double *diff_out, TR *coef, cudaStream_t st) {
   const int nk = (comp == 2) ? g.nz + 1 : g.nz;
   dim3 grd((g.nx + MB_X - 1) / MB_X, (g.ny + MB_Y - 1) / MB_Y, nk);
-  k_mom_rhs<T><<<grd, dim3(MB_X, MB_Y), 0, st>>>(comp, g, ph, helm_of(ph), u2, v2, w2, x64, mu, fcsf, c1, c0,
-                                                 s1, s0, conv2, csf2, rhs, diff_out, coef);
+  k_mom_rhs<T, TR><<<grd, dim3(MB_X, MB_Y), 0, st>>>(comp, g, ph, helm_of(ph), u2, v2, w2, x64, mu, fcsf, c1,
+                                                     c0, s1, s0, conv2, csf2, rhs, diff_out, coef);
   return cudaGetLastError();
 }
 
@@ -271,6 +274,14 @@ cudaError_t launch_mom_rhs(int comp, const Geo &g, const Phys &ph,
                          coef, st);
 }
 
+cudaError_t launch_mom_rhs64r32(int comp, const Geo &g, const Phys &ph, const double *u2, const double *v2,
+                                const double *w2, const double *mu, const double *fcsf, const double *c1,
+                                const double *c0, const double *s1, const double *s0, double *conv2,
+                                double *csf2, float *coef, cudaStream_t st) {
+  const double *x64 = (comp == 0) ? u2 : (comp == 1) ? v2 : w2;
+  return mom_rhs<double, float>(comp, g, ph, u2, v2, w2, x64, mu, fcsf, c1, c0, s1, s0, conv2, csf2, nullptr,
+                                nullptr, coef, st);
+}
 cudaError_t launch_mom_rhs32(int comp, const Geo &g, const Phys &ph, const float *u2, const float *v2,
                              const float *w2, const double *x64, const float *mu, const float *fcsf,
                              const double *c1, const double *c0, const double *s1, const double *s0,

@@ -47,6 +47,8 @@ struct PLevel {
   double cx, cy, cz;
   void *b = nullptr, *e = nullptr, *e2 = nullptr, *r = nullptr, *t = nullptr;
   void *thomas = nullptr;  // [3 classes][nz][2] = (cprime, inv_den)
+  int point = 0;  // near-isotropic level: red-black Gauss-Seidel instead of z-lines
+  double invd[3][3];  // point smoother: 1/diagonal by x class (first, interior, last) and z class
 };
 
 struct PoissonSolver {
@@ -445,6 +447,50 @@ static inline dim3 mg_grid(int nx, int ny, int nz) {
   return dim3((nx + MG_BX - 1) / MG_BX, (ny + MG_BY - 1) / MG_BY, nz);
 }
 
+// Red-black Gauss-Seidel half-sweep for near-isotropic levels (where
+// z-lines buy nothing): points with (i + j + k) % 2 == colour get
+// e = (b + sum of neighbour couplings) / diagonal; with `copy`, the other
+// colour is copied from ein to eout so that eout holds the whole iterate.
+// One thread per x pair.  zero_init: ein is zero (first half-sweep from a
+// zero start).
+template <typename R>
+struct InvD {
+  R v[3][3];
+};
+
+template <typename R, typename TB, typename TE, typename TO>
+__global__ void k_rbgs(LevArgs<R> L, InvD<R> inv, int colour, int zero_init, int copy, const TB *__restrict__ b,
+                       const TE *ein, TO *eout) {
+  const int nx = L.nx, ny = L.ny, nz = L.nz;
+  const int i2 = blockIdx.x * MG_BX + threadIdx.x, j = blockIdx.y * MG_BY + threadIdx.y, k = blockIdx.z;
+  if (2 * i2 >= nx || j >= ny) return;
+  const int plane = nx * ny;
+  const int jm = (j > 0) ? -nx : nx * (ny - 1), jp = (j < ny - 1) ? nx : -nx * (ny - 1);
+  const int zc = (nz == 1) ? 1 : ((k == 0) ? 0 : ((k == nz - 1) ? 2 : 1));
+  for (int q = 0; q < 2; q++) {
+    const int i = 2 * i2 + q;
+    if (i >= nx) break;
+    const int c = i + nx * j + plane * k;
+    if (((i + j + k) & 1) == colour) {
+      R acc = (R)b[c];
+      if (!zero_init) {
+        R sx = (R)0, sz = (R)0;
+        if (i > 0) sx += (R)ein[c - 1];
+        if (i < nx - 1) sx += (R)ein[c + 1];
+        if (k > 0) sz += (R)ein[c - plane];
+        if (k < nz - 1) sz += (R)ein[c + plane];
+        acc = fma(L.cx, sx, acc);
+        acc = fma(L.cy, (R)ein[c + jm] + (R)ein[c + jp], acc);
+        acc = fma(L.cz, sz, acc);
+      }
+      const int xc = (nx == 1) ? 1 : ((i == 0) ? 0 : ((i == nx - 1) ? 2 : 1));
+      eout[c] = (TO)(acc * inv.v[xc][zc]);
+    } else if (copy) {
+      eout[c] = (TO)ein[c];
+    }
+  }
+}
+
 template <typename R, typename TB, typename TE>
 __global__ void k_residual(LevArgs<R> L, const TB *__restrict__ b, const TE *__restrict__ e, R *__restrict__ r) {
   const int nx = L.nx, ny = L.ny, nz = L.nz;
@@ -693,6 +739,18 @@ cudaError_t poisson_create(const Geo &g, double cx, double cy, double cz, int fp
   const size_t esz = S->fp32 ? sizeof(float) : sizeof(double);
   for (size_t l = 0; l < S->lv.size(); l++) {
     PLevel &L = S->lv[l];
+    {
+      const double cmax = fmax(fmax(L.cx, L.cy), L.cz), cmin = fmin(fmin(L.cx, L.cy), L.cz);
+      // red-black needs an even periodic y extent (j = 0 and ny - 1 are
+      // neighbours); otherwise, or when z couplings dominate, z-lines
+      L.point = (cmax <= 2.0 * cmin && L.ny % 2 == 0) ? 1 : 0;
+      for (int a = 0; a < 3; a++)
+        for (int q = 0; q < 3; q++) {
+          const double nbx = (L.nx == 1) ? 0.0 : ((a == 1) ? 2.0 : 1.0);
+          const double nbz = (L.nz == 1) ? 0.0 : ((q == 1) ? 2.0 : 1.0);
+          L.invd[a][q] = 1.0 / (L.cx * nbx + 2.0 * L.cy + L.cz * nbz);
+        }
+    }
     const size_t bytes = esz * (size_t)L.n;
     if (l > 0) PCK(cudaMalloc(&L.b, bytes));
     PCK(cudaMalloc(&L.e, bytes));
@@ -878,6 +936,45 @@ static cudaError_t prolong_chain(const PLevel &F, const PLevel &C, const R *ec, 
   return cudaGetLastError();
 }
 
+template <typename R>
+static InvD<R> invd_of(const PLevel &L) {
+  InvD<R> v;
+  for (int a = 0; a < 3; a++)
+    for (int q = 0; q < 3; q++) v.v[a][q] = (R)L.invd[a][q];
+  return v;
+}
+
+// pre-smoothing from a zero start into e2: z-line Jacobi, or red then black
+template <typename R, typename TB>
+static void pre_smooth(const PLevel &L, R w, R w1, const TB *b, R *e2, cudaStream_t st, long *nl) {
+  if (!L.point) {
+    line_sweep<R, TB, R, R>(L, w, w1, 1, b, nullptr, e2, st);
+    (*nl)++;
+    return;
+  }
+  const LevArgs<R> A = largs<R>(L);
+  const dim3 grd = mg_grid((L.nx + 1) / 2, L.ny, L.nz);
+  k_rbgs<R, TB, R, R><<<grd, dim3(MG_BX, MG_BY), 0, st>>>(A, invd_of<R>(L), 0, 1, 0, b, e2, e2);
+  k_rbgs<R, TB, R, R><<<grd, dim3(MG_BX, MG_BY), 0, st>>>(A, invd_of<R>(L), 1, 0, 0, b, e2, e2);
+  *nl += 2;
+}
+
+// post-smoothing of e2 into res: z-line Jacobi, or black (in place) then red
+// (with the black values copied), the adjoint order of the pre-smoothing
+template <typename R, typename TB, typename TO>
+static void post_smooth(const PLevel &L, R w, R w1, const TB *b, R *e2, TO *res, cudaStream_t st, long *nl) {
+  if (!L.point) {
+    line_sweep<R, TB, R, TO>(L, w, w1, 0, b, e2, res, st);
+    (*nl)++;
+    return;
+  }
+  const LevArgs<R> A = largs<R>(L);
+  const dim3 grd = mg_grid((L.nx + 1) / 2, L.ny, L.nz);
+  k_rbgs<R, TB, R, R><<<grd, dim3(MG_BX, MG_BY), 0, st>>>(A, invd_of<R>(L), 1, 0, 0, b, e2, e2);
+  k_rbgs<R, TB, R, TO><<<grd, dim3(MG_BX, MG_BY), 0, st>>>(A, invd_of<R>(L), 0, 0, 1, b, e2, res);
+  *nl += 2;
+}
+
 // one symmetric V-cycle: out = M b0.  Every level pre-smooths into its
 // scratch e2 (one damped line-Jacobi sweep from zero), restricts the
 // residual, adds the prolonged coarse correction into e2 and post-smooths
@@ -936,16 +1033,16 @@ static cudaError_t vcycle(PoissonSolver *S, const double *b0, double *out, cudaS
     }
     const LevArgs<R> A = largs<R>(L);
     if (l == 0) {
-      line_sweep<R, double, R, R>(L, w, w1, 1, b0, nullptr, lvp(L.e2), st);
+      pre_smooth<R, double>(L, w, w1, b0, lvp(L.e2), st, nl);
       k_residual<R, double, R><<<mg_grid(L.nx, L.ny, L.nz), dim3(MG_BX, MG_BY), 0, st>>>(A, b0, lvp(L.e2),
                                                                                     lvp(L.r));
     } else {
-      line_sweep<R, R, R, R>(L, w, w1, 1, b, nullptr, lvp(L.e2), st);
+      pre_smooth<R, R>(L, w, w1, b, lvp(L.e2), st, nl);
       k_residual<R, R, R><<<mg_grid(L.nx, L.ny, L.nz), dim3(MG_BX, MG_BY), 0, st>>>(A, b, lvp(L.e2), lvp(L.r));
     }
     const PLevel &C = S->lv[l + 1];
     PCK(restrict_chain<R>(L, C, lvp(L.r), lvp(L.t), lvp(C.b), st, nl));
-    *nl += 2;
+    *nl += 1;
     PCK(cudaGetLastError());
   }
   for (int l = nlev - 2; l >= 0; l--) {
@@ -954,10 +1051,9 @@ static cudaError_t vcycle(PoissonSolver *S, const double *b0, double *out, cudaS
     const LevArgs<R> A = largs<R>(L);
     PCK(prolong_chain<R>(L, C, lvp(C.e), lvp(L.t), lvp(L.e2), st, nl));
     if (l == 0)
-      line_sweep<R, double, R, double>(L, w, w1, 0, b0, lvp(L.e2), out, st);
+      post_smooth<R, double, double>(L, w, w1, b0, lvp(L.e2), out, st, nl);
     else
-      line_sweep<R, R, R, R>(L, w, w1, 0, lvp(L.b), lvp(L.e2), lvp(L.e), st);
-    *nl += 1;
+      post_smooth<R, R, R>(L, w, w1, lvp(L.b), lvp(L.e2), lvp(L.e), st, nl);
     PCK(cudaGetLastError());
   }
   return cudaSuccess;

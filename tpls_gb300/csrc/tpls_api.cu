@@ -140,6 +140,9 @@ static int field_kind(int f) {
   }
 }
 
+// the momentum iterates are FP32 (the FP32-mixed form without FP64 momentum)
+static bool x3_fp32(const tpls_ctx *c) { return c->mixed && !(c->prm.fp64_parts & TPLS_PART_MOMENTUM); }
+
 static double *field_ptr(tpls_ctx *c, int f) {
   const int s0 = c->phase % 3, s1 = (c->phase + 1) % 3, s2 = (c->phase + 2) % 3;
   switch (f) {
@@ -168,9 +171,9 @@ static double *field_ptr(tpls_ctx *c, int f) {
     case TPLS_F_CONV2_PHI: return c->conv_phi[s1];
     case TPLS_F_PHI3: return c->phi2;
     case TPLS_F_RHS_P: return c->rhs_p;
-    case TPLS_F_U3: return c->mixed ? c->x3d : c->x3[0][c->x3_final[0]];
-    case TPLS_F_V3: return c->mixed ? c->x3d : c->x3[1][c->x3_final[1]];
-    case TPLS_F_W3: return c->mixed ? c->x3d : c->x3[2][c->x3_final[2]];
+    case TPLS_F_U3: return x3_fp32(c) ? c->x3d : c->x3[0][c->x3_final[0]];
+    case TPLS_F_V3: return x3_fp32(c) ? c->x3d : c->x3[1][c->x3_final[1]];
+    case TPLS_F_W3: return x3_fp32(c) ? c->x3d : c->x3[2][c->x3_final[2]];
     default: return nullptr;
   }
   (void)s2;
@@ -334,6 +337,30 @@ static int create_impl(int nx, int ny, int nz, const tpls_params *prm, const dou
     }
     TCK(alloc_field(c, 1, ny + 4, nz + 2, &c->mu));
   } else {
+    const int parts = prm->fp64_parts;
+    if (parts & TPLS_PART_LEVELSET) {
+      TCK(alloc_p(c, &c->phiB));
+      TCK(alloc_p(c, &c->D));
+    }
+    if (parts & (TPLS_PART_MOMENTUM | TPLS_PART_MOM_STENCIL)) {  // FP64 stencil inputs
+      double **pf2[] = {&c->fx, &c->fy, &c->fz};
+      for (double **p : pf2) TCK(alloc_p(c, p));
+      TCK(alloc_field(c, 1, ny + 4, nz + 2, &c->mu));
+    }
+    if (parts & TPLS_PART_MOMENTUM) {
+      double **px3[] = {&c->x3[0][0], &c->x3[0][1], &c->x3[1][0], &c->x3[1][1]};
+      for (double **p : px3) TCK(alloc_field(c, 0, ny + 2, nz, p));
+      TCK(alloc_field(c, 0, ny + 2, nz + 1, &c->x3[2][0]));
+      TCK(alloc_field(c, 0, ny + 2, nz + 1, &c->x3[2][1]));
+      for (int q = 0; q < 3; q++) {
+        void *b = nullptr;
+        const size_t n = (size_t)rec * c->px * (ny + 2) * (q == 2 ? nz + 1 : nz);
+        TCK(cudaMalloc(&b, n * sizeof(double)));
+        c->allocs.push_back(b);
+        TCK(cudaMemset(b, 0, n * sizeof(double)));
+        c->coef[q] = (double *)b;
+      }
+    }
     float **qf[] = {&c->phi32, &c->D32, &c->fx32, &c->fy32, &c->fz32, &c->prA32, &c->prB32};
     for (float **p : qf) TCK(alloc_p(c, p));
     float **quv[] = {&c->u32, &c->v32, &c->x3f[0][0], &c->x3f[0][1], &c->x3f[1][0], &c->x3f[1][1]};
@@ -388,7 +415,7 @@ static int create_impl(int nx, int ny, int nz, const tpls_params *prm, const dou
     c->scal_host = (double *)b;
   }
   TCK(poisson_create(c->g, 1.0 / (prm->dy * prm->dy), 1.0 / (prm->dx * prm->dx), 1.0 / (prm->dz * prm->dz),
-                     c->mixed, &c->ps));
+                     c->mixed && !(prm->fp64_parts & TPLS_PART_MULTIGRID), &c->ps));
   memset(&c->stats, 0, sizeof(c->stats));
   TCK(cudaDeviceSynchronize());
   return TPLS_OK;
@@ -474,7 +501,7 @@ int tpls_set_field(tpls_ctx *c, int f, const double *host) {
   double *d = field_ptr(c, f);
   if (!d) return TPLS_ERR_ARG;
   TCK(h2d(c, d, host, nz_planes(field_kind(f), c->nz)));
-  if (c->mixed && is_x3(f)) {
+  if (x3_fp32(c) && is_x3(f)) {
     size_t n;
     float *x = mixed_x3(c, f, &n);
     TCK(launch_to_float(d - XOFF, x - XOFF, n, c->st));
@@ -488,7 +515,7 @@ int tpls_get_field(tpls_ctx *c, int f, double *host) {
   if (!c || !host || f < 0 || f >= TPLS_F_COUNT) return TPLS_ERR_ARG;
   double *d = field_ptr(c, f);
   if (!d) return TPLS_ERR_ARG;
-  if (c->mixed && is_x3(f)) {
+  if (x3_fp32(c) && is_x3(f)) {
     size_t n;
     const float *x = mixed_x3(c, f, &n);
     TCK(launch_to_double(x - XOFF, d - XOFF, n, c->st));
@@ -685,67 +712,142 @@ static int step_once_mixed(tpls_ctx *c) {
   const Phys &ph = c->ph;
   cudaStream_t st = c->st;
   const int s0 = c->phase % 3, s1 = (c->phase + 1) % 3, s2 = (c->phase + 2) % 3;
+  const int parts = c->prm.fp64_parts;
+  const bool adv64 = parts & TPLS_PART_ADVECT, ls64 = parts & TPLS_PART_LEVELSET;
+  const bool mom64 = parts & TPLS_PART_MOMENTUM;
+  const bool sten64 = mom64 || (parts & TPLS_PART_MOM_STENCIL);
   {
     PhaseScope ps(c, TPLS_T_VISC);
-    LCK(c, launch_visc(g, ph, c->phi2, c->mu32, st));
+    if (sten64) LCK(c, launch_visc(g, ph, c->phi2, c->mu, st));
+    else LCK(c, launch_visc(g, ph, c->phi2, c->mu32, st));
   }
   {
     PhaseScope ps(c, TPLS_T_ADVECT);
-    LCK(c, launch_to_float(c->phi2 - XOFF, c->phi32 - XOFF, c->n_p, st));
-    LCK(c, launch_to_float(c->u2 - XOFF, c->u32 - XOFF, c->n_uv, st));
-    LCK(c, launch_to_float(c->v2 - XOFF, c->v32 - XOFF, c->n_uv, st));
-    LCK(c, launch_to_float(c->w2 - XOFF, c->w32 - XOFF, c->n_w, st));
-    LCK(c, launch_advect(g, ph, (const float *)c->phi32, c->u32, c->v32, c->w32, c->conv_phi[s2], st));
+    if (!sten64 || !adv64) {  // FP32 copies of the velocity state
+      LCK(c, launch_to_float(c->u2 - XOFF, c->u32 - XOFF, c->n_uv, st));
+      LCK(c, launch_to_float(c->v2 - XOFF, c->v32 - XOFF, c->n_uv, st));
+      LCK(c, launch_to_float(c->w2 - XOFF, c->w32 - XOFF, c->n_w, st));
+    }
+    if (adv64) {
+      LCK(c, launch_advect(g, ph, c->phi2, c->u2, c->v2, c->w2, c->conv_phi[s2], st));
+    } else {
+      LCK(c, launch_to_float(c->phi2 - XOFF, c->phi32 - XOFF, c->n_p, st));
+      LCK(c, launch_advect(g, ph, (const float *)c->phi32, c->u32, c->v32, c->w32, c->conv_phi[s2], st));
+    }
   }
   PhaseScope *ls_scope = new PhaseScope(c, TPLS_T_LEVELSET);
   LCK(c, launch_ls_ab3(g, ph, c->phi2, c->conv_phi[s0], c->conv_phi[s1], c->conv_phi[s2], c->phiA, st));
-  LCK(c, launch_ls_status(g, ph, c->phiA, c->D32, c->flags, st));
   const int L = c->prm.levelset;
+  if (ls64) LCK(c, launch_ls_status(g, ph, c->phiA, c->D, c->flags, st));
+  else LCK(c, launch_ls_status(g, ph, c->phiA, c->D32, c->flags, st));
   if (L <= 0) {
     TCK(cudaMemcpyAsync(c->phi2 - XOFF, c->phiA - XOFF, sizeof(double) * c->n_p, cudaMemcpyDeviceToDevice, st));
     TCK(cudaMemsetAsync(c->scal + SC_ERR_PHI, 0, sizeof(double), st));
   }
   for (int it = 1; it <= L; it++) {
-    const double *src64 = (it == 1) ? c->phiA : nullptr;
-    const float *src32 = (it == 1) ? nullptr : ((it % 2 == 0) ? c->prB32 : c->prA32);
-    double *dst64 = (it == L) ? c->phi2 : nullptr;
-    float *dst32 = (it == L) ? nullptr : ((it % 2 == 1) ? c->prB32 : c->prA32);
-    LCK(c, launch_ls_iter32(g, ph, src64, src32, c->D32, c->flags, dst64, dst32, (it == L) ? c->part : nullptr,
-                            st));
+    double *ep = (it == L) ? c->part : nullptr;
+    if (ls64) {
+      const double *src = (it == 1) ? c->phiA : ((it % 2 == 0) ? c->phiB : c->phiA);
+      double *dst = (it == L) ? c->phi2 : ((it % 2 == 1) ? c->phiB : c->phiA);
+      LCK(c, launch_ls_iter(g, ph, src, c->D, c->flags, dst, ep, st));
+    } else {
+      const double *src64 = (it == 1) ? c->phiA : nullptr;
+      const float *src32 = (it == 1) ? nullptr : ((it % 2 == 0) ? c->prB32 : c->prA32);
+      double *dst64 = (it == L) ? c->phi2 : nullptr;
+      float *dst32 = (it == L) ? nullptr : ((it % 2 == 1) ? c->prB32 : c->prA32);
+      LCK(c, launch_ls_iter32(g, ph, src64, src32, c->D32, c->flags, dst64, dst32, ep, st));
+    }
   }
   if (L > 0) LCK(c, finish_sum(c->part, ls_iter_blocks(g), c->scal + SC_ERR_PHI, 1, st));
   delete ls_scope;
-  {
-    PhaseScope ps(c, TPLS_T_CSF);
-    LCK(c, launch_csf(g, ph, c->phi2, c->fx32, c->fy32, c->fz32, st));
-  }
-  {
-    PhaseScope ps(c, TPLS_T_MOM_RHS);
-    LCK(c, launch_mom_rhs32(0, g, ph, c->u32, c->v32, c->w32, c->u2, c->mu32, c->fx32, c->conv_u[s1],
-                            c->conv_u[s0], c->csf_u[s1], c->csf_u[s0], c->conv_u[s2], c->csf_u[s2], c->coef32[0],
-                            st));
-    LCK(c, launch_mom_rhs32(1, g, ph, c->u32, c->v32, c->w32, c->v2, c->mu32, c->fy32, c->conv_v[s1],
-                            c->conv_v[s0], c->csf_v[s1], c->csf_v[s0], c->conv_v[s2], c->csf_v[s2], c->coef32[1],
-                            st));
-    LCK(c, launch_mom_rhs32(2, g, ph, c->u32, c->v32, c->w32, c->w2, c->mu32, c->fz32, c->conv_w[s1],
-                            c->conv_w[s0], c->csf_w[s1], c->csf_w[s0], c->conv_w[s2], c->csf_w[s2], c->coef32[2],
-                            st));
-  }
   int s;
-  if ((s = momentum<float>(c, 0, c->coef32[0], c->x3f[0], c->prm.mom_u))) return s;
-  if ((s = momentum<float>(c, 1, c->coef32[1], c->x3f[1], c->prm.mom_v))) return s;
-  if ((s = momentum<float>(c, 2, c->coef32[2], c->x3f[2], c->prm.mom_w))) return s;
-  const float *u3 = c->x3f[0][c->x3_final[0]], *v3 = c->x3f[1][c->x3_final[1]], *w3 = c->x3f[2][c->x3_final[2]];
+  const void *u3v;
+  const void *v3v, *w3v;
+  if (mom64) {
+    {
+      PhaseScope ps(c, TPLS_T_CSF);
+      LCK(c, launch_csf(g, ph, c->phi2, c->fx, c->fy, c->fz, st));
+    }
+    {
+      PhaseScope ps(c, TPLS_T_MOM_RHS);
+      LCK(c, launch_mom_rhs(0, g, ph, c->u2, c->v2, c->w2, c->mu, c->fx, c->conv_u[s1], c->conv_u[s0],
+                            c->csf_u[s1], c->csf_u[s0], c->conv_u[s2], c->csf_u[s2], nullptr, nullptr, c->coef[0],
+                            st));
+      LCK(c, launch_mom_rhs(1, g, ph, c->u2, c->v2, c->w2, c->mu, c->fy, c->conv_v[s1], c->conv_v[s0],
+                            c->csf_v[s1], c->csf_v[s0], c->conv_v[s2], c->csf_v[s2], nullptr, nullptr, c->coef[1],
+                            st));
+      LCK(c, launch_mom_rhs(2, g, ph, c->u2, c->v2, c->w2, c->mu, c->fz, c->conv_w[s1], c->conv_w[s0],
+                            c->csf_w[s1], c->csf_w[s0], c->conv_w[s2], c->csf_w[s2], nullptr, nullptr, c->coef[2],
+                            st));
+    }
+    if ((s = momentum<double>(c, 0, c->coef[0], c->x3[0], c->prm.mom_u))) return s;
+    if ((s = momentum<double>(c, 1, c->coef[1], c->x3[1], c->prm.mom_v))) return s;
+    if ((s = momentum<double>(c, 2, c->coef[2], c->x3[2], c->prm.mom_w))) return s;
+    u3v = c->x3[0][c->x3_final[0]];
+    v3v = c->x3[1][c->x3_final[1]];
+    w3v = c->x3[2][c->x3_final[2]];
+  } else if (sten64) {
+    {
+      PhaseScope ps(c, TPLS_T_CSF);
+      LCK(c, launch_csf(g, ph, c->phi2, c->fx, c->fy, c->fz, st));
+    }
+    {
+      PhaseScope ps(c, TPLS_T_MOM_RHS);
+      LCK(c, launch_mom_rhs64r32(0, g, ph, c->u2, c->v2, c->w2, c->mu, c->fx, c->conv_u[s1], c->conv_u[s0],
+                                 c->csf_u[s1], c->csf_u[s0], c->conv_u[s2], c->csf_u[s2], c->coef32[0], st));
+      LCK(c, launch_mom_rhs64r32(1, g, ph, c->u2, c->v2, c->w2, c->mu, c->fy, c->conv_v[s1], c->conv_v[s0],
+                                 c->csf_v[s1], c->csf_v[s0], c->conv_v[s2], c->csf_v[s2], c->coef32[1], st));
+      LCK(c, launch_mom_rhs64r32(2, g, ph, c->u2, c->v2, c->w2, c->mu, c->fz, c->conv_w[s1], c->conv_w[s0],
+                                 c->csf_w[s1], c->csf_w[s0], c->conv_w[s2], c->csf_w[s2], c->coef32[2], st));
+    }
+    if ((s = momentum<float>(c, 0, c->coef32[0], c->x3f[0], c->prm.mom_u))) return s;
+    if ((s = momentum<float>(c, 1, c->coef32[1], c->x3f[1], c->prm.mom_v))) return s;
+    if ((s = momentum<float>(c, 2, c->coef32[2], c->x3f[2], c->prm.mom_w))) return s;
+    u3v = c->x3f[0][c->x3_final[0]];
+    v3v = c->x3f[1][c->x3_final[1]];
+    w3v = c->x3f[2][c->x3_final[2]];
+  } else {
+    {
+      PhaseScope ps(c, TPLS_T_CSF);
+      LCK(c, launch_csf(g, ph, c->phi2, c->fx32, c->fy32, c->fz32, st));
+    }
+    {
+      PhaseScope ps(c, TPLS_T_MOM_RHS);
+      LCK(c, launch_mom_rhs32(0, g, ph, c->u32, c->v32, c->w32, c->u2, c->mu32, c->fx32, c->conv_u[s1],
+                              c->conv_u[s0], c->csf_u[s1], c->csf_u[s0], c->conv_u[s2], c->csf_u[s2],
+                              c->coef32[0], st));
+      LCK(c, launch_mom_rhs32(1, g, ph, c->u32, c->v32, c->w32, c->v2, c->mu32, c->fy32, c->conv_v[s1],
+                              c->conv_v[s0], c->csf_v[s1], c->csf_v[s0], c->conv_v[s2], c->csf_v[s2],
+                              c->coef32[1], st));
+      LCK(c, launch_mom_rhs32(2, g, ph, c->u32, c->v32, c->w32, c->w2, c->mu32, c->fz32, c->conv_w[s1],
+                              c->conv_w[s0], c->csf_w[s1], c->csf_w[s0], c->conv_w[s2], c->csf_w[s2],
+                              c->coef32[2], st));
+    }
+    if ((s = momentum<float>(c, 0, c->coef32[0], c->x3f[0], c->prm.mom_u))) return s;
+    if ((s = momentum<float>(c, 1, c->coef32[1], c->x3f[1], c->prm.mom_v))) return s;
+    if ((s = momentum<float>(c, 2, c->coef32[2], c->x3f[2], c->prm.mom_w))) return s;
+    u3v = c->x3f[0][c->x3_final[0]];
+    v3v = c->x3f[1][c->x3_final[1]];
+    w3v = c->x3f[2][c->x3_final[2]];
+  }
   int its = 0, reason = 0;
   double rn = 0.0, bn = 0.0;
   {
     PhaseScope ps(c, TPLS_T_PRESSURE);
-    LCK(c, launch_source(g, ph, u3, v3, w3, c->rhs_p, st));
-    if ((s = pressure_stage(c, u3, 1, &its, &rn, &bn, &reason))) return s;
+    if (mom64)
+      LCK(c, launch_source(g, ph, (const double *)u3v, (const double *)v3v, (const double *)w3v, c->rhs_p, st));
+    else
+      LCK(c, launch_source(g, ph, (const float *)u3v, (const float *)v3v, (const float *)w3v, c->rhs_p, st));
+    if ((s = pressure_stage(c, u3v, mom64 ? 0 : 1, &its, &rn, &bn, &reason))) return s;
   }
   {
     PhaseScope ps(c, TPLS_T_PROJECT);
-    LCK(c, launch_project(g, ph, u3, v3, w3, c->pres, c->u_inlet, c->u2, c->v2, c->w2, st));
+    if (mom64)
+      LCK(c, launch_project(g, ph, (const double *)u3v, (const double *)v3v, (const double *)w3v, c->pres,
+                            c->u_inlet, c->u2, c->v2, c->w2, st));
+    else
+      LCK(c, launch_project(g, ph, (const float *)u3v, (const float *)v3v, (const float *)w3v, c->pres,
+                            c->u_inlet, c->u2, c->v2, c->w2, st));
     TCK(cudaMemcpyAsync(c->pres_old - XOFF, c->pres - XOFF, sizeof(double) * c->n_p, cudaMemcpyDeviceToDevice,
                         st));
   }

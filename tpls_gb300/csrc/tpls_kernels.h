@@ -83,6 +83,15 @@ cudaError_t launch_mom_rhs32(int comp, const Geo &g, const Phys &ph,
                              const double *c0, const double *s1,
                              const double *s0, double *conv2, double *csf2,
                              float *coef, cudaStream_t st);
+// FP64 stencils and records rounded to FP32 records (FP32-mixed form with
+// TPLS_PART_MOM_STENCIL).
+cudaError_t launch_mom_rhs64r32(int comp, const Geo &g, const Phys &ph,
+                                const double *u2, const double *v2,
+                                const double *w2, const double *mu,
+                                const double *fcsf, const double *c1,
+                                const double *c0, const double *s1,
+                                const double *s0, double *conv2,
+                                double *csf2, float *coef, cudaStream_t st);
 // Standalone get_conv_all / get_diffusion_all (per-routine entries).
 cudaError_t launch_conv_diff(int comp, int want_conv, const Geo &g,
                              const Phys &ph, const double *u2,
