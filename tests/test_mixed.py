@@ -60,17 +60,20 @@ def test_mixed_twenty_steps_and_volume():
     mix.close()
 
 
-def test_mixed_deterministic_and_u3_view():
-    a, b = _ctx(1), _ctx(1)
+def test_mixed_deterministic_and_u3():
+    """Deterministic; u3 is the FP64 state plus the FP32 defect, close to
+    the FP64 form's u3 (not an FP32-rounded field)."""
+    a, b, r = _ctx(1), _ctx(1), _ctx(0)
     a.step(4)
     b.step(4)
+    r.step(4)
     sa, sb = a.get_state(), b.get_state()
     assert all(np.array_equal(sa[k], sb[k]) for k in STATE_FIELDS)
-    u3 = a.get_field("U3")  # the FP32 iterate widened to FP64
-    assert np.array_equal(u3, u3.astype(np.float32).astype(np.float64))
-    assert np.abs(u3[1:NX, 1:NY + 1, :]).max() > 1.0
-    a.close()
-    b.close()
+    u3 = a.get_field("U3")
+    assert not np.array_equal(u3, u3.astype(np.float32).astype(np.float64))
+    assert relmax(u3, r.get_field("U3"), ROWS) < 1e-6
+    for g in (a, b, r):
+        g.close()
 
 
 def test_mixed_with_every_part_fp64_equals_fp64_form():

@@ -189,9 +189,13 @@ __device__ __forceinline__ void store_rec<float>(float *rec, float a0, float a1,
   o[1] = make_float4(a4, a5, a6, 0.f);
 }
 
+// With X (the FP64 state of the component; FP32-mixed sweeps in defect form)
+// the stored b is that of d = x - X: b + sum(c_n X_n) - X_c, in FP64 with the
+// stored (rounded) coefficients, the neighbours taken as the sweeps take them.
 template <typename T, typename TR>
 __device__ __forceinline__ void write_coef(int comp, const Geo &g, const Helm &h, const FcT<T> &f,
-                                           double rhs, int k, TR *__restrict__ rec) {
+                                           double rhs, int k, const double *__restrict__ X, int c,
+                                           TR *__restrict__ rec) {
   const T ax2 = (T)h.ax2, ay2 = (T)h.ay2, az2 = (T)h.az2;
   const T diag = (T)1 + ax2 * (f.px + f.mx) + ay2 * (f.py + f.my) + az2 * (f.pz + f.mz);
   const T r = (T)1 / diag;
@@ -205,8 +209,32 @@ __device__ __forceinline__ void write_coef(int comp, const Geo &g, const Helm &h
       czp = (T)(-2) * czp;
     }
   }
-  store_rec<TR>(rec, (TR)(ax2 * f.px * r), (TR)(ax2 * f.mx * r), (TR)(ay2 * f.py * r), (TR)(ay2 * f.my * r),
-                (TR)czp, (TR)czm, (TR)((T)rhs * r));
+  const TR cxp = (TR)(ax2 * f.px * r), cxm = (TR)(ax2 * f.mx * r), cyp = (TR)(ay2 * f.py * r),
+           cym = (TR)(ay2 * f.my * r), tzp = (TR)czp, tzm = (TR)czm;
+  TR b;
+  if (X) {
+    const int sy = g.sy, sz = g.sz;
+    const double xc = X[c];
+    double zpv, zmv;
+    if (comp == 2) {
+      zpv = X[c + sz];
+      zmv = X[c - sz];
+    } else {
+      zpv = (k == g.nz - 1) ? xc : X[c + sz];
+      zmv = (k == 0) ? xc : X[c - sz];
+    }
+    double bd = rhs * (double)r;
+    bd = fma((double)cxp, X[c + 1], bd);
+    bd = fma((double)cxm, X[c - 1], bd);
+    bd = fma((double)cyp, X[c + sy], bd);
+    bd = fma((double)cym, X[c - sy], bd);
+    bd = fma((double)tzp, zpv, bd);
+    bd = fma((double)tzm, zmv, bd);
+    b = (TR)(bd - xc);
+  } else {
+    b = (TR)((T)rhs * r);
+  }
+  store_rec<TR>(rec, cxp, cxm, cyp, cym, tzp, tzm, b);
 }
 
 // X64 is the component's FP64 state (u2, v2 or w2): the right-hand side is
@@ -220,7 +248,7 @@ __global__ void __launch_bounds__(MB_X *MB_Y)
               const T *__restrict__ fc, const double *__restrict__ c1, const double *__restrict__ c0,
               const double *__restrict__ s1, const double *__restrict__ s0, double *__restrict__ conv2,
               double *__restrict__ csf2, double *__restrict__ rhs, double *__restrict__ diff_out,
-              TR *__restrict__ coef) {
+              TR *__restrict__ coef, int defect) {
   const int i = blockIdx.x * MB_X + threadIdx.x + 1, j = blockIdx.y * MB_Y + threadIdx.y + 1;
   const int k = blockIdx.z;
   if (i > g.nx || j > g.ny) return;
@@ -247,7 +275,8 @@ __global__ void __launch_bounds__(MB_X *MB_Y)
   csf2[c] = s2;
   if (rhs) rhs[c] = r;
   if (diff_out) diff_out[c] = diff;
-  if (coef && valid) write_coef<T, TR>(comp, g, hm, f, r, k, coef + 8 * (size_t)rec_slot(g, c, i));
+  if (coef && valid)
+    write_coef<T, TR>(comp, g, hm, f, r, k, defect ? X64 : nullptr, c, coef + 8 * (size_t)rec_slot(g, c, i));
 }
 
 template <typename T, typename TR = T>
@@ -257,8 +286,10 @@ static cudaError_t mom_rhs(int comp, const Geo &g, const Phys &ph, const T *u2, 
                            double *diff_out, TR *coef, cudaStream_t st) {
   const int nk = (comp == 2) ? g.nz + 1 : g.nz;
   dim3 grd((g.nx + MB_X - 1) / MB_X, (g.ny + MB_Y - 1) / MB_Y, nk);
+  // FP32 records feed the defect-form FP32 sweeps
+  const int defect = (sizeof(TR) == sizeof(float)) ? 1 : 0;
   k_mom_rhs<T, TR><<<grd, dim3(MB_X, MB_Y), 0, st>>>(comp, g, ph, helm_of(ph), u2, v2, w2, x64, mu, fcsf, c1,
-                                                     c0, s1, s0, conv2, csf2, rhs, diff_out, coef);
+                                                     c0, s1, s0, conv2, csf2, rhs, diff_out, coef, defect);
   return cudaGetLastError();
 }
 
@@ -415,7 +446,7 @@ __global__ void __launch_bounds__(MB_X *MB_Y)
     v = xc + 1.2 * (res - xc);
     put(g, x, i, j, k, v, fuse);
   }
-  if (bc) sor_bc(comp, g, h, x, P, i2, i, iend, v, j, k, fuse);
+  if (bc) sor_bc(comp, g, h, x, (const double *)nullptr, P, i2, i, iend, v, j, k, fuse);
 }
 
 // sor_iteration_allflux.f90:100-146 (and v, w): 2-D colouring, sequential
@@ -451,7 +482,7 @@ __global__ void __launch_bounds__(MB_X *MB_Y)
       put(g, x, i, j, k, v, fuse);
       prev = v;
     }
-    if (bc) sor_bc(comp, g, h, x, P, i2, i, iend, v, j, k, fuse);
+    if (bc) sor_bc(comp, g, h, x, (const double *)nullptr, P, i2, i, iend, v, j, k, fuse);
   }
 }
 

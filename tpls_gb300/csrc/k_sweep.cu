@@ -55,7 +55,7 @@ __device__ __forceinline__ T rec_apply(const Rec<T> &q, T xp, T xm, T yp, T ym, 
 template <typename T>
 __global__ void __launch_bounds__(SW_X *SW_Y)
     k_jacobi_c(int comp, Geo g, Helm h, const T *__restrict__ xo, const T *__restrict__ coef,
-               const double *__restrict__ P, T *__restrict__ x, int fuse) {
+               const double *__restrict__ P, const double *__restrict__ X, T *__restrict__ x, int fuse) {
   const int i = blockIdx.x * SW_X + threadIdx.x + 1, j = blockIdx.y * SW_Y + threadIdx.y + 1;
   const int k = blockIdx.z + (comp == 2 ? 1 : 0);
   const int iend = (comp == 0) ? g.nx - 1 : g.nx;
@@ -73,28 +73,31 @@ __global__ void __launch_bounds__(SW_X *SW_Y)
   }
   const T v = rec_apply(q, xo[c + 1], xo[c - 1], xo[c + sy], xo[c - sy], zp, zm);
   put(g, x, i, j, k, v, fuse);
+  const bool edge = (i == 1) || (i >= g.nx - 1) || (comp == 2 && (k == 1 || k == g.nz - 1));
+  if (!edge) return;
+  const double vx = xval(g, X, v, i, j, k);
   if (comp == 0) {
-    if (i == 1) put(g, x, 0, j, k, v, fuse);
+    if (i == 1) bput(g, x, X, 0, j, k, vx, fuse);
     if (i == g.nx - 1) {
-      put(g, x, g.nx, j, k, u_outlet(g, h, P, v, j, k), fuse);
-      put(g, x, g.nx + 1, j, k, (T)0, fuse);
+      bput(g, x, X, g.nx, j, k, u_outlet(g, h, P, vx, j, k), fuse);
+      bput(g, x, X, g.nx + 1, j, k, 0.0, fuse);
     }
   } else if (comp == 1) {
-    if (i == 1) put(g, x, 0, j, k, v, fuse);
-    if (i == g.nx) put(g, x, g.nx + 1, j, k, v, fuse);
+    if (i == 1) bput(g, x, X, 0, j, k, vx, fuse);
+    if (i == g.nx) bput(g, x, X, g.nx + 1, j, k, vx, fuse);
   } else {
     const int nz = g.nz;
-    if (k == 1) put(g, x, i, j, 0, (T)0, fuse);
-    if (k == nz - 1) put(g, x, i, j, nz, (T)0, fuse);
+    if (k == 1) bput(g, x, X, i, j, 0, 0.0, fuse);
+    if (k == nz - 1) bput(g, x, X, i, j, nz, 0.0, fuse);
     if (i == 1) {
-      put(g, x, 0, j, k, v, fuse);
-      if (k == 1) put(g, x, 0, j, 0, (T)0, fuse);
-      if (k == nz - 1) put(g, x, 0, j, nz, (T)0, fuse);
+      bput(g, x, X, 0, j, k, vx, fuse);
+      if (k == 1) bput(g, x, X, 0, j, 0, 0.0, fuse);
+      if (k == nz - 1) bput(g, x, X, 0, j, nz, 0.0, fuse);
     }
     if (i == g.nx) {
-      put(g, x, g.nx + 1, j, k, v, fuse);
-      if (k == 1) put(g, x, g.nx + 1, j, 0, (T)0, fuse);
-      if (k == nz - 1) put(g, x, g.nx + 1, j, nz, (T)0, fuse);
+      bput(g, x, X, g.nx + 1, j, k, vx, fuse);
+      if (k == 1) bput(g, x, X, g.nx + 1, j, 0, 0.0, fuse);
+      if (k == nz - 1) bput(g, x, X, g.nx + 1, j, nz, 0.0, fuse);
     }
   }
 }
@@ -104,7 +107,7 @@ __global__ void __launch_bounds__(SW_X *SW_Y)
 template <typename T>
 __global__ void __launch_bounds__(SW_X *SW_Y)
     k_sor_even_c(int comp, Geo g, Helm h, T *__restrict__ x, const T *__restrict__ coef,
-                 const double *__restrict__ P, int flg, int bc, int fuse) {
+                 const double *__restrict__ P, const double *__restrict__ X, int flg, int bc, int fuse) {
   const int i2 = blockIdx.x * SW_X + threadIdx.x, j = blockIdx.y * SW_Y + threadIdx.y + 1;
   const int k = blockIdx.z + (comp == 2 ? 1 : 0);
   const int iend = (comp == 0) ? g.nx - 1 : g.nx;
@@ -127,7 +130,7 @@ __global__ void __launch_bounds__(SW_X *SW_Y)
     v = xc + (T)1.2 * (res - xc);
     put(g, x, i, j, k, v, fuse);
   }
-  if (bc) sor_bc(comp, g, h, x, P, i2, i, iend, v, j, k, fuse);
+  if (bc) sor_bc(comp, g, h, x, X, P, i2, i, iend, v, j, k, fuse);
 }
 
 // Odd-iteration half-sweep (2-D colouring, sequential in k).  Within such a
@@ -181,7 +184,7 @@ __device__ __forceinline__ void sor_odd_produce(int comp, const Geo &g, const T 
 template <typename T>
 __global__ void __launch_bounds__(SO_T)
     k_sor_odd_c2(int comp, Geo g, Helm h, T *__restrict__ x, const T *__restrict__ coef,
-                 const double *__restrict__ P, int flg, int bc, int fuse) {
+                 const double *__restrict__ P, const double *__restrict__ X, int flg, int bc, int fuse) {
   __shared__ T sA[2][SO_KZ][32], sB[2][SO_KZ][32];
   const int j = blockIdx.y + 1;
   const int iend = (comp == 0) ? g.nx - 1 : g.nx;
@@ -208,7 +211,7 @@ __global__ void __launch_bounds__(SO_T)
             put(g, x, i, j, k, v, fuse);
             prev = v;
           }
-          if (bc) sor_bc(comp, g, h, x, P, i2, i, iend, v, j, k, fuse);
+          if (bc) sor_bc(comp, g, h, x, X, P, i2, i, iend, v, j, k, fuse);
         }
       }
     } else if (ch + 1 < nch) {
@@ -236,7 +239,7 @@ __global__ void __launch_bounds__(SO_T)
 template <typename T, int SO3_W>
 __global__ void __launch_bounds__(SO3_W * 32)
     k_sor_odd_c3(int comp, Geo g, Helm h, T *__restrict__ x, const T *__restrict__ coef,
-                 const double *__restrict__ P, int flg, int bc, int fuse) {
+                 const double *__restrict__ P, const double *__restrict__ X, int flg, int bc, int fuse) {
   extern __shared__ __align__(16) unsigned char so3_raw[];
   const int j = blockIdx.y + 1;
   const int iend = (comp == 0) ? g.nx - 1 : g.nx;
@@ -296,7 +299,7 @@ __global__ void __launch_bounds__(SO3_W * 32)
         v = fma(sp[(k - k0) * 32 + lane], xin, sy[(k - k0) * 32 + lane]);
         put(g, x, i, j, k, v, fuse);
       }
-      if (bc) sor_bc(comp, g, h, x, P, i2, i, iend, v, j, k, fuse);
+      if (bc) sor_bc(comp, g, h, x, X, P, i2, i, iend, v, j, k, fuse);
     }
   }
 }
@@ -322,53 +325,75 @@ cudaError_t sweep_init() {
 
 template <typename T>
 static cudaError_t jacobi_c(int comp, const Geo &g, const Phys &ph, const T *xo, const T *coef,
-                            const double *pres, T *x, int fuse, cudaStream_t st) {
+                            const double *pres, const double *X, T *x, int fuse, cudaStream_t st) {
   const int nk = (comp == 2) ? g.nz - 1 : g.nz;
   const int iend = (comp == 0) ? g.nx - 1 : g.nx;
   dim3 grd((iend + SW_X - 1) / SW_X, (g.ny + SW_Y - 1) / SW_Y, nk);
-  k_jacobi_c<T><<<grd, dim3(SW_X, SW_Y), 0, st>>>(comp, g, helm_of(ph), xo, coef, pres, x, fuse);
+  k_jacobi_c<T><<<grd, dim3(SW_X, SW_Y), 0, st>>>(comp, g, helm_of(ph), xo, coef, pres, X, x, fuse);
   return cudaGetLastError();
 }
 
 template <typename T>
 static cudaError_t sor_c(int comp, const Geo &g, const Phys &ph, T *x, const T *coef, const double *pres,
-                         int flg, int iteration_time, int bc, int fuse, cudaStream_t st) {
+                         const double *X, int flg, int iteration_time, int bc, int fuse, cudaStream_t st) {
   const int iend = (comp == 0) ? g.nx - 1 : g.nx;
   const int npairs = (iend + 1) / 2;
+  const Helm h = helm_of(ph);
   if (iteration_time % 2 == 0) {
     const int nk = (comp == 2) ? g.nz - 1 : g.nz;
     dim3 grd((npairs + SW_X - 1) / SW_X, (g.ny + SW_Y - 1) / SW_Y, nk);
-    k_sor_even_c<T><<<grd, dim3(SW_X, SW_Y), 0, st>>>(comp, g, helm_of(ph), x, coef, pres, flg, bc, fuse);
+    k_sor_even_c<T><<<grd, dim3(SW_X, SW_Y), 0, st>>>(comp, g, h, x, coef, pres, X, flg, bc, fuse);
   } else {
     dim3 grd((npairs + 31) / 32, g.ny, 1);
     // 16 chunks once columns are long enough to give each warp >= 8 levels
     const int w = (g.nz >= 128) ? 16 : 8;
     const size_t sm = so3_smem<T>(g, comp, w);
     if (sm <= SO3_SMEM_MAX && w == 16)
-      k_sor_odd_c3<T, 16><<<grd, 16 * 32, sm, st>>>(comp, g, helm_of(ph), x, coef, pres, flg, bc, fuse);
+      k_sor_odd_c3<T, 16><<<grd, 16 * 32, sm, st>>>(comp, g, h, x, coef, pres, X, flg, bc, fuse);
     else if (sm <= SO3_SMEM_MAX)
-      k_sor_odd_c3<T, 8><<<grd, 8 * 32, sm, st>>>(comp, g, helm_of(ph), x, coef, pres, flg, bc, fuse);
+      k_sor_odd_c3<T, 8><<<grd, 8 * 32, sm, st>>>(comp, g, h, x, coef, pres, X, flg, bc, fuse);
     else
-      k_sor_odd_c2<T><<<grd, SO_T, 0, st>>>(comp, g, helm_of(ph), x, coef, pres, flg, bc, fuse);
+      k_sor_odd_c2<T><<<grd, SO_T, 0, st>>>(comp, g, h, x, coef, pres, X, flg, bc, fuse);
   }
   return cudaGetLastError();
 }
 
 cudaError_t launch_jacobi_c(int comp, const Geo &g, const Phys &ph, const double *xo, const double *coef,
                             const double *pres, double *x, int fuse, cudaStream_t st) {
-  return jacobi_c(comp, g, ph, xo, coef, pres, x, fuse, st);
+  return jacobi_c(comp, g, ph, xo, coef, pres, nullptr, x, fuse, st);
 }
 cudaError_t launch_jacobi_c(int comp, const Geo &g, const Phys &ph, const float *xo, const float *coef,
-                            const double *pres, float *x, int fuse, cudaStream_t st) {
-  return jacobi_c(comp, g, ph, xo, coef, pres, x, fuse, st);
+                            const double *pres, const double *X, float *x, int fuse, cudaStream_t st) {
+  return jacobi_c(comp, g, ph, xo, coef, pres, X, x, fuse, st);
 }
 cudaError_t launch_sor_c(int comp, const Geo &g, const Phys &ph, double *x, const double *coef,
                          const double *pres, int flg, int iteration_time, int bc, int fuse, cudaStream_t st) {
-  return sor_c(comp, g, ph, x, coef, pres, flg, iteration_time, bc, fuse, st);
+  return sor_c(comp, g, ph, x, coef, pres, nullptr, flg, iteration_time, bc, fuse, st);
 }
 cudaError_t launch_sor_c(int comp, const Geo &g, const Phys &ph, float *x, const float *coef,
-                         const double *pres, int flg, int iteration_time, int bc, int fuse, cudaStream_t st) {
-  return sor_c(comp, g, ph, x, coef, pres, flg, iteration_time, bc, fuse, st);
+                         const double *pres, const double *X, int flg, int iteration_time, int bc, int fuse,
+                         cudaStream_t st) {
+  return sor_c(comp, g, ph, x, coef, pres, X, flg, iteration_time, bc, fuse, st);
+}
+
+// defect form: d = -X before the first sweep (the sweeps start from x = 0),
+// x = X + d after the last
+__global__ void k_defect_init(const double *__restrict__ X, float *__restrict__ d, size_t n) {
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
+    d[q] = (float)(-X[q]);
+}
+__global__ void k_defect_apply(const double *__restrict__ X, const float *__restrict__ d, double *__restrict__ x,
+                               size_t n) {
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
+    x[q] = X[q] + (double)d[q];
+}
+cudaError_t launch_defect_init(const double *X, float *d, size_t n, cudaStream_t st) {
+  k_defect_init<<<1216, 256, 0, st>>>(X, d, n);
+  return cudaGetLastError();
+}
+cudaError_t launch_defect_apply(const double *X, const float *d, double *x, size_t n, cudaStream_t st) {
+  k_defect_apply<<<1216, 256, 0, st>>>(X, d, x, n);
+  return cudaGetLastError();
 }
 
 }  // namespace tpls

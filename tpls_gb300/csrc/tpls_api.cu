@@ -45,7 +45,6 @@ struct tpls_ctx {
   float *phi32, *u32, *v32, *w32, *mu32, *D32, *fx32, *fy32, *fz32, *prA32, *prB32;
   float *coef32[3];
   float *x3f[3][2];
-  double *x3d = nullptr;  // FP64 view of u3/v3/w3 for tpls_get_field / tpls_set_field
   double *hbuf = nullptr; // interface height (nx*ny)
   size_t n_p, n_uv, n_w;  // elements of each allocation (incl. pitch and padding)
   double *part, *scal, *scal_host;
@@ -140,8 +139,6 @@ static int field_kind(int f) {
   }
 }
 
-// the momentum iterates are FP32 (the FP32-mixed form without FP64 momentum)
-static bool x3_fp32(const tpls_ctx *c) { return c->mixed && !(c->prm.fp64_parts & TPLS_PART_MOMENTUM); }
 
 static double *field_ptr(tpls_ctx *c, int f) {
   const int s0 = c->phase % 3, s1 = (c->phase + 1) % 3, s2 = (c->phase + 2) % 3;
@@ -171,9 +168,9 @@ static double *field_ptr(tpls_ctx *c, int f) {
     case TPLS_F_CONV2_PHI: return c->conv_phi[s1];
     case TPLS_F_PHI3: return c->phi2;
     case TPLS_F_RHS_P: return c->rhs_p;
-    case TPLS_F_U3: return x3_fp32(c) ? c->x3d : c->x3[0][c->x3_final[0]];
-    case TPLS_F_V3: return x3_fp32(c) ? c->x3d : c->x3[1][c->x3_final[1]];
-    case TPLS_F_W3: return x3_fp32(c) ? c->x3d : c->x3[2][c->x3_final[2]];
+    case TPLS_F_U3: return c->x3[0][c->x3_final[0]];
+    case TPLS_F_V3: return c->x3[1][c->x3_final[1]];
+    case TPLS_F_W3: return c->x3[2][c->x3_final[2]];
     default: return nullptr;
   }
   (void)s2;
@@ -347,10 +344,13 @@ static int create_impl(int nx, int ny, int nz, const tpls_params *prm, const dou
       for (double **p : pf2) TCK(alloc_p(c, p));
       TCK(alloc_field(c, 1, ny + 4, nz + 2, &c->mu));
     }
+    // FP64 u3, v3, w3 (the defect-form result, or the FP64 momentum iterates)
+    TCK(alloc_field(c, 0, ny + 2, nz, &c->x3[0][0]));
+    TCK(alloc_field(c, 0, ny + 2, nz, &c->x3[1][0]));
+    TCK(alloc_field(c, 0, ny + 2, nz + 1, &c->x3[2][0]));
     if (parts & TPLS_PART_MOMENTUM) {
-      double **px3[] = {&c->x3[0][0], &c->x3[0][1], &c->x3[1][0], &c->x3[1][1]};
+      double **px3[] = {&c->x3[0][1], &c->x3[1][1]};
       for (double **p : px3) TCK(alloc_field(c, 0, ny + 2, nz, p));
-      TCK(alloc_field(c, 0, ny + 2, nz + 1, &c->x3[2][0]));
       TCK(alloc_field(c, 0, ny + 2, nz + 1, &c->x3[2][1]));
       for (int q = 0; q < 3; q++) {
         void *b = nullptr;
@@ -376,7 +376,6 @@ static int create_impl(int nx, int ny, int nz, const tpls_params *prm, const dou
       c->coef32[q] = (float *)b;
     }
     TCK(alloc_field(c, 1, ny + 4, nz + 2, &c->mu32));
-    TCK(alloc_field(c, 0, ny + 2, nz + 1, &c->x3d));
   }
   {
     void *b = nullptr;
@@ -441,7 +440,7 @@ long long tpls_footprint_bytes(int nx, int ny, int nz, int precision) {
   } else {
     t += 7 * round_alloc(F * np) + 6 * round_alloc(F * nuv) + 3 * round_alloc(F * nw);
     t += 2 * round_alloc(F * nrec * nz) + round_alloc(F * nrec * (nz + 1)) + round_alloc(F * nmu);
-    t += round_alloc(D * nw);
+    t += 2 * round_alloc(D * nuv) + round_alloc(D * nw);  // FP64 u3, v3, w3
   }
   t += round_alloc(px * (ny + 2) * (nz + 2) + 64) + round_alloc(D * nz) + round_alloc(D * nx * ny);
   Geo g;
@@ -488,24 +487,12 @@ int tpls_gpu_create(int nx, int ny, int nz, const tpls_params *prm, const double
   return TPLS_OK;
 }
 
-// FP32 iterate behind U3/V3/W3 in the FP32-mixed form, and its element count
-static float *mixed_x3(tpls_ctx *c, int f, size_t *n) {
-  const int q = (f == TPLS_F_U3) ? 0 : ((f == TPLS_F_V3) ? 1 : 2);
-  *n = (q == 2) ? c->n_w : c->n_uv;
-  return c->x3f[q][c->x3_final[q]];
-}
-static bool is_x3(int f) { return f == TPLS_F_U3 || f == TPLS_F_V3 || f == TPLS_F_W3; }
 
 int tpls_set_field(tpls_ctx *c, int f, const double *host) {
   if (!c || !host || f < 0 || f >= TPLS_F_COUNT) return TPLS_ERR_ARG;
   double *d = field_ptr(c, f);
   if (!d) return TPLS_ERR_ARG;
   TCK(h2d(c, d, host, nz_planes(field_kind(f), c->nz)));
-  if (x3_fp32(c) && is_x3(f)) {
-    size_t n;
-    float *x = mixed_x3(c, f, &n);
-    TCK(launch_to_float(d - XOFF, x - XOFF, n, c->st));
-  }
   TCK(cudaStreamSynchronize(c->st));
   c->need_exchange = true;
   return TPLS_OK;
@@ -515,11 +502,6 @@ int tpls_get_field(tpls_ctx *c, int f, double *host) {
   if (!c || !host || f < 0 || f >= TPLS_F_COUNT) return TPLS_ERR_ARG;
   double *d = field_ptr(c, f);
   if (!d) return TPLS_ERR_ARG;
-  if (x3_fp32(c) && is_x3(f)) {
-    size_t n;
-    const float *x = mixed_x3(c, f, &n);
-    TCK(launch_to_double(x - XOFF, d - XOFF, n, c->st));
-  }
   TCK(d2h(c, host, d, nz_planes(field_kind(f), c->nz)));
   TCK(cudaStreamSynchronize(c->st));
   return TPLS_OK;
@@ -539,33 +521,54 @@ long tpls_kernel_launches(tpls_ctx *c) {
 
 extern "C++" {
 // One velocity component's Crank-Nicolson solve (main_ns_hybrid.F90:756-887)
-// on the iterate pair X (FP64, or FP32 in the FP32-mixed form).
+// on the iterate pair X: FP64, or in the FP32-mixed form the FP32 defect
+// d = x - base (base = the component's FP64 state), iterated from d = -base
+// (x = 0, the reference's start) and added back into out64 at the end.
 template <typename T>
-static int momentum(tpls_ctx *c, int comp, const T *coef, T **X, int max_iteration) {
+static int momentum(tpls_ctx *c, int comp, const T *coef, T **X, int max_iteration, const double *base = nullptr,
+                    double *out64 = nullptr) {
   const Geo &g = c->g;
   const int nzp = nz_planes(comp == 2 ? 2 : 1, c->nz);
   const int fuse = (g.ny % 2 == 0);
-  TCK(cudaMemsetAsync(X[0] - XOFF, 0, sizeof(T) * ((size_t)c->px * (c->ny + 2) * nzp + 8), c->st));
+  const size_t n = (size_t)c->px * (c->ny + 2) * nzp + 8;
+  if constexpr (sizeof(T) == sizeof(float)) {
+    LCK(c, launch_defect_init(base - XOFF, X[0] - XOFF, n, c->st));
+  } else {
+    TCK(cudaMemsetAsync(X[0] - XOFF, 0, sizeof(T) * n, c->st));
+  }
+  auto jac = [&](const T *src, T *dst) {
+    if constexpr (sizeof(T) == sizeof(float)) return launch_jacobi_c(comp, g, c->ph, src, coef, c->pres, base, dst,
+                                                                      fuse, c->st);
+    else return launch_jacobi_c(comp, g, c->ph, src, coef, c->pres, dst, fuse, c->st);
+  };
+  auto sor = [&](T *x, int flg, int it, int bc) {
+    if constexpr (sizeof(T) == sizeof(float)) return launch_sor_c(comp, g, c->ph, x, coef, c->pres, base, flg, it,
+                                                                   bc, fuse, c->st);
+    else return launch_sor_c(comp, g, c->ph, x, coef, c->pres, flg, it, bc, fuse, c->st);
+  };
   const int N = max_iteration / 2;
   for (int it = 1; it <= N; it++) {
     T *src = X[(it - 1) % 2], *dst = X[it % 2];
     {
       PhaseScope ps(c, TPLS_T_JACOBI);
-      LCK(c, launch_jacobi_c(comp, g, c->ph, src, coef, c->pres, dst, fuse, c->st));
+      LCK(c, jac(src, dst));
     }
     if (!fuse) LCK(c, launch_exchange(g, dst, nzp, c->st));
     {
       PhaseScope ps(c, (it % 2) ? TPLS_T_SOR_ODD : TPLS_T_SOR);
-      LCK(c, launch_sor_c(comp, g, c->ph, dst, coef, c->pres, 0, it, 0, fuse, c->st));
+      LCK(c, sor(dst, 0, it, 0));
     }
     if (!fuse) LCK(c, launch_exchange(g, dst, nzp, c->st));
     {
       PhaseScope ps(c, (it % 2) ? TPLS_T_SOR_ODD : TPLS_T_SOR);
-      LCK(c, launch_sor_c(comp, g, c->ph, dst, coef, c->pres, 1, it, 1, fuse, c->st));
+      LCK(c, sor(dst, 1, it, 1));
     }
     if (!fuse) LCK(c, launch_exchange(g, dst, nzp, c->st));
   }
   c->x3_final[comp] = N % 2;
+  if constexpr (sizeof(T) == sizeof(float)) {
+    LCK(c, launch_defect_apply(base - XOFF, X[N % 2] - XOFF, out64 - XOFF, n, c->st));
+  }
   const int nb = diff2_blocks(g, nzp);
   if (N >= 1) {
     LCK(c, launch_diff2(g, X[N % 2], X[(N - 1) % 2], nzp, c->part, c->st));
@@ -707,6 +710,17 @@ static int step_once(tpls_ctx *c) {
 // the AB3 updates, the momentum right-hand sides, the CG recurrences and the
 // projection stay FP64; every FP32 array is a rounded copy or an
 // intermediate of one step.
+// the three FP32 defect-form momentum solves of the FP32-mixed step, the
+// FP64 results in x3[q][0]
+static int sweeps32(tpls_ctx *c) {
+  int s;
+  if ((s = momentum<float>(c, 0, c->coef32[0], c->x3f[0], c->prm.mom_u, c->u2, c->x3[0][0]))) return s;
+  if ((s = momentum<float>(c, 1, c->coef32[1], c->x3f[1], c->prm.mom_v, c->v2, c->x3[1][0]))) return s;
+  if ((s = momentum<float>(c, 2, c->coef32[2], c->x3f[2], c->prm.mom_w, c->w2, c->x3[2][0]))) return s;
+  for (int q = 0; q < 3; q++) c->x3_final[q] = 0;
+  return TPLS_OK;
+}
+
 static int step_once_mixed(tpls_ctx *c) {
   const Geo &g = c->g;
   const Phys &ph = c->ph;
@@ -800,12 +814,10 @@ static int step_once_mixed(tpls_ctx *c) {
       LCK(c, launch_mom_rhs64r32(2, g, ph, c->u2, c->v2, c->w2, c->mu, c->fz, c->conv_w[s1], c->conv_w[s0],
                                  c->csf_w[s1], c->csf_w[s0], c->conv_w[s2], c->csf_w[s2], c->coef32[2], st));
     }
-    if ((s = momentum<float>(c, 0, c->coef32[0], c->x3f[0], c->prm.mom_u))) return s;
-    if ((s = momentum<float>(c, 1, c->coef32[1], c->x3f[1], c->prm.mom_v))) return s;
-    if ((s = momentum<float>(c, 2, c->coef32[2], c->x3f[2], c->prm.mom_w))) return s;
-    u3v = c->x3f[0][c->x3_final[0]];
-    v3v = c->x3f[1][c->x3_final[1]];
-    w3v = c->x3f[2][c->x3_final[2]];
+    if ((s = sweeps32(c))) return s;
+    u3v = c->x3[0][0];
+    v3v = c->x3[1][0];
+    w3v = c->x3[2][0];
   } else {
     {
       PhaseScope ps(c, TPLS_T_CSF);
@@ -823,31 +835,22 @@ static int step_once_mixed(tpls_ctx *c) {
                               c->conv_w[s0], c->csf_w[s1], c->csf_w[s0], c->conv_w[s2], c->csf_w[s2],
                               c->coef32[2], st));
     }
-    if ((s = momentum<float>(c, 0, c->coef32[0], c->x3f[0], c->prm.mom_u))) return s;
-    if ((s = momentum<float>(c, 1, c->coef32[1], c->x3f[1], c->prm.mom_v))) return s;
-    if ((s = momentum<float>(c, 2, c->coef32[2], c->x3f[2], c->prm.mom_w))) return s;
-    u3v = c->x3f[0][c->x3_final[0]];
-    v3v = c->x3f[1][c->x3_final[1]];
-    w3v = c->x3f[2][c->x3_final[2]];
+    if ((s = sweeps32(c))) return s;
+    u3v = c->x3[0][0];
+    v3v = c->x3[1][0];
+    w3v = c->x3[2][0];
   }
   int its = 0, reason = 0;
   double rn = 0.0, bn = 0.0;
   {
     PhaseScope ps(c, TPLS_T_PRESSURE);
-    if (mom64)
-      LCK(c, launch_source(g, ph, (const double *)u3v, (const double *)v3v, (const double *)w3v, c->rhs_p, st));
-    else
-      LCK(c, launch_source(g, ph, (const float *)u3v, (const float *)v3v, (const float *)w3v, c->rhs_p, st));
-    if ((s = pressure_stage(c, u3v, mom64 ? 0 : 1, &its, &rn, &bn, &reason))) return s;
+    LCK(c, launch_source(g, ph, (const double *)u3v, (const double *)v3v, (const double *)w3v, c->rhs_p, st));
+    if ((s = pressure_stage(c, u3v, 0, &its, &rn, &bn, &reason))) return s;
   }
   {
     PhaseScope ps(c, TPLS_T_PROJECT);
-    if (mom64)
-      LCK(c, launch_project(g, ph, (const double *)u3v, (const double *)v3v, (const double *)w3v, c->pres,
-                            c->u_inlet, c->u2, c->v2, c->w2, st));
-    else
-      LCK(c, launch_project(g, ph, (const float *)u3v, (const float *)v3v, (const float *)w3v, c->pres,
-                            c->u_inlet, c->u2, c->v2, c->w2, st));
+    LCK(c, launch_project(g, ph, (const double *)u3v, (const double *)v3v, (const double *)w3v, c->pres,
+                          c->u_inlet, c->u2, c->v2, c->w2, st));
     TCK(cudaMemcpyAsync(c->pres_old - XOFF, c->pres - XOFF, sizeof(double) * c->n_p, cudaMemcpyDeviceToDevice,
                         st));
   }

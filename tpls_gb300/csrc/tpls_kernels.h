@@ -122,14 +122,20 @@ cudaError_t launch_sor_c(int comp, const Geo &g, const Phys &ph, double *x,
                          const double *coef, const double *pres, int flg,
                          int iteration_time, int bc, int fuse_ghosts,
                          cudaStream_t st);
+// FP32 sweeps in defect form: x holds d = x - X for the FP64 base X (the
+// component's state), the records carry the correspondingly shifted b.
 cudaError_t launch_jacobi_c(int comp, const Geo &g, const Phys &ph,
                             const float *xo, const float *coef,
-                            const double *pres, float *x, int fuse_ghosts,
-                            cudaStream_t st);
+                            const double *pres, const double *X, float *x,
+                            int fuse_ghosts, cudaStream_t st);
 cudaError_t launch_sor_c(int comp, const Geo &g, const Phys &ph, float *x,
-                         const float *coef, const double *pres, int flg,
-                         int iteration_time, int bc, int fuse_ghosts,
-                         cudaStream_t st);
+                         const float *coef, const double *pres,
+                         const double *X, int flg, int iteration_time, int bc,
+                         int fuse_ghosts, cudaStream_t st);
+// d = -X (n elements) / x = X + d
+cudaError_t launch_defect_init(const double *X, float *d, size_t n, cudaStream_t st);
+cudaError_t launch_defect_apply(const double *X, const float *d, double *x, size_t n,
+                                cudaStream_t st);
 // One-time kernel attributes of the sweeps (dynamic shared memory).
 cudaError_t sweep_init();
 cudaError_t launch_bc(int comp, const Geo &g, const Phys &ph, double *x,

@@ -31,15 +31,29 @@ __device__ __forceinline__ void put(const Geo &g, T *x, int i, int j, int k, T v
   }
 }
 
-// u outlet, main_ns_hybrid.F90:768-776 (the pressure row index is the u row
-// index j, as written in the reference); evaluated in FP64.
+// Defect form.  The FP32-mixed sweeps iterate on d = x - X, X the FP64
+// velocity state of the step (u2, v2 or w2), so that FP32 rounding acts on
+// the small correction instead of on the velocity; the FP64 form passes
+// X = null and iterates on x itself.  Interior updates are the same affine
+// map in both (the records' b is shifted accordingly); boundary rows are
+// evaluated in x space in FP64 and stored back as x - X.
 template <typename T>
-__device__ __forceinline__ T u_outlet(const Geo &g, const Helm &h, const double *P, T unm1, int j,
-                                      int k) {
+__device__ __forceinline__ double xval(const Geo &g, const double *X, T d, int i, int j, int k) {
+  return X ? (double)d + X[TPLS_IDX(g, i, j, k)] : (double)d;
+}
+template <typename T>
+__device__ __forceinline__ void bput(const Geo &g, T *x, const double *X, int i, int j, int k, double v,
+                                     int fuse) {
+  put(g, x, i, j, k, (T)(X ? v - X[TPLS_IDX(g, i, j, k)] : v), fuse);
+}
+
+// u outlet, main_ns_hybrid.F90:768-776 (the pressure row index is the u row
+// index j, as written in the reference); x space, FP64.
+__device__ __forceinline__ double u_outlet(const Geo &g, const Helm &h, const double *P, double unm1, int j,
+                                           int k) {
   const int nx = g.nx;
-  return (T)((double)unm1 + h.dtdx * (P[TPLS_IDX(g, nx + 1, j, k + 1)] +
-                                      P[TPLS_IDX(g, nx - 1, j, k + 1)] -
-                                      2.0 * P[TPLS_IDX(g, nx, j, k + 1)]));
+  return unm1 + h.dtdx * (P[TPLS_IDX(g, nx + 1, j, k + 1)] + P[TPLS_IDX(g, nx - 1, j, k + 1)] -
+                          2.0 * P[TPLS_IDX(g, nx, j, k + 1)]);
 }
 
 // Post-sweep boundary rows (main_ns_hybrid.F90:784-799 u, :826-836 v,
@@ -48,19 +62,20 @@ __device__ __forceinline__ T u_outlet(const Geo &g, const Helm &h, const double 
 // fictitious point x(nx+1) = 0, for v and w the outlet copy.  A value of the
 // colour not relaxed in this half-sweep is read (it is final already).
 template <typename T>
-__device__ __forceinline__ void sor_bc(int comp, const Geo &g, const Helm &h, T *x, const double *P,
-                                       int i2, int i, int iend, T v, int j, int k, int fuse) {
+__device__ __forceinline__ void sor_bc(int comp, const Geo &g, const Helm &h, T *x, const double *X,
+                                       const double *P, int i2, int i, int iend, T v, int j, int k, int fuse) {
   if (i2 == 0) {
     const T v1 = (i == 1) ? v : x[TPLS_IDX(g, 1, j, k)];
-    put(g, x, 0, j, k, v1, fuse);
+    bput(g, x, X, 0, j, k, xval(g, X, v1, 1, j, k), fuse);
   }
   if (i2 == (iend - 1) / 2) {
     const T ve = (i == iend) ? v : x[TPLS_IDX(g, iend, j, k)];
+    const double vex = xval(g, X, ve, iend, j, k);
     if (comp == 0) {
-      put(g, x, g.nx, j, k, u_outlet(g, h, P, ve, j, k), fuse);
-      put(g, x, g.nx + 1, j, k, (T)0, fuse);
+      bput(g, x, X, g.nx, j, k, u_outlet(g, h, P, vex, j, k), fuse);
+      bput(g, x, X, g.nx + 1, j, k, 0.0, fuse);
     } else {
-      put(g, x, g.nx + 1, j, k, ve, fuse);
+      bput(g, x, X, g.nx + 1, j, k, vex, fuse);
     }
   }
 }
