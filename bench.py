@@ -96,6 +96,23 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(rows)}
 
 
+def max_over_ranks(values, dist=None, device="cpu"):
+    """Element-wise maximum of `values` over all ranks (one all-reduce): the
+    slowest replica's timings, which set the job's throughput."""
+    if dist is None:
+        return [float(v) for v in values]
+    import torch
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.tolist()]
+
+
+def replica_throughput(ws: int, units_per_rank: float, ms: float) -> float:
+    """Whole-job rate of ws independent replicas that each processed
+    units_per_rank units, over the slowest replica's time (ms)."""
+    return ws * units_per_rank / (ms / 1e3)
+
+
 def _dist():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -181,11 +198,8 @@ def run_gpu(args, ws, rank, local) -> dict | None:
         raise SystemExit("tpls_step failed in the phase-timing pass")
     phases = g.timing_read(reset=True)
     g.timing_enable(False)
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = ws * cells * args.steps / (ms / 1e3)
+    ms = max_over_ranks([ms], dist, "cuda")[0]
+    value = replica_throughput(ws, cells * args.steps, ms)
 
     # e2e: the per-step host-buffer path through the C ABI (pinned host state
     # uploaded, one step, state downloaded), CUDA events on the same stream
@@ -212,11 +226,8 @@ def run_gpu(args, ws, rank, local) -> dict | None:
     e1.record(ext)
     torch.cuda.synchronize()
     ems = e0.elapsed_time(e1)
-    if dist:
-        t = torch.tensor([ems], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ems = float(t.item())
-    e2e = ws * cells * ke / (ems / 1e3)
+    ems = max_over_ranks([ems], dist, "cuda")[0]
+    e2e = replica_throughput(ws, cells * ke, ems)
 
     if rank != 0:
         if dist:
@@ -308,7 +319,7 @@ def run_batch(args, ws, rank, local) -> dict | None:
     hosts = []
     members = []
     for inst in insts:
-        g = open_instance(inst, precision)
+        g = open_instance(inst, precision, tune=True)  # sweep tile shapes per grid (cached per shape)
         hosts.append(g.get_state())
         members.append(g)
     b = Batch(members)
@@ -347,15 +358,12 @@ def run_batch(args, ws, rank, local) -> dict | None:
     solo = None
     if not args.no_one_by_one:
         solo = run_one_by_one(insts, args.steps, precision, warmup=args.warmup)
-    if dist:
-        t = torch.tensor([sec, e2e_sec], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        sec, e2e_sec = float(t[0]), float(t[1])
+    sec, e2e_sec = max_over_ranks([sec, e2e_sec], dist, "cuda")
     if rank != 0:
         if dist:
             dist.destroy_process_group()
         return None
-    value = ws * cells * args.steps / sec
+    value = replica_throughput(ws, cells * args.steps, sec * 1e3)
     out = {
         "metric": "cell-steps/s",
         "value": value,

@@ -129,6 +129,17 @@ int tpls_step(tpls_ctx *ctx, int nsteps);
  * the solves' outcome is read by tpls_get_stats (p_worst) or tpls_step.
  * With graphs disabled or timing enabled it runs tpls_step. */
 int tpls_step_async(tpls_ctx *ctx, int nsteps);
+/* ---- sweep tile autotuner (no counterpart in the reference) ------------
+ * Times each candidate block shape of the Jacobi and even half-sweep
+ * kernels (reps launches each, on the context's own arrays) and keeps the
+ * fastest; results are cached per grid and sweep precision for the process.
+ * Clobbers the last step's U3/V3/W3 intermediates; captured step graphs are
+ * rebuilt at the next step (batches included).  The state a run produces
+ * does not depend on the choice (same arithmetic per point). */
+int tpls_autotune(tpls_ctx *ctx, int reps);
+/* tiles3 = {Jacobi shape 0..3, even shape 0..3, odd chunking 0..2} */
+int tpls_get_tiles(const tpls_ctx *ctx, int *tiles3);
+
 /* ---- job-serving helpers (no counterpart in the reference) ------------ */
 /* Device bytes tpls_gpu_create allocates for this grid and precision (each
  * allocation rounded to the allocator's 2 MiB unit), or -1 for bad

@@ -59,3 +59,22 @@ def test_draw_instances_is_seeded_and_in_range():
     for x in a:
         assert x.nx in range(64, 257, 32) and x.ny in range(32, 129, 32) and x.nz in range(32, 129, 16)
         assert 1.0 <= x.m <= 20.0 and 50.0 <= x.re <= 500.0 and 0.01 <= x.amp <= 0.1
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [0, 1])
+def test_autotuned_tiles_keep_results(precision):
+    """The tuner only picks among block shapes with the same per-point
+    arithmetic: a tuned context ends bit-identical to an untuned one."""
+    inst = _instances()[0]
+    a = open_instance(inst, precision)
+    b = open_instance(inst, precision, tune=True)
+    tiles = b.autotune(reps=3)
+    assert set(tiles) == {"jacobi", "sor_even", "sor_odd"}
+    b.set_state(a.get_state())
+    assert a.step(4) == 0 and b.step(4) == 0
+    sa, sb = a.get_state(), b.get_state()
+    for k in STATE_FIELDS:
+        assert np.array_equal(sa[k], sb[k]), k
+    a.close()
+    b.close()

@@ -128,6 +128,8 @@ def load_library(path: Path | None = None) -> C.CDLL:
     lib.tpls_step.argtypes = [C.c_void_p, C.c_int]
     lib.tpls_step_async.argtypes = [C.c_void_p, C.c_int]
     lib.tpls_graphs_enable.argtypes = [C.c_void_p, C.c_int]
+    lib.tpls_autotune.argtypes = [C.c_void_p, C.c_int]
+    lib.tpls_get_tiles.argtypes = [C.c_void_p, C.POINTER(C.c_int)]
     lib.tpls_get_stats.argtypes = [C.c_void_p, C.POINTER(TplsStats)]
     lib.tpls_sync.argtypes = [C.c_void_p]
     lib.tpls_kernel_launches.argtypes = [C.c_void_p]
@@ -263,6 +265,13 @@ class TplsGpu:
         """Enqueue nsteps graph-launched steps without waiting; the solves'
         outcome is in stats()["p_worst"]."""
         self._check(self.lib.tpls_step_async(self.ctx, nsteps))
+
+    def autotune(self, reps: int = 10) -> dict:
+        """Tile shapes of the sweep kernels chosen by timing (tpls_autotune)."""
+        self._check(self.lib.tpls_autotune(self.ctx, reps))
+        t = (C.c_int * 3)()
+        self._check(self.lib.tpls_get_tiles(self.ctx, t))
+        return {"jacobi": t[0], "sor_even": t[1], "sor_odd": t[2]}
 
     def graphs_enable(self, on: bool = True) -> None:
         self._check(self.lib.tpls_graphs_enable(self.ctx, 1 if on else 0))

@@ -15,7 +15,11 @@
 
 namespace tpls {
 
-constexpr int SW_X = 32, SW_Y = 4;
+// Tile shapes of the Jacobi and even-SOR kernels (block x threads over i or
+// i pairs, block y threads over j) the autotuner chooses from; variant 0 is
+// the default.
+constexpr int SW_NV = 4;
+constexpr int SW_SHAPES[SW_NV][2] = {{32, 4}, {32, 8}, {64, 4}, {16, 8}};
 
 template <typename T>
 struct Rec {
@@ -52,7 +56,7 @@ __device__ __forceinline__ T rec_apply(const Rec<T> &q, T xp, T xm, T yp, T ym, 
 }
 
 // Jacobi: x = J(xo) on the component's interior with its boundary rows.
-template <typename T>
+template <typename T, int SW_X, int SW_Y>
 __global__ void __launch_bounds__(SW_X *SW_Y)
     k_jacobi_c(int comp, Geo g, Helm h, const T *__restrict__ xo, const T *__restrict__ coef,
                const double *__restrict__ P, const double *__restrict__ X, T *__restrict__ x, int fuse) {
@@ -104,7 +108,7 @@ __global__ void __launch_bounds__(SW_X *SW_Y)
 
 // 3-D checkerboard half-sweep (even iteration_time), one thread per point
 // of the colour.
-template <typename T>
+template <typename T, int SW_X, int SW_Y>
 __global__ void __launch_bounds__(SW_X *SW_Y)
     k_sor_even_c(int comp, Geo g, Helm h, T *__restrict__ x, const T *__restrict__ coef,
                  const double *__restrict__ P, const double *__restrict__ X, int flg, int bc, int fuse) {
@@ -323,30 +327,57 @@ cudaError_t sweep_init() {
   return e;
 }
 
-template <typename T>
-static cudaError_t jacobi_c(int comp, const Geo &g, const Phys &ph, const T *xo, const T *coef,
-                            const double *pres, const double *X, T *x, int fuse, cudaStream_t st) {
+template <typename T, int BX, int BY>
+static void jacobi_v(int comp, const Geo &g, const Helm &h, const T *xo, const T *coef, const double *pres,
+                     const double *X, T *x, int fuse, cudaStream_t st) {
   const int nk = (comp == 2) ? g.nz - 1 : g.nz;
   const int iend = (comp == 0) ? g.nx - 1 : g.nx;
-  dim3 grd((iend + SW_X - 1) / SW_X, (g.ny + SW_Y - 1) / SW_Y, nk);
-  k_jacobi_c<T><<<grd, dim3(SW_X, SW_Y), 0, st>>>(comp, g, helm_of(ph), xo, coef, pres, X, x, fuse);
+  dim3 grd((iend + BX - 1) / BX, (g.ny + BY - 1) / BY, nk);
+  k_jacobi_c<T, BX, BY><<<grd, dim3(BX, BY), 0, st>>>(comp, g, h, xo, coef, pres, X, x, fuse);
+}
+
+template <typename T>
+static cudaError_t jacobi_c(int comp, const Geo &g, const Phys &ph, const T *xo, const T *coef,
+                            const double *pres, const double *X, T *x, int fuse, int tile, cudaStream_t st) {
+  const Helm h = helm_of(ph);
+  switch (tile) {
+    case 1: jacobi_v<T, 32, 8>(comp, g, h, xo, coef, pres, X, x, fuse, st); break;
+    case 2: jacobi_v<T, 64, 4>(comp, g, h, xo, coef, pres, X, x, fuse, st); break;
+    case 3: jacobi_v<T, 16, 8>(comp, g, h, xo, coef, pres, X, x, fuse, st); break;
+    default: jacobi_v<T, 32, 4>(comp, g, h, xo, coef, pres, X, x, fuse, st); break;
+  }
   return cudaGetLastError();
+}
+
+template <typename T, int BX, int BY>
+static void even_v(int comp, const Geo &g, const Helm &h, T *x, const T *coef, const double *pres,
+                   const double *X, int flg, int bc, int fuse, cudaStream_t st) {
+  const int iend = (comp == 0) ? g.nx - 1 : g.nx;
+  const int npairs = (iend + 1) / 2;
+  const int nk = (comp == 2) ? g.nz - 1 : g.nz;
+  dim3 grd((npairs + BX - 1) / BX, (g.ny + BY - 1) / BY, nk);
+  k_sor_even_c<T, BX, BY><<<grd, dim3(BX, BY), 0, st>>>(comp, g, h, x, coef, pres, X, flg, bc, fuse);
 }
 
 template <typename T>
 static cudaError_t sor_c(int comp, const Geo &g, const Phys &ph, T *x, const T *coef, const double *pres,
-                         const double *X, int flg, int iteration_time, int bc, int fuse, cudaStream_t st) {
+                         const double *X, int flg, int iteration_time, int bc, int fuse, int tile_even,
+                         int tile_odd, cudaStream_t st) {
   const int iend = (comp == 0) ? g.nx - 1 : g.nx;
   const int npairs = (iend + 1) / 2;
   const Helm h = helm_of(ph);
   if (iteration_time % 2 == 0) {
-    const int nk = (comp == 2) ? g.nz - 1 : g.nz;
-    dim3 grd((npairs + SW_X - 1) / SW_X, (g.ny + SW_Y - 1) / SW_Y, nk);
-    k_sor_even_c<T><<<grd, dim3(SW_X, SW_Y), 0, st>>>(comp, g, h, x, coef, pres, X, flg, bc, fuse);
+    switch (tile_even) {
+      case 1: even_v<T, 32, 8>(comp, g, h, x, coef, pres, X, flg, bc, fuse, st); break;
+      case 2: even_v<T, 64, 4>(comp, g, h, x, coef, pres, X, flg, bc, fuse, st); break;
+      case 3: even_v<T, 16, 8>(comp, g, h, x, coef, pres, X, flg, bc, fuse, st); break;
+      default: even_v<T, 32, 4>(comp, g, h, x, coef, pres, X, flg, bc, fuse, st); break;
+    }
   } else {
     dim3 grd((npairs + 31) / 32, g.ny, 1);
-    // 16 chunks once columns are long enough to give each warp >= 8 levels
-    const int w = (g.nz >= 128) ? 16 : 8;
+    // chunks per column: tile_odd 1 = 8 warps, 2 = 16 warps; 0 = by column
+    // length (16 once each warp gets >= 8 levels)
+    const int w = (tile_odd == 1) ? 8 : ((tile_odd == 2) ? 16 : ((g.nz >= 128) ? 16 : 8));
     const size_t sm = so3_smem<T>(g, comp, w);
     if (sm <= SO3_SMEM_MAX && w == 16)
       k_sor_odd_c3<T, 16><<<grd, 16 * 32, sm, st>>>(comp, g, h, x, coef, pres, X, flg, bc, fuse);
@@ -359,21 +390,23 @@ static cudaError_t sor_c(int comp, const Geo &g, const Phys &ph, T *x, const T *
 }
 
 cudaError_t launch_jacobi_c(int comp, const Geo &g, const Phys &ph, const double *xo, const double *coef,
-                            const double *pres, double *x, int fuse, cudaStream_t st) {
-  return jacobi_c(comp, g, ph, xo, coef, pres, nullptr, x, fuse, st);
+                            const double *pres, double *x, int fuse, cudaStream_t st, const SweepTiles &t) {
+  return jacobi_c(comp, g, ph, xo, coef, pres, nullptr, x, fuse, t.jac, st);
 }
 cudaError_t launch_jacobi_c(int comp, const Geo &g, const Phys &ph, const float *xo, const float *coef,
-                            const double *pres, const double *X, float *x, int fuse, cudaStream_t st) {
-  return jacobi_c(comp, g, ph, xo, coef, pres, X, x, fuse, st);
+                            const double *pres, const double *X, float *x, int fuse, cudaStream_t st,
+                            const SweepTiles &t) {
+  return jacobi_c(comp, g, ph, xo, coef, pres, X, x, fuse, t.jac, st);
 }
 cudaError_t launch_sor_c(int comp, const Geo &g, const Phys &ph, double *x, const double *coef,
-                         const double *pres, int flg, int iteration_time, int bc, int fuse, cudaStream_t st) {
-  return sor_c(comp, g, ph, x, coef, pres, nullptr, flg, iteration_time, bc, fuse, st);
+                         const double *pres, int flg, int iteration_time, int bc, int fuse, cudaStream_t st,
+                         const SweepTiles &t) {
+  return sor_c(comp, g, ph, x, coef, pres, nullptr, flg, iteration_time, bc, fuse, t.even, t.odd, st);
 }
 cudaError_t launch_sor_c(int comp, const Geo &g, const Phys &ph, float *x, const float *coef,
                          const double *pres, const double *X, int flg, int iteration_time, int bc, int fuse,
-                         cudaStream_t st) {
-  return sor_c(comp, g, ph, x, coef, pres, X, flg, iteration_time, bc, fuse, st);
+                         cudaStream_t st, const SweepTiles &t) {
+  return sor_c(comp, g, ph, x, coef, pres, X, flg, iteration_time, bc, fuse, t.even, t.odd, st);
 }
 
 // defect form: d = -X before the first sweep (the sweeps start from x = 0),

@@ -5,6 +5,9 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <array>
+#include <map>
+#include <mutex>
 #include <vector>
 
 #include "tpls_pressure.h"
@@ -46,6 +49,7 @@ struct tpls_ctx {
   float *coef32[3];
   float *x3f[3][2];
   double *hbuf = nullptr; // interface height (nx*ny)
+  double *stage = nullptr; // host-layout staging of one field ((nx+2)(ny+2)(nz+2))
   size_t n_p, n_uv, n_w;  // elements of each allocation (incl. pitch and padding)
   double *part, *scal, *scal_host;
   size_t part_len;
@@ -62,6 +66,8 @@ struct tpls_ctx {
   long g_static[3] = {0, 0, 0};  // kernels per launch outside the CG loop body
   long g_body = 0;               // kernels per CG iteration
   double its_accounted = 0.0;    // pressure iterations already counted in `launches`
+  SweepTiles tiles;              // sweep tile shapes (tpls_autotune)
+  int tune_version = 0;
   // phase timing (tpls_timing_*)
   bool timing = false;
   int cur_slot = TPLS_T_OTHER;
@@ -176,15 +182,33 @@ static double *field_ptr(tpls_ctx *c, int f) {
   (void)s2;
 }
 
+// Host fields (Fortran order, rows of nx+2) move through a contiguous
+// device staging buffer: one bulk copy at full link bandwidth, and a
+// repack kernel between the host row layout and the pitched device rows
+// (many short pitched rows copy at a fraction of the link's bandwidth).
+__global__ void k_repack(const double *__restrict__ src, int spitch, double *__restrict__ dst, int dpitch, int w,
+                         int rows) {
+  for (int r = blockIdx.y; r < rows; r += gridDim.y)
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < w; i += gridDim.x * blockDim.x)
+      dst[(size_t)r * dpitch + i] = src[(size_t)r * spitch + i];
+}
+static cudaError_t repack(const double *src, int spitch, double *dst, int dpitch, int w, int rows,
+                          cudaStream_t st) {
+  dim3 grd((w + 127) / 128, rows < 32768 ? rows : 32768);
+  k_repack<<<grd, 128, 0, st>>>(src, spitch, dst, dpitch, w, rows);
+  return cudaGetLastError();
+}
 static cudaError_t h2d(tpls_ctx *c, double *dev0, const double *host, int nzp) {
-  const size_t w = sizeof(double) * (size_t)(c->nx + 2);
-  return cudaMemcpy2DAsync(dev0, sizeof(double) * c->px, host, w, w, (size_t)(c->ny + 2) * nzp,
-                           cudaMemcpyHostToDevice, c->st);
+  const int w = c->nx + 2, rows = (c->ny + 2) * nzp;
+  cudaError_t e = cudaMemcpyAsync(c->stage, host, sizeof(double) * (size_t)w * rows, cudaMemcpyHostToDevice, c->st);
+  if (e != cudaSuccess) return e;
+  return repack(c->stage, w, dev0, c->px, w, rows, c->st);
 }
 static cudaError_t d2h(tpls_ctx *c, double *host, const double *dev0, int nzp) {
-  const size_t w = sizeof(double) * (size_t)(c->nx + 2);
-  return cudaMemcpy2DAsync(host, w, dev0, sizeof(double) * c->px, w, (size_t)(c->ny + 2) * nzp,
-                           cudaMemcpyDeviceToHost, c->st);
+  const int w = c->nx + 2, rows = (c->ny + 2) * nzp;
+  cudaError_t e = repack(dev0, c->px, c->stage, w, w, rows, c->st);
+  if (e != cudaSuccess) return e;
+  return cudaMemcpyAsync(host, c->stage, sizeof(double) * (size_t)w * rows, cudaMemcpyDeviceToHost, c->st);
 }
 // viscosity_aug (-1:nx+2,-1:ny+2,0:nz+1) <-> device mu (x 0..nx+1, y -1..ny+2)
 static cudaError_t h2d_mu(tpls_ctx *c, double *mu0, const double *host) {
@@ -397,6 +421,9 @@ static int create_impl(int nx, int ny, int nz, const tpls_params *prm, const dou
     TCK(cudaMalloc(&b, sizeof(double) * (size_t)nx * ny));
     c->allocs.push_back(b);
     c->hbuf = (double *)b;
+    TCK(cudaMalloc(&b, sizeof(double) * (size_t)(nx + 2) * (ny + 2) * (nz + 2)));
+    c->allocs.push_back(b);
+    c->stage = (double *)b;
   }
   c->part_len = (size_t)ls_iter_blocks(c->g);
   size_t d2 = (size_t)diff2_blocks(c->g, nz + 1);
@@ -443,6 +470,7 @@ long long tpls_footprint_bytes(int nx, int ny, int nz, int precision) {
     t += 2 * round_alloc(D * nuv) + round_alloc(D * nw);  // FP64 u3, v3, w3
   }
   t += round_alloc(px * (ny + 2) * (nz + 2) + 64) + round_alloc(D * nz) + round_alloc(D * nx * ny);
+  t += round_alloc(D * (size_t)(nx + 2) * (ny + 2) * (nz + 2));  // host-layout staging
   Geo g;
   g.nx = nx;
   g.ny = ny;
@@ -536,15 +564,16 @@ static int momentum(tpls_ctx *c, int comp, const T *coef, T **X, int max_iterati
   } else {
     TCK(cudaMemsetAsync(X[0] - XOFF, 0, sizeof(T) * n, c->st));
   }
+  const SweepTiles tl = c->tiles;
   auto jac = [&](const T *src, T *dst) {
     if constexpr (sizeof(T) == sizeof(float)) return launch_jacobi_c(comp, g, c->ph, src, coef, c->pres, base, dst,
-                                                                      fuse, c->st);
-    else return launch_jacobi_c(comp, g, c->ph, src, coef, c->pres, dst, fuse, c->st);
+                                                                      fuse, c->st, tl);
+    else return launch_jacobi_c(comp, g, c->ph, src, coef, c->pres, dst, fuse, c->st, tl);
   };
   auto sor = [&](T *x, int flg, int it, int bc) {
     if constexpr (sizeof(T) == sizeof(float)) return launch_sor_c(comp, g, c->ph, x, coef, c->pres, base, flg, it,
-                                                                   bc, fuse, c->st);
-    else return launch_sor_c(comp, g, c->ph, x, coef, c->pres, flg, it, bc, fuse, c->st);
+                                                                   bc, fuse, c->st, tl);
+    else return launch_sor_c(comp, g, c->ph, x, coef, c->pres, flg, it, bc, fuse, c->st, tl);
   };
   const int N = max_iteration / 2;
   for (int it = 1; it <= N; it++) {
@@ -956,6 +985,107 @@ int tpls_step_async(tpls_ctx *c, int nsteps) {
   return TPLS_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Tile-shape autotuner of the momentum sweeps: each candidate block shape of
+// the Jacobi and even half-sweep kernels is timed with CUDA events on the
+// context's own records and iterate arrays (reps launches of the u
+// component), the fastest kept.  Results are cached per (grid, sweep
+// precision) for the process, so batch members of one shape tune once.
+}  // extern "C"
+
+static std::mutex g_tune_mu;
+static std::map<std::array<int, 4>, SweepTiles> g_tune_cache;
+
+extern "C" {
+
+static void destroy_graphs(tpls_ctx *c) {
+  for (cudaGraphExec_t &ge : c->gexec)
+    if (ge) {
+      cudaGraphExecDestroy(ge);
+      ge = nullptr;
+    }
+}
+
+int tpls_autotune(tpls_ctx *c, int reps) {
+  if (!c || c->capturing || reps < 1) return TPLS_ERR_ARG;
+  const bool f32 = c->mixed && !(c->prm.fp64_parts & TPLS_PART_MOMENTUM);
+  const std::array<int, 4> key = {c->nx, c->ny, c->nz, f32 ? 1 : 0};
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune_cache.find(key);
+    if (it != g_tune_cache.end()) {
+      TCK(cudaStreamSynchronize(c->st));
+      c->tiles = it->second;
+      c->tune_version++;
+      destroy_graphs(c);
+      return TPLS_OK;
+    }
+  }
+  TCK(cudaStreamSynchronize(c->st));
+  const Geo &g = c->g;
+  const int fuse = (g.ny % 2 == 0);
+  cudaEvent_t e0, e1;
+  TCK(cudaEventCreate(&e0));
+  TCK(cudaEventCreate(&e1));
+  auto launch = [&](int kind, const SweepTiles &t) -> cudaError_t {
+    // kind 0: Jacobi, 1: even half-sweep, 2: odd half-sweep (component u)
+    if (f32) {
+      float *a = c->x3f[0][0], *b = c->x3f[0][1];
+      if (kind == 0) return launch_jacobi_c(0, g, c->ph, a, c->coef32[0], c->pres, c->u2, b, fuse, c->st, t);
+      return launch_sor_c(0, g, c->ph, b, c->coef32[0], c->pres, c->u2, 0, kind == 1 ? 2 : 1, 1, fuse, c->st, t);
+    }
+    double *a = c->x3[0][0], *b = c->x3[0][1];
+    if (kind == 0) return launch_jacobi_c(0, g, c->ph, a, c->coef[0], c->pres, b, fuse, c->st, t);
+    return launch_sor_c(0, g, c->ph, b, c->coef[0], c->pres, 0, kind == 1 ? 2 : 1, 1, fuse, c->st, t);
+  };
+  SweepTiles best = c->tiles;
+  // The odd half-sweep's chunking changes its rounding, so it is not tuned:
+  // a result must not depend on the tile shapes chosen.
+  const int ncand[2] = {4, 4};
+  cudaError_t err = cudaSuccess;
+  for (int kind = 0; kind < 2 && err == cudaSuccess; kind++) {
+    float tbest = 1e30f;
+    for (int v = 0; v < ncand[kind] && err == cudaSuccess; v++) {
+      SweepTiles t = best;
+      if (kind == 0) t.jac = v;
+      else if (kind == 1) t.even = v;
+      else t.odd = v + 1;
+      err = launch(kind, t);  // warm-up
+      if (err == cudaSuccess) err = cudaEventRecord(e0, c->st);
+      for (int r = 0; r < reps && err == cudaSuccess; r++) err = launch(kind, t);
+      if (err == cudaSuccess) err = cudaEventRecord(e1, c->st);
+      if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+      float ms = 0.f;
+      if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+      if (err == cudaSuccess && ms < tbest) {
+        tbest = ms;
+        if (kind == 0) best.jac = t.jac;
+        else if (kind == 1) best.even = t.even;
+        else best.odd = t.odd;
+      }
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  TCK(err);
+  c->tiles = best;
+  c->tune_version++;
+  destroy_graphs(c);
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune_cache[key] = best;
+  }
+  return TPLS_OK;
+}
+
+int tpls_get_tiles(const tpls_ctx *c, int *tiles3) {
+  if (!c || !tiles3) return TPLS_ERR_ARG;
+  tiles3[0] = c->tiles.jac;
+  tiles3[1] = c->tiles.even;
+  tiles3[2] = c->tiles.odd;
+  return TPLS_OK;
+}
+
 int tpls_graphs_enable(tpls_ctx *c, int on) {
   if (!c) return TPLS_ERR_ARG;
   TCK(cudaStreamSynchronize(c->st));
@@ -980,6 +1110,7 @@ struct tpls_batch {
   std::vector<cudaEvent_t> join;
   cudaGraphExec_t gexec[3] = {nullptr, nullptr, nullptr};
   std::vector<long> n_static[3];  // kernels per member outside the CG loop
+  std::vector<int> tune_seen;     // members' tune_version when the graphs were captured
 };
 
 extern "C" {
@@ -1062,6 +1193,17 @@ int tpls_batch_step_async(tpls_batch *b, int nsteps) {
     const int ph = b->m[0]->phase;
     for (tpls_ctx *c : b->m)
       if (c->phase != ph || c->timing) return TPLS_ERR_STATE;
+    bool stale = b->tune_seen.size() != (size_t)n;
+    for (int q = 0; q < n && !stale; q++) stale = (b->tune_seen[q] != b->m[q]->tune_version);
+    if (stale) {  // a member was retuned: recapture with its new tile shapes
+      for (cudaGraphExec_t &ge : b->gexec)
+        if (ge) {
+          cudaGraphExecDestroy(ge);
+          ge = nullptr;
+        }
+      b->tune_seen.resize(n);
+      for (int q = 0; q < n; q++) b->tune_seen[q] = b->m[q]->tune_version;
+    }
     for (int q = 0; q < n; q++) {  // host uploads: ghost rows, then order the member streams before the batch
       tpls_ctx *c = b->m[q];
       int s = prologue(c);

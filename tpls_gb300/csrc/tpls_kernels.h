@@ -111,27 +111,36 @@ cudaError_t launch_sor(int comp, const Geo &g, const Phys &ph, double *x,
                        const double *rhs, const double *mu,
                        const double *pres, int flg, int iteration_time,
                        int bc, int fuse_ghosts, cudaStream_t st);
+// Tile-shape choice of the sweep kernels (autotuned per grid): jac / even =
+// block shape index (0: 32x4, 1: 32x8, 2: 64x4, 3: 16x8), odd = chunks per
+// column (0: by column length, 1: 8 warps, 2: 16 warps).
+struct SweepTiles {
+  int jac = 0, even = 0, odd = 0;
+};
+
 // Sweeps on the per-point coefficient records written by launch_mom_rhs
 // (coef != null there): same updates and boundary rows as launch_jacobi /
 // launch_sor with bc = 1.
 cudaError_t launch_jacobi_c(int comp, const Geo &g, const Phys &ph,
                             const double *xo, const double *coef,
                             const double *pres, double *x, int fuse_ghosts,
-                            cudaStream_t st);
+                            cudaStream_t st, const SweepTiles &t = SweepTiles());
 cudaError_t launch_sor_c(int comp, const Geo &g, const Phys &ph, double *x,
                          const double *coef, const double *pres, int flg,
                          int iteration_time, int bc, int fuse_ghosts,
-                         cudaStream_t st);
+                         cudaStream_t st, const SweepTiles &t = SweepTiles());
 // FP32 sweeps in defect form: x holds d = x - X for the FP64 base X (the
 // component's state), the records carry the correspondingly shifted b.
 cudaError_t launch_jacobi_c(int comp, const Geo &g, const Phys &ph,
                             const float *xo, const float *coef,
                             const double *pres, const double *X, float *x,
-                            int fuse_ghosts, cudaStream_t st);
+                            int fuse_ghosts, cudaStream_t st,
+                            const SweepTiles &t = SweepTiles());
 cudaError_t launch_sor_c(int comp, const Geo &g, const Phys &ph, float *x,
                          const float *coef, const double *pres,
                          const double *X, int flg, int iteration_time, int bc,
-                         int fuse_ghosts, cudaStream_t st);
+                         int fuse_ghosts, cudaStream_t st,
+                         const SweepTiles &t = SweepTiles());
 // d = -X (n elements) / x = X + d
 cudaError_t launch_defect_init(const double *X, float *d, size_t n, cudaStream_t st);
 cudaError_t launch_defect_apply(const double *X, const float *d, double *x, size_t n,
