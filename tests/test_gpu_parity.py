@@ -238,3 +238,49 @@ def test_step_is_deterministic():
         g.close()
     for k in outs[0]:
         np.testing.assert_array_equal(outs[0][k], outs[1][k])
+
+
+# Edge sizes: the smallest grid the library accepts (nx=4, ny=3, nz=4: odd
+# ny, no multigrid coarsening in y), ragged odd sizes in every direction,
+# a one-row-pair spanwise extent, and a tall column (nz >> nx) that takes
+# the 16-chunk odd-SOR path.
+EDGE = {"min": (4, 3, 4), "ragged": (33, 17, 31), "flat": (40, 4, 12), "tall": (8, 6, 160)}
+
+
+@pytest.mark.parametrize("size", list(EDGE))
+def test_edge_sizes_match_oracle_per_step(size):
+    nx, ny, nz = EDGE[size]
+    params, uin, st = make_case("A", nx=nx, ny=ny, nz=nz, p_rtol=1e-14, p_maxits=400)
+    o = Oracle(nx, ny, nz, params, uin)
+    o.set_state(st)
+    g = TplsGpu(nx, ny, nz, params, uin)
+    rows = (slice(None), slice(1, ny + 1), slice(None))
+    for step in range(2):
+        g.set_state(o.get_state())
+        o.step(1)
+        g.step(1)
+        for k in ("PHI2", "U2", "V2", "W2"):
+            e = relmax(g.get_field(k), o.get_field(k), rows)
+            assert e < TOL, (size, step, k, e)
+    g.close()
+
+
+def test_argument_errors_are_reported():
+    """Bad bounds, missing arrays and out-of-range fields return
+    TPLS_ERR_ARG (1) without touching the device state."""
+    import ctypes as C
+    nx, ny, nz = 16, 8, 12
+    params, uin, st = make_case("A", nx=nx, ny=ny, nz=nz)
+    g = TplsGpu(nx, ny, nz, params, uin)
+    lib = g.lib
+    assert lib.tpls_set_field(g.ctx, 99, None) == 1
+    assert lib.tpls_step(g.ctx, -1) == 1
+    buf = np.zeros((nx + 2, ny + 2, nz + 2), order="F")
+    lib.tpls_exchange2d.argtypes = [C.c_void_p, C.POINTER(C.c_double)] + [C.POINTER(C.c_int)] * 6
+    ip = lambda v: C.byref(C.c_int(v))
+    dp = buf.ctypes.data_as(C.POINTER(C.c_double))
+    assert lib.tpls_exchange2d(g.ctx, dp, ip(nx + 1), ip(ny), ip(nz + 1), ip(1), ip(1), ip(0)) == 1  # ex != nx
+    assert lib.tpls_exchange2d(g.ctx, dp, ip(nx), ip(ny), ip(nz + 1), ip(1), ip(1), ip(0)) == 0
+    g.set_state(st)
+    assert g.step(1) == 0
+    g.close()

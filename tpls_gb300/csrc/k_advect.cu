@@ -156,16 +156,8 @@ __global__ void k_to_float(const double *__restrict__ a, float *__restrict__ b, 
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
     b[i] = (float)a[i];
 }
-__global__ void k_to_double(const float *__restrict__ a, double *__restrict__ b, size_t n) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    b[i] = (double)a[i];
-}
 cudaError_t launch_to_float(const double *a, float *b, size_t n, cudaStream_t st) {
   k_to_float<<<1216, 256, 0, st>>>(a, b, n);
-  return cudaGetLastError();
-}
-cudaError_t launch_to_double(const float *a, double *b, size_t n, cudaStream_t st) {
-  k_to_double<<<1216, 256, 0, st>>>(a, b, n);
   return cudaGetLastError();
 }
 

@@ -9,6 +9,8 @@
 // on the interior values it needs.  That replaces the reference's sequence
 // of interior pass + boundary passes + exchange2d with one launch, with
 // identical values.
+#include <type_traits>
+
 #include "tpls_kernels.h"
 
 namespace tpls {
@@ -111,8 +113,11 @@ cudaError_t launch_ls_status(const Geo &g, const Phys &ph, const double *phi3, f
 // copy, linear z extrapolation, periodic y.  err_part (optional) receives
 // one partial of sum((pr - pr_new)^2) per block over i 1..nx, j 1..ny,
 // k 0..nz+1.
-template <typename TC, typename TI>
-__device__ __forceinline__ TC rs_update(const Geo &g, TC h, TC ktau, const TI *__restrict__ pr0,
+// RT: type of the updated value.  The FP32-mixed form keeps the iterate in
+// FP64 (RT = double) and evaluates only the increment ktau*dc in FP32, so the
+// iterate accumulates no FP32 rounding across the iterations and steps.
+template <typename TC, typename TI, typename RT>
+__device__ __forceinline__ RT rs_update(const Geo &g, TC h, TC ktau, const TI *__restrict__ pr0,
                                         const TC *__restrict__ D, const signed char *__restrict__ flags,
                                         int i, int j, int k) {
   const int c = TPLS_IDX(g, i, j, k);
@@ -145,14 +150,15 @@ __device__ __forceinline__ TC rs_update(const Geo &g, TC h, TC ktau, const TI *_
   } else {
     dc = zero;
   }
-  return p - ktau * dc;
+  if constexpr (sizeof(RT) == sizeof(TC)) return p - ktau * dc;
+  else return (RT)pr0[c] - (RT)(ktau * dc);
 }
 
-template <typename TC, typename TI>
-__device__ __forceinline__ TC rs_val(const Geo &g, const Phys &ph, TC h, TC ktau, const TI *pr, const TC *D,
+template <typename TC, typename TI, typename RT>
+__device__ __forceinline__ RT rs_val(const Geo &g, const Phys &ph, TC h, TC ktau, const TI *pr, const TC *D,
                                      const signed char *flags, int i, int j, int k) {
-  if (i == 0) return (TC)((k * (double)h - 0.5 * (double)h) - ph.height);
-  return rs_update<TC, TI>(g, h, ktau, pr, D, flags, (i == g.nx + 1) ? g.nx : i, j, k);
+  if (i == 0) return (RT)((k * (double)h - 0.5 * (double)h) - ph.height);
+  return rs_update<TC, TI, RT>(g, h, ktau, pr, D, flags, (i == g.nx + 1) ? g.nx : i, j, k);
 }
 
 // TI/TO: storage of the input/output iterate; TC: arithmetic (double for
@@ -167,15 +173,16 @@ __global__ void __launch_bounds__(LS_BX *LS_BY)
   double e = 0.0;
   if (i <= g.nx + 1 && j <= g.ny + 1) {
     const int jj = wrapy(j, g.ny);
-    TC v;
+    using RT = typename std::conditional<sizeof(TO) == sizeof(double), double, TC>::type;
+    RT v;
     if (k == 0)
-      v = (TC)2 * rs_val<TC, TI>(g, ph, h, ktau, pr, D, flags, i, jj, 1) -
-          rs_val<TC, TI>(g, ph, h, ktau, pr, D, flags, i, jj, 2);
+      v = (RT)2 * rs_val<TC, TI, RT>(g, ph, h, ktau, pr, D, flags, i, jj, 1) -
+          rs_val<TC, TI, RT>(g, ph, h, ktau, pr, D, flags, i, jj, 2);
     else if (k == g.nz + 1)
-      v = (TC)2 * rs_val<TC, TI>(g, ph, h, ktau, pr, D, flags, i, jj, g.nz) -
-          rs_val<TC, TI>(g, ph, h, ktau, pr, D, flags, i, jj, g.nz - 1);
+      v = (RT)2 * rs_val<TC, TI, RT>(g, ph, h, ktau, pr, D, flags, i, jj, g.nz) -
+          rs_val<TC, TI, RT>(g, ph, h, ktau, pr, D, flags, i, jj, g.nz - 1);
     else
-      v = rs_val<TC, TI>(g, ph, h, ktau, pr, D, flags, i, jj, k);
+      v = rs_val<TC, TI, RT>(g, ph, h, ktau, pr, D, flags, i, jj, k);
     const int c = TPLS_IDX(g, i, j, k);
     if (err_part && i >= 1 && i <= g.nx && j >= 1 && j <= g.ny) {
       const double d = (double)pr[c] - (double)v;
@@ -214,13 +221,9 @@ cudaError_t launch_ls_iter(const Geo &g, const Phys &ph, const double *pr, const
                            const signed char *flags, double *pr_new, double *err_part, cudaStream_t st) {
   return ls_iter<double, double, double>(g, ph, pr, D, flags, pr_new, err_part, st);
 }
-cudaError_t launch_ls_iter32(const Geo &g, const Phys &ph, const double *pr64, const float *pr32,
-                             const float *D, const signed char *flags, double *out64, float *out32,
-                             double *err_part, cudaStream_t st) {
-  if (pr64 && out64) return ls_iter<float, double, double>(g, ph, pr64, D, flags, out64, err_part, st);
-  if (pr64) return ls_iter<float, double, float>(g, ph, pr64, D, flags, out32, err_part, st);
-  if (out64) return ls_iter<float, float, double>(g, ph, pr32, D, flags, out64, err_part, st);
-  return ls_iter<float, float, float>(g, ph, pr32, D, flags, out32, err_part, st);
+cudaError_t launch_ls_iter32(const Geo &g, const Phys &ph, const double *pr, const float *D,
+                             const signed char *flags, double *out, double *err_part, cudaStream_t st) {
+  return ls_iter<float, double, double>(g, ph, pr, D, flags, out, err_part, st);
 }
 
 // ---------------------------------------------------------------------------

@@ -191,7 +191,9 @@ __device__ __forceinline__ void store_rec<float>(float *rec, float a0, float a1,
 
 // With X (the FP64 state of the component; FP32-mixed sweeps in defect form)
 // the stored b is that of d = x - X: b + sum(c_n X_n) - X_c, in FP64 with the
-// stored (rounded) coefficients, the neighbours taken as the sweeps take them.
+// unrounded coefficients (T), the neighbours taken as the sweeps take them.
+// The sweeps then solve x = sum(c~_n x_n) + b + sum((c_n - c~_n) X_n): the
+// FP32 rounding c~ of the coefficients acts only on d = x - X, not on x.
 template <typename T, typename TR>
 __device__ __forceinline__ void write_coef(int comp, const Geo &g, const Helm &h, const FcT<T> &f,
                                            double rhs, int k, const double *__restrict__ X, int c,
@@ -209,8 +211,8 @@ __device__ __forceinline__ void write_coef(int comp, const Geo &g, const Helm &h
       czp = (T)(-2) * czp;
     }
   }
-  const TR cxp = (TR)(ax2 * f.px * r), cxm = (TR)(ax2 * f.mx * r), cyp = (TR)(ay2 * f.py * r),
-           cym = (TR)(ay2 * f.my * r), tzp = (TR)czp, tzm = (TR)czm;
+  const T exp_ = ax2 * f.px * r, exm = ax2 * f.mx * r, eyp = ay2 * f.py * r, eym = ay2 * f.my * r;
+  const TR cxp = (TR)exp_, cxm = (TR)exm, cyp = (TR)eyp, cym = (TR)eym, tzp = (TR)czp, tzm = (TR)czm;
   TR b;
   if (X) {
     const int sy = g.sy, sz = g.sz;
@@ -224,12 +226,12 @@ __device__ __forceinline__ void write_coef(int comp, const Geo &g, const Helm &h
       zmv = (k == 0) ? xc : X[c - sz];
     }
     double bd = rhs * (double)r;
-    bd = fma((double)cxp, X[c + 1], bd);
-    bd = fma((double)cxm, X[c - 1], bd);
-    bd = fma((double)cyp, X[c + sy], bd);
-    bd = fma((double)cym, X[c - sy], bd);
-    bd = fma((double)tzp, zpv, bd);
-    bd = fma((double)tzm, zmv, bd);
+    bd = fma((double)exp_, X[c + 1], bd);
+    bd = fma((double)exm, X[c - 1], bd);
+    bd = fma((double)eyp, X[c + sy], bd);
+    bd = fma((double)eym, X[c - sy], bd);
+    bd = fma((double)czp, zpv, bd);
+    bd = fma((double)czm, zmv, bd);
     b = (TR)(bd - xc);
   } else {
     b = (TR)((T)rhs * r);
@@ -583,10 +585,6 @@ cudaError_t launch_source(const Geo &g, const Phys &ph, const double *u3, const 
                           double *rhs_p, cudaStream_t st) {
   return source(g, ph, u3, v3, w3, rhs_p, st);
 }
-cudaError_t launch_source(const Geo &g, const Phys &ph, const float *u3, const float *v3, const float *w3,
-                          double *rhs_p, cudaStream_t st) {
-  return source(g, ph, u3, v3, w3, rhs_p, st);
-}
 
 // pressure.f90:59-134 get_uvw_pres, written out of place into the next
 // state's velocity arrays over x 0..nx+1 and every row (ghost rows as
@@ -626,16 +624,6 @@ cudaError_t launch_project(const Geo &g, const Phys &ph, const double *u3, const
                            cudaStream_t st) {
   return project(g, ph, u3, v3, w3, p, u_inlet, u_out, v_out, w_out, st);
 }
-cudaError_t launch_project(const Geo &g, const Phys &ph, const float *u3, const float *v3, const float *w3,
-                           const double *p, const double *u_inlet, double *u_out, double *v_out, double *w_out,
-                           cudaStream_t st) {
-  return project(g, ph, u3, v3, w3, p, u_inlet, u_out, v_out, w_out, st);
-}
 
-cudaError_t launch_bc(int comp, const Geo &g, const Phys &ph, double *x,
-                      const double *pres, cudaStream_t st) {
-  (void)comp; (void)g; (void)ph; (void)x; (void)pres; (void)st;
-  return cudaErrorNotSupported;
-}
 
 }  // namespace tpls

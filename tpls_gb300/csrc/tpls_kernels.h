@@ -31,7 +31,6 @@ cudaError_t launch_advect(const Geo &g, const Phys &ph, const float *phi2,
                           const float *u2, const float *v2, const float *w2,
                           double *conv2_phi, cudaStream_t st);
 cudaError_t launch_to_float(const double *a, float *b, size_t n, cudaStream_t st);
-cudaError_t launch_to_double(const float *a, double *b, size_t n, cudaStream_t st);
 
 // two_phase_levelset.f90 / levelset.f90
 cudaError_t launch_ls_ab3(const Geo &g, const Phys &ph, const double *phi2,
@@ -48,16 +47,14 @@ cudaError_t launch_csf(const Geo &g, const Phys &ph, const double *phi3,
 cudaError_t launch_visc(const Geo &g, const Phys &ph, const double *phi2,
                         double *mu, cudaStream_t st);
 // FP32-mixed form of the level-set kernels: status decided in FP64 with D
-// stored in FP32, the redistancing iterations in FP32 (first reads the FP64
-// phi3 when pr64 is given, last writes the FP64 state when out64 is given),
+// stored in FP32, the redistancing increments in FP32 on FP64 iterates,
 // CSF evaluated in FP64 and stored in FP32, viscosity stored in FP32 (the
 // Heaviside evaluated in FP64).
 cudaError_t launch_ls_status(const Geo &g, const Phys &ph, const double *phi3,
                              float *D, signed char *flags, cudaStream_t st);
-cudaError_t launch_ls_iter32(const Geo &g, const Phys &ph, const double *pr64,
-                             const float *pr32, const float *D,
-                             const signed char *flags, double *out64,
-                             float *out32, double *err_part, cudaStream_t st);
+cudaError_t launch_ls_iter32(const Geo &g, const Phys &ph, const double *pr,
+                             const float *D, const signed char *flags,
+                             double *out, double *err_part, cudaStream_t st);
 cudaError_t launch_csf(const Geo &g, const Phys &ph, const double *phi3,
                        float *fx, float *fy, float *fz, cudaStream_t st);
 cudaError_t launch_visc(const Geo &g, const Phys &ph, const double *phi2,
@@ -147,8 +144,6 @@ cudaError_t launch_defect_apply(const double *X, const float *d, double *x, size
                                 cudaStream_t st);
 // One-time kernel attributes of the sweeps (dynamic shared memory).
 cudaError_t sweep_init();
-cudaError_t launch_bc(int comp, const Geo &g, const Phys &ph, double *x,
-                      const double *pres, cudaStream_t st);
 cudaError_t launch_diff2(const Geo &g, const double *a, const double *b,
                          int nzp, double *part, cudaStream_t st);
 cudaError_t launch_diff2(const Geo &g, const float *a, const float *b,
@@ -159,16 +154,8 @@ int diff2_blocks(const Geo &g, int nzp);
 cudaError_t launch_source(const Geo &g, const Phys &ph, const double *u3,
                           const double *v3, const double *w3, double *rhs_p,
                           cudaStream_t st);
-cudaError_t launch_source(const Geo &g, const Phys &ph, const float *u3,
-                          const float *v3, const float *w3, double *rhs_p,
-                          cudaStream_t st);
 cudaError_t launch_project(const Geo &g, const Phys &ph, const double *u3,
                            const double *v3, const double *w3,
-                           const double *p, const double *u_inlet,
-                           double *u_out, double *v_out, double *w_out,
-                           cudaStream_t st);
-cudaError_t launch_project(const Geo &g, const Phys &ph, const float *u3,
-                           const float *v3, const float *w3,
                            const double *p, const double *u_inlet,
                            double *u_out, double *v_out, double *w_out,
                            cudaStream_t st);
