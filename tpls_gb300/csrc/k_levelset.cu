@@ -116,17 +116,11 @@ cudaError_t launch_ls_status(const Geo &g, const Phys &ph, const double *phi3, f
 // RT: type of the updated value.  The FP32-mixed form keeps the iterate in
 // FP64 (RT = double) and evaluates only the increment ktau*dc in FP32, so the
 // iterate accumulates no FP32 rounding across the iterations and steps.
-template <typename TC, typename TI, typename RT>
-__device__ __forceinline__ RT rs_update(const Geo &g, TC h, TC ktau, const TI *__restrict__ pr0,
-                                        const TC *__restrict__ D, const signed char *__restrict__ flags,
-                                        int i, int j, int k) {
-  const int c = TPLS_IDX(g, i, j, k);
-  const int f = flags[c];
-  struct Ld {
-    const TI *p;
-    __device__ TC operator[](int q) const { return (TC)p[q]; }
-  } pr{pr0};
-  const TC p = pr[c];
+// dc of the update at point c, p = its value, pr a loader of the stencil
+// values in the arithmetic type TC.
+template <typename TC, typename LD>
+__device__ __forceinline__ TC rs_dc(const Geo &g, TC h, const LD &pr, TC p, const TC *__restrict__ D, int f,
+                                   int c) {
   const TC sg = (TC)(((f >> 1) & 3) - 1);
   const TC zero = (TC)0;
   TC dc;
@@ -150,6 +144,23 @@ __device__ __forceinline__ RT rs_update(const Geo &g, TC h, TC ktau, const TI *_
   } else {
     dc = zero;
   }
+  return dc;
+}
+
+template <typename TC, typename TI>
+struct LdCvt {
+  const TI *p;
+  __device__ __forceinline__ TC operator[](int q) const { return (TC)p[q]; }
+};
+
+template <typename TC, typename TI, typename RT>
+__device__ __forceinline__ RT rs_update(const Geo &g, TC h, TC ktau, const TI *__restrict__ pr0,
+                                        const TC *__restrict__ D, const signed char *__restrict__ flags,
+                                        int i, int j, int k) {
+  const int c = TPLS_IDX(g, i, j, k);
+  const LdCvt<TC, TI> pr{pr0};
+  const TC p = pr[c];
+  const TC dc = rs_dc<TC>(g, h, pr, p, D, flags[c], c);
   if constexpr (sizeof(RT) == sizeof(TC)) return p - ktau * dc;
   else return (RT)pr0[c] - (RT)(ktau * dc);
 }
@@ -204,6 +215,92 @@ __global__ void __launch_bounds__(LS_BX *LS_BY)
   }
 }
 
+// FP32-mixed redistancing: the iterate is carried as a float pair
+// (hi, lo) with hi + lo holding ~48 bits of the FP64 value.  The stencil
+// reads the hi parts (FP32 arithmetic, no FP64 conversions on the common
+// path), and the increment is added into the pair with an error-free
+// two-sum, so the iterate accumulates no FP32 rounding over the iterations
+// (FP64<->FP32 conversions run on GB300's FP64 pipe, which made an FP64
+// iterate cost as much as FP64 arithmetic).  IN64: the input is the FP64
+// phi3 (first iteration); OUT64: the output is the FP64 state (last).
+struct FF {
+  float hi, lo;
+};
+__device__ __forceinline__ FF two_sum(float a, float b) {
+  const float s = a + b;
+  const float bp = s - a;
+  return FF{s, (a - (s - bp)) + (b - bp)};
+}
+__device__ __forceinline__ FF ff_split(double v) {
+  const float hi = (float)v;
+  return FF{hi, (float)(v - (double)hi)};
+}
+__device__ __forceinline__ double ff_dbl(const FF &v) { return (double)v.hi + (double)v.lo; }
+
+template <bool IN64>
+struct FFSrc {
+  const double *x64;
+  const float *hi, *lo;
+  __device__ __forceinline__ float operator[](int q) const { return IN64 ? (float)x64[q] : hi[q]; }
+  __device__ __forceinline__ double exact(int q) const { return IN64 ? x64[q] : (double)hi[q] + (double)lo[q]; }
+};
+
+template <bool IN64>
+__device__ __forceinline__ FF ff_val(const Geo &g, const Phys &ph, float h, float ktau, const FFSrc<IN64> &src,
+                                     const float *D, const signed char *flags, int i, int j, int k) {
+  if (i == 0) return ff_split((k * (double)h - 0.5 * (double)h) - ph.height);
+  if (i == g.nx + 1) i = g.nx;
+  const int c = TPLS_IDX(g, i, j, k);
+  const float p = src[c];
+  const float inc = ktau * rs_dc<float>(g, h, src, p, D, flags[c], c);
+  if (IN64) return ff_split(src.x64[c] - (double)inc);
+  return two_sum(src.hi[c], src.lo[c] - inc);
+}
+
+template <bool IN64, bool OUT64>
+__global__ void __launch_bounds__(LS_BX *LS_BY)
+    k_ls_iter_ff(Geo g, Phys ph, float h, float ktau, FFSrc<IN64> src, const float *__restrict__ D,
+                 const signed char *__restrict__ flags, double *__restrict__ out64, float *__restrict__ ohi,
+                 float *__restrict__ olo, double *__restrict__ err_part) {
+  const int i = blockIdx.x * LS_BX + threadIdx.x, j = blockIdx.y * LS_BY + threadIdx.y;
+  const int k = blockIdx.z;
+  double e = 0.0;
+  if (i <= g.nx + 1 && j <= g.ny + 1) {
+    const int jj = wrapy(j, g.ny);
+    const int c = TPLS_IDX(g, i, j, k);
+    FF v;
+    if (k == 0 || k == g.nz + 1) {  // linear extrapolation, in FP64
+      const int k1 = (k == 0) ? 1 : g.nz, k2 = (k == 0) ? 2 : g.nz - 1;
+      v = ff_split(2.0 * ff_dbl(ff_val<IN64>(g, ph, h, ktau, src, D, flags, i, jj, k1)) -
+                   ff_dbl(ff_val<IN64>(g, ph, h, ktau, src, D, flags, i, jj, k2)));
+    } else {
+      v = ff_val<IN64>(g, ph, h, ktau, src, D, flags, i, jj, k);
+    }
+    if (err_part && i >= 1 && i <= g.nx && j >= 1 && j <= g.ny) {
+      const double d = src.exact(c) - ff_dbl(v);
+      e = d * d;
+    }
+    if (OUT64) {
+      out64[c] = ff_dbl(v);
+    } else {
+      ohi[c] = v.hi;
+      olo[c] = v.lo;
+    }
+  }
+  if (err_part) {
+    __shared__ double s[LS_BX * LS_BY / 32];
+    for (int o = 16; o > 0; o >>= 1) e += __shfl_down_sync(0xffffffffu, e, o);
+    const int t = threadIdx.y * LS_BX + threadIdx.x;
+    if ((t & 31) == 0) s[t >> 5] = e;
+    __syncthreads();
+    if (t == 0) {
+      double a = 0.0;
+      for (int q = 0; q < LS_BX * LS_BY / 32; q++) a += s[q];
+      err_part[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)] = a;
+    }
+  }
+}
+
 int ls_iter_blocks(const Geo &g) {
   dim3 gr = full_grid(g, g.nz + 2);
   return (int)(gr.x * gr.y * gr.z);
@@ -221,9 +318,28 @@ cudaError_t launch_ls_iter(const Geo &g, const Phys &ph, const double *pr, const
                            const signed char *flags, double *pr_new, double *err_part, cudaStream_t st) {
   return ls_iter<double, double, double>(g, ph, pr, D, flags, pr_new, err_part, st);
 }
-cudaError_t launch_ls_iter32(const Geo &g, const Phys &ph, const double *pr, const float *D,
-                             const signed char *flags, double *out, double *err_part, cudaStream_t st) {
-  return ls_iter<float, double, double>(g, ph, pr, D, flags, out, err_part, st);
+cudaError_t launch_ls_iter_ff(const Geo &g, const Phys &ph, const double *in64, const float *hi,
+                              const float *lo, const float *D, const signed char *flags, double *out64,
+                              float *ohi, float *olo, double *err_part, cudaStream_t st) {
+  const float h = (float)ph.dx, ktau = (float)(0.3 * ph.dx / ph.dx);
+  const dim3 grd = full_grid(g, g.nz + 2), blk(LS_BX, LS_BY);
+  if (in64) {
+    const FFSrc<true> src{in64, nullptr, nullptr};
+    if (out64)
+      k_ls_iter_ff<true, true><<<grd, blk, 0, st>>>(g, ph, h, ktau, src, D, flags, out64, nullptr, nullptr,
+                                                   err_part);
+    else
+      k_ls_iter_ff<true, false><<<grd, blk, 0, st>>>(g, ph, h, ktau, src, D, flags, nullptr, ohi, olo, err_part);
+  } else {
+    const FFSrc<false> src{nullptr, hi, lo};
+    if (out64)
+      k_ls_iter_ff<false, true><<<grd, blk, 0, st>>>(g, ph, h, ktau, src, D, flags, out64, nullptr, nullptr,
+                                                    err_part);
+    else
+      k_ls_iter_ff<false, false><<<grd, blk, 0, st>>>(g, ph, h, ktau, src, D, flags, nullptr, ohi, olo,
+                                                     err_part);
+  }
+  return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------

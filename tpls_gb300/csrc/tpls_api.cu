@@ -46,6 +46,7 @@ struct tpls_ctx {
   // (the state above stays FP64)
   int mixed = 0;
   float *phi32, *u32, *v32, *w32, *mu32, *D32, *fx32, *fy32, *fz32;
+  float *ffh[2], *ffl[2];  // float-pair redistancing iterates (hi, lo), ping-pong
   float *coef32[3];
   float *x3f[3][2];
   double *hbuf = nullptr; // interface height (nx*ny)
@@ -359,8 +360,10 @@ static int create_impl(int nx, int ny, int nz, const tpls_params *prm, const dou
     TCK(alloc_field(c, 1, ny + 4, nz + 2, &c->mu));
   } else {
     const int parts = prm->fp64_parts;
-    TCK(alloc_p(c, &c->phiB));  // FP64 iterates of the redistancing
-    if (parts & TPLS_PART_LEVELSET) TCK(alloc_p(c, &c->D));
+    if (parts & TPLS_PART_LEVELSET) {
+      TCK(alloc_p(c, &c->phiB));
+      TCK(alloc_p(c, &c->D));
+    }
     if (parts & (TPLS_PART_MOMENTUM | TPLS_PART_MOM_STENCIL)) {  // FP64 stencil inputs
       double **pf2[] = {&c->fx, &c->fy, &c->fz};
       for (double **p : pf2) TCK(alloc_p(c, p));
@@ -383,7 +386,8 @@ static int create_impl(int nx, int ny, int nz, const tpls_params *prm, const dou
         c->coef[q] = (double *)b;
       }
     }
-    float **qf[] = {&c->phi32, &c->D32, &c->fx32, &c->fy32, &c->fz32};
+    float **qf[] = {&c->phi32, &c->D32, &c->fx32, &c->fy32, &c->fz32, &c->ffh[0], &c->ffl[0], &c->ffh[1],
+                    &c->ffl[1]};
     for (float **p : qf) TCK(alloc_p(c, p));
     float **quv[] = {&c->u32, &c->v32, &c->x3f[0][0], &c->x3f[0][1], &c->x3f[1][0], &c->x3f[1][1]};
     for (float **p : quv) TCK(alloc_field(c, 0, ny + 2, nz, p));
@@ -463,7 +467,7 @@ long long tpls_footprint_bytes(int nx, int ny, int nz, int precision) {
     t += 5 * round_alloc(D * np) + 4 * round_alloc(D * nuv) + 2 * round_alloc(D * nw);
     t += 2 * round_alloc(D * nrec * nz) + round_alloc(D * nrec * (nz + 1)) + round_alloc(D * nmu);
   } else {
-    t += 5 * round_alloc(F * np) + round_alloc(D * np) + 6 * round_alloc(F * nuv) + 3 * round_alloc(F * nw);
+    t += 9 * round_alloc(F * np) + 6 * round_alloc(F * nuv) + 3 * round_alloc(F * nw);
     t += 2 * round_alloc(F * nrec * nz) + round_alloc(F * nrec * (nz + 1)) + round_alloc(F * nmu);
     t += 2 * round_alloc(D * nuv) + round_alloc(D * nw);  // FP64 u3, v3, w3
   }
@@ -791,10 +795,10 @@ static int step_once_mixed(tpls_ctx *c) {
       const double *src = (it == 1) ? c->phiA : ((it % 2 == 0) ? c->phiB : c->phiA);
       double *dst = (it == L) ? c->phi2 : ((it % 2 == 1) ? c->phiB : c->phiA);
       LCK(c, launch_ls_iter(g, ph, src, c->D, c->flags, dst, ep, st));
-    } else {  // FP32 increments on FP64 iterates
-      const double *src = (it == 1) ? c->phiA : ((it % 2 == 0) ? c->phiB : c->phiA);
-      double *dst = (it == L) ? c->phi2 : ((it % 2 == 1) ? c->phiB : c->phiA);
-      LCK(c, launch_ls_iter32(g, ph, src, c->D32, c->flags, dst, ep, st));
+    } else {  // FP32 increments on float-pair iterates: it reads pair it%2, writes pair (it+1)%2
+      const int ri = it % 2, wi = (it + 1) % 2;
+      LCK(c, launch_ls_iter_ff(g, ph, (it == 1) ? c->phiA : nullptr, c->ffh[ri], c->ffl[ri], c->D32, c->flags,
+                               (it == L) ? c->phi2 : nullptr, c->ffh[wi], c->ffl[wi], ep, st));
     }
   }
   if (L > 0) LCK(c, finish_sum(c->part, ls_iter_blocks(g), c->scal + SC_ERR_PHI, 1, st));

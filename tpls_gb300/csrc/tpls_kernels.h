@@ -47,14 +47,18 @@ cudaError_t launch_csf(const Geo &g, const Phys &ph, const double *phi3,
 cudaError_t launch_visc(const Geo &g, const Phys &ph, const double *phi2,
                         double *mu, cudaStream_t st);
 // FP32-mixed form of the level-set kernels: status decided in FP64 with D
-// stored in FP32, the redistancing increments in FP32 on FP64 iterates,
+// stored in FP32, the redistancing increments in FP32 on float-pair iterates,
 // CSF evaluated in FP64 and stored in FP32, viscosity stored in FP32 (the
 // Heaviside evaluated in FP64).
 cudaError_t launch_ls_status(const Geo &g, const Phys &ph, const double *phi3,
                              float *D, signed char *flags, cudaStream_t st);
-cudaError_t launch_ls_iter32(const Geo &g, const Phys &ph, const double *pr,
-                             const float *D, const signed char *flags,
-                             double *out, double *err_part, cudaStream_t st);
+// in64 (FP64 input, first iteration) or the float pair (hi, lo); out64
+// (FP64 output, last iteration) or the float pair (ohi, olo).
+cudaError_t launch_ls_iter_ff(const Geo &g, const Phys &ph, const double *in64,
+                              const float *hi, const float *lo, const float *D,
+                              const signed char *flags, double *out64,
+                              float *ohi, float *olo, double *err_part,
+                              cudaStream_t st);
 cudaError_t launch_csf(const Geo &g, const Phys &ph, const double *phi3,
                        float *fx, float *fy, float *fz, cudaStream_t st);
 cudaError_t launch_visc(const Geo &g, const Phys &ph, const double *phi2,
