@@ -160,8 +160,9 @@ def run_gpu(args, ws, rank, local) -> dict | None:
     w = WORKLOADS[args.config]
     precision = _precision(args)
     parts = args.fp64_parts if precision == 1 else 0
-    params, uin, st = make_case(args.config, p_rtol=args.p_rtol, precision=precision, fp64_parts=parts)
-    nx, ny, nz = w.nx, w.ny, w.nz
+    nx, ny, nz = args.grid if args.grid else (w.nx, w.ny, w.nz)
+    params, uin, st = make_case(args.config, nx=nx, ny=ny, nz=nz, p_rtol=args.p_rtol, precision=precision,
+                                fp64_parts=parts)
     cells = nx * ny * nz
     g = TplsGpu(nx, ny, nz, params, uin)
     g.set_state(st)
@@ -252,7 +253,7 @@ def run_gpu(args, ws, rank, local) -> dict | None:
     fp64_pct = _profile_figure("fp64pipe", dominant, wl)
     cpu = None
     if ws == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(args.config, args.cpu_seconds)
+        cpu = cpu_baseline(args.config, args.cpu_seconds, (nx, ny, nz))
     out = {
         "metric": "cell-steps/s",
         "value": value,
@@ -266,7 +267,8 @@ def run_gpu(args, ws, rank, local) -> dict | None:
         "vs_baseline": None,
         "dtype": "f64" if precision == 0 else "f32 stencils/sweeps/smoothing + f64 state/dots/coarse solve",
         "data": "synthetic: seeded two-layer channel (4-mode interface, +-1e-3 velocity noise), no dataset",
-        "config": {"workload": w.name, "grid": [nx, ny, nz], "cells": cells, "m": w.m, "re": w.re,
+        "config": {"workload": w.name if not args.grid else f"{w.name}, resized to {nx}x{ny}x{nz}",
+                   "grid": [nx, ny, nz], "cells": cells, "m": w.m, "re": w.re,
                    "mom_uvw": params.mom_u, "levelset": params.levelset, "p_rtol": params.p_rtol,
                    "precision": "fp64" if precision == 0 else "fp32-mixed",
                    "fp64_parts": parts,
@@ -457,7 +459,7 @@ def _precision(args) -> int:
     return 1 if args.config in ("C", "D") else 0
 
 
-def cpu_baseline(config: str, seconds: float) -> dict:
+def cpu_baseline(config: str, seconds: float, grid=None) -> dict:
     """The oracle (C restatement of the reference routines, OpenMP over all
     host cores) on the same workload, as many whole timesteps as fit in
     about `seconds` (at least one)."""
@@ -466,8 +468,9 @@ def cpu_baseline(config: str, seconds: float) -> dict:
     cores = os.cpu_count() or 1
     set_threads(cores)
     w = WORKLOADS[config]
-    params, uin, st = make_case(config)
-    o = Oracle(w.nx, w.ny, w.nz, params, uin)
+    nx, ny, nz = grid if grid else (w.nx, w.ny, w.nz)
+    params, uin, st = make_case(config, nx=nx, ny=ny, nz=nz)
+    o = Oracle(nx, ny, nz, params, uin)
     o.set_state(st)
     n = 0
     t0 = time.perf_counter()
@@ -478,8 +481,9 @@ def cpu_baseline(config: str, seconds: float) -> dict:
             break
     dt = time.perf_counter() - t0
     o.close()
-    return {"value": w.nx * w.ny * w.nz * n / dt, "unit": "cell-steps/s", "cores": cores, "kind": "port",
-            "sample": f"{n} full timestep(s) of {w.name} from the seeded initial state"}
+    return {"value": nx * ny * nz * n / dt, "unit": "cell-steps/s", "cores": cores, "kind": "port",
+            "sample": f"{n} full timestep(s) of the {nx}x{ny}x{nz} channel of {w.name.split(':')[0]} "
+                      f"from the seeded initial state"}
 
 
 def run_reference(args, ws, rank) -> dict | None:
@@ -539,6 +543,8 @@ def main():
     ap.add_argument("--ref-seconds", type=float, default=120.0)
     ap.add_argument("--instances", type=int, default=48)
     ap.add_argument("--no-one-by-one", action="store_true")
+    ap.add_argument("--grid", type=int, nargs=3, default=None, metavar=("NX", "NY", "NZ"),
+                    help="resize the workload (small cases for profiling captures)")
     ap.add_argument("--jobs", type=int, default=16)
     ap.add_argument("--rate", type=float, default=1.0)
     args = ap.parse_args()

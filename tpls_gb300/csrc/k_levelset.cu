@@ -245,16 +245,38 @@ struct FFSrc {
   __device__ __forceinline__ double exact(int q) const { return IN64 ? x64[q] : (double)hi[q] + (double)lo[q]; }
 };
 
+// inlet row (levelset.f90:168-177), FP64, out of line (see below)
+__device__ __noinline__ FF ff_inlet(float h, double height, int k) {
+  return ff_split((k * (double)h - 0.5 * (double)h) - height);
+}
+
 template <bool IN64>
 __device__ __forceinline__ FF ff_val(const Geo &g, const Phys &ph, float h, float ktau, const FFSrc<IN64> &src,
                                      const float *D, const signed char *flags, int i, int j, int k) {
-  if (i == 0) return ff_split((k * (double)h - 0.5 * (double)h) - ph.height);
+  if (i == 0) return ff_inlet(h, ph.height, k);
   if (i == g.nx + 1) i = g.nx;
   const int c = TPLS_IDX(g, i, j, k);
   const float p = src[c];
   const float inc = ktau * rs_dc<float>(g, h, src, p, D, flags[c], c);
   if (IN64) return ff_split(src.x64[c] - (double)inc);
   return two_sum(src.hi[c], src.lo[c] - inc);
+}
+
+// The FP64 paths of the float-pair iteration (the extrapolated ghost planes,
+// the residual of the last iteration) are kept out of line: if-converted
+// into the kernel body their FP64 instructions would be issued, predicated
+// off, for every point and fill GB300's slow FP64 pipe.
+template <bool IN64>
+__device__ __noinline__ FF ff_ghost_plane(const Geo &g, const Phys &ph, float h, float ktau, const FFSrc<IN64> &src,
+                                          const float *D, const signed char *flags, int i, int jj, int k) {
+  const int k1 = (k == 0) ? 1 : g.nz, k2 = (k == 0) ? 2 : g.nz - 1;
+  return ff_split(2.0 * ff_dbl(ff_val<IN64>(g, ph, h, ktau, src, D, flags, i, jj, k1)) -
+                  ff_dbl(ff_val<IN64>(g, ph, h, ktau, src, D, flags, i, jj, k2)));
+}
+template <bool IN64>
+__device__ __noinline__ double ff_sq_change(const FFSrc<IN64> &src, int c, FF v) {
+  const double d = src.exact(c) - ff_dbl(v);
+  return d * d;
 }
 
 template <bool IN64, bool OUT64>
@@ -269,17 +291,11 @@ __global__ void __launch_bounds__(LS_BX *LS_BY)
     const int jj = wrapy(j, g.ny);
     const int c = TPLS_IDX(g, i, j, k);
     FF v;
-    if (k == 0 || k == g.nz + 1) {  // linear extrapolation, in FP64
-      const int k1 = (k == 0) ? 1 : g.nz, k2 = (k == 0) ? 2 : g.nz - 1;
-      v = ff_split(2.0 * ff_dbl(ff_val<IN64>(g, ph, h, ktau, src, D, flags, i, jj, k1)) -
-                   ff_dbl(ff_val<IN64>(g, ph, h, ktau, src, D, flags, i, jj, k2)));
-    } else {
+    if (k == 0 || k == g.nz + 1)  // linear extrapolation, in FP64
+      v = ff_ghost_plane<IN64>(g, ph, h, ktau, src, D, flags, i, jj, k);
+    else
       v = ff_val<IN64>(g, ph, h, ktau, src, D, flags, i, jj, k);
-    }
-    if (err_part && i >= 1 && i <= g.nx && j >= 1 && j <= g.ny) {
-      const double d = src.exact(c) - ff_dbl(v);
-      e = d * d;
-    }
+    if (err_part && i >= 1 && i <= g.nx && j >= 1 && j <= g.ny) e = ff_sq_change<IN64>(src, c, v);
     if (OUT64) {
       out64[c] = ff_dbl(v);
     } else {
