@@ -301,6 +301,83 @@ def run_gpu(args, ws, rank, local) -> dict | None:
     return out
 
 
+def run_accuracy(args) -> dict:
+    """Error of the FP32-mixed form against the FP64 form on one workload.
+
+    Both forms start from the same seeded state and step side by side (FP64
+    pressure solves at rtol 1e-10 in both, so the solver tolerance does not
+    mask the arithmetic); at each checkpoint the relative max-norm difference
+    of phi, u, v, w and p over the interior rows, and each form's liquid-volume
+    drift from the initial volume, are recorded.  Not a throughput line."""
+    import numpy as np
+    import torch
+    from tpls_gb300.api import TplsGpu
+    from tpls_gb300.channel import WORKLOADS, make_case
+
+    torch.cuda.set_device(0)
+    w = WORKLOADS[args.config]
+    nx, ny, nz = args.grid if args.grid else (w.nx, w.ny, w.nz)
+
+    def open_form(prec, parts, rtol=1e-10):
+        p, u, st = make_case(args.config, nx=nx, ny=ny, nz=nz, precision=prec, fp64_parts=parts,
+                             p_rtol=rtol, p_maxits=400)
+        g = TplsGpu(nx, ny, nz, p, u)
+        g.set_state(st)
+        return g
+
+    def rel(a, b):
+        a, b = a[:, 1:ny + 1, :], b[:, 1:ny + 1, :]
+        den = float(np.max(np.abs(b))) or 1.0
+        return float(np.max(np.abs(a - b))) / den
+
+    ref = open_form(0, 0)
+    if args.compare_rtol > 0.0:  # the FP64 form at another pressure tolerance (the reference's is 1e-5)
+        mix = open_form(0, 0, args.compare_rtol)
+    elif args.perturb > 0.0:  # the FP64 form against itself with u perturbed: the workload's own sensitivity
+        mix = open_form(0, 0)
+        u = mix.get_field(args.perturb_field)
+        rng = np.random.default_rng(7)
+        mix.set_field(args.perturb_field, np.asfortranarray(u * (1.0 + args.perturb * rng.standard_normal(u.shape))))
+    else:
+        mix = open_form(1, args.fp64_parts)
+    v0 = ref.stats()["liquid_volume"]
+    if args.accuracy_every > 0:
+        marks = list(range(args.accuracy_every, args.accuracy + 1, args.accuracy_every))
+    else:
+        marks = sorted({m for m in (20, 50, 100, 200, 500, 1000) if m < args.accuracy} | {args.accuracy})
+    rows, done = [], 0
+    for m in marks:
+        for g in (ref, mix):
+            if g.step(m - done) != 0:
+                raise SystemExit(f"tpls_step failed before step {m}")
+        done = m
+        row = {"step": m}
+        for f in ("PHI2", "U2", "V2", "W2", "PRES"):
+            a, b = mix.get_field(f), ref.get_field(f)
+            row[f.rstrip("2").lower()] = rel(a, b)
+            if f in ("PHI2", "U2"):  # where the largest difference sits (i, j, k of the field's array)
+                d = np.abs(a[:, 1:ny + 1, :] - b[:, 1:ny + 1, :])
+                i, j, k = np.unravel_index(int(np.argmax(d)), d.shape)
+                row[f.rstrip("2").lower() + "_at"] = [int(i), int(j) + 1, int(k)]
+            if f == "PHI2":  # near the interface (|phi| < 3 dz), where curvature amplifies it: in units of dz
+                band = np.abs(b[:, 1:ny + 1, :]) < 3.0 / nz
+                row["phi_band_dz"] = float(np.max(d[band])) * nz if band.any() else 0.0
+        row["volume_drift_fp64"] = (ref.stats()["liquid_volume"] - v0) / v0
+        row["volume_drift_mixed"] = (mix.stats()["liquid_volume"] - v0) / v0
+        rows.append(row)
+    ref.close()
+    mix.close()
+    if args.compare_rtol > 0.0:
+        what = f"fp64 at pressure rtol {args.compare_rtol:g} vs fp64 at rtol 1e-10"
+    elif args.perturb > 0.0:
+        what = f"fp64 with {args.perturb_field} perturbed by {args.perturb:g} (relative, seeded normal) vs fp64"
+    else:
+        what = "fp32-mixed relative max-norm error vs fp64"
+    return {"metric": what, "workload": w.name,
+            "grid": [nx, ny, nz], "fp64_parts": args.fp64_parts, "p_rtol": 1e-10,
+            "region": "interior rows j=1..ny, every i and z plane", "checkpoints": rows}
+
+
 def run_batch(args, ws, rank, local) -> dict | None:
     """The batched workload: 48 seeded instances of uneven grids, FP32-mixed,
     all advanced by one CUDA-graph launch per batch step; compared with the
@@ -547,11 +624,24 @@ def main():
                     help="resize the workload (small cases for profiling captures)")
     ap.add_argument("--jobs", type=int, default=16)
     ap.add_argument("--rate", type=float, default=1.0)
+    ap.add_argument("--accuracy", type=int, default=0, metavar="STEPS",
+                    help="instead of timing: step the FP64 and FP32-mixed forms side by side for STEPS "
+                         "steps and print their differences (one JSON line)")
+    ap.add_argument("--accuracy-every", type=int, default=0, metavar="N",
+                    help="with --accuracy: a checkpoint every N steps")
+    ap.add_argument("--perturb-field", default="U2", choices=["U2", "PHI2"])
+    ap.add_argument("--compare-rtol", type=float, default=0.0,
+                    help="with --accuracy: compare the FP64 form at this pressure rtol with the FP64 form at 1e-10")
+    ap.add_argument("--perturb", type=float, default=0.0,
+                    help="with --accuracy: compare the FP64 form with itself started from u perturbed by this "
+                         "relative amount (how far the workload amplifies a rounding-sized difference)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3  # timing rule: at least 3 warm-up steps
     ws, rank, local = _dist()
-    if args.impl == "reference":
+    if args.accuracy > 0:
+        out = run_accuracy(args) if rank == 0 else None
+    elif args.impl == "reference":
         out = run_reference(args, ws, rank)
     elif args.config == "D":
         out = run_batch(args, ws, rank, local)

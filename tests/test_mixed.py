@@ -1,8 +1,9 @@
 """FP32-mixed form (TPLS_PREC_FP32_MIXED) against the FP64 GPU form.
 
 The mixed form runs WENO5, redistancing, CSF, the momentum stencils and
-sweeps and the multigrid smoothing in FP32 on rounded copies of the FP64
-state; the state, the AB3 updates, the right-hand sides, the CG recurrences
+sweeps and the multigrid smoothing in FP32 (WENO5 on rounded copies of the
+FP64 state, the momentum stencils on the state split into exact FP32
+pairs); the state, the AB3 updates, the CG recurrences
 and dot products, the coarsest solve, the projection and the volume
 integral stay FP64.  Tolerances (relative max-norm over the field):
 phi and u 1e-5 after one step and after 20 steps; v and w (whose scale is
@@ -87,5 +88,24 @@ def test_mixed_with_every_part_fp64_equals_fp64_form():
     a, b = ref.get_state(), mix.get_state()
     assert all(np.array_equal(a[k], b[k]) for k in STATE_FIELDS)
     assert np.array_equal(ref.get_field("U3"), mix.get_field("U3"))
+    ref.close()
+    mix.close()
+
+
+@pytest.mark.parametrize("parts", [0, 16])
+def test_mixed_hundred_steps_fp32_and_fp64_stencils(parts):
+    """100 steps with the momentum stencils in FP32 (parts 0: velocity
+    values split into exact FP32 pairs, the sweeps' coefficients recomputed
+    from the FP32 viscosity) and in FP64 (parts 16): phi and u stay within
+    1e-5 of the FP64 form, v and w within 1e-4, the liquid volume within
+    1e-8."""
+    ref = _ctx(0)
+    mix = _ctx(1, fp64_parts=parts)
+    assert ref.step(100) == 0 and mix.step(100) == 0
+    e = {k: relmax(mix.get_field(k), ref.get_field(k), ROWS) for k in ("PHI2", "U2", "V2", "W2")}
+    assert e["PHI2"] < 1e-5 and e["U2"] < 1e-5, e
+    assert e["V2"] < 1e-4 and e["W2"] < 1e-4, e
+    vr, vm = ref.stats()["liquid_volume"], mix.stats()["liquid_volume"]
+    assert abs(vm - vr) <= 1e-8 * abs(vr)
     ref.close()
     mix.close()

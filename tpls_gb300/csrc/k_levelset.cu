@@ -12,6 +12,7 @@
 #include <type_traits>
 
 #include "tpls_kernels.h"
+#include "tpls_pair.cuh"
 
 namespace tpls {
 
@@ -217,12 +218,13 @@ __global__ void __launch_bounds__(LS_BX *LS_BY)
 
 // FP32-mixed redistancing: the iterate is carried as a float pair
 // (hi, lo) with hi + lo holding ~48 bits of the FP64 value.  The stencil
-// reads the hi parts (FP32 arithmetic, no FP64 conversions on the common
-// path), and the increment is added into the pair with an error-free
-// two-sum, so the iterate accumulates no FP32 rounding over the iterations
-// (FP64<->FP32 conversions run on GB300's FP64 pipe, which made an FP64
-// iterate cost as much as FP64 arithmetic).  IN64: the input is the FP64
-// phi3 (first iteration); OUT64: the output is the FP64 state (last).
+// takes its differences from the pairs (FP32 arithmetic, no FP64
+// instruction on the common path), and the increment is added into the pair
+// with an error-free two-sum, so the iterate accumulates no FP32 rounding
+// over the iterations (FP64<->FP32 conversions run on GB300's FP64 pipe,
+// which made an FP64 iterate cost as much as FP64 arithmetic).  IN64: the
+// input is the FP64 phi3 (first iteration), split by integer operations;
+// OUT64: the output is the FP64 state (last).
 struct FF {
   float hi, lo;
 };
@@ -241,9 +243,37 @@ template <bool IN64>
 struct FFSrc {
   const double *x64;
   const float *hi, *lo;
-  __device__ __forceinline__ float operator[](int q) const { return IN64 ? (float)x64[q] : hi[q]; }
+  // the stencil value as a pair: split by integer operations from the FP64
+  // phi3 on the first iteration, the stored pair afterwards
+  __device__ __forceinline__ F2 pair(int q) const {
+    if (IN64) return split_bits(x64[q]);
+    return F2{hi[q], lo[q]};
+  }
   __device__ __forceinline__ double exact(int q) const { return IN64 ? x64[q] : (double)hi[q] + (double)lo[q]; }
 };
+
+// rs_dc on pairs: the one-sided differences of the Godunov gradient are
+// taken from the pairs ((hi_a - hi_b) + (lo_a - lo_b)), so they carry FP32
+// precision relative to the difference, not to |phi|; the rest is FP32.
+template <bool IN64>
+__device__ __forceinline__ float rs_dc_pair(const Geo &g, float h, const FFSrc<IN64> &src, F2 p,
+                                            const float *__restrict__ D, int f, int c) {
+  const float sg = (float)(((f >> 1) & 3) - 1);
+  if (f & 1) return sg * fabsf(val(p)) - D[c];
+  if (sg > 0.0f) {  // max(p - min(p[i-1], p[i+1]), 0), likewise y, z (see rs_dc)
+    const float ax = fmaxf(dif(p, pmin(src.pair(c - 1), src.pair(c + 1))), 0.0f);
+    const float ay = fmaxf(dif(p, pmin(src.pair(c - g.sy), src.pair(c + g.sy))), 0.0f);
+    const float az = fmaxf(dif(p, pmin(src.pair(c - g.sz), src.pair(c + g.sz))), 0.0f);
+    return sg * (sqrtf(ax * ax + ay * ay + az * az) - h);
+  }
+  if (sg < 0.0f) {
+    const float ax = fmaxf(dif(pmax(src.pair(c - 1), src.pair(c + 1)), p), 0.0f);
+    const float ay = fmaxf(dif(pmax(src.pair(c - g.sy), src.pair(c + g.sy)), p), 0.0f);
+    const float az = fmaxf(dif(pmax(src.pair(c - g.sz), src.pair(c + g.sz)), p), 0.0f);
+    return sg * (sqrtf(ax * ax + az * az + ay * ay) - h);
+  }
+  return 0.0f;
+}
 
 // inlet row (levelset.f90:168-177), FP64, out of line (see below)
 __device__ __noinline__ FF ff_inlet(float h, double height, int k) {
@@ -256,10 +286,9 @@ __device__ __forceinline__ FF ff_val(const Geo &g, const Phys &ph, float h, floa
   if (i == 0) return ff_inlet(h, ph.height, k);
   if (i == g.nx + 1) i = g.nx;
   const int c = TPLS_IDX(g, i, j, k);
-  const float p = src[c];
-  const float inc = ktau * rs_dc<float>(g, h, src, p, D, flags[c], c);
-  if (IN64) return ff_split(src.x64[c] - (double)inc);
-  return two_sum(src.hi[c], src.lo[c] - inc);
+  const F2 p = src.pair(c);
+  const float inc = ktau * rs_dc_pair<IN64>(g, h, src, p, D, flags[c], c);
+  return two_sum(p.h, p.l - inc);
 }
 
 // The FP64 paths of the float-pair iteration (the extrapolated ghost planes,

@@ -20,52 +20,9 @@
 // ghost row written in the same half-sweep); for odd ny the caller runs a
 // separate exchange after each half-sweep instead.
 #include "tpls_sweep.cuh"
+#include "tpls_pair.cuh"
 
 namespace tpls {
-
-template <typename T>
-struct FcT {
-  T px, mx, py, my, pz, mz;
-};
-using Fc = FcT<double>;
-
-
-// face viscosities, momentum_allflux.f90:91-98 (u), :145-152 (v), :187-194 (w)
-template <typename T>
-__device__ __forceinline__ FcT<T> faces(int comp, const Geo &g, const T *__restrict__ mu, int i, int j,
-                                        int k) {
-  const int sy = g.sy, sz = g.szm;
-  FcT<T> f;
-  if (comp == 0) {
-    const T *m = mu + TPLS_IDXM(g, i, j + 1, k + 1);
-    const T a = m[0], b = m[1];
-    f.px = b;
-    f.mx = a;
-    f.py = (a + b + m[sy] + m[1 + sy]) * (T)0.25;
-    f.my = (a + b + m[-sy] + m[1 - sy]) * (T)0.25;
-    f.pz = (a + b + m[sz] + m[1 + sz]) * (T)0.25;
-    f.mz = (a + b + m[-sz] + m[1 - sz]) * (T)0.25;
-  } else if (comp == 1) {
-    const T *m = mu + TPLS_IDXM(g, i, j + 1, k + 1);
-    const T a = m[0], b = m[-sy];
-    f.px = (a + b + m[1] + m[1 - sy]) * (T)0.25;
-    f.mx = (a + b + m[-1] + m[-1 - sy]) * (T)0.25;
-    f.py = a;
-    f.my = b;
-    f.pz = (a + b + m[sz] + m[sz - sy]) * (T)0.25;
-    f.mz = (a + b + m[-sz] + m[-sz - sy]) * (T)0.25;
-  } else {
-    const T *m = mu + TPLS_IDXM(g, i, j + 1, k);
-    const T a = m[0], b = m[sz];
-    f.px = (a + b + m[1] + m[1 + sz]) * (T)0.25;
-    f.mx = (a + b + m[-1] + m[-1 + sz]) * (T)0.25;
-    f.py = (a + b + m[sy] + m[sy + sz]) * (T)0.25;
-    f.my = (a + b + m[-sy] + m[-sy + sz]) * (T)0.25;
-    f.pz = b;
-    f.mz = a;
-  }
-  return f;
-}
 
 // jacobi_iteration_allflux.f90:84-90 (same form in every Jacobi/SOR routine)
 __device__ __forceinline__ double helm(const Fc &f, const Helm &h, double xp, double xm,
@@ -236,7 +193,8 @@ __device__ __forceinline__ void write_coef(int comp, const Geo &g, const Helm &h
   } else {
     b = (TR)((T)rhs * r);
   }
-  store_rec<TR>(rec, cxp, cxm, cyp, cym, tzp, tzm, b);
+  if constexpr (sizeof(TR) == sizeof(float)) rec[0] = b;  // FP32 sweeps recompute the coefficients
+  else store_rec<TR>(rec, cxp, cxm, cyp, cym, tzp, tzm, b);
 }
 
 // X64 is the component's FP64 state (u2, v2 or w2): the right-hand side is
@@ -278,7 +236,8 @@ __global__ void __launch_bounds__(MB_X *MB_Y)
   if (rhs) rhs[c] = r;
   if (diff_out) diff_out[c] = diff;
   if (coef && valid)
-    write_coef<T, TR>(comp, g, hm, f, r, k, defect ? X64 : nullptr, c, coef + 8 * (size_t)rec_slot(g, c, i));
+    write_coef<T, TR>(comp, g, hm, f, r, k, defect ? X64 : nullptr, c,
+                      coef + (sizeof(TR) == sizeof(float) ? 1 : 8) * (size_t)rec_slot(g, c, i));
 }
 
 template <typename T, typename TR = T>
@@ -310,17 +269,181 @@ cudaError_t launch_mom_rhs(int comp, const Geo &g, const Phys &ph,
 cudaError_t launch_mom_rhs64r32(int comp, const Geo &g, const Phys &ph, const double *u2, const double *v2,
                                 const double *w2, const double *mu, const double *fcsf, const double *c1,
                                 const double *c0, const double *s1, const double *s0, double *conv2,
-                                double *csf2, float *coef, cudaStream_t st) {
+                                double *csf2, float *bdef, cudaStream_t st) {
   const double *x64 = (comp == 0) ? u2 : (comp == 1) ? v2 : w2;
   return mom_rhs<double, float>(comp, g, ph, u2, v2, w2, x64, mu, fcsf, c1, c0, s1, s0, conv2, csf2, nullptr,
-                                nullptr, coef, st);
+                                nullptr, bdef, st);
 }
-cudaError_t launch_mom_rhs32(int comp, const Geo &g, const Phys &ph, const float *u2, const float *v2,
-                             const float *w2, const double *x64, const float *mu, const float *fcsf,
-                             const double *c1, const double *c0, const double *s1, const double *s0,
-                             double *conv2, double *csf2, float *coef, cudaStream_t st) {
-  return mom_rhs<float>(comp, g, ph, u2, v2, w2, x64, mu, fcsf, c1, c0, s1, s0, conv2, csf2, nullptr, nullptr,
-                        coef, st);
+// ---------------------------------------------------------------------------
+// FP32 momentum stencils of the FP32-mixed form on the FP64 velocity state.
+//
+// Each FP64 value is split by integer operations into an FP32 pair
+// (hi = the value truncated to 24 significant bits, lo = the FP32 rounding
+// of the remainder), so no FP64 instruction is issued: on GB300 FP64
+// arithmetic and FP64<->FP32 conversions share a pipe 64x slower than FP32.
+// Neighbour differences are formed as (hi_a - hi_b) + (lo_a - lo_b), which
+// carries the FP32 precision of the difference itself instead of that of
+// the O(|u|) values: the stencils' cancellations (first and second
+// differences of a smooth field) then cost 1e-7 of the difference, not of
+// |u|.  Sums and products use the pair rounded to FP32.
+__device__ __forceinline__ F2 ld2(const double *__restrict__ p) { return split_bits(__ldg(p)); }
+
+// float constants of one step (computed on the host in FP64, then rounded)
+struct MomF {
+  float rdx, rdy, rdz, dt, ax2, ay2, az2;
+};
+
+// get_conv_all / get_diffusion_all point forms (momentum_allflux.f90:22-471)
+// on split values; the same operations as conv_diff with every difference
+// of two velocity values taken from the pairs.  At the walls (u, v: k = 0
+// and nz-1) the ghost value -2 x + x(k+-1)/3 enters as the difference
+// x(k+-1)/3 - 3 x.
+__device__ __forceinline__ CDT<float> conv_diff_pair(int comp, const Geo &g, const MomF &m,
+                                                     const double *__restrict__ U, const double *__restrict__ V,
+                                                     const double *__restrict__ W, const FcT<float> &f, int i,
+                                                     int j, int k) {
+  const int sy = g.sy, sz = g.sz, nzu = g.nz;
+  const int c = TPLS_IDX(g, i, j, k);
+  const float h = 0.5f, third = (float)(1.0 / 3.0), rdx = m.rdx, rdy = m.rdy, rdz = m.rdz;
+  CDT<float> r;
+  if (comp == 0 || comp == 1) {
+    const double *S = comp == 0 ? U : V;
+    const F2 x = ld2(S + c), xe = ld2(S + c + 1), xw = ld2(S + c - 1), xn = ld2(S + c + sy), xs = ld2(S + c - sy);
+    float dT, dB, dzc;  // x(k+1) - x, x - x(k-1) (ghosts at the walls), centred z difference term
+    if (k == 0) {
+      const F2 xt = ld2(S + c + sz);
+      dT = dif(xt, x);
+      dB = (3.0f * x.h - xt.h * third) + (3.0f * x.l - xt.l * third);
+      dzc = (val(x) + val(xt)) * (h * rdz);
+    } else if (k == nzu - 1) {
+      const F2 xb = ld2(S + c - sz);
+      dB = dif(x, xb);
+      dT = (xb.h * third - 3.0f * x.h) + (xb.l * third - 3.0f * x.l);
+      dzc = -(val(x) + val(xb)) * (h * rdz);
+    } else {
+      const F2 xt = ld2(S + c + sz), xb = ld2(S + c - sz);
+      dT = dif(xt, x);
+      dB = dif(x, xb);
+      dzc = h * dif(xt, xb) * rdz;
+    }
+    const float dE = dif(xe, x), dW = dif(x, xw), dN = dif(xn, x), dS = dif(x, xs);
+    float t1, E, Wt, N, Sf, O, I;
+    if (comp == 0) {
+      const F2 v0 = ld2(V + c), v1 = ld2(V + c + 1), v2 = ld2(V + c + sy), v3 = ld2(V + c + 1 + sy);
+      const F2 w0 = ld2(W + c), w1 = ld2(W + c + 1), w2 = ld2(W + c + sz), w3 = ld2(W + c + 1 + sz);
+      const float tempv = (val(v0) + val(v1) + val(v2) + val(v3)) * 0.25f;
+      const float tempw = (val(w0) + val(w1) + val(w2) + val(w3)) * 0.25f;
+      const float Xc = h * dif(xe, xw) * rdx * val(x);
+      const float Yc = h * dif(xn, xs) * rdy * tempv;
+      t1 = Xc + Yc + dzc * tempw;
+      E = f.px * dE * rdx;
+      Wt = f.mx * dW * rdx;
+      N = f.py * dif(v3, v2) * rdx;
+      Sf = f.my * dif(v1, v0) * rdx;
+      O = f.pz * dif(w3, w2) * rdx;
+      I = f.mz * dif(w1, w0) * rdx;
+    } else {
+      const F2 u0 = ld2(U + c - 1 - sy), u1 = ld2(U + c - 1), u2 = ld2(U + c - sy), u3 = ld2(U + c);
+      const F2 w0 = ld2(W + c - sy), w1 = ld2(W + c), w2 = ld2(W + c - sy + sz), w3 = ld2(W + c + sz);
+      const float tempu = (val(u0) + val(u1) + val(u2) + val(u3)) * 0.25f;
+      const float tempw = (val(w0) + val(w1) + val(w2) + val(w3)) * 0.25f;
+      const float Yc = h * dif(xn, xs) * rdy * val(x);
+      const float Xc = h * dif(xe, xw) * rdx * tempu;
+      t1 = Xc + Yc + dzc * tempw;
+      E = f.px * dif(u3, u2) * rdy;
+      Wt = f.mx * dif(u1, u0) * rdy;
+      N = f.py * dN * rdy;
+      Sf = f.my * dS * rdy;
+      O = f.pz * dif(w3, w2) * rdy;
+      I = f.mz * dif(w1, w0) * rdy;
+    }
+    r.conv = t1 - ((E - Wt) * rdx + (N - Sf) * rdy + (O - I) * rdz);
+    r.diff = (f.px * dE - f.mx * dW) * (rdx * rdx) + (f.py * dN - f.my * dS) * (rdy * rdy) +
+             (f.pz * dT - f.mz * dB) * (rdz * rdz);
+  } else {
+    const F2 x = ld2(W + c), xe = ld2(W + c + 1), xw = ld2(W + c - 1), xn = ld2(W + c + sy), xs = ld2(W + c - sy);
+    const F2 xt = ld2(W + c + sz), xb = ld2(W + c - sz);
+    const F2 u0 = ld2(U + c - 1 - sz), u1 = ld2(U + c - 1), u2 = ld2(U + c - sz), u3 = ld2(U + c);
+    const F2 v0 = ld2(V + c - sz), v1 = ld2(V + c), v2 = ld2(V + c + sy - sz), v3 = ld2(V + c + sy);
+    const float tempu = (val(u0) + val(u1) + val(u2) + val(u3)) * 0.25f;
+    const float tempv = (val(v0) + val(v1) + val(v2) + val(v3)) * 0.25f;
+    const float Zc = h * dif(xt, xb) * rdz * val(x);
+    const float Xc = h * dif(xe, xw) * rdx * tempu;
+    const float Yc = h * dif(xn, xs) * rdy * tempv;
+    const float t1 = Xc + Yc + Zc;
+    const float dE = dif(xe, x), dW = dif(x, xw), dN = dif(xn, x), dS = dif(x, xs);
+    const float dT = dif(xt, x), dB = dif(x, xb);
+    const float E = f.px * dif(u3, u2) * rdz, Wt = f.mx * dif(u1, u0) * rdz;
+    const float N = f.py * dif(v3, v2) * rdz, Sf = f.my * dif(v1, v0) * rdz;
+    const float O = f.pz * dT * rdz, I = f.mz * dB * rdz;
+    r.conv = t1 - ((E - Wt) * rdx + (N - Sf) * rdy + (O - I) * rdz);
+    r.diff = (f.px * dE - f.mx * dW) * (rdx * rdx) + (f.py * dN - f.my * dS) * (rdy * rdy) +
+             (f.pz * dT - f.mz * dB) * (rdz * rdz);
+  }
+  return r;
+}
+
+// Right-hand side of the FP32-mixed form's sweeps, with no FP64 arithmetic.
+// The sweeps solve for the defect d = x - X (X the FP64 state of the
+// component): with diag x - sum(a_n x_n) = rhs and diag = 1 + sum(a_n), the
+// defect equation's right-hand side is
+//   R = (rhs - X) + sum(a_n (X_n - X)) = dt (diff - AB3(conv) + AB3(csf)),
+// because sum(a_n (X_n - X)) = (dt/2) diff for the same ghost-substituted
+// neighbours (main_ns_hybrid.F90:743-751 for rhs).  R is a small quantity,
+// so its FP32 rounding acts on the step's increment, not on |u|.  Stored:
+// b = R / diag, one float per point in record-slot order (the sweeps
+// recompute the coefficients from mu).  The AB3 histories are read and
+// written as FP64 arrays holding FP32 values.
+__global__ void __launch_bounds__(MB_X *MB_Y)
+    k_mom_rhs_pair(int comp, Geo g, MomF m, const double *__restrict__ U, const double *__restrict__ V,
+                   const double *__restrict__ W, const float *__restrict__ mu, const float *__restrict__ fc,
+                   const double *__restrict__ c1, const double *__restrict__ c0, const double *__restrict__ s1,
+                   const double *__restrict__ s0, double *__restrict__ conv2, double *__restrict__ csf2,
+                   float *__restrict__ bdef) {
+  const int i = blockIdx.x * MB_X + threadIdx.x + 1, j = blockIdx.y * MB_Y + threadIdx.y + 1;
+  const int k = blockIdx.z;
+  if (i > g.nx || j > g.ny) return;
+  const int c = TPLS_IDX(g, i, j, k);
+  CDT<float> cd = {0.0f, 0.0f};
+  const bool valid = cd_valid(comp, g, i, k);
+  FcT<float> f;
+  if (valid) {
+    f = faces<float>(comp, g, mu, i, j, k);
+    cd = conv_diff_pair(comp, g, m, U, V, W, f, i, j, k);
+  }
+  // main_ns_hybrid.F90:629-641 face averages of the CSF force
+  float s2;
+  if (comp == 0) s2 = (fc[TPLS_IDX(g, i + 1, j + 1, k + 1)] + fc[TPLS_IDX(g, i, j + 1, k + 1)]) * 0.5f;
+  else if (comp == 1) s2 = (fc[TPLS_IDX(g, i, j + 1, k + 1)] + fc[TPLS_IDX(g, i, j, k + 1)]) * 0.5f;
+  else s2 = (fc[TPLS_IDX(g, i, j + 1, k + 1)] + fc[TPLS_IDX(g, i, j + 1, k)]) * 0.5f;
+  const float a23 = (float)(23.0 / 12.0), a43 = (float)(4.0 / 3.0), a512 = (float)(5.0 / 12.0);
+  const float abc = a23 * cd.conv - a43 * round_bits(c1[c]) + a512 * round_bits(c0[c]);
+  const float abs_ = a23 * s2 - a43 * round_bits(s1[c]) + a512 * round_bits(s0[c]);
+  conv2[c] = widen_bits(cd.conv);
+  csf2[c] = widen_bits(s2);
+  if (!valid) return;
+  const float diag = 1.0f + m.ax2 * (f.px + f.mx) + m.ay2 * (f.py + f.my) + m.az2 * (f.pz + f.mz);
+  bdef[rec_slot(g, c, i)] = m.dt * (cd.diff - abc + abs_) / diag;
+}
+
+cudaError_t launch_mom_rhs_pair(int comp, const Geo &g, const Phys &ph, const double *u2, const double *v2,
+                                const double *w2, const float *mu, const float *fcsf, const double *c1,
+                                const double *c0, const double *s1, const double *s0, double *conv2,
+                                double *csf2, float *bdef, cudaStream_t st) {
+  const Helm hm = helm_of(ph);
+  MomF m;
+  m.rdx = (float)(1.0 / ph.dx);
+  m.rdy = (float)(1.0 / ph.dy);
+  m.rdz = (float)(1.0 / ph.dz);
+  m.dt = (float)ph.dt;
+  m.ax2 = (float)hm.ax2;
+  m.ay2 = (float)hm.ay2;
+  m.az2 = (float)hm.az2;
+  const int nk = (comp == 2) ? g.nz + 1 : g.nz;
+  dim3 grd((g.nx + MB_X - 1) / MB_X, (g.ny + MB_Y - 1) / MB_Y, nk);
+  k_mom_rhs_pair<<<grd, dim3(MB_X, MB_Y), 0, st>>>(comp, g, m, u2, v2, w2, mu, fcsf, c1, c0, s1, s0, conv2, csf2,
+                                                   bdef);
+  return cudaGetLastError();
 }
 
 // standalone get_conv_all / get_diffusion_all: out = conv or diff on the

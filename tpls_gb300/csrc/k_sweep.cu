@@ -8,9 +8,13 @@
 // by the Helmholtz diagonal (see write_coef in k_momentum.cu).  A sweep
 // point is then x_new = sum(c_n x_n) + b: seven FMAs instead of the face
 // averages, diagonal and division of the reference's form, evaluated once
-// per step instead of once per sweep.  Templated on the storage/arithmetic
-// type: double for the FP64 form, float for the FP32-mixed form (records
-// of 8 floats, velocity in FP32 during the sweeps).
+// per step instead of once per sweep: on GB300's FP64 pipe the 64-byte
+// record is the cheaper side of that trade.  The FP32 sweeps of the
+// FP32-mixed form take the other side: FP32 arithmetic is 64x faster, so
+// they recompute the coefficients per point from the FP32 viscosity and read
+// only b (4 bytes), cutting a Jacobi point from ~40 to ~16 bytes of traffic.
+// Templated on the arithmetic type and the coefficient source (records, or
+// MuCoef).
 #include "tpls_sweep.cuh"
 
 namespace tpls {
@@ -55,17 +59,46 @@ __device__ __forceinline__ T rec_apply(const Rec<T> &q, T xp, T xm, T yp, T ym, 
   return fma(q.zm, zm, v);
 }
 
+// Coefficients of point (i, j, k): the FP64 form reads its record; the FP32
+// sweeps recompute the six coefficients from the FP32 viscosity exactly as
+// the right-hand side kernels do (face averages, diagonal, wall rule folded
+// into the z slots for u and v) and read b alone.
+__device__ __forceinline__ Rec<double> get_rec(int, const Geo &g, const double *__restrict__ coef, int c, int i,
+                                               int, int, bool stream) {
+  return load_rec(coef, rec_slot(g, c, i), stream);
+}
+__device__ __forceinline__ Rec<float> get_rec(int comp, const Geo &g, const MuCoef &s, int c, int i, int j, int k,
+                                              bool stream) {
+  const FcT<float> f = faces<float>(comp, g, s.mu, i, j, k);
+  const float diag = 1.0f + s.ax2 * (f.px + f.mx) + s.ay2 * (f.py + f.my) + s.az2 * (f.pz + f.mz);
+  const float r = 1.0f / diag;
+  float czp = s.az2 * f.pz * r, czm = s.az2 * f.mz * r;
+  if (comp != 2) {
+    if (k == 0) {
+      czp += czm * (float)(1.0 / 3.0);
+      czm = -2.0f * czm;
+    } else if (k == g.nz - 1) {
+      czm += czp * (float)(1.0 / 3.0);
+      czp = -2.0f * czp;
+    }
+  }
+  const float *bp = s.b + rec_slot(g, c, i);
+  Rec<float> q = {s.ax2 * f.px * r, s.ax2 * f.mx * r, s.ay2 * f.py * r, s.ay2 * f.my * r, czp, czm,
+                  stream ? __ldcs(bp) : __ldg(bp)};
+  return q;
+}
+
 // Jacobi: x = J(xo) on the component's interior with its boundary rows.
-template <typename T, int SW_X, int SW_Y>
+template <typename T, typename CS, int SW_X, int SW_Y>
 __global__ void __launch_bounds__(SW_X *SW_Y)
-    k_jacobi_c(int comp, Geo g, Helm h, const T *__restrict__ xo, const T *__restrict__ coef,
+    k_jacobi_c(int comp, Geo g, Helm h, const T *__restrict__ xo, const CS coef,
                const double *__restrict__ P, const double *__restrict__ X, T *__restrict__ x, int fuse) {
   const int i = blockIdx.x * SW_X + threadIdx.x + 1, j = blockIdx.y * SW_Y + threadIdx.y + 1;
   const int k = blockIdx.z + (comp == 2 ? 1 : 0);
   const int iend = (comp == 0) ? g.nx - 1 : g.nx;
   if (i > iend || j > g.ny) return;
   const int c = TPLS_IDX(g, i, j, k), sy = g.sy, sz = g.sz;
-  const Rec<T> q = load_rec(coef, rec_slot(g, c, i), false);
+  const Rec<T> q = get_rec(comp, g, coef, c, i, j, k, false);
   const T xc = xo[c];
   T zp, zm;
   if (comp == 2) {
@@ -108,9 +141,9 @@ __global__ void __launch_bounds__(SW_X *SW_Y)
 
 // 3-D checkerboard half-sweep (even iteration_time), one thread per point
 // of the colour.
-template <typename T, int SW_X, int SW_Y>
+template <typename T, typename CS, int SW_X, int SW_Y>
 __global__ void __launch_bounds__(SW_X *SW_Y)
-    k_sor_even_c(int comp, Geo g, Helm h, T *__restrict__ x, const T *__restrict__ coef,
+    k_sor_even_c(int comp, Geo g, Helm h, T *__restrict__ x, const CS coef,
                  const double *__restrict__ P, const double *__restrict__ X, int flg, int bc, int fuse) {
   const int i2 = blockIdx.x * SW_X + threadIdx.x, j = blockIdx.y * SW_Y + threadIdx.y + 1;
   const int k = blockIdx.z + (comp == 2 ? 1 : 0);
@@ -120,7 +153,7 @@ __global__ void __launch_bounds__(SW_X *SW_Y)
   T v = 0;
   if (i <= iend) {
     const int c = TPLS_IDX(g, i, j, k), sy = g.sy, sz = g.sz;
-    const Rec<T> q = load_rec(coef, rec_slot(g, c, i), false);
+    const Rec<T> q = get_rec(comp, g, coef, c, i, j, k, false);
     const T xc = x[c];
     T zp, zm;
     if (comp == 2) {
@@ -150,9 +183,9 @@ __global__ void __launch_bounds__(SW_X *SW_Y)
 // x field stays resident in L2.
 constexpr int SO_KZ = 32, SO_T = 256;
 
-template <typename T>
+template <typename T, typename CS>
 __device__ __forceinline__ void sor_odd_produce(int comp, const Geo &g, const T *__restrict__ x,
-                                                const T *__restrict__ coef, int j, int par, int npair,
+                                                const CS coef, int j, int par, int npair,
                                                 int iend, int k0, int kc, int kn, T (*sA)[32],
                                                 T (*sB)[32], int t0, int nthr) {
   const int sy = g.sy, sz = g.sz, nz = g.nz;
@@ -162,7 +195,7 @@ __device__ __forceinline__ void sor_odd_produce(int comp, const Geo &g, const T 
     T A = 0, B = 0;
     if (i2 < npair && i <= iend) {
       const int c = TPLS_IDX(g, i, j, k);
-      const Rec<T> q = load_rec(coef, rec_slot(g, c, i), true);
+      const Rec<T> q = get_rec(comp, g, coef, c, i, j, k, true);
       const T xc = x[c];
       T zp;
       if (comp == 2) zp = x[c + sz];
@@ -185,9 +218,9 @@ __device__ __forceinline__ void sor_odd_produce(int comp, const Geo &g, const T 
   }
 }
 
-template <typename T>
+template <typename T, typename CS>
 __global__ void __launch_bounds__(SO_T)
-    k_sor_odd_c2(int comp, Geo g, Helm h, T *__restrict__ x, const T *__restrict__ coef,
+    k_sor_odd_c2(int comp, Geo g, Helm h, T *__restrict__ x, const CS coef,
                  const double *__restrict__ P, const double *__restrict__ X, int flg, int bc, int fuse) {
   __shared__ T sA[2][SO_KZ][32], sB[2][SO_KZ][32];
   const int j = blockIdx.y + 1;
@@ -240,9 +273,9 @@ __global__ void __launch_bounds__(SO_T)
 // the result differs from the level-by-level order only by rounding (P
 // decays like (1.2 czm)^m, so x_in's contribution is weighted by it).
 // Shared memory: 2 (nlev + W) 32 values of T; W = 8 or 16 warps.
-template <typename T, int SO3_W>
+template <typename T, typename CS, int SO3_W>
 __global__ void __launch_bounds__(SO3_W * 32)
-    k_sor_odd_c3(int comp, Geo g, Helm h, T *__restrict__ x, const T *__restrict__ coef,
+    k_sor_odd_c3(int comp, Geo g, Helm h, T *__restrict__ x, const CS coef,
                  const double *__restrict__ P, const double *__restrict__ X, int flg, int bc, int fuse) {
   extern __shared__ __align__(16) unsigned char so3_raw[];
   const int j = blockIdx.y + 1;
@@ -266,7 +299,7 @@ __global__ void __launch_bounds__(SO3_W * 32)
 #pragma unroll 2
     for (int k = kb; k < ke; k++) {
       const int c = TPLS_IDX(g, i, j, k);
-      const Rec<T> q = load_rec(coef, rec_slot(g, c, i), true);
+      const Rec<T> q = get_rec(comp, g, coef, c, i, j, k, true);
       const T xc = x[c];
       T zp;
       if (comp == 2) zp = x[c + sz];
@@ -317,50 +350,50 @@ constexpr size_t SO3_SMEM_MAX = 200 * 1024;
 
 cudaError_t sweep_init() {
   const int m = (int)SO3_SMEM_MAX;
-  cudaError_t e = cudaFuncSetAttribute(k_sor_odd_c3<double, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+  cudaError_t e = cudaFuncSetAttribute(k_sor_odd_c3<double, const double *, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_sor_odd_c3<double, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    e = cudaFuncSetAttribute(k_sor_odd_c3<double, const double *, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_sor_odd_c3<float, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    e = cudaFuncSetAttribute(k_sor_odd_c3<float, MuCoef, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_sor_odd_c3<float, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    e = cudaFuncSetAttribute(k_sor_odd_c3<float, MuCoef, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
   return e;
 }
 
-template <typename T, int BX, int BY>
-static void jacobi_v(int comp, const Geo &g, const Helm &h, const T *xo, const T *coef, const double *pres,
+template <typename T, typename CS, int BX, int BY>
+static void jacobi_v(int comp, const Geo &g, const Helm &h, const T *xo, CS coef, const double *pres,
                      const double *X, T *x, int fuse, cudaStream_t st) {
   const int nk = (comp == 2) ? g.nz - 1 : g.nz;
   const int iend = (comp == 0) ? g.nx - 1 : g.nx;
   dim3 grd((iend + BX - 1) / BX, (g.ny + BY - 1) / BY, nk);
-  k_jacobi_c<T, BX, BY><<<grd, dim3(BX, BY), 0, st>>>(comp, g, h, xo, coef, pres, X, x, fuse);
+  k_jacobi_c<T, CS, BX, BY><<<grd, dim3(BX, BY), 0, st>>>(comp, g, h, xo, coef, pres, X, x, fuse);
 }
 
-template <typename T>
-static cudaError_t jacobi_c(int comp, const Geo &g, const Phys &ph, const T *xo, const T *coef,
-                            const double *pres, const double *X, T *x, int fuse, int tile, cudaStream_t st) {
+template <typename T, typename CS>
+static cudaError_t jacobi_c(int comp, const Geo &g, const Phys &ph, const T *xo, CS coef, const double *pres,
+                            const double *X, T *x, int fuse, int tile, cudaStream_t st) {
   const Helm h = helm_of(ph);
   switch (tile) {
-    case 1: jacobi_v<T, 32, 8>(comp, g, h, xo, coef, pres, X, x, fuse, st); break;
-    case 2: jacobi_v<T, 64, 4>(comp, g, h, xo, coef, pres, X, x, fuse, st); break;
-    case 3: jacobi_v<T, 16, 8>(comp, g, h, xo, coef, pres, X, x, fuse, st); break;
-    default: jacobi_v<T, 32, 4>(comp, g, h, xo, coef, pres, X, x, fuse, st); break;
+    case 1: jacobi_v<T, CS, 32, 8>(comp, g, h, xo, coef, pres, X, x, fuse, st); break;
+    case 2: jacobi_v<T, CS, 64, 4>(comp, g, h, xo, coef, pres, X, x, fuse, st); break;
+    case 3: jacobi_v<T, CS, 16, 8>(comp, g, h, xo, coef, pres, X, x, fuse, st); break;
+    default: jacobi_v<T, CS, 32, 4>(comp, g, h, xo, coef, pres, X, x, fuse, st); break;
   }
   return cudaGetLastError();
 }
 
-template <typename T, int BX, int BY>
-static void even_v(int comp, const Geo &g, const Helm &h, T *x, const T *coef, const double *pres,
-                   const double *X, int flg, int bc, int fuse, cudaStream_t st) {
+template <typename T, typename CS, int BX, int BY>
+static void even_v(int comp, const Geo &g, const Helm &h, T *x, CS coef, const double *pres, const double *X,
+                   int flg, int bc, int fuse, cudaStream_t st) {
   const int iend = (comp == 0) ? g.nx - 1 : g.nx;
   const int npairs = (iend + 1) / 2;
   const int nk = (comp == 2) ? g.nz - 1 : g.nz;
   dim3 grd((npairs + BX - 1) / BX, (g.ny + BY - 1) / BY, nk);
-  k_sor_even_c<T, BX, BY><<<grd, dim3(BX, BY), 0, st>>>(comp, g, h, x, coef, pres, X, flg, bc, fuse);
+  k_sor_even_c<T, CS, BX, BY><<<grd, dim3(BX, BY), 0, st>>>(comp, g, h, x, coef, pres, X, flg, bc, fuse);
 }
 
-template <typename T>
-static cudaError_t sor_c(int comp, const Geo &g, const Phys &ph, T *x, const T *coef, const double *pres,
+template <typename T, typename CS>
+static cudaError_t sor_c(int comp, const Geo &g, const Phys &ph, T *x, CS coef, const double *pres,
                          const double *X, int flg, int iteration_time, int bc, int fuse, int tile_even,
                          int tile_odd, cudaStream_t st) {
   const int iend = (comp == 0) ? g.nx - 1 : g.nx;
@@ -368,10 +401,10 @@ static cudaError_t sor_c(int comp, const Geo &g, const Phys &ph, T *x, const T *
   const Helm h = helm_of(ph);
   if (iteration_time % 2 == 0) {
     switch (tile_even) {
-      case 1: even_v<T, 32, 8>(comp, g, h, x, coef, pres, X, flg, bc, fuse, st); break;
-      case 2: even_v<T, 64, 4>(comp, g, h, x, coef, pres, X, flg, bc, fuse, st); break;
-      case 3: even_v<T, 16, 8>(comp, g, h, x, coef, pres, X, flg, bc, fuse, st); break;
-      default: even_v<T, 32, 4>(comp, g, h, x, coef, pres, X, flg, bc, fuse, st); break;
+      case 1: even_v<T, CS, 32, 8>(comp, g, h, x, coef, pres, X, flg, bc, fuse, st); break;
+      case 2: even_v<T, CS, 64, 4>(comp, g, h, x, coef, pres, X, flg, bc, fuse, st); break;
+      case 3: even_v<T, CS, 16, 8>(comp, g, h, x, coef, pres, X, flg, bc, fuse, st); break;
+      default: even_v<T, CS, 32, 4>(comp, g, h, x, coef, pres, X, flg, bc, fuse, st); break;
     }
   } else {
     dim3 grd((npairs + 31) / 32, g.ny, 1);
@@ -380,20 +413,31 @@ static cudaError_t sor_c(int comp, const Geo &g, const Phys &ph, T *x, const T *
     const int w = (tile_odd == 1) ? 8 : ((tile_odd == 2) ? 16 : ((g.nz >= 128) ? 16 : 8));
     const size_t sm = so3_smem<T>(g, comp, w);
     if (sm <= SO3_SMEM_MAX && w == 16)
-      k_sor_odd_c3<T, 16><<<grd, 16 * 32, sm, st>>>(comp, g, h, x, coef, pres, X, flg, bc, fuse);
+      k_sor_odd_c3<T, CS, 16><<<grd, 16 * 32, sm, st>>>(comp, g, h, x, coef, pres, X, flg, bc, fuse);
     else if (sm <= SO3_SMEM_MAX)
-      k_sor_odd_c3<T, 8><<<grd, 8 * 32, sm, st>>>(comp, g, h, x, coef, pres, X, flg, bc, fuse);
+      k_sor_odd_c3<T, CS, 8><<<grd, 8 * 32, sm, st>>>(comp, g, h, x, coef, pres, X, flg, bc, fuse);
     else
-      k_sor_odd_c2<T><<<grd, SO_T, 0, st>>>(comp, g, h, x, coef, pres, X, flg, bc, fuse);
+      k_sor_odd_c2<T, CS><<<grd, SO_T, 0, st>>>(comp, g, h, x, coef, pres, X, flg, bc, fuse);
   }
   return cudaGetLastError();
+}
+
+MuCoef mu_coef(const Phys &ph, const float *mu, const float *b) {
+  const Helm h = helm_of(ph);
+  MuCoef m;
+  m.mu = mu;
+  m.b = b;
+  m.ax2 = (float)h.ax2;
+  m.ay2 = (float)h.ay2;
+  m.az2 = (float)h.az2;
+  return m;
 }
 
 cudaError_t launch_jacobi_c(int comp, const Geo &g, const Phys &ph, const double *xo, const double *coef,
                             const double *pres, double *x, int fuse, cudaStream_t st, const SweepTiles &t) {
   return jacobi_c(comp, g, ph, xo, coef, pres, nullptr, x, fuse, t.jac, st);
 }
-cudaError_t launch_jacobi_c(int comp, const Geo &g, const Phys &ph, const float *xo, const float *coef,
+cudaError_t launch_jacobi_c(int comp, const Geo &g, const Phys &ph, const float *xo, const MuCoef &coef,
                             const double *pres, const double *X, float *x, int fuse, cudaStream_t st,
                             const SweepTiles &t) {
   return jacobi_c(comp, g, ph, xo, coef, pres, X, x, fuse, t.jac, st);
@@ -403,7 +447,7 @@ cudaError_t launch_sor_c(int comp, const Geo &g, const Phys &ph, double *x, cons
                          const SweepTiles &t) {
   return sor_c(comp, g, ph, x, coef, pres, nullptr, flg, iteration_time, bc, fuse, t.even, t.odd, st);
 }
-cudaError_t launch_sor_c(int comp, const Geo &g, const Phys &ph, float *x, const float *coef,
+cudaError_t launch_sor_c(int comp, const Geo &g, const Phys &ph, float *x, const MuCoef &coef,
                          const double *pres, const double *X, int flg, int iteration_time, int bc, int fuse,
                          cudaStream_t st, const SweepTiles &t) {
   return sor_c(comp, g, ph, x, coef, pres, X, flg, iteration_time, bc, fuse, t.even, t.odd, st);

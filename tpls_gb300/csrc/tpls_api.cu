@@ -47,7 +47,7 @@ struct tpls_ctx {
   int mixed = 0;
   float *phi32, *u32, *v32, *w32, *mu32, *D32, *fx32, *fy32, *fz32;
   float *ffh[2], *ffl[2];  // float-pair redistancing iterates (hi, lo), ping-pong
-  float *coef32[3];
+  float *bdef[3];  // FP32-mixed: defect b of the FP32 sweeps (one float per point)
   float *x3f[3][2];
   double *hbuf = nullptr; // interface height (nx*ny)
   double *stage = nullptr; // host-layout staging of one field ((nx+2)(ny+2)(nz+2))
@@ -395,11 +395,11 @@ static int create_impl(int nx, int ny, int nz, const tpls_params *prm, const dou
     for (float **p : qw) TCK(alloc_field(c, 0, ny + 2, nz + 1, p));
     for (int q = 0; q < 3; q++) {
       void *b = nullptr;
-      const size_t n = (size_t)rec * c->px * (ny + 2) * (q == 2 ? nz + 1 : nz);
+      const size_t n = (size_t)c->px * (ny + 2) * (q == 2 ? nz + 1 : nz);
       TCK(cudaMalloc(&b, n * sizeof(float)));
       c->allocs.push_back(b);
       TCK(cudaMemset(b, 0, n * sizeof(float)));
-      c->coef32[q] = (float *)b;
+      c->bdef[q] = (float *)b;
     }
     TCK(alloc_field(c, 1, ny + 4, nz + 2, &c->mu32));
   }
@@ -468,7 +468,7 @@ long long tpls_footprint_bytes(int nx, int ny, int nz, int precision) {
     t += 2 * round_alloc(D * nrec * nz) + round_alloc(D * nrec * (nz + 1)) + round_alloc(D * nmu);
   } else {
     t += 9 * round_alloc(F * np) + 6 * round_alloc(F * nuv) + 3 * round_alloc(F * nw);
-    t += 2 * round_alloc(F * nrec * nz) + round_alloc(F * nrec * (nz + 1)) + round_alloc(F * nmu);
+    t += 2 * round_alloc(F * (nrec / 8) * nz) + round_alloc(F * (nrec / 8) * (nz + 1)) + round_alloc(F * nmu);
     t += 2 * round_alloc(D * nuv) + round_alloc(D * nw);  // FP64 u3, v3, w3
   }
   t += round_alloc(px * (ny + 2) * (nz + 2) + 64) + round_alloc(D * nz) + round_alloc(D * nx * ny);
@@ -554,8 +554,8 @@ extern "C++" {
 // on the iterate pair X: FP64, or in the FP32-mixed form the FP32 defect
 // d = x - base (base = the component's FP64 state), iterated from d = -base
 // (x = 0, the reference's start) and added back into out64 at the end.
-template <typename T>
-static int momentum(tpls_ctx *c, int comp, const T *coef, T **X, int max_iteration, const double *base = nullptr,
+template <typename T, typename CS>
+static int momentum(tpls_ctx *c, int comp, CS coef, T **X, int max_iteration, const double *base = nullptr,
                     double *out64 = nullptr) {
   const Geo &g = c->g;
   const int nzp = nz_planes(comp == 2 ? 2 : 1, c->nz);
@@ -711,9 +711,9 @@ static int step_once(tpls_ctx *c) {
   delete rhs_scope;
   // momentum sweeps (:756-887)
   int s;
-  if ((s = momentum<double>(c, 0, c->coef[0], c->x3[0], c->prm.mom_u))) return s;
-  if ((s = momentum<double>(c, 1, c->coef[1], c->x3[1], c->prm.mom_v))) return s;
-  if ((s = momentum<double>(c, 2, c->coef[2], c->x3[2], c->prm.mom_w))) return s;
+  if ((s = momentum<double, const double *>(c, 0, c->coef[0], c->x3[0], c->prm.mom_u))) return s;
+  if ((s = momentum<double, const double *>(c, 1, c->coef[1], c->x3[1], c->prm.mom_v))) return s;
+  if ((s = momentum<double, const double *>(c, 2, c->coef[2], c->x3[2], c->prm.mom_w))) return s;
   double *u3 = c->x3[0][c->x3_final[0]], *v3 = c->x3[1][c->x3_final[1]], *w3 = c->x3[2][c->x3_final[2]];
   // pressure source (:892) and solve (:897-913)
   int its = 0, reason = 0;
@@ -745,9 +745,13 @@ static int step_once(tpls_ctx *c) {
 // FP64 results in x3[q][0]
 static int sweeps32(tpls_ctx *c) {
   int s;
-  if ((s = momentum<float>(c, 0, c->coef32[0], c->x3f[0], c->prm.mom_u, c->u2, c->x3[0][0]))) return s;
-  if ((s = momentum<float>(c, 1, c->coef32[1], c->x3f[1], c->prm.mom_v, c->v2, c->x3[1][0]))) return s;
-  if ((s = momentum<float>(c, 2, c->coef32[2], c->x3f[2], c->prm.mom_w, c->w2, c->x3[2][0]))) return s;
+  const Phys &ph = c->ph;
+  if ((s = momentum<float>(c, 0, mu_coef(ph, c->mu32, c->bdef[0]), c->x3f[0], c->prm.mom_u, c->u2, c->x3[0][0])))
+    return s;
+  if ((s = momentum<float>(c, 1, mu_coef(ph, c->mu32, c->bdef[1]), c->x3f[1], c->prm.mom_v, c->v2, c->x3[1][0])))
+    return s;
+  if ((s = momentum<float>(c, 2, mu_coef(ph, c->mu32, c->bdef[2]), c->x3f[2], c->prm.mom_w, c->w2, c->x3[2][0])))
+    return s;
   for (int q = 0; q < 3; q++) c->x3_final[q] = 0;
   return TPLS_OK;
 }
@@ -764,11 +768,12 @@ static int step_once_mixed(tpls_ctx *c) {
   {
     PhaseScope ps(c, TPLS_T_VISC);
     if (sten64) LCK(c, launch_visc(g, ph, c->phi2, c->mu, st));
-    else LCK(c, launch_visc(g, ph, c->phi2, c->mu32, st));
+    // the FP32 sweeps recompute their coefficients from the FP32 viscosity
+    if (!mom64) LCK(c, launch_visc(g, ph, c->phi2, c->mu32, st));
   }
   {
     PhaseScope ps(c, TPLS_T_ADVECT);
-    if (!sten64 || !adv64) {  // FP32 copies of the velocity state
+    if (!adv64) {  // FP32 copies of the velocity state for the FP32 WENO5
       LCK(c, launch_to_float(c->u2 - XOFF, c->u32 - XOFF, c->n_uv, st));
       LCK(c, launch_to_float(c->v2 - XOFF, c->v32 - XOFF, c->n_uv, st));
       LCK(c, launch_to_float(c->w2 - XOFF, c->w32 - XOFF, c->n_w, st));
@@ -823,9 +828,9 @@ static int step_once_mixed(tpls_ctx *c) {
                             c->csf_w[s1], c->csf_w[s0], c->conv_w[s2], c->csf_w[s2], nullptr, nullptr, c->coef[2],
                             st));
     }
-    if ((s = momentum<double>(c, 0, c->coef[0], c->x3[0], c->prm.mom_u))) return s;
-    if ((s = momentum<double>(c, 1, c->coef[1], c->x3[1], c->prm.mom_v))) return s;
-    if ((s = momentum<double>(c, 2, c->coef[2], c->x3[2], c->prm.mom_w))) return s;
+    if ((s = momentum<double, const double *>(c, 0, c->coef[0], c->x3[0], c->prm.mom_u))) return s;
+    if ((s = momentum<double, const double *>(c, 1, c->coef[1], c->x3[1], c->prm.mom_v))) return s;
+    if ((s = momentum<double, const double *>(c, 2, c->coef[2], c->x3[2], c->prm.mom_w))) return s;
     u3v = c->x3[0][c->x3_final[0]];
     v3v = c->x3[1][c->x3_final[1]];
     w3v = c->x3[2][c->x3_final[2]];
@@ -837,11 +842,11 @@ static int step_once_mixed(tpls_ctx *c) {
     {
       PhaseScope ps(c, TPLS_T_MOM_RHS);
       LCK(c, launch_mom_rhs64r32(0, g, ph, c->u2, c->v2, c->w2, c->mu, c->fx, c->conv_u[s1], c->conv_u[s0],
-                                 c->csf_u[s1], c->csf_u[s0], c->conv_u[s2], c->csf_u[s2], c->coef32[0], st));
+                                 c->csf_u[s1], c->csf_u[s0], c->conv_u[s2], c->csf_u[s2], c->bdef[0], st));
       LCK(c, launch_mom_rhs64r32(1, g, ph, c->u2, c->v2, c->w2, c->mu, c->fy, c->conv_v[s1], c->conv_v[s0],
-                                 c->csf_v[s1], c->csf_v[s0], c->conv_v[s2], c->csf_v[s2], c->coef32[1], st));
+                                 c->csf_v[s1], c->csf_v[s0], c->conv_v[s2], c->csf_v[s2], c->bdef[1], st));
       LCK(c, launch_mom_rhs64r32(2, g, ph, c->u2, c->v2, c->w2, c->mu, c->fz, c->conv_w[s1], c->conv_w[s0],
-                                 c->csf_w[s1], c->csf_w[s0], c->conv_w[s2], c->csf_w[s2], c->coef32[2], st));
+                                 c->csf_w[s1], c->csf_w[s0], c->conv_w[s2], c->csf_w[s2], c->bdef[2], st));
     }
     if ((s = sweeps32(c))) return s;
     u3v = c->x3[0][0];
@@ -854,15 +859,12 @@ static int step_once_mixed(tpls_ctx *c) {
     }
     {
       PhaseScope ps(c, TPLS_T_MOM_RHS);
-      LCK(c, launch_mom_rhs32(0, g, ph, c->u32, c->v32, c->w32, c->u2, c->mu32, c->fx32, c->conv_u[s1],
-                              c->conv_u[s0], c->csf_u[s1], c->csf_u[s0], c->conv_u[s2], c->csf_u[s2],
-                              c->coef32[0], st));
-      LCK(c, launch_mom_rhs32(1, g, ph, c->u32, c->v32, c->w32, c->v2, c->mu32, c->fy32, c->conv_v[s1],
-                              c->conv_v[s0], c->csf_v[s1], c->csf_v[s0], c->conv_v[s2], c->csf_v[s2],
-                              c->coef32[1], st));
-      LCK(c, launch_mom_rhs32(2, g, ph, c->u32, c->v32, c->w32, c->w2, c->mu32, c->fz32, c->conv_w[s1],
-                              c->conv_w[s0], c->csf_w[s1], c->csf_w[s0], c->conv_w[s2], c->csf_w[s2],
-                              c->coef32[2], st));
+      LCK(c, launch_mom_rhs_pair(0, g, ph, c->u2, c->v2, c->w2, c->mu32, c->fx32, c->conv_u[s1], c->conv_u[s0],
+                                 c->csf_u[s1], c->csf_u[s0], c->conv_u[s2], c->csf_u[s2], c->bdef[0], st));
+      LCK(c, launch_mom_rhs_pair(1, g, ph, c->u2, c->v2, c->w2, c->mu32, c->fy32, c->conv_v[s1], c->conv_v[s0],
+                                 c->csf_v[s1], c->csf_v[s0], c->conv_v[s2], c->csf_v[s2], c->bdef[1], st));
+      LCK(c, launch_mom_rhs_pair(2, g, ph, c->u2, c->v2, c->w2, c->mu32, c->fz32, c->conv_w[s1], c->conv_w[s0],
+                                 c->csf_w[s1], c->csf_w[s0], c->conv_w[s2], c->csf_w[s2], c->bdef[2], st));
     }
     if ((s = sweeps32(c))) return s;
     u3v = c->x3[0][0];
@@ -1031,8 +1033,9 @@ int tpls_autotune(tpls_ctx *c, int reps) {
     // kind 0: Jacobi, 1: even half-sweep, 2: odd half-sweep (component u)
     if (f32) {
       float *a = c->x3f[0][0], *b = c->x3f[0][1];
-      if (kind == 0) return launch_jacobi_c(0, g, c->ph, a, c->coef32[0], c->pres, c->u2, b, fuse, c->st, t);
-      return launch_sor_c(0, g, c->ph, b, c->coef32[0], c->pres, c->u2, 0, kind == 1 ? 2 : 1, 1, fuse, c->st, t);
+      const MuCoef mc = mu_coef(c->ph, c->mu32, c->bdef[0]);
+      if (kind == 0) return launch_jacobi_c(0, g, c->ph, a, mc, c->pres, c->u2, b, fuse, c->st, t);
+      return launch_sor_c(0, g, c->ph, b, mc, c->pres, c->u2, 0, kind == 1 ? 2 : 1, 1, fuse, c->st, t);
     }
     double *a = c->x3[0][0], *b = c->x3[0][1];
     if (kind == 0) return launch_jacobi_c(0, g, c->ph, a, c->coef[0], c->pres, b, fuse, c->st, t);

@@ -74,25 +74,26 @@ cudaError_t launch_mom_rhs(int comp, const Geo &g, const Phys &ph,
                            const double *s0, double *conv2, double *csf2,
                            double *rhs, double *diff_out, double *coef,
                            cudaStream_t st);
-// FP32-mixed form: stencils on FP32 copies of u, v, w, mu and the CSF force,
-// right-hand side assembled in FP64 from the component's FP64 state x64,
-// coefficient records (8 floats per point) for the FP32 sweeps.
-cudaError_t launch_mom_rhs32(int comp, const Geo &g, const Phys &ph,
-                             const float *u2, const float *v2, const float *w2,
-                             const double *x64, const float *mu,
-                             const float *fcsf, const double *c1,
-                             const double *c0, const double *s1,
-                             const double *s0, double *conv2, double *csf2,
-                             float *coef, cudaStream_t st);
-// FP64 stencils and records rounded to FP32 records (FP32-mixed form with
-// TPLS_PART_MOM_STENCIL).
+// FP32-mixed form: FP32 stencils on the FP64 velocity state split into
+// FP32 pairs by integer operations, FP32 viscosity and CSF force; writes the
+// defect-form b of the FP32 sweeps (one float per point, rec_slot order)
+// and the AB3 histories.
+cudaError_t launch_mom_rhs_pair(int comp, const Geo &g, const Phys &ph,
+                                const double *u2, const double *v2,
+                                const double *w2, const float *mu,
+                                const float *fcsf, const double *c1,
+                                const double *c0, const double *s1,
+                                const double *s0, double *conv2, double *csf2,
+                                float *coef, cudaStream_t st);
+// FP64 stencils writing the defect-form b of the FP32 sweeps (FP32-mixed
+// form with TPLS_PART_MOM_STENCIL; one float per point, rec_slot order).
 cudaError_t launch_mom_rhs64r32(int comp, const Geo &g, const Phys &ph,
                                 const double *u2, const double *v2,
                                 const double *w2, const double *mu,
                                 const double *fcsf, const double *c1,
                                 const double *c0, const double *s1,
                                 const double *s0, double *conv2,
-                                double *csf2, float *coef, cudaStream_t st);
+                                double *csf2, float *bdef, cudaStream_t st);
 // Standalone get_conv_all / get_diffusion_all (per-routine entries).
 cudaError_t launch_conv_diff(int comp, int want_conv, const Geo &g,
                              const Phys &ph, const double *u2,
@@ -131,14 +132,24 @@ cudaError_t launch_sor_c(int comp, const Geo &g, const Phys &ph, double *x,
                          int iteration_time, int bc, int fuse_ghosts,
                          cudaStream_t st, const SweepTiles &t = SweepTiles());
 // FP32 sweeps in defect form: x holds d = x - X for the FP64 base X (the
-// component's state), the records carry the correspondingly shifted b.
+// component's state).  Their coefficients are recomputed per point from the
+// FP32 viscosity field (face averages and Helmholtz diagonal: a few dozen
+// FP32 operations, cheaper than reading a 32-byte record), and only the
+// defect right-hand side b (already divided by the diagonal) is stored, one
+// float per point in record-slot order.
+struct MuCoef {
+  const float *mu;     // viscosity on the p-grid with two periodic ghost rows
+  const float *b;      // per-point b, rec_slot order
+  float ax2, ay2, az2;  // dt/(2 d^2) per axis
+};
+MuCoef mu_coef(const Phys &ph, const float *mu, const float *b);
 cudaError_t launch_jacobi_c(int comp, const Geo &g, const Phys &ph,
-                            const float *xo, const float *coef,
+                            const float *xo, const MuCoef &coef,
                             const double *pres, const double *X, float *x,
                             int fuse_ghosts, cudaStream_t st,
                             const SweepTiles &t = SweepTiles());
 cudaError_t launch_sor_c(int comp, const Geo &g, const Phys &ph, float *x,
-                         const float *coef, const double *pres,
+                         const MuCoef &coef, const double *pres,
                          const double *X, int flg, int iteration_time, int bc,
                          int fuse_ghosts, cudaStream_t st,
                          const SweepTiles &t = SweepTiles());

@@ -12,6 +12,50 @@ struct Helm {
   double dtdx;           // dt/dx (u outlet condition)
 };
 
+template <typename T>
+struct FcT {
+  T px, mx, py, my, pz, mz;
+};
+using Fc = FcT<double>;
+
+
+// face viscosities, momentum_allflux.f90:91-98 (u), :145-152 (v), :187-194 (w)
+template <typename T>
+__device__ __forceinline__ FcT<T> faces(int comp, const Geo &g, const T *__restrict__ mu, int i, int j,
+                                        int k) {
+  const int sy = g.sy, sz = g.szm;
+  FcT<T> f;
+  if (comp == 0) {
+    const T *m = mu + TPLS_IDXM(g, i, j + 1, k + 1);
+    const T a = m[0], b = m[1];
+    f.px = b;
+    f.mx = a;
+    f.py = (a + b + m[sy] + m[1 + sy]) * (T)0.25;
+    f.my = (a + b + m[-sy] + m[1 - sy]) * (T)0.25;
+    f.pz = (a + b + m[sz] + m[1 + sz]) * (T)0.25;
+    f.mz = (a + b + m[-sz] + m[1 - sz]) * (T)0.25;
+  } else if (comp == 1) {
+    const T *m = mu + TPLS_IDXM(g, i, j + 1, k + 1);
+    const T a = m[0], b = m[-sy];
+    f.px = (a + b + m[1] + m[1 - sy]) * (T)0.25;
+    f.mx = (a + b + m[-1] + m[-1 - sy]) * (T)0.25;
+    f.py = a;
+    f.my = b;
+    f.pz = (a + b + m[sz] + m[sz - sy]) * (T)0.25;
+    f.mz = (a + b + m[-sz] + m[-sz - sy]) * (T)0.25;
+  } else {
+    const T *m = mu + TPLS_IDXM(g, i, j + 1, k);
+    const T a = m[0], b = m[sz];
+    f.px = (a + b + m[1] + m[1 + sz]) * (T)0.25;
+    f.mx = (a + b + m[-1] + m[-1 + sz]) * (T)0.25;
+    f.py = (a + b + m[sy] + m[sy + sz]) * (T)0.25;
+    f.my = (a + b + m[-sy] + m[-sy + sz]) * (T)0.25;
+    f.pz = b;
+    f.mz = a;
+  }
+  return f;
+}
+
 // Slot of point (i, j, k) (linear index c, 1 <= i <= nx) in the coefficient
 // record arrays.  Each (j, k) row keeps the records of odd i in its first
 // half and of even i in its second half (the row pitch sy is a multiple of
