@@ -4,12 +4,14 @@
 // velocity being relaxed (double, or float in the FP32-mixed form).
 #pragma once
 #include "tpls_kernels.h"
+#include "tpls_pair.cuh"
 
 namespace tpls {
 
 struct Helm {
   double ax2, ay2, az2;  // dt/(2 d^2)
   double dtdx;           // dt/dx (u outlet condition)
+  float dtdxf;           // the same, rounded, for the FP32 defect-form sweeps
 };
 
 template <typename T>
@@ -75,51 +77,106 @@ __device__ __forceinline__ void put(const Geo &g, T *x, int i, int j, int k, T v
   }
 }
 
-// Defect form.  The FP32-mixed sweeps iterate on d = x - X, X the FP64
-// velocity state of the step (u2, v2 or w2), so that FP32 rounding acts on
-// the small correction instead of on the velocity; the FP64 form passes
-// X = null and iterates on x itself.  Interior updates are the same affine
-// map in both (the records' b is shifted accordingly); boundary rows are
-// evaluated in x space in FP64 and stored back as x - X.
-template <typename T>
-__device__ __forceinline__ double xval(const Geo &g, const double *X, T d, int i, int j, int k) {
-  return X ? (double)d + X[TPLS_IDX(g, i, j, k)] : (double)d;
+// Boundary rows.  The FP64 form iterates on x itself (X = null); the
+// FP32-mixed sweeps iterate on d = x - X, X the FP64 velocity state of the
+// step (u2, v2 or w2), so that FP32 rounding acts on the small correction
+// instead of on the velocity.  A boundary relation of x becomes one of d
+// whose FP64 parts are differences of nearby X (and P) values, taken from
+// FP32 pairs (integer splitting, tpls_pair.cuh): the FP32 sweeps issue no
+// FP64 instruction, which on GB300's FP64 pipe made the boundary threads
+// the critical path of every sweep.
+//
+// copy x(it) = x(is) (inlet / outlet copies)
+__device__ __forceinline__ void bc_copy(const Geo &g, double *x, const double *, int it, int, int j, int k,
+                                        double vs, int fuse) {
+  put(g, x, it, j, k, vs, fuse);
 }
-template <typename T>
-__device__ __forceinline__ void bput(const Geo &g, T *x, const double *X, int i, int j, int k, double v,
-                                     int fuse) {
-  put(g, x, i, j, k, (T)(X ? v - X[TPLS_IDX(g, i, j, k)] : v), fuse);
+__device__ __forceinline__ void bc_copy(const Geo &g, float *x, const double *X, int it, int is, int j, int k,
+                                        float ds, int fuse) {
+  const F2 a = split_bits(X[TPLS_IDX(g, is, j, k)]), b = split_bits(X[TPLS_IDX(g, it, j, k)]);
+  put(g, x, it, j, k, ds + dif(a, b), fuse);
+}
+// x(i, j, k) = 0 (u fictitious point, w walls)
+__device__ __forceinline__ void bc_zero(const Geo &g, double *x, const double *, int i, int j, int k, int fuse) {
+  put(g, x, i, j, k, 0.0, fuse);
+}
+__device__ __forceinline__ void bc_zero(const Geo &g, float *x, const double *X, int i, int j, int k, int fuse) {
+  put(g, x, i, j, k, -round_bits(X[TPLS_IDX(g, i, j, k)]), fuse);
 }
 
 // u outlet, main_ns_hybrid.F90:768-776 (the pressure row index is the u row
-// index j, as written in the reference); x space, FP64.
+// index j, as written in the reference):
+//   x(nx) = x(nx-1) + dt/dx (P(nx+1) + P(nx-1) - 2 P(nx))
 __device__ __forceinline__ double u_outlet(const Geo &g, const Helm &h, const double *P, double unm1, int j,
                                            int k) {
   const int nx = g.nx;
   return unm1 + h.dtdx * (P[TPLS_IDX(g, nx + 1, j, k + 1)] + P[TPLS_IDX(g, nx - 1, j, k + 1)] -
                           2.0 * P[TPLS_IDX(g, nx, j, k + 1)]);
 }
+__device__ __forceinline__ void bc_u_outlet(const Geo &g, const Helm &h, const double *P, double *x,
+                                            const double *, int j, int k, double vm1, int fuse) {
+  put(g, x, g.nx, j, k, u_outlet(g, h, P, vm1, j, k), fuse);
+}
+// defect form: d(nx) = d(nx-1) + (X(nx-1) - X(nx)) + dt/dx ((P+ - P0) - (P0 - P-))
+__device__ __forceinline__ void bc_u_outlet(const Geo &g, const Helm &h, const double *P, float *x,
+                                            const double *X, int j, int k, float dm1, int fuse) {
+  const int nx = g.nx;
+  const F2 pp = split_bits(P[TPLS_IDX(g, nx + 1, j, k + 1)]), p0 = split_bits(P[TPLS_IDX(g, nx, j, k + 1)]);
+  const F2 pm = split_bits(P[TPLS_IDX(g, nx - 1, j, k + 1)]);
+  const F2 xa = split_bits(X[TPLS_IDX(g, nx - 1, j, k)]), xb = split_bits(X[TPLS_IDX(g, nx, j, k)]);
+  put(g, x, nx, j, k, dm1 + dif(xa, xb) + h.dtdxf * (dif(pp, p0) - dif(p0, pm)), fuse);
+}
 
-// Post-sweep boundary rows (main_ns_hybrid.F90:784-799 u, :826-836 v,
-// :860-879 w), written by the thread that owns the first / last x pair:
-// the inlet copy x(0) = x(1), for u the pressure outlet x(nx) and the
-// fictitious point x(nx+1) = 0, for v and w the outlet copy.  A value of the
-// colour not relaxed in this half-sweep is read (it is final already).
+// Post-sweep boundary rows of the Jacobi sweep at point (i, j, k) with new
+// value v (main_ns_hybrid.F90:784-799 u, :826-836 v, :860-879 w).
+template <typename T>
+__device__ __forceinline__ void jacobi_bc(int comp, const Geo &g, const Helm &h, T *x, const double *X,
+                                          const double *P, int i, int j, int k, T v, int fuse) {
+  if (comp == 0) {
+    if (i == 1) bc_copy(g, x, X, 0, 1, j, k, v, fuse);
+    if (i == g.nx - 1) {
+      bc_u_outlet(g, h, P, x, X, j, k, v, fuse);
+      bc_zero(g, x, X, g.nx + 1, j, k, fuse);
+    }
+  } else if (comp == 1) {
+    if (i == 1) bc_copy(g, x, X, 0, 1, j, k, v, fuse);
+    if (i == g.nx) bc_copy(g, x, X, g.nx + 1, g.nx, j, k, v, fuse);
+  } else {
+    const int nz = g.nz;
+    if (k == 1) bc_zero(g, x, X, i, j, 0, fuse);
+    if (k == nz - 1) bc_zero(g, x, X, i, j, nz, fuse);
+    if (i == 1) {
+      bc_copy(g, x, X, 0, 1, j, k, v, fuse);
+      if (k == 1) bc_zero(g, x, X, 0, j, 0, fuse);
+      if (k == nz - 1) bc_zero(g, x, X, 0, j, nz, fuse);
+    }
+    if (i == g.nx) {
+      bc_copy(g, x, X, g.nx + 1, g.nx, j, k, v, fuse);
+      if (k == 1) bc_zero(g, x, X, g.nx + 1, j, 0, fuse);
+      if (k == nz - 1) bc_zero(g, x, X, g.nx + 1, j, nz, fuse);
+    }
+  }
+}
+
+// Post-sweep boundary rows of a red-black half-sweep, written by the thread
+// that owns the first / last x pair: the inlet copy x(0) = x(1), for u the
+// pressure outlet x(nx) and the fictitious point x(nx+1) = 0, for v and w
+// the outlet copy.  A value of the colour not relaxed in this half-sweep is
+// read (it is final already).
 template <typename T>
 __device__ __forceinline__ void sor_bc(int comp, const Geo &g, const Helm &h, T *x, const double *X,
                                        const double *P, int i2, int i, int iend, T v, int j, int k, int fuse) {
   if (i2 == 0) {
     const T v1 = (i == 1) ? v : x[TPLS_IDX(g, 1, j, k)];
-    bput(g, x, X, 0, j, k, xval(g, X, v1, 1, j, k), fuse);
+    bc_copy(g, x, X, 0, 1, j, k, v1, fuse);
   }
   if (i2 == (iend - 1) / 2) {
     const T ve = (i == iend) ? v : x[TPLS_IDX(g, iend, j, k)];
-    const double vex = xval(g, X, ve, iend, j, k);
     if (comp == 0) {
-      bput(g, x, X, g.nx, j, k, u_outlet(g, h, P, vex, j, k), fuse);
-      bput(g, x, X, g.nx + 1, j, k, 0.0, fuse);
+      bc_u_outlet(g, h, P, x, X, j, k, ve, fuse);
+      bc_zero(g, x, X, g.nx + 1, j, k, fuse);
     } else {
-      bput(g, x, X, g.nx + 1, j, k, vex, fuse);
+      bc_copy(g, x, X, g.nx + 1, iend, j, k, ve, fuse);
     }
   }
 }
@@ -130,6 +187,7 @@ static inline Helm helm_of(const Phys &ph) {
   h.ay2 = (ph.dt / (ph.dy * ph.dy)) / 2.0;
   h.az2 = (ph.dt / (ph.dz * ph.dz)) / 2.0;
   h.dtdx = ph.dt / ph.dx;
+  h.dtdxf = (float)h.dtdx;
   return h;
 }
 
