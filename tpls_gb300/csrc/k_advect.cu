@@ -10,6 +10,7 @@
 // The periodic-y halo of the reference's 3-ghost phi_augaug copy becomes a
 // wrapped row index; no augmented array is built.
 #include "tpls_kernels.h"
+#include "tpls_pair.cuh"
 
 namespace tpls {
 
@@ -154,7 +155,7 @@ cudaError_t launch_advect(const Geo &g, const Phys &ph, const float *phi2, const
 // FP64 state used by the FP32-mixed form)
 __global__ void k_to_float(const double *__restrict__ a, float *__restrict__ b, size_t n) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    b[i] = (float)a[i];
+    b[i] = round_bits(a[i]);  // integer split: no FP64-pipe conversion
 }
 cudaError_t launch_to_float(const double *a, float *b, size_t n, cudaStream_t st) {
   k_to_float<<<1216, 256, 0, st>>>(a, b, n);
@@ -199,9 +200,34 @@ __global__ void k_finish_sum(const double *part, int nparts, double *out, int no
   }
 }
 
-cudaError_t finish_sum(const double *part, int nparts, double *out, int nout,
-                       cudaStream_t st) {
-  k_finish_sum<<<1, 256, 0, st>>>(part, nparts, out, nout);
+// Sums of contiguous chunks of the partials, one block per chunk, each in a
+// fixed order (the first stage of finish_sum for long partial arrays).
+__global__ void k_chunk_sum(const double *__restrict__ part, int nparts, int chunk, double *__restrict__ out) {
+  __shared__ double s[256];
+  const int lo = blockIdx.x * chunk, hi = min(nparts, lo + chunk);
+  double acc = 0.0;
+  for (int p = lo + (int)threadIdx.x; p < hi; p += blockDim.x) acc += part[p];
+  s[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) s[threadIdx.x] += s[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[blockIdx.x] = s[0];
+}
+
+static int chunk_blocks(int nparts) { return min(FS_TAIL, (nparts + 2047) / 2048); }
+
+int finish_sum_kernels(int nparts, int nout) { return (nout == 1 && nparts > FS_ONE_BLOCK) ? 2 : 1; }
+
+cudaError_t finish_sum(double *part, int nparts, double *out, int nout, cudaStream_t st) {
+  if (finish_sum_kernels(nparts, nout) == 2) {
+    const int nb = chunk_blocks(nparts), chunk = (nparts + nb - 1) / nb;
+    k_chunk_sum<<<nb, 256, 0, st>>>(part, nparts, chunk, part + nparts);
+    k_finish_sum<<<1, 256, 0, st>>>(part + nparts, nb, out, 1);
+  } else {
+    k_finish_sum<<<1, 256, 0, st>>>(part, nparts, out, nout);
+  }
   return cudaGetLastError();
 }
 

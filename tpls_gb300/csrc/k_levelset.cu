@@ -302,11 +302,6 @@ __device__ __noinline__ FF ff_ghost_plane(const Geo &g, const Phys &ph, float h,
   return ff_split(2.0 * ff_dbl(ff_val<IN64>(g, ph, h, ktau, src, D, flags, i, jj, k1)) -
                   ff_dbl(ff_val<IN64>(g, ph, h, ktau, src, D, flags, i, jj, k2)));
 }
-template <bool IN64>
-__device__ __noinline__ double ff_sq_change(const FFSrc<IN64> &src, int c, FF v) {
-  const double d = src.exact(c) - ff_dbl(v);
-  return d * d;
-}
 
 template <bool IN64, bool OUT64>
 __global__ void __launch_bounds__(LS_BX *LS_BY)
@@ -315,7 +310,7 @@ __global__ void __launch_bounds__(LS_BX *LS_BY)
                  float *__restrict__ olo, double *__restrict__ err_part) {
   const int i = blockIdx.x * LS_BX + threadIdx.x, j = blockIdx.y * LS_BY + threadIdx.y;
   const int k = blockIdx.z;
-  double e = 0.0;
+  float e = 0.0f;
   if (i <= g.nx + 1 && j <= g.ny + 1) {
     const int jj = wrapy(j, g.ny);
     const int c = TPLS_IDX(g, i, j, k);
@@ -324,9 +319,12 @@ __global__ void __launch_bounds__(LS_BX *LS_BY)
       v = ff_ghost_plane<IN64>(g, ph, h, ktau, src, D, flags, i, jj, k);
     else
       v = ff_val<IN64>(g, ph, h, ktau, src, D, flags, i, jj, k);
-    if (err_part && i >= 1 && i <= g.nx && j >= 1 && j <= g.ny) e = ff_sq_change<IN64>(src, c, v);
-    if (OUT64) {
-      out64[c] = ff_dbl(v);
+    if (err_part && i >= 1 && i <= g.nx && j >= 1 && j <= g.ny) {  // the iteration's change, from pairs
+      const float d = dif(src.pair(c), F2{v.hi, v.lo});
+      e = d * d;
+    }
+    if (OUT64) {  // exact widening by integer operations, one FP64 add
+      out64[c] = widen_bits(v.hi) + widen_bits(v.lo);
     } else {
       ohi[c] = v.hi;
       olo[c] = v.lo;
@@ -336,7 +334,7 @@ __global__ void __launch_bounds__(LS_BX *LS_BY)
     __shared__ double s[LS_BX * LS_BY / 32];
     for (int o = 16; o > 0; o >>= 1) e += __shfl_down_sync(0xffffffffu, e, o);
     const int t = threadIdx.y * LS_BX + threadIdx.x;
-    if ((t & 31) == 0) s[t >> 5] = e;
+    if ((t & 31) == 0) s[t >> 5] = widen_bits(e);
     __syncthreads();
     if (t == 0) {
       double a = 0.0;
@@ -521,9 +519,37 @@ cudaError_t launch_visc(const Geo &g, const Phys &ph, const double *phi2,
   k_visc<double><<<grd, dim3(LS_BX, LS_BY), 0, st>>>(g, ph, phi2, mu);
   return cudaGetLastError();
 }
+// The FP32 viscosity of the FP32-mixed form: the same formula in FP32 on
+// phi rounded to FP32 by integer operations (the smoothed Heaviside is
+// continuous at |phi| = sw, so the band test needs no FP64 either).
+struct ViscF {
+  float sw, half_rsw, pi_rsw, half_rpi, mp, mm;
+};
+__global__ void k_visc32(Geo g, ViscF v, const double *__restrict__ phi, float *__restrict__ mu) {
+  const int i = blockIdx.x * LS_BX + threadIdx.x, j = blockIdx.y * LS_BY + threadIdx.y - 1;
+  const int k = blockIdx.z;
+  if (i > g.nx + 1 || j > g.ny + 2) return;
+  const float p = round_bits(phi[TPLS_IDX(g, i, wrapy(j, g.ny), k)]);
+  float hv;
+  if (p < -v.sw)
+    hv = 0.0f;
+  else if (p > v.sw)
+    hv = 1.0f;
+  else
+    hv = 0.5f + p * v.half_rsw + v.half_rpi * sinf(v.pi_rsw * p);
+  mu[TPLS_IDXM(g, i, j, k)] = v.mp * hv + v.mm * (1.0f - hv);
+}
+
 cudaError_t launch_visc(const Geo &g, const Phys &ph, const double *phi2, float *mu, cudaStream_t st) {
   dim3 grd((g.nx + 2 + LS_BX - 1) / LS_BX, (g.ny + 4 + LS_BY - 1) / LS_BY, g.nz + 2);
-  k_visc<float><<<grd, dim3(LS_BX, LS_BY), 0, st>>>(g, ph, phi2, mu);
+  ViscF v;
+  v.sw = (float)ph.sw;
+  v.half_rsw = (float)(1.0 / (2.0 * ph.sw));
+  v.pi_rsw = (float)(TPLS_PI_SP / ph.sw);
+  v.half_rpi = (float)(1.0 / (2.0 * TPLS_PI_SP));
+  v.mp = (float)(ph.mu_plus / ph.re);
+  v.mm = (float)(ph.mu_minus / ph.re);
+  k_visc32<<<grd, dim3(LS_BX, LS_BY), 0, st>>>(g, v, phi2, mu);
   return cudaGetLastError();
 }
 

@@ -635,20 +635,28 @@ cudaError_t launch_sor(int comp, const Geo &g, const Phys &ph, double *x,
 
 // get_difference: per-block partials of sum (a-b)^2 over i 1..nx, j 1..ny,
 // planes 0..nzp-1.
+// Sum of squared differences of two iterates (the sweeps' convergence
+// diagnostic), one partial per block.  FP64 iterates are differenced and
+// summed in FP64; FP32 iterates in FP32 up to the warp sums (exactly
+// widened), so the FP32 form issues no FP64 instruction per point.
 template <typename T>
 __global__ void k_diff2(Geo g, const T *__restrict__ a, const T *__restrict__ b, double *__restrict__ part) {
   const int i = blockIdx.x * MB_X + threadIdx.x + 1, j = blockIdx.y * MB_Y + threadIdx.y + 1;
   const int k = blockIdx.z;
-  double e = 0.0;
+  T e = (T)0;
   if (i <= g.nx && j <= g.ny) {
     const int c = TPLS_IDX(g, i, j, k);
-    const double d = (double)a[c] - (double)b[c];
+    const T d = a[c] - b[c];
     e = d * d;
   }
   __shared__ double s[MB_X * MB_Y / 32];
   for (int o = 16; o > 0; o >>= 1) e += __shfl_down_sync(0xffffffffu, e, o);
   const int t = threadIdx.y * MB_X + threadIdx.x;
-  if ((t & 31) == 0) s[t >> 5] = e;
+  if constexpr (sizeof(T) == sizeof(float)) {
+    if ((t & 31) == 0) s[t >> 5] = widen_bits(e);
+  } else {
+    if ((t & 31) == 0) s[t >> 5] = e;
+  }
   __syncthreads();
   if (t == 0) {
     double acc = 0.0;

@@ -591,15 +591,15 @@ cudaError_t launch_sor_c(int comp, const Geo &g, const Phys &ph, float *x, const
 }
 
 // defect form: d = -X before the first sweep (the sweeps start from x = 0),
-// x = X + d after the last
+// x = X + d after the last (conversions by integer operations, tpls_pair.cuh)
 __global__ void k_defect_init(const double *__restrict__ X, float *__restrict__ d, size_t n) {
   for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
-    d[q] = (float)(-X[q]);
+    d[q] = -round_bits(X[q]);
 }
 __global__ void k_defect_apply(const double *__restrict__ X, const float *__restrict__ d, double *__restrict__ x,
                                size_t n) {
   for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
-    x[q] = X[q] + (double)d[q];
+    x[q] = X[q] + widen_bits(d[q]);
 }
 cudaError_t launch_defect_init(const double *X, float *d, size_t n, cudaStream_t st) {
   k_defect_init<<<1216, 256, 0, st>>>(X, d, n);

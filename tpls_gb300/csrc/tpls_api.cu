@@ -94,6 +94,13 @@ enum { SC_ERR_PHI = 0, SC_ERR_U, SC_ERR_V, SC_ERR_W, SC_VOL, SC_N };
     cudaError_t e_ = (x);                                                \
     if (e_ != cudaSuccess) return TPLS_ERR_CUDA_BASE + (int)e_;          \
   } while (0)
+// finish_sum launches one or two kernels: count both
+#define FSUM(ctx, part, n, out, st)                                      \
+  do {                                                                   \
+    LCK(ctx, finish_sum(part, n, out, 1, st));                           \
+    (ctx)->launches += finish_sum_kernels(n, 1) - 1;                     \
+    (ctx)->t_n[(ctx)->cur_slot] += finish_sum_kernels(n, 1) - 1;         \
+  } while (0)
 #define LCK(ctx, x)                                                      \
   do {                                                                   \
     cudaError_t e_ = (x);                                                \
@@ -432,7 +439,7 @@ static int create_impl(int nx, int ny, int nz, const tpls_params *prm, const dou
   if (d2 > c->part_len) c->part_len = d2;
   {
     void *b = nullptr;
-    TCK(cudaMalloc(&b, sizeof(double) * c->part_len));
+    TCK(cudaMalloc(&b, sizeof(double) * (c->part_len + FS_TAIL)));
     c->allocs.push_back(b);
     c->part = (double *)b;
     TCK(cudaMalloc(&b, sizeof(double) * SC_N));
@@ -483,7 +490,7 @@ long long tpls_footprint_bytes(int nx, int ny, int nz, int precision) {
   size_t part = (size_t)ls_iter_blocks(g);
   const size_t d2 = (size_t)diff2_blocks(g, nz + 1);
   if (d2 > part) part = d2;
-  t += round_alloc(D * part) + round_alloc(D * SC_N);
+  t += round_alloc(D * (part + FS_TAIL)) + round_alloc(D * SC_N);
   t += poisson_footprint(g, precision == TPLS_PREC_FP32_MIXED, round_alloc);
   return (long long)t;
 }
@@ -603,7 +610,7 @@ static int momentum(tpls_ctx *c, int comp, CS coef, T **X, int max_iteration, co
   const int nb = diff2_blocks(g, nzp);
   if (N >= 1) {
     LCK(c, launch_diff2(g, X[N % 2], X[(N - 1) % 2], nzp, c->part, c->st));
-    LCK(c, finish_sum(c->part, nb, c->scal + SC_ERR_U + comp, 1, c->st));
+    FSUM(c, c->part, nb, c->scal + SC_ERR_U + comp, c->st);
   } else {
     TCK(cudaMemsetAsync(c->scal + SC_ERR_U + comp, 0, sizeof(double), c->st));
   }
@@ -690,7 +697,7 @@ static int step_once(tpls_ctx *c) {
     double *dst = (it == L) ? c->phi2 : ((it % 2 == 1) ? c->phiB : c->phiA);
     LCK(c, launch_ls_iter(g, ph, src, c->D, c->flags, dst, (it == L) ? c->part : nullptr, st));
   }
-  if (L > 0) LCK(c, finish_sum(c->part, ls_iter_blocks(g), c->scal + SC_ERR_PHI, 1, st));
+  if (L > 0) FSUM(c, c->part, ls_iter_blocks(g), c->scal + SC_ERR_PHI, st);
   delete ls_scope;
   // CSF from the redistanced phi3 (:618-641)
   {
@@ -806,7 +813,7 @@ static int step_once_mixed(tpls_ctx *c) {
                                (it == L) ? c->phi2 : nullptr, c->ffh[wi], c->ffl[wi], ep, st));
     }
   }
-  if (L > 0) LCK(c, finish_sum(c->part, ls_iter_blocks(g), c->scal + SC_ERR_PHI, 1, st));
+  if (L > 0) FSUM(c, c->part, ls_iter_blocks(g), c->scal + SC_ERR_PHI, st);
   delete ls_scope;
   int s;
   const void *u3v;
@@ -1333,7 +1340,7 @@ int tpls_get_stats(tpls_ctx *c, tpls_stats *out) {
   dim3 grd((g.nx + 31) / 32, (g.ny + 3) / 4, g.nz);
   k_volume<<<grd, dim3(32, 4), 0, c->st>>>(g, c->ph, c->phi2, c->part);
   LCK(c, cudaGetLastError());
-  LCK(c, finish_sum(c->part, (int)(grd.x * grd.y * grd.z), c->scal + SC_VOL, 1, c->st));
+  FSUM(c, c->part, (int)(grd.x * grd.y * grd.z), c->scal + SC_VOL, c->st);
   TCK(cudaMemcpyAsync(c->scal_host, c->scal, sizeof(double) * SC_N, cudaMemcpyDeviceToHost, c->st));
   TCK(cudaStreamSynchronize(c->st));
   c->stats.err_phi = c->scal_host[SC_ERR_PHI];
@@ -1513,7 +1520,7 @@ int tpls_do_tpls(tpls_ctx *c, double *phi2, double *phi3, double *conv0_phi, dou
     LCK(c, launch_ls_iter(c->g, ph, src, Dd, c->scr_flags, dst, (it == L) ? c->part : nullptr, c->st));
     src = dst;
   }
-  if (L > 0) LCK(c, finish_sum(c->part, ls_iter_blocks(c->g), c->scal + SC_ERR_PHI, 1, c->st));
+  if (L > 0) FSUM(c, c->part, ls_iter_blocks(c->g), c->scal + SC_ERR_PHI, c->st);
   TCK(d2h(c, phi3, src, nz + 2));
   TCK(cudaMemcpyAsync(c->scal_host, c->scal, sizeof(double) * SC_N, cudaMemcpyDeviceToHost, c->st));
   TCK(cudaStreamSynchronize(c->st));
@@ -1695,7 +1702,7 @@ int tpls_get_difference(tpls_ctx *c, const double *ua, const double *ub, const i
   TCK(h2d(c, c->scr[0], ua, nzp));
   TCK(h2d(c, c->scr[1], ub, nzp));
   LCK(c, launch_diff2(c->g, c->scr[0], c->scr[1], nzp, c->part, c->st));
-  LCK(c, finish_sum(c->part, diff2_blocks(c->g, nzp), c->scal + SC_ERR_U, 1, c->st));
+  FSUM(c, c->part, diff2_blocks(c->g, nzp), c->scal + SC_ERR_U, c->st);
   TCK(cudaMemcpyAsync(c->scal_host, c->scal, sizeof(double) * SC_N, cudaMemcpyDeviceToHost, c->st));
   TCK(cudaStreamSynchronize(c->st));
   *diff = c->scal_host[SC_ERR_U];

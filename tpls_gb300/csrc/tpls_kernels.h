@@ -12,9 +12,15 @@ struct Phys {
 };
 
 // Deterministic block-partial reduction buffer: kernels write one partial
-// per block into part[], finish_sum() adds them in a fixed order.
-cudaError_t finish_sum(const double *part, int nparts, double *out, int nout,
+// per block into part[], finish_sum() adds them in a fixed order.  Above
+// FS_ONE_BLOCK partials (nout = 1) it first sums contiguous chunks on many
+// SMs into part[nparts ...] (a single SM's FP64 pipe would take ~90 us for
+// the 285k partials of a 512x256x256 sweep), so part[] must hold FS_TAIL
+// doubles after the partials; finish_sum_kernels() is the launch count.
+constexpr int FS_TAIL = 1024, FS_ONE_BLOCK = 8192;
+cudaError_t finish_sum(double *part, int nparts, double *out, int nout,
                        cudaStream_t st);
+int finish_sum_kernels(int nparts, int nout);
 
 // advect_phi.f90 / weno.f90: conv2_phi from phi2, u2, v2, w2.
 cudaError_t launch_advect(const Geo &g, const Phys &ph, const double *phi2,
