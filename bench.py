@@ -120,17 +120,20 @@ def _dist():
     return ws, rank, local
 
 
-def _algorithmic_bytes(nx, ny, nz, mom):
-    """Compulsory bytes of the momentum-sweep launches (FP64, per point of
-    the component grid): Jacobi 32 B (x_old, RHS, mu read, x written), a
-    red-black half-sweep 28 B (x and mu read in full, RHS of the relaxed
-    colour, that colour written).  Returns (Jacobi bytes, odd half-sweep
-    bytes, Jacobi launches, odd half-sweep launches) of one step."""
+def _algorithmic_bytes(nx, ny, nz, mom, esz=8):
+    """Compulsory bytes of the momentum-sweep launches, per point of the
+    component grid.  FP64 (esz 8): Jacobi 32 B (x_old, RHS, mu read, x
+    written), a red-black half-sweep 28 B (x and mu read in full, RHS of the
+    relaxed colour, that colour written).  FP32 sweeps (esz 4; x, mu and the
+    defect b in FP32): Jacobi 16 B, half-sweep 12 B.  Returns (Jacobi bytes,
+    odd half-sweep bytes, Jacobi launches, odd half-sweep launches) of one
+    step."""
     pts = [(nx - 1) * ny * nz, nx * ny * nz, nx * ny * (nz - 1)]
     outer = mom // 2
     n_odd = (outer + 1) // 2  # outer iterations 1, 3, 5, ... use the odd sweep
-    jac = sum(32.0 * p for p in pts) * outer
-    sor_odd = sum(28.0 * p for p in pts) * 2 * n_odd
+    jac_pt, half_pt = (32.0, 28.0) if esz == 8 else (16.0, 12.0)
+    jac = sum(jac_pt * p for p in pts) * outer
+    sor_odd = sum(half_pt * p for p in pts) * 2 * n_odd
     return jac, sor_odd, 3 * outer, 6 * n_odd
 
 
@@ -238,14 +241,14 @@ def run_gpu(args, ws, rank, local) -> dict | None:
 
     peaks = _peaks()
     hbm = float(peaks.get("hbm_gbs", 6800.0))
-    jac_b, sor_b, jac_n, sor_n = _algorithmic_bytes(nx, ny, nz, params.mom_u)
+    esz = 4 if precision == 1 and not (parts & 4) else 8  # FP32 sweeps unless momentum is kept in FP64
+    jac_b, sor_b, jac_n, sor_n = _algorithmic_bytes(nx, ny, nz, params.mom_u, esz)
     # dominant kernel of the step: the odd-iteration red-black half-sweep
     # (k_sor_odd_c3), its launches timed with CUDA events on the library's
     # stream in the phase pass
     sor_ms, sor_l = phases["sor_odd"]
     dominant = "k_sor_odd_c3"
-    esz = 4.0 if precision == 1 else 8.0
-    per_launch_b = sor_b / sor_n * (esz / 8.0)
+    per_launch_b = sor_b / sor_n
     avg_ms = sor_ms / max(sor_l, 1)
     achieved = per_launch_b / (avg_ms / 1e3) / 1e9
     wl = f"{nx}x{ny}x{nz}-{'fp64' if precision == 0 else 'mixed'}"
@@ -284,9 +287,10 @@ def run_gpu(args, ws, rank, local) -> dict | None:
                      "avg_launch_ms": avg_ms,
                      "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": traffic, "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback",
-                     "note": "achieved = algorithmic bytes (28 B per component point per half-sweep) / "
-                             "event time; traffic = ncu DRAM bytes per launch (profiles/); the FP64 form's "
-                             "kernels are bound by GB300's FP64 pipe (1.01 TFLOP/s), see fp64_pipe"},
+                     "note": "achieved = algorithmic bytes (28 B per component point per half-sweep in FP64, "
+                             "12 B in the FP32 sweeps) / event time; traffic = ncu DRAM bytes per launch "
+                             "(profiles/); the FP64 form's kernels are bound by GB300's FP64 pipe "
+                             "(1.01 TFLOP/s), see fp64_pipe"},
         "fp64_pipe": {"kernel": dominant, "ncu_active_pct_of_peak": fp64_pct,
                       "source": "ncu sm__pipe_fp64_cycles_active of the same kernel (profiles/)"},
         "phases_ms_per_step": {k: v[0] / nph for k, v in phases.items()},

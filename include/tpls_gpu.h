@@ -145,7 +145,10 @@ int tpls_get_tiles(const tpls_ctx *ctx, int *tiles3);
 /* ---- job-serving helpers (no counterpart in the reference) ------------ */
 /* Device bytes tpls_gpu_create allocates for this grid and precision (each
  * allocation rounded to the allocator's 2 MiB unit), or -1 for bad
- * arguments.  Host-only: used for admission before anything is allocated. */
+ * arguments.  Host-only: used for admission before anything is allocated.
+ * For TPLS_PREC_FP32_MIXED it counts the FP64 stencil inputs of
+ * TPLS_PART_MOM_STENCIL (an upper bound when that part is off); keeping
+ * TPLS_PART_MOMENTUM or TPLS_PART_LEVELSET in FP64 allocates more. */
 long long tpls_footprint_bytes(int nx, int ny, int nz, int precision);
 /* 1 when every step enqueued on the context has finished, 0 while work is
  * pending, or an error status.  Does not block. */

@@ -477,6 +477,9 @@ long long tpls_footprint_bytes(int nx, int ny, int nz, int precision) {
     t += 9 * round_alloc(F * np) + 6 * round_alloc(F * nuv) + 3 * round_alloc(F * nw);
     t += 2 * round_alloc(F * (nrec / 8) * nz) + round_alloc(F * (nrec / 8) * (nz + 1)) + round_alloc(F * nmu);
     t += 2 * round_alloc(D * nuv) + round_alloc(D * nw);  // FP64 u3, v3, w3
+    // FP64 momentum-stencil inputs (CSF force, viscosity) of TPLS_PART_MOM_STENCIL,
+    // the setting served and batched jobs use; counted for every mixed context
+    t += 3 * round_alloc(D * np) + round_alloc(D * nmu);
   }
   t += round_alloc(px * (ny + 2) * (nz + 2) + 64) + round_alloc(D * nz) + round_alloc(D * nx * ny);
   t += round_alloc(D * (size_t)(nx + 2) * (ny + 2) * (nz + 2));  // host-layout staging
