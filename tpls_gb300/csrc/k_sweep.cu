@@ -71,7 +71,7 @@ __device__ __forceinline__ Rec<float> get_rec(int comp, const Geo &g, const MuCo
                                               bool stream) {
   const FcT<float> f = faces<float>(comp, g, s.mu, i, j, k);
   const float diag = 1.0f + s.ax2 * (f.px + f.mx) + s.ay2 * (f.py + f.my) + s.az2 * (f.pz + f.mz);
-  const float r = 1.0f / diag;
+  const float r = __fdividef(1.0f, diag);  // diag >= 1: the fast reciprocal is within 2 ulp
   float czp = s.az2 * f.pz * r, czm = s.az2 * f.mz * r;
   if (comp != 2) {
     if (k == 0) {
@@ -89,10 +89,11 @@ __device__ __forceinline__ Rec<float> get_rec(int comp, const Geo &g, const MuCo
 }
 
 // Jacobi: x = J(xo) on the component's interior with its boundary rows.
-template <typename T, typename CS, int SW_X, int SW_Y>
+template <typename T, typename CS, int CC, int SW_X, int SW_Y>
 __global__ void __launch_bounds__(SW_X *SW_Y)
-    k_jacobi_c(int comp, Geo g, Helm h, const T *__restrict__ xo, const CS coef,
+    k_jacobi_c(int comp_, Geo g, Helm h, const T *__restrict__ xo, const CS coef,
                const double *__restrict__ P, const double *__restrict__ X, T *__restrict__ x, int fuse) {
+  const int comp = (CC >= 0) ? CC : comp_;
   const int i = blockIdx.x * SW_X + threadIdx.x + 1, j = blockIdx.y * SW_Y + threadIdx.y + 1;
   const int k = blockIdx.z + (comp == 2 ? 1 : 0);
   const int iend = (comp == 0) ? g.nx - 1 : g.nx;
@@ -198,7 +199,7 @@ struct MuColumn {
 template <int COMP>
 __device__ __forceinline__ Rec<float> mu_rec_of(const Geo &g, const MuCoef &s, const FcT<float> &f, int k, float b) {
   const float diag = 1.0f + s.ax2 * (f.px + f.mx) + s.ay2 * (f.py + f.my) + s.az2 * (f.pz + f.mz);
-  const float r = 1.0f / diag;
+  const float r = __fdividef(1.0f, diag);  // diag >= 1: the fast reciprocal is within 2 ulp
   float czp = s.az2 * f.pz * r, czm = s.az2 * f.mz * r;
   if (COMP != 2) {
     if (k == 0) {
@@ -248,10 +249,11 @@ __global__ void __launch_bounds__(SW_X *SW_Y)
 
 // 3-D checkerboard half-sweep (even iteration_time), one thread per point
 // of the colour.
-template <typename T, typename CS, int SW_X, int SW_Y>
+template <typename T, typename CS, int CC, int SW_X, int SW_Y>
 __global__ void __launch_bounds__(SW_X *SW_Y)
-    k_sor_even_c(int comp, Geo g, Helm h, T *__restrict__ x, const CS coef,
+    k_sor_even_c(int comp_, Geo g, Helm h, T *__restrict__ x, const CS coef,
                  const double *__restrict__ P, const double *__restrict__ X, int flg, int bc, int fuse) {
+  const int comp = (CC >= 0) ? CC : comp_;
   const int i2 = blockIdx.x * SW_X + threadIdx.x, j = blockIdx.y * SW_Y + threadIdx.y + 1;
   const int k = blockIdx.z + (comp == 2 ? 1 : 0);
   const int iend = (comp == 0) ? g.nx - 1 : g.nx;
@@ -325,10 +327,11 @@ __device__ __forceinline__ void sor_odd_produce(int comp, const Geo &g, const T 
   }
 }
 
-template <typename T, typename CS>
+template <typename T, typename CS, int CC>
 __global__ void __launch_bounds__(SO_T)
-    k_sor_odd_c2(int comp, Geo g, Helm h, T *__restrict__ x, const CS coef,
+    k_sor_odd_c2(int comp_, Geo g, Helm h, T *__restrict__ x, const CS coef,
                  const double *__restrict__ P, const double *__restrict__ X, int flg, int bc, int fuse) {
+  const int comp = (CC >= 0) ? CC : comp_;
   __shared__ T sA[2][SO_KZ][32], sB[2][SO_KZ][32];
   const int j = blockIdx.y + 1;
   const int iend = (comp == 0) ? g.nx - 1 : g.nx;
@@ -380,10 +383,11 @@ __global__ void __launch_bounds__(SO_T)
 // the result differs from the level-by-level order only by rounding (P
 // decays like (1.2 czm)^m, so x_in's contribution is weighted by it).
 // Shared memory: 2 (nlev + W) 32 values of T; W = 8 or 16 warps.
-template <typename T, typename CS, int SO3_W>
+template <typename T, typename CS, int CC, int SO3_W>
 __global__ void __launch_bounds__(SO3_W * 32)
-    k_sor_odd_c3(int comp, Geo g, Helm h, T *__restrict__ x, const CS coef,
+    k_sor_odd_c3(int comp_, Geo g, Helm h, T *__restrict__ x, const CS coef,
                  const double *__restrict__ P, const double *__restrict__ X, int flg, int bc, int fuse) {
+  const int comp = (CC >= 0) ? CC : comp_;
   extern __shared__ __align__(16) unsigned char so3_raw[];
   const int j = blockIdx.y + 1;
   const int iend = (comp == 0) ? g.nx - 1 : g.nx;
@@ -455,51 +459,56 @@ static size_t so3_smem(const Geo &g, int comp, int w) {
 }
 constexpr size_t SO3_SMEM_MAX = 200 * 1024;
 
-cudaError_t sweep_init() {
-  const int m = (int)SO3_SMEM_MAX;
-  cudaError_t e = cudaFuncSetAttribute(k_sor_odd_c3<double, const double *, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+template <typename T, typename CS, int CC>
+static cudaError_t so3_attr(int m) {
+  cudaError_t e = cudaFuncSetAttribute(k_sor_odd_c3<T, CS, CC, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_sor_odd_c3<double, const double *, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_sor_odd_c3<float, MuCoef, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_sor_odd_c3<float, MuCoef, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    e = cudaFuncSetAttribute(k_sor_odd_c3<T, CS, CC, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
   return e;
 }
 
-template <typename T, typename CS, int BX, int BY>
+cudaError_t sweep_init() {
+  const int m = (int)SO3_SMEM_MAX;
+  cudaError_t e = so3_attr<double, const double *, -1>(m);
+  if (e == cudaSuccess) e = so3_attr<float, MuCoef, 0>(m);
+  if (e == cudaSuccess) e = so3_attr<float, MuCoef, 1>(m);
+  if (e == cudaSuccess) e = so3_attr<float, MuCoef, 2>(m);
+  return e;
+}
+
+template <typename T, typename CS, int CC, int BX, int BY>
 static void jacobi_v(int comp, const Geo &g, const Helm &h, const T *xo, CS coef, const double *pres,
                      const double *X, T *x, int fuse, cudaStream_t st) {
   const int nk = (comp == 2) ? g.nz - 1 : g.nz;
   const int iend = (comp == 0) ? g.nx - 1 : g.nx;
   dim3 grd((iend + BX - 1) / BX, (g.ny + BY - 1) / BY, nk);
-  k_jacobi_c<T, CS, BX, BY><<<grd, dim3(BX, BY), 0, st>>>(comp, g, h, xo, coef, pres, X, x, fuse);
+  k_jacobi_c<T, CS, CC, BX, BY><<<grd, dim3(BX, BY), 0, st>>>(comp, g, h, xo, coef, pres, X, x, fuse);
 }
 
-template <typename T, typename CS>
+template <typename T, typename CS, int CC>
 static cudaError_t jacobi_c(int comp, const Geo &g, const Phys &ph, const T *xo, CS coef, const double *pres,
                             const double *X, T *x, int fuse, int tile, cudaStream_t st) {
   const Helm h = helm_of(ph);
   switch (tile) {
-    case 1: jacobi_v<T, CS, 32, 8>(comp, g, h, xo, coef, pres, X, x, fuse, st); break;
-    case 2: jacobi_v<T, CS, 64, 4>(comp, g, h, xo, coef, pres, X, x, fuse, st); break;
-    case 3: jacobi_v<T, CS, 16, 8>(comp, g, h, xo, coef, pres, X, x, fuse, st); break;
-    default: jacobi_v<T, CS, 32, 4>(comp, g, h, xo, coef, pres, X, x, fuse, st); break;
+    case 1: jacobi_v<T, CS, CC, 32, 8>(comp, g, h, xo, coef, pres, X, x, fuse, st); break;
+    case 2: jacobi_v<T, CS, CC, 64, 4>(comp, g, h, xo, coef, pres, X, x, fuse, st); break;
+    case 3: jacobi_v<T, CS, CC, 16, 8>(comp, g, h, xo, coef, pres, X, x, fuse, st); break;
+    default: jacobi_v<T, CS, CC, 32, 4>(comp, g, h, xo, coef, pres, X, x, fuse, st); break;
   }
   return cudaGetLastError();
 }
 
-template <typename T, typename CS, int BX, int BY>
+template <typename T, typename CS, int CC, int BX, int BY>
 static void even_v(int comp, const Geo &g, const Helm &h, T *x, CS coef, const double *pres, const double *X,
                    int flg, int bc, int fuse, cudaStream_t st) {
   const int iend = (comp == 0) ? g.nx - 1 : g.nx;
   const int npairs = (iend + 1) / 2;
   const int nk = (comp == 2) ? g.nz - 1 : g.nz;
   dim3 grd((npairs + BX - 1) / BX, (g.ny + BY - 1) / BY, nk);
-  k_sor_even_c<T, CS, BX, BY><<<grd, dim3(BX, BY), 0, st>>>(comp, g, h, x, coef, pres, X, flg, bc, fuse);
+  k_sor_even_c<T, CS, CC, BX, BY><<<grd, dim3(BX, BY), 0, st>>>(comp, g, h, x, coef, pres, X, flg, bc, fuse);
 }
 
-template <typename T, typename CS>
+template <typename T, typename CS, int CC>
 static cudaError_t sor_c(int comp, const Geo &g, const Phys &ph, T *x, CS coef, const double *pres,
                          const double *X, int flg, int iteration_time, int bc, int fuse, int tile_even,
                          int tile_odd, cudaStream_t st) {
@@ -508,10 +517,10 @@ static cudaError_t sor_c(int comp, const Geo &g, const Phys &ph, T *x, CS coef, 
   const Helm h = helm_of(ph);
   if (iteration_time % 2 == 0) {
     switch (tile_even) {
-      case 1: even_v<T, CS, 32, 8>(comp, g, h, x, coef, pres, X, flg, bc, fuse, st); break;
-      case 2: even_v<T, CS, 64, 4>(comp, g, h, x, coef, pres, X, flg, bc, fuse, st); break;
-      case 3: even_v<T, CS, 16, 8>(comp, g, h, x, coef, pres, X, flg, bc, fuse, st); break;
-      default: even_v<T, CS, 32, 4>(comp, g, h, x, coef, pres, X, flg, bc, fuse, st); break;
+      case 1: even_v<T, CS, CC, 32, 8>(comp, g, h, x, coef, pres, X, flg, bc, fuse, st); break;
+      case 2: even_v<T, CS, CC, 64, 4>(comp, g, h, x, coef, pres, X, flg, bc, fuse, st); break;
+      case 3: even_v<T, CS, CC, 16, 8>(comp, g, h, x, coef, pres, X, flg, bc, fuse, st); break;
+      default: even_v<T, CS, CC, 32, 4>(comp, g, h, x, coef, pres, X, flg, bc, fuse, st); break;
     }
   } else {
     dim3 grd((npairs + 31) / 32, g.ny, 1);
@@ -520,11 +529,11 @@ static cudaError_t sor_c(int comp, const Geo &g, const Phys &ph, T *x, CS coef, 
     const int w = (tile_odd == 1) ? 8 : ((tile_odd == 2) ? 16 : ((g.nz >= 128) ? 16 : 8));
     const size_t sm = so3_smem<T>(g, comp, w);
     if (sm <= SO3_SMEM_MAX && w == 16)
-      k_sor_odd_c3<T, CS, 16><<<grd, 16 * 32, sm, st>>>(comp, g, h, x, coef, pres, X, flg, bc, fuse);
+      k_sor_odd_c3<T, CS, CC, 16><<<grd, 16 * 32, sm, st>>>(comp, g, h, x, coef, pres, X, flg, bc, fuse);
     else if (sm <= SO3_SMEM_MAX)
-      k_sor_odd_c3<T, CS, 8><<<grd, 8 * 32, sm, st>>>(comp, g, h, x, coef, pres, X, flg, bc, fuse);
+      k_sor_odd_c3<T, CS, CC, 8><<<grd, 8 * 32, sm, st>>>(comp, g, h, x, coef, pres, X, flg, bc, fuse);
     else
-      k_sor_odd_c2<T, CS><<<grd, SO_T, 0, st>>>(comp, g, h, x, coef, pres, X, flg, bc, fuse);
+      k_sor_odd_c2<T, CS, CC><<<grd, SO_T, 0, st>>>(comp, g, h, x, coef, pres, X, flg, bc, fuse);
   }
   return cudaGetLastError();
 }
@@ -542,7 +551,7 @@ MuCoef mu_coef(const Phys &ph, const float *mu, const float *b) {
 
 cudaError_t launch_jacobi_c(int comp, const Geo &g, const Phys &ph, const double *xo, const double *coef,
                             const double *pres, double *x, int fuse, cudaStream_t st, const SweepTiles &t) {
-  return jacobi_c(comp, g, ph, xo, coef, pres, nullptr, x, fuse, t.jac, st);
+  return jacobi_c<double, const double *, -1>(comp, g, ph, xo, coef, pres, nullptr, x, fuse, t.jac, st);
 }
 constexpr int SW_K = 8;  // levels per thread of the column-marching FP32 Jacobi
 
@@ -571,7 +580,11 @@ cudaError_t launch_jacobi_c(int comp, const Geo &g, const Phys &ph, const float 
                             const SweepTiles &t) {
   // variants 0-3: one point per thread; 4-7: the same tiles marching
   // columns of SW_K levels (the same arithmetic, bit-identical results)
-  if (t.jac < SW_NV) return jacobi_c(comp, g, ph, xo, coef, pres, X, x, fuse, t.jac, st);
+  if (t.jac < SW_NV) {
+    if (comp == 0) return jacobi_c<float, MuCoef, 0>(comp, g, ph, xo, coef, pres, X, x, fuse, t.jac, st);
+    if (comp == 1) return jacobi_c<float, MuCoef, 1>(comp, g, ph, xo, coef, pres, X, x, fuse, t.jac, st);
+    return jacobi_c<float, MuCoef, 2>(comp, g, ph, xo, coef, pres, X, x, fuse, t.jac, st);
+  }
   const Helm h = helm_of(ph);
   const int v = t.jac - SW_NV;
   if (comp == 0) jacobi_m<0>(g, h, xo, coef, pres, X, x, fuse, v, st);
@@ -582,12 +595,17 @@ cudaError_t launch_jacobi_c(int comp, const Geo &g, const Phys &ph, const float 
 cudaError_t launch_sor_c(int comp, const Geo &g, const Phys &ph, double *x, const double *coef,
                          const double *pres, int flg, int iteration_time, int bc, int fuse, cudaStream_t st,
                          const SweepTiles &t) {
-  return sor_c(comp, g, ph, x, coef, pres, nullptr, flg, iteration_time, bc, fuse, t.even, t.odd, st);
+  return sor_c<double, const double *, -1>(comp, g, ph, x, coef, pres, nullptr, flg, iteration_time, bc, fuse, t.even,
+                                          t.odd, st);
 }
 cudaError_t launch_sor_c(int comp, const Geo &g, const Phys &ph, float *x, const MuCoef &coef,
                          const double *pres, const double *X, int flg, int iteration_time, int bc, int fuse,
                          cudaStream_t st, const SweepTiles &t) {
-  return sor_c(comp, g, ph, x, coef, pres, X, flg, iteration_time, bc, fuse, t.even, t.odd, st);
+  if (comp == 0)
+    return sor_c<float, MuCoef, 0>(comp, g, ph, x, coef, pres, X, flg, iteration_time, bc, fuse, t.even, t.odd, st);
+  if (comp == 1)
+    return sor_c<float, MuCoef, 1>(comp, g, ph, x, coef, pres, X, flg, iteration_time, bc, fuse, t.even, t.odd, st);
+  return sor_c<float, MuCoef, 2>(comp, g, ph, x, coef, pres, X, flg, iteration_time, bc, fuse, t.even, t.odd, st);
 }
 
 // defect form: d = -X before the first sweep (the sweeps start from x = 0),
