@@ -146,61 +146,28 @@ __device__ __forceinline__ void store_rec<float>(float *rec, float a0, float a1,
   o[1] = make_float4(a4, a5, a6, 0.f);
 }
 
-// With X (the FP64 state of the component; FP32-mixed sweeps in defect form)
-// the stored b is that of d = x - X: b + sum(c_n X_n) - X_c, in FP64 with the
-// unrounded coefficients (T), the neighbours taken as the sweeps take them.
-// The sweeps then solve x = sum(c~_n x_n) + b + sum((c_n - c~_n) X_n): the
-// FP32 rounding c~ of the coefficients acts only on d = x - X, not on x.
-template <typename T, typename TR>
-__device__ __forceinline__ void write_coef(int comp, const Geo &g, const Helm &h, const FcT<T> &f,
-                                           double rhs, int k, const double *__restrict__ X, int c,
-                                           TR *__restrict__ rec) {
-  const T ax2 = (T)h.ax2, ay2 = (T)h.ay2, az2 = (T)h.az2;
-  const T diag = (T)1 + ax2 * (f.px + f.mx) + ay2 * (f.py + f.my) + az2 * (f.pz + f.mz);
-  const T r = (T)1 / diag;
-  T czp = az2 * f.pz * r, czm = az2 * f.mz * r;
+// The record of one point of the FP64 sweeps.
+__device__ __forceinline__ void write_coef(int comp, const Geo &g, const Helm &h, const FcT<double> &f,
+                                           double rhs, int k, double *__restrict__ rec) {
+  const double ax2 = h.ax2, ay2 = h.ay2, az2 = h.az2;
+  const double diag = 1.0 + ax2 * (f.px + f.mx) + ay2 * (f.py + f.my) + az2 * (f.pz + f.mz);
+  const double r = 1.0 / diag;
+  double czp = az2 * f.pz * r, czm = az2 * f.mz * r;
   if (comp != 2) {
     if (k == 0) {
-      czp += czm * (T)(1.0 / 3.0);
-      czm = (T)(-2) * czm;
+      czp += czm * (1.0 / 3.0);
+      czm = -2.0 * czm;
     } else if (k == g.nz - 1) {
-      czm += czp * (T)(1.0 / 3.0);
-      czp = (T)(-2) * czp;
+      czm += czp * (1.0 / 3.0);
+      czp = -2.0 * czp;
     }
   }
-  const T exp_ = ax2 * f.px * r, exm = ax2 * f.mx * r, eyp = ay2 * f.py * r, eym = ay2 * f.my * r;
-  const TR cxp = (TR)exp_, cxm = (TR)exm, cyp = (TR)eyp, cym = (TR)eym, tzp = (TR)czp, tzm = (TR)czm;
-  TR b;
-  if (X) {
-    const int sy = g.sy, sz = g.sz;
-    const double xc = X[c];
-    double zpv, zmv;
-    if (comp == 2) {
-      zpv = X[c + sz];
-      zmv = X[c - sz];
-    } else {
-      zpv = (k == g.nz - 1) ? xc : X[c + sz];
-      zmv = (k == 0) ? xc : X[c - sz];
-    }
-    double bd = rhs * (double)r;
-    bd = fma((double)exp_, X[c + 1], bd);
-    bd = fma((double)exm, X[c - 1], bd);
-    bd = fma((double)eyp, X[c + sy], bd);
-    bd = fma((double)eym, X[c - sy], bd);
-    bd = fma((double)czp, zpv, bd);
-    bd = fma((double)czm, zmv, bd);
-    b = (TR)(bd - xc);
-  } else {
-    b = (TR)((T)rhs * r);
-  }
-  if constexpr (sizeof(TR) == sizeof(float)) rec[0] = b;  // FP32 sweeps recompute the coefficients
-  else store_rec<TR>(rec, cxp, cxm, cyp, cym, tzp, tzm, b);
+  store_rec<double>(rec, ax2 * f.px * r, ax2 * f.mx * r, ay2 * f.py * r, ay2 * f.my * r, czp, czm, rhs * r);
 }
 
-// X64 is the component's FP64 state (u2, v2 or w2): the right-hand side is
-// assembled in FP64 even when the stencils run in FP32 (T = float).
-// TR: storage of the sweep records (T, or float when FP64 stencils feed the
-// FP32 sweeps of the FP32-mixed form).
+// FP64 stencils.  TR = double: the FP64 form's right-hand side and 64-byte
+// sweep records (X64 = the component's FP64 state u2, v2 or w2); TR = float:
+// the FP32-mixed form with FP64 stencils, which stores the defect b alone.
 template <typename T, typename TR>
 __global__ void __launch_bounds__(MB_X *MB_Y)
     k_mom_rhs(int comp, Geo g, Phys ph, Helm hm, const T *__restrict__ U, const T *__restrict__ V,
@@ -208,7 +175,7 @@ __global__ void __launch_bounds__(MB_X *MB_Y)
               const T *__restrict__ fc, const double *__restrict__ c1, const double *__restrict__ c0,
               const double *__restrict__ s1, const double *__restrict__ s0, double *__restrict__ conv2,
               double *__restrict__ csf2, double *__restrict__ rhs, double *__restrict__ diff_out,
-              TR *__restrict__ coef, int defect) {
+              TR *__restrict__ coef) {
   const int i = blockIdx.x * MB_X + threadIdx.x + 1, j = blockIdx.y * MB_Y + threadIdx.y + 1;
   const int k = blockIdx.z;
   if (i > g.nx || j > g.ny) return;
@@ -218,26 +185,41 @@ __global__ void __launch_bounds__(MB_X *MB_Y)
   FcT<T> f;
   if (valid) {
     f = faces(comp, g, mu, i, j, k);
-    cd = conv_diff<T>(comp, g, (T)(1.0 / ph.dx), (T)(1.0 / ph.dy), (T)(1.0 / ph.dz), U, V, W, f, i, j, k);
+    // 1/dx, 1/dy, 1/dz from the host (the same IEEE quotients, not three FP64
+    // divisions per point on GB300's FP64 pipe)
+    cd = conv_diff<T>(comp, g, (T)hm.rdx, (T)hm.rdy, (T)hm.rdz, U, V, W, f, i, j, k);
   }
   // main_ns_hybrid.F90:629-641 face averages of the CSF force
   double s2;
   if (comp == 0) s2 = ((double)fc[TPLS_IDX(g, i + 1, j + 1, k + 1)] + (double)fc[TPLS_IDX(g, i, j + 1, k + 1)]) * 0.5;
   else if (comp == 1) s2 = ((double)fc[TPLS_IDX(g, i, j + 1, k + 1)] + (double)fc[TPLS_IDX(g, i, j, k + 1)]) * 0.5;
   else s2 = ((double)fc[TPLS_IDX(g, i, j + 1, k + 1)] + (double)fc[TPLS_IDX(g, i, j + 1, k)]) * 0.5;
-  const double X = X64[c];
   const double dt = ph.dt, conv = (double)cd.conv, diff = (double)cd.diff;
-  // main_ns_hybrid.F90:743-751 (AB3 convection and CSF, CN diffusion)
-  const double r = X - dt * ((23.0 / 12.0) * conv - (4.0 / 3.0) * c1[c] + (5.0 / 12.0) * c0[c]) +
-                   (dt / 2.0) * diff +
-                   dt * ((23.0 / 12.0) * s2 - (4.0 / 3.0) * s1[c] + (5.0 / 12.0) * s0[c]);
-  conv2[c] = conv;
-  csf2[c] = s2;
-  if (rhs) rhs[c] = r;
-  if (diff_out) diff_out[c] = diff;
-  if (coef && valid)
-    write_coef<T, TR>(comp, g, hm, f, r, k, defect ? X64 : nullptr, c,
-                      coef + (sizeof(TR) == sizeof(float) ? 1 : 8) * (size_t)rec_slot(g, c, i));
+  if constexpr (sizeof(TR) == sizeof(float)) {
+    // FP32 defect-form sweeps: b = R / diag with R = dt (diff - AB3(conv) +
+    // AB3(csf)), the defect equation's right-hand side (see k_mom_rhs_pair),
+    // here in FP64; the sweeps rebuild the coefficients themselves
+    conv2[c] = conv;
+    csf2[c] = s2;
+    if (coef && valid) {
+      const double abc = (23.0 / 12.0) * conv - (4.0 / 3.0) * c1[c] + (5.0 / 12.0) * c0[c];
+      const double abs_ = (23.0 / 12.0) * s2 - (4.0 / 3.0) * s1[c] + (5.0 / 12.0) * s0[c];
+      const double diag =
+          1.0 + hm.ax2 * (f.px + f.mx) + hm.ay2 * (f.py + f.my) + hm.az2 * (f.pz + f.mz);
+      coef[rec_slot(g, c, i)] = (TR)(dt * (diff - abc + abs_) / diag);
+    }
+  } else {
+    const double X = X64[c];
+    // main_ns_hybrid.F90:743-751 (AB3 convection and CSF, CN diffusion)
+    const double r = X - dt * ((23.0 / 12.0) * conv - (4.0 / 3.0) * c1[c] + (5.0 / 12.0) * c0[c]) +
+                     (dt / 2.0) * diff +
+                     dt * ((23.0 / 12.0) * s2 - (4.0 / 3.0) * s1[c] + (5.0 / 12.0) * s0[c]);
+    conv2[c] = conv;
+    csf2[c] = s2;
+    if (rhs) rhs[c] = r;
+    if (diff_out) diff_out[c] = diff;
+    if (coef && valid) write_coef(comp, g, hm, f, r, k, coef + 8 * (size_t)rec_slot(g, c, i));
+  }
 }
 
 template <typename T, typename TR = T>
@@ -247,10 +229,8 @@ static cudaError_t mom_rhs(int comp, const Geo &g, const Phys &ph, const T *u2, 
                            double *diff_out, TR *coef, cudaStream_t st) {
   const int nk = (comp == 2) ? g.nz + 1 : g.nz;
   dim3 grd((g.nx + MB_X - 1) / MB_X, (g.ny + MB_Y - 1) / MB_Y, nk);
-  // FP32 records feed the defect-form FP32 sweeps
-  const int defect = (sizeof(TR) == sizeof(float)) ? 1 : 0;
   k_mom_rhs<T, TR><<<grd, dim3(MB_X, MB_Y), 0, st>>>(comp, g, ph, helm_of(ph), u2, v2, w2, x64, mu, fcsf, c1,
-                                                     c0, s1, s0, conv2, csf2, rhs, diff_out, coef, defect);
+                                                     c0, s1, s0, conv2, csf2, rhs, diff_out, coef);
   return cudaGetLastError();
 }
 

@@ -12,6 +12,7 @@ struct Helm {
   double ax2, ay2, az2;  // dt/(2 d^2)
   double dtdx;           // dt/dx (u outlet condition)
   float dtdxf;           // the same, rounded, for the FP32 defect-form sweeps
+  double rdx, rdy, rdz;  // 1/dx, 1/dy, 1/dz
 };
 
 template <typename T>
@@ -188,6 +189,9 @@ static inline Helm helm_of(const Phys &ph) {
   h.az2 = (ph.dt / (ph.dz * ph.dz)) / 2.0;
   h.dtdx = ph.dt / ph.dx;
   h.dtdxf = (float)h.dtdx;
+  h.rdx = 1.0 / ph.dx;
+  h.rdy = 1.0 / ph.dy;
+  h.rdz = 1.0 / ph.dz;
   return h;
 }
 
