@@ -169,6 +169,9 @@ def run_gpu(args, ws, rank, local) -> dict | None:
     cells = nx * ny * nz
     g = TplsGpu(nx, ny, nz, params, uin)
     g.set_state(st)
+    # the library's sweep-tile autotuner, on request (results do not depend on
+    # its choice; timed on single kernels, it can pick tiles slower in the step)
+    tiles = g.autotune(5) if args.autotune else None
     rc = g.step(args.warmup)
     g.sync()
     if rc != 0:
@@ -275,6 +278,7 @@ def run_gpu(args, ws, rank, local) -> dict | None:
                    "mom_uvw": params.mom_u, "levelset": params.levelset, "p_rtol": params.p_rtol,
                    "precision": "fp64" if precision == 0 else "fp32-mixed",
                    "fp64_parts": parts,
+                   "sweep_tiles": tiles,
                    "parallelism": f"{ws} independent replica(s), no sharding",
                    "l2": f"working set ~{cells * 500 / 1e9:.0f} GB per step >> 129 MB L2 (no flush needed)",
                    "launch": "one CUDA graph per step (device-side WHILE node for the pressure CG)",
@@ -628,6 +632,7 @@ def main():
                     help="resize the workload (small cases for profiling captures)")
     ap.add_argument("--jobs", type=int, default=16)
     ap.add_argument("--rate", type=float, default=1.0)
+    ap.add_argument("--autotune", action="store_true", help="run the sweep-tile autotuner before timing")
     ap.add_argument("--accuracy", type=int, default=0, metavar="STEPS",
                     help="instead of timing: step the FP64 and FP32-mixed forms side by side for STEPS "
                          "steps and print their differences (one JSON line)")

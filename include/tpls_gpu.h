@@ -137,9 +137,7 @@ int tpls_step_async(tpls_ctx *ctx, int nsteps);
  * rebuilt at the next step (batches included).  The state a run produces
  * does not depend on the choice (same arithmetic per point). */
 int tpls_autotune(tpls_ctx *ctx, int reps);
-/* tiles3 = {Jacobi variant 0..3 (0..7 for the FP32 sweeps of the FP32-mixed
-   form: 4..7 are the same shapes marching columns of levels), even shape 0..3,
-   odd chunking 0..2} */
+/* tiles3 = {Jacobi shape 0..3, even shape 0..3, odd chunking 0..2} */
 int tpls_get_tiles(const tpls_ctx *ctx, int *tiles3);
 
 /* ---- job-serving helpers (no counterpart in the reference) ------------ */

@@ -115,138 +115,6 @@ __global__ void __launch_bounds__(SW_X *SW_Y)
   if (edge) jacobi_bc(comp, g, h, x, X, P, i, j, k, v, fuse);
 }
 
-// Face viscosities of one (i, j) column of component COMP, marching up in
-// k: a level loads only the viscosity values of its new plane and keeps the
-// planes below in registers.  The sums keep the operand order of faces(),
-// so the coefficients are bit for bit those of get_rec.
-template <int COMP>
-struct MuColumn {
-  const float *m;  // mu at (i, j+1, k+1) for u and v, (i, j+1, k) for w
-  int sy, sz;
-  float p0, q0, p1, q1;  // u, v: the pair summed first on planes k and k+1
-  float c0, e0, w0, n0, s0;  // w: plane k's centre, x and y neighbours
-  __device__ __forceinline__ void start(const Geo &g, const float *mu, int i, int j, int k) {
-    sy = g.sy;
-    sz = g.szm;
-    if (COMP == 0) {
-      m = mu + TPLS_IDXM(g, i, j + 1, k + 1);
-      p0 = m[-sz];
-      q0 = m[1 - sz];
-      p1 = m[0];
-      q1 = m[1];
-    } else if (COMP == 1) {
-      m = mu + TPLS_IDXM(g, i, j + 1, k + 1);
-      p0 = m[-sz];
-      q0 = m[-sz - sy];
-      p1 = m[0];
-      q1 = m[-sy];
-    } else {
-      m = mu + TPLS_IDXM(g, i, j + 1, k);
-      c0 = m[0];
-      e0 = m[1];
-      w0 = m[-1];
-      n0 = m[sy];
-      s0 = m[-sy];
-    }
-  }
-  // faces of the current level, then advance to the next
-  __device__ __forceinline__ FcT<float> next() {
-    FcT<float> f;
-    if (COMP == 0) {
-      const float a = p1, b = q1, c = m[sz], d = m[1 + sz];
-      f.px = b;
-      f.mx = a;
-      f.py = (a + b + m[sy] + m[1 + sy]) * 0.25f;
-      f.my = (a + b + m[-sy] + m[1 - sy]) * 0.25f;
-      f.pz = (a + b + c + d) * 0.25f;
-      f.mz = (a + b + p0 + q0) * 0.25f;
-      p0 = a;
-      q0 = b;
-      p1 = c;
-      q1 = d;
-    } else if (COMP == 1) {
-      const float a = p1, b = q1, c = m[sz], d = m[sz - sy];
-      f.px = (a + b + m[1] + m[1 - sy]) * 0.25f;
-      f.mx = (a + b + m[-1] + m[-1 - sy]) * 0.25f;
-      f.py = a;
-      f.my = b;
-      f.pz = (a + b + c + d) * 0.25f;
-      f.mz = (a + b + p0 + q0) * 0.25f;
-      p0 = a;
-      q0 = b;
-      p1 = c;
-      q1 = d;
-    } else {
-      const float a = c0, b = m[sz], e1 = m[1 + sz], w1 = m[-1 + sz], n1 = m[sy + sz], s1 = m[-sy + sz];
-      f.px = (a + b + e0 + e1) * 0.25f;
-      f.mx = (a + b + w0 + w1) * 0.25f;
-      f.py = (a + b + n0 + n1) * 0.25f;
-      f.my = (a + b + s0 + s1) * 0.25f;
-      f.pz = b;
-      f.mz = a;
-      c0 = b;
-      e0 = e1;
-      w0 = w1;
-      n0 = n1;
-      s0 = s1;
-    }
-    m += sz;
-    return f;
-  }
-};
-
-// get_rec's coefficients from the faces of a level
-template <int COMP>
-__device__ __forceinline__ Rec<float> mu_rec_of(const Geo &g, const MuCoef &s, const FcT<float> &f, int k, float b) {
-  const float diag = 1.0f + s.ax2 * (f.px + f.mx) + s.ay2 * (f.py + f.my) + s.az2 * (f.pz + f.mz);
-  const float r = __fdividef(1.0f, diag);  // diag >= 1: the fast reciprocal is within 2 ulp
-  float czp = s.az2 * f.pz * r, czm = s.az2 * f.mz * r;
-  if (COMP != 2) {
-    if (k == 0) {
-      czp += czm * (float)(1.0 / 3.0);
-      czm = -2.0f * czm;
-    } else if (k == g.nz - 1) {
-      czm += czp * (float)(1.0 / 3.0);
-      czp = -2.0f * czp;
-    }
-  }
-  Rec<float> q = {s.ax2 * f.px * r, s.ax2 * f.mx * r, s.ay2 * f.py * r, s.ay2 * f.my * r, czp, czm, b};
-  return q;
-}
-
-// FP32 Jacobi (defect form) marching a column of SW_K levels per thread:
-// the same update and boundary rows as k_jacobi_c, with the viscosity and
-// the x values of the planes below carried in registers.
-template <int COMP, int SW_X, int SW_Y, int SW_K>
-__global__ void __launch_bounds__(SW_X *SW_Y)
-    k_jacobi_m(Geo g, Helm h, const float *__restrict__ xo, const MuCoef s, const double *__restrict__ P,
-               const double *__restrict__ X, float *__restrict__ x, int fuse) {
-  const int i = blockIdx.x * SW_X + threadIdx.x + 1, j = blockIdx.y * SW_Y + threadIdx.y + 1;
-  const int klo = (COMP == 2) ? 1 : 0, khi = g.nz - 1;  // the component's levels
-  const int kb = klo + blockIdx.z * SW_K, ke = min(kb + SW_K - 1, khi);
-  const int iend = (COMP == 0) ? g.nx - 1 : g.nx;
-  if (i > iend || j > g.ny) return;
-  const int sy = g.sy, sz = g.sz;
-  MuColumn<COMP> mc;
-  mc.start(g, s.mu, i, j, kb);
-  int c = TPLS_IDX(g, i, j, kb);
-  float xc = xo[c];
-  float xm = (COMP == 2 || kb > 0) ? xo[c - sz] : xc;
-#pragma unroll 1
-  for (int k = kb; k <= ke; k++, c += sz) {
-    const FcT<float> f = mc.next();
-    const Rec<float> q = mu_rec_of<COMP>(g, s, f, k, __ldg(s.b + rec_slot(g, c, i)));
-    const float xp = (COMP != 2 && k == g.nz - 1) ? xc : xo[c + sz];
-    const float zm = (COMP != 2 && k == 0) ? xc : xm;
-    const float v = rec_apply(q, xo[c + 1], xo[c - 1], xo[c + sy], xo[c - sy], xp, zm);
-    put(g, x, i, j, k, v, fuse);
-    const bool edge = (i == 1) || (i >= g.nx - 1) || (COMP == 2 && (k == 1 || k == g.nz - 1));
-    if (edge) jacobi_bc(COMP, g, h, x, X, P, i, j, k, v, fuse);
-    xm = xc;
-    xc = xp;
-  }
-}
-
 // 3-D checkerboard half-sweep (even iteration_time), one thread per point
 // of the colour.
 template <typename T, typename CS, int CC, int SW_X, int SW_Y>
@@ -553,44 +421,12 @@ cudaError_t launch_jacobi_c(int comp, const Geo &g, const Phys &ph, const double
                             const double *pres, double *x, int fuse, cudaStream_t st, const SweepTiles &t) {
   return jacobi_c<double, const double *, -1>(comp, g, ph, xo, coef, pres, nullptr, x, fuse, t.jac, st);
 }
-constexpr int SW_K = 8;  // levels per thread of the column-marching FP32 Jacobi
-
-template <int COMP, int BX, int BY>
-static void jacobi_m_v(const Geo &g, const Helm &h, const float *xo, const MuCoef &s, const double *pres,
-                       const double *X, float *x, int fuse, cudaStream_t st) {
-  const int nlev = (COMP == 2) ? g.nz - 1 : g.nz;
-  const int iend = (COMP == 0) ? g.nx - 1 : g.nx;
-  dim3 grd((iend + BX - 1) / BX, (g.ny + BY - 1) / BY, (nlev + SW_K - 1) / SW_K);
-  k_jacobi_m<COMP, BX, BY, SW_K><<<grd, dim3(BX, BY), 0, st>>>(g, h, xo, s, pres, X, x, fuse);
-}
-
-template <int COMP>
-static void jacobi_m(const Geo &g, const Helm &h, const float *xo, const MuCoef &s, const double *pres,
-                     const double *X, float *x, int fuse, int tile, cudaStream_t st) {
-  switch (tile) {
-    case 1: jacobi_m_v<COMP, 32, 8>(g, h, xo, s, pres, X, x, fuse, st); break;
-    case 2: jacobi_m_v<COMP, 64, 4>(g, h, xo, s, pres, X, x, fuse, st); break;
-    case 3: jacobi_m_v<COMP, 16, 8>(g, h, xo, s, pres, X, x, fuse, st); break;
-    default: jacobi_m_v<COMP, 32, 4>(g, h, xo, s, pres, X, x, fuse, st); break;
-  }
-}
-
 cudaError_t launch_jacobi_c(int comp, const Geo &g, const Phys &ph, const float *xo, const MuCoef &coef,
                             const double *pres, const double *X, float *x, int fuse, cudaStream_t st,
                             const SweepTiles &t) {
-  // variants 0-3: one point per thread; 4-7: the same tiles marching
-  // columns of SW_K levels (the same arithmetic, bit-identical results)
-  if (t.jac < SW_NV) {
-    if (comp == 0) return jacobi_c<float, MuCoef, 0>(comp, g, ph, xo, coef, pres, X, x, fuse, t.jac, st);
-    if (comp == 1) return jacobi_c<float, MuCoef, 1>(comp, g, ph, xo, coef, pres, X, x, fuse, t.jac, st);
-    return jacobi_c<float, MuCoef, 2>(comp, g, ph, xo, coef, pres, X, x, fuse, t.jac, st);
-  }
-  const Helm h = helm_of(ph);
-  const int v = t.jac - SW_NV;
-  if (comp == 0) jacobi_m<0>(g, h, xo, coef, pres, X, x, fuse, v, st);
-  else if (comp == 1) jacobi_m<1>(g, h, xo, coef, pres, X, x, fuse, v, st);
-  else jacobi_m<2>(g, h, xo, coef, pres, X, x, fuse, v, st);
-  return cudaGetLastError();
+  if (comp == 0) return jacobi_c<float, MuCoef, 0>(comp, g, ph, xo, coef, pres, X, x, fuse, t.jac, st);
+  if (comp == 1) return jacobi_c<float, MuCoef, 1>(comp, g, ph, xo, coef, pres, X, x, fuse, t.jac, st);
+  return jacobi_c<float, MuCoef, 2>(comp, g, ph, xo, coef, pres, X, x, fuse, t.jac, st);
 }
 cudaError_t launch_sor_c(int comp, const Geo &g, const Phys &ph, double *x, const double *coef,
                          const double *pres, int flg, int iteration_time, int bc, int fuse, cudaStream_t st,

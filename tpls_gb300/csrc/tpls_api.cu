@@ -1054,8 +1054,7 @@ int tpls_autotune(tpls_ctx *c, int reps) {
   SweepTiles best = c->tiles;
   // The odd half-sweep's chunking changes its rounding, so it is not tuned:
   // a result must not depend on the tile shapes chosen.
-  // FP32 Jacobi: four column-marching and four point-per-thread variants
-  const int ncand[2] = {f32 ? 8 : 4, 4};
+  const int ncand[2] = {4, 4};
   cudaError_t err = cudaSuccess;
   for (int kind = 0; kind < 2 && err == cudaSuccess; kind++) {
     float tbest = 1e30f;
