@@ -271,6 +271,7 @@ __device__ __forceinline__ F2 ld2(const double *__restrict__ p) { return split_b
 // float constants of one step (computed on the host in FP64, then rounded)
 struct MomF {
   float rdx, rdy, rdz, dt, ax2, ay2, az2;
+  double dt64;
 };
 
 // get_conv_all / get_diffusion_all point forms (momentum_allflux.f90:22-471)
@@ -363,20 +364,22 @@ __device__ __forceinline__ CDT<float> conv_diff_pair(int comp, const Geo &g, con
   return r;
 }
 
-// Right-hand side of the FP32-mixed form's sweeps, with no FP64 arithmetic.
+// Right-hand side of the FP32-mixed form's sweeps with FP32 stencils.
 // The sweeps solve for the defect d = x - X (X the FP64 state of the
 // component): with diag x - sum(a_n x_n) = rhs and diag = 1 + sum(a_n), the
 // defect equation's right-hand side is
 //   R = (rhs - X) + sum(a_n (X_n - X)) = dt (diff - AB3(conv) + AB3(csf)),
 // because sum(a_n (X_n - X)) = (dt/2) diff for the same ghost-substituted
-// neighbours (main_ns_hybrid.F90:743-751 for rhs).  R is a small quantity,
-// so its FP32 rounding acts on the step's increment, not on |u|.  Stored:
-// b = R / diag, one float per point in record-slot order (the sweeps
-// recompute the coefficients from mu).  The AB3 histories are read and
-// written as FP64 arrays holding FP32 values.
+// neighbours (main_ns_hybrid.F90:743-751 for rhs).  conv and diff come from
+// the FP32 pair stencils; the CSF force, the AB3 histories and R stay FP64
+// (eleven FP64 operations per point): the CSF force is large at the
+// interface, where it is balanced by the pressure gradient outside R, so its
+// rounding is not relative to the step's increment.  Stored: b = R / diag,
+// one float per point in record-slot order (the sweeps recompute the
+// coefficients from mu).  conv is stored into its FP64 history exactly.
 __global__ void __launch_bounds__(MB_X *MB_Y)
     k_mom_rhs_pair(int comp, Geo g, MomF m, const double *__restrict__ U, const double *__restrict__ V,
-                   const double *__restrict__ W, const float *__restrict__ mu, const float *__restrict__ fc,
+                   const double *__restrict__ W, const float *__restrict__ mu, const double *__restrict__ fc,
                    const double *__restrict__ c1, const double *__restrict__ c0, const double *__restrict__ s1,
                    const double *__restrict__ s0, double *__restrict__ conv2, double *__restrict__ csf2,
                    float *__restrict__ bdef) {
@@ -392,22 +395,23 @@ __global__ void __launch_bounds__(MB_X *MB_Y)
     cd = conv_diff_pair(comp, g, m, U, V, W, f, i, j, k);
   }
   // main_ns_hybrid.F90:629-641 face averages of the CSF force
-  float s2;
-  if (comp == 0) s2 = (fc[TPLS_IDX(g, i + 1, j + 1, k + 1)] + fc[TPLS_IDX(g, i, j + 1, k + 1)]) * 0.5f;
-  else if (comp == 1) s2 = (fc[TPLS_IDX(g, i, j + 1, k + 1)] + fc[TPLS_IDX(g, i, j, k + 1)]) * 0.5f;
-  else s2 = (fc[TPLS_IDX(g, i, j + 1, k + 1)] + fc[TPLS_IDX(g, i, j + 1, k)]) * 0.5f;
-  const float a23 = (float)(23.0 / 12.0), a43 = (float)(4.0 / 3.0), a512 = (float)(5.0 / 12.0);
-  const float abc = a23 * cd.conv - a43 * round_bits(c1[c]) + a512 * round_bits(c0[c]);
-  const float abs_ = a23 * s2 - a43 * round_bits(s1[c]) + a512 * round_bits(s0[c]);
-  conv2[c] = widen_bits(cd.conv);
-  csf2[c] = widen_bits(s2);
+  double s2;
+  if (comp == 0) s2 = (fc[TPLS_IDX(g, i + 1, j + 1, k + 1)] + fc[TPLS_IDX(g, i, j + 1, k + 1)]) * 0.5;
+  else if (comp == 1) s2 = (fc[TPLS_IDX(g, i, j + 1, k + 1)] + fc[TPLS_IDX(g, i, j, k + 1)]) * 0.5;
+  else s2 = (fc[TPLS_IDX(g, i, j + 1, k + 1)] + fc[TPLS_IDX(g, i, j + 1, k)]) * 0.5;
+  const double conv = widen_bits(cd.conv);
+  conv2[c] = conv;
+  csf2[c] = s2;
   if (!valid) return;
+  const double abc = (23.0 / 12.0) * conv - (4.0 / 3.0) * c1[c] + (5.0 / 12.0) * c0[c];
+  const double abs_ = (23.0 / 12.0) * s2 - (4.0 / 3.0) * s1[c] + (5.0 / 12.0) * s0[c];
+  const double R = m.dt64 * (widen_bits(cd.diff) - abc + abs_);
   const float diag = 1.0f + m.ax2 * (f.px + f.mx) + m.ay2 * (f.py + f.my) + m.az2 * (f.pz + f.mz);
-  bdef[rec_slot(g, c, i)] = m.dt * (cd.diff - abc + abs_) / diag;
+  bdef[rec_slot(g, c, i)] = round_bits(R) / diag;
 }
 
 cudaError_t launch_mom_rhs_pair(int comp, const Geo &g, const Phys &ph, const double *u2, const double *v2,
-                                const double *w2, const float *mu, const float *fcsf, const double *c1,
+                                const double *w2, const float *mu, const double *fcsf, const double *c1,
                                 const double *c0, const double *s1, const double *s0, double *conv2,
                                 double *csf2, float *bdef, cudaStream_t st) {
   const Helm hm = helm_of(ph);
@@ -416,6 +420,7 @@ cudaError_t launch_mom_rhs_pair(int comp, const Geo &g, const Phys &ph, const do
   m.rdy = (float)(1.0 / ph.dy);
   m.rdz = (float)(1.0 / ph.dz);
   m.dt = (float)ph.dt;
+  m.dt64 = ph.dt;
   m.ax2 = (float)hm.ax2;
   m.ay2 = (float)hm.ay2;
   m.az2 = (float)hm.az2;

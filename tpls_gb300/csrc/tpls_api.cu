@@ -45,7 +45,7 @@ struct tpls_ctx {
   // FP32-mixed form: FP32 copies of the step inputs and FP32 work arrays
   // (the state above stays FP64)
   int mixed = 0;
-  float *phi32, *u32, *v32, *w32, *mu32, *D32, *fx32, *fy32, *fz32;
+  float *phi32, *u32, *v32, *w32, *mu32, *D32;
   float *ffh[2], *ffl[2];  // float-pair redistancing iterates (hi, lo), ping-pong
   float *bdef[3];  // FP32-mixed: defect b of the FP32 sweeps (one float per point)
   float *x3f[3][2];
@@ -371,10 +371,10 @@ static int create_impl(int nx, int ny, int nz, const tpls_params *prm, const dou
       TCK(alloc_p(c, &c->phiB));
       TCK(alloc_p(c, &c->D));
     }
-    if (parts & (TPLS_PART_MOMENTUM | TPLS_PART_MOM_STENCIL)) {  // FP64 stencil inputs
+    {  // FP64 CSF force (every setting); FP64 viscosity for FP64 stencils
       double **pf2[] = {&c->fx, &c->fy, &c->fz};
       for (double **p : pf2) TCK(alloc_p(c, p));
-      TCK(alloc_field(c, 1, ny + 4, nz + 2, &c->mu));
+      if (parts & (TPLS_PART_MOMENTUM | TPLS_PART_MOM_STENCIL)) TCK(alloc_field(c, 1, ny + 4, nz + 2, &c->mu));
     }
     // FP64 u3, v3, w3 (the defect-form result, or the FP64 momentum iterates)
     TCK(alloc_field(c, 0, ny + 2, nz, &c->x3[0][0]));
@@ -393,8 +393,7 @@ static int create_impl(int nx, int ny, int nz, const tpls_params *prm, const dou
         c->coef[q] = (double *)b;
       }
     }
-    float **qf[] = {&c->phi32, &c->D32, &c->fx32, &c->fy32, &c->fz32, &c->ffh[0], &c->ffl[0], &c->ffh[1],
-                    &c->ffl[1]};
+    float **qf[] = {&c->phi32, &c->D32, &c->ffh[0], &c->ffl[0], &c->ffh[1], &c->ffl[1]};
     for (float **p : qf) TCK(alloc_p(c, p));
     float **quv[] = {&c->u32, &c->v32, &c->x3f[0][0], &c->x3f[0][1], &c->x3f[1][0], &c->x3f[1][1]};
     for (float **p : quv) TCK(alloc_field(c, 0, ny + 2, nz, p));
@@ -474,11 +473,11 @@ long long tpls_footprint_bytes(int nx, int ny, int nz, int precision) {
     t += 5 * round_alloc(D * np) + 4 * round_alloc(D * nuv) + 2 * round_alloc(D * nw);
     t += 2 * round_alloc(D * nrec * nz) + round_alloc(D * nrec * (nz + 1)) + round_alloc(D * nmu);
   } else {
-    t += 9 * round_alloc(F * np) + 6 * round_alloc(F * nuv) + 3 * round_alloc(F * nw);
+    t += 6 * round_alloc(F * np) + 6 * round_alloc(F * nuv) + 3 * round_alloc(F * nw);
     t += 2 * round_alloc(F * (nrec / 8) * nz) + round_alloc(F * (nrec / 8) * (nz + 1)) + round_alloc(F * nmu);
     t += 2 * round_alloc(D * nuv) + round_alloc(D * nw);  // FP64 u3, v3, w3
-    // FP64 momentum-stencil inputs (CSF force, viscosity) of TPLS_PART_MOM_STENCIL,
-    // the setting served and batched jobs use; counted for every mixed context
+    // FP64 CSF force, and the FP64 viscosity of TPLS_PART_MOM_STENCIL (the
+    // setting served and batched jobs use; counted for every mixed context)
     t += 3 * round_alloc(D * np) + round_alloc(D * nmu);
   }
   t += round_alloc(px * (ny + 2) * (nz + 2) + 64) + round_alloc(D * nz) + round_alloc(D * nx * ny);
@@ -865,15 +864,15 @@ static int step_once_mixed(tpls_ctx *c) {
   } else {
     {
       PhaseScope ps(c, TPLS_T_CSF);
-      LCK(c, launch_csf(g, ph, c->phi2, c->fx32, c->fy32, c->fz32, st));
+      LCK(c, launch_csf(g, ph, c->phi2, c->fx, c->fy, c->fz, st));
     }
     {
       PhaseScope ps(c, TPLS_T_MOM_RHS);
-      LCK(c, launch_mom_rhs_pair(0, g, ph, c->u2, c->v2, c->w2, c->mu32, c->fx32, c->conv_u[s1], c->conv_u[s0],
+      LCK(c, launch_mom_rhs_pair(0, g, ph, c->u2, c->v2, c->w2, c->mu32, c->fx, c->conv_u[s1], c->conv_u[s0],
                                  c->csf_u[s1], c->csf_u[s0], c->conv_u[s2], c->csf_u[s2], c->bdef[0], st));
-      LCK(c, launch_mom_rhs_pair(1, g, ph, c->u2, c->v2, c->w2, c->mu32, c->fy32, c->conv_v[s1], c->conv_v[s0],
+      LCK(c, launch_mom_rhs_pair(1, g, ph, c->u2, c->v2, c->w2, c->mu32, c->fy, c->conv_v[s1], c->conv_v[s0],
                                  c->csf_v[s1], c->csf_v[s0], c->conv_v[s2], c->csf_v[s2], c->bdef[1], st));
-      LCK(c, launch_mom_rhs_pair(2, g, ph, c->u2, c->v2, c->w2, c->mu32, c->fz32, c->conv_w[s1], c->conv_w[s0],
+      LCK(c, launch_mom_rhs_pair(2, g, ph, c->u2, c->v2, c->w2, c->mu32, c->fz, c->conv_w[s1], c->conv_w[s0],
                                  c->csf_w[s1], c->csf_w[s0], c->conv_w[s2], c->csf_w[s2], c->bdef[2], st));
     }
     if ((s = sweeps32(c))) return s;

@@ -81,13 +81,13 @@ cudaError_t launch_mom_rhs(int comp, const Geo &g, const Phys &ph,
                            double *rhs, double *diff_out, double *coef,
                            cudaStream_t st);
 // FP32-mixed form: FP32 stencils on the FP64 velocity state split into
-// FP32 pairs by integer operations, FP32 viscosity and CSF force; writes the
-// defect-form b of the FP32 sweeps (one float per point, rec_slot order)
-// and the AB3 histories.
+// FP32 pairs by integer operations and FP32 viscosity, FP64 CSF force and
+// AB3 combination; writes the defect-form b of the FP32 sweeps (one float
+// per point, rec_slot order) and the AB3 histories.
 cudaError_t launch_mom_rhs_pair(int comp, const Geo &g, const Phys &ph,
                                 const double *u2, const double *v2,
                                 const double *w2, const float *mu,
-                                const float *fcsf, const double *c1,
+                                const double *fcsf, const double *c1,
                                 const double *c0, const double *s1,
                                 const double *s0, double *conv2, double *csf2,
                                 float *coef, cudaStream_t st);
