@@ -1,9 +1,11 @@
 #!/usr/bin/env python
 """Throughput of the TPLS per-timestep hot path on GB300.
 
-Default workload: the plain FP64 form on the 256x128x192 channel (m=2,
-Re=200, 4-mode seeded interface, mom_u/v/w = 30, levelset = 10, PETSc's
-default pressure rtol 1e-5), K timed steps after W warm-up steps.
+Default workload: the FP64 form on the 256x128x192 channel (m=2, Re=200,
+4-mode seeded interface, mom_u/v/w = 30, levelset = 10, PETSc's default
+pressure rtol 1e-5), K timed steps after W warm-up steps.  The FP64 form's
+CG preconditioner runs its multigrid levels in FP32 (tpls_params.mg_fp32;
+--mg-fp64 for FP64 levels): CG, its residuals and the solution stay FP64.
 
 Arms
   (default) the CUDA library through its C ABI, device-resident state;
@@ -165,7 +167,7 @@ def run_gpu(args, ws, rank, local) -> dict | None:
     parts = args.fp64_parts if precision == 1 else 0
     nx, ny, nz = args.grid if args.grid else (w.nx, w.ny, w.nz)
     params, uin, st = make_case(args.config, nx=nx, ny=ny, nz=nz, p_rtol=args.p_rtol, precision=precision,
-                                fp64_parts=parts)
+                                fp64_parts=parts, mg_fp32=0 if (precision != 0 or args.mg_fp64) else 1)
     cells = nx * ny * nz
     g = TplsGpu(nx, ny, nz, params, uin)
     g.set_state(st)
@@ -278,6 +280,7 @@ def run_gpu(args, ws, rank, local) -> dict | None:
                    "mom_uvw": params.mom_u, "levelset": params.levelset, "p_rtol": params.p_rtol,
                    "precision": "fp64" if precision == 0 else "fp32-mixed",
                    "fp64_parts": parts,
+                   "mg_fp32": params.mg_fp32,
                    "sweep_tiles": tiles,
                    "parallelism": f"{ws} independent replica(s), no sharding",
                    "l2": f"working set ~{cells * 500 / 1e9:.0f} GB per step >> 129 MB L2 (no flush needed)",
@@ -633,6 +636,9 @@ def main():
     ap.add_argument("--jobs", type=int, default=16)
     ap.add_argument("--rate", type=float, default=1.0)
     ap.add_argument("--autotune", action="store_true", help="run the sweep-tile autotuner before timing")
+    ap.add_argument("--mg-fp64", action="store_true",
+                    help="FP64 form: FP64 multigrid levels in the CG preconditioner (default: FP32 levels, "
+                         "tpls_params.mg_fp32 = 1; CG stays FP64 and meets p_rtol on its FP64 residual)")
     ap.add_argument("--accuracy", type=int, default=0, metavar="STEPS",
                     help="instead of timing: step the FP64 and FP32-mixed forms side by side for STEPS "
                          "steps and print their differences (one JSON line)")

@@ -39,7 +39,8 @@ extern "C" {
 #define TPLS_KSP_DIVERGED_ITS (-3)
 #define TPLS_KSP_DIVERGED_NAN (-9)
 
-#define TPLS_PREC_FP64 0      /* plain FP64 everywhere */
+#define TPLS_PREC_FP64 0      /* FP64 everywhere (optionally FP32 multigrid
+                                  levels in the CG preconditioner: mg_fp32) */
 #define TPLS_PREC_FP32_MIXED 1 /* FP32 stencils/sweeps/smoothing, FP64 state,
                                   dots, residuals, volume integral, coarse solve */
 
@@ -56,7 +57,10 @@ typedef struct tpls_params {
   int precision;                  /* TPLS_PREC_* */
   int fp64_parts;                 /* FP32-mixed form only: TPLS_PART_* bits of
                                      the parts kept in FP64 (0 = all FP32) */
-  int reserved[5];
+  int mg_fp32;                    /* FP64 form: 1 = FP32 multigrid levels in the
+                                     CG preconditioner (CG itself stays FP64 and
+                                     meets p_rtol on its FP64 residual) */
+  int reserved[4];
 } tpls_params;
 
 /* Parts of the FP32-mixed form that can be kept in FP64 (tpls_params.fp64_parts). */
@@ -64,8 +68,8 @@ typedef struct tpls_params {
 #define TPLS_PART_LEVELSET 2  /* redistancing iterations */
 #define TPLS_PART_MOMENTUM 4  /* momentum stencils, records and sweeps */
 #define TPLS_PART_MULTIGRID 8 /* multigrid preconditioner */
-#define TPLS_PART_MOM_STENCIL 16 /* momentum stencils and sweep records in FP64
-                                    (records stored FP32 for FP32 sweeps) */
+#define TPLS_PART_MOM_STENCIL 16 /* momentum stencils in FP64 (the FP32 sweeps'
+                                    defect right-hand side stored FP32) */
 
 /* Per-step diagnostics, the quantities the reference logs each timestep
  * (main_ns_hybrid.F90:601-605, 803-808, 840-845, 882-887, 903-911). */

@@ -203,6 +203,29 @@ def test_full_steps_match_oracle(size):
     g.close()
 
 
+def test_full_steps_match_oracle_fp32_preconditioner():
+    """The FP64 form with FP32 multigrid levels in its CG preconditioner
+    (tpls_params.mg_fp32): CG stays FP64 and is held to the same tight
+    tolerance, so the per-step parity bounds are the same as above."""
+    nx, ny, nz = SIZES[next(iter(SIZES))]
+    params, uin, st = make_case("A", nx=nx, ny=ny, nz=nz, p_rtol=1e-14, p_maxits=400, mg_fp32=1)
+    o = Oracle(nx, ny, nz, params, uin)
+    o.set_state(st)
+    g = TplsGpu(nx, ny, nz, params, uin)
+    rows = (slice(None), slice(1, ny + 1), slice(None))
+    for step in range(3):
+        g.set_state(o.get_state())
+        o.step(1)
+        g.step(1)
+        for k in ("PHI2", "U2", "V2", "W2"):
+            e = relmax(g.get_field(k), o.get_field(k), rows)
+            assert e < TOL, (step, k, e)
+        dp = (g.get_field("PRES") - o.get_field("PRES"))[1:nx + 1, 1:ny + 1, 1:nz + 1]
+        assert np.max(np.abs(dp)) <= 1e-11 * np.max(np.abs(o.get_field("PRES"))), step
+        assert g.stats()["p_reason"] == 2
+    g.close()
+
+
 @pytest.mark.parametrize("size", list(SIZES))
 def test_free_running_steps_track_oracle(size):
     """Both sides stepping on their own state for 4 steps.  The reference's

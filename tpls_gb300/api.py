@@ -55,7 +55,7 @@ class TplsParams(C.Structure):
                 ("height", C.c_double), ("scap", C.c_double), ("smooth_width", C.c_double),
                 ("mom_u", C.c_int), ("mom_v", C.c_int), ("mom_w", C.c_int), ("levelset", C.c_int),
                 ("p_rtol", C.c_double), ("p_maxits", C.c_int), ("precision", C.c_int),
-                ("fp64_parts", C.c_int), ("reserved", C.c_int * 5)]
+                ("fp64_parts", C.c_int), ("mg_fp32", C.c_int), ("reserved", C.c_int * 4)]
 
 
 class TplsStats(C.Structure):
@@ -89,6 +89,7 @@ class Params:
     p_maxits: int = 200
     precision: int = TPLS_PREC_FP64
     fp64_parts: int = 0  # FP32-mixed form: PART_* bits kept in FP64
+    mg_fp32: int = 0  # FP64 form: FP32 multigrid levels in the CG preconditioner
     extra: dict = field(default_factory=dict)
 
     def to_c(self) -> TplsParams:

@@ -115,7 +115,7 @@ def interface_height(w: Workload, x: np.ndarray, y: np.ndarray, Lx: float, Ly: f
 
 def make_case(w: Workload | str, *, nx: int | None = None, ny: int | None = None, nz: int | None = None,
               mom: int = 30, levelset: int = 10, p_rtol: float = 1e-5, p_maxits: int = 200,
-              precision: int = 0, fp64_parts: int = 0):
+              precision: int = 0, fp64_parts: int = 0, mg_fp32: int = 0):
     """Returns (params, u_inlet, state) for a workload, optionally resized.
 
     state maps TPLS field names (tpls_gb300.api.STATE_FIELDS subset) to
@@ -138,7 +138,8 @@ def make_case(w: Workload | str, *, nx: int | None = None, ny: int | None = None
     dt = min(0.2 * dx / umax, 0.5 * np.sqrt(dx ** 3 / (2.0 * np.pi)))
     params = Params(dx=dx, dy=dy, dz=dz, dt=dt, re=w.re, mu_plus=mu_plus, mu_minus=mu_minus, height=0.5,
                     scap=1.0, smooth_width=sw, mom_u=mom, mom_v=mom, mom_w=mom, levelset=levelset,
-                    p_rtol=p_rtol, p_maxits=p_maxits, precision=precision, fp64_parts=fp64_parts)
+                    p_rtol=p_rtol, p_maxits=p_maxits, precision=precision, fp64_parts=fp64_parts,
+                    mg_fp32=mg_fp32)
     xi = (np.arange(nx + 2) - 0.5) * dx
     yj = (np.arange(ny + 2) - 0.5) * dy
     zk = (np.arange(nz + 2) - 0.5) * dz

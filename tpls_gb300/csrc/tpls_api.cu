@@ -449,7 +449,7 @@ static int create_impl(int nx, int ny, int nz, const tpls_params *prm, const dou
     c->scal_host = (double *)b;
   }
   TCK(poisson_create(c->g, 1.0 / (prm->dy * prm->dy), 1.0 / (prm->dx * prm->dx), 1.0 / (prm->dz * prm->dz),
-                     c->mixed && !(prm->fp64_parts & TPLS_PART_MULTIGRID), &c->ps));
+                     c->mixed ? !(prm->fp64_parts & TPLS_PART_MULTIGRID) : (prm->mg_fp32 != 0), &c->ps));
   memset(&c->stats, 0, sizeof(c->stats));
   TCK(cudaDeviceSynchronize());
   return TPLS_OK;
