@@ -127,23 +127,13 @@ __device__ __forceinline__ bool cd_valid(int comp, const Geo &g, int i, int k) {
 // at k = 0 the czm slot multiplies the point itself and czp absorbs czm/3;
 // at k = nz-1 the czp slot multiplies the point itself and czm absorbs
 // czp/3.  One 64-byte record per point: (cxp, cxm, cyp, cym, czp, czm, b, 0).
-template <typename T>
-__device__ __forceinline__ void store_rec(T *rec, T a0, T a1, T a2, T a3, T a4, T a5, T a6);
-template <>
-__device__ __forceinline__ void store_rec<double>(double *rec, double a0, double a1, double a2, double a3,
-                                                  double a4, double a5, double a6) {
+__device__ __forceinline__ void store_rec(double *rec, double a0, double a1, double a2, double a3, double a4,
+                                          double a5, double a6) {
   double2 *o = reinterpret_cast<double2 *>(rec);
   o[0] = make_double2(a0, a1);
   o[1] = make_double2(a2, a3);
   o[2] = make_double2(a4, a5);
   o[3] = make_double2(a6, 0.0);
-}
-template <>
-__device__ __forceinline__ void store_rec<float>(float *rec, float a0, float a1, float a2, float a3, float a4,
-                                                 float a5, float a6) {
-  float4 *o = reinterpret_cast<float4 *>(rec);
-  o[0] = make_float4(a0, a1, a2, a3);
-  o[1] = make_float4(a4, a5, a6, 0.f);
 }
 
 // The record of one point of the FP64 sweeps.
@@ -162,7 +152,7 @@ __device__ __forceinline__ void write_coef(int comp, const Geo &g, const Helm &h
       czp = -2.0 * czp;
     }
   }
-  store_rec<double>(rec, ax2 * f.px * r, ax2 * f.mx * r, ay2 * f.py * r, ay2 * f.my * r, czp, czm, rhs * r);
+  store_rec(rec, ax2 * f.px * r, ax2 * f.mx * r, ay2 * f.py * r, ay2 * f.my * r, czp, czm, rhs * r);
 }
 
 // FP64 stencils.  TR = double: the FP64 form's right-hand side and 64-byte

@@ -30,22 +30,12 @@ struct Rec {
   T xp, xm, yp, ym, zp, zm, b;
 };
 
-// record of point c (8 values per point; `stream` = evict-first loads)
-template <typename T>
-__device__ __forceinline__ Rec<T> load_rec(const T *__restrict__ coef, int c, bool stream);
-template <>
-__device__ __forceinline__ Rec<double> load_rec<double>(const double *__restrict__ coef, int c, bool stream) {
+// record of point c of the FP64 sweeps (8 doubles; `stream` = evict-first loads)
+__device__ __forceinline__ Rec<double> load_rec(const double *__restrict__ coef, int c, bool stream) {
   const double2 *r = reinterpret_cast<const double2 *>(coef + 8 * (size_t)c);
   const double2 a = stream ? __ldcs(r) : __ldg(r), b = stream ? __ldcs(r + 1) : __ldg(r + 1);
   const double2 d = stream ? __ldcs(r + 2) : __ldg(r + 2), e = stream ? __ldcs(r + 3) : __ldg(r + 3);
   Rec<double> q = {a.x, a.y, b.x, b.y, d.x, d.y, e.x};
-  return q;
-}
-template <>
-__device__ __forceinline__ Rec<float> load_rec<float>(const float *__restrict__ coef, int c, bool stream) {
-  const float4 *r = reinterpret_cast<const float4 *>(coef + 8 * (size_t)c);
-  const float4 a = stream ? __ldcs(r) : __ldg(r), b = stream ? __ldcs(r + 1) : __ldg(r + 1);
-  Rec<float> q = {a.x, a.y, a.z, a.w, b.x, b.y, b.z};
   return q;
 }
 
