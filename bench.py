@@ -154,7 +154,7 @@ def _profile_figure(tag: str, kernel: str, workload: str):
 
 def run_gpu(args, ws, rank, local) -> dict | None:
     import torch
-    from tpls_gb300.api import STATE_FIELDS, TplsGpu
+    from tpls_gb300.api import TplsGpu
     from tpls_gb300.channel import WORKLOADS, make_case
 
     torch.cuda.set_device(local)
@@ -167,7 +167,8 @@ def run_gpu(args, ws, rank, local) -> dict | None:
     parts = args.fp64_parts if precision == 1 else 0
     nx, ny, nz = args.grid if args.grid else (w.nx, w.ny, w.nz)
     params, uin, st = make_case(args.config, nx=nx, ny=ny, nz=nz, p_rtol=args.p_rtol, precision=precision,
-                                fp64_parts=parts, mg_fp32=0 if (precision != 0 or args.mg_fp64) else 1)
+                                fp64_parts=parts, mg_fp32=0 if (precision != 0 or args.mg_fp64) else 1,
+                                idm=args.idm, pe=args.dim_pe)
     cells = nx * ny * nz
     g = TplsGpu(nx, ny, nz, params, uin)
     g.set_state(st)
@@ -214,7 +215,8 @@ def run_gpu(args, ws, rank, local) -> dict | None:
     # uploaded, one step, state downloaded), CUDA events on the same stream
     ke = max(1, min(args.steps, args.e2e_steps))
     host = {}
-    for k in STATE_FIELDS:
+    state_fields = g.state_fields()
+    for k in state_fields:
         a = g.get_field(k)
         buf = torch.empty(tuple(reversed(a.shape)), dtype=torch.float64, pin_memory=True).numpy().T
         buf[...] = a
@@ -226,11 +228,11 @@ def run_gpu(args, ws, rank, local) -> dict | None:
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(ext)
     for _ in range(ke):
-        for k in STATE_FIELDS:
+        for k in state_fields:
             g.set_field(k, host[k])
         if g.step(1) != 0:
             raise SystemExit("tpls_step failed in the end-to-end region")
-        for k in STATE_FIELDS:
+        for k in state_fields:
             g.get_field_into(k, host[k])
     e1.record(ext)
     torch.cuda.synchronize()
@@ -281,6 +283,8 @@ def run_gpu(args, ws, rank, local) -> dict | None:
                    "precision": "fp64" if precision == 0 else "fp32-mixed",
                    "fp64_parts": parts,
                    "mg_fp32": params.mg_fp32,
+                   "idm": args.idm,
+                   "dim_pe": args.dim_pe if args.idm == "dim" else None,
                    "sweep_tiles": tiles,
                    "parallelism": f"{ws} independent replica(s), no sharding",
                    "l2": f"working set ~{cells * 500 / 1e9:.0f} GB per step >> 129 MB L2 (no flush needed)",
@@ -288,7 +292,8 @@ def run_gpu(args, ws, rank, local) -> dict | None:
                    "grid_geometry": "cubic cells dx=dy=dz=1/nz (the reference's initialisation grid)",
                    "baseline_metric": BASELINE_METRIC},
         "e2e": {"value": e2e, "unit": "cell-steps/s", "h2d_bytes_per_step": bi, "d2h_bytes_per_step": bi,
-                "steps": ke, "path": "tpls_set_field x20 -> tpls_step(1) -> tpls_get_field x20 per step"},
+                "steps": ke, "path": f"tpls_set_field x{len(state_fields)} -> tpls_step(1) -> "
+                                     f"tpls_get_field x{len(state_fields)} per step"},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "kernel": dominant, "bytes_per_launch": per_launch_b,
                      "avg_launch_ms": avg_ms,
@@ -636,6 +641,9 @@ def main():
     ap.add_argument("--jobs", type=int, default=16)
     ap.add_argument("--rate", type=float, default=1.0)
     ap.add_argument("--autotune", action="store_true", help="run the sweep-tile autotuner before timing")
+    ap.add_argument("--idm", choices=["lsm", "dim"], default="lsm",
+                    help="interface method: level set (default) or diffuse interface (FP64 form)")
+    ap.add_argument("--dim-pe", type=float, default=1000.0, help="diffuse interface: Peclet number Pe")
     ap.add_argument("--mg-fp64", action="store_true",
                     help="FP64 form: FP64 multigrid levels in the CG preconditioner (default: FP32 levels, "
                          "tpls_params.mg_fp32 = 1; CG stays FP64 and meets p_rtol on its FP64 residual)")

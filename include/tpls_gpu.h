@@ -60,8 +60,16 @@ typedef struct tpls_params {
   int mg_fp32;                    /* FP64 form: 1 = FP32 multigrid levels in the
                                      CG preconditioner (CG itself stays FP64 and
                                      meets p_rtol on its FP64 residual) */
-  int reserved[4];
+  int idm;                        /* idm: TPLS_IDM_LSM (level set, default) or
+                                     TPLS_IDM_DIM (diffuse interface, FP64 form) */
+  int max_iteration_dim;          /* max_iteration_dim (DIM SOR iterations) */
+  int reserved[2];
+  double epn, pe;                 /* epn, Pe (DIM interface width, Peclet number) */
 } tpls_params;
+
+/* Interface method (main_ns_hybrid.F90:595-612, option_names.F90:35-37). */
+#define TPLS_IDM_LSM 0
+#define TPLS_IDM_DIM 1
 
 /* Parts of the FP32-mixed form that can be kept in FP64 (tpls_params.fp64_parts). */
 #define TPLS_PART_ADVECT 1    /* WENO5 advection */
@@ -102,10 +110,14 @@ enum tpls_field {
   TPLS_F_CONV0_PHI, TPLS_F_CONV1_PHI,                             /* P */
   /* intermediates of the last step (read-only) */
   TPLS_F_CONV2_PHI,     /* P  */
-  TPLS_F_PHI3,          /* P  */
+  TPLS_F_PHI3,          /* P  (DIM: the reference's phi3 array, the starting
+                                  guess of the next step's iteration: 0 at
+                                  creation, then the last step's phi) */
   TPLS_F_RHS_P,         /* P  */
   TPLS_F_U3, TPLS_F_V3, /* UV (before projection) */
   TPLS_F_W3,            /* W  */
+  /* diffuse-interface state (TPLS_IDM_DIM contexts only) */
+  TPLS_F_CONVPREV_PHI,  /* P  ConvPrevPhi (main_ns_hybrid.F90:449, cahn_hilliard_solver.f90:270) */
   TPLS_F_COUNT
 };
 
@@ -245,6 +257,21 @@ int tpls_do_tpls(tpls_ctx *ctx, double *phi2, double *phi3,
                  const int *neighbours, const int *comm2d_quasiperiodic,
                  const double *height, double *err2, const double *dx,
                  const double *dz, const double *dt);
+
+/* cahn_hilliard_solver.f90:41-382  dim (diffuse-interface update): phi and
+ * phiOld are the concentration fields C = phi + 0.5 (the driver passes
+ * phi2+0.5 and phi_old+0.5, main_ns_hybrid.F90:608), phiNew holds the
+ * starting guess on entry and C^{n+1} on return, ConvPrevPhi is updated in
+ * place.  p-grid arrays, host memory. */
+int tpls_dim(tpls_ctx *ctx, const int *maxl, const int *maxn, const double *dx,
+             const double *dy, const double *dz, const double *dt,
+             const double *epn, const double *pe, const double *phi,
+             const double *phi_old, const double *conv2_phi,
+             double *conv_prev_phi, double *phi_new, const int *sx,
+             const int *ex, const int *sy, const int *ey, const int *sz_p,
+             const int *ez_p, const double *height, const int *stride_p_xz,
+             const int *stride_p_yz, const int *neighbours,
+             const int *comm2d_quasiperiodic, const int *max_iteration_dim);
 
 /* levelset.f90:241-242  get_csf */
 int tpls_get_csf(tpls_ctx *ctx, double *fx_csf, double *fy_csf,

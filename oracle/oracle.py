@@ -116,8 +116,9 @@ class Oracle:
             self.set_field(k, v)
 
     def get_state(self):
-        from tpls_gb300.api import STATE_FIELDS
-        return {k: self.get_field(k) for k in STATE_FIELDS}
+        from tpls_gb300.api import DIM_STATE_FIELDS, IDM_DIM, STATE_FIELDS
+        names = STATE_FIELDS + (DIM_STATE_FIELDS if self.params.idm == IDM_DIM else [])
+        return {k: self.get_field(k) for k in names}
 
     def step(self, nsteps=1):
         self.lib.orc_step(self.ctx, int(nsteps))
@@ -135,6 +136,16 @@ class Oracle:
         self.lib.orc_do_advect_phi(self.nx, self.ny, self.nz, _p(phi2), _p(u2), _p(v2), _p(w2), _p(conv),
                                    C.c_double(dx), C.c_double(dy), C.c_double(dz))
         return conv
+
+    def dim(self, phi, phi_old, conv2_phi, conv_prev_phi, phi_new, max_iteration_dim, epn, pe, height, dx,
+            dy, dz, dt):
+        """cahn_hilliard_solver.f90:41 dim -> (phi_new, conv_prev_phi) (copies)."""
+        phi_new = np.array(phi_new, order="F", copy=True)
+        conv_prev_phi = np.array(conv_prev_phi, order="F", copy=True)
+        self.lib.orc_dim(self.nx, self.ny, self.nz, C.c_double(dx), C.c_double(dy), C.c_double(dz),
+                         C.c_double(dt), C.c_double(epn), C.c_double(pe), _p(phi), _p(phi_old), _p(conv2_phi),
+                         _p(conv_prev_phi), _p(phi_new), C.c_double(height), int(max_iteration_dim))
+        return phi_new, conv_prev_phi
 
     def do_tpls(self, phi2, conv0_phi, conv1_phi, conv2_phi, max_iteration_levelset, height, dx, dz, dt,
                 phi3=None):

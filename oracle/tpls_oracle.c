@@ -506,6 +506,146 @@ void orc_csf_faces(int nx, int ny, int nz, const double *fx, const double *fy,
 }
 
 /* ------------------------------------------------------------------------
+ * cahn_hilliard_solver.f90:41-382 dim: the diffuse-interface (Cahn-Hilliard)
+ * update on one rank (sx=1, ex=nx, sy=1, ey=ny, maxl=nx+1, maxn=nz+1).
+ * phi, phi_old: concentration C (p-grid); phi_new: starting guess in,
+ * C^{n+1} out; conv_prev: ConvPrevPhi, updated.  bulkE0, d2phi and source0
+ * are the routine's automatic arrays (NaN canaries where it leaves them
+ * undefined).  The routine's max-norm residual is never used by the
+ * reference and is not computed.
+ * ---------------------------------------------------------------------- */
+static double dim_mob(double c1) { /* dsqrt(c1*c1*(1-|c1|)*(1-|c1|)) */
+  return sqrt(c1 * c1 * (1.0 - fabs(c1)) * (1.0 - fabs(c1)));
+}
+
+void orc_dim(int nx, int ny, int nz, double dx, double dy, double dz, double dt,
+             double epn, double pe, const double *phi, const double *phi_old,
+             const double *conv2_phi, double *conv_prev, double *phi_new,
+             double height, int max_iteration_dim) {
+  DIMS;
+  const int maxl = nx + 1, maxn = nz + 1;
+  const size_t np = (size_t)orc_size_p(nx, ny, nz);
+  const double nmda = 0.25, tao = 0.25, alfa1 = 1.1;
+  double *bulk = alloc_nan(np), *d2 = alloc_nan(np), *src = alloc_nan(np);
+  const double epn2 = epn * epn;
+  /* :110-125 */
+  for (int k = 1; k <= maxn - 1; k++)
+    for (int j = 1; j <= ny; j++)
+      for (int i = 1; i <= nx; i++) {
+        const double p = phi[IX(i, j, k)];
+        bulk[IX(i, j, k)] = (1.0 - 3.0 * p + 2.0 * p * p) * p / 2.0;
+        d2[IX(i, j, k)] = (phi[IX(i + 1, j, k)] - 2.0 * p + phi[IX(i - 1, j, k)]) / dx / dx +
+                          (phi[IX(i, j + 1, k)] - 2.0 * p + phi[IX(i, j - 1, k)]) / dy / dy +
+                          (phi[IX(i, j, k + 1)] - 2.0 * p + phi[IX(i, j, k - 1)]) / dz / dz;
+      }
+  /* :128-137 z ghost planes, :140-143 exchange, :146-172 x ghost planes */
+  for (int j = 1; j <= ny; j++)
+    for (int i = 1; i <= nx; i++) {
+      bulk[IX(i, j, 0)] = bulk[IX(i, j, 1)];
+      bulk[IX(i, j, maxn)] = bulk[IX(i, j, maxn - 1)];
+      d2[IX(i, j, 0)] = d2[IX(i, j, 1)];
+      d2[IX(i, j, maxn)] = d2[IX(i, j, maxn - 1)];
+    }
+  orc_exchange2d(nx, ny, 0, nz + 1, bulk);
+  orc_exchange2d(nx, ny, 0, nz + 1, d2);
+  for (int k = 1; k <= maxn - 1; k++)
+    for (int j = 1; j <= ny; j++) {
+      d2[IX(0, j, k)] = d2[IX(1, j, k)];
+      bulk[IX(0, j, k)] = bulk[IX(1, j, k)];
+      d2[IX(maxl, j, k)] = d2[IX(maxl - 1, j, k)];
+      bulk[IX(maxl, j, k)] = bulk[IX(maxl - 1, j, k)];
+    }
+  /* :174-233 source term and ConvPrevPhi */
+  for (int k = 1; k <= maxn - 1; k++)
+    for (int j = 1; j <= ny; j++)
+      for (int i = 1; i <= nx; i++) {
+        const double p = phi[IX(i, j, k)];
+        const double a1 = dim_mob((phi[IX(i - 1, j, k)] + p) / 2.0);
+        const double a2 = dim_mob((phi[IX(i + 1, j, k)] + p) / 2.0);
+        const double a3 = dim_mob((phi[IX(i, j - 1, k)] + p) / 2.0);
+        const double a4 = dim_mob((phi[IX(i, j + 1, k)] + p) / 2.0);
+        const double a5 = dim_mob((k + 1 == 2) ? p : (phi[IX(i, j, k - 1)] + p) / 2.0);
+        const double a6 = dim_mob((phi[IX(i, j, k + 1)] + p) / 2.0);
+        const double bc = bulk[IX(i, j, k)], lc = d2[IX(i, j, k)];
+        const double temp1 =
+            (a2 * (bulk[IX(i + 1, j, k)] - bc) - a1 * (bc - bulk[IX(i - 1, j, k)])) / dx / dx +
+            (a4 * (bulk[IX(i, j + 1, k)] - bc) - a3 * (bc - bulk[IX(i, j - 1, k)])) / dy / dy +
+            (a6 * (bulk[IX(i, j, k + 1)] - bc) - a5 * (bc - bulk[IX(i, j, k - 1)])) / dz / dz;
+        const double temp2 = (d2[IX(i + 1, j, k)] - 2.0 * lc + d2[IX(i - 1, j, k)]) / dx / dx +
+                             (d2[IX(i, j + 1, k)] - 2.0 * lc + d2[IX(i, j - 1, k)]) / dy / dy +
+                             (d2[IX(i, j, k + 1)] - 2.0 * lc + d2[IX(i, j, k - 1)]) / dz / dz;
+        const double temp3 =
+            (a2 * (d2[IX(i + 1, j, k)] - lc) - a1 * (lc - d2[IX(i - 1, j, k)])) / dx / dx +
+            (a4 * (d2[IX(i, j + 1, k)] - lc) - a3 * (lc - d2[IX(i, j - 1, k)])) / dy / dy +
+            (a6 * (d2[IX(i, j, k + 1)] - lc) - a5 * (lc - d2[IX(i, j, k - 1)])) / dz / dz;
+        const double temp4 = (temp1 - epn2 * temp3) / epn - nmda * tao / 2.0 * lc + epn2 * nmda / 2.0 * temp2;
+        const double temp5 = temp4 / pe - conv2_phi[IX(i, j, k)];
+        src[IX(i, j, k)] = temp5 * 2.0 - conv_prev[IX(i, j, k)];
+        conv_prev[IX(i, j, k)] = temp5;
+      }
+  /* :236-238 (dx**2.d0 folds to dx*dx; dx**4.d0 is a pow) */
+  const double a1 = 1.0 / (dx * dx) + 1.0 / (dy * dy) + 1.0 / (dz * dz);
+  const double a2 = 2.0 / pow(dx, 4.0) + 2.0 / pow(dy, 4.0) + 2.0 / pow(dz, 4.0);
+  const double diagonal = 1.5 + nmda / 2.0 / pe * dt * (2.0 * tao * a1 + epn2 * (4.0 * a1 * a1 + a2));
+  /* :241-366 SOR */
+  for (int it = 1; it <= max_iteration_dim; it++) {
+    for (int k = 1; k <= maxn - 1; k++)
+      for (int j = 1; j <= ny; j++)
+        for (int i = 1; i <= nx; i++) {
+          const double p = phi_new[IX(i, j, k)];
+          d2[IX(i, j, k)] = (phi_new[IX(i + 1, j, k)] - 2.0 * p + phi_new[IX(i - 1, j, k)]) / dx / dx +
+                            (phi_new[IX(i, j + 1, k)] - 2.0 * p + phi_new[IX(i, j - 1, k)]) / dy / dy +
+                            (phi_new[IX(i, j, k + 1)] - 2.0 * p + phi_new[IX(i, j, k - 1)]) / dz / dz;
+        }
+    for (int j = 1; j <= ny; j++)
+      for (int i = 1; i <= nx; i++) {
+        d2[IX(i, j, 0)] = d2[IX(i, j, 1)];
+        d2[IX(i, j, maxn)] = d2[IX(i, j, maxn - 1)];
+      }
+    orc_exchange2d(nx, ny, 0, nz + 1, d2);
+    for (int k = 1; k <= maxn - 1; k++)
+      for (int j = 1; j <= ny; j++) {
+        d2[IX(0, j, k)] = d2[IX(1, j, k)];
+        d2[IX(maxl, j, k)] = d2[IX(maxl - 1, j, k)];
+      }
+    for (int k = 1; k <= maxn - 1; k++)
+      for (int j = 1; j <= ny; j++)
+        for (int i = 1; i <= nx; i++) {
+          const double l = d2[IX(i, j, k)];
+          bulk[IX(i, j, k)] = (d2[IX(i + 1, j, k)] - 2.0 * l + d2[IX(i - 1, j, k)]) / dx / dx +
+                              (d2[IX(i, j + 1, k)] - 2.0 * l + d2[IX(i, j - 1, k)]) / dy / dy +
+                              (d2[IX(i, j, k + 1)] - 2.0 * l + d2[IX(i, j, k - 1)]) / dz / dz;
+        }
+    for (int k = 1; k <= maxn - 1; k++)
+      for (int j = 1; j <= ny; j++)
+        for (int i = 1; i <= nx; i++) {
+          const size_t c = IX(i, j, k);
+          const double some = 2.0 * phi[c] - 0.5 * phi_old[c] - 1.5 * phi_new[c] + dt * src[c] +
+                              dt * nmda / 2.0 / pe * (tao * d2[c] - epn2 * bulk[c]);
+          double v = phi_new[c] + alfa1 * some / diagonal;
+          if (v < 0.0) v = 0.0;
+          if (v > 1.0) v = 1.0;
+          phi_new[c] = v;
+        }
+    for (int j = 1; j <= ny; j++)
+      for (int i = 1; i <= nx; i++) {
+        phi_new[IX(i, j, 0)] = phi_new[IX(i, j, 1)];
+        phi_new[IX(i, j, maxn)] = phi_new[IX(i, j, maxn - 1)];
+      }
+    orc_exchange2d(nx, ny, 0, nz + 1, phi_new);
+    for (int k = 1; k <= maxn - 1; k++)
+      for (int j = 1; j <= ny; j++) {
+        const double z_val = k * dz - 0.5 * dz;
+        phi_new[IX(0, j, k)] = 0.5 + 0.5 * tanh((z_val - height) / (2.0 * sqrt(2.0) * epn));
+        phi_new[IX(maxl, j, k)] = phi_new[IX(maxl - 1, j, k)];
+      }
+  }
+  free(bulk);
+  free(d2);
+  free(src);
+}
+
+/* ------------------------------------------------------------------------
  * momentum_allflux.f90:474-521 get_viscosity over i=1..nx, plus
  * main_ns_hybrid.F90:651-718: viscosity2_aug interior copy, the x ghost
  * planes from phi2(0,:,:) and phi2(nx+1,:,:), exchange2d_aug1 (rows 0, ny+1)
@@ -1181,6 +1321,7 @@ struct orc_ctx {
   double *fx, *fy, *fz, *csf_u2, *csf_v2, *csf_w2, *va;
   double *conv2_u, *conv2_v, *conv2_w, *diff_u, *diff_v, *diff_w;
   double *rhs_u, *rhs_v, *rhs_w, *u3_old, *v3_old, *w3_old;
+  double *dim_c;  /* phi2 + 0.5 / phi2 - 0.5 temporaries of the diffuse-interface step */
   tpls_stats st;
 };
 
@@ -1235,6 +1376,7 @@ orc_ctx *orc_create(int nx, int ny, int nz, const tpls_params *prm,
   c->u3_old = alloc_zero(nuv);
   c->v3_old = alloc_zero(nuv);
   c->w3_old = alloc_zero(nw);
+  c->dim_c = alloc_zero(np);
   return c;
 }
 
@@ -1243,7 +1385,7 @@ void orc_destroy(orc_ctx *c) {
   for (int f = 0; f < TPLS_F_COUNT; f++) free(c->f[f]);
   double *s[] = {c->u_inlet, c->fx, c->fy, c->fz, c->csf_u2, c->csf_v2, c->csf_w2, c->va,
                  c->conv2_u, c->conv2_v, c->conv2_w, c->diff_u, c->diff_v, c->diff_w,
-                 c->rhs_u, c->rhs_v, c->rhs_w, c->u3_old, c->v3_old, c->w3_old};
+                 c->rhs_u, c->rhs_v, c->rhs_w, c->u3_old, c->v3_old, c->w3_old, c->dim_c};
   for (size_t q = 0; q < sizeof(s) / sizeof(s[0]); q++) free(s[q]);
   free(c);
 }
@@ -1288,9 +1430,19 @@ void orc_step(orc_ctx *c, int nsteps) {
     double *u2 = F[TPLS_F_U2], *v2 = F[TPLS_F_V2], *w2 = F[TPLS_F_W2];
     /* :585 advection */
     orc_do_advect_phi(nx, ny, nz, F[TPLS_F_PHI2], u2, v2, w2, F[TPLS_F_CONV2_PHI], dx, dy, dz);
-    /* :596 level-set update + redistancing */
-    orc_do_tpls(nx, ny, nz, F[TPLS_F_PHI2], F[TPLS_F_PHI3], F[TPLS_F_CONV0_PHI], F[TPLS_F_CONV1_PHI],
-                F[TPLS_F_CONV2_PHI], P->levelset, P->height, dx, dz, dt, &c->st.err_phi);
+    if (P->idm == TPLS_IDM_DIM) {
+      /* :608-611 diffuse interface: dim(phi2+0.5, phi_old+0.5, ..., phi3), then
+       * phi3 = phi3 - 0.5; phi_old equals phi2 at every step (:444, :2508) */
+      for (size_t e = 0; e < np; e++) c->dim_c[e] = F[TPLS_F_PHI2][e] + 0.5;
+      orc_dim(nx, ny, nz, dx, dy, dz, dt, P->epn, P->pe, c->dim_c, c->dim_c, F[TPLS_F_CONV2_PHI],
+              F[TPLS_F_CONVPREV_PHI], F[TPLS_F_PHI3], P->height, P->max_iteration_dim);
+      for (size_t e = 0; e < np; e++) F[TPLS_F_PHI3][e] = F[TPLS_F_PHI3][e] - 0.5;
+      c->st.err_phi = 0.0;
+    } else {
+      /* :596 level-set update + redistancing */
+      orc_do_tpls(nx, ny, nz, F[TPLS_F_PHI2], F[TPLS_F_PHI3], F[TPLS_F_CONV0_PHI], F[TPLS_F_CONV1_PHI],
+                  F[TPLS_F_CONV2_PHI], P->levelset, P->height, dx, dz, dt, &c->st.err_phi);
+    }
     /* :618-641 CSF */
     orc_exchange2d(nx, ny, 0, nz + 1, F[TPLS_F_PHI3]);
     orc_get_csf(nx, ny, nz, c->fx, c->fy, c->fz, F[TPLS_F_PHI3], dx, dy, dz, P->scap, P->smooth_width);
@@ -1298,9 +1450,14 @@ void orc_step(orc_ctx *c, int nsteps) {
     orc_exchange2d(nx, ny, 0, nz + 1, c->fy);
     orc_exchange2d(nx, ny, 0, nz + 1, c->fz);
     orc_csf_faces(nx, ny, nz, c->fx, c->fy, c->fz, c->csf_u2, c->csf_v2, c->csf_w2);
-    /* :646-724 viscosity from phi2 (the pre-advection level set) */
-    orc_viscosity_aug(nx, ny, nz, F[TPLS_F_PHI2], c->va, P->smooth_width, P->re, P->mu_minus,
-                      P->mu_plus);
+    /* :646-724 viscosity from phi2 (the pre-advection level set); the
+     * diffuse-interface method passes phi2-0.5 (:650, :667, :692) */
+    const double *vphi = F[TPLS_F_PHI2];
+    if (P->idm == TPLS_IDM_DIM) {
+      for (size_t e = 0; e < np; e++) c->dim_c[e] = F[TPLS_F_PHI2][e] - 0.5;
+      vphi = c->dim_c;
+    }
+    orc_viscosity_aug(nx, ny, nz, vphi, c->va, P->smooth_width, P->re, P->mu_minus, P->mu_plus);
     /* :728-735 */
     orc_exchange2d(nx, ny, 0, nz - 1, u2);
     orc_exchange2d(nx, ny, 0, nz - 1, v2);

@@ -49,6 +49,10 @@ void orc_do_levelset_iteration(int nx, int ny, int nz, const double *phi,
                                double *phi_reinit, const double *D,
                                const int *istatus, const double *sgn, double h,
                                double height, double *err);
+void orc_dim(int nx, int ny, int nz, double dx, double dy, double dz, double dt,
+             double epn, double pe, const double *phi, const double *phi_old,
+             const double *conv2_phi, double *conv_prev, double *phi_new,
+             double height, int max_iteration_dim);
 void orc_do_tpls(int nx, int ny, int nz, const double *phi2, double *phi3,
                  const double *c0, const double *c1, const double *c2,
                  int levelset, double height, double dx, double dz, double dt,

@@ -61,6 +61,11 @@ def test_create_rejects_bad_arguments_before_device_work():
     assert lib.tpls_gpu_create(64, 32, 48, C.byref(bad), up, C.byref(out)) == 1
     badp = Params(**{**params.__dict__, "precision": 7}).to_c()
     assert lib.tpls_gpu_create(64, 32, 48, C.byref(badp), up, C.byref(out)) == 1
+    # the diffuse-interface method: FP64 form only, with epn > 0 and Pe > 0
+    dparams, _, _ = make_case("A", idm="dim")
+    for change in ({"precision": 1}, {"epn": 0.0}, {"pe": 0.0}, {"max_iteration_dim": -1}, {"idm": 2}):
+        bd = Params(**{**dparams.__dict__, **change}).to_c()
+        assert lib.tpls_gpu_create(64, 32, 48, C.byref(bd), up, C.byref(out)) == 1, change
     assert not out.value
 
 

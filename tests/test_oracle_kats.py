@@ -349,3 +349,52 @@ def test_oracle_step_is_deterministic_and_finite():
     for k in outs[0]:
         assert np.all(np.isfinite(outs[0][k])), k
         np.testing.assert_array_equal(outs[0][k], outs[1][k])
+
+
+def _dim_oracle(nx=24, ny=10, nz=14):
+    params, uin, _ = make_case("A", nx=nx, ny=ny, nz=nz, idm="dim")
+    return params, Oracle(nx, ny, nz, params, uin)
+
+
+def test_dim_keeps_a_uniform_concentration_away_from_the_inlet():
+    """cahn_hilliard_solver.f90 dim on a uniform C with no advection and no
+    history: the bulk and Laplacian terms vanish, so C stays exactly c0
+    except where the inlet profile has reached; each SOR iteration widens
+    that reach by two cells (grad^2 of grad^2)."""
+    p, o = _dim_oracle()
+    nx, ny, nz = o.nx, o.ny, o.nz
+    c0 = 0.3
+    C = np.full((nx + 2, ny + 2, nz + 2), c0, order="F")
+    zero = np.zeros_like(C, order="F")
+    its = 3
+    new, cprev = o.dim(C, C, zero, zero, C, its, p.epn, p.pe, p.height, p.dx, p.dy, p.dz, p.dt)
+    far = new[2 * its + 2:nx + 1, 1:ny + 1, 1:nz + 1]
+    assert np.array_equal(far, np.full_like(far, c0))
+    assert np.all(cprev[1:nx + 1, 1:ny + 1, 1:nz + 1] == 0.0)
+    # the inlet column carries the reference's tanh profile
+    z = (np.arange(1, nz + 1) - 0.5) * p.dz
+    prof = 0.5 + 0.5 * np.tanh((z - p.height) / (2.0 * np.sqrt(2.0) * p.epn))
+    assert np.allclose(new[0, 1:ny + 1, 1:nz + 1], prof[None, :], rtol=0, atol=1e-15)
+
+
+def test_dim_clamps_to_the_unit_interval_and_steps_stay_finite():
+    """The update clamps C^{n+1} to [0, 1] (cahn_hilliard_solver.f90:311-312);
+    whole diffuse-interface steps of the oracle stay finite with phi = C - 0.5
+    inside [-0.5, 0.5] on the interior."""
+    p, o = _dim_oracle()
+    nx, ny, nz = o.nx, o.ny, o.nz
+    rng = np.random.default_rng(3)
+    C = np.asfortranarray(rng.uniform(-0.2, 1.2, size=(nx + 2, ny + 2, nz + 2)))
+    zero = np.zeros_like(C, order="F")
+    new, _ = o.dim(C, C, zero, zero, C, 2, p.epn, p.pe, p.height, p.dx, p.dy, p.dz, p.dt)
+    inner = new[1:nx + 1, 1:ny + 1, 1:nz + 1]
+    assert inner.min() >= 0.0 and inner.max() <= 1.0
+    params, uin, st = make_case("A", nx=nx, ny=ny, nz=nz, idm="dim")
+    o2 = Oracle(nx, ny, nz, params, uin)
+    o2.set_state(st)
+    o2.step(3)
+    phi = o2.get_field("PHI2")
+    assert np.isfinite(phi).all()
+    inter = phi[1:nx + 1, 1:ny + 1, 1:nz + 1]
+    assert inter.min() >= -0.5 and inter.max() <= 0.5
+    assert np.isfinite(o2.get_field("U2")).all()

@@ -39,7 +39,7 @@ TIMERS = ["advect", "levelset", "csf", "visc", "mom_rhs", "jacobi", "sor_even", 
 F = dict(PHI2=0, U2=1, V2=2, W2=3, PRES=4, PRES_OLD=5, CONV0_U=6, CONV1_U=7, CONV0_V=8,
          CONV1_V=9, CONV0_W=10, CONV1_W=11, CSF_U0=12, CSF_U1=13, CSF_V0=14, CSF_V1=15,
          CSF_W0=16, CSF_W1=17, CONV0_PHI=18, CONV1_PHI=19, CONV2_PHI=20, PHI3=21, RHS_P=22,
-         U3=23, V3=24, W3=25)
+         U3=23, V3=24, W3=25, CONVPREV_PHI=26)
 FIELD_KIND = {name: ("uv" if name in ("U2", "V2", "CONV0_U", "CONV1_U", "CONV0_V", "CONV1_V",
                                       "CSF_U0", "CSF_U1", "CSF_V0", "CSF_V1", "U3", "V3")
                      else "w" if name in ("W2", "CONV0_W", "CONV1_W", "CSF_W0", "CSF_W1", "W3")
@@ -47,6 +47,10 @@ FIELD_KIND = {name: ("uv" if name in ("U2", "V2", "CONV0_U", "CONV1_U", "CONV0_V
 STATE_FIELDS = ["PHI2", "U2", "V2", "W2", "PRES", "PRES_OLD", "CONV0_U", "CONV1_U", "CONV0_V",
                 "CONV1_V", "CONV0_W", "CONV1_W", "CSF_U0", "CSF_U1", "CSF_V0", "CSF_V1",
                 "CSF_W0", "CSF_W1", "CONV0_PHI", "CONV1_PHI"]
+# the diffuse-interface method's extra state: ConvPrevPhi and the reference's
+# phi3 array (the next step's starting guess)
+DIM_STATE_FIELDS = ["CONVPREV_PHI", "PHI3"]
+IDM_LSM, IDM_DIM = 0, 1
 
 
 class TplsParams(C.Structure):
@@ -55,7 +59,9 @@ class TplsParams(C.Structure):
                 ("height", C.c_double), ("scap", C.c_double), ("smooth_width", C.c_double),
                 ("mom_u", C.c_int), ("mom_v", C.c_int), ("mom_w", C.c_int), ("levelset", C.c_int),
                 ("p_rtol", C.c_double), ("p_maxits", C.c_int), ("precision", C.c_int),
-                ("fp64_parts", C.c_int), ("mg_fp32", C.c_int), ("reserved", C.c_int * 4)]
+                ("fp64_parts", C.c_int), ("mg_fp32", C.c_int), ("idm", C.c_int),
+                ("max_iteration_dim", C.c_int), ("reserved", C.c_int * 2), ("epn", C.c_double),
+                ("pe", C.c_double)]
 
 
 class TplsStats(C.Structure):
@@ -90,6 +96,10 @@ class Params:
     precision: int = TPLS_PREC_FP64
     fp64_parts: int = 0  # FP32-mixed form: PART_* bits kept in FP64
     mg_fp32: int = 0  # FP64 form: FP32 multigrid levels in the CG preconditioner
+    idm: int = IDM_LSM  # interface method: level set or diffuse interface (FP64 form)
+    max_iteration_dim: int = 18  # tpls_config.opt default
+    epn: float = 0.0  # diffuse interface width
+    pe: float = 1.0  # Peclet number of the diffuse-interface method
     extra: dict = field(default_factory=dict)
 
     def to_c(self) -> TplsParams:
@@ -254,8 +264,11 @@ class TplsGpu:
         for k, v in state.items():
             self.set_field(k, v)
 
+    def state_fields(self) -> list:
+        return STATE_FIELDS + (DIM_STATE_FIELDS if self.params.idm == IDM_DIM else [])
+
     def get_state(self) -> dict:
-        return {k: self.get_field(k) for k in STATE_FIELDS}
+        return {k: self.get_field(k) for k in self.state_fields()}
 
     def step(self, nsteps: int = 1) -> int:
         """nsteps timesteps on device-resident state; returns the status
@@ -317,6 +330,21 @@ class TplsGpu:
             _i(nx), nb, _i(0), _d(dx), _d(dy), _d(dz), *([_i(0)] * 10))
         self._check(s)
         return conv
+
+    def dim(self, phi, phi_old, conv2_phi, conv_prev_phi, phi_new, max_iteration_dim, epn, pe, height, dx,
+            dy, dz, dt):
+        """cahn_hilliard_solver.f90:41 dim -> (phi_new, conv_prev_phi) (C fields, copies)."""
+        nz = self.nz
+        phi_new = np.array(phi_new, order="F", copy=True)
+        conv_prev_phi = np.array(conv_prev_phi, order="F", copy=True)
+        b = self._b()
+        nb = (C.c_int * 6)(*([-2] * 6))
+        s = self.lib.tpls_dim(self.ctx, _i(self.nx + 1), _i(nz + 1), _d(dx), _d(dy), _d(dz), _d(dt), _d(epn),
+                              _d(pe), _ptr(phi), _ptr(phi_old), _ptr(conv2_phi), _ptr(conv_prev_phi),
+                              _ptr(phi_new), b["sx"], b["ex"], b["sy"], b["ey"], _i(0), _i(nz + 1), _d(height),
+                              _i(0), _i(0), nb, _i(0), _i(max_iteration_dim))
+        self._check(s)
+        return phi_new, conv_prev_phi
 
     def do_tpls(self, phi2, conv0_phi, conv1_phi, conv2_phi, max_iteration_levelset, height, dx, dz,
                 dt, phi3=None):

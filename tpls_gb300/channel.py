@@ -115,7 +115,8 @@ def interface_height(w: Workload, x: np.ndarray, y: np.ndarray, Lx: float, Ly: f
 
 def make_case(w: Workload | str, *, nx: int | None = None, ny: int | None = None, nz: int | None = None,
               mom: int = 30, levelset: int = 10, p_rtol: float = 1e-5, p_maxits: int = 200,
-              precision: int = 0, fp64_parts: int = 0, mg_fp32: int = 0):
+              precision: int = 0, fp64_parts: int = 0, mg_fp32: int = 0, idm: str = "lsm",
+              epn: float | None = None, pe: float = 1000.0, max_iteration_dim: int = 18):
     """Returns (params, u_inlet, state) for a workload, optionally resized.
 
     state maps TPLS field names (tpls_gb300.api.STATE_FIELDS subset) to
@@ -139,11 +140,14 @@ def make_case(w: Workload | str, *, nx: int | None = None, ny: int | None = None
     params = Params(dx=dx, dy=dy, dz=dz, dt=dt, re=w.re, mu_plus=mu_plus, mu_minus=mu_minus, height=0.5,
                     scap=1.0, smooth_width=sw, mom_u=mom, mom_v=mom, mom_w=mom, levelset=levelset,
                     p_rtol=p_rtol, p_maxits=p_maxits, precision=precision, fp64_parts=fp64_parts,
-                    mg_fp32=mg_fp32)
+                    mg_fp32=mg_fp32, idm=1 if idm == "dim" else 0, max_iteration_dim=max_iteration_dim,
+                    epn=(1.5 * dz if epn is None else epn), pe=pe)
     xi = (np.arange(nx + 2) - 0.5) * dx
     yj = (np.arange(ny + 2) - 0.5) * dy
     zk = (np.arange(nz + 2) - 0.5) * dz
     h = interface_height(w, xi[:, None], yj[None, :], Lx, Ly)
+    # the same phi = z - h for both interface methods, as the reference's
+    # initial-condition program writes it (create_initial_conditions_program.F90)
     phi = np.asfortranarray(zk[None, None, :] - h[:, :, None])
     u = np.asfortranarray(np.broadcast_to(uz[None, None, :], (nx + 2, ny + 2, nz)).copy())
     v = np.zeros((nx + 2, ny + 2, nz), order="F")
@@ -164,4 +168,9 @@ def make_case(w: Workload | str, *, nx: int | None = None, ny: int | None = None
     pres = np.asfortranarray(np.broadcast_to(-xp[:, None, None], (nx + 2, ny + 2, nz + 2)).copy())
     state = {"PHI2": phi, "U2": u, "V2": v, "W2": wv, "PRES": pres,
              "PRES_OLD": np.zeros_like(pres, order="F")}
+    if params.idm == 1:
+        # the diffuse-interface iteration starts from phi3; the harness seeds it
+        # with the initial phi (the reference's driver starts it at 0)
+        state["PHI3"] = phi.copy(order="F")
+        state["CONVPREV_PHI"] = np.zeros_like(phi, order="F")
     return params, np.ascontiguousarray(uz), state

@@ -1,7 +1,8 @@
 """Checkpoint / restart of a channel: the full device state (phi, u, v, w,
 p, p_old and the AB3 histories, in the phase-independent order the C ABI
-uses) with the grid and parameters, in one .npz file.  Restarting from a
-checkpoint continues bit-identically."""
+uses; ConvPrevPhi and phi3 for the diffuse-interface method) with the grid
+and parameters, in one .npz file.  Restarting from a checkpoint continues
+bit-identically."""
 from __future__ import annotations
 
 import dataclasses
@@ -9,7 +10,7 @@ import json
 
 import numpy as np
 
-from .api import STATE_FIELDS, Params, TplsGpu
+from .api import Params, TplsGpu
 
 
 def save_checkpoint(g: TplsGpu, path) -> None:
@@ -25,5 +26,5 @@ def load_checkpoint(path) -> TplsGpu:
     nx, ny, nz = (int(v) for v in z["grid"])
     meta = json.loads(str(z["params"]))
     g = TplsGpu(nx, ny, nz, Params(**meta), z["u_inlet"])
-    g.set_state({k: np.asfortranarray(z[f"f_{k}"]) for k in STATE_FIELDS})
+    g.set_state({k: np.asfortranarray(z[f"f_{k}"]) for k in g.state_fields()})
     return g

@@ -498,11 +498,13 @@ cudaError_t launch_csf(const Geo &g, const Phys &ph, const double *phi3, float *
 // planes of main_ns_hybrid.F90:653-710 use the same formula and the same
 // single-precision pi) and the 2-row periodic-y augmentation.
 template <typename T>
-__global__ void k_visc(Geo g, Phys ph, const double *__restrict__ phi, T *__restrict__ mu) {
+__global__ void k_visc(Geo g, Phys ph, const double *__restrict__ phi, double off, T *__restrict__ mu) {
   const int i = blockIdx.x * LS_BX + threadIdx.x, j = blockIdx.y * LS_BY + threadIdx.y - 1;
   const int k = blockIdx.z;
   if (i > g.nx + 1 || j > g.ny + 2) return;
-  const double p = phi[TPLS_IDX(g, i, wrapy(j, g.ny), k)];
+  // off: -0.5 for the diffuse-interface method, which passes phi2-0.5
+  // (main_ns_hybrid.F90:650, :667, :692)
+  const double p = phi[TPLS_IDX(g, i, wrapy(j, g.ny), k)] + off;
   double hv;
   if (p < -ph.sw)
     hv = 0.0;
@@ -514,9 +516,9 @@ __global__ void k_visc(Geo g, Phys ph, const double *__restrict__ phi, T *__rest
 }
 
 cudaError_t launch_visc(const Geo &g, const Phys &ph, const double *phi2,
-                        double *mu, cudaStream_t st) {
+                        double *mu, cudaStream_t st, double phi_offset) {
   dim3 grd((g.nx + 2 + LS_BX - 1) / LS_BX, (g.ny + 4 + LS_BY - 1) / LS_BY, g.nz + 2);
-  k_visc<double><<<grd, dim3(LS_BX, LS_BY), 0, st>>>(g, ph, phi2, mu);
+  k_visc<double><<<grd, dim3(LS_BX, LS_BY), 0, st>>>(g, ph, phi2, phi_offset, mu);
   return cudaGetLastError();
 }
 // The FP32 viscosity of the FP32-mixed form: the same formula in FP32 on

@@ -42,6 +42,12 @@ struct tpls_ctx {
   double *x3[3][2];  // momentum ping-pong per component
   int x3_final[3] = {0, 0, 0};
   double *u_inlet;
+  // diffuse-interface method (idm = dim, FP64 form): ConvPrevPhi and the
+  // reference's phi3 (the next step's starting guess) are state; bulkE0 and
+  // source0 are work arrays, the iterate ping-pongs through phiA / phiB and
+  // d2phi lives in D
+  int dim = 0;
+  double *convprev = nullptr, *phi3d = nullptr, *dimE = nullptr, *dimS = nullptr;
   // FP32-mixed form: FP32 copies of the step inputs and FP32 work arrays
   // (the state above stays FP64)
   int mixed = 0;
@@ -180,7 +186,8 @@ static double *field_ptr(tpls_ctx *c, int f) {
     // last step's intermediates: after the rotation the step's conv2 sits
     // in the conv1 slot
     case TPLS_F_CONV2_PHI: return c->conv_phi[s1];
-    case TPLS_F_PHI3: return c->phi2;
+    case TPLS_F_PHI3: return c->dim ? c->phi3d : c->phi2;
+    case TPLS_F_CONVPREV_PHI: return c->convprev;
     case TPLS_F_RHS_P: return c->rhs_p;
     case TPLS_F_U3: return c->x3[0][c->x3_final[0]];
     case TPLS_F_V3: return c->x3[1][c->x3_final[1]];
@@ -365,6 +372,11 @@ static int create_impl(int nx, int ny, int nz, const tpls_params *prm, const dou
       c->coef[q] = (double *)b;
     }
     TCK(alloc_field(c, 1, ny + 4, nz + 2, &c->mu));
+    if (prm->idm == TPLS_IDM_DIM) {
+      c->dim = 1;
+      double **pd[] = {&c->convprev, &c->phi3d, &c->dimE, &c->dimS};
+      for (double **p : pd) TCK(alloc_p(c, p));  // zeroed: ConvPrevPhi = 0, phi3 = 0 (:443, :449)
+    }
   } else {
     const int parts = prm->fp64_parts;
     if (parts & TPLS_PART_LEVELSET) {
@@ -470,7 +482,8 @@ long long tpls_footprint_bytes(int nx, int ny, int nz, int precision) {
   const size_t D = sizeof(double), F = sizeof(float);
   size_t t = 8 * round_alloc(D * np) + 14 * round_alloc(D * nuv) + 7 * round_alloc(D * nw);
   if (precision == TPLS_PREC_FP64) {
-    t += 5 * round_alloc(D * np) + 4 * round_alloc(D * nuv) + 2 * round_alloc(D * nw);
+    // (+4 p-grid arrays of the diffuse-interface method, counted for every FP64 context)
+    t += 9 * round_alloc(D * np) + 4 * round_alloc(D * nuv) + 2 * round_alloc(D * nw);
     t += 2 * round_alloc(D * nrec * nz) + round_alloc(D * nrec * (nz + 1)) + round_alloc(D * nmu);
   } else {
     t += 6 * round_alloc(F * np) + 6 * round_alloc(F * nuv) + 3 * round_alloc(F * nw);
@@ -516,6 +529,11 @@ int tpls_gpu_create(int nx, int ny, int nz, const tpls_params *prm, const double
         prm->smooth_width > 0))
     return TPLS_ERR_ARG;
   if (prm->precision != TPLS_PREC_FP64 && prm->precision != TPLS_PREC_FP32_MIXED) return TPLS_ERR_ARG;
+  if (prm->idm != TPLS_IDM_LSM && prm->idm != TPLS_IDM_DIM) return TPLS_ERR_ARG;
+  // the diffuse-interface method is built for the FP64 form
+  if (prm->idm == TPLS_IDM_DIM &&
+      !(prm->precision == TPLS_PREC_FP64 && prm->epn > 0 && prm->pe > 0 && prm->max_iteration_dim >= 0))
+    return TPLS_ERR_ARG;
   tpls_ctx *c = new tpls_ctx();
   int s = create_impl(nx, ny, nz, prm, u_inlet, c);
   if (s != TPLS_OK) {
@@ -670,15 +688,39 @@ static int finish_eager(tpls_ctx *c, int its, double rn, double bn, int reason) 
   return TPLS_OK;
 }
 
+// Diffuse-interface update of one step (main_ns_hybrid.F90:608-611): dim on
+// C = phi2 + 0.5 (phi_old equals phi2 at every step, :444 and :2508) from
+// the starting guess phi3, then phi3 = phiNew - 0.5 into phi2 and phi3.
+// The reference logs no residual for it; err_phi reads 0.
+static int dim_stage(tpls_ctx *c, const double *conv2_phi) {
+  const Geo &g = c->g;
+  cudaStream_t st = c->st;
+  const DimK q = dim_constants(c->ph, c->prm.epn, c->prm.pe);
+  LCK(c, launch_dim_prep(g, q, c->phi2, 0.5, c->dimE, c->D, st));
+  LCK(c, launch_dim_source(g, q, c->phi2, 0.5, c->dimE, c->D, conv2_phi, c->convprev, c->dimS, st));
+  const double *pin = c->phi3d;
+  double *pp[2] = {c->phiA, c->phiB};
+  for (int it = 1; it <= c->prm.max_iteration_dim; it++) {
+    double *out = pp[(it - 1) % 2];
+    LCK(c, launch_dim_lap(g, q, pin, c->D, st));
+    LCK(c, launch_dim_update(g, q, c->phi2, 0.5, c->phi2, 0.5, c->dimS, pin, c->D, out, st));
+    pin = out;
+  }
+  LCK(c, launch_dim_finish(g, pin, c->phi2, c->phi3d, st));
+  TCK(cudaMemsetAsync(c->scal + SC_ERR_PHI, 0, sizeof(double), st));
+  return TPLS_OK;
+}
+
 static int step_once(tpls_ctx *c) {
   const Geo &g = c->g;
   const Phys &ph = c->ph;
   cudaStream_t st = c->st;
   const int s0 = c->phase % 3, s1 = (c->phase + 1) % 3, s2 = (c->phase + 2) % 3;
-  // viscosity from the pre-advection level set (main_ns_hybrid.F90:646-724)
+  // viscosity from the pre-advection level set (main_ns_hybrid.F90:646-724);
+  // the diffuse-interface method passes phi2-0.5
   {
     PhaseScope ps(c, TPLS_T_VISC);
-    LCK(c, launch_visc(g, ph, c->phi2, c->mu, st));
+    LCK(c, launch_visc(g, ph, c->phi2, c->mu, st, c->dim ? -0.5 : 0.0));
   }
   // advection (:585) and level-set update + redistancing (:596)
   {
@@ -686,20 +728,25 @@ static int step_once(tpls_ctx *c) {
     LCK(c, launch_advect(g, ph, c->phi2, c->u2, c->v2, c->w2, c->conv_phi[s2], st));
   }
   PhaseScope *ls_scope = new PhaseScope(c, TPLS_T_LEVELSET);
-  LCK(c, launch_ls_ab3(g, ph, c->phi2, c->conv_phi[s0], c->conv_phi[s1], c->conv_phi[s2], c->phiA, st));
-  LCK(c, launch_ls_status(g, ph, c->phiA, c->D, c->flags, st));
-  const int L = c->prm.levelset;
-  if (L <= 0) {
-    TCK(cudaMemcpyAsync(c->phi2 - XOFF, c->phiA - XOFF, sizeof(double) * ((size_t)c->px * (c->ny + 2) * (c->nz + 2)),
-                        cudaMemcpyDeviceToDevice, st));
-    TCK(cudaMemsetAsync(c->scal + SC_ERR_PHI, 0, sizeof(double), st));
+  if (c->dim) {
+    int sd;
+    if ((sd = dim_stage(c, c->conv_phi[s2]))) return sd;
+  } else {
+    LCK(c, launch_ls_ab3(g, ph, c->phi2, c->conv_phi[s0], c->conv_phi[s1], c->conv_phi[s2], c->phiA, st));
+    LCK(c, launch_ls_status(g, ph, c->phiA, c->D, c->flags, st));
+    const int L = c->prm.levelset;
+    if (L <= 0) {
+      TCK(cudaMemcpyAsync(c->phi2 - XOFF, c->phiA - XOFF,
+                          sizeof(double) * ((size_t)c->px * (c->ny + 2) * (c->nz + 2)), cudaMemcpyDeviceToDevice, st));
+      TCK(cudaMemsetAsync(c->scal + SC_ERR_PHI, 0, sizeof(double), st));
+    }
+    for (int it = 1; it <= L; it++) {
+      const double *src = (it == 1) ? c->phiA : ((it % 2 == 0) ? c->phiB : c->phiA);
+      double *dst = (it == L) ? c->phi2 : ((it % 2 == 1) ? c->phiB : c->phiA);
+      LCK(c, launch_ls_iter(g, ph, src, c->D, c->flags, dst, (it == L) ? c->part : nullptr, st));
+    }
+    if (L > 0) FSUM(c, c->part, ls_iter_blocks(g), c->scal + SC_ERR_PHI, st);
   }
-  for (int it = 1; it <= L; it++) {
-    const double *src = (it == 1) ? c->phiA : ((it % 2 == 0) ? c->phiB : c->phiA);
-    double *dst = (it == L) ? c->phi2 : ((it % 2 == 1) ? c->phiB : c->phiA);
-    LCK(c, launch_ls_iter(g, ph, src, c->D, c->flags, dst, (it == L) ? c->part : nullptr, st));
-  }
-  if (L > 0) FSUM(c, c->part, ls_iter_blocks(g), c->scal + SC_ERR_PHI, st);
   delete ls_scope;
   // CSF from the redistanced phi3 (:618-641)
   {
@@ -1526,6 +1573,50 @@ int tpls_do_tpls(tpls_ctx *c, double *phi2, double *phi3, double *conv0_phi, dou
   TCK(cudaMemcpyAsync(c->scal_host, c->scal, sizeof(double) * SC_N, cudaMemcpyDeviceToHost, c->st));
   TCK(cudaStreamSynchronize(c->st));
   *err2 = c->scal_host[SC_ERR_PHI];
+  return TPLS_OK;
+}
+
+int tpls_dim(tpls_ctx *c, const int *maxl, const int *maxn, const double *dx, const double *dy, const double *dz,
+             const double *dt, const double *epn, const double *pe, const double *phi, const double *phi_old,
+             const double *conv2_phi, double *conv_prev_phi, double *phi_new, const int *sx, const int *ex,
+             const int *sy, const int *ey, const int *sz_p, const int *ez_p, const double *height, const int *,
+             const int *, const int *, const int *, const int *max_iteration_dim) {
+  CHECKB(c, sx, ex, sy, ey);
+  const int nz = c->nz;
+  REQ(dx && dy && dz && dt && epn && pe && phi && phi_old && conv2_phi && conv_prev_phi && phi_new && height &&
+      max_iteration_dim);
+  REQ(*epn > 0 && *pe > 0 && *max_iteration_dim >= 0);
+  REQ(!maxl || *maxl == c->nx + 1);
+  REQ(!maxn || *maxn == nz + 1);
+  REQ(!sz_p || *sz_p == 0);
+  REQ(!ez_p || *ez_p == nz + 1);
+  int s;
+  if ((s = scratch(c))) return s;
+  Phys ph = phys_with(c, dx, dy, dz, dt);
+  ph.height = *height;
+  const DimK q = dim_constants(ph, *epn, *pe);
+  // scr[5] holds bulkE0 until the source term is formed, then the iterate's
+  // second buffer
+  double *P = c->scr[0], *O = c->scr[1], *C2 = c->scr[2], *CP = c->scr[3], *N0 = c->scr[4], *N1 = c->scr[5],
+         *L = c->scr[6], *S = c->scr[7];
+  TCK(h2d(c, P, phi, nz + 2));
+  TCK(h2d(c, O, phi_old, nz + 2));
+  TCK(h2d(c, C2, conv2_phi, nz + 2));
+  TCK(h2d(c, CP, conv_prev_phi, nz + 2));
+  TCK(h2d(c, N0, phi_new, nz + 2));
+  LCK(c, launch_dim_prep(c->g, q, P, 0.0, N1, L, c->st));
+  LCK(c, launch_dim_source(c->g, q, P, 0.0, N1, L, C2, CP, S, c->st));
+  const double *pin = N0;
+  double *pp[2] = {N1, N0};
+  for (int it = 1; it <= *max_iteration_dim; it++) {
+    double *out = pp[(it - 1) % 2];
+    LCK(c, launch_dim_lap(c->g, q, pin, L, c->st));
+    LCK(c, launch_dim_update(c->g, q, P, 0.0, O, 0.0, S, pin, L, out, c->st));
+    pin = out;
+  }
+  TCK(d2h(c, phi_new, pin, nz + 2));
+  TCK(d2h(c, conv_prev_phi, CP, nz + 2));
+  TCK(cudaStreamSynchronize(c->st));
   return TPLS_OK;
 }
 

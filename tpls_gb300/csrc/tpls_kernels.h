@@ -38,6 +38,26 @@ cudaError_t launch_advect(const Geo &g, const Phys &ph, const float *phi2,
                           double *conv2_phi, cudaStream_t st);
 cudaError_t launch_to_float(const double *a, float *b, size_t n, cudaStream_t st);
 
+// cahn_hilliard_solver.f90:41-382 dim (diffuse interface), see k_dim.cu.
+// phi + add is the concentration C (the driver's phi2 + 0.5).
+struct DimK {
+  double rdx2, rdy2, rdz2;  // 1/dx/dx, 1/dy/dy, 1/dz/dz
+  double epn2, repn, rpe;   // epn^2, 1/epn, 1/Pe
+  double c_nt2, c_en2;      // nmda*tao/2, epn^2*nmda/2
+  double dt, kc, tao, alfa1, rdiag;  // kc = dt*nmda/2/Pe, rdiag = 1/diagonal
+  double dz, height, zden;  // inlet profile: 0.5+0.5 tanh((z-height)/zden)
+};
+DimK dim_constants(const Phys &ph, double epn, double pe);
+cudaError_t launch_dim_prep(const Geo &g, const DimK &q, const double *phi, double add, double *e0, double *l0,
+                            cudaStream_t st);
+cudaError_t launch_dim_source(const Geo &g, const DimK &q, const double *phi, double add, const double *e0,
+                              const double *l0, const double *conv2, double *cprev, double *src, cudaStream_t st);
+cudaError_t launch_dim_lap(const Geo &g, const DimK &q, const double *pin, double *l, cudaStream_t st);
+cudaError_t launch_dim_update(const Geo &g, const DimK &q, const double *phi, double add, const double *phio,
+                              double addo, const double *src, const double *pin, const double *l, double *pout,
+                              cudaStream_t st);
+cudaError_t launch_dim_finish(const Geo &g, const double *pfin, double *phi2, double *phi3, cudaStream_t st);
+
 // two_phase_levelset.f90 / levelset.f90
 cudaError_t launch_ls_ab3(const Geo &g, const Phys &ph, const double *phi2,
                           const double *c0, const double *c1, const double *c2,
@@ -51,7 +71,7 @@ int ls_iter_blocks(const Geo &g);
 cudaError_t launch_csf(const Geo &g, const Phys &ph, const double *phi3,
                        double *fx, double *fy, double *fz, cudaStream_t st);
 cudaError_t launch_visc(const Geo &g, const Phys &ph, const double *phi2,
-                        double *mu, cudaStream_t st);
+                        double *mu, cudaStream_t st, double phi_offset = 0.0);
 // FP32-mixed form of the level-set kernels: status decided in FP64 with D
 // stored in FP32, the redistancing increments in FP32 on float-pair iterates,
 // CSF evaluated in FP64 and stored in FP32, viscosity stored in FP32 (the
