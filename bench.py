@@ -39,7 +39,7 @@ sys.path.insert(0, str(ROOT))
 
 import numpy as np  # noqa: E402
 
-BASELINE_METRIC = "cell-steps/s FP64 vs FP32-mixed at stated phi/u error; jobs/s, p50/p99 latency"
+HEADLINE_METRIC = "cell-steps/s FP64 vs FP32-mixed at stated phi/u error; jobs/s, p50/p99 latency"
 
 
 def _peaks() -> dict:
@@ -290,7 +290,7 @@ def run_gpu(args, ws, rank, local) -> dict | None:
                    "l2": f"working set ~{cells * 500 / 1e9:.0f} GB per step >> 129 MB L2 (no flush needed)",
                    "launch": "one CUDA graph per step (device-side WHILE node for the pressure CG)",
                    "grid_geometry": "cubic cells dx=dy=dz=1/nz (the reference's initialisation grid)",
-                   "baseline_metric": BASELINE_METRIC},
+                   "headline_metric": HEADLINE_METRIC},
         "e2e": {"value": e2e, "unit": "cell-steps/s", "h2d_bytes_per_step": bi, "d2h_bytes_per_step": bi,
                 "steps": ke, "path": f"tpls_set_field x{len(state_fields)} -> tpls_step(1) -> "
                                      f"tpls_get_field x{len(state_fields)} per step"},
@@ -479,7 +479,7 @@ def run_batch(args, ws, rank, local) -> dict | None:
                    "launch": "one CUDA graph per batch step (every member's step as a branch)",
                    "timing": "host wall clock around synchronised batch steps",
                    "l2": f"working set ~{cells * 300 / 1e9:.0f} GB per step >> 129 MB L2",
-                   "baseline_metric": BASELINE_METRIC},
+                   "headline_metric": HEADLINE_METRIC},
         "jobs_per_s": ws * len(insts) / sec,
         "e2e": {"value": ws * cells * args.steps / e2e_sec, "unit": "cell-steps/s",
                 "h2d_bytes_per_step": bi / args.steps, "d2h_bytes_per_step": bi / args.steps,
@@ -537,7 +537,7 @@ def run_serve(args, ws, rank, local) -> dict | None:
                                f"{args.rate} jobs/s, grids up to 384x192x192, budgets 50-1000 steps, 160 GB "
                                f"admission, snapshots every 50 steps",
                    "timing": "host wall clock from the first arrival to the last completion",
-                   "baseline_metric": BASELINE_METRIC},
+                   "headline_metric": HEADLINE_METRIC},
         "serve": forms,
         "p50_latency_s": mx["p50_latency_s"],
         "p99_latency_s": mx["p99_latency_s"],
