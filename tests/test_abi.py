@@ -90,3 +90,31 @@ def test_base_profile_matches_oracle_recurrence():
             diag = (mpk + mmk) / (dz * dz)
             ref[k] = (1.0 / diag) * (((mpk * upz + mmk * umz) / (dz * dz)) - dpdl)
     assert np.max(np.abs(u - ref[:nz])) <= 1e-12 * np.max(np.abs(ref))
+
+
+@pytest.mark.parametrize("cls_name,c_name", [("TplsParams", "tpls_params"),
+                                             ("TplsStats", "tpls_stats")])
+def test_ctypes_structs_match_header_layout(tmp_path, cls_name, c_name):
+    """The Python mirrors of the header's structs have the C compiler's size and
+    field offsets (a drifted mirror would pass garbage to every entry point)."""
+    import shutil
+    import subprocess
+    import tpls_gb300.api as api
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    cls = getattr(api, cls_name)
+    lines = [f'printf("size %zu\\n", sizeof({c_name}));']
+    for f, _ in cls._fields_:
+        lines.append(f'printf("{f} %zu\\n", offsetof({c_name}, {f}));')
+    src = tmp_path / "layout.c"
+    src.write_text("#include <stddef.h>\n#include <stdio.h>\n#include \"tpls_gpu.h\"\n"
+                   "int main(void) {\n" + "\n".join(lines) + "\nreturn 0;\n}\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c11", "-I", str(ROOT / "include"), str(src), "-o", str(exe)],
+                   check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
+    got = dict(line.split() for line in out.splitlines())
+    assert int(got["size"]) == C.sizeof(cls)
+    for f, _ in cls._fields_:
+        assert int(got[f]) == getattr(cls, f).offset, f
