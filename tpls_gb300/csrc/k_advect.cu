@@ -39,6 +39,16 @@ __device__ __forceinline__ T weno5(T v1, T v2, T v3, T v4, T v5) {
   return (n1 * p1 + n2 * p2 + n3 * p3) / (n1 + n2 + n3);
 }
 
+// The upwind WENO5 value on the face between c0 and p1 of a line of six
+// points m2 m1 c0 p1 p2 p3: the stencil m2..p2 when the face velocity is
+// >= 0, else p3..m1 (weno.f90:52-60, 64-72).  The stencil is selected before
+// the one weno5 evaluation, so a warp whose lanes see both signs does not
+// run weno5 twice.
+template <typename T>
+__device__ __forceinline__ T weno_up(bool pos, T m2, T m1, T c0, T p1, T p2, T p3) {
+  return weno5(pos ? m2 : p3, pos ? m1 : p2, pos ? c0 : p1, pos ? p1 : c0, pos ? p2 : m1);
+}
+
 // dfx at u-index (iu, jp-1, kp-1): phi along x at p-row jp, level kp.
 // WENO for 3 <= iu <= nx-2, first-order upwind otherwise (weno.f90:45-100).
 template <typename T>
@@ -48,10 +58,8 @@ __device__ __forceinline__ T xface(const Geo &g, const T *__restrict__ phi,
   const int ju = (jp - 1 == 0) ? g.ny : jp - 1;
   const T vel = u[TPLS_IDX(g, iu, ju, kp - 1)];
   const T *row = phi + TPLS_IDX(g, 0, jp, kp);
-  if (iu >= 3 && iu <= g.nx - 2) {
-    if (vel >= (T)0) return weno5(row[iu - 2], row[iu - 1], row[iu], row[iu + 1], row[iu + 2]);
-    return weno5(row[iu + 3], row[iu + 2], row[iu + 1], row[iu], row[iu - 1]);
-  }
+  if (iu >= 3 && iu <= g.nx - 2)
+    return weno_up(vel >= (T)0, row[iu - 2], row[iu - 1], row[iu], row[iu + 1], row[iu + 2], row[iu + 3]);
   return (vel >= (T)0) ? row[iu] : row[iu + 1];
 }
 
@@ -67,57 +75,71 @@ __device__ __forceinline__ T yface(const Geo &g, const T *__restrict__ phi,
   const T *col = phi + TPLS_IDX(g, ip, 0, kp);
   const int sy = g.sy;
 #define PY(jj) col[sy * wrapy((jj), ny)]
-  if (vel >= (T)0) return weno5(PY(jv - 2), PY(jv - 1), PY(jv), PY(jv + 1), PY(jv + 2));
-  return weno5(PY(jv + 3), PY(jv + 2), PY(jv + 1), PY(jv), PY(jv - 1));
+  return weno_up(vel >= (T)0, PY(jv - 2), PY(jv - 1), PY(jv), PY(jv + 1), PY(jv + 2), PY(jv + 3));
 #undef PY
-}
-
-// dfz at w-index (ip, jp-1, kw): phi along z at x=ip, row jp.  WENO for
-// 3 <= kw <= nz-2, arithmetic mean otherwise (weno.f90:136-166).
-template <typename T>
-__device__ __forceinline__ T zface(const Geo &g, const T *__restrict__ phi,
-                                        const T *__restrict__ w, int ip, int jp,
-                                        int kw) {
-  const int ju = (jp - 1 == 0) ? g.ny : jp - 1;
-  const T *col = phi + TPLS_IDX(g, ip, jp, 0);
-  const int sz = g.sz;
-  if (kw >= 3 && kw <= g.nz - 2) {
-    const T vel = w[TPLS_IDX(g, ip, ju, kw)];
-    if (vel >= (T)0)
-      return weno5(col[sz * (kw - 2)], col[sz * (kw - 1)], col[sz * kw], col[sz * (kw + 1)],
-                   col[sz * (kw + 2)]);
-    return weno5(col[sz * (kw + 3)], col[sz * (kw + 2)], col[sz * (kw + 1)], col[sz * kw],
-                 col[sz * (kw - 1)]);
-  }
-  return (col[sz * kw] + col[sz * (kw + 1)]) / (T)2;
 }
 
 constexpr int ADV_BX = 32, ADV_BY = 8;
 constexpr int ADV_KC = 16;  // z levels per thread (column chunk)
 
+// One block covers 32 x 8 columns and a chunk of ADV_KC levels.  At each
+// level every thread computes the x-face right of its cell and the y-face
+// above it; the faces left of the block's first column (8, one per row) are
+// computed by eight lanes of warp 1 and those below its first row (32) by
+// warp 0, so the extra faces cost about two warp evaluations per block and
+// level instead of one per warp.  Faces pass through a double-buffered
+// shared tile (one barrier per level).  The z-faces come from a six-point
+// window of the column held in registers, one new load per level.
 template <typename T>
-__global__ void __launch_bounds__(ADV_BX *ADV_BY)
+__global__ void __launch_bounds__(ADV_BX *ADV_BY, 4)
     k_advect(Geo g, T rdx, T rdy, T rdz, const T *__restrict__ phi, const T *__restrict__ u,
              const T *__restrict__ v, const T *__restrict__ w, double *__restrict__ conv) {
-  __shared__ T yf_s[ADV_BY][ADV_BX];
+  __shared__ T xs[2][ADV_BY][ADV_BX + 1];  // x-faces iu = i0-1 .. i0+31 per row
+  __shared__ T ys[2][ADV_BY + 1][ADV_BX];  // y-faces jv = j0-1 .. j0+7 per column
   const int tx = threadIdx.x, ty = threadIdx.y;
-  const int i = blockIdx.x * ADV_BX + tx + 1;
-  const int j = blockIdx.y * ADV_BY + ty + 1;
+  const int i0 = blockIdx.x * ADV_BX + 1, j0 = blockIdx.y * ADV_BY + 1;
+  const int i = i0 + tx, j = j0 + ty;
   const int k0 = blockIdx.z * ADV_KC + 1, k1 = min(k0 + ADV_KC - 1, g.nz);
   const bool act = (i <= g.nx) && (j <= g.ny);
   const int ic = act ? i : 1, jc = act ? j : 1;  // clamped for inactive lanes
   const int jm = (jc == 1) ? g.ny : jc - 1;      // u/v/w row index j-1 (wrapped)
-  T zlo = zface(g, phi, w, ic, jc, k0 - 1);
+  // the row whose left x-face this lane computes when it is one of warp 1's
+  // first eight lanes (clamped like jc)
+  const int jx = (j0 + tx <= g.ny) ? j0 + tx : 1;
+  // z window c0..c5 = phi(ic, jc, kw-2 .. kw+3) for the z-face kw (w-index),
+  // indices clamped to the array's 0..nz+1; the clamped entries are read only
+  // where the face is the arithmetic mean of c2 and c3 (kw < 3 or kw > nz-2)
+  const T *col = phi + TPLS_IDX(g, ic, jc, 0);
+  const int sz = g.sz, nzp1 = g.nz + 1;
+  auto zld = [&](int kk) { return col[(size_t)sz * min(max(kk, 0), nzp1)]; };
+  // dfz at w-index (ic, jc-1, kw): WENO for 3 <= kw <= nz-2, arithmetic mean
+  // otherwise (weno.f90:136-166)
+  auto zface = [&](int kw, T c0, T c1, T c2, T c3, T c4, T c5) -> T {
+    if (kw >= 3 && kw <= g.nz - 2) return weno_up(w[TPLS_IDX(g, ic, jm, kw)] >= (T)0, c0, c1, c2, c3, c4, c5);
+    return (c2 + c3) / (T)2;
+  };
+  T c0 = zld(k0 - 3), c1 = zld(k0 - 2), c2 = zld(k0 - 1), c3 = zld(k0), c4 = zld(k0 + 1), c5 = zld(k0 + 2);
+  T zlo = zface(k0 - 1, c0, c1, c2, c3, c4, c5);
   for (int k = k0; k <= k1; k++) {
+    const int b = k & 1;
+    c0 = c1;
+    c1 = c2;
+    c2 = c3;
+    c3 = c4;
+    c4 = c5;
+    c5 = zld(k + 3);
     const T xo = xface(g, phi, u, ic, jc, k);
-    T xl = __shfl_up_sync(0xffffffffu, xo, 1);
-    if (tx == 0) xl = xface(g, phi, u, ic - 1, jc, k);
     const T yo = yface(g, phi, v, ic, jc, k);
-    yf_s[ty][tx] = yo;
+    xs[b][ty][tx + 1] = xo;
+    ys[b][ty + 1][tx] = yo;
+    if (ty == 0)
+      ys[b][0][tx] = yface(g, phi, v, ic, jc - 1, k);
+    else if (ty == 1 && tx < ADV_BY)
+      xs[b][tx][0] = xface(g, phi, u, i0 - 1, jx, k);
+    const T zo = zface(k, c0, c1, c2, c3, c4, c5);
     __syncthreads();
-    const T yl = (ty > 0) ? yf_s[ty - 1][tx] : yface(g, phi, v, ic, jc - 1, k);
-    const T zo = zface(g, phi, w, ic, jc, k);
     if (act) {
+      const T xl = xs[b][ty][tx], yl = ys[b][ty][tx];
       const T fxp = u[TPLS_IDX(g, i, jm, k - 1)] * xo;
       const T fxm = u[TPLS_IDX(g, i - 1, jm, k - 1)] * xl;
       const T fyp = v[TPLS_IDX(g, i, j, k - 1)] * yo;
@@ -127,7 +149,6 @@ __global__ void __launch_bounds__(ADV_BX *ADV_BY)
       conv[TPLS_IDX(g, i, j, k)] = (double)((fxp - fxm) * rdx + (fyp - fym) * rdy + (fzp - fzm) * rdz);
     }
     zlo = zo;
-    __syncthreads();
   }
 }
 

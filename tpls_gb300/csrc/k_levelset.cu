@@ -122,26 +122,30 @@ cudaError_t launch_ls_status(const Geo &g, const Phys &ph, const double *phi3, f
 template <typename TC, typename LD>
 __device__ __forceinline__ TC rs_dc(const Geo &g, TC h, const LD &pr, TC p, const TC *__restrict__ D, int f,
                                    int c) {
-  const TC sg = (TC)(((f >> 1) & 3) - 1);
+  // s = sign(phi) + 1.  The products sg * X of the reference (sg = -1, 0, 1)
+  // are written as selects and negations, which are exact: no int-to-FP64
+  // conversion, compare or multiply on GB300's FP64 pipe.
+  const int s = (f >> 1) & 3;
   const TC zero = (TC)0;
   TC dc;
   if (f & 1) {
-    dc = sg * fabs(p) - D[c];
-  } else if (sg > zero) {
+    const TC ap = fabs(p);
+    dc = ((s == 2) ? ap : ((s == 0) ? -ap : zero)) - D[c];
+  } else if (s == 2) {
     // max(aP^2, bM^2) with aP = max(p - p[i-1], 0), bM = min(p[i+1] - p, 0)
     // equals max(p - min(p[i-1], p[i+1]), 0)^2 bit for bit (rounding of a
     // difference and of a square are monotone), likewise in y and z.
     const TC ax = fmax(p - fmin(pr[c - 1], pr[c + 1]), zero);
     const TC ay = fmax(p - fmin(pr[c - g.sy], pr[c + g.sy]), zero);
     const TC az = fmax(p - fmin(pr[c - g.sz], pr[c + g.sz]), zero);
-    dc = sg * (sqrt(ax * ax + ay * ay + az * az) - h);
-  } else if (sg < zero) {
+    dc = sqrt(ax * ax + ay * ay + az * az) - h;
+  } else if (s == 0) {
     // max(bP^2, aM^2) = max(max(p[i-1], p[i+1]) - p, 0)^2, likewise y, z
     const TC ax = fmax(fmax(pr[c - 1], pr[c + 1]) - p, zero);
     const TC ay = fmax(fmax(pr[c - g.sy], pr[c + g.sy]) - p, zero);
     const TC az = fmax(fmax(pr[c - g.sz], pr[c + g.sz]) - p, zero);
     // levelset.f90:274-275 sums x, then z, then y
-    dc = sg * (sqrt(ax * ax + az * az + ay * ay) - h);
+    dc = -(sqrt(ax * ax + az * az + ay * ay) - h);
   } else {
     dc = zero;
   }
