@@ -39,6 +39,15 @@ __device__ __forceinline__ T weno5(T v1, T v2, T v3, T v4, T v5) {
   return (n1 * p1 + n2 * p2 + n3 * p3) / (n1 + n2 + n3);
 }
 
+// vel >= 0 (-0 included) from the sign bit for FP64, so the upwind choice
+// takes no FP64 compare; a NaN velocity (a diverged state) may pick either
+// stencil.
+__device__ __forceinline__ bool upwind_pos(double v) {
+  const long long b = __double_as_longlong(v);
+  return b >= 0 || b == (long long)0x8000000000000000ULL;
+}
+__device__ __forceinline__ bool upwind_pos(float v) { return v >= 0.0f; }
+
 // The upwind WENO5 value on the face between c0 and p1 of a line of six
 // points m2 m1 c0 p1 p2 p3: the stencil m2..p2 when the face velocity is
 // >= 0, else p3..m1 (weno.f90:52-60, 64-72).  The stencil is selected before
@@ -59,8 +68,8 @@ __device__ __forceinline__ T xface(const Geo &g, const T *__restrict__ phi,
   const T vel = u[TPLS_IDX(g, iu, ju, kp - 1)];
   const T *row = phi + TPLS_IDX(g, 0, jp, kp);
   if (iu >= 3 && iu <= g.nx - 2)
-    return weno_up(vel >= (T)0, row[iu - 2], row[iu - 1], row[iu], row[iu + 1], row[iu + 2], row[iu + 3]);
-  return (vel >= (T)0) ? row[iu] : row[iu + 1];
+    return weno_up(upwind_pos(vel), row[iu - 2], row[iu - 1], row[iu], row[iu + 1], row[iu + 2], row[iu + 3]);
+  return (upwind_pos(vel)) ? row[iu] : row[iu + 1];
 }
 
 // dfy at v-index (ip, jv, kp-1): phi along y at x=ip, level kp, periodic
@@ -75,7 +84,7 @@ __device__ __forceinline__ T yface(const Geo &g, const T *__restrict__ phi,
   const T *col = phi + TPLS_IDX(g, ip, 0, kp);
   const int sy = g.sy;
 #define PY(jj) col[sy * wrapy((jj), ny)]
-  return weno_up(vel >= (T)0, PY(jv - 2), PY(jv - 1), PY(jv), PY(jv + 1), PY(jv + 2), PY(jv + 3));
+  return weno_up(upwind_pos(vel), PY(jv - 2), PY(jv - 1), PY(jv), PY(jv + 1), PY(jv + 2), PY(jv + 3));
 #undef PY
 }
 
@@ -115,7 +124,7 @@ __global__ void __launch_bounds__(ADV_BX *ADV_BY, 4)
   // dfz at w-index (ic, jc-1, kw): WENO for 3 <= kw <= nz-2, arithmetic mean
   // otherwise (weno.f90:136-166)
   auto zface = [&](int kw, T c0, T c1, T c2, T c3, T c4, T c5) -> T {
-    if (kw >= 3 && kw <= g.nz - 2) return weno_up(w[TPLS_IDX(g, ic, jm, kw)] >= (T)0, c0, c1, c2, c3, c4, c5);
+    if (kw >= 3 && kw <= g.nz - 2) return weno_up(upwind_pos(w[TPLS_IDX(g, ic, jm, kw)]), c0, c1, c2, c3, c4, c5);
     return (c2 + c3) / (T)2;
   };
   T c0 = zld(k0 - 3), c1 = zld(k0 - 2), c2 = zld(k0 - 1), c3 = zld(k0), c4 = zld(k0 + 1), c5 = zld(k0 + 2);

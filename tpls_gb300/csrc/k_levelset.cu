@@ -9,6 +9,7 @@
 // on the interior values it needs.  That replaces the reference's sequence
 // of interior pass + boundary passes + exchange2d with one launch, with
 // identical values.
+#include <cstring>
 #include <type_traits>
 
 #include "tpls_kernels.h"
@@ -64,6 +65,17 @@ cudaError_t launch_ls_ab3(const Geo &g, const Phys &ph, const double *phi2,
 // levelset.f90:17-94 get_levelset_status with h = dx.  flags packs the
 // indicator istatus (bit 0) and sign(phi)+1 (bits 1-2); D and flags are 0
 // outside the interior.
+// p*q <= 0 for the rounded FP64 product, from the operands' bits: a zero
+// operand or differing signs, as long as the product cannot underflow to
+// zero (both magnitudes >= 2^-511, biased exponent >= 512); smaller nonzero
+// operands take the FP64 product itself.
+__device__ __forceinline__ bool prod_le0(double p, double q) {
+  const long long a = __double_as_longlong(p), b = __double_as_longlong(q);
+  if ((a << 1) == 0 || (b << 1) == 0) return true;
+  if (((a >> 52) & 0x7ff) >= 512 && ((b >> 52) & 0x7ff) >= 512) return (a ^ b) < 0;
+  return p * q <= 0.0;
+}
+
 template <typename T>
 __global__ void k_ls_status(Geo g, double h, const double *__restrict__ phi, T *__restrict__ D,
                             signed char *__restrict__ flags) {
@@ -78,19 +90,24 @@ __global__ void k_ls_status(Geo g, double h, const double *__restrict__ phi, T *
   }
   // FP64 in both forms: the status flags are discrete decisions, so the
   // FP32-mixed form takes them from the same arithmetic as the FP64 form
-  // and only stores D in FP32.
+  // and only stores D in FP32.  Signs, the test min(p*q) <= 0 and the
+  // maxima are taken from the bit patterns (exact; GB300's FP64 pipe keeps
+  // only the band's arithmetic).
   const double p = phi[c];
   const double pxp = phi[c + 1], pxm = phi[c - 1], pyp = phi[c + g.sy], pym = phi[c - g.sy];
   const double pzp = phi[c + g.sz], pzm = phi[c - g.sz];
-  const int sgn = (p < 0.0) ? -1 : ((p > 0.0) ? 1 : 0);
-  const double mn = fmin(fmin(fmin(p * pxp, p * pxm), fmin(p * pyp, p * pym)), fmin(p * pzp, p * pzm));
-  const int st = (mn <= 0.0) ? 1 : 0;
+  const long long pb = __double_as_longlong(p);
+  const int sgn = ((pb << 1) == 0) ? 0 : ((pb < 0) ? -1 : 1);
+  const int st = (prod_le0(p, pxp) || prod_le0(p, pxm) || prod_le0(p, pyp) || prod_le0(p, pym) ||
+                  prod_le0(p, pzp) || prod_le0(p, pzm))
+                     ? 1
+                     : 0;
   double d = 0.0;
   if (st) {
     const double gx = pxp - pxm, gy = pyp - pym, gz = pzp - pzm;
     const double b1 = sqrt(gx * gx + gy * gy + gz * gz) * 0.5;
-    double mx = fmax(fmax(fabs(pxp - p), fabs(pxm - p)), fmax(fabs(pyp - p), fabs(pym - p)));
-    mx = fmax(fmax(mx, fmax(fabs(pzp - p), fabs(pzm - p))), fmax(b1, h));
+    double mx = dmax_bits(dmax_bits(fabs(pxp - p), fabs(pxm - p)), dmax_bits(fabs(pyp - p), fabs(pym - p)));
+    mx = dmax_bits(dmax_bits(mx, dmax_bits(fabs(pzp - p), fabs(pzm - p))), dmax_bits(b1, h));
     d = h * p / mx;
   }
   D[c] = (T)d;
@@ -119,6 +136,25 @@ cudaError_t launch_ls_status(const Geo &g, const Phys &ph, const double *phi3, f
 // iterate accumulates no FP32 rounding across the iterations and steps.
 // dc of the update at point c, p = its value, pr a loader of the stencil
 // values in the arithmetic type TC.
+// min, max and max(., 0) of the stencil: for FP64 by integer operations
+// (GB300's FP64 pipe would otherwise spend 9 of ~25 instructions per point on
+// them), for FP32 on the FP32 pipe.
+template <typename TC>
+__device__ __forceinline__ TC rs_min(TC a, TC b) {
+  if constexpr (sizeof(TC) == sizeof(double)) return dmin_bits(a, b);
+  else return fminf(a, b);
+}
+template <typename TC>
+__device__ __forceinline__ TC rs_max(TC a, TC b) {
+  if constexpr (sizeof(TC) == sizeof(double)) return dmax_bits(a, b);
+  else return fmaxf(a, b);
+}
+template <typename TC>
+__device__ __forceinline__ TC rs_pos(TC a) {
+  if constexpr (sizeof(TC) == sizeof(double)) return dpos_bits(a);
+  else return fmaxf(a, 0.0f);
+}
+
 template <typename TC, typename LD>
 __device__ __forceinline__ TC rs_dc(const Geo &g, TC h, const LD &pr, TC p, const TC *__restrict__ D, int f,
                                    int c) {
@@ -135,15 +171,15 @@ __device__ __forceinline__ TC rs_dc(const Geo &g, TC h, const LD &pr, TC p, cons
     // max(aP^2, bM^2) with aP = max(p - p[i-1], 0), bM = min(p[i+1] - p, 0)
     // equals max(p - min(p[i-1], p[i+1]), 0)^2 bit for bit (rounding of a
     // difference and of a square are monotone), likewise in y and z.
-    const TC ax = fmax(p - fmin(pr[c - 1], pr[c + 1]), zero);
-    const TC ay = fmax(p - fmin(pr[c - g.sy], pr[c + g.sy]), zero);
-    const TC az = fmax(p - fmin(pr[c - g.sz], pr[c + g.sz]), zero);
+    const TC ax = rs_pos(p - rs_min(pr[c - 1], pr[c + 1]));
+    const TC ay = rs_pos(p - rs_min(pr[c - g.sy], pr[c + g.sy]));
+    const TC az = rs_pos(p - rs_min(pr[c - g.sz], pr[c + g.sz]));
     dc = sqrt(ax * ax + ay * ay + az * az) - h;
   } else if (s == 0) {
     // max(bP^2, aM^2) = max(max(p[i-1], p[i+1]) - p, 0)^2, likewise y, z
-    const TC ax = fmax(fmax(pr[c - 1], pr[c + 1]) - p, zero);
-    const TC ay = fmax(fmax(pr[c - g.sy], pr[c + g.sy]) - p, zero);
-    const TC az = fmax(fmax(pr[c - g.sz], pr[c + g.sz]) - p, zero);
+    const TC ax = rs_pos(rs_max(pr[c - 1], pr[c + 1]) - p);
+    const TC ay = rs_pos(rs_max(pr[c - g.sy], pr[c + g.sy]) - p);
+    const TC az = rs_pos(rs_max(pr[c - g.sz], pr[c + g.sz]) - p);
     // levelset.f90:274-275 sums x, then z, then y
     dc = -(sqrt(ax * ax + az * az + ay * ay) - h);
   } else {
@@ -501,28 +537,46 @@ cudaError_t launch_csf(const Geo &g, const Phys &ph, const double *phi3, float *
 // momentum_allflux.f90:474-521 get_viscosity on x = 0..nx+1 (the ghost
 // planes of main_ns_hybrid.F90:653-710 use the same formula and the same
 // single-precision pi) and the 2-row periodic-y augmentation.
+// Outside the band |p| <= sw the smoothed Heaviside is exactly 0 or 1 and the
+// viscosity exactly mu_minus/re or mu_plus/re (the host's IEEE quotients,
+// mlo and mhi); the band test compares order keys of the bit patterns
+// (klo = key(-sw), khi = key(sw)), so those points use no FP64 instruction.
 template <typename T>
-__global__ void k_visc(Geo g, Phys ph, const double *__restrict__ phi, double off, T *__restrict__ mu) {
+__global__ void k_visc(Geo g, Phys ph, const double *__restrict__ phi, double off, long long klo,
+                       long long khi, double mlo, double mhi, T *__restrict__ mu) {
   const int i = blockIdx.x * LS_BX + threadIdx.x, j = blockIdx.y * LS_BY + threadIdx.y - 1;
   const int k = blockIdx.z;
   if (i > g.nx + 1 || j > g.ny + 2) return;
   // off: -0.5 for the diffuse-interface method, which passes phi2-0.5
-  // (main_ns_hybrid.F90:650, :667, :692)
-  const double p = phi[TPLS_IDX(g, i, wrapy(j, g.ny), k)] + off;
-  double hv;
-  if (p < -ph.sw)
-    hv = 0.0;
-  else if (p > ph.sw)
-    hv = 1.0;
-  else
-    hv = 0.5 + (p / (2.0 * ph.sw)) + (1.0 / (2.0 * TPLS_PI_SP)) * sin(TPLS_PI_SP * p / ph.sw);
-  mu[TPLS_IDXM(g, i, j, k)] = (T)((ph.mu_plus * hv + ph.mu_minus * (1.0 - hv)) / ph.re);
+  // (main_ns_hybrid.F90:650, :667, :692); 0 for the level set, where adding
+  // it would change nothing but the sign of a zero
+  double p = phi[TPLS_IDX(g, i, wrapy(j, g.ny), k)];
+  if (__double_as_longlong(off) != 0) p += off;
+  const long long kp = dkey(p);
+  double m;
+  if (kp < klo) {
+    m = mlo;
+  } else if (kp > khi) {
+    m = mhi;
+  } else {
+    const double hv = 0.5 + (p / (2.0 * ph.sw)) + (1.0 / (2.0 * TPLS_PI_SP)) * sin(TPLS_PI_SP * p / ph.sw);
+    m = (ph.mu_plus * hv + ph.mu_minus * (1.0 - hv)) / ph.re;
+  }
+  mu[TPLS_IDXM(g, i, j, k)] = (T)m;
+}
+
+static long long host_dkey(double a) {
+  long long b;
+  memcpy(&b, &a, sizeof b);
+  return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
 }
 
 cudaError_t launch_visc(const Geo &g, const Phys &ph, const double *phi2,
                         double *mu, cudaStream_t st, double phi_offset) {
   dim3 grd((g.nx + 2 + LS_BX - 1) / LS_BX, (g.ny + 4 + LS_BY - 1) / LS_BY, g.nz + 2);
-  k_visc<double><<<grd, dim3(LS_BX, LS_BY), 0, st>>>(g, ph, phi2, phi_offset, mu);
+  k_visc<double><<<grd, dim3(LS_BX, LS_BY), 0, st>>>(g, ph, phi2, phi_offset, host_dkey(-ph.sw),
+                                                     host_dkey(ph.sw), ph.mu_minus / ph.re,
+                                                     ph.mu_plus / ph.re, mu);
   return cudaGetLastError();
 }
 // The FP32 viscosity of the FP32-mixed form: the same formula in FP32 on

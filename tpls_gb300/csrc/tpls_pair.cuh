@@ -63,4 +63,20 @@ __device__ __forceinline__ float round_bits(double x) { return val(split_bits(x)
 __device__ __forceinline__ F2 pmin(F2 a, F2 b) { return (b.h < a.h || (b.h == a.h && b.l < a.l)) ? b : a; }
 __device__ __forceinline__ F2 pmax(F2 a, F2 b) { return (b.h > a.h || (b.h == a.h && b.l > a.l)) ? b : a; }
 
+// FP64 min and max by integer operations.  The key maps the bit pattern of
+// a double to a signed integer with the same order (negative values have
+// their magnitude bits flipped), so for non-NaN a, b: a < b iff
+// dkey(a) < dkey(b), with -0 just below +0.  That differs from fmin/fmax
+// only in which zero a (+0, -0) tie returns; every use here squares the
+// result or subtracts it from a value and squares that, where the sign of
+// a zero does not survive.
+__device__ __forceinline__ long long dkey(double a) {
+  const long long b = __double_as_longlong(a);
+  return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+__device__ __forceinline__ double dmin_bits(double a, double b) { return (dkey(b) < dkey(a)) ? b : a; }
+__device__ __forceinline__ double dmax_bits(double a, double b) { return (dkey(a) < dkey(b)) ? b : a; }
+// max(a, 0) for a not NaN: +0 for a <= 0 (the sign bit decides)
+__device__ __forceinline__ double dpos_bits(double a) { return (__double_as_longlong(a) < 0) ? 0.0 : a; }
+
 }  // namespace tpls
