@@ -67,13 +67,34 @@ cudaError_t launch_ls_ab3(const Geo &g, const Phys &ph, const double *phi2,
 // outside the interior.
 // p*q <= 0 for the rounded FP64 product, from the operands' bits: a zero
 // operand or differing signs, as long as the product cannot underflow to
-// zero (both magnitudes >= 2^-511, biased exponent >= 512); smaller nonzero
-// operands take the FP64 product itself.
-__device__ __forceinline__ bool prod_le0(double p, double q) {
+// zero (both magnitudes >= 2^-511, biased exponent >= 512).  Returns 1 for
+// <= 0, 0 for > 0 and 2 when an operand is too small to decide by bits.
+__device__ __forceinline__ int prod_le0_bits(double p, double q) {
   const long long a = __double_as_longlong(p), b = __double_as_longlong(q);
-  if ((a << 1) == 0 || (b << 1) == 0) return true;
-  if (((a >> 52) & 0x7ff) >= 512 && ((b >> 52) & 0x7ff) >= 512) return (a ^ b) < 0;
-  return p * q <= 0.0;
+  if ((a << 1) == 0 || (b << 1) == 0) return 1;
+  if (((a >> 52) & 0x7ff) >= 512 && ((b >> 52) & 0x7ff) >= 512) return ((a ^ b) < 0) ? 1 : 0;
+  return 2;
+}
+
+// levelset.f90:60-71 the reference's test itself, for points with an operand
+// below 2^-511 (a call, so the other points carry none of its FP64
+// instructions)
+__device__ __noinline__ int status_products(double p, double pxp, double pxm, double pyp, double pym, double pzp,
+                                            double pzm) {
+  const double mn = fmin(fmin(fmin(p * pxp, p * pxm), fmin(p * pyp, p * pym)), fmin(p * pzp, p * pzm));
+  return (mn <= 0.0) ? 1 : 0;
+}
+
+// levelset.f90:75-85 the distance estimate D of an interface point.  A
+// call: about 6% of the warps hold an interface point, and if-converted into
+// the kernel its ~30 FP64 instructions would occupy the FP64 pipe in all.
+__device__ __noinline__ double status_distance(double h, double p, double pxp, double pxm, double pyp,
+                                               double pym, double pzp, double pzm) {
+  const double gx = pxp - pxm, gy = pyp - pym, gz = pzp - pzm;
+  const double b1 = sqrt(gx * gx + gy * gy + gz * gz) * 0.5;
+  double mx = dmax_bits(dmax_bits(fabs(pxp - p), fabs(pxm - p)), dmax_bits(fabs(pyp - p), fabs(pym - p)));
+  mx = dmax_bits(dmax_bits(mx, dmax_bits(fabs(pzp - p), fabs(pzm - p))), dmax_bits(b1, h));
+  return h * p / mx;
 }
 
 template <typename T>
@@ -98,18 +119,10 @@ __global__ void k_ls_status(Geo g, double h, const double *__restrict__ phi, T *
   const double pzp = phi[c + g.sz], pzm = phi[c - g.sz];
   const long long pb = __double_as_longlong(p);
   const int sgn = ((pb << 1) == 0) ? 0 : ((pb < 0) ? -1 : 1);
-  const int st = (prod_le0(p, pxp) || prod_le0(p, pxm) || prod_le0(p, pyp) || prod_le0(p, pym) ||
-                  prod_le0(p, pzp) || prod_le0(p, pzm))
-                     ? 1
-                     : 0;
-  double d = 0.0;
-  if (st) {
-    const double gx = pxp - pxm, gy = pyp - pym, gz = pzp - pzm;
-    const double b1 = sqrt(gx * gx + gy * gy + gz * gz) * 0.5;
-    double mx = dmax_bits(dmax_bits(fabs(pxp - p), fabs(pxm - p)), dmax_bits(fabs(pyp - p), fabs(pym - p)));
-    mx = dmax_bits(dmax_bits(mx, dmax_bits(fabs(pzp - p), fabs(pzm - p))), dmax_bits(b1, h));
-    d = h * p / mx;
-  }
+  const int q = prod_le0_bits(p, pxp) | prod_le0_bits(p, pxm) | prod_le0_bits(p, pyp) |
+                prod_le0_bits(p, pym) | prod_le0_bits(p, pzp) | prod_le0_bits(p, pzm);
+  const int st = (q & 2) ? status_products(p, pxp, pxm, pyp, pym, pzp, pzm) : (q & 1);
+  const double d = st ? status_distance(h, p, pxp, pxm, pyp, pym, pzp, pzm) : 0.0;
   D[c] = (T)d;
   flags[c] = (signed char)(st | ((sgn + 1) << 1));
 }
@@ -136,23 +149,10 @@ cudaError_t launch_ls_status(const Geo &g, const Phys &ph, const double *phi3, f
 // iterate accumulates no FP32 rounding across the iterations and steps.
 // dc of the update at point c, p = its value, pr a loader of the stencil
 // values in the arithmetic type TC.
-// min, max and max(., 0) of the stencil: for FP64 by integer operations
-// (GB300's FP64 pipe would otherwise spend 9 of ~25 instructions per point on
-// them), for FP32 on the FP32 pipe.
-template <typename TC>
-__device__ __forceinline__ TC rs_min(TC a, TC b) {
-  if constexpr (sizeof(TC) == sizeof(double)) return dmin_bits(a, b);
-  else return fminf(a, b);
-}
-template <typename TC>
-__device__ __forceinline__ TC rs_max(TC a, TC b) {
-  if constexpr (sizeof(TC) == sizeof(double)) return dmax_bits(a, b);
-  else return fmaxf(a, b);
-}
-template <typename TC>
-__device__ __forceinline__ TC rs_pos(TC a) {
-  if constexpr (sizeof(TC) == sizeof(double)) return dpos_bits(a);
-  else return fmaxf(a, 0.0f);
+// v with its sign bit flipped when m is the sign mask (exact negation by an
+// integer operation)
+__device__ __forceinline__ double neg_if(double v, long long m) {
+  return __longlong_as_double(__double_as_longlong(v) ^ m);
 }
 
 template <typename TC, typename LD>
@@ -163,29 +163,46 @@ __device__ __forceinline__ TC rs_dc(const Geo &g, TC h, const LD &pr, TC p, cons
   // conversion, compare or multiply on GB300's FP64 pipe.
   const int s = (f >> 1) & 3;
   const TC zero = (TC)0;
-  TC dc;
   if (f & 1) {
     const TC ap = fabs(p);
-    dc = ((s == 2) ? ap : ((s == 0) ? -ap : zero)) - D[c];
-  } else if (s == 2) {
+    return ((s == 2) ? ap : ((s == 0) ? -ap : zero)) - D[c];
+  }
+  if constexpr (sizeof(TC) == sizeof(double)) {
+    // One evaluation for both signs (a warp straddling the interface would
+    // otherwise run both, and predicated-off FP64 instructions still hold
+    // the FP64 pipe).  With sigma = sign(phi) and m its sign mask:
+    //   phi > 0: a = max(p - min(l, r), 0)
+    //   phi < 0: a = max(max(l, r) - p, 0) = max((-p) - min(-l, -r), 0),
+    // exactly ((-p) - (-M) = M - p in IEEE arithmetic), and
+    // dc = sigma (sqrt(ax^2 + ay^2 + az^2) - h), the sum taken in the
+    // reference's order: x, y, z for phi > 0 and x, z, y for phi < 0
+    // (levelset.f90:274-275).
     // max(aP^2, bM^2) with aP = max(p - p[i-1], 0), bM = min(p[i+1] - p, 0)
     // equals max(p - min(p[i-1], p[i+1]), 0)^2 bit for bit (rounding of a
     // difference and of a square are monotone), likewise in y and z.
-    const TC ax = rs_pos(p - rs_min(pr[c - 1], pr[c + 1]));
-    const TC ay = rs_pos(p - rs_min(pr[c - g.sy], pr[c + g.sy]));
-    const TC az = rs_pos(p - rs_min(pr[c - g.sz], pr[c + g.sz]));
-    dc = sqrt(ax * ax + ay * ay + az * az) - h;
-  } else if (s == 0) {
-    // max(bP^2, aM^2) = max(max(p[i-1], p[i+1]) - p, 0)^2, likewise y, z
-    const TC ax = rs_pos(rs_max(pr[c - 1], pr[c + 1]) - p);
-    const TC ay = rs_pos(rs_max(pr[c - g.sy], pr[c + g.sy]) - p);
-    const TC az = rs_pos(rs_max(pr[c - g.sz], pr[c + g.sz]) - p);
-    // levelset.f90:274-275 sums x, then z, then y
-    dc = -(sqrt(ax * ax + az * az + ay * ay) - h);
+    if (s == 1) return zero;
+    const long long m = (s == 0) ? (long long)0x8000000000000000ULL : 0LL;
+    const double sp = neg_if(p, m);
+    const double ax = dpos_bits(sp - dmin_bits(neg_if(pr[c - 1], m), neg_if(pr[c + 1], m)));
+    const double ay = dpos_bits(sp - dmin_bits(neg_if(pr[c - g.sy], m), neg_if(pr[c + g.sy], m)));
+    const double az = dpos_bits(sp - dmin_bits(neg_if(pr[c - g.sz], m), neg_if(pr[c + g.sz], m)));
+    const double a2 = (s == 2) ? ay : az, a3 = (s == 2) ? az : ay;
+    return neg_if(sqrt(ax * ax + a2 * a2 + a3 * a3) - h, m);
   } else {
-    dc = zero;
+    if (s == 2) {
+      const TC ax = fmaxf(p - fminf(pr[c - 1], pr[c + 1]), zero);
+      const TC ay = fmaxf(p - fminf(pr[c - g.sy], pr[c + g.sy]), zero);
+      const TC az = fmaxf(p - fminf(pr[c - g.sz], pr[c + g.sz]), zero);
+      return sqrt(ax * ax + ay * ay + az * az) - h;
+    }
+    if (s == 0) {
+      const TC ax = fmaxf(fmaxf(pr[c - 1], pr[c + 1]) - p, zero);
+      const TC ay = fmaxf(fmaxf(pr[c - g.sy], pr[c + g.sy]) - p, zero);
+      const TC az = fmaxf(fmaxf(pr[c - g.sz], pr[c + g.sz]) - p, zero);
+      return -(sqrt(ax * ax + az * az + ay * ay) - h);
+    }
+    return zero;
   }
-  return dc;
 }
 
 template <typename TC, typename TI>
@@ -206,17 +223,27 @@ __device__ __forceinline__ RT rs_update(const Geo &g, TC h, TC ktau, const TI *_
   else return (RT)pr0[c] - (RT)(ktau * dc);
 }
 
+// levelset.f90 inlet value (k - 1/2) h - height at i = 0.  A call, not
+// inline code: if-converted it would put its FP64 instructions on every
+// lane's FP64 pipe, and only one column of the grid takes it.
+__device__ __noinline__ double ls_inlet(double h, double height, int k) {
+  return (k * h - 0.5 * h) - height;
+}
+
 template <typename TC, typename TI, typename RT>
 __device__ __forceinline__ RT rs_val(const Geo &g, const Phys &ph, TC h, TC ktau, const TI *pr, const TC *D,
                                      const signed char *flags, int i, int j, int k) {
-  if (i == 0) return (RT)((k * (double)h - 0.5 * (double)h) - ph.height);
+  if (i == 0) return (RT)ls_inlet((double)h, ph.height, k);
   return rs_update<TC, TI, RT>(g, h, ktau, pr, D, flags, (i == g.nx + 1) ? g.nx : i, j, k);
 }
 
 // TI/TO: storage of the input/output iterate; TC: arithmetic (double for
 // the FP64 form; float for the FP32-mixed form, whose first iteration reads
 // the FP64 phi3 and whose last writes the FP64 state).
-template <typename TC, typename TI, typename TO>
+// ERR: the launch also writes the error partials (the last iteration only;
+// a compile-time switch, so the other iterations carry no predicated-off
+// FP64 instructions for it).
+template <typename TC, typename TI, typename TO, bool ERR>
 __global__ void __launch_bounds__(LS_BX *LS_BY)
     k_ls_iter(Geo g, Phys ph, TC h, TC ktau, const TI *__restrict__ pr, const TC *__restrict__ D,
               const signed char *__restrict__ flags, TO *__restrict__ out, double *__restrict__ err_part) {
@@ -236,13 +263,13 @@ __global__ void __launch_bounds__(LS_BX *LS_BY)
     else
       v = rs_val<TC, TI, RT>(g, ph, h, ktau, pr, D, flags, i, jj, k);
     const int c = TPLS_IDX(g, i, j, k);
-    if (err_part && i >= 1 && i <= g.nx && j >= 1 && j <= g.ny) {
+    if (ERR && i >= 1 && i <= g.nx && j >= 1 && j <= g.ny) {
       const double d = (double)pr[c] - (double)v;
       e = d * d;
     }
     out[c] = (TO)v;
   }
-  if (err_part) {
+  if constexpr (ERR) {
     __shared__ double s[LS_BX * LS_BY / 32];
     for (int o = 16; o > 0; o >>= 1) e += __shfl_down_sync(0xffffffffu, e, o);
     const int t = threadIdx.y * LS_BX + threadIdx.x;
@@ -393,8 +420,12 @@ template <typename TC, typename TI, typename TO>
 static cudaError_t ls_iter(const Geo &g, const Phys &ph, const TI *pr, const TC *D, const signed char *flags,
                            TO *pr_new, double *err_part, cudaStream_t st) {
   const double h = ph.dx, dtau = 0.3 * h;
-  k_ls_iter<TC, TI, TO><<<full_grid(g, g.nz + 2), dim3(LS_BX, LS_BY), 0, st>>>(g, ph, (TC)h, (TC)(dtau / h), pr,
-                                                                              D, flags, pr_new, err_part);
+  if (err_part)
+    k_ls_iter<TC, TI, TO, true><<<full_grid(g, g.nz + 2), dim3(LS_BX, LS_BY), 0, st>>>(
+        g, ph, (TC)h, (TC)(dtau / h), pr, D, flags, pr_new, err_part);
+  else
+    k_ls_iter<TC, TI, TO, false><<<full_grid(g, g.nz + 2), dim3(LS_BX, LS_BY), 0, st>>>(
+        g, ph, (TC)h, (TC)(dtau / h), pr, D, flags, pr_new, err_part);
   return cudaGetLastError();
 }
 cudaError_t launch_ls_iter(const Geo &g, const Phys &ph, const double *pr, const double *D,
@@ -444,7 +475,10 @@ __device__ __forceinline__ F3 csf_point(const Geo &g, const Phys &ph, double max
   } fi{fi0};
   const double p64 = fi0[c];
   F3 r = {0.0, 0.0, 0.0};
-  if (p64 < -ph.sw || p64 > ph.sw) return r;  // band decision in FP64 in both forms
+  // band decision on the FP64 value in both forms, by order keys of the bit
+  // patterns (exact; no FP64 compare)
+  const long long kp = dkey(p64);
+  if (kp < dkey(-ph.sw) || kp > dkey(ph.sw)) return r;
   const T p = (T)p64;
   const int sy = g.sy, sz = g.sz;
   const T rdx = (T)(1.0 / ph.dx), rdy = (T)(1.0 / ph.dy), rdz = (T)(1.0 / ph.dz);
@@ -541,7 +575,7 @@ cudaError_t launch_csf(const Geo &g, const Phys &ph, const double *phi3, float *
 // viscosity exactly mu_minus/re or mu_plus/re (the host's IEEE quotients,
 // mlo and mhi); the band test compares order keys of the bit patterns
 // (klo = key(-sw), khi = key(sw)), so those points use no FP64 instruction.
-template <typename T>
+template <typename T, bool OFF>
 __global__ void k_visc(Geo g, Phys ph, const double *__restrict__ phi, double off, long long klo,
                        long long khi, double mlo, double mhi, T *__restrict__ mu) {
   const int i = blockIdx.x * LS_BX + threadIdx.x, j = blockIdx.y * LS_BY + threadIdx.y - 1;
@@ -549,9 +583,9 @@ __global__ void k_visc(Geo g, Phys ph, const double *__restrict__ phi, double of
   if (i > g.nx + 1 || j > g.ny + 2) return;
   // off: -0.5 for the diffuse-interface method, which passes phi2-0.5
   // (main_ns_hybrid.F90:650, :667, :692); 0 for the level set, where adding
-  // it would change nothing but the sign of a zero
+  // it would change nothing but the sign of a zero (OFF false: no add)
   double p = phi[TPLS_IDX(g, i, wrapy(j, g.ny), k)];
-  if (__double_as_longlong(off) != 0) p += off;
+  if constexpr (OFF) p += off;
   const long long kp = dkey(p);
   double m;
   if (kp < klo) {
@@ -574,9 +608,12 @@ static long long host_dkey(double a) {
 cudaError_t launch_visc(const Geo &g, const Phys &ph, const double *phi2,
                         double *mu, cudaStream_t st, double phi_offset) {
   dim3 grd((g.nx + 2 + LS_BX - 1) / LS_BX, (g.ny + 4 + LS_BY - 1) / LS_BY, g.nz + 2);
-  k_visc<double><<<grd, dim3(LS_BX, LS_BY), 0, st>>>(g, ph, phi2, phi_offset, host_dkey(-ph.sw),
-                                                     host_dkey(ph.sw), ph.mu_minus / ph.re,
-                                                     ph.mu_plus / ph.re, mu);
+  const long long klo = host_dkey(-ph.sw), khi = host_dkey(ph.sw);
+  const double mlo = ph.mu_minus / ph.re, mhi = ph.mu_plus / ph.re;
+  if (phi_offset != 0.0)
+    k_visc<double, true><<<grd, dim3(LS_BX, LS_BY), 0, st>>>(g, ph, phi2, phi_offset, klo, khi, mlo, mhi, mu);
+  else
+    k_visc<double, false><<<grd, dim3(LS_BX, LS_BY), 0, st>>>(g, ph, phi2, phi_offset, klo, khi, mlo, mhi, mu);
   return cudaGetLastError();
 }
 // The FP32 viscosity of the FP32-mixed form: the same formula in FP32 on

@@ -42,7 +42,10 @@ struct CDT {
   T conv, diff;
 };
 
-template <typename T>
+// INTERIOR: the caller knows 0 < k < nz-1, so the wall-level forms of u and
+// v (k = 0, nz-1) are left out at compile time (if-converted, their FP64
+// instructions would occupy GB300's FP64 pipe on every level).
+template <typename T, bool INTERIOR = false>
 __device__ __forceinline__ CDT<T> conv_diff(int comp, const Geo &g, T rdx, T rdy, T rdz,
                                             const T *__restrict__ U, const T *__restrict__ V,
                                             const T *__restrict__ W, const FcT<T> &f, int i, int j,
@@ -50,6 +53,7 @@ __device__ __forceinline__ CDT<T> conv_diff(int comp, const Geo &g, T rdx, T rdy
   const int sy = g.sy, sz = g.sz, nzu = g.nz;  // u/v have planes 0..nz-1
   const int c = TPLS_IDX(g, i, j, k);
   const T h = (T)0.5, two = (T)2, third = (T)(1.0 / 3.0);
+  const bool kb = !INTERIOR && k == 0, kt = !INTERIOR && k == nzu - 1;
   CDT<T> r;
   if (comp == 0) {
     const T x = U[c];
@@ -58,16 +62,17 @@ __device__ __forceinline__ CDT<T> conv_diff(int comp, const Geo &g, T rdx, T rdy
     const T Xc = h * (U[c + 1] - U[c - 1]) * rdx * x;
     const T Yc = h * (U[c + sy] - U[c - sy]) * rdy * tempv;
     T dz_;
-    if (k == 0) dz_ = (x + U[c + sz]) * (h * rdz);
-    else if (k == nzu - 1) dz_ = -(x + U[c - sz]) * (h * rdz);
+    if (kb) dz_ = (x + U[c + sz]) * (h * rdz);
+    else if (kt) dz_ = -(x + U[c - sz]) * (h * rdz);
     else dz_ = h * (U[c + sz] - U[c - sz]) * rdz;
     const T t1 = Xc + Yc + dz_ * tempw;
     const T E = f.px * (U[c + 1] - x) * rdx, Wt = f.mx * (x - U[c - 1]) * rdx;
     const T N = f.py * (V[c + 1 + sy] - V[c + sy]) * rdx, S = f.my * (V[c + 1] - V[c]) * rdx;
     const T O = f.pz * (W[c + 1 + sz] - W[c + sz]) * rdx, I = f.mz * (W[c + 1] - W[c]) * rdx;
     r.conv = t1 - ((E - Wt) * rdx + (N - S) * rdy + (O - I) * rdz);
-    const T umz = (k == 0) ? -two * x + U[c + sz] * third : U[c - sz];
-    const T upz = (k == nzu - 1) ? -two * x + U[c - sz] * third : U[c + sz];
+    // loads only the planes each form uses (no plane -1 at k = 0, no plane nz at k = nz-1)
+    const T umz = kb ? -two * x + U[c + sz] * third : U[c - sz];
+    const T upz = kt ? -two * x + U[c - sz] * third : U[c + sz];
     r.diff = (f.px * (U[c + 1] - x) - f.mx * (x - U[c - 1])) * (rdx * rdx) +
              (f.py * (U[c + sy] - x) - f.my * (x - U[c - sy])) * (rdy * rdy) +
              (f.pz * (upz - x) - f.mz * (x - umz)) * (rdz * rdz);
@@ -78,16 +83,17 @@ __device__ __forceinline__ CDT<T> conv_diff(int comp, const Geo &g, T rdx, T rdy
     const T Yc = h * (V[c + sy] - V[c - sy]) * rdy * x;
     const T Xc = h * (V[c + 1] - V[c - 1]) * rdx * tempu;
     T dz_;
-    if (k == 0) dz_ = (x + V[c + sz]) * (h * rdz);
-    else if (k == nzu - 1) dz_ = -(x + V[c - sz]) * (h * rdz);
+    if (kb) dz_ = (x + V[c + sz]) * (h * rdz);
+    else if (kt) dz_ = -(x + V[c - sz]) * (h * rdz);
     else dz_ = h * (V[c + sz] - V[c - sz]) * rdz;
     const T t1 = Xc + Yc + dz_ * tempw;
     const T E = f.px * (U[c] - U[c - sy]) * rdy, Wt = f.mx * (U[c - 1] - U[c - 1 - sy]) * rdy;
     const T N = f.py * (V[c + sy] - x) * rdy, S = f.my * (x - V[c - sy]) * rdy;
     const T O = f.pz * (W[c + sz] - W[c - sy + sz]) * rdy, I = f.mz * (W[c] - W[c - sy]) * rdy;
     r.conv = t1 - ((E - Wt) * rdx + (N - S) * rdy + (O - I) * rdz);
-    const T vmz = (k == 0) ? -two * x + V[c + sz] * third : V[c - sz];
-    const T vpz = (k == nzu - 1) ? -two * x + V[c - sz] * third : V[c + sz];
+    // loads only the planes each form uses (no plane -1 at k = 0, no plane nz at k = nz-1)
+    const T vmz = kb ? -two * x + V[c + sz] * third : V[c - sz];
+    const T vpz = kt ? -two * x + V[c - sz] * third : V[c + sz];
     r.diff = (f.px * (V[c + 1] - x) - f.mx * (x - V[c - 1])) * (rdx * rdx) +
              (f.py * (V[c + sy] - x) - f.my * (x - V[c - sy])) * (rdy * rdy) +
              (f.pz * (vpz - x) - f.mz * (x - vmz)) * (rdz * rdz);
@@ -137,13 +143,14 @@ __device__ __forceinline__ void store_rec(double *rec, double a0, double a1, dou
 }
 
 // The record of one point of the FP64 sweeps.
+template <bool INTERIOR>
 __device__ __forceinline__ void write_coef(int comp, const Geo &g, const Helm &h, const FcT<double> &f,
                                            double rhs, int k, double *__restrict__ rec) {
   const double ax2 = h.ax2, ay2 = h.ay2, az2 = h.az2;
   const double diag = 1.0 + ax2 * (f.px + f.mx) + ay2 * (f.py + f.my) + az2 * (f.pz + f.mz);
   const double r = 1.0 / diag;
   double czp = az2 * f.pz * r, czm = az2 * f.mz * r;
-  if (comp != 2) {
+  if (!INTERIOR && comp != 2) {
     if (k == 0) {
       czp += czm * (1.0 / 3.0);
       czm = -2.0 * czm;
@@ -158,17 +165,16 @@ __device__ __forceinline__ void write_coef(int comp, const Geo &g, const Helm &h
 // FP64 stencils.  TR = double: the FP64 form's right-hand side and 64-byte
 // sweep records (X64 = the component's FP64 state u2, v2 or w2); TR = float:
 // the FP32-mixed form with FP64 stencils, which stores the defect b alone.
-template <typename T, typename TR>
-__global__ void __launch_bounds__(MB_X *MB_Y)
-    k_mom_rhs(int comp, Geo g, Phys ph, Helm hm, const T *__restrict__ U, const T *__restrict__ V,
-              const T *__restrict__ W, const double *__restrict__ X64, const T *__restrict__ mu,
-              const T *__restrict__ fc, const double *__restrict__ c1, const double *__restrict__ c0,
-              const double *__restrict__ s1, const double *__restrict__ s0, double *__restrict__ conv2,
-              double *__restrict__ csf2, double *__restrict__ rhs, double *__restrict__ diff_out,
-              TR *__restrict__ coef) {
-  const int i = blockIdx.x * MB_X + threadIdx.x + 1, j = blockIdx.y * MB_Y + threadIdx.y + 1;
-  const int k = blockIdx.z;
-  if (i > g.nx || j > g.ny) return;
+template <typename T, typename TR, bool INTERIOR>
+__device__ __forceinline__ void mom_rhs_point(int comp, const Geo &g, const Phys &ph, const Helm &hm,
+                                              const T *__restrict__ U, const T *__restrict__ V,
+                                              const T *__restrict__ W, const double *__restrict__ X64,
+                                              const T *__restrict__ mu, const T *__restrict__ fc,
+                                              const double *__restrict__ c1, const double *__restrict__ c0,
+                                              const double *__restrict__ s1, const double *__restrict__ s0,
+                                              double *__restrict__ conv2, double *__restrict__ csf2,
+                                              double *__restrict__ rhs, double *__restrict__ diff_out,
+                                              TR *__restrict__ coef, int i, int j, int k) {
   const int c = TPLS_IDX(g, i, j, k);
   CDT<T> cd = {(T)0, (T)0};
   const bool valid = cd_valid(comp, g, i, k);
@@ -177,7 +183,7 @@ __global__ void __launch_bounds__(MB_X *MB_Y)
     f = faces(comp, g, mu, i, j, k);
     // 1/dx, 1/dy, 1/dz from the host (the same IEEE quotients, not three FP64
     // divisions per point on GB300's FP64 pipe)
-    cd = conv_diff<T>(comp, g, (T)hm.rdx, (T)hm.rdy, (T)hm.rdz, U, V, W, f, i, j, k);
+    cd = conv_diff<T, INTERIOR>(comp, g, (T)hm.rdx, (T)hm.rdy, (T)hm.rdz, U, V, W, f, i, j, k);
   }
   // main_ns_hybrid.F90:629-641 face averages of the CSF force
   double s2;
@@ -208,8 +214,30 @@ __global__ void __launch_bounds__(MB_X *MB_Y)
     csf2[c] = s2;
     if (rhs) rhs[c] = r;
     if (diff_out) diff_out[c] = diff;
-    if (coef && valid) write_coef(comp, g, hm, f, r, k, coef + 8 * (size_t)rec_slot(g, c, i));
+    if (coef && valid) write_coef<INTERIOR>(comp, g, hm, f, r, k, coef + 8 * (size_t)rec_slot(g, c, i));
   }
+}
+
+// CC: the velocity component at compile time.  The wall levels of u and v
+// (k = 0, nz-1) take their own copy of the point code by a block-uniform
+// branch, so the interior levels carry none of the wall forms.
+template <typename T, typename TR, int CC>
+__global__ void __launch_bounds__(MB_X *MB_Y)
+    k_mom_rhs(Geo g, Phys ph, Helm hm, const T *__restrict__ U, const T *__restrict__ V,
+              const T *__restrict__ W, const double *__restrict__ X64, const T *__restrict__ mu,
+              const T *__restrict__ fc, const double *__restrict__ c1, const double *__restrict__ c0,
+              const double *__restrict__ s1, const double *__restrict__ s0, double *__restrict__ conv2,
+              double *__restrict__ csf2, double *__restrict__ rhs, double *__restrict__ diff_out,
+              TR *__restrict__ coef) {
+  const int i = blockIdx.x * MB_X + threadIdx.x + 1, j = blockIdx.y * MB_Y + threadIdx.y + 1;
+  const int k = blockIdx.z;
+  if (i > g.nx || j > g.ny) return;
+  if (CC != 2 && (k == 0 || k == g.nz - 1))
+    mom_rhs_point<T, TR, false>(CC, g, ph, hm, U, V, W, X64, mu, fc, c1, c0, s1, s0, conv2, csf2, rhs, diff_out,
+                                coef, i, j, k);
+  else
+    mom_rhs_point<T, TR, true>(CC, g, ph, hm, U, V, W, X64, mu, fc, c1, c0, s1, s0, conv2, csf2, rhs, diff_out,
+                               coef, i, j, k);
 }
 
 template <typename T, typename TR = T>
@@ -219,8 +247,16 @@ static cudaError_t mom_rhs(int comp, const Geo &g, const Phys &ph, const T *u2, 
                            double *diff_out, TR *coef, cudaStream_t st) {
   const int nk = (comp == 2) ? g.nz + 1 : g.nz;
   dim3 grd((g.nx + MB_X - 1) / MB_X, (g.ny + MB_Y - 1) / MB_Y, nk);
-  k_mom_rhs<T, TR><<<grd, dim3(MB_X, MB_Y), 0, st>>>(comp, g, ph, helm_of(ph), u2, v2, w2, x64, mu, fcsf, c1,
-                                                     c0, s1, s0, conv2, csf2, rhs, diff_out, coef);
+  const Helm hm = helm_of(ph);
+  if (comp == 0)
+    k_mom_rhs<T, TR, 0><<<grd, dim3(MB_X, MB_Y), 0, st>>>(g, ph, hm, u2, v2, w2, x64, mu, fcsf, c1, c0, s1, s0,
+                                                          conv2, csf2, rhs, diff_out, coef);
+  else if (comp == 1)
+    k_mom_rhs<T, TR, 1><<<grd, dim3(MB_X, MB_Y), 0, st>>>(g, ph, hm, u2, v2, w2, x64, mu, fcsf, c1, c0, s1, s0,
+                                                          conv2, csf2, rhs, diff_out, coef);
+  else
+    k_mom_rhs<T, TR, 2><<<grd, dim3(MB_X, MB_Y), 0, st>>>(g, ph, hm, u2, v2, w2, x64, mu, fcsf, c1, c0, s1, s0,
+                                                          conv2, csf2, rhs, diff_out, coef);
   return cudaGetLastError();
 }
 
