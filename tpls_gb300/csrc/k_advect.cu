@@ -43,8 +43,8 @@ __device__ __forceinline__ T weno5(T v1, T v2, T v3, T v4, T v5) {
 // takes no FP64 compare; a NaN velocity (a diverged state) may pick either
 // stencil.
 __device__ __forceinline__ bool upwind_pos(double v) {
-  const long long b = __double_as_longlong(v);
-  return b >= 0 || b == (long long)0x8000000000000000ULL;
+  const int hi = __double2hiint(v);
+  return hi >= 0 || (hi == (int)0x80000000 && __double2loint(v) == 0);
 }
 __device__ __forceinline__ bool upwind_pos(float v) { return v >= 0.0f; }
 

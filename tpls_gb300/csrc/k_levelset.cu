@@ -70,9 +70,9 @@ cudaError_t launch_ls_ab3(const Geo &g, const Phys &ph, const double *phi2,
 // zero (both magnitudes >= 2^-511, biased exponent >= 512).  Returns 1 for
 // <= 0, 0 for > 0 and 2 when an operand is too small to decide by bits.
 __device__ __forceinline__ int prod_le0_bits(double p, double q) {
-  const long long a = __double_as_longlong(p), b = __double_as_longlong(q);
-  if ((a << 1) == 0 || (b << 1) == 0) return 1;
-  if (((a >> 52) & 0x7ff) >= 512 && ((b >> 52) & 0x7ff) >= 512) return ((a ^ b) < 0) ? 1 : 0;
+  const int ha = __double2hiint(p), hb = __double2hiint(q);
+  if (((ha & 0x7fffffff) | __double2loint(p)) == 0 || ((hb & 0x7fffffff) | __double2loint(q)) == 0) return 1;
+  if (((ha >> 20) & 0x7ff) >= 512 && ((hb >> 20) & 0x7ff) >= 512) return ((ha ^ hb) < 0) ? 1 : 0;
   return 2;
 }
 
@@ -117,8 +117,8 @@ __global__ void k_ls_status(Geo g, double h, const double *__restrict__ phi, T *
   const double p = phi[c];
   const double pxp = phi[c + 1], pxm = phi[c - 1], pyp = phi[c + g.sy], pym = phi[c - g.sy];
   const double pzp = phi[c + g.sz], pzm = phi[c - g.sz];
-  const long long pb = __double_as_longlong(p);
-  const int sgn = ((pb << 1) == 0) ? 0 : ((pb < 0) ? -1 : 1);
+  const int ph = __double2hiint(p);
+  const int sgn = (((ph & 0x7fffffff) | __double2loint(p)) == 0) ? 0 : ((ph < 0) ? -1 : 1);
   const int q = prod_le0_bits(p, pxp) | prod_le0_bits(p, pxm) | prod_le0_bits(p, pyp) |
                 prod_le0_bits(p, pym) | prod_le0_bits(p, pzp) | prod_le0_bits(p, pzm);
   const int st = (q & 2) ? status_products(p, pxp, pxm, pyp, pym, pzp, pzm) : (q & 1);
@@ -151,8 +151,8 @@ cudaError_t launch_ls_status(const Geo &g, const Phys &ph, const double *phi3, f
 // values in the arithmetic type TC.
 // v with its sign bit flipped when m is the sign mask (exact negation by an
 // integer operation)
-__device__ __forceinline__ double neg_if(double v, long long m) {
-  return __longlong_as_double(__double_as_longlong(v) ^ m);
+__device__ __forceinline__ double neg_if(double v, int m) {
+  return __hiloint2double(__double2hiint(v) ^ m, __double2loint(v));
 }
 
 template <typename TC, typename LD>
@@ -181,7 +181,7 @@ __device__ __forceinline__ TC rs_dc(const Geo &g, TC h, const LD &pr, TC p, cons
     // equals max(p - min(p[i-1], p[i+1]), 0)^2 bit for bit (rounding of a
     // difference and of a square are monotone), likewise in y and z.
     if (s == 1) return zero;
-    const long long m = (s == 0) ? (long long)0x8000000000000000ULL : 0LL;
+    const int m = (s == 0) ? (int)0x80000000 : 0;
     const double sp = neg_if(p, m);
     const double ax = dpos_bits(sp - dmin_bits(neg_if(pr[c - 1], m), neg_if(pr[c + 1], m)));
     const double ay = dpos_bits(sp - dmin_bits(neg_if(pr[c - g.sy], m), neg_if(pr[c + g.sy], m)));

@@ -69,14 +69,15 @@ __device__ __forceinline__ F2 pmax(F2 a, F2 b) { return (b.h > a.h || (b.h == a.
 // dkey(a) < dkey(b), with -0 just below +0.  That differs from fmin/fmax
 // only in which zero a (+0, -0) tie returns; every use here squares the
 // result or subtracts it from a value and squares that, where the sign of
-// a zero does not survive.
+// a zero does not survive.  The key and the sign tests work on the two
+// 32-bit words of the double (no 64-bit integer shift).
 __device__ __forceinline__ long long dkey(double a) {
-  const long long b = __double_as_longlong(a);
-  return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+  const int hi = __double2hiint(a), s = hi >> 31;
+  return __double_as_longlong(__hiloint2double(hi ^ (s & 0x7fffffff), __double2loint(a) ^ s));
 }
 __device__ __forceinline__ double dmin_bits(double a, double b) { return (dkey(b) < dkey(a)) ? b : a; }
 __device__ __forceinline__ double dmax_bits(double a, double b) { return (dkey(a) < dkey(b)) ? b : a; }
 // max(a, 0) for a not NaN: +0 for a <= 0 (the sign bit decides)
-__device__ __forceinline__ double dpos_bits(double a) { return (__double_as_longlong(a) < 0) ? 0.0 : a; }
+__device__ __forceinline__ double dpos_bits(double a) { return (__double2hiint(a) < 0) ? 0.0 : a; }
 
 }  // namespace tpls
