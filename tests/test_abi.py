@@ -118,3 +118,11 @@ def test_ctypes_structs_match_header_layout(tmp_path, cls_name, c_name):
     assert int(got["size"]) == C.sizeof(cls)
     for f, _ in cls._fields_:
         assert int(got[f]) == getattr(cls, f).offset, f
+
+
+def test_integration_guide_names_every_entry_point():
+    """INTEGRATION.md, the guide a maintainer binds the library from, names
+    every function include/tpls_gpu.h declares."""
+    guide = (ROOT / "INTEGRATION.md").read_text()
+    missing = [n for n in declared_functions() if n not in guide]
+    assert not missing, missing
