@@ -32,7 +32,7 @@ extern "C" {
 #define TPLS_ERR_ARG 1         /* bad argument / bounds mismatch */
 #define TPLS_ERR_ALLOC 2       /* device allocation failed */
 #define TPLS_ERR_STATE 3       /* call sequence error */
-#define TPLS_ERR_NOT_BUILT 4   /* feature not available in this build */
+#define TPLS_ERR_NOT_BUILT 4   /* feature not compiled into the library */
 #define TPLS_ERR_CUDA_BASE 1000 /* + cudaError_t */
 #define TPLS_KSP_CONVERGED_RTOL 2
 #define TPLS_KSP_CONVERGED_ATOL 3
