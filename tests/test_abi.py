@@ -126,3 +126,16 @@ def test_integration_guide_names_every_entry_point():
     guide = (ROOT / "INTEGRATION.md").read_text()
     missing = [n for n in declared_functions() if n not in guide]
     assert not missing, missing
+
+
+def test_missing_native_library_fails_loudly(tmp_path, monkeypatch):
+    """No CPU fallback: without the built library the loader and the context
+    constructor raise instead of computing anything."""
+    import tpls_gb300.api as api
+    with pytest.raises(api.TplsError, match="not found"):
+        api.load_library(tmp_path / "missing.so")
+    monkeypatch.setattr(api, "LIB_PATH", tmp_path / "missing.so")
+    monkeypatch.setattr(api, "_lib", None)
+    params, uin, _ = make_case("A", nx=8, ny=4, nz=6)
+    with pytest.raises(api.TplsError, match="not found"):
+        api.TplsGpu(8, 4, 6, params, uin)
