@@ -134,8 +134,8 @@ def test_missing_native_library_fails_loudly(tmp_path, monkeypatch):
     import tpls_gb300.api as api
     with pytest.raises(api.TplsError, match="not found"):
         api.load_library(tmp_path / "missing.so")
+    params, uin, _ = make_case("A", nx=8, ny=4, nz=6)   # uses the library: before removing it
     monkeypatch.setattr(api, "LIB_PATH", tmp_path / "missing.so")
     monkeypatch.setattr(api, "_lib", None)
-    params, uin, _ = make_case("A", nx=8, ny=4, nz=6)
     with pytest.raises(api.TplsError, match="not found"):
         api.TplsGpu(8, 4, 6, params, uin)
