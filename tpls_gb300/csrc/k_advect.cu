@@ -2,11 +2,12 @@
 // conservative flux divergence (advect_phi.f90:19-119, weno.f90:18-215).
 //
 // One thread per (i,j) column of p-cells, marching a chunk of 16 z levels
-// (one z-face below the chunk is computed at its start).  Each face
-// value is computed once: the x-face below a thread comes from its lower
-// lane by warp shuffle (lane 0 computes it), the y-face below from the row
-// below through shared memory (row 0 of the block computes it), and the
-// z-face below is the previous level's z-face held in a register.
+// (one z-face below the chunk is computed at its start).  Each face value
+// is computed once: the x-face left of a thread is its left neighbour's
+// right face and the y-face below is the lower row's upper face, both
+// through a shared tile (the block's left and bottom edge faces computed by
+// one warp each), and the z-face below is the previous level's z-face held
+// in a register.
 // The periodic-y halo of the reference's 3-ghost phi_augaug copy becomes a
 // wrapped row index; no augmented array is built.
 #include "tpls_kernels.h"

@@ -138,6 +138,12 @@ cudaError_t launch_ls_status(const Geo &g, const Phys &ph, const double *phi3, f
   return cudaGetLastError();
 }
 
+// v with its sign bit flipped when m is the sign mask (exact negation by an
+// integer operation on the high word)
+__device__ __forceinline__ double neg_if(double v, int m) {
+  return __hiloint2double(__double2hiint(v) ^ m, __double2loint(v));
+}
+
 // ---------------------------------------------------------------------------
 // levelset.f90:97-237 do_levelset_iteration: one Godunov pseudo-time step
 // with dtau = 0.3h (h = dx), then the inlet value (with dz = h), the outlet
@@ -149,12 +155,6 @@ cudaError_t launch_ls_status(const Geo &g, const Phys &ph, const double *phi3, f
 // iterate accumulates no FP32 rounding across the iterations and steps.
 // dc of the update at point c, p = its value, pr a loader of the stencil
 // values in the arithmetic type TC.
-// v with its sign bit flipped when m is the sign mask (exact negation by an
-// integer operation)
-__device__ __forceinline__ double neg_if(double v, int m) {
-  return __hiloint2double(__double2hiint(v) ^ m, __double2loint(v));
-}
-
 template <typename TC, typename LD>
 __device__ __forceinline__ TC rs_dc(const Geo &g, TC h, const LD &pr, TC p, const TC *__restrict__ D, int f,
                                    int c) {
