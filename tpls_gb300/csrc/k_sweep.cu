@@ -19,12 +19,6 @@
 
 namespace tpls {
 
-// Tile shapes of the Jacobi and even-SOR kernels (block x threads over i or
-// i pairs, block y threads over j) the autotuner chooses from; variant 0 is
-// the default.
-constexpr int SW_NV = 4;
-constexpr int SW_SHAPES[SW_NV][2] = {{32, 4}, {32, 8}, {64, 4}, {16, 8}};
-
 template <typename T>
 struct Rec {
   T xp, xm, yp, ym, zp, zm, b;
@@ -343,6 +337,9 @@ static void jacobi_v(int comp, const Geo &g, const Helm &h, const T *xo, CS coef
   k_jacobi_c<T, CS, CC, BX, BY><<<grd, dim3(BX, BY), 0, st>>>(comp, g, h, xo, coef, pres, X, x, fuse);
 }
 
+// tile: the block shape (threads over i, or i pairs, by threads over j) the
+// autotuner chooses among for the Jacobi and even-SOR kernels: 0 = 32x4 (the
+// default), 1 = 32x8, 2 = 64x4, 3 = 16x8.
 template <typename T, typename CS, int CC>
 static cudaError_t jacobi_c(int comp, const Geo &g, const Phys &ph, const T *xo, CS coef, const double *pres,
                             const double *X, T *x, int fuse, int tile, cudaStream_t st) {
