@@ -89,3 +89,32 @@ def test_checkpoint_restart_is_bit_identical(tmp_path):
         assert np.array_equal(sa[k], sc[k]), k
     a.close()
     c.close()
+
+
+def test_checkpoint_file_holds_the_whole_state(tmp_path):
+    """A checkpoint written from a channel mid-run holds everything a restart
+    needs: restoring the file into a fresh channel and stepping on gives the
+    uninterrupted run bit for bit (checked on the CPU oracle, which has the
+    same field interface as the GPU context)."""
+    import json
+
+    from oracle.oracle import Oracle
+    from tpls_gb300.api import Params
+    from tpls_gb300.channel import make_case
+    from tpls_gb300.checkpoint import save_checkpoint
+    params, uin, st = make_case("A", nx=12, ny=6, nz=8)
+    a = Oracle(12, 6, 8, params, uin)
+    a.set_state(st)
+    a.step(2)
+    f = tmp_path / "ck.npz"
+    save_checkpoint(a, f)
+    z = np.load(f, allow_pickle=False)
+    assert list(z["grid"]) == [12, 6, 8] and np.array_equal(z["u_inlet"], uin)
+    meta = json.loads(str(z["params"]))
+    assert Params(**meta) == params
+    b = Oracle(12, 6, 8, Params(**meta), z["u_inlet"])
+    b.set_state({k[2:]: np.asfortranarray(z[k]) for k in z.files if k.startswith("f_")})
+    a.step(2)
+    b.step(2)
+    for k, v in a.get_state().items():
+        assert np.array_equal(v, b.get_field(k)), k
