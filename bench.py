@@ -3,9 +3,9 @@
 
 Default workload: the FP64 form on the 256x128x192 channel (m=2, Re=200,
 4-mode seeded interface, mom_u/v/w = 30, levelset = 10, PETSc's default
-pressure rtol 1e-5), K timed steps after W warm-up steps.  The FP64 form's
-CG preconditioner runs its multigrid levels in FP32 (tpls_params.mg_fp32;
---mg-fp64 for FP64 levels): CG, its residuals and the solution stay FP64.
+pressure rtol 1e-5), K timed steps after W warm-up steps, FP64 throughout
+(--mg-fp32: FP32 multigrid levels in the CG preconditioner, with CG, its
+residuals and the solution still FP64).
 
 Arms
   (default) the CUDA library through its C ABI, device-resident state;
@@ -139,16 +139,23 @@ def _algorithmic_bytes(nx, ny, nz, mom, esz=8):
     return jac, sor_odd, 3 * outer, 6 * n_odd
 
 
-def _profile_figure(tag: str, kernel: str, workload: str):
+def _profile_figure(tag: str, kernel: str, workload: str) -> dict | None:
     """A figure from the committed ncu summaries: lines
-    '<tag> <kernel> <workload>: <number> ...' (tag 'traffic' = DRAM bytes per
-    launch, 'fp64pipe' = FP64 pipe active % of peak)."""
+    '<tag> <kernel> <workload>: <number> build <digest>' (tag 'traffic' =
+    DRAM bytes per launch, 'fp64pipe' = FP64 pipe active % of peak; digest =
+    tpls_gb300.build.source_digest() of the build the capture was taken of).
+    Returns {"value", "file", "build", "current"}: `current` says whether the
+    capture is of the sources this run was built from.  ncu figures are not
+    measured by this run; a figure whose build differs is reported only
+    under its capture record."""
     import re
+    from tpls_gb300.build import source_digest
     for f in sorted((ROOT / "profiles").glob("*.md")):
         for line in f.read_text().splitlines():
-            m = re.match(r"(\S+) (\S+) (\S+): ([0-9.]+)", line.strip())
+            m = re.match(r"(\S+) (\S+) (\S+): ([0-9.]+) build ([0-9a-f]+)", line.strip())
             if m and m.group(1) == tag and m.group(2) == kernel and m.group(3) == workload:
-                return float(m.group(4))
+                return {"value": float(m.group(4)), "file": f"profiles/{f.name}", "build": m.group(5),
+                        "current": m.group(5) == source_digest()}
     return None
 
 
@@ -167,7 +174,7 @@ def run_gpu(args, ws, rank, local) -> dict | None:
     parts = args.fp64_parts if precision == 1 else 0
     nx, ny, nz = args.grid if args.grid else (w.nx, w.ny, w.nz)
     params, uin, st = make_case(args.config, nx=nx, ny=ny, nz=nz, p_rtol=args.p_rtol, precision=precision,
-                                fp64_parts=parts, mg_fp32=0 if (precision != 0 or args.mg_fp64) else 1,
+                                fp64_parts=parts, mg_fp32=1 if (precision == 0 and args.mg_fp32) else 0,
                                 idm=args.idm, pe=args.dim_pe)
     cells = nx * ny * nz
     g = TplsGpu(nx, ny, nz, params, uin)
@@ -259,8 +266,9 @@ def run_gpu(args, ws, rank, local) -> dict | None:
     avg_ms = sor_ms / max(sor_l, 1)
     achieved = per_launch_b / (avg_ms / 1e3) / 1e9
     wl = f"{nx}x{ny}x{nz}-{'fp64' if precision == 0 else 'mixed'}"
-    traffic = _profile_figure("traffic", dominant, wl)
-    fp64_pct = _profile_figure("fp64pipe", dominant, wl)
+    traffic_cap = _profile_figure("traffic", dominant, wl)
+    fp64_cap = _profile_figure("fp64pipe", dominant, wl)
+    traffic = traffic_cap["value"] if traffic_cap and traffic_cap["current"] else None
     cpu = None
     if ws == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(args.config, args.cpu_seconds, (nx, ny, nz))
@@ -298,13 +306,13 @@ def run_gpu(args, ws, rank, local) -> dict | None:
         "roofline": {"bound": "hbm", "kernel": dominant, "bytes_per_launch": per_launch_b,
                      "avg_launch_ms": avg_ms,
                      "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": traffic, "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback",
+                     "traffic": traffic, "traffic_capture": traffic_cap,
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback",
                      "note": "achieved = algorithmic bytes (28 B per component point per half-sweep in FP64, "
-                             "12 B in the FP32 sweeps) / event time; traffic = ncu DRAM bytes per launch "
-                             "(profiles/); the FP64 form's kernels are bound by GB300's FP64 pipe "
-                             "(1.01 TFLOP/s), see fp64_pipe"},
-        "fp64_pipe": {"kernel": dominant, "ncu_active_pct_of_peak": fp64_pct,
-                      "source": "ncu sm__pipe_fp64_cycles_active of the same kernel (profiles/)"},
+                             "12 B in the FP32 sweeps) / CUDA-event time measured in this run; traffic = ncu "
+                             "DRAM bytes per launch from the committed capture named in traffic_capture, "
+                             "given only when that capture is of this run's sources (null otherwise)"},
+        "fp64_pipe_capture": fp64_cap,
         "phases_ms_per_step": {k: v[0] / nph for k, v in phases.items()},
         "phases_note": f"eager pass of {nph} steps with events between phases",
         "pressure": {"its_last": stats["p_its"], "reason_last": stats["p_reason"]},
@@ -582,12 +590,14 @@ def cpu_baseline(config: str, seconds: float, grid=None) -> dict:
 def run_reference(args, ws, rank) -> dict | None:
     if rank != 0:
         return None
-    from oracle.oracle import Oracle, set_threads
+    from oracle.oracle import Oracle, base_profile, set_threads
     from tpls_gb300.channel import WORKLOADS, make_case
     cores = os.cpu_count() or 1
     set_threads(cores)
     w = WORKLOADS[args.config if args.config in WORKLOADS else "B"]
-    params, uin, st = make_case(w, p_rtol=args.p_rtol)
+    # the CPU arm builds its initial state with the oracle's base profile, so
+    # it never maps the CUDA library
+    params, uin, st = make_case(w, p_rtol=args.p_rtol, profile=base_profile)
     o = Oracle(w.nx, w.ny, w.nz, params, uin)
     o.set_state(st)
     o.step(min(args.warmup, 1))
@@ -644,9 +654,9 @@ def main():
     ap.add_argument("--idm", choices=["lsm", "dim"], default="lsm",
                     help="interface method: level set (default) or diffuse interface (FP64 form)")
     ap.add_argument("--dim-pe", type=float, default=1000.0, help="diffuse interface: Peclet number Pe")
-    ap.add_argument("--mg-fp64", action="store_true",
-                    help="FP64 form: FP64 multigrid levels in the CG preconditioner (default: FP32 levels, "
-                         "tpls_params.mg_fp32 = 1; CG stays FP64 and meets p_rtol on its FP64 residual)")
+    ap.add_argument("--mg-fp32", action="store_true",
+                    help="FP64 form: FP32 multigrid levels in the CG preconditioner (tpls_params.mg_fp32 = 1; "
+                         "CG stays FP64 and meets p_rtol on its FP64 residual). Default: FP64 throughout")
     ap.add_argument("--accuracy", type=int, default=0, metavar="STEPS",
                     help="instead of timing: step the FP64 and FP32-mixed forms side by side for STEPS "
                          "steps and print their differences (one JSON line)")

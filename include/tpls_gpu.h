@@ -392,8 +392,10 @@ int tpls_pressure_solve(tpls_ctx *ctx, double *pres, const double *pres_old,
  * partial per row), so ny*nzp may not exceed TPLS_NOALLOC_MAX_ROWS (larger
  * calls return TPLS_ERR_NOALLOC_LIMIT and launch nothing).  The first call
  * on a device looks up that array's device address (make it before any
- * stream capture).  All calls share the array: calls that overlap on the GPU
- * race and must be serialised by the caller. */
+ * stream capture) and keeps it for the life of the process: a
+ * cudaDeviceReset of that device destroys the array, and the entry must not
+ * be called on that device afterwards.  All calls share the array: calls
+ * that overlap on the GPU race and must be serialised by the caller. */
 #define TPLS_NOALLOC_MAX_ROWS 65536
 #define TPLS_ERR_NOALLOC_LIMIT 5
 int tpls_get_difference_noalloc(const double *ua, const double *ub, int nx,

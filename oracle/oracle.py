@@ -65,6 +65,17 @@ def weno5(v1, v2, v3, v4, v5) -> float:
     return load().orc_weno5(v1, v2, v3, v4, v5)
 
 
+def base_profile(nz, dz, re, dpdl, mu_minus, mu_plus, height, smooth_width) -> np.ndarray:
+    """twophase_initialisation_wave.F90:79-122 base velocity u(z) (nz values);
+    same arguments as tpls_gb300.api.base_profile."""
+    lib = load()
+    out = np.zeros(int(nz))
+    lib.orc_base_profile(int(nz), C.c_double(dz), C.c_double(re), C.c_double(dpdl), C.c_double(mu_minus),
+                         C.c_double(mu_plus), C.c_double(height), C.c_double(smooth_width),
+                         out.ctypes.data_as(_DP))
+    return out
+
+
 class Oracle:
     """CPU restatement of one channel (single MPI rank semantics)."""
 

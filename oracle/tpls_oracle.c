@@ -1524,3 +1524,48 @@ void orc_step(orc_ctx *c, int nsteps) {
     c->st.liquid_volume = liquid_volume(c);
   }
 }
+
+/* ------------------------------------------------------------------------
+ * Base state of the two-layer channel: twophase_initialisation_wave.F90:79-122.
+ * visc_oned(k), k = 0..n (n = nz+1), from the smoothed Heaviside of
+ * phi = z - height with pi the single-precision literal 3.14159265359
+ * (:54); then num_iterations = 10000 in-place Gauss-Seidel sweeps of
+ * (d/dz)(mu du/dz) = dpdl over u2_oned(0..n-2) with the wall ghost rule
+ * -2 u(0) + u(1)/3 at both ends (:101-120).  Output u_oned(0..nz-1).
+ * ---------------------------------------------------------------------- */
+void orc_base_profile(int nz, double dz, double reynolds, double dpdl,
+                      double mu_minus, double mu_plus, double height,
+                      double smooth_width, double *u_oned) {
+  const double pi = (double)3.14159265359f;
+  const int n = nz + 1;
+  double *visc_oned = (double *)malloc(sizeof(double) * (size_t)(n + 1));
+  double *u2 = (double *)calloc((size_t)(n - 1), sizeof(double));
+  for (int k = 0; k <= n; k++) {
+    double z_val = dz * k - (dz / 2.0);
+    double phi_val = z_val - height;
+    double heaviside_phi;
+    if (phi_val < -smooth_width)
+      heaviside_phi = 0.0;
+    else if (phi_val > smooth_width)
+      heaviside_phi = 1.0;
+    else
+      heaviside_phi = 0.5 + (phi_val / (2.0 * smooth_width)) +
+                      (1.0 / (2.0 * pi)) * sin(pi * phi_val / smooth_width);
+    double temp = mu_plus * heaviside_phi + mu_minus * (1.0 - heaviside_phi);
+    visc_oned[k] = temp / reynolds;
+  }
+  const double rhs = dpdl;
+  for (int it = 1; it <= 10000; it++) {
+    for (int k = 0; k <= n - 2; k++) {
+      double u_minusz = (k == 0) ? -2.0 * u2[0] + u2[1] / 3.0 : u2[k - 1];
+      double u_plusz = (k == n - 2) ? -2.0 * u2[n - 2] + u2[n - 3] / 3.0 : u2[k + 1];
+      double mu_minusk = (visc_oned[k] + visc_oned[k + 1]) / 2.0;
+      double mu_plusk = (visc_oned[k + 2] + visc_oned[k + 1]) / 2.0;
+      double diag_val = (mu_plusk + mu_minusk) / (dz * dz);
+      u2[k] = (1.0 / diag_val) * (((mu_plusk * u_plusz + mu_minusk * u_minusz) / (dz * dz)) - rhs);
+    }
+  }
+  for (int k = 0; k < nz; k++) u_oned[k] = u2[k];
+  free(visc_oned);
+  free(u2);
+}

@@ -95,6 +95,10 @@ void orc_pressure_solve(int nx, int ny, int nz, double *pres,
                         const double *u_inlet, double dx, double dy,
                         double dz, double dt, double *rnorm);
 void orc_exchange2d(int nx, int ny, int zlo, int zhi, double *a);
+/* twophase_initialisation_wave.F90:79-122: base velocity u(z), nz values. */
+void orc_base_profile(int nz, double dz, double reynolds, double dpdl,
+                      double mu_minus, double mu_plus, double height,
+                      double smooth_width, double *u_oned);
 
 /* ---- whole-step driver (main_ns_hybrid.F90:583-918, 2480-2509) ---- */
 orc_ctx *orc_create(int nx, int ny, int nz, const tpls_params *prm,

@@ -2,11 +2,19 @@
 seeded inputs (tolerance: 1e-11 relative max-norm for the FP64 form).
 
 Sizes: the 64x32x48 workload, a small even grid and an odd grid
-(37x19x23: odd ny exercises the unfused ghost-row path of the sweeps)."""
+(37x19x23: odd ny exercises the unfused ghost-row path of the sweeps), on
+cubic cells; and the 2*pi x pi x 1 channel the configurations name
+(dx = 2 pi/nx, dy = pi/ny, dz = 1/nz) at 64x32x48 (dx = dy = 4.7 dz),
+37x19x23 (dx, dy and dz all differ) and 48x32x40 (dx = 1.33 dy = 5.2 dz), so
+that a swapped spacing anywhere in the stencils or the pressure operator
+(compute_matrix puts 1/dy^2 on the physical-x neighbours,
+pressure_solver.F90:394-421) shows."""
+import os
+
 import numpy as np
 import pytest
 
-from oracle.oracle import Oracle
+from oracle.oracle import Oracle, set_threads
 from tpls_gb300.api import TplsGpu
 from tpls_gb300.channel import make_case
 
@@ -15,12 +23,17 @@ from _util import relmax
 pytestmark = pytest.mark.gpu
 
 TOL = 1e-11
-SIZES = {"A": (64, 32, 48), "even": (32, 16, 24), "odd": (37, 19, 23)}
+SIZES = {"A": (64, 32, 48), "even": (32, 16, 24), "odd": (37, 19, 23),
+         "A-box": (64, 32, 48), "odd-box": (37, 19, 23), "aniso-box": (48, 32, 40)}
+
+
+def _geometry(size):
+    return "box" if size.endswith("-box") else "cubic"
 
 
 def _case(size, steps=1, **kw):
     nx, ny, nz = SIZES[size]
-    params, uin, st = make_case("A", nx=nx, ny=ny, nz=nz, **kw)
+    params, uin, st = make_case("A", nx=nx, ny=ny, nz=nz, geometry=_geometry(size), **kw)
     o = Oracle(nx, ny, nz, params, uin)
     o.set_state(st)
     if steps:
@@ -176,19 +189,9 @@ def test_pressure_solve_reference_rtol(setup):
     assert np.max(np.abs(d)) <= 1e-5 * np.max(np.abs(po - po[1:-1, 1:-1, 1:-1].mean()))
 
 
-@pytest.mark.parametrize("size", list(SIZES))
-def test_full_steps_match_oracle(size):
-    """Whole timesteps on device-resident state, per step: before every step
-    the GPU context is loaded with the oracle's state, both take one step,
-    and phi, u, v, w must match to 1e-11 (pressure solved to 1e-14 so the
-    solve's own tolerance is not what is measured)."""
-    nx, ny, nz = SIZES[size]
-    params, uin, st = make_case("A", nx=nx, ny=ny, nz=nz, p_rtol=1e-14, p_maxits=400)
-    o = Oracle(nx, ny, nz, params, uin)
-    o.set_state(st)
-    g = TplsGpu(nx, ny, nz, params, uin)
+def _steps_match(o, g, nx, ny, nz, nsteps):
     rows = (slice(None), slice(1, ny + 1), slice(None))
-    for step in range(4):
+    for step in range(nsteps):
         g.set_state(o.get_state())
         o.step(1)
         g.step(1)
@@ -200,7 +203,45 @@ def test_full_steps_match_oracle(size):
         so, sg = o.stats(), g.stats()
         assert abs(sg["liquid_volume"] - so["liquid_volume"]) <= 1e-12 * abs(so["liquid_volume"])
         assert sg["p_reason"] == 2
+
+
+@pytest.mark.parametrize("size", list(SIZES))
+def test_full_steps_match_oracle(size):
+    """Whole timesteps on device-resident state, per step: before every step
+    the GPU context is loaded with the oracle's state, both take one step,
+    and phi, u, v, w must match to 1e-11 (pressure solved to 1e-14 so the
+    solve's own tolerance is not what is measured).  Four steps on cubic
+    cells, two on the 2*pi x pi x 1 box (the reference's h = dx
+    redistancing degrades that channel over ~85 steps, not over two)."""
+    nx, ny, nz = SIZES[size]
+    params, uin, st = make_case("A", nx=nx, ny=ny, nz=nz, p_rtol=1e-14, p_maxits=400, geometry=_geometry(size))
+    o = Oracle(nx, ny, nz, params, uin)
+    o.set_state(st)
+    g = TplsGpu(nx, ny, nz, params, uin)
+    _steps_match(o, g, nx, ny, nz, 2 if _geometry(size) == "box" else 4)
     g.close()
+
+
+@pytest.mark.parametrize("geometry", ["cubic", "box"])
+def test_headline_grid_step_matches_oracle(geometry):
+    """One step at the benchmark grid, 256x128x192 (6.3 M cells): the oracle
+    takes the seeded state one step (all host cores), the GPU is loaded with
+    that state, both take the next step, and phi, u, v, w and p must agree to
+    1e-11 with the pressure solved to 1e-14.  Cubic cells are the timed
+    workload; the box is the 2*pi x pi x 1 channel the configuration names."""
+    set_threads(os.cpu_count() or 1)
+    try:
+        nx, ny, nz = 256, 128, 192
+        params, uin, st = make_case("B", p_rtol=1e-14, p_maxits=400, geometry=geometry)
+        o = Oracle(nx, ny, nz, params, uin)
+        o.set_state(st)
+        o.step(1)  # non-zero AB3 histories
+        g = TplsGpu(nx, ny, nz, params, uin)
+        _steps_match(o, g, nx, ny, nz, 1)
+        g.close()
+        o.close()
+    finally:
+        set_threads(int(os.environ.get("TPLS_ORACLE_THREADS", "1")))
 
 
 def test_full_steps_match_oracle_fp32_preconditioner():

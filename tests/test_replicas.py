@@ -73,9 +73,17 @@ def test_reference_arm_rank0_prints_the_contract_line():
     with no host-device bytes (one 256x128x192 step on the host cores)."""
     import json
     env = {k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK")}
-    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--steps", "1",
-                        "--warmup", "1"], capture_output=True, text=True, env=env, timeout=600, cwd=ROOT)
+    # run bench.py's main in a process that afterwards reports whether the
+    # CUDA library was ever mapped: the CPU arm must not load the product
+    code = ("import runpy, sys; sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', '--warmup', '1']; "
+            "runpy.run_path('bench.py', run_name='__main__'); "
+            "maps = open('/proc/self/maps').read(); "
+            "print('MAPS', int('libtpls_gb300' in maps), int('liboracle' in maps), file=sys.stderr)")
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env, timeout=600,
+                       cwd=ROOT)
     assert r.returncode == 0, r.stderr[-2000:]
+    maps = [ln.split() for ln in r.stderr.splitlines() if ln.startswith("MAPS ")]
+    assert maps == [["MAPS", "0", "1"]], r.stderr[-2000:]
     lines = [ln for ln in r.stdout.splitlines() if ln.strip()]
     assert len(lines) == 1
     d = json.loads(lines[0])

@@ -25,30 +25,35 @@ def _noalloc(lib):
 
 
 def test_no_alloc_difference_matches_allocating_entry_twice():
+    """Two calls in a row, the second on a smaller grid (fewer rows than the
+    first call left in the shared scratch): each must equal the NumPy sum of
+    (ua - ub)^2 over i 1..nx, j 1..ny and every plane, and the allocating
+    entry's result."""
     torch = pytest.importorskip("torch")
     from tpls_gb300.api import TplsGpu, load_library
     from tpls_gb300.channel import make_case
 
     lib = load_library()
     fn = _noalloc(lib)
-    nx, ny, nz = 37, 19, 23
-    params, uin, _ = make_case("A", nx=nx, ny=ny, nz=nz)
-    g = TplsGpu(nx, ny, nz, params, uin)
     rng = np.random.default_rng(2026)
     out = torch.zeros(1, dtype=torch.float64, device="cuda")
     stream = torch.cuda.current_stream().cuda_stream
-    for call in range(2):
+    for call, (nx, ny, nz) in enumerate(((37, 19, 23), (20, 11, 9))):
+        params, uin, _ = make_case("A", nx=nx, ny=ny, nz=nz)
+        g = TplsGpu(nx, ny, nz, params, uin)
         ua = np.asfortranarray(rng.normal(size=(nx + 2, ny + 2, nz)) * (call + 1))
         ub = np.asfortranarray(rng.normal(size=(nx + 2, ny + 2, nz)))
-        expect = g.get_difference(ua, ub)
+        d = (ua - ub)[1:nx + 1, 1:ny + 1, :]
+        expect = float(np.sum(d * d))
+        assert abs(g.get_difference(ua, ub) - expect) <= TOL * expect
+        g.close()
         da = torch.from_numpy(ua.ravel(order="F")).cuda()
         db = torch.from_numpy(ub.ravel(order="F")).cuda()
         s = fn(da.data_ptr(), db.data_ptr(), nx, ny, nz, out.data_ptr(), stream)
         assert s == 0, lib.tpls_status_string(s)
         torch.cuda.synchronize()
         got = float(out.item())
-        assert abs(got - expect) <= TOL * abs(expect), (call, got, expect)
-    g.close()
+        assert abs(got - expect) <= TOL * expect, (call, got, expect)
 
 
 def test_no_alloc_rejects_sizes_beyond_its_scratch():

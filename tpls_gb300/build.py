@@ -46,6 +46,18 @@ def _run(cmd: list[str]) -> None:
         sys.stderr.write(r.stdout + r.stderr)
 
 
+def source_digest() -> str:
+    """12 hex digits of SHA-256 over the CUDA sources, headers and build
+    flags: names the build an ncu capture was taken of."""
+    import hashlib
+    h = hashlib.sha256(" ".join(ARCH + NVCC_FLAGS[:-1]).encode())
+    files = sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.cuh"))
+    for f in files + [ROOT / "include" / "tpls_gpu.h"]:
+        h.update(f.name.encode())
+        h.update(f.read_bytes())
+    return h.hexdigest()[:12]
+
+
 def _stale(target: Path, sources: list[Path]) -> bool:
     if not target.exists():
         return True

@@ -2,18 +2,24 @@
 benchmark configurations) built with the reference's own initial-condition
 routine for the base flow.
 
-Channel: cubic cells dx = dy = dz = 1/nz, Lz = 1, Lx = nx dz, Ly = ny dz
-(the grid of twophase_initialisation_wave.F90:66-75); inlet/outlet in x,
-periodic y, no-slip walls in z (the reference's boundary conditions).  Two
-layers: mu_minus = m below the interface (phi < 0), mu_plus = 1 above;
-viscosity (mu)/Re.
+Two geometries:
 
-Cubic cells are required by the reference's redistancing: levelset.f90
-uses one spacing h = dx for every direction (the Godunov gradient and the
-inlet row z = k h - h/2, levelset.f90:168-177), so on a 2*pi x pi x 1 box
+* ``"cubic"`` (default): cubic cells dx = dy = dz = 1/nz, Lz = 1,
+  Lx = nx dz, Ly = ny dz (the grid of twophase_initialisation_wave.F90:66-75);
+* ``"box"``: the 2*pi x pi x 1 channel, dx = 2 pi/nx, dy = pi/ny, dz = 1/nz
+  (dx, dy and dz all differ on grids such as 37x19x23).
+
+Inlet/outlet in x, periodic y, no-slip walls in z (the reference's boundary
+conditions).  Two layers: mu_minus = m below the interface (phi < 0),
+mu_plus = 1 above; viscosity (mu)/Re.
+
+Long runs use cubic cells: the reference's redistancing (levelset.f90) uses
+one spacing h = dx for every direction (the Godunov gradient and the inlet
+row z = k h - h/2, levelset.f90:168-177), so on the 2*pi x pi x 1 box
 (dx = 4.7 dz at 256x128x192) it drives phi towards a distance function
 stretched 4.7 times in z; the interface band collapses and the reference's
-algorithm diverges (NaN near step 85 at 256x128x192).
+algorithm diverges (NaN near step 85 at 256x128x192).  A few steps on the
+box are well-defined arithmetic, which the parity tests check.
 
 * phi = z - h(x, y) on every p-grid point including ghosts, with cell
   centres x_i = (i-1/2)dx, y_j = (j-1/2)dy, z_k = (k-1/2)dz;
@@ -116,22 +122,31 @@ def interface_height(w: Workload, x: np.ndarray, y: np.ndarray, Lx: float, Ly: f
 def make_case(w: Workload | str, *, nx: int | None = None, ny: int | None = None, nz: int | None = None,
               mom: int = 30, levelset: int = 10, p_rtol: float = 1e-5, p_maxits: int = 200,
               precision: int = 0, fp64_parts: int = 0, mg_fp32: int = 0, idm: str = "lsm",
-              epn: float | None = None, pe: float = 1000.0, max_iteration_dim: int = 18):
+              epn: float | None = None, pe: float = 1000.0, max_iteration_dim: int = 18,
+              geometry: str = "cubic", profile=None):
     """Returns (params, u_inlet, state) for a workload, optionally resized.
 
     state maps TPLS field names (tpls_gb300.api.STATE_FIELDS subset) to
-    Fortran-ordered arrays; fields not given start at zero."""
+    Fortran-ordered arrays; fields not given start at zero.  `profile` is
+    the base-state routine (the signature of api.base_profile; default: the
+    library's host code)."""
     if isinstance(w, str):
         w = WORKLOADS[w]
     nx = nx or w.nx
     ny = ny or w.ny
     nz = nz or w.nz
     dz = 1.0 / nz
-    dx = dy = dz
-    Lx, Ly = nx * dx, ny * dy
+    if geometry == "cubic":
+        dx = dy = dz
+        Lx, Ly = nx * dx, ny * dy
+    elif geometry == "box":
+        Lx, Ly = 2.0 * np.pi, np.pi
+        dx, dy = Lx / nx, Ly / ny
+    else:
+        raise ValueError(f"unknown geometry {geometry!r}")
     sw = 1.5 * dx
     mu_minus, mu_plus = w.m, 1.0
-    uz = base_profile(nz, dz, w.re, -1.0, mu_minus, mu_plus, 0.5, sw)
+    uz = (profile or base_profile)(nz, dz, w.re, -1.0, mu_minus, mu_plus, 0.5, sw)
     umax = float(np.max(np.abs(uz)))
     # CFL 0.2 on the base flow, and half the capillary limit of the explicit
     # surface-tension term, sqrt(rho dx^3 / (2 pi sigma)) with rho = 1 and

@@ -35,7 +35,10 @@ static __device__ __align__(256) double g_noalloc_partials[kMaxRows];
 
 // Device address of g_noalloc_partials per device ordinal.  In host code the
 // array's name is only a host-side stand-in, so the address is looked up
-// once per device, with that device current, by the first call made on it.
+// once per device, with that device current, by the first call made on it,
+// and kept until the process exits.  cudaDeviceReset destroys the context
+// that holds the array, so the kept address does not survive it: the entry
+// is not for use on a device after a reset.
 double *g_partials_addr[kMaxDevices] = {nullptr};
 std::mutex g_partials_mu;
 

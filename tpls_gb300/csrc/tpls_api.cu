@@ -727,44 +727,46 @@ static int step_once(tpls_ctx *c) {
     PhaseScope ps(c, TPLS_T_ADVECT);
     LCK(c, launch_advect(g, ph, c->phi2, c->u2, c->v2, c->w2, c->conv_phi[s2], st));
   }
-  PhaseScope *ls_scope = new PhaseScope(c, TPLS_T_LEVELSET);
-  if (c->dim) {
-    int sd;
-    if ((sd = dim_stage(c, c->conv_phi[s2]))) return sd;
-  } else {
-    LCK(c, launch_ls_ab3(g, ph, c->phi2, c->conv_phi[s0], c->conv_phi[s1], c->conv_phi[s2], c->phiA, st));
-    LCK(c, launch_ls_status(g, ph, c->phiA, c->D, c->flags, st));
-    const int L = c->prm.levelset;
-    if (L <= 0) {
-      TCK(cudaMemcpyAsync(c->phi2 - XOFF, c->phiA - XOFF,
-                          sizeof(double) * ((size_t)c->px * (c->ny + 2) * (c->nz + 2)), cudaMemcpyDeviceToDevice, st));
-      TCK(cudaMemsetAsync(c->scal + SC_ERR_PHI, 0, sizeof(double), st));
+  {
+    PhaseScope ls_scope(c, TPLS_T_LEVELSET);
+    if (c->dim) {
+      int sd;
+      if ((sd = dim_stage(c, c->conv_phi[s2]))) return sd;
+    } else {
+      LCK(c, launch_ls_ab3(g, ph, c->phi2, c->conv_phi[s0], c->conv_phi[s1], c->conv_phi[s2], c->phiA, st));
+      LCK(c, launch_ls_status(g, ph, c->phiA, c->D, c->flags, st));
+      const int L = c->prm.levelset;
+      if (L <= 0) {
+        TCK(cudaMemcpyAsync(c->phi2 - XOFF, c->phiA - XOFF,
+                            sizeof(double) * ((size_t)c->px * (c->ny + 2) * (c->nz + 2)), cudaMemcpyDeviceToDevice, st));
+        TCK(cudaMemsetAsync(c->scal + SC_ERR_PHI, 0, sizeof(double), st));
+      }
+      for (int it = 1; it <= L; it++) {
+        const double *src = (it == 1) ? c->phiA : ((it % 2 == 0) ? c->phiB : c->phiA);
+        double *dst = (it == L) ? c->phi2 : ((it % 2 == 1) ? c->phiB : c->phiA);
+        LCK(c, launch_ls_iter(g, ph, src, c->D, c->flags, dst, (it == L) ? c->part : nullptr, st));
+      }
+      if (L > 0) FSUM(c, c->part, ls_iter_blocks(g), c->scal + SC_ERR_PHI, st);
     }
-    for (int it = 1; it <= L; it++) {
-      const double *src = (it == 1) ? c->phiA : ((it % 2 == 0) ? c->phiB : c->phiA);
-      double *dst = (it == L) ? c->phi2 : ((it % 2 == 1) ? c->phiB : c->phiA);
-      LCK(c, launch_ls_iter(g, ph, src, c->D, c->flags, dst, (it == L) ? c->part : nullptr, st));
-    }
-    if (L > 0) FSUM(c, c->part, ls_iter_blocks(g), c->scal + SC_ERR_PHI, st);
   }
-  delete ls_scope;
   // CSF from the redistanced phi3 (:618-641)
   {
     PhaseScope ps(c, TPLS_T_CSF);
     LCK(c, launch_csf(g, ph, c->phi2, c->fx, c->fy, c->fz, st));
   }
-  PhaseScope *rhs_scope = new PhaseScope(c, TPLS_T_MOM_RHS);
-  // convective / diffusive terms and AB3 + CN right-hand sides (:728-751)
-  LCK(c, launch_mom_rhs(0, g, ph, c->u2, c->v2, c->w2, c->mu, c->fx, c->conv_u[s1], c->conv_u[s0],
-                        c->csf_u[s1], c->csf_u[s0], c->conv_u[s2], c->csf_u[s2], nullptr, nullptr, c->coef[0],
-                        st));
-  LCK(c, launch_mom_rhs(1, g, ph, c->u2, c->v2, c->w2, c->mu, c->fy, c->conv_v[s1], c->conv_v[s0],
-                        c->csf_v[s1], c->csf_v[s0], c->conv_v[s2], c->csf_v[s2], nullptr, nullptr, c->coef[1],
-                        st));
-  LCK(c, launch_mom_rhs(2, g, ph, c->u2, c->v2, c->w2, c->mu, c->fz, c->conv_w[s1], c->conv_w[s0],
-                        c->csf_w[s1], c->csf_w[s0], c->conv_w[s2], c->csf_w[s2], nullptr, nullptr, c->coef[2],
-                        st));
-  delete rhs_scope;
+  {
+    PhaseScope rhs_scope(c, TPLS_T_MOM_RHS);
+    // convective / diffusive terms and AB3 + CN right-hand sides (:728-751)
+    LCK(c, launch_mom_rhs(0, g, ph, c->u2, c->v2, c->w2, c->mu, c->fx, c->conv_u[s1], c->conv_u[s0],
+                          c->csf_u[s1], c->csf_u[s0], c->conv_u[s2], c->csf_u[s2], nullptr, nullptr, c->coef[0],
+                          st));
+    LCK(c, launch_mom_rhs(1, g, ph, c->u2, c->v2, c->w2, c->mu, c->fy, c->conv_v[s1], c->conv_v[s0],
+                          c->csf_v[s1], c->csf_v[s0], c->conv_v[s2], c->csf_v[s2], nullptr, nullptr, c->coef[1],
+                          st));
+    LCK(c, launch_mom_rhs(2, g, ph, c->u2, c->v2, c->w2, c->mu, c->fz, c->conv_w[s1], c->conv_w[s0],
+                          c->csf_w[s1], c->csf_w[s0], c->conv_w[s2], c->csf_w[s2], nullptr, nullptr, c->coef[2],
+                          st));
+  }
   // momentum sweeps (:756-887)
   int s;
   if ((s = momentum<double, const double *>(c, 0, c->coef[0], c->x3[0], c->prm.mom_u))) return s;
@@ -841,29 +843,30 @@ static int step_once_mixed(tpls_ctx *c) {
       LCK(c, launch_advect(g, ph, (const float *)c->phi32, c->u32, c->v32, c->w32, c->conv_phi[s2], st));
     }
   }
-  PhaseScope *ls_scope = new PhaseScope(c, TPLS_T_LEVELSET);
-  LCK(c, launch_ls_ab3(g, ph, c->phi2, c->conv_phi[s0], c->conv_phi[s1], c->conv_phi[s2], c->phiA, st));
-  const int L = c->prm.levelset;
-  if (ls64) LCK(c, launch_ls_status(g, ph, c->phiA, c->D, c->flags, st));
-  else LCK(c, launch_ls_status(g, ph, c->phiA, c->D32, c->flags, st));
-  if (L <= 0) {
-    TCK(cudaMemcpyAsync(c->phi2 - XOFF, c->phiA - XOFF, sizeof(double) * c->n_p, cudaMemcpyDeviceToDevice, st));
-    TCK(cudaMemsetAsync(c->scal + SC_ERR_PHI, 0, sizeof(double), st));
-  }
-  for (int it = 1; it <= L; it++) {
-    double *ep = (it == L) ? c->part : nullptr;
-    if (ls64) {
-      const double *src = (it == 1) ? c->phiA : ((it % 2 == 0) ? c->phiB : c->phiA);
-      double *dst = (it == L) ? c->phi2 : ((it % 2 == 1) ? c->phiB : c->phiA);
-      LCK(c, launch_ls_iter(g, ph, src, c->D, c->flags, dst, ep, st));
-    } else {  // FP32 increments on float-pair iterates: it reads pair it%2, writes pair (it+1)%2
-      const int ri = it % 2, wi = (it + 1) % 2;
-      LCK(c, launch_ls_iter_ff(g, ph, (it == 1) ? c->phiA : nullptr, c->ffh[ri], c->ffl[ri], c->D32, c->flags,
-                               (it == L) ? c->phi2 : nullptr, c->ffh[wi], c->ffl[wi], ep, st));
+  {
+    PhaseScope ls_scope(c, TPLS_T_LEVELSET);
+    LCK(c, launch_ls_ab3(g, ph, c->phi2, c->conv_phi[s0], c->conv_phi[s1], c->conv_phi[s2], c->phiA, st));
+    const int L = c->prm.levelset;
+    if (ls64) LCK(c, launch_ls_status(g, ph, c->phiA, c->D, c->flags, st));
+    else LCK(c, launch_ls_status(g, ph, c->phiA, c->D32, c->flags, st));
+    if (L <= 0) {
+      TCK(cudaMemcpyAsync(c->phi2 - XOFF, c->phiA - XOFF, sizeof(double) * c->n_p, cudaMemcpyDeviceToDevice, st));
+      TCK(cudaMemsetAsync(c->scal + SC_ERR_PHI, 0, sizeof(double), st));
     }
+    for (int it = 1; it <= L; it++) {
+      double *ep = (it == L) ? c->part : nullptr;
+      if (ls64) {
+        const double *src = (it == 1) ? c->phiA : ((it % 2 == 0) ? c->phiB : c->phiA);
+        double *dst = (it == L) ? c->phi2 : ((it % 2 == 1) ? c->phiB : c->phiA);
+        LCK(c, launch_ls_iter(g, ph, src, c->D, c->flags, dst, ep, st));
+      } else {  // FP32 increments on float-pair iterates: it reads pair it%2, writes pair (it+1)%2
+        const int ri = it % 2, wi = (it + 1) % 2;
+        LCK(c, launch_ls_iter_ff(g, ph, (it == 1) ? c->phiA : nullptr, c->ffh[ri], c->ffl[ri], c->D32, c->flags,
+                                 (it == L) ? c->phi2 : nullptr, c->ffh[wi], c->ffl[wi], ep, st));
+      }
+    }
+    if (L > 0) FSUM(c, c->part, ls_iter_blocks(g), c->scal + SC_ERR_PHI, st);
   }
-  if (L > 0) FSUM(c, c->part, ls_iter_blocks(g), c->scal + SC_ERR_PHI, st);
-  delete ls_scope;
   int s;
   const void *u3v;
   const void *v3v, *w3v;
