@@ -33,6 +33,7 @@ extern "C" {
 #define TPLS_ERR_ALLOC 2       /* device allocation failed */
 #define TPLS_ERR_STATE 3       /* call sequence error */
 #define TPLS_ERR_NOT_BUILT 4   /* feature not compiled into the library */
+#define TPLS_ERR_IO 6          /* a file could not be opened, written or parsed */
 #define TPLS_ERR_CUDA_BASE 1000 /* + cudaError_t */
 #define TPLS_KSP_CONVERGED_RTOL 2
 #define TPLS_KSP_CONVERGED_ATOL 3
@@ -132,6 +133,11 @@ int tpls_gpu_create(int nx, int ny, int nz, const tpls_params *prm,
 int tpls_gpu_destroy(tpls_ctx *ctx);
 int tpls_set_field(tpls_ctx *ctx, int field, const double *host);
 int tpls_get_field(tpls_ctx *ctx, int field, double *host);
+/* Grid of the context. */
+int tpls_get_dims(const tpls_ctx *ctx, int *nx, int *ny, int *nz);
+/* Step counter reported in tpls_stats.steps_done, for a restarted run that
+ * continues an earlier one's count (the driver's `iteration`). */
+int tpls_set_steps_done(tpls_ctx *ctx, long steps_done);
 /* Device-resident fast path: nsteps full timesteps of main_ns_hybrid.F90:
  * 583-918 followed by the history rotation :2480-2509.  Returns TPLS_OK;
  * TPLS_KSP_DIVERGED_ITS if any pressure solve hit p_maxits (the remaining
@@ -400,6 +406,54 @@ int tpls_pressure_solve(tpls_ctx *ctx, double *pres, const double *pres_old,
 #define TPLS_ERR_NOALLOC_LIMIT 5
 int tpls_get_difference_noalloc(const double *ua, const double *ub, int nx,
                                 int ny, int nzp, double *diff, void *stream);
+
+/* ---- backup / restart files ----------------------------------------------
+ * io.F90:647-716 backup_channel: the reference's text backup (one record
+ * per point, i fastest: u2, conv0_u, conv1_u over the u grid; the same for
+ * v; w2, conv0_w, conv1_w over the w grid; phi, conv0_phi, conv1_phi and
+ * pres, pres_old over the p grid), from host arrays with the routine's
+ * argument list (l = nx+1, m = ny+1, n = nz+1, by reference).  Values carry
+ * 17 significant digits, so a load restores them bit for bit.  Returns
+ * TPLS_ERR_IO when the file cannot be written. */
+int tpls_write_backup(const double *u2, const double *v2, const double *w2,
+                      const double *conv0_u, const double *conv1_u,
+                      const double *conv0_v, const double *conv1_v,
+                      const double *conv0_w, const double *conv1_w,
+                      const double *pres_old, const double *pres,
+                      const double *phi, const double *conv0_phi,
+                      const double *conv1_phi, const int *l, const int *m,
+                      const int *n, const char *filename);
+/* io.F90:721-791 dataload_channel: reads that layout (any list-directed
+ * number form: E or D exponents, r*value repeats); TPLS_ERR_IO when the file
+ * is missing or short. */
+int tpls_read_backup(double *u2, double *v2, double *w2, double *conv0_u,
+                     double *conv1_u, double *conv0_v, double *conv1_v,
+                     double *conv0_w, double *conv1_w, double *pres_old,
+                     double *pres, double *phi, double *conv0_phi,
+                     double *conv1_phi, const int *l, const int *m,
+                     const int *n, const char *filename);
+/* No counterpart in the reference, whose backup leaves out the AB3 history
+ * of the surface-tension force: csf_u0, csf_u1 over the u grid, csf_v0,
+ * csf_v1 over the v grid, csf_w0, csf_w1 over the w grid, in the same text
+ * style.  With it a restart continues the run bit for bit. */
+int tpls_write_backup_csf(const double *csf_u0, const double *csf_u1,
+                          const double *csf_v0, const double *csf_v1,
+                          const double *csf_w0, const double *csf_w1,
+                          const int *l, const int *m, const int *n,
+                          const char *filename);
+int tpls_read_backup_csf(double *csf_u0, double *csf_u1, double *csf_v0,
+                         double *csf_v1, double *csf_w0, double *csf_w1,
+                         const int *l, const int *m, const int *n,
+                         const char *filename);
+/* The same files written from / read into a context's device state
+ * (main_ns_hybrid.F90:2450-2468 writes fieldbackup0.dat / fieldbackup1.dat
+ * alternately).  csf_filename may be NULL (the CSF histories are then not
+ * written / left as they are).  The load reads both files completely before
+ * it changes the device state. */
+int tpls_backup_channel(tpls_ctx *ctx, const char *filename,
+                        const char *csf_filename);
+int tpls_dataload_channel(tpls_ctx *ctx, const char *filename,
+                          const char *csf_filename);
 
 /* mpi.f90:110  exchange2d on one rank = periodic-y ghost rows over the full
  * x span, for an array (0:nx+1,0:ny+1,sz:ez). */

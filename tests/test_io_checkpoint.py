@@ -83,10 +83,12 @@ def test_checkpoint_restart_is_bit_identical(tmp_path):
     save_checkpoint(b, tmp_path / "ck.npz")
     b.close()
     c = load_checkpoint(tmp_path / "ck.npz")
+    assert c.stats()["steps_done"] == 2  # the step count continues
     c.step(3)
     sa, sc = a.get_state(), c.get_state()
     for k in STATE_FIELDS:
         assert np.array_equal(sa[k], sc[k]), k
+    assert c.stats()["steps_done"] == 5
     a.close()
     c.close()
 
@@ -118,3 +120,112 @@ def test_checkpoint_file_holds_the_whole_state(tmp_path):
     b.step(2)
     for k, v in a.get_state().items():
         assert np.array_equal(v, b.get_field(k)), k
+
+
+# ---- the reference's backup format (io.F90:647-791) -------------------------
+
+_BK_NAMES = ["u2", "v2", "w2", "conv0_u", "conv1_u", "conv0_v", "conv1_v", "conv0_w", "conv1_w", "pres_old",
+             "pres", "phi", "conv0_phi", "conv1_phi"]
+
+
+def _bk_shapes(nx, ny, nz):
+    uv, w, p = (nx + 2, ny + 2, nz), (nx + 2, ny + 2, nz + 1), (nx + 2, ny + 2, nz + 2)
+    return {"u2": uv, "v2": uv, "w2": w, "conv0_u": uv, "conv1_u": uv, "conv0_v": uv, "conv1_v": uv,
+            "conv0_w": w, "conv1_w": w, "pres_old": p, "pres": p, "phi": p, "conv0_phi": p, "conv1_phi": p}
+
+
+def _bk_call(fn, arrays, nx, ny, nz, path):
+    import ctypes as C
+    dp = [a.ctypes.data_as(C.POINTER(C.c_double)) for a in arrays]
+    l, m, n = C.c_int(nx + 1), C.c_int(ny + 1), C.c_int(nz + 1)
+    return fn(*dp, C.byref(l), C.byref(m), C.byref(n), str(path).encode())
+
+
+def test_reference_backup_layout_and_round_trip(tmp_path):
+    """tpls_write_backup writes backup_channel's records (i fastest; u, v, w
+    blocks of three values, phi block of three, pres block of two) with 17
+    significant digits, and tpls_read_backup restores them bit for bit."""
+    from tpls_gb300.api import load_library
+    lib = load_library()
+    nx, ny, nz = 5, 3, 4
+    rng = np.random.default_rng(3)
+    sh = _bk_shapes(nx, ny, nz)
+    arrs = {k: np.asfortranarray(rng.normal(size=sh[k]) * 10.0 ** rng.integers(-8, 8)) for k in _BK_NAMES}
+    f = tmp_path / "fieldbackup0.dat"
+    assert _bk_call(lib.tpls_write_backup, [arrs[k] for k in _BK_NAMES], nx, ny, nz, f) == 0
+    lines = f.read_text().splitlines()
+    nuv, nw, np_ = (nx + 2) * (ny + 2) * nz, (nx + 2) * (ny + 2) * (nz + 1), (nx + 2) * (ny + 2) * (nz + 2)
+    assert len(lines) == 2 * nuv + nw + 2 * np_
+    rows = [[float(t) for t in ln.split()] for ln in lines]
+    # record c of the u block: u2, conv0_u, conv1_u at Fortran position c
+    c = 17
+    assert rows[c] == [arrs["u2"].ravel(order="F")[c], arrs["conv0_u"].ravel(order="F")[c],
+                       arrs["conv1_u"].ravel(order="F")[c]]
+    last = rows[-1]
+    assert last == [arrs["pres"].ravel(order="F")[-1], arrs["pres_old"].ravel(order="F")[-1]]
+    back = {k: np.zeros(sh[k], order="F") for k in _BK_NAMES}
+    assert _bk_call(lib.tpls_read_backup, [back[k] for k in _BK_NAMES], nx, ny, nz, f) == 0
+    for k in _BK_NAMES:
+        assert np.array_equal(back[k], arrs[k]), k
+
+
+def test_reference_backup_reads_fortran_list_directed_forms(tmp_path):
+    """A file in the forms a Fortran list-directed write or a hand edit
+    produces (D exponents, comma separators, r*value repeats) reads like the
+    reference's dataload_channel would; a short or missing file is
+    TPLS_ERR_IO (6)."""
+    from tpls_gb300.api import load_library
+    lib = load_library()
+    nx, ny, nz = 2, 2, 3
+    sh = _bk_shapes(nx, ny, nz)
+    nuv, nw, np_ = 4 * 4 * nz, 4 * 4 * (nz + 1), 4 * 4 * (nz + 2)
+    parts = ["   1.0000000000000000       0.50000000000000000      -2.5000000000000000D-002"]
+    parts += ["%d*0.0" % (3 * nuv - 3)]
+    parts += ["1.5E+00, 2, 3"] * nuv
+    parts += ["  -7.0D0  8.0  9.0"] * nw
+    parts += ["4.0 5.0 6.0"] * np_
+    parts += ["1.0D+01 2.0d+01"] * np_
+    f = tmp_path / "ref.dat"
+    f.write_text("\n".join(parts) + "\n")
+    back = {k: np.full(sh[k], np.nan, order="F") for k in _BK_NAMES}
+    assert _bk_call(lib.tpls_read_backup, [back[k] for k in _BK_NAMES], nx, ny, nz, f) == 0
+    u = back["u2"].ravel(order="F")
+    assert u[0] == 1.0 and back["conv0_u"].ravel(order="F")[0] == 0.5
+    assert back["conv1_u"].ravel(order="F")[0] == -0.025 and u[1] == 0.0
+    assert np.all(back["v2"] == 1.5) and np.all(back["conv1_v"] == 3.0) and np.all(back["w2"] == -7.0)
+    assert np.all(back["phi"] == 4.0) and np.all(back["pres"] == 10.0) and np.all(back["pres_old"] == 20.0)
+    short = tmp_path / "short.dat"
+    short.write_text("\n".join(parts[:-5]) + "\n")
+    assert _bk_call(lib.tpls_read_backup, [back[k] for k in _BK_NAMES], nx, ny, nz, short) == 6
+    assert _bk_call(lib.tpls_read_backup, [back[k] for k in _BK_NAMES], nx, ny, nz, tmp_path / "none.dat") == 6
+
+
+@pytest.mark.gpu
+def test_reference_backup_restart_is_bit_identical(tmp_path):
+    """Backup after 2 steps (the reference's file plus the CSF companion),
+    restart a fresh context from it, 3 more steps: bit-identical to 5
+    uninterrupted steps, with the step count carried over."""
+    from tpls_gb300.api import STATE_FIELDS, TplsGpu
+    from tpls_gb300.channel import make_case
+    from tpls_gb300.checkpoint import backup_channel, csf_companion, dataload_channel
+    nx, ny, nz = 32, 16, 24
+    params, uin, st = make_case("A", nx=nx, ny=ny, nz=nz)
+    a = TplsGpu(nx, ny, nz, params, uin)
+    a.set_state(st)
+    a.step(5)
+    b = TplsGpu(nx, ny, nz, params, uin)
+    b.set_state(st)
+    b.step(2)
+    f = tmp_path / "fieldbackup0.dat"
+    backup_channel(b, f)
+    assert (tmp_path / "fieldbackup0_csf.dat").exists() and csf_companion(f).endswith("fieldbackup0_csf.dat")
+    b.close()
+    c = TplsGpu(nx, ny, nz, params, uin)
+    dataload_channel(c, f, steps_done=2)
+    c.step(3)
+    sa, sc = a.get_state(), c.get_state()
+    for k in STATE_FIELDS:
+        assert np.array_equal(sa[k], sc[k]), k
+    assert c.stats()["steps_done"] == 5
+    a.close()
+    c.close()

@@ -26,23 +26,29 @@ NX, NY, NZ = 64, 32, 48
 ROWS = (slice(None), slice(1, NY + 1), slice(None))
 
 
-def _ctx(precision, **kw):
-    params, uin, st = make_case("A", nx=NX, ny=NY, nz=NZ, precision=precision, **kw)
-    g = TplsGpu(NX, NY, NZ, params, uin)
+def _ctx(precision, size=(NX, NY, NZ), **kw):
+    nx, ny, nz = size
+    params, uin, st = make_case("A", nx=nx, ny=ny, nz=nz, precision=precision, **kw)
+    g = TplsGpu(nx, ny, nz, params, uin)
     g.set_state(st)
     return g
 
 
-def test_mixed_one_step_from_fp64_state():
-    ref = _ctx(0, p_rtol=1e-12, p_maxits=400)
+# the FP32 sweeps own four x points per thread: 37 and 33 leave ragged last
+# groups (one point for v and w at 33), odd ny takes the unfused ghost-row
+# path, and 8x6x160 is a tall column for the odd half-sweep's column march
+@pytest.mark.parametrize("size", [(NX, NY, NZ), (37, 19, 23), (33, 17, 31), (8, 6, 160)])
+def test_mixed_one_step_from_fp64_state(size):
+    ref = _ctx(0, size, p_rtol=1e-12, p_maxits=400)
     ref.step(5)
     s5 = ref.get_state()
-    mix = _ctx(1, p_rtol=1e-12, p_maxits=400)
+    mix = _ctx(1, size, p_rtol=1e-12, p_maxits=400)
     mix.set_state(s5)
-    ref2 = _ctx(0, p_rtol=1e-12, p_maxits=400)
+    ref2 = _ctx(0, size, p_rtol=1e-12, p_maxits=400)
     ref2.set_state(s5)
     assert ref2.step(1) == 0 and mix.step(1) == 0
-    e = {k: relmax(mix.get_field(k), ref2.get_field(k), ROWS) for k in ("PHI2", "U2", "V2", "W2", "PRES")}
+    rows = (slice(None), slice(1, size[1] + 1), slice(None))
+    e = {k: relmax(mix.get_field(k), ref2.get_field(k), rows) for k in ("PHI2", "U2", "V2", "W2", "PRES")}
     assert e["PHI2"] < 1e-5 and e["U2"] < 1e-5, e
     assert e["V2"] < 1e-4 and e["W2"] < 1e-4, e
     assert e["PRES"] < 1e-3, e
@@ -92,13 +98,13 @@ def test_mixed_with_every_part_fp64_equals_fp64_form():
     mix.close()
 
 
-@pytest.mark.parametrize("parts", [0, 16])
+@pytest.mark.parametrize("parts", [0, 16, 18])
 def test_mixed_hundred_steps_fp32_and_fp64_stencils(parts):
     """100 steps with the momentum stencils in FP32 (parts 0: velocity
     values split into exact FP32 pairs, the sweeps' coefficients recomputed
     from the FP32 viscosity) and in FP64 (parts 16): phi and u stay within
     1e-5 of the FP64 form, v and w within 1e-4, the liquid volume within
-    1e-8."""
+    1e-8.  Parts 18 also keeps redistancing in FP64."""
     ref = _ctx(0)
     mix = _ctx(1, fp64_parts=parts)
     assert ref.step(100) == 0 and mix.step(100) == 0

@@ -151,6 +151,9 @@ def load_library(path: Path | None = None) -> C.CDLL:
     lib.tpls_timing_read.argtypes = [C.c_void_p, _DP, C.POINTER(C.c_long), C.c_int]
     lib.tpls_stream.argtypes = [C.c_void_p]
     lib.tpls_stream.restype = C.c_void_p
+    lib.tpls_set_steps_done.argtypes = [C.c_void_p, C.c_long]
+    lib.tpls_backup_channel.argtypes = [C.c_void_p, C.c_char_p, C.c_char_p]
+    lib.tpls_dataload_channel.argtypes = [C.c_void_p, C.c_char_p, C.c_char_p]
     if path is None:
         _lib = lib
     return lib
@@ -286,6 +289,21 @@ class TplsGpu:
         t = (C.c_int * 3)()
         self._check(self.lib.tpls_get_tiles(self.ctx, t))
         return {"jacobi": t[0], "sor_even": t[1], "sor_odd": t[2]}
+
+    def set_steps_done(self, n: int) -> None:
+        """Continue an earlier run's step count (tpls_stats.steps_done)."""
+        self._check(self.lib.tpls_set_steps_done(self.ctx, int(n)))
+
+    def backup_channel(self, filename, csf_filename=None) -> None:
+        """io.F90:647 backup_channel of the device state: the reference's
+        text backup, plus (csf_filename) the CSF histories it leaves out."""
+        self._check(self.lib.tpls_backup_channel(self.ctx, str(filename).encode(),
+                                                 None if csf_filename is None else str(csf_filename).encode()))
+
+    def dataload_channel(self, filename, csf_filename=None) -> None:
+        """io.F90:721 dataload_channel into the device state."""
+        self._check(self.lib.tpls_dataload_channel(self.ctx, str(filename).encode(),
+                                                   None if csf_filename is None else str(csf_filename).encode()))
 
     def graphs_enable(self, on: bool = True) -> None:
         self._check(self.lib.tpls_graphs_enable(self.ctx, 1 if on else 0))

@@ -393,11 +393,12 @@ static cudaError_t sor_c(int comp, const Geo &g, const Phys &ph, T *x, CS coef, 
   return cudaGetLastError();
 }
 
-MuCoef mu_coef(const Phys &ph, const float *mu, const float *b) {
+MuCoef mu_coef(const Phys &ph, const float *mu, const float *b, const float4 *bco) {
   const Helm h = helm_of(ph);
   MuCoef m;
   m.mu = mu;
   m.b = b;
+  m.bco = bco;
   m.ax2 = (float)h.ax2;
   m.ay2 = (float)h.ay2;
   m.az2 = (float)h.az2;
@@ -411,9 +412,7 @@ cudaError_t launch_jacobi_c(int comp, const Geo &g, const Phys &ph, const double
 cudaError_t launch_jacobi_c(int comp, const Geo &g, const Phys &ph, const float *xo, const MuCoef &coef,
                             const double *pres, const double *X, float *x, int fuse, cudaStream_t st,
                             const SweepTiles &t) {
-  if (comp == 0) return jacobi_c<float, MuCoef, 0>(comp, g, ph, xo, coef, pres, X, x, fuse, t.jac, st);
-  if (comp == 1) return jacobi_c<float, MuCoef, 1>(comp, g, ph, xo, coef, pres, X, x, fuse, t.jac, st);
-  return jacobi_c<float, MuCoef, 2>(comp, g, ph, xo, coef, pres, X, x, fuse, t.jac, st);
+  return launch_sweep4(0, comp, g, helm_of(ph), xo, x, coef, pres, X, 0, 1, fuse, t.jac, st);
 }
 cudaError_t launch_sor_c(int comp, const Geo &g, const Phys &ph, double *x, const double *coef,
                          const double *pres, int flg, int iteration_time, int bc, int fuse, cudaStream_t st,
@@ -424,6 +423,8 @@ cudaError_t launch_sor_c(int comp, const Geo &g, const Phys &ph, double *x, cons
 cudaError_t launch_sor_c(int comp, const Geo &g, const Phys &ph, float *x, const MuCoef &coef,
                          const double *pres, const double *X, int flg, int iteration_time, int bc, int fuse,
                          cudaStream_t st, const SweepTiles &t) {
+  if (iteration_time % 2 == 0)  // checkerboard half-sweep: four x points per thread (k_sweep32.cu)
+    return launch_sweep4(1, comp, g, helm_of(ph), x, x, coef, pres, X, flg, bc, fuse, t.even, st);
   if (comp == 0)
     return sor_c<float, MuCoef, 0>(comp, g, ph, x, coef, pres, X, flg, iteration_time, bc, fuse, t.even, t.odd, st);
   if (comp == 1)

@@ -54,6 +54,7 @@ struct tpls_ctx {
   float *phi32, *u32, *v32, *w32, *mu32, *D32;
   float *ffh[2], *ffl[2];  // float-pair redistancing iterates (hi, lo), ping-pong
   float *bdef[3];  // FP32-mixed: defect b of the FP32 sweeps (one float per point)
+  float4 *bco32[3];  // FP32-mixed: boundary-row offsets of the FP32 sweeps per (j, k) row
   float *x3f[3][2];
   double *hbuf = nullptr; // interface height (nx*ny)
   double *stage = nullptr; // host-layout staging of one field ((nx+2)(ny+2)(nz+2))
@@ -418,6 +419,12 @@ static int create_impl(int nx, int ny, int nz, const tpls_params *prm, const dou
       c->allocs.push_back(b);
       TCK(cudaMemset(b, 0, n * sizeof(float)));
       c->bdef[q] = (float *)b;
+      void *o = nullptr;
+      const size_t no = (size_t)(ny + 2) * (nz + 1);
+      TCK(cudaMalloc(&o, no * sizeof(float4)));
+      c->allocs.push_back(o);
+      TCK(cudaMemset(o, 0, no * sizeof(float4)));
+      c->bco32[q] = (float4 *)o;
     }
     TCK(alloc_field(c, 1, ny + 4, nz + 2, &c->mu32));
   }
@@ -488,6 +495,7 @@ long long tpls_footprint_bytes(int nx, int ny, int nz, int precision) {
   } else {
     t += 6 * round_alloc(F * np) + 6 * round_alloc(F * nuv) + 3 * round_alloc(F * nw);
     t += 2 * round_alloc(F * (nrec / 8) * nz) + round_alloc(F * (nrec / 8) * (nz + 1)) + round_alloc(F * nmu);
+    t += 3 * round_alloc(4 * F * (size_t)(ny + 2) * (nz + 1));  // boundary-row offsets of the FP32 sweeps
     t += 2 * round_alloc(D * nuv) + round_alloc(D * nw);  // FP64 u3, v3, w3
     // FP64 CSF force, and the FP64 viscosity of TPLS_PART_MOM_STENCIL (the
     // setting served and batched jobs use; counted for every mixed context)
@@ -590,6 +598,7 @@ static int momentum(tpls_ctx *c, int comp, CS coef, T **X, int max_iteration, co
   const size_t n = (size_t)c->px * (c->ny + 2) * nzp + 8;
   if constexpr (sizeof(T) == sizeof(float)) {
     LCK(c, launch_defect_init(base - XOFF, X[0] - XOFF, n, c->st));
+    LCK(c, launch_bc32_prep(comp, g, c->ph, base, c->pres, c->bco32[comp], c->st));
   } else {
     TCK(cudaMemsetAsync(X[0] - XOFF, 0, sizeof(T) * n, c->st));
   }
@@ -804,11 +813,11 @@ static int step_once(tpls_ctx *c) {
 static int sweeps32(tpls_ctx *c) {
   int s;
   const Phys &ph = c->ph;
-  if ((s = momentum<float>(c, 0, mu_coef(ph, c->mu32, c->bdef[0]), c->x3f[0], c->prm.mom_u, c->u2, c->x3[0][0])))
+  if ((s = momentum<float>(c, 0, mu_coef(ph, c->mu32, c->bdef[0], c->bco32[0]), c->x3f[0], c->prm.mom_u, c->u2, c->x3[0][0])))
     return s;
-  if ((s = momentum<float>(c, 1, mu_coef(ph, c->mu32, c->bdef[1]), c->x3f[1], c->prm.mom_v, c->v2, c->x3[1][0])))
+  if ((s = momentum<float>(c, 1, mu_coef(ph, c->mu32, c->bdef[1], c->bco32[1]), c->x3f[1], c->prm.mom_v, c->v2, c->x3[1][0])))
     return s;
-  if ((s = momentum<float>(c, 2, mu_coef(ph, c->mu32, c->bdef[2]), c->x3f[2], c->prm.mom_w, c->w2, c->x3[2][0])))
+  if ((s = momentum<float>(c, 2, mu_coef(ph, c->mu32, c->bdef[2], c->bco32[2]), c->x3f[2], c->prm.mom_w, c->w2, c->x3[2][0])))
     return s;
   for (int q = 0; q < 3; q++) c->x3_final[q] = 0;
   return TPLS_OK;
@@ -1092,7 +1101,7 @@ int tpls_autotune(tpls_ctx *c, int reps) {
     // kind 0: Jacobi, 1: even half-sweep, 2: odd half-sweep (component u)
     if (f32) {
       float *a = c->x3f[0][0], *b = c->x3f[0][1];
-      const MuCoef mc = mu_coef(c->ph, c->mu32, c->bdef[0]);
+      const MuCoef mc = mu_coef(c->ph, c->mu32, c->bdef[0], c->bco32[0]);
       if (kind == 0) return launch_jacobi_c(0, g, c->ph, a, mc, c->pres, c->u2, b, fuse, c->st, t);
       return launch_sor_c(0, g, c->ph, b, mc, c->pres, c->u2, 0, kind == 1 ? 2 : 1, 1, fuse, c->st, t);
     }
@@ -1401,6 +1410,20 @@ int tpls_get_stats(tpls_ctx *c, tpls_stats *out) {
   c->stats.liquid_volume = c->scal_host[SC_VOL] * c->prm.dx * c->prm.dy * c->prm.dz;
   *out = c->stats;
   c->stats.p_worst = 0;
+  return TPLS_OK;
+}
+
+int tpls_get_dims(const tpls_ctx *c, int *nx, int *ny, int *nz) {
+  if (!c || !nx || !ny || !nz) return TPLS_ERR_ARG;
+  *nx = c->nx;
+  *ny = c->ny;
+  *nz = c->nz;
+  return TPLS_OK;
+}
+
+int tpls_set_steps_done(tpls_ctx *c, long steps_done) {
+  if (!c || steps_done < 0) return TPLS_ERR_ARG;
+  c->stats.steps_done = steps_done;
   return TPLS_OK;
 }
 

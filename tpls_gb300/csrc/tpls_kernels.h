@@ -167,8 +167,19 @@ struct MuCoef {
   const float *mu;     // viscosity on the p-grid with two periodic ghost rows
   const float *b;      // per-point b, rec_slot order
   float ax2, ay2, az2;  // dt/(2 d^2) per axis
+  // per (j, k) row (index j + (ny+2) k): the boundary-row offsets of the
+  // defect iterate, constant during one momentum solve (launch_bc32_prep):
+  // x = inlet copy offset, y = outlet offset, z = u's fictitious-point value
+  const float4 *bco;
 };
-MuCoef mu_coef(const Phys &ph, const float *mu, const float *b);
+MuCoef mu_coef(const Phys &ph, const float *mu, const float *b, const float4 *bco = nullptr);
+// The boundary-row offsets of the FP32 defect sweeps of component comp for
+// the base state X (u2, v2 or w2) and pressure P: inlet d(0) = d(1) +
+// (X(1) - X(0)); outlet u: d(nx) = d(nx-1) + (X(nx-1) - X(nx)) + dt/dx
+// ((P+ - P0) - (P0 - P-)) and d(nx+1) = -X(nx+1); outlet v, w: d(nx+1) =
+// d(nx) + (X(nx) - X(nx+1)).  Differences taken from FP32 pairs.
+cudaError_t launch_bc32_prep(int comp, const Geo &g, const Phys &ph, const double *X, const double *P,
+                             float4 *bco, cudaStream_t st);
 cudaError_t launch_jacobi_c(int comp, const Geo &g, const Phys &ph,
                             const float *xo, const MuCoef &coef,
                             const double *pres, const double *X, float *x,

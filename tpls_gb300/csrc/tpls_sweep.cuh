@@ -182,6 +182,12 @@ __device__ __forceinline__ void sor_bc(int comp, const Geo &g, const Helm &h, T 
   }
 }
 
+// FP32 Jacobi (mode 0) and checkerboard half-sweep (mode 1) with four x
+// points per thread (k_sweep32.cu); tile = rows per block choice.
+cudaError_t launch_sweep4(int mode, int comp, const Geo &g, const Helm &h, const float *xo, float *x,
+                          const MuCoef &s, const double *P, const double *X, int flg, int bc, int fuse, int tile,
+                          cudaStream_t st);
+
 static inline Helm helm_of(const Phys &ph) {
   Helm h;
   h.ax2 = (ph.dt / (ph.dx * ph.dx)) / 2.0;
