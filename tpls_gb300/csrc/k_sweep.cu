@@ -304,6 +304,104 @@ __global__ void __launch_bounds__(SO3_W * 32)
   }
 }
 
+// The same half-sweep in super-chunks of SOC_SC levels with a carried
+// value, so shared memory stays bounded for any column length (36 KB for
+// FP64) and several blocks share an SM.  Per super-chunk:
+//   1. produce: A and B of every (level, column) pair, a warp per level and
+//      a lane per column, all pairs independent (their loads overlap);
+//   2. scan: warp w runs the recurrence over its SOC_SC/SOC_W levels from a
+//      zero start, keeping y(k) and P(k) = prod B in place of A and B;
+//   3. each warp folds the chunk ends below it and the carried value into
+//      x_in and writes x = y + P x_in with the boundary rows; the last
+//      level's x is carried into the next super-chunk.
+// The chunk boundaries differ from k_sor_odd_c3's, and so does the
+// rounding (a few ulp, the level-by-level order being the oracle's).
+constexpr int SOC_W = 8, SOC_SC = 64;
+
+template <typename T, typename CS, int CC>
+__global__ void __launch_bounds__(SOC_W * 32)
+    k_sor_odd_c4(int comp_, Geo g, Helm h, T *__restrict__ x, const CS coef,
+                 const double *__restrict__ P, const double *__restrict__ X, int flg, int bc, int fuse) {
+  const int comp = (CC >= 0) ? CC : comp_;
+  __shared__ T sA[SOC_SC][32], sB[SOC_SC][32];
+  __shared__ T ey[SOC_W][32], ep[SOC_W][32], scarry[32];
+  const int j = blockIdx.y + 1;
+  const int iend = (comp == 0) ? g.nx - 1 : g.nx;
+  const int npair = (iend + 1) / 2;
+  const int par = (j + flg) & 1;
+  const int k0 = (comp == 2) ? 1 : 0, k1 = g.nz - 1;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int i2 = blockIdx.x * 32 + lane, i = 2 * i2 + 1 + par;
+  const bool act = (i2 < npair) && (i <= iend);
+  const int sy_ = g.sy, sz = g.sz, nz = g.nz;
+  constexpr int PER = SOC_SC / SOC_W;
+  T carry = 0;  // x of the level below the super-chunk (k0 has B = 0)
+  for (int kc = k0; kc <= k1; kc += SOC_SC) {
+    const int n = min(SOC_SC, k1 - kc + 1);
+    // 1. produce
+#pragma unroll 4
+    for (int r = 0; r < PER; r++) {
+      const int lk = w + r * SOC_W, k = kc + lk;
+      if (lk < n) {
+        T A = 0, B = 0;
+        if (act) {
+          const int c = TPLS_IDX(g, i, j, k);
+          const Rec<T> q = get_rec(comp, g, coef, c, i, j, k, true);
+          const T xc = x[c];
+          T zp;
+          if (comp == 2) zp = x[c + sz];
+          else zp = (k == nz - 1) ? xc : x[c + sz];
+          T part = fma(q.xp, x[c + 1], q.b);
+          part = fma(q.xm, x[c - 1], part);
+          part = fma(q.yp, x[c + sy_], part);
+          part = fma(q.ym, x[c - sy_], part);
+          part = fma(q.zp, zp, part);
+          if (k == k0) {  // the point below is a wall value (w) or the point itself (u, v)
+            const T zm = (comp == 2) ? x[c - sz] : xc;
+            A = xc + (T)1.2 * (fma(q.zm, zm, part) - xc);
+          } else {
+            A = xc + (T)1.2 * (part - xc);
+            B = (T)1.2 * q.zm;
+          }
+        }
+        sA[lk][lane] = A;
+        sB[lk][lane] = B;
+      }
+    }
+    __syncthreads();
+    // 2. scan of this warp's levels
+    const int lb = w * PER, le = min(n, lb + PER);
+    T yv = 0, pv = 1;
+    for (int lk = lb; lk < le; lk++) {
+      const T B = sB[lk][lane];
+      yv = fma(B, yv, sA[lk][lane]);
+      pv = B * pv;
+      sA[lk][lane] = yv;
+      sB[lk][lane] = pv;
+    }
+    ey[w][lane] = yv;  // an empty chunk passes x_in through (y 0, P 1)
+    ep[w][lane] = pv;
+    __syncthreads();
+    // 3. fold and write
+    T xin = carry;
+    for (int v = 0; v < w; v++) xin = fma(ep[v][lane], xin, ey[v][lane]);
+    if (i2 < npair) {
+      for (int lk = lb; lk < le; lk++) {
+        const int k = kc + lk;
+        T v = 0;
+        if (i <= iend) {
+          v = fma(sB[lk][lane], xin, sA[lk][lane]);
+          put(g, x, i, j, k, v, fuse);
+        }
+        if (bc) sor_bc(comp, g, h, x, X, P, i2, i, iend, v, j, k, fuse);
+        if (lk == n - 1) scarry[lane] = v;
+      }
+    }
+    __syncthreads();
+    carry = scarry[lane];
+  }
+}
+
 template <typename T>
 static size_t so3_smem(const Geo &g, int comp, int w) {
   const int nlev = g.nz - (comp == 2 ? 1 : 0);
@@ -379,9 +477,14 @@ static cudaError_t sor_c(int comp, const Geo &g, const Phys &ph, T *x, CS coef, 
     }
   } else {
     dim3 grd((npairs + 31) / 32, g.ny, 1);
-    // chunks per column: tile_odd 1 = 8 warps, 2 = 16 warps; 0 = by column
-    // length (16 once each warp gets >= 8 levels)
-    const int w = (tile_odd == 1) ? 8 : ((tile_odd == 2) ? 16 : ((g.nz >= 128) ? 16 : 8));
+    // tile_odd 0: super-chunked column scan (bounded shared memory); 1, 2:
+    // whole-column scan with 8 or 16 chunks (its shared memory grows with
+    // nz; the one-warp recurrence beyond SO3_SMEM_MAX)
+    if (tile_odd == 0) {
+      k_sor_odd_c4<T, CS, CC><<<grd, SOC_W * 32, 0, st>>>(comp, g, h, x, coef, pres, X, flg, bc, fuse);
+      return cudaGetLastError();
+    }
+    const int w = (tile_odd == 1) ? 8 : 16;
     const size_t sm = so3_smem<T>(g, comp, w);
     if (sm <= SO3_SMEM_MAX && w == 16)
       k_sor_odd_c3<T, CS, CC, 16><<<grd, 16 * 32, sm, st>>>(comp, g, h, x, coef, pres, X, flg, bc, fuse);
