@@ -425,7 +425,38 @@ def run_batch(args, ws, rank, local) -> dict | None:
         g = open_instance(inst, precision, tune=True)  # sweep tile shapes per grid (cached per shape)
         hosts.append(g.get_state())
         members.append(g)
-    b = Batch(members)
+    # the other launch form of the same members, timed first for comparison
+    # (graph branches per member vs multi-instance sweep launches)
+    def timed(multi: bool, mem, st0, steps):
+        for m, h in zip(mem, st0):
+            m.set_state(h)
+        bb = Batch(mem, multi_sweeps=multi)
+        if bb.step(args.warmup) != 0:
+            raise SystemExit("batch warm-up failed")
+        torch.cuda.synchronize()
+        ta = time.perf_counter()
+        if bb.step(steps) != 0:
+            raise SystemExit("batch step failed")
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - ta
+        bb.close()
+        return dt
+    other = timed(not args.multi_sweeps, members, hosts, args.steps)
+    small = None
+    if args.small_instances > 0:  # many small grids, where per-launch overhead dominates
+        sm_insts = draw_instances(args.small_instances, max_dims=(64, 32, 32))
+        sm_mem = [open_instance(i, precision, tune=True) for i in sm_insts]
+        sm_st = [g.get_state() for g in sm_mem]
+        sm_cells = sum(i.cells for i in sm_insts)
+        t_br, t_mu = timed(False, sm_mem, sm_st, args.steps), timed(True, sm_mem, sm_st, args.steps)
+        small = {"instances": len(sm_insts), "grid": [64, 32, 32], "steps": args.steps,
+                 "branches_cell_steps_per_s": sm_cells * args.steps / t_br,
+                 "multi_sweeps_cell_steps_per_s": sm_cells * args.steps / t_mu}
+        for g in sm_mem:
+            g.close()
+    for m, h in zip(members, hosts):
+        m.set_state(h)
+    b = Batch(members, multi_sweeps=args.multi_sweeps)
     if b.step(args.warmup) != 0:
         raise SystemExit("batch warm-up failed")
     ext = torch.cuda.ExternalStream(members[0].stream_ptr())
@@ -484,7 +515,9 @@ def run_batch(args, ws, rank, local) -> dict | None:
                                f"{'fp64' if precision == 0 else 'fp32-mixed'}",
                    "instances": len(insts), "total_cells": cells,
                    "grids": [[i.nx, i.ny, i.nz] for i in insts],
-                   "launch": "one CUDA graph per batch step (every member's step as a branch)",
+                   "launch": "one CUDA graph per batch step: every member's step as a branch" +
+                             ("; the FP32 momentum sweeps as one multi-instance launch per sweep over all "
+                              "members' tiles (atomic ticket)" if args.multi_sweeps else ""),
                    "timing": "host wall clock around synchronised batch steps",
                    "l2": f"working set ~{cells * 300 / 1e9:.0f} GB per step >> 129 MB L2",
                    "headline_metric": HEADLINE_METRIC},
@@ -493,6 +526,9 @@ def run_batch(args, ws, rank, local) -> dict | None:
                 "h2d_bytes_per_step": bi / args.steps, "d2h_bytes_per_step": bi / args.steps,
                 "path": "tpls_set_field x20 per member -> tpls_batch_step(steps) -> tpls_get_field x20 per member"},
         "gpu_launches": launches,
+        "other_launch_form": {"form": "branches" if args.multi_sweeps else "multi_sweeps",
+                              "cell_steps_per_s": ws * cells * args.steps / other},
+        "small_grids": small,
         "one_by_one": None if solo is None else {
             "seconds": solo["seconds"], "value": cells * args.steps / solo["seconds"],
             "batched_speedup": solo["seconds"] / sec},
@@ -516,11 +552,14 @@ def run_serve(args, ws, rank, local) -> dict | None:
         return None
     forms = {}
     clocks = None
+    njobs = {"fp32_mixed": args.jobs, "fp64": args.jobs_fp64 if args.jobs_fp64 is not None else args.jobs}
     for name, prec in (("fp32_mixed", 1), ("fp64", 0)):
-        jobs = draw_jobs(2000, rate=args.rate, precision=prec)[:args.jobs]
+        if njobs[name] <= 0:
+            continue
+        jobs = draw_jobs(2000, rate=args.rate, precision=prec)[:njobs[name]]
         sampler = ClockSampler(local)
         srv = Server(GpuBackend(), budget_bytes=160e9, max_active=64)
-        res = srv.run(jobs)
+        res = srv.run(jobs, time_scale=args.time_scale)
         c = sampler.stop()
         clocks = clocks or c
         sm = summarize(res)
@@ -541,8 +580,9 @@ def run_serve(args, ws, rank, local) -> dict | None:
         "vs_baseline": None,
         "dtype": "fp32-mixed (fp64 form alongside)",
         "data": "synthetic: seeded Poisson job stream, no dataset",
-        "config": {"workload": f"E: first {args.jobs} jobs of the seeded 2000-job stream, Poisson arrivals at "
-                               f"{args.rate} jobs/s, grids up to 384x192x192, budgets 50-1000 steps, 160 GB "
+        "config": {"workload": f"E: first {args.jobs} jobs (FP32-mixed; {njobs['fp64']} in FP64) of the seeded "
+                               f"2000-job stream, Poisson arrivals at {args.rate} jobs/s scaled by "
+                               f"{args.time_scale}, grids up to 384x192x192, budgets 50-1000 steps, 160 GB "
                                f"admission, snapshots every 50 steps",
                    "timing": "host wall clock from the first arrival to the last completion",
                    "headline_metric": HEADLINE_METRIC},
@@ -640,16 +680,24 @@ def main():
     ap.add_argument("--precision", choices=["fp64", "mixed"], default=None,
                     help="default: fp64 for A/B/M, mixed for C/D")
     ap.add_argument("--phase-steps", type=int, default=20)
-    ap.add_argument("--fp64-parts", type=int, default=16,
-                    help="FP32-mixed form: TPLS_PART_* bits kept in FP64 (default 16: momentum stencils, "
-                         "the setting that holds phi/u within 1e-5 of the FP64 form)")
+    ap.add_argument("--fp64-parts", type=int, default=2,
+                    help="FP32-mixed form: TPLS_PART_* bits kept in FP64 (default 2: the redistancing "
+                         "iterations, the setting that holds phi/u within 1e-7 of the FP64 form over 500 "
+                         "steps)")
     ap.add_argument("--ref-seconds", type=float, default=120.0)
     ap.add_argument("--instances", type=int, default=48)
+    ap.add_argument("--multi-sweeps", action="store_true",
+                    help="batched workload: the FP32 momentum sweeps as multi-instance launches")
+    ap.add_argument("--small-instances", type=int, default=0,
+                    help="batched workload: also time this many 64x32x32 instances in both launch forms")
     ap.add_argument("--no-one-by-one", action="store_true")
     ap.add_argument("--grid", type=int, nargs=3, default=None, metavar=("NX", "NY", "NZ"),
                     help="resize the workload (small cases for profiling captures)")
-    ap.add_argument("--jobs", type=int, default=16)
+    ap.add_argument("--jobs", type=int, default=16, help="served stream: jobs in the FP32-mixed run")
+    ap.add_argument("--jobs-fp64", type=int, default=None, help="served stream: jobs in the FP64 run (default --jobs)")
     ap.add_argument("--rate", type=float, default=1.0)
+    ap.add_argument("--time-scale", type=float, default=1.0,
+                    help="served stream: arrival times multiplied by this factor")
     ap.add_argument("--autotune", action="store_true", help="run the sweep-tile autotuner before timing")
     ap.add_argument("--idm", choices=["lsm", "dim"], default="lsm",
                     help="interface method: level set (default) or diffuse interface (FP64 form)")

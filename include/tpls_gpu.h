@@ -166,9 +166,9 @@ int tpls_get_tiles(const tpls_ctx *ctx, int *tiles3);
 /* Device bytes tpls_gpu_create allocates for this grid and precision (each
  * allocation rounded to the allocator's 2 MiB unit), or -1 for bad
  * arguments.  Host-only: used for admission before anything is allocated.
- * For TPLS_PREC_FP32_MIXED it counts the FP64 stencil inputs of
- * TPLS_PART_MOM_STENCIL (an upper bound when that part is off); keeping
- * TPLS_PART_MOMENTUM or TPLS_PART_LEVELSET in FP64 allocates more. */
+ * For TPLS_PREC_FP32_MIXED it counts the FP64 arrays of TPLS_PART_LEVELSET
+ * and TPLS_PART_MOM_STENCIL (an upper bound when those parts are off);
+ * keeping TPLS_PART_MOMENTUM in FP64 allocates more. */
 long long tpls_footprint_bytes(int nx, int ny, int nz, int precision);
 /* 1 when every step enqueued on the context has finished, 0 while work is
  * pending, or an error status.  Does not block. */
@@ -197,6 +197,16 @@ int tpls_batch_step_async(tpls_batch *b, int nsteps);
 /* The same, then wait; returns the lowest pressure reason of any member
  * (0 when every solve converged) or an error. */
 int tpls_batch_step(tpls_batch *b, int nsteps);
+/* on = 1: run the members' FP32 momentum sweeps (every Jacobi sweep and
+ * half-sweep of the three components) as multi-instance launches: one
+ * persistent launch per sweep for all members, blocks taking the members'
+ * tiles in order from an atomic ticket, instead of one launch per member.
+ * The rest of each member's step stays a parallel branch of the batch
+ * graph.  Results are bit-identical to on = 0.  Requires every member to be
+ * in the FP32-mixed form with FP32 sweeps (TPLS_PART_MOMENTUM not kept in
+ * FP64), an even ny, and the same mom_u, mom_v, mom_w; TPLS_ERR_ARG
+ * otherwise.  on = 0 returns to one branch per member. */
+int tpls_batch_multi_sweeps(tpls_batch *b, int on);
 
 /* Graph mode on (1, default) or off (0: every step launched kernel by
  * kernel, the pressure iterations driven by the host).  Both give

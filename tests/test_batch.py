@@ -41,6 +41,49 @@ def test_batch_members_match_solo_runs(precision):
 
 
 @pytest.mark.gpu
+def test_multi_instance_sweeps_match_solo_runs():
+    """The batch with its members' FP32 momentum sweeps as multi-instance
+    launches (one persistent launch per sweep over every member's tiles):
+    each member ends bit-identical to the same channel stepped alone, on
+    uneven grids (nx = 33 leaves ragged four-point groups)."""
+    insts = [Instance(0, 64, 32, 32, 2.0, 1.0, 100.0, 0.05, 11), Instance(1, 33, 18, 40, 7.5, 3.0, 300.0, 0.08, 12),
+             Instance(2, 96, 32, 16, 1.3, 5.0, 60.0, 0.02, 13), Instance(3, 128, 64, 48, 4.0, 2.0, 200.0, 0.06, 14)]
+    solo = []
+    for inst in insts:
+        g = open_instance(inst, 1)
+        assert g.step(5) == 0
+        solo.append(g.get_state())
+        g.close()
+    members = [open_instance(i, 1) for i in insts]
+    b = Batch(members, multi_sweeps=True)
+    assert b.step(2) == 0
+    b.step_async(3)
+    assert b.step(0) == 0
+    for g, ref in zip(members, solo):
+        st = g.get_state()
+        for k in STATE_FIELDS:
+            assert np.array_equal(st[k], ref[k]), k
+    b.close()
+    for g in members:
+        g.close()
+
+
+@pytest.mark.gpu
+def test_multi_instance_sweeps_refuse_ineligible_members():
+    """FP64 members, or an odd ny (whose ghost rows need separate exchanges),
+    are refused with TPLS_ERR_ARG; the batch then steps as before."""
+    from tpls_gb300.api import TplsError
+    a = open_instance(_instances()[0], 0)
+    with pytest.raises(TplsError):
+        Batch([a], multi_sweeps=True)
+    c = open_instance(_instances()[1], 1)  # ny = 19
+    with pytest.raises(TplsError):
+        Batch([c], multi_sweeps=True)
+    a.close()
+    c.close()
+
+
+@pytest.mark.gpu
 def test_batch_rejects_misaligned_members():
     insts = _instances()[:2]
     a, c = open_instance(insts[0], 1), open_instance(insts[1], 1)

@@ -98,13 +98,14 @@ def test_mixed_with_every_part_fp64_equals_fp64_form():
     mix.close()
 
 
-@pytest.mark.parametrize("parts", [0, 16, 18])
+@pytest.mark.parametrize("parts", [0, 2, 16, 18])
 def test_mixed_hundred_steps_fp32_and_fp64_stencils(parts):
     """100 steps with the momentum stencils in FP32 (parts 0: velocity
     values split into exact FP32 pairs, the sweeps' coefficients recomputed
     from the FP32 viscosity) and in FP64 (parts 16): phi and u stay within
     1e-5 of the FP64 form, v and w within 1e-4, the liquid volume within
-    1e-8.  Parts 18 also keeps redistancing in FP64."""
+    1e-8.  Parts 2 keeps the redistancing iterations in FP64 (the default
+    setting), parts 18 both."""
     ref = _ctx(0)
     mix = _ctx(1, fp64_parts=parts)
     assert ref.step(100) == 0 and mix.step(100) == 0

@@ -66,6 +66,55 @@ def test_mock_server_budget_limits_concurrency():
     assert all(r.admitted >= fin[0] - 1e-9 for r in res[2:])
 
 
+def test_mock_server_fails_a_diverged_job_at_once_and_frees_its_slot():
+    """A job whose pressure solve reports DIVERGED_NAN (injected on the host
+    from step 100) is failed at the first chunk that shows it, closed, and
+    its slot goes to the queue; every other job runs to its budget."""
+    clk = FakeClock()
+    jobs = [JobSpec(q, 64, 32, 32, 2.0, 1.0, 100.0, 0.05, 400, 1, 0.01 * q, 7 + q) for q in range(4)]
+    be = MockBackend(clk, rate=1e8, bytes_per_cell=100.0, fail_at={1: 100})
+    fp = be.footprint(jobs[0])
+    srv = Server(be, budget_bytes=2 * fp + 1, max_active=16, clock=clk, sleep=clk.sleep, idle_sleep=1e-3)
+    res = srv.run(jobs)
+    bad = res[1]
+    assert bad.failed and bad.worst_reason == -9 and bad.steps_done == 100
+    assert [s.step for s in bad.snapshots] == [50]  # no snapshot of the diverged state
+    for r in res[:1] + res[2:]:
+        assert not r.failed and r.steps_done == 400
+    # job 2 arrived while 0 and 1 ran: it got job 1's slot before job 0 finished
+    assert res[2].admitted < res[0].finished
+    assert sorted(be.closed) == [0, 1, 2, 3]
+    assert summarize(res)["failed_jobs"] == 1
+
+
+def test_mock_server_creates_and_destroys_contexts_off_the_issue_thread():
+    """Context creation and teardown run on the server's worker thread; the
+    steps are issued from the scheduler's thread."""
+    import threading
+    clk = FakeClock()
+    seen = {"open": set(), "close": set(), "enqueue": set()}
+
+    class Recording(MockBackend):
+        def open(self, spec):
+            seen["open"].add(threading.current_thread().name)
+            return super().open(spec)
+
+        def close(self, h):
+            seen["close"].add(threading.current_thread().name)
+            return super().close(h)
+
+        def enqueue(self, h, n):
+            seen["enqueue"].add(threading.current_thread().name)
+            return super().enqueue(h, n)
+
+    res = Server(Recording(clk, rate=5e8), budget_bytes=2e9, max_active=4, clock=clk, sleep=clk.sleep,
+                 idle_sleep=1e-3).run(_jobs(6))
+    assert all(r.steps_done == r.spec.steps for r in res)
+    main = threading.current_thread().name
+    assert seen["enqueue"] == {main}
+    assert main not in seen["open"] and main not in seen["close"]
+
+
 def test_mock_server_rejects_job_over_budget():
     clk = FakeClock()
     be = MockBackend(clk)

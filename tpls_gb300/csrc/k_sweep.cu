@@ -318,20 +318,23 @@ __global__ void __launch_bounds__(SO3_W * 32)
 // rounding (a few ulp, the level-by-level order being the oracle's).
 constexpr int SOC_W = 8, SOC_SC = 64;
 
+// One tile: 32 columns (x pairs from bx*32) of row j = by+1.  Every thread
+// of the block runs it (it synchronises the block).
 template <typename T, typename CS, int CC>
-__global__ void __launch_bounds__(SOC_W * 32)
-    k_sor_odd_c4(int comp_, Geo g, Helm h, T *__restrict__ x, const CS coef,
-                 const double *__restrict__ P, const double *__restrict__ X, int flg, int bc, int fuse) {
+__device__ __forceinline__ void sor_odd_c4_tile(int comp_, const Geo &g, const Helm &h, T *__restrict__ x,
+                                                const CS &coef, const double *__restrict__ P,
+                                                const double *__restrict__ X, int flg, int bc, int fuse, int bx,
+                                                int by) {
   const int comp = (CC >= 0) ? CC : comp_;
   __shared__ T sA[SOC_SC][32], sB[SOC_SC][32];
   __shared__ T ey[SOC_W][32], ep[SOC_W][32], scarry[32];
-  const int j = blockIdx.y + 1;
+  const int j = by + 1;
   const int iend = (comp == 0) ? g.nx - 1 : g.nx;
   const int npair = (iend + 1) / 2;
   const int par = (j + flg) & 1;
   const int k0 = (comp == 2) ? 1 : 0, k1 = g.nz - 1;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int i2 = blockIdx.x * 32 + lane, i = 2 * i2 + 1 + par;
+  const int i2 = bx * 32 + lane, i = 2 * i2 + 1 + par;
   const bool act = (i2 < npair) && (i <= iend);
   const int sy_ = g.sy, sz = g.sz, nz = g.nz;
   constexpr int PER = SOC_SC / SOC_W;
@@ -400,6 +403,61 @@ __global__ void __launch_bounds__(SOC_W * 32)
     __syncthreads();
     carry = scarry[lane];
   }
+}
+
+template <typename T, typename CS, int CC>
+__global__ void __launch_bounds__(SOC_W * 32)
+    k_sor_odd_c4(int comp_, Geo g, Helm h, T *__restrict__ x, const CS coef,
+                 const double *__restrict__ P, const double *__restrict__ X, int flg, int bc, int fuse) {
+  sor_odd_c4_tile<T, CS, CC>(comp_, g, h, x, coef, P, X, flg, bc, fuse, blockIdx.x, blockIdx.y);
+}
+
+// Multi-instance odd half-sweep of the FP32 sweeps of a batch: the tiles of
+// every member (32 columns of one row each) taken in order by an atomic
+// ticket, as k_sweep4_multi.
+template <int CC>
+__global__ void __launch_bounds__(SOC_W * 32)
+    k_odd_multi(const SweepMember *__restrict__ mem, const int *__restrict__ prefix, int n, int src, int flg,
+                int bc, unsigned *ctr) {
+  __shared__ int s_t;
+  const int total = prefix[n];
+  for (;;) {
+    if (threadIdx.x == 0) s_t = (int)atomicAdd(&ctr[0], 1u);
+    __syncthreads();
+    const int t = s_t;
+    __syncthreads();
+    if (t >= total) break;
+    int m = 0;
+    while (prefix[m + 1] <= t) m++;
+    const SweepMember &M = mem[m];
+    const int iend = (CC == 0) ? M.g.nx - 1 : M.g.nx;
+    const int gx = ((iend + 1) / 2 + 31) / 32;
+    const int lt = t - prefix[m];
+    sor_odd_c4_tile<float, MuCoef, CC>(CC, M.g, M.h, M.x[CC][src], M.s[CC], M.P, M.X[CC], flg, bc, M.fuse,
+                                       lt % gx, lt / gx);
+  }
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(&ctr[1], 1u) == gridDim.x - 1) {
+      ctr[0] = 0u;
+      ctr[1] = 0u;
+    }
+  }
+}
+
+int odd_tiles(int comp, const Geo &g) {
+  const int iend = (comp == 0) ? g.nx - 1 : g.nx;
+  return (((iend + 1) / 2 + 31) / 32) * g.ny;
+}
+
+cudaError_t launch_odd_multi(int comp, const SweepMember *mem, const int *prefix, int n, int total_tiles, int src,
+                             int flg, int bc, unsigned *ctr, int nblocks, cudaStream_t st) {
+  const int nb = total_tiles < nblocks ? total_tiles : nblocks;
+  if (nb <= 0) return cudaSuccess;
+  if (comp == 0) k_odd_multi<0><<<nb, SOC_W * 32, 0, st>>>(mem, prefix, n, src, flg, bc, ctr);
+  else if (comp == 1) k_odd_multi<1><<<nb, SOC_W * 32, 0, st>>>(mem, prefix, n, src, flg, bc, ctr);
+  else k_odd_multi<2><<<nb, SOC_W * 32, 0, st>>>(mem, prefix, n, src, flg, bc, ctr);
+  return cudaGetLastError();
 }
 
 template <typename T>

@@ -185,15 +185,18 @@ __device__ __forceinline__ void load_b(const Geo &g, const float *__restrict__ b
   }
 }
 
+// One tile (block (bx, by, bz) of the single-instance grid) of the sweep;
+// the single-instance kernel runs one per block, the multi-instance kernel
+// of a batch any tile of any member.
 template <int CC, int MODE, int BY>
-__global__ void __launch_bounds__(32 * BY)
-    k_sweep4(Geo g, Helm h, const float *__restrict__ xo, float *x, MuCoef s, const double *__restrict__ X,
-             int flg, int bc, int fuse) {
-  const int lane = threadIdx.x, q = blockIdx.x * 32 + lane;
-  const int j = blockIdx.y * BY + threadIdx.y + 1;
+__device__ __forceinline__ void sweep4_tile(const Geo &g, const Helm &h, const float *__restrict__ xo, float *x,
+                                            const MuCoef &s, const double *__restrict__ X, int flg, int bc,
+                                            int fuse, int bx, int by, int bz) {
+  const int lane = threadIdx.x, q = bx * 32 + lane;
+  const int j = by * BY + threadIdx.y + 1;
   if (j > g.ny) return;  // uniform per warp
   const int nx = g.nx, nz = g.nz, sy = g.sy, sz = g.sz;
-  const int k = blockIdx.z + ((CC == 2) ? 1 : 0);
+  const int k = bz + ((CC == 2) ? 1 : 0);
   const int iend = (CC == 0) ? nx - 1 : nx;
   const int G = (iend + 3) >> 2;
   const bool act = q < G;
@@ -294,6 +297,59 @@ __global__ void __launch_bounds__(32 * BY)
 }
 
 template <int CC, int MODE, int BY>
+__global__ void __launch_bounds__(32 * BY)
+    k_sweep4(Geo g, Helm h, const float *__restrict__ xo, float *x, MuCoef s, const double *__restrict__ X,
+             int flg, int bc, int fuse) {
+  sweep4_tile<CC, MODE, BY>(g, h, xo, x, s, X, flg, bc, fuse, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+// tiles of the single-instance grid of component CC (4 rows per block)
+__host__ __device__ inline void sweep4_grid(int cc, const Geo &g, int *gx, int *gy, int *gz) {
+  const int iend = (cc == 0) ? g.nx - 1 : g.nx;
+  *gx = ((iend + 3) / 4 + 31) / 32;
+  *gy = (g.ny + 3) / 4;
+  *gz = (cc == 2) ? g.nz - 1 : g.nz;
+}
+
+// Multi-instance form: one persistent launch runs the sweep of component CC
+// for every member of a batch.  The work is the list of all members' tiles
+// (prefix[m] = first tile of member m); blocks take tiles in order by an
+// atomic ticket, so uneven members share the GPU without one launch each.
+// No block waits for another; the last block to leave resets the ticket
+// for the next launch.
+template <int CC, int MODE>
+__global__ void __launch_bounds__(128)
+    k_sweep4_multi(const SweepMember *__restrict__ mem, const int *__restrict__ prefix, int n, int src, int flg,
+                   int bc, unsigned *ctr) {
+  __shared__ int s_t;
+  const int total = prefix[n];
+  for (;;) {
+    if (threadIdx.x == 0 && threadIdx.y == 0) s_t = (int)atomicAdd(&ctr[0], 1u);
+    __syncthreads();
+    const int t = s_t;
+    __syncthreads();
+    if (t >= total) break;
+    int m = 0;
+    while (prefix[m + 1] <= t) m++;
+    const SweepMember &M = mem[m];
+    int gx, gy, gz;
+    sweep4_grid(CC, M.g, &gx, &gy, &gz);
+    const int lt = t - prefix[m];
+    const int bx = lt % gx, by = (lt / gx) % gy, bz = lt / (gx * gy);
+    const float *xo = M.x[CC][src];
+    float *xd = (MODE == M_JAC) ? M.x[CC][1 - src] : M.x[CC][src];
+    sweep4_tile<CC, MODE, 4>(M.g, M.h, xo, xd, M.s[CC], M.X[CC], flg, bc, M.fuse, bx, by, bz);
+  }
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    __threadfence();
+    if (atomicAdd(&ctr[1], 1u) == gridDim.x - 1) {
+      ctr[0] = 0u;
+      ctr[1] = 0u;
+    }
+  }
+}
+
+template <int CC, int MODE, int BY>
 cudaError_t launch4(const Geo &g, const Helm &h, const float *xo, float *x, const MuCoef &s, const double *X,
                     int flg, int bc, int fuse, cudaStream_t st) {
   const int iend = (CC == 0) ? g.nx - 1 : g.nx;
@@ -350,6 +406,32 @@ cudaError_t launch_sweep4(int mode, int comp, const Geo &g, const Helm &h, const
                           cudaStream_t st) {
   if (mode == M_JAC) return by_comp<M_JAC>(comp, tile, g, h, xo, x, s, X, flg, bc, fuse, st);
   return by_comp<M_EVEN>(comp, tile, g, h, xo, x, s, X, flg, bc, fuse, st);
+}
+
+int sweep4_tiles(int comp, const Geo &g) {
+  int gx, gy, gz;
+  sweep4_grid(comp, g, &gx, &gy, &gz);
+  return gx * gy * gz;
+}
+
+cudaError_t launch_sweep4_multi(int mode, int comp, const SweepMember *mem, const int *prefix, int n,
+                                int total_tiles, int src, int flg, int bc, unsigned *ctr, int nblocks,
+                                cudaStream_t st) {
+  const int nb = total_tiles < nblocks ? total_tiles : nblocks;
+  if (nb <= 0) return cudaSuccess;
+  const dim3 blk(32, 4);
+#define TPLS_M4(C, M) k_sweep4_multi<C, M><<<nb, blk, 0, st>>>(mem, prefix, n, src, flg, bc, ctr)
+  if (mode == M_JAC) {
+    if (comp == 0) TPLS_M4(0, M_JAC);
+    else if (comp == 1) TPLS_M4(1, M_JAC);
+    else TPLS_M4(2, M_JAC);
+  } else {
+    if (comp == 0) TPLS_M4(0, M_EVEN);
+    else if (comp == 1) TPLS_M4(1, M_EVEN);
+    else TPLS_M4(2, M_EVEN);
+  }
+#undef TPLS_M4
+  return cudaGetLastError();
 }
 
 cudaError_t launch_bc32_prep(int comp, const Geo &g, const Phys &ph, const double *X, const double *P,

@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "tpls_pressure.h"
+#include "tpls_sweep.cuh"
 
 using namespace tpls;
 
@@ -497,9 +498,10 @@ long long tpls_footprint_bytes(int nx, int ny, int nz, int precision) {
     t += 2 * round_alloc(F * (nrec / 8) * nz) + round_alloc(F * (nrec / 8) * (nz + 1)) + round_alloc(F * nmu);
     t += 3 * round_alloc(4 * F * (size_t)(ny + 2) * (nz + 1));  // boundary-row offsets of the FP32 sweeps
     t += 2 * round_alloc(D * nuv) + round_alloc(D * nw);  // FP64 u3, v3, w3
-    // FP64 CSF force, and the FP64 viscosity of TPLS_PART_MOM_STENCIL (the
-    // setting served and batched jobs use; counted for every mixed context)
-    t += 3 * round_alloc(D * np) + round_alloc(D * nmu);
+    // FP64 CSF force, the FP64 iterate pair and distance of
+    // TPLS_PART_LEVELSET (the setting served and batched jobs use) and the
+    // FP64 viscosity of TPLS_PART_MOM_STENCIL, counted for every mixed context
+    t += 3 * round_alloc(D * np) + 2 * round_alloc(D * np) + round_alloc(D * nmu);
   }
   t += round_alloc(px * (ny + 2) * (nz + 2) + 64) + round_alloc(D * nz) + round_alloc(D * nx * ny);
   t += round_alloc(D * (size_t)(nx + 2) * (ny + 2) * (nz + 2));  // host-layout staging
@@ -585,6 +587,38 @@ long tpls_kernel_launches(tpls_ctx *c) {
 }
 
 extern "C++" {
+// Begin and end of one component's FP32 defect-form momentum solve: d = -X
+// and the boundary-row offsets before the sweeps; x = X + d into the FP64
+// u3 / v3 / w3 and the logged get_difference of the last two iterates after
+// them.  Shared by momentum<float> and the multi-instance sweeps of a batch.
+static const double *mom32_base(tpls_ctx *c, int comp) { return comp == 0 ? c->u2 : (comp == 1 ? c->v2 : c->w2); }
+static size_t mom32_len(tpls_ctx *c, int comp) {
+  return (size_t)c->px * (c->ny + 2) * nz_planes(comp == 2 ? 2 : 1, c->nz) + 8;
+}
+static int mom32_iters(tpls_ctx *c, int comp) {
+  return (comp == 0 ? c->prm.mom_u : (comp == 1 ? c->prm.mom_v : c->prm.mom_w)) / 2;
+}
+static int mom32_begin(tpls_ctx *c, int comp) {
+  const double *base = mom32_base(c, comp);
+  LCK(c, launch_defect_init(base - XOFF, c->x3f[comp][0] - XOFF, mom32_len(c, comp), c->st));
+  LCK(c, launch_bc32_prep(comp, c->g, c->ph, base, c->pres, c->bco32[comp], c->st));
+  return TPLS_OK;
+}
+static int mom32_end(tpls_ctx *c, int comp, int N) {
+  float **X = c->x3f[comp];
+  const int nzp = nz_planes(comp == 2 ? 2 : 1, c->nz);
+  LCK(c, launch_defect_apply(mom32_base(c, comp) - XOFF, X[N % 2] - XOFF, c->x3[comp][0] - XOFF,
+                             mom32_len(c, comp), c->st));
+  if (N >= 1) {
+    LCK(c, launch_diff2(c->g, X[N % 2], X[(N - 1) % 2], nzp, c->part, c->st));
+    FSUM(c, c->part, diff2_blocks(c->g, nzp), c->scal + SC_ERR_U + comp, c->st);
+  } else {
+    TCK(cudaMemsetAsync(c->scal + SC_ERR_U + comp, 0, sizeof(double), c->st));
+  }
+  c->x3_final[comp] = 0;
+  return TPLS_OK;
+}
+
 // One velocity component's Crank-Nicolson solve (main_ns_hybrid.F90:756-887)
 // on the iterate pair X: FP64, or in the FP32-mixed form the FP32 defect
 // d = x - base (base = the component's FP64 state), iterated from d = -base
@@ -597,8 +631,8 @@ static int momentum(tpls_ctx *c, int comp, CS coef, T **X, int max_iteration, co
   const int fuse = (g.ny % 2 == 0);
   const size_t n = (size_t)c->px * (c->ny + 2) * nzp + 8;
   if constexpr (sizeof(T) == sizeof(float)) {
-    LCK(c, launch_defect_init(base - XOFF, X[0] - XOFF, n, c->st));
-    LCK(c, launch_bc32_prep(comp, g, c->ph, base, c->pres, c->bco32[comp], c->st));
+    int s = mom32_begin(c, comp);
+    if (s) return s;
   } else {
     TCK(cudaMemsetAsync(X[0] - XOFF, 0, sizeof(T) * n, c->st));
   }
@@ -632,10 +666,10 @@ static int momentum(tpls_ctx *c, int comp, CS coef, T **X, int max_iteration, co
     }
     if (!fuse) LCK(c, launch_exchange(g, dst, nzp, c->st));
   }
-  c->x3_final[comp] = N % 2;
   if constexpr (sizeof(T) == sizeof(float)) {
-    LCK(c, launch_defect_apply(base - XOFF, X[N % 2] - XOFF, out64 - XOFF, n, c->st));
+    return mom32_end(c, comp, N);
   }
+  c->x3_final[comp] = N % 2;
   const int nb = diff2_blocks(g, nzp);
   if (N >= 1) {
     LCK(c, launch_diff2(g, X[N % 2], X[(N - 1) % 2], nzp, c->part, c->st));
@@ -823,7 +857,14 @@ static int sweeps32(tpls_ctx *c) {
   return TPLS_OK;
 }
 
-static int step_once_mixed(tpls_ctx *c) {
+// The FP32-mixed step in three stages: the front (viscosity, advection,
+// level set, CSF and the momentum right-hand sides, and the FP64 sweeps when
+// the momentum part is kept in FP64), the FP32 momentum solves (sweeps32, or
+// the multi-instance launches of a batch) and the back (pressure solve and
+// projection).
+static bool mixed_fp32_sweeps(const tpls_ctx *c) { return !(c->prm.fp64_parts & TPLS_PART_MOMENTUM); }
+
+static int mixed_front(tpls_ctx *c) {
   const Geo &g = c->g;
   const Phys &ph = c->ph;
   cudaStream_t st = c->st;
@@ -877,8 +918,6 @@ static int step_once_mixed(tpls_ctx *c) {
     if (L > 0) FSUM(c, c->part, ls_iter_blocks(g), c->scal + SC_ERR_PHI, st);
   }
   int s;
-  const void *u3v;
-  const void *v3v, *w3v;
   if (mom64) {
     {
       PhaseScope ps(c, TPLS_T_CSF);
@@ -899,9 +938,6 @@ static int step_once_mixed(tpls_ctx *c) {
     if ((s = momentum<double, const double *>(c, 0, c->coef[0], c->x3[0], c->prm.mom_u))) return s;
     if ((s = momentum<double, const double *>(c, 1, c->coef[1], c->x3[1], c->prm.mom_v))) return s;
     if ((s = momentum<double, const double *>(c, 2, c->coef[2], c->x3[2], c->prm.mom_w))) return s;
-    u3v = c->x3[0][c->x3_final[0]];
-    v3v = c->x3[1][c->x3_final[1]];
-    w3v = c->x3[2][c->x3_final[2]];
   } else if (sten64) {
     {
       PhaseScope ps(c, TPLS_T_CSF);
@@ -916,10 +952,6 @@ static int step_once_mixed(tpls_ctx *c) {
       LCK(c, launch_mom_rhs64r32(2, g, ph, c->u2, c->v2, c->w2, c->mu, c->fz, c->conv_w[s1], c->conv_w[s0],
                                  c->csf_w[s1], c->csf_w[s0], c->conv_w[s2], c->csf_w[s2], c->bdef[2], st));
     }
-    if ((s = sweeps32(c))) return s;
-    u3v = c->x3[0][0];
-    v3v = c->x3[1][0];
-    w3v = c->x3[2][0];
   } else {
     {
       PhaseScope ps(c, TPLS_T_CSF);
@@ -934,11 +966,16 @@ static int step_once_mixed(tpls_ctx *c) {
       LCK(c, launch_mom_rhs_pair(2, g, ph, c->u2, c->v2, c->w2, c->mu32, c->fz, c->conv_w[s1], c->conv_w[s0],
                                  c->csf_w[s1], c->csf_w[s0], c->conv_w[s2], c->csf_w[s2], c->bdef[2], st));
     }
-    if ((s = sweeps32(c))) return s;
-    u3v = c->x3[0][0];
-    v3v = c->x3[1][0];
-    w3v = c->x3[2][0];
   }
+  return TPLS_OK;
+}
+
+static int mixed_back(tpls_ctx *c) {
+  const Geo &g = c->g;
+  const Phys &ph = c->ph;
+  cudaStream_t st = c->st;
+  const void *u3v = c->x3[0][c->x3_final[0]], *v3v = c->x3[1][c->x3_final[1]], *w3v = c->x3[2][c->x3_final[2]];
+  int s;
   int its = 0, reason = 0;
   double rn = 0.0, bn = 0.0;
   {
@@ -955,6 +992,13 @@ static int step_once_mixed(tpls_ctx *c) {
   }
   if (c->capturing) return TPLS_OK;
   return finish_eager(c, its, rn, bn, reason);
+}
+
+static int step_once_mixed(tpls_ctx *c) {
+  int s = mixed_front(c);
+  if (s) return s;
+  if (mixed_fp32_sweeps(c) && (s = sweeps32(c))) return s;
+  return mixed_back(c);
 }
 
 // One step as a CUDA-graph launch; the graph of this history phase is
@@ -1177,11 +1221,21 @@ int tpls_graphs_enable(tpls_ctx *c, int on) {
 struct tpls_batch {
   std::vector<tpls_ctx *> m;
   cudaStream_t st = nullptr;
-  cudaEvent_t fork = nullptr, done = nullptr;
+  cudaEvent_t fork = nullptr, fork2 = nullptr, done = nullptr;
   std::vector<cudaEvent_t> join;
   cudaGraphExec_t gexec[3] = {nullptr, nullptr, nullptr};
   std::vector<long> n_static[3];  // kernels per member outside the CG loop
   std::vector<int> tune_seen;     // members' tune_version when the graphs were captured
+  // multi-instance FP32 momentum sweeps: device member descriptors, tile
+  // prefixes per (kind, component) (kind 0: Jacobi / checkerboard grid,
+  // 1: odd half-sweep grid), the ticket counters, and the launches per step
+  int multi = 0;
+  SweepMember *dmem = nullptr;
+  int *dprefix = nullptr;
+  int total[2][3] = {{0, 0, 0}, {0, 0, 0}};
+  unsigned *dctr = nullptr;
+  int nblocks = 0;
+  long n_multi = 0;
 };
 
 extern "C" {
@@ -1193,6 +1247,10 @@ int tpls_batch_destroy(tpls_batch *b) {
     if (ge) cudaGraphExecDestroy(ge);
   for (cudaEvent_t e : b->join) cudaEventDestroy(e);
   if (b->fork) cudaEventDestroy(b->fork);
+  if (b->fork2) cudaEventDestroy(b->fork2);
+  if (b->dmem) cudaFree(b->dmem);
+  if (b->dprefix) cudaFree(b->dprefix);
+  if (b->dctr) cudaFree(b->dctr);
   if (b->done) cudaEventDestroy(b->done);
   if (b->st) cudaStreamDestroy(b->st);
   delete b;
@@ -1211,6 +1269,7 @@ int tpls_batch_create(tpls_ctx *const *ctxs, int n, tpls_batch **out) {
   b->m.assign(ctxs, ctxs + n);
   cudaError_t e = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork2, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
   b->join.assign(n, nullptr);
   for (int q = 0; q < n && e == cudaSuccess; q++) e = cudaEventCreateWithFlags(&b->join[q], cudaEventDisableTiming);
@@ -1222,10 +1281,35 @@ int tpls_batch_create(tpls_ctx *const *ctxs, int n, tpls_batch **out) {
   return TPLS_OK;
 }
 
+// The momentum sweeps of every member as multi-instance launches on the
+// batch stream (main_ns_hybrid.F90:756-887 per component: Jacobi, then the
+// two half-sweeps, mom/2 times), in each member's own launch order.
+static int batch_multi_sweeps(tpls_batch *b) {
+  const int n = (int)b->m.size();
+  for (int comp = 0; comp < 3; comp++) {
+    const int N = mom32_iters(b->m[0], comp);
+    const int *pf0 = b->dprefix + (0 * 3 + comp) * (n + 1), *pf1 = b->dprefix + (1 * 3 + comp) * (n + 1);
+    for (int it = 1; it <= N; it++) {
+      const int src = (it - 1) % 2, dst = it % 2;
+      TCK(launch_sweep4_multi(0, comp, b->dmem, pf0, n, b->total[0][comp], src, 0, 1, b->dctr, b->nblocks, b->st));
+      for (int flg = 0; flg < 2; flg++) {
+        if (it % 2 == 0)
+          TCK(launch_sweep4_multi(1, comp, b->dmem, pf0, n, b->total[0][comp], dst, flg, flg, b->dctr, b->nblocks,
+                                  b->st));
+        else
+          TCK(launch_odd_multi(comp, b->dmem, pf1, n, b->total[1][comp], dst, flg, flg, b->dctr, b->nblocks, b->st));
+      }
+      b->n_multi += 3;
+    }
+  }
+  return TPLS_OK;
+}
+
 static int batch_capture(tpls_batch *b, int ph) {
   const int n = (int)b->m.size();
   std::vector<long> l0(n);
   for (int q = 0; q < n; q++) l0[q] = b->m[q]->launches;
+  b->n_multi = 0;
   TCK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
   int s = TPLS_OK;
   cudaError_t e = cudaEventRecord(b->fork, b->st);
@@ -1234,10 +1318,30 @@ static int batch_capture(tpls_batch *b, int ph) {
     e = cudaStreamWaitEvent(c->st, b->fork, 0);
     if (e != cudaSuccess) break;
     c->capturing = true;
-    s = c->mixed ? step_once_mixed(c) : step_once(c);
+    if (b->multi) {  // front stage and the start of the FP32 momentum solves
+      s = mixed_front(c);
+      for (int comp = 0; comp < 3 && s == TPLS_OK; comp++) s = mom32_begin(c, comp);
+    } else {
+      s = c->mixed ? step_once_mixed(c) : step_once(c);
+    }
     c->capturing = false;
     if (s == TPLS_OK) e = cudaEventRecord(b->join[q], c->st);
     if (s == TPLS_OK && e == cudaSuccess) e = cudaStreamWaitEvent(b->st, b->join[q], 0);
+  }
+  if (b->multi && s == TPLS_OK && e == cudaSuccess) {
+    s = batch_multi_sweeps(b);
+    if (s == TPLS_OK) e = cudaEventRecord(b->fork2, b->st);
+    for (int q = 0; q < n && s == TPLS_OK && e == cudaSuccess; q++) {
+      tpls_ctx *c = b->m[q];
+      e = cudaStreamWaitEvent(c->st, b->fork2, 0);
+      if (e != cudaSuccess) break;
+      c->capturing = true;
+      for (int comp = 0; comp < 3 && s == TPLS_OK; comp++) s = mom32_end(c, comp, mom32_iters(c, comp));
+      if (s == TPLS_OK) s = mixed_back(c);
+      c->capturing = false;
+      if (s == TPLS_OK) e = cudaEventRecord(b->join[q], c->st);
+      if (s == TPLS_OK && e == cudaSuccess) e = cudaStreamWaitEvent(b->st, b->join[q], 0);
+    }
   }
   cudaGraph_t gr = nullptr;
   const cudaError_t ee = cudaStreamEndCapture(b->st, &gr);
@@ -1254,6 +1358,63 @@ static int batch_capture(tpls_batch *b, int ph) {
   const cudaError_t ei = cudaGraphInstantiate(&b->gexec[ph], gr, 0);
   cudaGraphDestroy(gr);
   TCK(ei);
+  return TPLS_OK;
+}
+
+int tpls_batch_multi_sweeps(tpls_batch *b, int on) {
+  if (!b || (on != 0 && on != 1)) return TPLS_ERR_ARG;
+  const int n = (int)b->m.size();
+  if (on) {
+    int dev0 = -1;
+    for (tpls_ctx *c : b->m) {
+      if (!c->mixed || !mixed_fp32_sweeps(c) || c->ny % 2 != 0) return TPLS_ERR_ARG;
+      for (int comp = 0; comp < 3; comp++)
+        if (mom32_iters(c, comp) != mom32_iters(b->m[0], comp)) return TPLS_ERR_ARG;
+    }
+    TCK(cudaGetDevice(&dev0));
+    if (!b->dmem) {
+      std::vector<SweepMember> hm(n);
+      std::vector<int> pre(6 * (n + 1), 0);
+      for (int q = 0; q < n; q++) {
+        tpls_ctx *c = b->m[q];
+        SweepMember &M = hm[q];
+        M.g = c->g;
+        M.h = helm_of(c->ph);
+        for (int comp = 0; comp < 3; comp++) {
+          M.s[comp] = mu_coef(c->ph, c->mu32, c->bdef[comp], c->bco32[comp]);
+          M.x[comp][0] = c->x3f[comp][0];
+          M.x[comp][1] = c->x3f[comp][1];
+          M.X[comp] = mom32_base(c, comp);
+        }
+        M.P = c->pres;
+        M.fuse = 1;
+      }
+      for (int kind = 0; kind < 2; kind++)
+        for (int comp = 0; comp < 3; comp++) {
+          int *pf = pre.data() + (kind * 3 + comp) * (n + 1);
+          for (int q = 0; q < n; q++)
+            pf[q + 1] = pf[q] + (kind == 0 ? sweep4_tiles(comp, b->m[q]->g) : odd_tiles(comp, b->m[q]->g));
+          b->total[kind][comp] = pf[n];
+        }
+      TCK(cudaMalloc(&b->dmem, sizeof(SweepMember) * n));
+      TCK(cudaMalloc(&b->dprefix, sizeof(int) * pre.size()));
+      TCK(cudaMalloc(&b->dctr, 2 * sizeof(unsigned)));
+      TCK(cudaMemcpy(b->dmem, hm.data(), sizeof(SweepMember) * n, cudaMemcpyHostToDevice));
+      TCK(cudaMemcpy(b->dprefix, pre.data(), sizeof(int) * pre.size(), cudaMemcpyHostToDevice));
+      TCK(cudaMemset(b->dctr, 0, 2 * sizeof(unsigned)));
+      int sms = 0;
+      TCK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev0));
+      b->nblocks = 8 * sms;
+    }
+  }
+  if (b->multi != on) {
+    b->multi = on;
+    for (cudaGraphExec_t &ge : b->gexec)
+      if (ge) {
+        cudaGraphExecDestroy(ge);
+        ge = nullptr;
+      }
+  }
   return TPLS_OK;
 }
 
@@ -1291,7 +1452,8 @@ int tpls_batch_step_async(tpls_batch *b, int nsteps) {
     for (int q = 0; q < n; q++) {
       tpls_ctx *c = b->m[q];
       TCK(cudaStreamWaitEvent(c->st, b->done, 0));  // later work on a member follows the batch step
-      c->launches += b->n_static[ph][q];
+      // (the multi-instance sweep launches of a step are counted with member 0)
+      c->launches += b->n_static[ph][q] + (q == 0 ? b->n_multi : 0);
       c->phase = (ph + 1) % 3;
       c->stats.steps_done++;
       c->graph_pending = true;

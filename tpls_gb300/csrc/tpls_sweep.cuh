@@ -182,6 +182,34 @@ __device__ __forceinline__ void sor_bc(int comp, const Geo &g, const Helm &h, T 
   }
 }
 
+// One batch member's arguments of the FP32 sweeps, for the multi-instance
+// launches of a batch (device array, one entry per member).
+struct SweepMember {
+  Geo g;
+  Helm h;
+  MuCoef s[3];          // per component: viscosity, b, scales, boundary offsets
+  float *x[3][2];       // per component: the defect iterate pair
+  const double *X[3];   // per component: the FP64 base state (u2, v2, w2)
+  const double *P;      // pressure (u outlet)
+  int fuse;             // periodic ghost rows written by the sweeps (even ny)
+};
+// Tiles of the single-instance FP32 Jacobi / checkerboard grid (4 rows per
+// block) and of the odd half-sweep grid of component comp.
+int sweep4_tiles(int comp, const Geo &g);
+int odd_tiles(int comp, const Geo &g);
+// One launch of the FP32 Jacobi (mode 0) or checkerboard (mode 1) sweep of
+// component comp over all n members: prefix[m] = first tile of member m,
+// prefix[n] = total_tiles (device array); Jacobi reads x[comp][src] and
+// writes x[comp][1-src], the half-sweep relaxes x[comp][src]; ctr = two
+// zeroed unsigned counters (left zero by the launch); nblocks = persistent
+// blocks.
+cudaError_t launch_sweep4_multi(int mode, int comp, const SweepMember *mem, const int *prefix, int n,
+                                int total_tiles, int src, int flg, int bc, unsigned *ctr, int nblocks,
+                                cudaStream_t st);
+// The odd half-sweep (2-D colouring) of component comp over all members.
+cudaError_t launch_odd_multi(int comp, const SweepMember *mem, const int *prefix, int n, int total_tiles,
+                             int src, int flg, int bc, unsigned *ctr, int nblocks, cudaStream_t st);
+
 // FP32 Jacobi (mode 0) and checkerboard half-sweep (mode 1) with four x
 // points per thread (k_sweep32.cu); tile = rows per block choice.
 cudaError_t launch_sweep4(int mode, int comp, const Geo &g, const Helm &h, const float *xo, float *x,
