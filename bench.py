@@ -258,10 +258,10 @@ def run_gpu(args, ws, rank, local) -> dict | None:
     esz = 4 if precision == 1 and not (parts & 4) else 8  # FP32 sweeps unless momentum is kept in FP64
     jac_b, sor_b, jac_n, sor_n = _algorithmic_bytes(nx, ny, nz, params.mom_u, esz)
     # dominant kernel of the step: the odd-iteration red-black half-sweep
-    # (k_sor_odd_c3), its launches timed with CUDA events on the library's
+    # (k_sor_odd_c4), its launches timed with CUDA events on the library's
     # stream in the phase pass
     sor_ms, sor_l = phases["sor_odd"]
-    dominant = "k_sor_odd_c3"
+    dominant = "k_sor_odd_c4"
     per_launch_b = sor_b / sor_n
     avg_ms = sor_ms / max(sor_l, 1)
     achieved = per_launch_b / (avg_ms / 1e3) / 1e9

@@ -135,6 +135,25 @@ int tpls_set_field(tpls_ctx *ctx, int field, const double *host);
 int tpls_get_field(tpls_ctx *ctx, int field, double *host);
 /* Grid of the context. */
 int tpls_get_dims(const tpls_ctx *ctx, int *nx, int *ny, int *nz);
+/* Several fields per call (no counterpart in the reference, which keeps its
+ * arrays on the host): fields[i] to / from host[i], in the layouts of
+ * tpls_set_field / tpls_get_field, without a host wait between fields.
+ * The copies run on the context's own copy streams through a ring of four
+ * staging buffers (three allocated on the first call), so successive
+ * fields overlap, and an upload of an array still being downloaded waits
+ * for that download on the device: a get of the state followed by a set
+ * of the same arrays runs both copy directions at once.  Both calls return
+ * once the copies are enqueued: steps enqueued afterwards run after the
+ * uploads; the host arrays of a get may be read after tpls_sync (or
+ * tpls_xfer_join and a wait on the context's stream).  Pinned host memory
+ * gives the link's full speed. */
+int tpls_set_fields(tpls_ctx *ctx, int n, const int *fields,
+                    const double *const *host);
+int tpls_get_fields(tpls_ctx *ctx, int n, const int *fields,
+                    double *const *host);
+/* Make later work on the context's stream (tpls_stream) wait for every
+ * download enqueued so far. */
+int tpls_xfer_join(tpls_ctx *ctx);
 /* Step counter reported in tpls_stats.steps_done, for a restarted run that
  * continues an earlier one's count (the driver's `iteration`). */
 int tpls_set_steps_done(tpls_ctx *ctx, long steps_done);
@@ -213,6 +232,7 @@ int tpls_batch_multi_sweeps(tpls_batch *b, int on);
  * bit-identical results. */
 int tpls_graphs_enable(tpls_ctx *ctx, int on);
 int tpls_get_stats(tpls_ctx *ctx, tpls_stats *out);
+/* Waits for the context's stream and its copy streams. */
 int tpls_sync(tpls_ctx *ctx);
 const char *tpls_status_string(int status);
 /* Number of kernels the library has launched on this context (counted on

@@ -21,6 +21,23 @@ constexpr int kMaxScratch = 8;
 
 }  // namespace
 
+// Batched host transfers: a ring of staging buffers (slot 0 is the
+// context's own staging buffer, the others are allocated on first use) and
+// one copy stream per direction.  A field's copy and its repack run on
+// different streams, ordered by events, so successive fields overlap and a
+// download followed by an upload of the same host arrays uses both copy
+// directions at once.
+struct Xfer {
+  static constexpr int K = 4;
+  cudaStream_t h2d = nullptr, d2h = nullptr;
+  double *slot[K] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t free_ev[K] = {nullptr, nullptr, nullptr, nullptr};  // the slot may be refilled
+  cudaEvent_t ready_ev[K] = {nullptr, nullptr, nullptr, nullptr};  // the slot holds its data
+  cudaEvent_t d2h_last = nullptr;  // the last download enqueued
+  int next = 0;
+  std::map<const void *, cudaEvent_t> host_done;  // last download into each host array
+};
+
 struct tpls_ctx {
   int nx, ny, nz;
   tpls_params prm;
@@ -59,6 +76,7 @@ struct tpls_ctx {
   float *x3f[3][2];
   double *hbuf = nullptr; // interface height (nx*ny)
   double *stage = nullptr; // host-layout staging of one field ((nx+2)(ny+2)(nz+2))
+  struct Xfer *xf = nullptr;  // batched host transfers (tpls_set_fields / tpls_get_fields)
   size_t n_p, n_uv, n_w;  // elements of each allocation (incl. pitch and padding)
   double *part, *scal, *scal_host;
   size_t part_len;
@@ -312,8 +330,25 @@ const char *tpls_status_string(int s) {
   return "unknown status";
 }
 
+static void xfer_destroy(Xfer *x) {
+  if (!x) return;
+  if (x->h2d) cudaStreamSynchronize(x->h2d);
+  if (x->d2h) cudaStreamSynchronize(x->d2h);
+  for (int q = 0; q < Xfer::K; q++) {
+    if (x->free_ev[q]) cudaEventDestroy(x->free_ev[q]);
+    if (x->ready_ev[q]) cudaEventDestroy(x->ready_ev[q]);
+  }
+  for (auto &kv : x->host_done) cudaEventDestroy(kv.second);
+  if (x->d2h_last) cudaEventDestroy(x->d2h_last);
+  if (x->h2d) cudaStreamDestroy(x->h2d);
+  if (x->d2h) cudaStreamDestroy(x->d2h);
+  delete x;
+}
+
 int tpls_gpu_destroy(tpls_ctx *c) {
   if (!c) return TPLS_OK;
+  xfer_destroy(c->xf);
+  c->xf = nullptr;
   if (c->st) cudaStreamSynchronize(c->st);
   timing_flush(c);
   for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
@@ -555,10 +590,20 @@ int tpls_gpu_create(int nx, int ny, int nz, const tpls_params *prm, const double
 }
 
 
+// Single-field transfers use slot 0 synchronously: wait for batched
+// transfers still using it.
+static cudaError_t xfer_quiesce(tpls_ctx *c) {
+  if (!c->xf) return cudaSuccess;
+  cudaError_t e = cudaStreamSynchronize(c->xf->h2d);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->xf->d2h);
+  return e;
+}
+
 int tpls_set_field(tpls_ctx *c, int f, const double *host) {
   if (!c || !host || f < 0 || f >= TPLS_F_COUNT) return TPLS_ERR_ARG;
   double *d = field_ptr(c, f);
   if (!d) return TPLS_ERR_ARG;
+  TCK(xfer_quiesce(c));
   TCK(h2d(c, d, host, nz_planes(field_kind(f), c->nz)));
   TCK(cudaStreamSynchronize(c->st));
   c->need_exchange = true;
@@ -569,13 +614,104 @@ int tpls_get_field(tpls_ctx *c, int f, double *host) {
   if (!c || !host || f < 0 || f >= TPLS_F_COUNT) return TPLS_ERR_ARG;
   double *d = field_ptr(c, f);
   if (!d) return TPLS_ERR_ARG;
+  TCK(xfer_quiesce(c));
   TCK(d2h(c, host, d, nz_planes(field_kind(f), c->nz)));
   TCK(cudaStreamSynchronize(c->st));
   return TPLS_OK;
 }
 
+static cudaError_t xfer_init(tpls_ctx *c) {
+  if (c->xf) return cudaSuccess;
+  Xfer *x = new Xfer();
+  cudaError_t e = cudaStreamCreateWithFlags(&x->h2d, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&x->d2h, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&x->d2h_last, cudaEventDisableTiming);
+  const size_t n = (size_t)(c->nx + 2) * (c->ny + 2) * (c->nz + 2);
+  x->slot[0] = c->stage;
+  for (int q = 1; q < Xfer::K && e == cudaSuccess; q++) {
+    void *b = nullptr;
+    e = cudaMalloc(&b, n * sizeof(double));
+    if (e == cudaSuccess) {
+      c->allocs.push_back(b);
+      x->slot[q] = (double *)b;
+    }
+  }
+  for (int q = 0; q < Xfer::K && e == cudaSuccess; q++) {
+    e = cudaEventCreateWithFlags(&x->free_ev[q], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&x->ready_ev[q], cudaEventDisableTiming);
+  }
+  if (e != cudaSuccess) {
+    xfer_destroy(x);
+    return e;
+  }
+  c->xf = x;
+  return cudaSuccess;
+}
+
+int tpls_set_fields(tpls_ctx *c, int n, const int *fields, const double *const *hosts) {
+  if (!c || n < 0 || (n > 0 && (!fields || !hosts))) return TPLS_ERR_ARG;
+  for (int i = 0; i < n; i++)
+    if (!hosts[i] || fields[i] < 0 || fields[i] >= TPLS_F_COUNT || !field_ptr(c, fields[i])) return TPLS_ERR_ARG;
+  TCK(xfer_init(c));
+  Xfer *x = c->xf;
+  for (int i = 0; i < n; i++) {
+    const int f = fields[i], nzp = nz_planes(field_kind(f), c->nz);
+    const int w = c->nx + 2, rows = (c->ny + 2) * nzp;
+    const int q = x->next;
+    x->next = (q + 1) % Xfer::K;
+    TCK(cudaStreamWaitEvent(x->h2d, x->free_ev[q], 0));
+    auto hd = x->host_done.find(hosts[i]);  // a download into this array still in flight
+    if (hd != x->host_done.end()) TCK(cudaStreamWaitEvent(x->h2d, hd->second, 0));
+    TCK(cudaMemcpyAsync(x->slot[q], hosts[i], sizeof(double) * (size_t)w * rows, cudaMemcpyHostToDevice, x->h2d));
+    TCK(cudaEventRecord(x->ready_ev[q], x->h2d));
+    TCK(cudaStreamWaitEvent(c->st, x->ready_ev[q], 0));
+    LCK(c, repack(x->slot[q], w, field_ptr(c, f), c->px, w, rows, c->st));
+    TCK(cudaEventRecord(x->free_ev[q], c->st));
+  }
+  if (n > 0) c->need_exchange = true;
+  return TPLS_OK;
+}
+
+int tpls_get_fields(tpls_ctx *c, int n, const int *fields, double *const *hosts) {
+  if (!c || n < 0 || (n > 0 && (!fields || !hosts))) return TPLS_ERR_ARG;
+  for (int i = 0; i < n; i++)
+    if (!hosts[i] || fields[i] < 0 || fields[i] >= TPLS_F_COUNT || !field_ptr(c, fields[i])) return TPLS_ERR_ARG;
+  TCK(xfer_init(c));
+  Xfer *x = c->xf;
+  if (x->host_done.size() > 256) {  // bounded bookkeeping: settle and forget
+    TCK(cudaStreamSynchronize(x->d2h));
+    for (auto &kv : x->host_done) cudaEventDestroy(kv.second);
+    x->host_done.clear();
+  }
+  for (int i = 0; i < n; i++) {
+    const int f = fields[i], nzp = nz_planes(field_kind(f), c->nz);
+    const int w = c->nx + 2, rows = (c->ny + 2) * nzp;
+    const int q = x->next;
+    x->next = (q + 1) % Xfer::K;
+    TCK(cudaStreamWaitEvent(c->st, x->free_ev[q], 0));
+    LCK(c, repack(field_ptr(c, f), c->px, x->slot[q], w, w, rows, c->st));
+    TCK(cudaEventRecord(x->ready_ev[q], c->st));
+    TCK(cudaStreamWaitEvent(x->d2h, x->ready_ev[q], 0));
+    TCK(cudaMemcpyAsync(hosts[i], x->slot[q], sizeof(double) * (size_t)w * rows, cudaMemcpyDeviceToHost, x->d2h));
+    TCK(cudaEventRecord(x->free_ev[q], x->d2h));
+    cudaEvent_t &ev = x->host_done[hosts[i]];
+    if (!ev) TCK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    TCK(cudaEventRecord(ev, x->d2h));
+  }
+  if (n > 0) TCK(cudaEventRecord(x->d2h_last, x->d2h));
+  return TPLS_OK;
+}
+
+int tpls_xfer_join(tpls_ctx *c) {
+  if (!c) return TPLS_ERR_ARG;
+  if (!c->xf) return TPLS_OK;
+  TCK(cudaStreamWaitEvent(c->st, c->xf->d2h_last, 0));
+  return TPLS_OK;
+}
+
 int tpls_sync(tpls_ctx *c) {
   if (!c) return TPLS_ERR_ARG;
+  TCK(xfer_quiesce(c));
   TCK(cudaStreamSynchronize(c->st));
   return TPLS_OK;
 }
