@@ -138,8 +138,8 @@ int tpls_get_dims(const tpls_ctx *ctx, int *nx, int *ny, int *nz);
 /* Several fields per call (no counterpart in the reference, which keeps its
  * arrays on the host): fields[i] to / from host[i], in the layouts of
  * tpls_set_field / tpls_get_field, without a host wait between fields.
- * The copies run on the context's own copy streams through a ring of four
- * staging buffers (three allocated on the first call), so successive
+ * The copies run on the context's own copy streams through two staging
+ * buffers per direction (three allocated on the first call), so successive
  * fields overlap, and an upload of an array still being downloaded waits
  * for that download on the device: a get of the state followed by a set
  * of the same arrays runs both copy directions at once.  Both calls return
@@ -178,7 +178,7 @@ int tpls_step_async(tpls_ctx *ctx, int nsteps);
  * rebuilt at the next step (batches included).  The state a run produces
  * does not depend on the choice (same arithmetic per point). */
 int tpls_autotune(tpls_ctx *ctx, int reps);
-/* tiles3 = {Jacobi shape 0..3, even shape 0..3, odd chunking 0..2} */
+/* tiles3 = {Jacobi shape 0..3, even shape 0..3, odd half-sweep shape (0)} */
 int tpls_get_tiles(const tpls_ctx *ctx, int *tiles3);
 
 /* ---- job-serving helpers (no counterpart in the reference) ------------ */

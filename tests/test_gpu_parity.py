@@ -306,9 +306,10 @@ def test_step_is_deterministic():
 
 # Edge sizes: the smallest grid the library accepts (nx=4, ny=3, nz=4: odd
 # ny, no multigrid coarsening in y), ragged odd sizes in every direction,
-# a one-row-pair spanwise extent, and a tall column (nz >> nx) that takes
-# the 16-chunk odd-SOR path.
-EDGE = {"min": (4, 3, 4), "ragged": (33, 17, 31), "flat": (40, 4, 12), "tall": (8, 6, 160)}
+# a one-row-pair spanwise extent, and tall columns (nz >> nx) whose odd
+# half-sweeps cross 3 and 7 super-chunks of 64 levels.
+EDGE = {"min": (4, 3, 4), "ragged": (33, 17, 31), "flat": (40, 4, 12), "tall": (8, 6, 160),
+        "taller": (8, 6, 400)}
 
 
 @pytest.mark.parametrize("size", list(EDGE))

@@ -79,3 +79,35 @@ def test_graph_mode_survives_field_upload():
     assert all(np.array_equal(a[k], b[k]) for k in STATE_FIELDS)
     g.close()
     h.close()
+
+
+def test_batched_transfers_match_single_field_path():
+    """tpls_set_fields / tpls_get_fields: a download of the whole state
+    followed, without a host wait, by an upload of the same arrays leaves
+    the state as it was (the upload waits for the download on the device);
+    a context loaded with set_fields steps bit-identically to one loaded
+    field by field; get_fields returns what get_field does."""
+    nx, ny, nz = 37, 19, 23
+    params, uin, st = make_case("A", nx=nx, ny=ny, nz=nz)
+    a = TplsGpu(nx, ny, nz, params, uin)
+    b = TplsGpu(nx, ny, nz, params, uin)
+    a.set_state(st)
+    a.step(2)
+    ref = a.get_state()
+    bufs = {k: np.zeros_like(v, order="F") for k, v in ref.items()}
+    for _ in range(3):  # round trips through the same host arrays
+        a.get_fields_into(bufs)
+        a.set_fields(bufs)
+    a.sync()
+    for k, v in a.get_state().items():
+        assert np.array_equal(v, ref[k]), k
+    b.set_fields(bufs)
+    assert a.step(2) == 0 and b.step(2) == 0
+    out = {k: np.zeros_like(v, order="F") for k, v in ref.items()}
+    b.get_fields_into(out)
+    b.sync()
+    sa = a.get_state()
+    for k in sa:
+        assert np.array_equal(out[k], sa[k]), k
+    a.close()
+    b.close()

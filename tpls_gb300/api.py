@@ -152,6 +152,9 @@ def load_library(path: Path | None = None) -> C.CDLL:
     lib.tpls_stream.argtypes = [C.c_void_p]
     lib.tpls_stream.restype = C.c_void_p
     lib.tpls_set_steps_done.argtypes = [C.c_void_p, C.c_long]
+    lib.tpls_set_fields.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(_DP)]
+    lib.tpls_get_fields.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(_DP)]
+    lib.tpls_xfer_join.argtypes = [C.c_void_p]
     lib.tpls_backup_channel.argtypes = [C.c_void_p, C.c_char_p, C.c_char_p]
     lib.tpls_dataload_channel.argtypes = [C.c_void_p, C.c_char_p, C.c_char_p]
     if path is None:
@@ -262,6 +265,35 @@ class TplsGpu:
             raise ValueError(f"{name}: shape {out.shape} != {self.shape(FIELD_KIND[name])}")
         self._check(self.lib.tpls_get_field(self.ctx, F[name], _ptr(out)))
         return out
+
+    def set_fields(self, arrays: dict) -> None:
+        """Upload several fields in one tpls_set_fields call (enqueued, no
+        host wait between fields; later steps run after the uploads).  The
+        arrays must stay alive and unchanged until the context is synced."""
+        names = list(arrays)
+        for k in names:
+            a = arrays[k]
+            if not (a.dtype == np.float64 and a.flags.f_contiguous) or a.shape != self.shape(FIELD_KIND[k]):
+                raise ValueError(f"{k}: needs a Fortran-ordered float64 array of shape {self.shape(FIELD_KIND[k])}")
+        ids = (C.c_int * len(names))(*[F[k] for k in names])
+        ptrs = (_DP * len(names))(*[_ptr(arrays[k]) for k in names])
+        self._check(self.lib.tpls_set_fields(self.ctx, len(names), ids, ptrs))
+
+    def get_fields_into(self, arrays: dict) -> None:
+        """Download several fields into existing Fortran-ordered arrays in one
+        tpls_get_fields call; the arrays hold the data after sync()."""
+        names = list(arrays)
+        for k in names:
+            a = arrays[k]
+            if not (a.dtype == np.float64 and a.flags.f_contiguous) or a.shape != self.shape(FIELD_KIND[k]):
+                raise ValueError(f"{k}: needs a Fortran-ordered float64 array of shape {self.shape(FIELD_KIND[k])}")
+        ids = (C.c_int * len(names))(*[F[k] for k in names])
+        ptrs = (_DP * len(names))(*[_ptr(arrays[k]) for k in names])
+        self._check(self.lib.tpls_get_fields(self.ctx, len(names), ids, ptrs))
+
+    def xfer_join(self) -> None:
+        """Later work on the context's stream waits for the downloads so far."""
+        self._check(self.lib.tpls_xfer_join(self.ctx))
 
     def set_state(self, state: dict) -> None:
         for k, v in state.items():

@@ -136,176 +136,15 @@ __global__ void __launch_bounds__(SW_X *SW_Y)
 // relaxed point below it in its own column, so the update is the recurrence
 //   x_new(k) = A(k) + B(k) x_new(k-1),
 //   A = x + 1.2 (partial - x),  B = 1.2 czm   (partial = all terms but czm),
-// with A and B known before the sweep.  A block owns 32 columns of one row
-// (one per x pair).  Warp 0 runs the recurrence of chunk c (SO_KZ levels)
-// while warps 1..7 compute A and B of chunk c+1 into the other half of a
-// double-buffered shared array, so the dependent FMA chain overlaps the
-// parallel work.  Coefficient records are streamed (evict-first) so the
-// x field stays resident in L2.
-constexpr int SO_KZ = 32, SO_T = 256;
-
-template <typename T, typename CS>
-__device__ __forceinline__ void sor_odd_produce(int comp, const Geo &g, const T *__restrict__ x,
-                                                const CS coef, int j, int par, int npair,
-                                                int iend, int k0, int kc, int kn, T (*sA)[32],
-                                                T (*sB)[32], int t0, int nthr) {
-  const int sy = g.sy, sz = g.sz, nz = g.nz;
-  for (int t = t0; t < kn * 32; t += nthr) {
-    const int lk = t >> 5, col = t & 31;
-    const int i2 = blockIdx.x * 32 + col, i = 2 * i2 + 1 + par, k = kc + lk;
-    T A = 0, B = 0;
-    if (i2 < npair && i <= iend) {
-      const int c = TPLS_IDX(g, i, j, k);
-      const Rec<T> q = get_rec(comp, g, coef, c, i, j, k, true);
-      const T xc = x[c];
-      T zp;
-      if (comp == 2) zp = x[c + sz];
-      else zp = (k == nz - 1) ? xc : x[c + sz];
-      T part = fma(q.xp, x[c + 1], q.b);
-      part = fma(q.xm, x[c - 1], part);
-      part = fma(q.yp, x[c + sy], part);
-      part = fma(q.ym, x[c - sy], part);
-      part = fma(q.zp, zp, part);
-      if (k == k0) {  // the point below is a wall value (w) or the point itself (u, v)
-        const T zm = (comp == 2) ? x[c - sz] : xc;
-        A = xc + (T)1.2 * (fma(q.zm, zm, part) - xc);
-      } else {
-        A = xc + (T)1.2 * (part - xc);
-        B = (T)1.2 * q.zm;
-      }
-    }
-    sA[lk][col] = A;
-    sB[lk][col] = B;
-  }
-}
-
-template <typename T, typename CS, int CC>
-__global__ void __launch_bounds__(SO_T)
-    k_sor_odd_c2(int comp_, Geo g, Helm h, T *__restrict__ x, const CS coef,
-                 const double *__restrict__ P, const double *__restrict__ X, int flg, int bc, int fuse) {
-  const int comp = (CC >= 0) ? CC : comp_;
-  __shared__ T sA[2][SO_KZ][32], sB[2][SO_KZ][32];
-  const int j = blockIdx.y + 1;
-  const int iend = (comp == 0) ? g.nx - 1 : g.nx;
-  const int npair = (iend + 1) / 2;
-  const int par = (j + flg) & 1;
-  const int k0 = (comp == 2) ? 1 : 0, k1 = g.nz - 1;
-  const int nch = (k1 - k0 + SO_KZ) / SO_KZ;
-  const int warp = threadIdx.x >> 5;
-  sor_odd_produce(comp, g, x, coef, j, par, npair, iend, k0, k0, min(SO_KZ, k1 - k0 + 1), sA[0], sB[0],
-                  (int)threadIdx.x, SO_T);
-  __syncthreads();
-  T prev = 0;  // owned by warp 0
-  for (int ch = 0; ch < nch; ch++) {
-    const int kc = k0 + ch * SO_KZ, kn = min(SO_KZ, k1 - kc + 1), buf = ch & 1;
-    if (warp == 0) {
-      const int col = threadIdx.x;
-      const int i2 = blockIdx.x * 32 + col, i = 2 * i2 + 1 + par;
-      if (i2 < npair) {
-        for (int lk = 0; lk < kn; lk++) {
-          const int k = kc + lk;
-          T v = 0;
-          if (i <= iend) {
-            v = fma(sB[buf][lk][col], prev, sA[buf][lk][col]);
-            put(g, x, i, j, k, v, fuse);
-            prev = v;
-          }
-          if (bc) sor_bc(comp, g, h, x, X, P, i2, i, iend, v, j, k, fuse);
-        }
-      }
-    } else if (ch + 1 < nch) {
-      const int kc2 = kc + SO_KZ;
-      sor_odd_produce(comp, g, x, coef, j, par, npair, iend, k0, kc2, min(SO_KZ, k1 - kc2 + 1), sA[buf ^ 1],
-                      sB[buf ^ 1], (int)threadIdx.x - 32, SO_T - 32);
-    }
-    __syncthreads();
-  }
-}
-
-// The same half-sweep with the column recurrence split across warps.  A
-// block holds 32 columns (lanes) and SO3_W chunks of consecutive levels
-// (warps):
-//   1. every warp runs the recurrence over its chunk from a zero start,
-//      keeping y(k), the chunk-local solution, and P(k), the product of the
-//      B factors since the chunk start, in shared memory;
-//   2. each warp folds the ends of the chunks below it into x_in, the value
-//      entering its chunk;
-//   3. x(k) = y(k) + P(k) x_in for the chunk, written with the boundary rows.
-// The dependent chain per column becomes nz/SO3_W levels plus SO3_W folds;
-// the result differs from the level-by-level order only by rounding (P
-// decays like (1.2 czm)^m, so x_in's contribution is weighted by it).
-// Shared memory: 2 (nlev + W) 32 values of T; W = 8 or 16 warps.
-template <typename T, typename CS, int CC, int SO3_W>
-__global__ void __launch_bounds__(SO3_W * 32)
-    k_sor_odd_c3(int comp_, Geo g, Helm h, T *__restrict__ x, const CS coef,
-                 const double *__restrict__ P, const double *__restrict__ X, int flg, int bc, int fuse) {
-  const int comp = (CC >= 0) ? CC : comp_;
-  extern __shared__ __align__(16) unsigned char so3_raw[];
-  const int j = blockIdx.y + 1;
-  const int iend = (comp == 0) ? g.nx - 1 : g.nx;
-  const int npair = (iend + 1) / 2;
-  const int par = (j + flg) & 1;
-  const int k0 = (comp == 2) ? 1 : 0, k1 = g.nz - 1;
-  const int nlev = k1 - k0 + 1;
-  T *sy = reinterpret_cast<T *>(so3_raw);  // [nlev][32]
-  T *sp = sy + (size_t)nlev * 32;          // [nlev][32]
-  T *ey = sp + (size_t)nlev * 32;          // [SO3_W][32]
-  T *ep = ey + SO3_W * 32;                 // [SO3_W][32]
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int i2 = blockIdx.x * 32 + lane, i = 2 * i2 + 1 + par;
-  const bool act = (i2 < npair) && (i <= iend);
-  const int per = (nlev + SO3_W - 1) / SO3_W;
-  const int kb = k0 + w * per, ke = min(k1 + 1, kb + per);
-  const int sy_ = g.sy, sz = g.sz, nz = g.nz;
-  T yv = 0, pv = 1;
-  if (act) {
-#pragma unroll 2
-    for (int k = kb; k < ke; k++) {
-      const int c = TPLS_IDX(g, i, j, k);
-      const Rec<T> q = get_rec(comp, g, coef, c, i, j, k, true);
-      const T xc = x[c];
-      T zp;
-      if (comp == 2) zp = x[c + sz];
-      else zp = (k == nz - 1) ? xc : x[c + sz];
-      T part = fma(q.xp, x[c + 1], q.b);
-      part = fma(q.xm, x[c - 1], part);
-      part = fma(q.yp, x[c + sy_], part);
-      part = fma(q.ym, x[c - sy_], part);
-      part = fma(q.zp, zp, part);
-      T A, B;
-      if (k == k0) {  // the point below is a wall value (w) or the point itself (u, v)
-        const T zm = (comp == 2) ? x[c - sz] : xc;
-        A = xc + (T)1.2 * (fma(q.zm, zm, part) - xc);
-        B = 0;
-      } else {
-        A = xc + (T)1.2 * (part - xc);
-        B = (T)1.2 * q.zm;
-      }
-      yv = fma(B, yv, A);
-      pv = B * pv;
-      sy[(k - k0) * 32 + lane] = yv;
-      sp[(k - k0) * 32 + lane] = pv;
-    }
-  }
-  ey[w * 32 + lane] = yv;  // an empty chunk passes x_in through (y 0, P 1)
-  ep[w * 32 + lane] = pv;
-  __syncthreads();
-  T xin = 0;
-  for (int v = 0; v < w; v++) xin = fma(ep[v * 32 + lane], xin, ey[v * 32 + lane]);
-  if (i2 < npair) {
-    for (int k = kb; k < ke; k++) {
-      T v = 0;
-      if (i <= iend) {
-        v = fma(sp[(k - k0) * 32 + lane], xin, sy[(k - k0) * 32 + lane]);
-        put(g, x, i, j, k, v, fuse);
-      }
-      if (bc) sor_bc(comp, g, h, x, X, P, i2, i, iend, v, j, k, fuse);
-    }
-  }
-}
-
-// The same half-sweep in super-chunks of SOC_SC levels with a carried
-// value, so shared memory stays bounded for any column length (36 KB for
+// with A and B known before the sweep; the column is split into chunks whose
+// recurrences run in parallel from a zero start and are then joined:
+// x = y + P x_in, with y the chunk-local solution, P the product of the B
+// factors since the chunk start and x_in the value entering the chunk.
+// Coefficient records are streamed (evict-first) so the x field stays
+// resident in L2.
+//
+// The kernel walks the column in super-chunks of SOC_SC levels with a
+// carried value, so shared memory stays bounded for any column length (36 KB for
 // FP64) and several blocks share an SM.  Per super-chunk:
 //   1. produce: A and B of every (level, column) pair, a warp per level and
 //      a lane per column, all pairs independent (their loads overlap);
@@ -314,8 +153,8 @@ __global__ void __launch_bounds__(SO3_W * 32)
 //   3. each warp folds the chunk ends below it and the carried value into
 //      x_in and writes x = y + P x_in with the boundary rows; the last
 //      level's x is carried into the next super-chunk.
-// The chunk boundaries differ from k_sor_odd_c3's, and so does the
-// rounding (a few ulp, the level-by-level order being the oracle's).
+// The rounding differs from the level-by-level order (the oracle's) by a
+// few ulp.
 constexpr int SOC_W = 8, SOC_SC = 64;
 
 // One tile: 32 columns (x pairs from bx*32) of row j = by+1.  Every thread
@@ -390,14 +229,28 @@ __device__ __forceinline__ void sor_odd_c4_tile(int comp_, const Geo &g, const H
     for (int v = 0; v < w; v++) xin = fma(ep[v][lane], xin, ey[v][lane]);
     if (i2 < npair) {
       for (int lk = lb; lk < le; lk++) {
-        const int k = kc + lk;
         T v = 0;
         if (i <= iend) {
           v = fma(sB[lk][lane], xin, sA[lk][lane]);
-          put(g, x, i, j, k, v, fuse);
+          put(g, x, i, j, kc + lk, v, fuse);
         }
-        if (bc) sor_bc(comp, g, h, x, X, P, i2, i, iend, v, j, k, fuse);
+        sA[lk][lane] = v;  // kept for the boundary rows below
         if (lk == n - 1) scarry[lane] = v;
+      }
+      // boundary rows of these levels, by the owners of the first and last
+      // pairs, after the writes: the point each boundary copies (relaxed
+      // here, or of the other colour and final) is loaded for all levels at
+      // once instead of level by level.  Nothing in this sweep reads the
+      // boundary values of these levels.
+      if (bc && (i2 == 0 || i2 == (iend - 1) / 2)) {
+        const int ib = (i2 == 0) ? 1 : iend;
+        T src[PER];
+#pragma unroll
+        for (int l = 0; l < PER; l++)
+          src[l] = (lb + l < le) ? ((i != ib) ? x[TPLS_IDX(g, ib, j, kc + lb + l)] : sA[lb + l][lane]) : (T)0;
+#pragma unroll
+        for (int l = 0; l < PER; l++)
+          if (lb + l < le) sor_bc(comp, g, h, x, X, P, i2, ib, iend, src[l], j, kc + lb + l, fuse);
       }
     }
     __syncthreads();
@@ -460,29 +313,7 @@ cudaError_t launch_odd_multi(int comp, const SweepMember *mem, const int *prefix
   return cudaGetLastError();
 }
 
-template <typename T>
-static size_t so3_smem(const Geo &g, int comp, int w) {
-  const int nlev = g.nz - (comp == 2 ? 1 : 0);
-  return sizeof(T) * 2 * ((size_t)nlev + w) * 32;
-}
-constexpr size_t SO3_SMEM_MAX = 200 * 1024;
-
-template <typename T, typename CS, int CC>
-static cudaError_t so3_attr(int m) {
-  cudaError_t e = cudaFuncSetAttribute(k_sor_odd_c3<T, CS, CC, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_sor_odd_c3<T, CS, CC, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
-  return e;
-}
-
-cudaError_t sweep_init() {
-  const int m = (int)SO3_SMEM_MAX;
-  cudaError_t e = so3_attr<double, const double *, -1>(m);
-  if (e == cudaSuccess) e = so3_attr<float, MuCoef, 0>(m);
-  if (e == cudaSuccess) e = so3_attr<float, MuCoef, 1>(m);
-  if (e == cudaSuccess) e = so3_attr<float, MuCoef, 2>(m);
-  return e;
-}
+cudaError_t sweep_init() { return cudaSuccess; }
 
 template <typename T, typename CS, int CC, int BX, int BY>
 static void jacobi_v(int comp, const Geo &g, const Helm &h, const T *xo, CS coef, const double *pres,
@@ -534,22 +365,10 @@ static cudaError_t sor_c(int comp, const Geo &g, const Phys &ph, T *x, CS coef, 
       default: even_v<T, CS, CC, 32, 4>(comp, g, h, x, coef, pres, X, flg, bc, fuse, st); break;
     }
   } else {
+    // one block per 32 columns of a row, the column in super-chunks
+    (void)tile_odd;
     dim3 grd((npairs + 31) / 32, g.ny, 1);
-    // tile_odd 0: super-chunked column scan (bounded shared memory); 1, 2:
-    // whole-column scan with 8 or 16 chunks (its shared memory grows with
-    // nz; the one-warp recurrence beyond SO3_SMEM_MAX)
-    if (tile_odd == 0) {
-      k_sor_odd_c4<T, CS, CC><<<grd, SOC_W * 32, 0, st>>>(comp, g, h, x, coef, pres, X, flg, bc, fuse);
-      return cudaGetLastError();
-    }
-    const int w = (tile_odd == 1) ? 8 : 16;
-    const size_t sm = so3_smem<T>(g, comp, w);
-    if (sm <= SO3_SMEM_MAX && w == 16)
-      k_sor_odd_c3<T, CS, CC, 16><<<grd, 16 * 32, sm, st>>>(comp, g, h, x, coef, pres, X, flg, bc, fuse);
-    else if (sm <= SO3_SMEM_MAX)
-      k_sor_odd_c3<T, CS, CC, 8><<<grd, 8 * 32, sm, st>>>(comp, g, h, x, coef, pres, X, flg, bc, fuse);
-    else
-      k_sor_odd_c2<T, CS, CC><<<grd, SO_T, 0, st>>>(comp, g, h, x, coef, pres, X, flg, bc, fuse);
+    k_sor_odd_c4<T, CS, CC><<<grd, SOC_W * 32, 0, st>>>(comp, g, h, x, coef, pres, X, flg, bc, fuse);
   }
   return cudaGetLastError();
 }

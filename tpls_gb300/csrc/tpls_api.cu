@@ -21,20 +21,22 @@ constexpr int kMaxScratch = 8;
 
 }  // namespace
 
-// Batched host transfers: a ring of staging buffers (slot 0 is the
-// context's own staging buffer, the others are allocated on first use) and
-// one copy stream per direction.  A field's copy and its repack run on
+// Batched host transfers: per direction a ring of two staging buffers (the
+// context's own staging buffer is one of them, the other three are
+// allocated on first use) and one copy stream.  A field's copy and its repack run on
 // different streams, ordered by events, so successive fields overlap and a
 // download followed by an upload of the same host arrays uses both copy
 // directions at once.
 struct Xfer {
-  static constexpr int K = 4;
+  // per direction (0: uploads, 1: downloads) a ring of K staging slots, so a
+  // download and an upload never wait for each other's slots
+  static constexpr int K = 2;
   cudaStream_t h2d = nullptr, d2h = nullptr;
-  double *slot[K] = {nullptr, nullptr, nullptr, nullptr};
-  cudaEvent_t free_ev[K] = {nullptr, nullptr, nullptr, nullptr};  // the slot may be refilled
-  cudaEvent_t ready_ev[K] = {nullptr, nullptr, nullptr, nullptr};  // the slot holds its data
+  double *slot[2][K] = {{nullptr, nullptr}, {nullptr, nullptr}};
+  cudaEvent_t free_ev[2][K] = {{nullptr, nullptr}, {nullptr, nullptr}};   // the slot may be refilled
+  cudaEvent_t ready_ev[2][K] = {{nullptr, nullptr}, {nullptr, nullptr}};  // the slot holds its data
   cudaEvent_t d2h_last = nullptr;  // the last download enqueued
-  int next = 0;
+  int next[2] = {0, 0};
   std::map<const void *, cudaEvent_t> host_done;  // last download into each host array
 };
 
@@ -334,10 +336,11 @@ static void xfer_destroy(Xfer *x) {
   if (!x) return;
   if (x->h2d) cudaStreamSynchronize(x->h2d);
   if (x->d2h) cudaStreamSynchronize(x->d2h);
-  for (int q = 0; q < Xfer::K; q++) {
-    if (x->free_ev[q]) cudaEventDestroy(x->free_ev[q]);
-    if (x->ready_ev[q]) cudaEventDestroy(x->ready_ev[q]);
-  }
+  for (int d = 0; d < 2; d++)
+    for (int q = 0; q < Xfer::K; q++) {
+      if (x->free_ev[d][q]) cudaEventDestroy(x->free_ev[d][q]);
+      if (x->ready_ev[d][q]) cudaEventDestroy(x->ready_ev[d][q]);
+    }
   for (auto &kv : x->host_done) cudaEventDestroy(kv.second);
   if (x->d2h_last) cudaEventDestroy(x->d2h_last);
   if (x->h2d) cudaStreamDestroy(x->h2d);
@@ -627,19 +630,20 @@ static cudaError_t xfer_init(tpls_ctx *c) {
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&x->d2h, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&x->d2h_last, cudaEventDisableTiming);
   const size_t n = (size_t)(c->nx + 2) * (c->ny + 2) * (c->nz + 2);
-  x->slot[0] = c->stage;
-  for (int q = 1; q < Xfer::K && e == cudaSuccess; q++) {
-    void *b = nullptr;
-    e = cudaMalloc(&b, n * sizeof(double));
-    if (e == cudaSuccess) {
-      c->allocs.push_back(b);
-      x->slot[q] = (double *)b;
+  x->slot[1][0] = c->stage;
+  for (int d = 0; d < 2 && e == cudaSuccess; d++)
+    for (int q = 0; q < Xfer::K && e == cudaSuccess; q++) {
+      if (!x->slot[d][q]) {
+        void *b = nullptr;
+        e = cudaMalloc(&b, n * sizeof(double));
+        if (e == cudaSuccess) {
+          c->allocs.push_back(b);
+          x->slot[d][q] = (double *)b;
+        }
+      }
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&x->free_ev[d][q], cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&x->ready_ev[d][q], cudaEventDisableTiming);
     }
-  }
-  for (int q = 0; q < Xfer::K && e == cudaSuccess; q++) {
-    e = cudaEventCreateWithFlags(&x->free_ev[q], cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&x->ready_ev[q], cudaEventDisableTiming);
-  }
   if (e != cudaSuccess) {
     xfer_destroy(x);
     return e;
@@ -657,16 +661,17 @@ int tpls_set_fields(tpls_ctx *c, int n, const int *fields, const double *const *
   for (int i = 0; i < n; i++) {
     const int f = fields[i], nzp = nz_planes(field_kind(f), c->nz);
     const int w = c->nx + 2, rows = (c->ny + 2) * nzp;
-    const int q = x->next;
-    x->next = (q + 1) % Xfer::K;
-    TCK(cudaStreamWaitEvent(x->h2d, x->free_ev[q], 0));
+    const int q = x->next[0];
+    x->next[0] = (q + 1) % Xfer::K;
+    TCK(cudaStreamWaitEvent(x->h2d, x->free_ev[0][q], 0));
     auto hd = x->host_done.find(hosts[i]);  // a download into this array still in flight
     if (hd != x->host_done.end()) TCK(cudaStreamWaitEvent(x->h2d, hd->second, 0));
-    TCK(cudaMemcpyAsync(x->slot[q], hosts[i], sizeof(double) * (size_t)w * rows, cudaMemcpyHostToDevice, x->h2d));
-    TCK(cudaEventRecord(x->ready_ev[q], x->h2d));
-    TCK(cudaStreamWaitEvent(c->st, x->ready_ev[q], 0));
-    LCK(c, repack(x->slot[q], w, field_ptr(c, f), c->px, w, rows, c->st));
-    TCK(cudaEventRecord(x->free_ev[q], c->st));
+    TCK(cudaMemcpyAsync(x->slot[0][q], hosts[i], sizeof(double) * (size_t)w * rows, cudaMemcpyHostToDevice,
+                        x->h2d));
+    TCK(cudaEventRecord(x->ready_ev[0][q], x->h2d));
+    TCK(cudaStreamWaitEvent(c->st, x->ready_ev[0][q], 0));
+    LCK(c, repack(x->slot[0][q], w, field_ptr(c, f), c->px, w, rows, c->st));
+    TCK(cudaEventRecord(x->free_ev[0][q], c->st));
   }
   if (n > 0) c->need_exchange = true;
   return TPLS_OK;
@@ -686,14 +691,15 @@ int tpls_get_fields(tpls_ctx *c, int n, const int *fields, double *const *hosts)
   for (int i = 0; i < n; i++) {
     const int f = fields[i], nzp = nz_planes(field_kind(f), c->nz);
     const int w = c->nx + 2, rows = (c->ny + 2) * nzp;
-    const int q = x->next;
-    x->next = (q + 1) % Xfer::K;
-    TCK(cudaStreamWaitEvent(c->st, x->free_ev[q], 0));
-    LCK(c, repack(field_ptr(c, f), c->px, x->slot[q], w, w, rows, c->st));
-    TCK(cudaEventRecord(x->ready_ev[q], c->st));
-    TCK(cudaStreamWaitEvent(x->d2h, x->ready_ev[q], 0));
-    TCK(cudaMemcpyAsync(hosts[i], x->slot[q], sizeof(double) * (size_t)w * rows, cudaMemcpyDeviceToHost, x->d2h));
-    TCK(cudaEventRecord(x->free_ev[q], x->d2h));
+    const int q = x->next[1];
+    x->next[1] = (q + 1) % Xfer::K;
+    TCK(cudaStreamWaitEvent(c->st, x->free_ev[1][q], 0));
+    LCK(c, repack(field_ptr(c, f), c->px, x->slot[1][q], w, w, rows, c->st));
+    TCK(cudaEventRecord(x->ready_ev[1][q], c->st));
+    TCK(cudaStreamWaitEvent(x->d2h, x->ready_ev[1][q], 0));
+    TCK(cudaMemcpyAsync(hosts[i], x->slot[1][q], sizeof(double) * (size_t)w * rows, cudaMemcpyDeviceToHost,
+                        x->d2h));
+    TCK(cudaEventRecord(x->free_ev[1][q], x->d2h));
     cudaEvent_t &ev = x->host_done[hosts[i]];
     if (!ev) TCK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
     TCK(cudaEventRecord(ev, x->d2h));

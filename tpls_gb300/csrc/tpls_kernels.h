@@ -140,8 +140,8 @@ cudaError_t launch_sor(int comp, const Geo &g, const Phys &ph, double *x,
                        const double *pres, int flg, int iteration_time,
                        int bc, int fuse_ghosts, cudaStream_t st);
 // Tile-shape choice of the sweep kernels (autotuned per grid): jac / even =
-// block shape index (0: 32x4, 1: 32x8, 2: 64x4, 3: 16x8), odd = chunks per
-// column (0: by column length, 1: 8 warps, 2: 16 warps).
+// block shape index (0: 32x4, 1: 32x8, 2: 64x4, 3: 16x8); odd is always 0
+// (the odd half-sweep has one shape).
 struct SweepTiles {
   int jac = 0, even = 0, odd = 0;
 };
