@@ -161,7 +161,7 @@ def _profile_figure(tag: str, kernel: str, workload: str) -> dict | None:
 
 def run_gpu(args, ws, rank, local) -> dict | None:
     import torch
-    from tpls_gb300.api import TplsGpu
+    from tpls_gb300.api import TPLS_FLAG_NO_TMA, TplsGpu
     from tpls_gb300.channel import WORKLOADS, make_case
 
     torch.cuda.set_device(local)
@@ -175,7 +175,7 @@ def run_gpu(args, ws, rank, local) -> dict | None:
     nx, ny, nz = args.grid if args.grid else (w.nx, w.ny, w.nz)
     params, uin, st = make_case(args.config, nx=nx, ny=ny, nz=nz, p_rtol=args.p_rtol, precision=precision,
                                 fp64_parts=parts, mg_fp32=1 if (precision == 0 and args.mg_fp32) else 0,
-                                idm=args.idm, pe=args.dim_pe)
+                                idm=args.idm, pe=args.dim_pe, flags=TPLS_FLAG_NO_TMA if args.no_tma else 0)
     cells = nx * ny * nz
     g = TplsGpu(nx, ny, nz, params, uin)
     g.set_state(st)
@@ -291,6 +291,8 @@ def run_gpu(args, ws, rank, local) -> dict | None:
                    "precision": "fp64" if precision == 0 else "fp32-mixed",
                    "fp64_parts": parts,
                    "mg_fp32": params.mg_fp32,
+                   "advect_phi": ("read through the caches" if (args.no_tma or precision == 0)
+                                  else "tiles staged by TMA (cp.async.bulk.tensor)"),
                    "idm": args.idm,
                    "dim_pe": args.dim_pe if args.idm == "dim" else None,
                    "sweep_tiles": tiles,
@@ -595,6 +597,102 @@ def run_serve(args, ws, rank, local) -> dict | None:
     }
 
 
+def run_routine_costs(args) -> dict:
+    """What a driver that adopts the per-routine entries pays per timestep:
+    each entry of one step of the reference's loop (main_ns_hybrid.F90:
+    583-913) called on this workload's arrays, once with plain (pageable)
+    host arrays, copied in and out around every call, and once with the
+    same arrays registered (tpls_register_host: device-resident behind the
+    same addresses).  Host wall clock per call (every entry waits for its
+    kernels), times the calls a step makes; the device-resident tpls_step
+    beside it.  The driver's own host loops between the calls (boundary
+    rows, the AB3 sums) are not included."""
+    import torch
+    from tpls_gb300.api import TplsGpu
+    from tpls_gb300.channel import WORKLOADS, make_case
+    torch.cuda.set_device(0)
+    w = WORKLOADS[args.config]
+    nx, ny, nz = args.grid if args.grid else (w.nx, w.ny, w.nz)
+    p, uin, st = make_case(args.config, nx=nx, ny=ny, nz=nz, p_rtol=args.p_rtol)
+    g = TplsGpu(nx, ny, nz, p, uin)
+    g.set_state(st)
+    f = lambda k: np.array(st[k], order="F")  # noqa: E731
+    a = {k.lower(): f(k) for k in ("PHI2", "U2", "V2", "W2", "U3", "V3", "W3", "PRES", "PRES_OLD", "CONV0_PHI",
+                                   "CONV1_PHI", "CONV2_PHI")}
+    a.update(phi3=g.zeros("p"), fx=g.zeros("p"), fy=g.zeros("p"), fz=g.zeros("p"), rhs_p=g.zeros("p"),
+             va=np.zeros(g.shape("va"), order="F"))
+    for k in ("u", "v"):
+        a.update({f"{k}3_old": g.zeros("uv"), f"rhs_{k}": g.zeros("uv"), f"conv_{k}": g.zeros("uv"),
+                  f"diff_{k}": g.zeros("uv")})
+    a.update(w3_old=g.zeros("w"), rhs_w=g.zeros("w"), conv_w=g.zeros("w"), diff_w=g.zeros("w"))
+    dx, dy, dz, dt = p.dx, p.dy, p.dz, p.dt
+    x3 = {0: ("u3", "u3_old", "rhs_u"), 1: ("v3", "v3_old", "rhs_v"), 2: ("w3", "w3_old", "rhs_w")}
+    jac = {0: g.do_jacobi_u, 1: g.do_jacobi_v, 2: g.do_jacobi_w}
+    sor = {0: g.do_sor_u, 1: g.do_sor_v, 2: g.do_sor_w}
+    mom = p.mom_u // 2
+    # (name, calls per step, call)
+    entries = [
+        ("do_advect_phi", 1, lambda: g.do_advect_phi(a["phi2"], a["u2"], a["v2"], a["w2"], dx, dy, dz,
+                                                     conv2_phi=a["conv2_phi"])),
+        ("do_tpls", 1, lambda: g.do_tpls(a["phi2"], a["conv0_phi"], a["conv1_phi"], a["conv2_phi"], p.levelset,
+                                         p.height, dx, dz, dt, phi3=a["phi3"])),
+        ("get_csf", 1, lambda: g.get_csf(a["phi3"], dx, dy, dz, p.scap, p.smooth_width, a["fx"], a["fy"],
+                                         a["fz"])),
+        ("get_viscosity", 1, lambda: g.get_viscosity(a["phi2"], p.smooth_width, p.re, p.mu_minus, p.mu_plus,
+                                                     viscosity_aug=a["va"])),
+        ("get_conv_all", 1, lambda: g.get_conv_all(a["va"], a["u2"], a["v2"], a["w2"], dx, dy, dz,
+                                                   out=(a["conv_u"], a["conv_v"], a["conv_w"]))),
+        ("get_diffusion_all", 1, lambda: g.get_diffusion_all(a["va"], a["u2"], a["v2"], a["w2"], dx, dy, dz,
+                                                             out=(a["diff_u"], a["diff_v"], a["diff_w"]))),
+    ]
+    for c, nm in ((0, "u"), (1, "v"), (2, "w")):
+        x, xo, r = x3[c]
+        entries.append((f"do_jacobi_{nm}", mom, lambda c=c, x=x, xo=xo, r=r: jac[c](a[x], a[xo], a[r], a["va"],
+                                                                                   dx, dy, dz, dt)))
+        entries.append((f"do_sor_{nm}", 2 * mom, lambda c=c, x=x, r=r: sor[c](a[x], a[r], a["va"], dx, dy, dz,
+                                                                             dt, 0, 1)))
+        entries.append((f"get_difference ({nm})", 1, lambda x=x, xo=xo: g.get_difference(a[x], a[xo])))
+    entries += [
+        ("exchange2d", 3 * 3 * mom + 11, lambda: g.exchange2d(a["u3"])),
+        ("get_source_pres", 1, lambda: g.get_source_pres(a["u3"], a["v3"], a["w3"], dx, dy, dz, dt,
+                                                         rhs=a["rhs_p"])),
+        ("pressure_solve", 1, lambda: g.pressure_solve(a["pres_old"], a["rhs_p"], a["u3"], uin, dx, dy, dz, dt,
+                                                       rtol=p.p_rtol, maxits=p.p_maxits, pres=a["pres"])),
+        ("get_uvw_pres", 1, lambda: g.get_uvw_pres(a["u2"], a["v2"], a["w2"], a["pres"], dx, dy, dz, dt, uin)),
+    ]
+    reps = max(1, args.routine_reps)
+    table = {}
+    for form in ("host", "registered"):
+        if form == "registered":
+            for x in a.values():
+                g.register_host(x)
+        for name, n, fn in entries:
+            fn()  # warm-up (scratch allocation on the first call)
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                fn()
+            table.setdefault(name, {"calls_per_step": n})[f"{form}_ms"] = (time.perf_counter() - t0) / reps * 1e3
+        if form == "registered":
+            g.download_host()
+    tot = {f: sum(v["calls_per_step"] * v[f"{f}_ms"] for v in table.values()) for f in ("host", "registered")}
+    g.set_state(st)
+    g.step(3)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    g.step(5)
+    torch.cuda.synchronize()
+    step_ms = (time.perf_counter() - t0) / 5 * 1e3
+    g.close()
+    return {"routine_costs": True, "config": {"workload": f"{args.config}: {nx}x{ny}x{nz} FP64 channel",
+                                              "calls": "one timestep of main_ns_hybrid.F90:583-913 "
+                                                       f"(mom_uvw {p.mom_u}, levelset {p.levelset})",
+                                              "host_arrays": "pageable numpy, Fortran order"},
+            "per_entry": {k: {x: (round(y, 4) if isinstance(y, float) else y) for x, y in v.items()}
+                          for k, v in table.items()},
+            "ms_per_step": {"per_routine_host_arrays": tot["host"], "per_routine_registered": tot["registered"],
+                            "tpls_step_device_resident": step_ms}}
+
+
 def _precision(args) -> int:
     if args.precision is not None:
         return 0 if args.precision == "fp64" else 1
@@ -703,6 +801,13 @@ def main():
     ap.add_argument("--idm", choices=["lsm", "dim"], default="lsm",
                     help="interface method: level set (default) or diffuse interface (FP64 form)")
     ap.add_argument("--dim-pe", type=float, default=1000.0, help="diffuse interface: Peclet number Pe")
+    ap.add_argument("--routine-costs", action="store_true",
+                    help="per-routine entries' cost per timestep, host arrays vs registered arrays (not a "
+                         "bench line)")
+    ap.add_argument("--routine-reps", type=int, default=3)
+    ap.add_argument("--no-tma", action="store_true",
+                    help="FP32-mixed form: advection reads phi through the caches instead of TMA-staged tiles "
+                         "(tpls_params.flags = TPLS_FLAG_NO_TMA; bit-identical)")
     ap.add_argument("--mg-fp32", action="store_true",
                     help="FP64 form: FP32 multigrid levels in the CG preconditioner (tpls_params.mg_fp32 = 1; "
                          "CG stays FP64 and meets p_rtol on its FP64 residual). Default: FP64 throughout")
@@ -721,7 +826,9 @@ def main():
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3  # timing rule: at least 3 warm-up steps
     ws, rank, local = _dist()
-    if args.accuracy > 0:
+    if args.routine_costs:
+        out = run_routine_costs(args) if rank == 0 else None
+    elif args.accuracy > 0:
         out = run_accuracy(args) if rank == 0 else None
     elif args.impl == "reference":
         out = run_reference(args, ws, rank)

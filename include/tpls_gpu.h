@@ -64,9 +64,15 @@ typedef struct tpls_params {
   int idm;                        /* idm: TPLS_IDM_LSM (level set, default) or
                                      TPLS_IDM_DIM (diffuse interface, FP64 form) */
   int max_iteration_dim;          /* max_iteration_dim (DIM SOR iterations) */
-  int reserved[2];
+  int flags;                      /* TPLS_FLAG_* (0 = defaults) */
+  int reserved;
   double epn, pe;                 /* epn, Pe (DIM interface width, Peclet number) */
 } tpls_params;
+
+/* tpls_params.flags: TPLS_FLAG_NO_TMA makes the FP32-mixed form's advection
+ * read phi through the caches instead of staging its tiles with TMA
+ * (bit-identical results). */
+#define TPLS_FLAG_NO_TMA 1
 
 /* Interface method (main_ns_hybrid.F90:595-612, option_names.F90:35-37). */
 #define TPLS_IDM_LSM 0
@@ -93,7 +99,9 @@ typedef struct tpls_stats {
   double liquid_volume; /* sum over cells of (1-H(phi)) dV after the step */
   int p_worst;      /* lowest reason of the solves since the previous
                        tpls_get_stats (0 when none diverged) */
-  int reserved_i[3];
+  int kernel_timeouts; /* blocks whose bounded wait for staged data ran out
+                          (their outputs are NaN); 0 in a healthy run */
+  int reserved_i[2];
 } tpls_stats;
 
 /* Field identifiers for tpls_set_field / tpls_get_field and the oracle.
@@ -234,6 +242,14 @@ int tpls_graphs_enable(tpls_ctx *ctx, int on);
 int tpls_get_stats(tpls_ctx *ctx, tpls_stats *out);
 /* Waits for the context's stream and its copy streams. */
 int tpls_sync(tpls_ctx *ctx);
+/* Self-test of the bounded wait of the TMA-staged advection (no
+ * counterpart in the reference): one block of that kernel is launched
+ * with no load issued, so its wait for the staged tile runs out after a
+ * short limit; *timeouts returns how many blocks reported it (1) and
+ * *nan_out whether the block wrote NaN into its output cells (1), into a
+ * scratch array (the context's state is untouched).  TPLS_ERR_STATE for a
+ * context without the TMA path (FP64 form, or TPLS_FLAG_NO_TMA). */
+int tpls_selftest_wait_limit(tpls_ctx *ctx, int *timeouts, int *nan_out);
 const char *tpls_status_string(int status);
 /* Number of kernels the library has launched on this context (counted on
  * the host at every launch site). */
@@ -261,6 +277,27 @@ void *tpls_stream(tpls_ctx *ctx);
 int tpls_base_profile(int nz, double dz, double re, double dpdl,
                       double mu_minus, double mu_plus, double height,
                       double smooth_width, double *u_oned);
+
+/* ---- host-array registry ----------------------------------------------
+ * Keeps the driver's arrays (state.F90:21-53: phi2, u2, u3, RHS_u,
+ * viscosity2_aug, pres, ...) device-resident while its call sites in
+ * main_ns_hybrid.F90 keep passing the same host addresses to the
+ * per-routine entries below.  tpls_register_host(ctx, a, n) allocates a
+ * device mirror of the n doubles at a and copies them once; from then on
+ * every copy the library makes to or from an address inside [a, a+n)
+ * (the per-routine entries, tpls_set_field/get_field and the batched
+ * transfers) goes to the same place in the mirror, so a routine's inputs
+ * and outputs stay on the device and the host array is NOT updated.
+ * tpls_download_host(ctx, a) refreshes the host array from its mirror (at
+ * the driver's output frequency; a = NULL: every registered array),
+ * tpls_upload_host(ctx, a) the mirror from the host array (after host code
+ * changed it).  Registered ranges may not overlap (TPLS_ERR_ARG).  Mirrors
+ * are freed by tpls_unregister_host or tpls_gpu_destroy (no copy back), and
+ * are not counted by tpls_footprint_bytes. */
+int tpls_register_host(tpls_ctx *ctx, double *host, long long count);
+int tpls_unregister_host(tpls_ctx *ctx, double *host);
+int tpls_download_host(tpls_ctx *ctx, double *host);
+int tpls_upload_host(tpls_ctx *ctx, const double *host);
 
 /* ---- per-routine drop-in entries (host arrays) ------------------------ */
 

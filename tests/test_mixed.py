@@ -15,7 +15,7 @@ liquid volume equal to 1e-8 relative after 20 steps."""
 import numpy as np
 import pytest
 
-from tpls_gb300.api import STATE_FIELDS, TplsGpu
+from tpls_gb300.api import STATE_FIELDS, TPLS_FLAG_NO_TMA, TplsGpu
 from tpls_gb300.channel import make_case
 
 from _util import relmax
@@ -116,3 +116,39 @@ def test_mixed_hundred_steps_fp32_and_fp64_stencils(parts):
     assert abs(vm - vr) <= 1e-8 * abs(vr)
     ref.close()
     mix.close()
+
+
+def test_tma_staged_advection_is_bit_identical():
+    """The FP32 advection with its phi tiles staged by TMA (the default)
+    against the same kernel reading phi through the caches
+    (TPLS_FLAG_NO_TMA): same arithmetic, so the states are bit-identical,
+    on the 64x32x48 channel and on ragged grids (partial tiles at the x, y
+    and z ends, ny below the tile height); no block's wait ran out."""
+    for size in ((NX, NY, NZ), (37, 5, 23), (70, 19, 9)):
+        a = _ctx(1, size, fp64_parts=2)
+        b = _ctx(1, size, fp64_parts=2, flags=TPLS_FLAG_NO_TMA)
+        assert a.step(3) == 0 and b.step(3) == 0
+        sa, sb = a.get_state(), b.get_state()
+        for k in STATE_FIELDS:
+            assert np.array_equal(sa[k], sb[k]), (size, k)
+        assert np.array_equal(a.get_field("CONV2_PHI"), b.get_field("CONV2_PHI"))
+        assert a.stats()["kernel_timeouts"] == 0
+        a.close()
+        b.close()
+
+
+def test_tma_wait_limit_reports_and_returns():
+    """The staged advection's wait for its tile is bounded: a block launched
+    with no load issued (nothing completes its barrier) gives up after the
+    limit, reports it and writes NaN instead of leaving garbage; the context
+    stays usable."""
+    import ctypes as C
+    g = _ctx(1, fp64_parts=2)
+    t, nan = C.c_int(-1), C.c_int(-1)
+    assert g.lib.tpls_selftest_wait_limit(g.ctx, C.byref(t), C.byref(nan)) == 0
+    assert t.value == 1 and nan.value == 1
+    assert g.step(2) == 0 and g.stats()["kernel_timeouts"] == 0
+    f = _ctx(0)
+    assert f.lib.tpls_selftest_wait_limit(f.ctx, C.byref(t), C.byref(nan)) == 3  # no TMA path
+    g.close()
+    f.close()

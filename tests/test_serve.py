@@ -171,3 +171,40 @@ def test_gpu_server_result_same_alone_and_in_mix():
         assert rm.worst_reason == 0
         h = rm.snapshots[-1].height
         assert np.all((h > 0.2) & (h < 0.8))  # the interface stays near mid-channel
+
+
+@pytest.mark.gpu
+def test_contexts_created_on_a_thread_while_steps_are_captured():
+    """Contexts created and destroyed on a worker thread while the main
+    thread captures other contexts' step graphs (each context's first three
+    steps capture one graph each), as the server does: every capture and
+    every step succeeds."""
+    import threading
+    from tpls_gb300.batch import Instance, open_instance
+    stop = threading.Event()
+    errors, churned = [], []
+
+    def churn():
+        try:
+            q = 0
+            while not stop.is_set():
+                g = open_instance(Instance(100 + q, 96, 64, 48, 2.0, 1.0, 100.0, 0.05, 50 + q), q % 2)
+                g.close()
+                q += 1
+            churned.append(q)
+        except Exception as e:  # reported on the main thread
+            errors.append(e)
+
+    t = threading.Thread(target=churn)
+    t.start()
+    try:
+        for q in range(12):
+            g = open_instance(Instance(q, 64, 32, 32, 2.0, 1.0, 100.0, 0.05, 7 + q), q % 2)
+            assert g.step(3) == 0
+            assert g.stats()["p_worst"] == 0
+            g.close()
+    finally:
+        stop.set()
+        t.join()
+    assert not errors, errors
+    assert churned and churned[0] > 0

@@ -31,6 +31,7 @@ LIB_PATH = _ROOT / "_lib" / "libtpls_gb300.so"
 TPLS_PREC_FP64 = 0
 TPLS_PREC_FP32_MIXED = 1
 PART_ADVECT, PART_LEVELSET, PART_MOMENTUM, PART_MULTIGRID, PART_MOM_STENCIL = 1, 2, 4, 8, 16
+TPLS_FLAG_NO_TMA = 1  # tpls_params.flags: advection without TMA-staged tiles
 
 # field ids (enum tpls_field)
 TIMERS = ["advect", "levelset", "csf", "visc", "mom_rhs", "jacobi", "sor_even", "sor_odd", "pressure", "project",
@@ -60,7 +61,7 @@ class TplsParams(C.Structure):
                 ("mom_u", C.c_int), ("mom_v", C.c_int), ("mom_w", C.c_int), ("levelset", C.c_int),
                 ("p_rtol", C.c_double), ("p_maxits", C.c_int), ("precision", C.c_int),
                 ("fp64_parts", C.c_int), ("mg_fp32", C.c_int), ("idm", C.c_int),
-                ("max_iteration_dim", C.c_int), ("reserved", C.c_int * 2), ("epn", C.c_double),
+                ("max_iteration_dim", C.c_int), ("flags", C.c_int), ("reserved", C.c_int), ("epn", C.c_double),
                 ("pe", C.c_double)]
 
 
@@ -68,7 +69,8 @@ class TplsStats(C.Structure):
     _fields_ = [("err_phi", C.c_double), ("err_u", C.c_double), ("err_v", C.c_double),
                 ("err_w", C.c_double), ("p_rnorm", C.c_double), ("p_bnorm", C.c_double),
                 ("p_its", C.c_int), ("p_reason", C.c_int), ("steps_done", C.c_long),
-                ("liquid_volume", C.c_double), ("p_worst", C.c_int), ("reserved_i", C.c_int * 3)]
+                ("liquid_volume", C.c_double), ("p_worst", C.c_int), ("kernel_timeouts", C.c_int),
+                ("reserved_i", C.c_int * 2)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved_i"}
@@ -100,6 +102,7 @@ class Params:
     max_iteration_dim: int = 18  # tpls_config.opt default
     epn: float = 0.0  # diffuse interface width
     pe: float = 1.0  # Peclet number of the diffuse-interface method
+    flags: int = 0  # TPLS_FLAG_* (1: no TMA staging in the FP32 advection)
     extra: dict = field(default_factory=dict)
 
     def to_c(self) -> TplsParams:
@@ -155,6 +158,11 @@ def load_library(path: Path | None = None) -> C.CDLL:
     lib.tpls_set_fields.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(_DP)]
     lib.tpls_get_fields.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(_DP)]
     lib.tpls_xfer_join.argtypes = [C.c_void_p]
+    lib.tpls_selftest_wait_limit.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    lib.tpls_register_host.argtypes = [C.c_void_p, _DP, C.c_longlong]
+    lib.tpls_unregister_host.argtypes = [C.c_void_p, _DP]
+    lib.tpls_download_host.argtypes = [C.c_void_p, _DP]
+    lib.tpls_upload_host.argtypes = [C.c_void_p, _DP]
     lib.tpls_backup_channel.argtypes = [C.c_void_p, C.c_char_p, C.c_char_p]
     lib.tpls_dataload_channel.argtypes = [C.c_void_p, C.c_char_p, C.c_char_p]
     if path is None:
@@ -208,6 +216,7 @@ class TplsGpu:
         if uin.shape != (nz,):
             raise ValueError("u_inlet must have nz entries")
         self.u_inlet = uin
+        self._registered = {}  # address -> array registered with tpls_register_host
         h = C.c_void_p()
         s = self.lib.tpls_gpu_create(nx, ny, nz, C.byref(self._cp), uin.ctypes.data_as(_DP), C.byref(h))
         self._check(s)
@@ -322,6 +331,25 @@ class TplsGpu:
         self._check(self.lib.tpls_get_tiles(self.ctx, t))
         return {"jacobi": t[0], "sor_even": t[1], "sor_odd": t[2]}
 
+    def register_host(self, a: np.ndarray) -> None:
+        """Keep a host array device-resident behind its address
+        (tpls_register_host): routines called with it read and write its
+        device mirror, and `a` itself changes only on download_host."""
+        self._check(self.lib.tpls_register_host(self.ctx, _ptr(a), a.size))
+        self._registered[a.ctypes.data] = a  # the address must stay valid
+
+    def unregister_host(self, a: np.ndarray) -> None:
+        self._check(self.lib.tpls_unregister_host(self.ctx, _ptr(a)))
+        self._registered.pop(a.ctypes.data, None)
+
+    def download_host(self, a: np.ndarray | None = None) -> None:
+        """Host array(s) <- device mirror(s) (all registered when a is None)."""
+        self._check(self.lib.tpls_download_host(self.ctx, _ptr(a)))
+
+    def upload_host(self, a: np.ndarray | None = None) -> None:
+        """Device mirror(s) <- host array(s) (all registered when a is None)."""
+        self._check(self.lib.tpls_upload_host(self.ctx, _ptr(a)))
+
     def set_steps_done(self, n: int) -> None:
         """Continue an earlier run's step count (tpls_stats.steps_done)."""
         self._check(self.lib.tpls_set_steps_done(self.ctx, int(n)))
@@ -367,11 +395,11 @@ class TplsGpu:
         return {k: (ms[i], n[i]) for i, k in enumerate(TIMERS)}
 
     # -- per-routine drop-in entries ----------------------------------------
-    def do_advect_phi(self, phi2, u2, v2, w2, dx, dy, dz):
+    def do_advect_phi(self, phi2, u2, v2, w2, dx, dy, dz, conv2_phi=None):
         """advect_phi.f90:19 -> conv2_phi; u2, v2, w2 get their halo rows
         exchanged in place, as in the reference."""
         nx, ny, nz = self.nx, self.ny, self.nz
-        conv = self.zeros("p")
+        conv = self.zeros("p") if conv2_phi is None else conv2_phi
         b = self._b()
         nb = (C.c_int * 6)(*([-2] * 6))
         s = self.lib.tpls_do_advect_phi(
@@ -433,21 +461,21 @@ class TplsGpu:
         self._check(s)
         return va
 
-    def _conv_diff(self, fn, va, u2, v2, w2, dx, dy, dz):
-        ou, ov, ow = self.zeros("uv"), self.zeros("uv"), self.zeros("w")
+    def _conv_diff(self, fn, va, u2, v2, w2, dx, dy, dz, out=None):
+        ou, ov, ow = (self.zeros("uv"), self.zeros("uv"), self.zeros("w")) if out is None else out
         b = self._b()
         s = fn(self.ctx, _ptr(ou), _ptr(ov), _ptr(ow), _ptr(va), _ptr(u2), _ptr(v2), _ptr(w2), b["sx"],
                b["sy"], b["ex"], b["ey"], _i(self.nz + 1), _i(self.nx), _d(dx), _d(dy), _d(dz))
         self._check(s)
         return ou, ov, ow
 
-    def get_conv_all(self, viscosity_aug, u2, v2, w2, dx, dy, dz):
+    def get_conv_all(self, viscosity_aug, u2, v2, w2, dx, dy, dz, out=None):
         """momentum_allflux.f90:224 -> (conv_u2, conv_v2, conv_w2)."""
-        return self._conv_diff(self.lib.tpls_get_conv_all, viscosity_aug, u2, v2, w2, dx, dy, dz)
+        return self._conv_diff(self.lib.tpls_get_conv_all, viscosity_aug, u2, v2, w2, dx, dy, dz, out)
 
-    def get_diffusion_all(self, viscosity_aug, u2, v2, w2, dx, dy, dz):
+    def get_diffusion_all(self, viscosity_aug, u2, v2, w2, dx, dy, dz, out=None):
         """momentum_allflux.f90:22 -> (diff_u, diff_v, diff_w)."""
-        return self._conv_diff(self.lib.tpls_get_diffusion_all, viscosity_aug, u2, v2, w2, dx, dy, dz)
+        return self._conv_diff(self.lib.tpls_get_diffusion_all, viscosity_aug, u2, v2, w2, dx, dy, dz, out)
 
     def _jac(self, fn, x3, x3_old, rhs, va, dx, dy, dz, dt):
         b = self._b()
@@ -497,9 +525,9 @@ class TplsGpu:
         self._check(s)
         return out.value
 
-    def get_source_pres(self, u3, v3, w3, dx, dy, dz, dt):
+    def get_source_pres(self, u3, v3, w3, dx, dy, dz, dt, rhs=None):
         """pressure.f90:16 -> RHS_p."""
-        rhs = self.zeros("p")
+        rhs = self.zeros("p") if rhs is None else rhs
         b = self._b()
         s = self.lib.tpls_get_source_pres(self.ctx, _ptr(rhs), _ptr(u3), _ptr(v3), _ptr(w3), b["ex"], b["ey"],
                                           b["sx"], b["sy"], _i(self.nz + 1), _d(dx), _d(dy), _d(dz), _d(dt))
@@ -516,10 +544,10 @@ class TplsGpu:
         self._check(s)
         return u3, v3, w3
 
-    def pressure_solve(self, pres_old, rhs_p, u3, u_inlet, dx, dy, dz, dt, rtol=0.0, maxits=0):
+    def pressure_solve(self, pres_old, rhs_p, u3, u_inlet, dx, dy, dz, dt, rtol=0.0, maxits=0, pres=None):
         """`pres=pres_old; KSPSolve; copy_pressure_out_of_petsc`
         (main_ns_hybrid.F90:896-913) -> (pres, its, rnorm, reason)."""
-        pres = self.zeros("p")
+        pres = self.zeros("p") if pres is None else pres
         its, rn, rs = C.c_int(0), C.c_double(0.0), C.c_int(0)
         uin = np.ascontiguousarray(u_inlet, dtype=np.float64)
         s = self.lib.tpls_pressure_solve(self.ctx, _ptr(pres), _ptr(pres_old), _ptr(rhs_p), _ptr(u3),

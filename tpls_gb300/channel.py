@@ -123,7 +123,7 @@ def make_case(w: Workload | str, *, nx: int | None = None, ny: int | None = None
               mom: int = 30, levelset: int = 10, p_rtol: float = 1e-5, p_maxits: int = 200,
               precision: int = 0, fp64_parts: int = 0, mg_fp32: int = 0, idm: str = "lsm",
               epn: float | None = None, pe: float = 1000.0, max_iteration_dim: int = 18,
-              geometry: str = "cubic", profile=None):
+              geometry: str = "cubic", profile=None, flags: int = 0):
     """Returns (params, u_inlet, state) for a workload, optionally resized.
 
     state maps TPLS field names (tpls_gb300.api.STATE_FIELDS subset) to
@@ -156,7 +156,7 @@ def make_case(w: Workload | str, *, nx: int | None = None, ny: int | None = None
                     scap=1.0, smooth_width=sw, mom_u=mom, mom_v=mom, mom_w=mom, levelset=levelset,
                     p_rtol=p_rtol, p_maxits=p_maxits, precision=precision, fp64_parts=fp64_parts,
                     mg_fp32=mg_fp32, idm=1 if idm == "dim" else 0, max_iteration_dim=max_iteration_dim,
-                    epn=(1.5 * dz if epn is None else epn), pe=pe)
+                    epn=(1.5 * dz if epn is None else epn), pe=pe, flags=flags)
     xi = (np.arange(nx + 2) - 0.5) * dx
     yj = (np.arange(ny + 2) - 0.5) * dy
     zk = (np.arange(nz + 2) - 0.5) * dz

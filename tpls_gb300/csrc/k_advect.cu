@@ -10,6 +10,10 @@
 // in a register.
 // The periodic-y halo of the reference's 3-ghost phi_augaug copy becomes a
 // wrapped row index; no augmented array is built.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <stdint.h>
+
 #include "tpls_kernels.h"
 #include "tpls_pair.cuh"
 
@@ -160,6 +164,192 @@ __global__ void __launch_bounds__(ADV_BX *ADV_BY, 4)
     }
     zlo = zo;
   }
+}
+
+// ---------------------------------------------------------------------------
+// The FP32 advection with phi staged by TMA.  A block (32 x 8 cells of
+// AT_TZ levels) loads the phi tile with its 3-cell halos into shared memory
+// by cp.async.bulk.tensor: one load per y row (AT_NR rows j0-3 .. j0+10),
+// each a 40 x 1 x AT_NZ box of the FP32 phi copy, so the periodic y wrap of
+// the reference's phi_augaug is just the row coordinate; the x start is the
+// tile's first halo column rounded down to a 16-byte boundary, and levels
+// outside the array read as zero (only the arithmetic-mean z-faces sit near
+// them, and those read levels 0..nz+1).  The loads complete on one mbarrier;
+// every thread then evaluates the same faces as k_advect<float>, operation
+// for operation, from shared memory, so the result is bit-identical.  The
+// velocities are read from global memory as before.
+//
+// The wait on the mbarrier is bounded (`limit` polls): when it runs out the
+// block adds 1 to *kto, writes NaN into its output cells (the step's
+// pressure solve then reports DIVERGED_NAN), waits again, bounded, for any
+// copy still in flight, and returns.  arm = 0 issues no load (the
+// self-test of that path: nothing completes the barrier).
+constexpr int AT_BX = 32, AT_BY = 8, AT_TZ = 8;
+constexpr int AT_W = 40;               // staged x extent (floats)
+constexpr int AT_NR = AT_BY + 6;       // staged rows
+constexpr int AT_NZ = AT_TZ + 6;       // staged levels
+constexpr int AT_SLAB = 576;           // floats per row slab (40 x 14 = 560, padded to 128 bytes)
+static_assert(AT_W * AT_NZ <= AT_SLAB && (AT_SLAB * 4) % 128 == 0, "slab layout");
+constexpr unsigned AT_TX_BYTES = AT_NR * AT_W * AT_NZ * 4;
+
+__device__ __forceinline__ unsigned smem_addr(const void *p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity, int limit) {
+  for (int it = 0; it < limit; it++) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
+__global__ void __launch_bounds__(AT_BX *AT_BY)
+    k_advect_tma(const __grid_constant__ CUtensorMap phimap, Geo g, float rdx, float rdy, float rdz,
+                 const float *__restrict__ u, const float *__restrict__ v, const float *__restrict__ w,
+                 double *__restrict__ conv, double *kto, int arm, int limit) {
+  __shared__ __align__(128) float sphi[AT_NR * AT_SLAB];
+  __shared__ float xs[2][AT_BY][AT_BX + 1];
+  __shared__ float ys[2][AT_BY + 1][AT_BX];
+  __shared__ __align__(8) unsigned long long bar;
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * AT_BX + tx;
+  const int i0 = blockIdx.x * AT_BX + 1, j0 = blockIdx.y * AT_BY + 1;
+  const int k0 = blockIdx.z * AT_TZ + 1, k1 = min(k0 + AT_TZ - 1, g.nz);
+  const int x0 = blockIdx.x * AT_BX;  // row-start element of the slab: XOFF + i0 - 4, 16-byte aligned
+  const unsigned sbar = smem_addr(&bar);
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sbar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (tid == 0 && arm) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(sbar), "r"(AT_TX_BYTES) : "memory");
+    const unsigned long long map = reinterpret_cast<unsigned long long>(&phimap);
+    for (int r = 0; r < AT_NR; r++) {
+      const int jw = ((j0 - 4 + r) % g.ny + g.ny) % g.ny + 1;  // periodic row in 1..ny for any ny
+      asm volatile(
+          "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+          "[%5];" ::"r"(smem_addr(sphi + r * AT_SLAB)),
+          "l"(map), "r"(x0), "r"(jw), "r"(k0 - 3), "r"(sbar)
+          : "memory");
+    }
+  }
+  const bool ok = __syncthreads_and(mbar_wait(sbar, 0, limit));
+  const int i = i0 + tx, j = j0 + ty;
+  const bool act = (i <= g.nx) && (j <= g.ny);
+  if (!ok) {
+    if (tid == 0) atomicAdd(kto, 1.0);
+    if (act)
+      for (int k = k0; k <= k1; k++) conv[TPLS_IDX(g, i, j, k)] = __longlong_as_double(0x7ff8000000000000ll);
+    if (arm) mbar_wait(sbar, 0, limit);  // copies still in flight land before the block leaves
+    return;
+  }
+  // phi at (x index ii, row r of the staged tile, level kk)
+  auto PH = [&](int ii, int r, int kk) { return sphi[r * AT_SLAB + (kk - k0 + 3) * AT_W + (ii + XOFF - x0)]; };
+  // Velocity indices are clamped into the grid for lanes outside it; the
+  // staged indices of such a lane stay its own tile position (in the
+  // staged tile, results unused), so every shared-memory read is in range.
+  const int ic = act ? i : 1, jc = act ? j : 1;
+  const int ii = i0 + tx, jj = j0 + ty;  // staged column / row of this thread (= i, j when active)
+  const int jm = (jc == 1) ? g.ny : jc - 1;
+  const int jx = (j0 + tx <= g.ny) ? j0 + tx : 1;
+  const int rown = ty + 3;  // staged row of this thread's cell row
+  // dfx at u-index iu (staged column iu, velocity column iv) of staged row r
+  // (velocity p-row jp), level kp (as xface)
+  auto xf = [&](int iu, int iv, int r, int jp, int kp) -> float {
+    const int ju = (jp - 1 == 0) ? g.ny : jp - 1;
+    const float vel = u[TPLS_IDX(g, iv, ju, kp - 1)];
+    if (iu >= 3 && iu <= g.nx - 2)
+      return weno_up(upwind_pos(vel), PH(iu - 2, r, kp), PH(iu - 1, r, kp), PH(iu, r, kp), PH(iu + 1, r, kp),
+                     PH(iu + 2, r, kp), PH(iu + 3, r, kp));
+    return (upwind_pos(vel)) ? PH(iu, r, kp) : PH(iu + 1, r, kp);
+  };
+  // dfy at staged v-index jv (rows jv-2..jv+3 staged at jv-2-(j0-3)) and
+  // velocity v-index jvv, staged column ip, velocity column ipv, level kp
+  // (as yface)
+  auto yf = [&](int ip, int ipv, int jv, int jvv, int kp) -> float {
+    const int rb = jv - j0 + 1;
+    const float vel = v[TPLS_IDX(g, ipv, (jvv == 0) ? g.ny : jvv, kp - 1)];
+    return weno_up(upwind_pos(vel), PH(ip, rb, kp), PH(ip, rb + 1, kp), PH(ip, rb + 2, kp), PH(ip, rb + 3, kp),
+                   PH(ip, rb + 4, kp), PH(ip, rb + 5, kp));
+  };
+  auto zf = [&](int kw, float c0, float c1, float c2, float c3, float c4, float c5) -> float {
+    if (kw >= 3 && kw <= g.nz - 2) return weno_up(upwind_pos(w[TPLS_IDX(g, ic, jm, kw)]), c0, c1, c2, c3, c4, c5);
+    return (c2 + c3) / 2.0f;
+  };
+  float c0 = PH(ii, rown, k0 - 3), c1 = PH(ii, rown, k0 - 2), c2 = PH(ii, rown, k0 - 1), c3 = PH(ii, rown, k0);
+  float c4 = PH(ii, rown, k0 + 1), c5 = PH(ii, rown, k0 + 2);
+  float zlo = zf(k0 - 1, c0, c1, c2, c3, c4, c5);
+  for (int k = k0; k <= k1; k++) {
+    const int b = k & 1;
+    c0 = c1;
+    c1 = c2;
+    c2 = c3;
+    c3 = c4;
+    c4 = c5;
+    c5 = PH(ii, rown, k + 3);
+    const float xo = xf(ii, ic, rown, jc, k);
+    const float yo = yf(ii, ic, jj, jc, k);
+    xs[b][ty][tx + 1] = xo;
+    ys[b][ty + 1][tx] = yo;
+    if (ty == 0)
+      ys[b][0][tx] = yf(ii, ic, j0 - 1, jc - 1, k);
+    else if (ty == 1 && tx < AT_BY)
+      xs[b][tx][0] = xf(i0 - 1, i0 - 1, tx + 3, jx, k);
+    const float zo = zf(k, c0, c1, c2, c3, c4, c5);
+    __syncthreads();
+    if (act) {
+      const float xl = xs[b][ty][tx], yl = ys[b][ty][tx];
+      const float fxp = u[TPLS_IDX(g, i, jm, k - 1)] * xo;
+      const float fxm = u[TPLS_IDX(g, i - 1, jm, k - 1)] * xl;
+      const float fyp = v[TPLS_IDX(g, i, j, k - 1)] * yo;
+      const float fym = v[TPLS_IDX(g, i, jm, k - 1)] * yl;
+      const float fzp = w[TPLS_IDX(g, i, jm, k)] * zo;
+      const float fzm = w[TPLS_IDX(g, i, jm, k - 1)] * zlo;
+      conv[TPLS_IDX(g, i, j, k)] = (double)((fxp - fxm) * rdx + (fyp - fym) * rdy + (fzp - fzm) * rdz);
+    }
+    zlo = zo;
+  }
+}
+
+// Tensor map of the FP32 phi copy for k_advect_tma: 3-D (x row elements,
+// y rows 0..ny+1, z planes 0..nz+1) over the whole pitched allocation.
+cudaError_t advect_tma_map(const Geo &g, const float *phi32, void *map128) {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  if (!encode) {
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+    if (e != cudaSuccess) return e;
+    if (q != cudaDriverEntryPointSuccess || !fn) return cudaErrorNotSupported;
+    encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }
+  const float *base = phi32 - XOFF;  // the allocation: row starts on 16-byte boundaries
+  const cuuint64_t dims[3] = {(cuuint64_t)g.sy, (cuuint64_t)(g.ny + 2), (cuuint64_t)(g.nz + 2)};
+  const cuuint64_t strides[2] = {(cuuint64_t)g.sy * 4, (cuuint64_t)g.sz * 4};
+  const cuuint32_t box[3] = {AT_W, 1, AT_NZ}, es[3] = {1, 1, 1};
+  if ((reinterpret_cast<uintptr_t>(base) & 15) || (strides[0] & 15) || (strides[1] & 15)) return cudaErrorInvalidValue;
+  const CUresult r = encode(reinterpret_cast<CUtensorMap *>(map128), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
+                            const_cast<float *>(base), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+cudaError_t launch_advect_tma(const Geo &g, const Phys &ph, const void *map128, const float *u2, const float *v2,
+                              const float *w2, double *conv2_phi, double *kto, cudaStream_t st, int arm, int limit,
+                              int one_block) {
+  dim3 blk(AT_BX, AT_BY), grd((g.nx + AT_BX - 1) / AT_BX, (g.ny + AT_BY - 1) / AT_BY, (g.nz + AT_TZ - 1) / AT_TZ);
+  if (one_block) grd = dim3(1, 1, 1);
+  const CUtensorMap &m = *reinterpret_cast<const CUtensorMap *>(map128);
+  k_advect_tma<<<grd, blk, 0, st>>>(m, g, (float)(1.0 / ph.dx), (float)(1.0 / ph.dy), (float)(1.0 / ph.dz), u2, v2,
+                                    w2, conv2_phi, kto, arm, limit);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_advect(const Geo &g, const Phys &ph, const double *phi2,

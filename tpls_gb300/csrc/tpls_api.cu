@@ -19,6 +19,15 @@ namespace {
 
 constexpr int kMaxScratch = 8;
 
+// Stream captures and the calls that act on the whole device (allocation,
+// release, stream and graph creation) are serialised across host threads,
+// so a context can be created or destroyed on one thread while another
+// thread captures a step graph: a call of that kind issued during another
+// thread's capture can invalidate it.  Recursive: destroy runs inside a
+// failed create.
+std::recursive_mutex g_dev_mu;
+using DevLock = std::lock_guard<std::recursive_mutex>;
+
 }  // namespace
 
 // Batched host transfers: per direction a ring of two staging buffers (the
@@ -38,6 +47,12 @@ struct Xfer {
   cudaEvent_t d2h_last = nullptr;  // the last download enqueued
   int next[2] = {0, 0};
   std::map<const void *, cudaEvent_t> host_done;  // last download into each host array
+};
+
+// A registered host array (tpls_register_host): its device mirror.
+struct HostReg {
+  double *mirror;
+  size_t count;  // doubles
 };
 
 struct tpls_ctx {
@@ -79,6 +94,9 @@ struct tpls_ctx {
   double *hbuf = nullptr; // interface height (nx*ny)
   double *stage = nullptr; // host-layout staging of one field ((nx+2)(ny+2)(nz+2))
   struct Xfer *xf = nullptr;  // batched host transfers (tpls_set_fields / tpls_get_fields)
+  std::map<const double *, HostReg> hreg;  // registered host arrays by base address
+  alignas(64) unsigned char advmap[128];  // FP32-mixed: tensor map of phi32 for the TMA advection
+  bool adv_tma = false;
   size_t n_p, n_uv, n_w;  // elements of each allocation (incl. pitch and padding)
   double *part, *scal, *scal_host;
   size_t part_len;
@@ -115,7 +133,7 @@ struct tpls_ctx {
   signed char *scr_flags = nullptr;
 };
 
-enum { SC_ERR_PHI = 0, SC_ERR_U, SC_ERR_V, SC_ERR_W, SC_VOL, SC_N };
+enum { SC_ERR_PHI = 0, SC_ERR_U, SC_ERR_V, SC_ERR_W, SC_VOL, SC_KTO, SC_N };
 
 #define TCK(x)                                                           \
   do {                                                                   \
@@ -159,7 +177,7 @@ static cudaError_t alloc_field(tpls_ctx *c, int rows_before, int rows, int nzp, 
   cudaError_t e = cudaMalloc(&base, n * sizeof(T));
   if (e != cudaSuccess) return e;
   c->allocs.push_back(base);
-  e = cudaMemset(base, 0, n * sizeof(T));
+  e = cudaMemsetAsync(base, 0, n * sizeof(T), c->st);
   if (e != cudaSuccess) return e;
   *out = (T *)base + XOFF + (size_t)c->px * rows_before;
   return cudaSuccess;
@@ -235,28 +253,46 @@ static cudaError_t repack(const double *src, int spitch, double *dst, int dpitch
   k_repack<<<grd, 128, 0, st>>>(src, spitch, dst, dpitch, w, rows);
   return cudaGetLastError();
 }
+// The address the library copies from or to for `count` doubles at a host
+// address: inside a registered host array, the same place in its device
+// mirror; otherwise the host address itself.  Copies use cudaMemcpyDefault,
+// so either kind of address works.
+template <typename P>
+static P hmap(const tpls_ctx *c, P host, size_t count) {
+  if (c->hreg.empty() || !host) return host;
+  const double *h = (const double *)host;
+  auto it = c->hreg.upper_bound(h);
+  if (it == c->hreg.begin()) return host;
+  --it;
+  const double *b = it->first;
+  if (h >= b && (size_t)(h - b) + count <= it->second.count) return (P)(it->second.mirror + (h - b));
+  return host;
+}
+
 static cudaError_t h2d(tpls_ctx *c, double *dev0, const double *host, int nzp) {
   const int w = c->nx + 2, rows = (c->ny + 2) * nzp;
-  cudaError_t e = cudaMemcpyAsync(c->stage, host, sizeof(double) * (size_t)w * rows, cudaMemcpyHostToDevice, c->st);
+  const size_t n = (size_t)w * rows;
+  cudaError_t e = cudaMemcpyAsync(c->stage, hmap(c, host, n), sizeof(double) * n, cudaMemcpyDefault, c->st);
   if (e != cudaSuccess) return e;
   return repack(c->stage, w, dev0, c->px, w, rows, c->st);
 }
 static cudaError_t d2h(tpls_ctx *c, double *host, const double *dev0, int nzp) {
   const int w = c->nx + 2, rows = (c->ny + 2) * nzp;
+  const size_t n = (size_t)w * rows;
   cudaError_t e = repack(dev0, c->px, c->stage, w, w, rows, c->st);
   if (e != cudaSuccess) return e;
-  return cudaMemcpyAsync(host, c->stage, sizeof(double) * (size_t)w * rows, cudaMemcpyDeviceToHost, c->st);
+  return cudaMemcpyAsync(hmap(c, host, n), c->stage, sizeof(double) * n, cudaMemcpyDefault, c->st);
 }
 // viscosity_aug (-1:nx+2,-1:ny+2,0:nz+1) <-> device mu (x 0..nx+1, y -1..ny+2)
 static cudaError_t h2d_mu(tpls_ctx *c, double *mu0, const double *host) {
-  const size_t w = sizeof(double) * (size_t)(c->nx + 2);
-  return cudaMemcpy2DAsync(mu0 - c->px, sizeof(double) * c->px, host + 1, sizeof(double) * (c->nx + 4), w,
-                           (size_t)(c->ny + 4) * (c->nz + 2), cudaMemcpyHostToDevice, c->st);
+  const size_t w = sizeof(double) * (size_t)(c->nx + 2), n = (size_t)(c->nx + 4) * (c->ny + 4) * (c->nz + 2);
+  return cudaMemcpy2DAsync(mu0 - c->px, sizeof(double) * c->px, hmap(c, host, n) + 1, sizeof(double) * (c->nx + 4),
+                           w, (size_t)(c->ny + 4) * (c->nz + 2), cudaMemcpyDefault, c->st);
 }
 static cudaError_t d2h_mu(tpls_ctx *c, double *host, const double *mu0) {
-  const size_t w = sizeof(double) * (size_t)(c->nx + 2);
-  return cudaMemcpy2DAsync(host + 1, sizeof(double) * (c->nx + 4), mu0 - c->px, sizeof(double) * c->px, w,
-                           (size_t)(c->ny + 4) * (c->nz + 2), cudaMemcpyDeviceToHost, c->st);
+  const size_t w = sizeof(double) * (size_t)(c->nx + 2), n = (size_t)(c->nx + 4) * (c->ny + 4) * (c->nz + 2);
+  return cudaMemcpy2DAsync(hmap(c, host, n) + 1, sizeof(double) * (c->nx + 4), mu0 - c->px, sizeof(double) * c->px,
+                           w, (size_t)(c->ny + 4) * (c->nz + 2), cudaMemcpyDefault, c->st);
 }
 
 static Phys phys_from(const tpls_params &p) {
@@ -350,6 +386,7 @@ static void xfer_destroy(Xfer *x) {
 
 int tpls_gpu_destroy(tpls_ctx *c) {
   if (!c) return TPLS_OK;
+  DevLock lk(g_dev_mu);
   xfer_destroy(c->xf);
   c->xf = nullptr;
   if (c->st) cudaStreamSynchronize(c->st);
@@ -358,6 +395,7 @@ int tpls_gpu_destroy(tpls_ctx *c) {
   for (cudaGraphExec_t ge : c->gexec)
     if (ge) cudaGraphExecDestroy(ge);
   poisson_destroy(c->ps);
+  for (auto &kv : c->hreg) cudaFree(kv.second.mirror);
   for (void *p : c->allocs) cudaFree(p);
   if (c->scal_host) cudaFreeHost(c->scal_host);
   if (c->st) cudaStreamDestroy(c->st);
@@ -408,7 +446,7 @@ static int create_impl(int nx, int ny, int nz, const tpls_params *prm, const dou
       const size_t n = (size_t)rec * c->px * (ny + 2) * (q == 2 ? nz + 1 : nz);
       TCK(cudaMalloc(&b, n * sizeof(double)));
       c->allocs.push_back(b);
-      TCK(cudaMemset(b, 0, n * sizeof(double)));
+      TCK(cudaMemsetAsync(b, 0, n * sizeof(double), c->st));
       c->coef[q] = (double *)b;
     }
     TCK(alloc_field(c, 1, ny + 4, nz + 2, &c->mu));
@@ -441,7 +479,7 @@ static int create_impl(int nx, int ny, int nz, const tpls_params *prm, const dou
         const size_t n = (size_t)rec * c->px * (ny + 2) * (q == 2 ? nz + 1 : nz);
         TCK(cudaMalloc(&b, n * sizeof(double)));
         c->allocs.push_back(b);
-        TCK(cudaMemset(b, 0, n * sizeof(double)));
+        TCK(cudaMemsetAsync(b, 0, n * sizeof(double), c->st));
         c->coef[q] = (double *)b;
       }
     }
@@ -456,23 +494,25 @@ static int create_impl(int nx, int ny, int nz, const tpls_params *prm, const dou
       const size_t n = (size_t)c->px * (ny + 2) * (q == 2 ? nz + 1 : nz);
       TCK(cudaMalloc(&b, n * sizeof(float)));
       c->allocs.push_back(b);
-      TCK(cudaMemset(b, 0, n * sizeof(float)));
+      TCK(cudaMemsetAsync(b, 0, n * sizeof(float), c->st));
       c->bdef[q] = (float *)b;
       void *o = nullptr;
       const size_t no = (size_t)(ny + 2) * (nz + 1);
       TCK(cudaMalloc(&o, no * sizeof(float4)));
       c->allocs.push_back(o);
-      TCK(cudaMemset(o, 0, no * sizeof(float4)));
+      TCK(cudaMemsetAsync(o, 0, no * sizeof(float4), c->st));
       c->bco32[q] = (float4 *)o;
     }
     TCK(alloc_field(c, 1, ny + 4, nz + 2, &c->mu32));
+    if (!(prm->flags & TPLS_FLAG_NO_TMA) && advect_tma_map(c->g, c->phi32, c->advmap) == cudaSuccess)
+      c->adv_tma = true;  // else the advection reads phi through the caches
   }
   {
     void *b = nullptr;
     const size_t n = (size_t)c->px * (ny + 2) * (nz + 2) + 64;
     TCK(cudaMalloc(&b, n));
     c->allocs.push_back(b);
-    TCK(cudaMemset(b, 0, n));
+    TCK(cudaMemsetAsync(b, 0, n, c->st));
     c->flags = (signed char *)b + XOFF;
   }
   {
@@ -480,7 +520,7 @@ static int create_impl(int nx, int ny, int nz, const tpls_params *prm, const dou
     TCK(cudaMalloc(&b, sizeof(double) * nz));
     c->allocs.push_back(b);
     c->u_inlet = (double *)b;
-    TCK(cudaMemcpy(c->u_inlet, u_inlet, sizeof(double) * nz, cudaMemcpyHostToDevice));
+    TCK(cudaMemcpyAsync(c->u_inlet, u_inlet, sizeof(double) * nz, cudaMemcpyHostToDevice, c->st));
   }
   {
     void *b = nullptr;
@@ -502,14 +542,17 @@ static int create_impl(int nx, int ny, int nz, const tpls_params *prm, const dou
     TCK(cudaMalloc(&b, sizeof(double) * SC_N));
     c->allocs.push_back(b);
     c->scal = (double *)b;
-    TCK(cudaMemset(c->scal, 0, sizeof(double) * SC_N));
+    TCK(cudaMemsetAsync(c->scal, 0, sizeof(double) * SC_N, c->st));
     TCK(cudaMallocHost(&b, sizeof(double) * SC_N));
     c->scal_host = (double *)b;
   }
   TCK(poisson_create(c->g, 1.0 / (prm->dy * prm->dy), 1.0 / (prm->dx * prm->dx), 1.0 / (prm->dz * prm->dz),
                      c->mixed ? !(prm->fp64_parts & TPLS_PART_MULTIGRID) : (prm->mg_fp32 != 0), &c->ps));
   memset(&c->stats, 0, sizeof(c->stats));
-  TCK(cudaDeviceSynchronize());
+  // the solver set-up's copies ran on the legacy stream, the zero fills on
+  // the context's; no device-wide synchronisation (see g_dev_mu)
+  TCK(cudaStreamSynchronize(cudaStreamLegacy));
+  TCK(cudaStreamSynchronize(c->st));
   return TPLS_OK;
 }
 
@@ -582,6 +625,7 @@ int tpls_gpu_create(int nx, int ny, int nz, const tpls_params *prm, const double
   if (prm->idm == TPLS_IDM_DIM &&
       !(prm->precision == TPLS_PREC_FP64 && prm->epn > 0 && prm->pe > 0 && prm->max_iteration_dim >= 0))
     return TPLS_ERR_ARG;
+  DevLock lk(g_dev_mu);
   tpls_ctx *c = new tpls_ctx();
   int s = create_impl(nx, ny, nz, prm, u_inlet, c);
   if (s != TPLS_OK) {
@@ -625,6 +669,7 @@ int tpls_get_field(tpls_ctx *c, int f, double *host) {
 
 static cudaError_t xfer_init(tpls_ctx *c) {
   if (c->xf) return cudaSuccess;
+  DevLock lk(g_dev_mu);
   Xfer *x = new Xfer();
   cudaError_t e = cudaStreamCreateWithFlags(&x->h2d, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&x->d2h, cudaStreamNonBlocking);
@@ -666,8 +711,8 @@ int tpls_set_fields(tpls_ctx *c, int n, const int *fields, const double *const *
     TCK(cudaStreamWaitEvent(x->h2d, x->free_ev[0][q], 0));
     auto hd = x->host_done.find(hosts[i]);  // a download into this array still in flight
     if (hd != x->host_done.end()) TCK(cudaStreamWaitEvent(x->h2d, hd->second, 0));
-    TCK(cudaMemcpyAsync(x->slot[0][q], hosts[i], sizeof(double) * (size_t)w * rows, cudaMemcpyHostToDevice,
-                        x->h2d));
+    TCK(cudaMemcpyAsync(x->slot[0][q], hmap(c, hosts[i], (size_t)w * rows), sizeof(double) * (size_t)w * rows,
+                        cudaMemcpyDefault, x->h2d));
     TCK(cudaEventRecord(x->ready_ev[0][q], x->h2d));
     TCK(cudaStreamWaitEvent(c->st, x->ready_ev[0][q], 0));
     LCK(c, repack(x->slot[0][q], w, field_ptr(c, f), c->px, w, rows, c->st));
@@ -697,14 +742,40 @@ int tpls_get_fields(tpls_ctx *c, int n, const int *fields, double *const *hosts)
     LCK(c, repack(field_ptr(c, f), c->px, x->slot[1][q], w, w, rows, c->st));
     TCK(cudaEventRecord(x->ready_ev[1][q], c->st));
     TCK(cudaStreamWaitEvent(x->d2h, x->ready_ev[1][q], 0));
-    TCK(cudaMemcpyAsync(hosts[i], x->slot[1][q], sizeof(double) * (size_t)w * rows, cudaMemcpyDeviceToHost,
-                        x->d2h));
+    TCK(cudaMemcpyAsync(hmap(c, hosts[i], (size_t)w * rows), x->slot[1][q], sizeof(double) * (size_t)w * rows,
+                        cudaMemcpyDefault, x->d2h));
     TCK(cudaEventRecord(x->free_ev[1][q], x->d2h));
     cudaEvent_t &ev = x->host_done[hosts[i]];
     if (!ev) TCK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
     TCK(cudaEventRecord(ev, x->d2h));
   }
   if (n > 0) TCK(cudaEventRecord(x->d2h_last, x->d2h));
+  return TPLS_OK;
+}
+
+int tpls_selftest_wait_limit(tpls_ctx *c, int *timeouts, int *nan_out) {
+  if (!c || !timeouts || !nan_out) return TPLS_ERR_ARG;
+  if (!c->adv_tma) return TPLS_ERR_STATE;
+  DevLock lk(g_dev_mu);
+  TCK(cudaStreamSynchronize(c->st));
+  double *conv = nullptr, *kto = nullptr;
+  const size_t n = c->n_p;
+  cudaError_t e = cudaMalloc(&conv, sizeof(double) * n);
+  if (e == cudaSuccess) e = cudaMalloc(&kto, sizeof(double));
+  if (e == cudaSuccess) e = cudaMemsetAsync(conv, 0, sizeof(double) * n, c->st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(kto, 0, sizeof(double), c->st);
+  if (e == cudaSuccess)  // no load issued: the block's wait runs out after 64 polls
+    e = launch_advect_tma(c->g, c->ph, c->advmap, c->u32, c->v32, c->w32, conv + XOFF, kto, c->st, 0, 64, 1);
+  double h[2] = {0.0, 0.0};
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&h[0], kto, sizeof(double), cudaMemcpyDeviceToHost, c->st);
+  if (e == cudaSuccess)  // the first cell of the block's tile, (1, 1, 1)
+    e = cudaMemcpyAsync(&h[1], conv + XOFF + TPLS_IDX(c->g, 1, 1, 1), sizeof(double), cudaMemcpyDeviceToHost, c->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+  if (conv) cudaFree(conv);
+  if (kto) cudaFree(kto);
+  TCK(e);
+  *timeouts = (int)h[0];
+  *nan_out = (h[1] != h[1]) ? 1 : 0;
   return TPLS_OK;
 }
 
@@ -719,6 +790,63 @@ int tpls_sync(tpls_ctx *c) {
   if (!c) return TPLS_ERR_ARG;
   TCK(xfer_quiesce(c));
   TCK(cudaStreamSynchronize(c->st));
+  return TPLS_OK;
+}
+
+int tpls_register_host(tpls_ctx *c, double *host, long long count) {
+  if (!c || !host || count <= 0) return TPLS_ERR_ARG;
+  const double *h = host;
+  auto it = c->hreg.upper_bound(h);  // no overlap with a registered array
+  if (it != c->hreg.end() && it->first < h + count) return TPLS_ERR_ARG;
+  if (it != c->hreg.begin()) {
+    --it;
+    if (h < it->first + it->second.count) return TPLS_ERR_ARG;
+  }
+  DevLock lk(g_dev_mu);
+  TCK(xfer_quiesce(c));
+  TCK(cudaStreamSynchronize(c->st));
+  void *m = nullptr;
+  TCK(cudaMalloc(&m, sizeof(double) * (size_t)count));
+  const cudaError_t e = cudaMemcpyAsync(m, host, sizeof(double) * (size_t)count, cudaMemcpyDefault, c->st);
+  const cudaError_t e2 = (e == cudaSuccess) ? cudaStreamSynchronize(c->st) : e;
+  if (e2 != cudaSuccess) {
+    cudaFree(m);
+    return TPLS_ERR_CUDA_BASE + (int)e2;
+  }
+  c->hreg[h] = HostReg{(double *)m, (size_t)count};
+  return TPLS_OK;
+}
+
+// host == nullptr: every registered array
+static int host_refresh(tpls_ctx *c, const double *host, bool down) {
+  if (!c) return TPLS_ERR_ARG;
+  TCK(xfer_quiesce(c));
+  bool found = false;
+  for (auto &kv : c->hreg) {
+    if (host && kv.first != host) continue;
+    found = true;
+    double *h = const_cast<double *>(kv.first);
+    const size_t bytes = sizeof(double) * kv.second.count;
+    if (down) TCK(cudaMemcpyAsync(h, kv.second.mirror, bytes, cudaMemcpyDefault, c->st));
+    else TCK(cudaMemcpyAsync(kv.second.mirror, h, bytes, cudaMemcpyDefault, c->st));
+  }
+  if (host && !found) return TPLS_ERR_ARG;
+  TCK(cudaStreamSynchronize(c->st));
+  return TPLS_OK;
+}
+
+int tpls_download_host(tpls_ctx *c, double *host) { return host_refresh(c, host, true); }
+int tpls_upload_host(tpls_ctx *c, const double *host) { return host_refresh(c, host, false); }
+
+int tpls_unregister_host(tpls_ctx *c, double *host) {
+  if (!c || !host) return TPLS_ERR_ARG;
+  auto it = c->hreg.find(host);
+  if (it == c->hreg.end()) return TPLS_ERR_ARG;
+  DevLock lk(g_dev_mu);
+  TCK(xfer_quiesce(c));
+  TCK(cudaStreamSynchronize(c->st));
+  cudaFree(it->second.mirror);
+  c->hreg.erase(it);
   return TPLS_OK;
 }
 
@@ -1032,7 +1160,10 @@ static int mixed_front(tpls_ctx *c) {
       LCK(c, launch_advect(g, ph, c->phi2, c->u2, c->v2, c->w2, c->conv_phi[s2], st));
     } else {
       LCK(c, launch_to_float(c->phi2 - XOFF, c->phi32 - XOFF, c->n_p, st));
-      LCK(c, launch_advect(g, ph, (const float *)c->phi32, c->u32, c->v32, c->w32, c->conv_phi[s2], st));
+      if (c->adv_tma)  // phi tiles staged by TMA (same arithmetic, bit-identical)
+        LCK(c, launch_advect_tma(g, ph, c->advmap, c->u32, c->v32, c->w32, c->conv_phi[s2], c->scal + SC_KTO, st));
+      else
+        LCK(c, launch_advect(g, ph, (const float *)c->phi32, c->u32, c->v32, c->w32, c->conv_phi[s2], st));
     }
   }
   {
@@ -1150,6 +1281,7 @@ static int step_graph(tpls_ctx *c) {
   if (s) return s;
   const int ph = c->phase;
   if (!c->gexec[ph]) {
+    DevLock lk(g_dev_mu);
     const long l0 = c->launches;
     TCK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
     c->capturing = true;
@@ -1384,6 +1516,7 @@ extern "C" {
 
 int tpls_batch_destroy(tpls_batch *b) {
   if (!b) return TPLS_OK;
+  DevLock lk(g_dev_mu);
   if (b->st) cudaStreamSynchronize(b->st);
   for (cudaGraphExec_t ge : b->gexec)
     if (ge) cudaGraphExecDestroy(ge);
@@ -1407,6 +1540,7 @@ int tpls_batch_create(tpls_ctx *const *ctxs, int n, tpls_batch **out) {
     for (int r = 0; r < q; r++)
       if (ctxs[r] == ctxs[q]) return TPLS_ERR_ARG;
   }
+  DevLock lk(g_dev_mu);
   tpls_batch *b = new tpls_batch();
   b->m.assign(ctxs, ctxs + n);
   cudaError_t e = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking);
@@ -1452,6 +1586,7 @@ static int batch_capture(tpls_batch *b, int ph) {
   std::vector<long> l0(n);
   for (int q = 0; q < n; q++) l0[q] = b->m[q]->launches;
   b->n_multi = 0;
+  DevLock lk(g_dev_mu);
   TCK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
   int s = TPLS_OK;
   cudaError_t e = cudaEventRecord(b->fork, b->st);
@@ -1538,12 +1673,14 @@ int tpls_batch_multi_sweeps(tpls_batch *b, int on) {
             pf[q + 1] = pf[q] + (kind == 0 ? sweep4_tiles(comp, b->m[q]->g) : odd_tiles(comp, b->m[q]->g));
           b->total[kind][comp] = pf[n];
         }
+      DevLock lk(g_dev_mu);
       TCK(cudaMalloc(&b->dmem, sizeof(SweepMember) * n));
       TCK(cudaMalloc(&b->dprefix, sizeof(int) * pre.size()));
       TCK(cudaMalloc(&b->dctr, 2 * sizeof(unsigned)));
       TCK(cudaMemcpy(b->dmem, hm.data(), sizeof(SweepMember) * n, cudaMemcpyHostToDevice));
       TCK(cudaMemcpy(b->dprefix, pre.data(), sizeof(int) * pre.size(), cudaMemcpyHostToDevice));
       TCK(cudaMemset(b->dctr, 0, 2 * sizeof(unsigned)));
+      TCK(cudaStreamSynchronize(cudaStreamLegacy));  // before any stream of the batch reads them
       int sms = 0;
       TCK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev0));
       b->nblocks = 8 * sms;
@@ -1712,6 +1849,7 @@ int tpls_get_stats(tpls_ctx *c, tpls_stats *out) {
   c->stats.err_v = c->scal_host[SC_ERR_V];
   c->stats.err_w = c->scal_host[SC_ERR_W];
   c->stats.liquid_volume = c->scal_host[SC_VOL] * c->prm.dx * c->prm.dy * c->prm.dz;
+  c->stats.kernel_timeouts = (int)c->scal_host[SC_KTO];
   *out = c->stats;
   c->stats.p_worst = 0;
   return TPLS_OK;
@@ -1784,6 +1922,7 @@ static int check_bounds(const tpls_ctx *c, const int *sx, const int *ex, const i
 
 static int scratch(tpls_ctx *c) {
   if (c->scr[0]) return TPLS_OK;
+  DevLock lk(g_dev_mu);
   for (int q = 0; q < kMaxScratch; q++) TCK(alloc_p(c, &c->scr[q]));
   TCK(alloc_field(c, 1, c->ny + 4, c->nz + 2, &c->scr_mu));
   void *b = nullptr;
@@ -2168,7 +2307,7 @@ int tpls_get_uvw_pres(tpls_ctx *c, double *u3, double *v3, double *w3, const dou
   TCK(h2d(c, V, v3, nz));
   TCK(h2d(c, W, w3, nz + 1));
   TCK(h2d(c, P, p, nz + 2));
-  TCK(cudaMemcpyAsync(c->scr_uin, u_inlet, sizeof(double) * nz, cudaMemcpyHostToDevice, c->st));
+  TCK(cudaMemcpyAsync(c->scr_uin, hmap(c, u_inlet, nz), sizeof(double) * nz, cudaMemcpyDefault, c->st));
   LCK(c, launch_project(c->g, ph, U, V, W, P, c->scr_uin, UO, VO, WO, c->st));
   // the reference updates rows 1..ny only; its ghost rows keep their values
   const size_t w = sizeof(double) * (size_t)(c->nx + 2);
@@ -2177,9 +2316,10 @@ int tpls_get_uvw_pres(tpls_ctx *c, double *u3, double *v3, double *w3, const dou
     double *srcs[3] = {UO, VO, WO};
     for (int q = 0; q < 3; q++) {
       if (q < 2 && k == nz) continue;
-      TCK(cudaMemcpy2DAsync(dsts[q] + (size_t)(c->nx + 2) * ((size_t)(c->ny + 2) * k + 1), w,
+      double *d = hmap(c, dsts[q] + (size_t)(c->nx + 2) * ((size_t)(c->ny + 2) * k + 1), (size_t)(c->nx + 2) * c->ny);
+      TCK(cudaMemcpy2DAsync(d, w,
                             srcs[q] + (size_t)c->g.sz * k + c->g.sy, sizeof(double) * c->px, w, c->ny,
-                            cudaMemcpyDeviceToHost, c->st));
+                            cudaMemcpyDefault, c->st));
     }
   }
   TCK(cudaStreamSynchronize(c->st));
@@ -2201,7 +2341,7 @@ int tpls_pressure_solve(tpls_ctx *c, double *pres, const double *pres_old, const
   TCK(h2d(c, PO, pres_old, nz + 2));
   TCK(h2d(c, R, rhs_p, nz + 2));
   TCK(h2d(c, U, u3, nz));
-  TCK(cudaMemcpyAsync(c->scr_uin, u_inlet, sizeof(double) * nz, cudaMemcpyHostToDevice, c->st));
+  TCK(cudaMemcpyAsync(c->scr_uin, hmap(c, u_inlet, nz), sizeof(double) * nz, cudaMemcpyDefault, c->st));
   const double rt = (rtol && *rtol > 0) ? *rtol : c->prm.p_rtol;
   const int mi = (maxits && *maxits > 0) ? *maxits : c->prm.p_maxits;
   double bn = 0.0;

@@ -37,6 +37,14 @@ cudaError_t launch_advect(const Geo &g, const Phys &ph, const float *phi2,
                           const float *u2, const float *v2, const float *w2,
                           double *conv2_phi, cudaStream_t st);
 cudaError_t launch_to_float(const double *a, float *b, size_t n, cudaStream_t st);
+// The same FP32 advection with phi staged by TMA: map128 = a 128-byte,
+// 64-byte-aligned tensor map made by advect_tma_map for the FP32 phi copy;
+// kto counts blocks whose wait for the staged tile ran out (limit polls).
+// arm = 0 and one_block = 1: the self-test of that limit (nothing issued).
+cudaError_t advect_tma_map(const Geo &g, const float *phi32, void *map128);
+cudaError_t launch_advect_tma(const Geo &g, const Phys &ph, const void *map128, const float *u2, const float *v2,
+                              const float *w2, double *conv2_phi, double *kto, cudaStream_t st, int arm = 1,
+                              int limit = 1 << 22, int one_block = 0);
 
 // cahn_hilliard_solver.f90:41-382 dim (diffuse interface), see k_dim.cu.
 // phi + add is the concentration C (the driver's phi2 + 0.5).
