@@ -16,7 +16,7 @@ NX, NY, NZ = 37, 19, 23
 
 def _inputs(g, st, seed):
     rng = np.random.default_rng(seed)
-    u3, v3, w3 = (np.array(st[k], order="F") for k in ("U3", "V3", "W3"))
+    u3, v3, w3 = (np.array(st[k], order="F") for k in ("U2", "V2", "W2"))
     rhs_u = np.asfortranarray(rng.normal(scale=1e-3, size=g.shape("uv")))
     va = np.zeros(g.shape("va"), order="F")
     return {"u3": u3, "v3": v3, "w3": w3, "rhs_u": rhs_u, "va": va,
@@ -67,7 +67,7 @@ def test_registry_upload_download_and_overlap():
     p, uin, st = make_case("A", nx=NX, ny=NY, nz=NZ)
     g = TplsGpu(NX, NY, NZ, p, uin)
     try:
-        u = np.array(st["U3"], order="F")
+        u = np.array(st["U2"], order="F")
         g.register_host(u)
         with pytest.raises(TplsError):
             g.register_host(u)  # overlaps the registered range
