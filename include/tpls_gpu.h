@@ -19,7 +19,9 @@
  *   - calls on one context are single-threaded and stream-ordered; separate
  *     contexts may be driven from separate host threads.
  * The per-routine entries take HOST arrays (copied in and out around the
- * kernels); tpls_step() runs whole timesteps on device-resident state.
+ * kernels, or standing for device mirrors once registered with
+ * tpls_register_host); tpls_step() runs whole timesteps on device-resident
+ * state.
  */
 #ifndef TPLS_GPU_H
 #define TPLS_GPU_H
@@ -146,15 +148,17 @@ int tpls_get_dims(const tpls_ctx *ctx, int *nx, int *ny, int *nz);
 /* Several fields per call (no counterpart in the reference, which keeps its
  * arrays on the host): fields[i] to / from host[i], in the layouts of
  * tpls_set_field / tpls_get_field, without a host wait between fields.
- * The copies run on the context's own copy streams through two staging
- * buffers per direction (three allocated on the first call), so successive
- * fields overlap, and an upload of an array still being downloaded waits
- * for that download on the device: a get of the state followed by a set
- * of the same arrays runs both copy directions at once.  Both calls return
- * once the copies are enqueued: steps enqueued afterwards run after the
- * uploads; the host arrays of a get may be read after tpls_sync (or
- * tpls_xfer_join and a wait on the context's stream).  Pinned host memory
- * gives the link's full speed. */
+ * Downloads are 2-D copies from the device fields on one copy stream;
+ * uploads go through two staging buffers (one allocated on the first call)
+ * on another and are repacked on the context's stream, so successive
+ * fields overlap.  An upload of an array still being downloaded, or into a
+ * field still being downloaded, waits for that download on the device: a
+ * get of the state followed by a set of the same arrays runs both copy
+ * directions at once.  Both calls return once the copies are enqueued:
+ * steps enqueued afterwards run after the uploads and do not overwrite a
+ * field before its download has read it; the host arrays of a get may be
+ * read after tpls_sync (or tpls_xfer_join and a wait on the context's
+ * stream).  Pinned host memory gives the link's full speed. */
 int tpls_set_fields(tpls_ctx *ctx, int n, const int *fields,
                     const double *const *host);
 int tpls_get_fields(tpls_ctx *ctx, int n, const int *fields,

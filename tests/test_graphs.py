@@ -111,3 +111,24 @@ def test_batched_transfers_match_single_field_path():
         assert np.array_equal(out[k], sa[k]), k
     a.close()
     b.close()
+
+
+@pytest.mark.gpu
+def test_download_is_not_overwritten_by_the_next_steps():
+    """tpls_get_fields returns before its copies finish; steps enqueued right
+    after it (graph-launched and async) wait for them, so the host arrays
+    hold the state of the call, not of a later step."""
+    nx, ny, nz = 64, 32, 48
+    params, uin, st = make_case("A", nx=nx, ny=ny, nz=nz)
+    g = TplsGpu(nx, ny, nz, params, uin)
+    g.set_state(st)
+    g.step(1)
+    ref = g.get_state()
+    bufs = {k: np.zeros_like(v, order="F") for k, v in ref.items()}
+    g.get_fields_into(bufs)
+    g.step_async(3)  # no host wait between the download and the steps
+    g.sync()
+    for k in ref:
+        assert np.array_equal(bufs[k], ref[k]), k
+    assert not np.array_equal(g.get_field("PHI2"), ref["PHI2"])
+    g.close()

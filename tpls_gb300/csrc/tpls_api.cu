@@ -30,22 +30,28 @@ using DevLock = std::lock_guard<std::recursive_mutex>;
 
 }  // namespace
 
-// Batched host transfers: per direction a ring of two staging buffers (the
-// context's own staging buffer is one of them, the other three are
-// allocated on first use) and one copy stream.  A field's copy and its repack run on
-// different streams, ordered by events, so successive fields overlap and a
-// download followed by an upload of the same host arrays uses both copy
-// directions at once.
+// Batched host transfers.  Downloads are 2-D copies straight from a field's
+// pitched rows into the host layout on their own stream (no staging, no
+// repack); uploads go through a ring of two contiguous staging buffers (the
+// context's own staging buffer and one allocated on first use) on a second
+// stream and are repacked into the field on the context's stream (a 2-D
+// upload of rows this short runs at a fraction of the link's rate).  A field
+// uploaded after a download into the same host array, or from the same
+// field, waits for that download on the device, so a download of the state
+// followed by an upload of the same arrays uses both copy directions at once.
+// Later work on the context's stream waits for pending downloads lazily
+// (xfer_fence), so those uploads do not queue behind them.
 struct Xfer {
-  // per direction (0: uploads, 1: downloads) a ring of K staging slots, so a
-  // download and an upload never wait for each other's slots
-  static constexpr int K = 2;
+  static constexpr int K = 2;  // upload staging slots
   cudaStream_t h2d = nullptr, d2h = nullptr;
-  double *slot[2][K] = {{nullptr, nullptr}, {nullptr, nullptr}};
-  cudaEvent_t free_ev[2][K] = {{nullptr, nullptr}, {nullptr, nullptr}};   // the slot may be refilled
-  cudaEvent_t ready_ev[2][K] = {{nullptr, nullptr}, {nullptr, nullptr}};  // the slot holds its data
-  cudaEvent_t d2h_last = nullptr;  // the last download enqueued
-  int next[2] = {0, 0};
+  double *slot[K] = {nullptr, nullptr};
+  cudaEvent_t free_ev[K] = {nullptr, nullptr};   // the slot may be refilled
+  cudaEvent_t ready_ev[K] = {nullptr, nullptr};  // the slot holds its data
+  cudaEvent_t st_ev = nullptr;                   // the context's stream at a download call
+  cudaEvent_t d2h_last = nullptr;                // the last download enqueued
+  cudaEvent_t field_dl[TPLS_F_COUNT] = {};       // the last download from each field
+  bool dl_pending = false;                       // downloads the context's stream has not waited for
+  int next = 0;
   std::map<const void *, cudaEvent_t> host_done;  // last download into each host array
 };
 
@@ -372,12 +378,14 @@ static void xfer_destroy(Xfer *x) {
   if (!x) return;
   if (x->h2d) cudaStreamSynchronize(x->h2d);
   if (x->d2h) cudaStreamSynchronize(x->d2h);
-  for (int d = 0; d < 2; d++)
-    for (int q = 0; q < Xfer::K; q++) {
-      if (x->free_ev[d][q]) cudaEventDestroy(x->free_ev[d][q]);
-      if (x->ready_ev[d][q]) cudaEventDestroy(x->ready_ev[d][q]);
-    }
+  for (int q = 0; q < Xfer::K; q++) {
+    if (x->free_ev[q]) cudaEventDestroy(x->free_ev[q]);
+    if (x->ready_ev[q]) cudaEventDestroy(x->ready_ev[q]);
+  }
+  for (cudaEvent_t e : x->field_dl)
+    if (e) cudaEventDestroy(e);
   for (auto &kv : x->host_done) cudaEventDestroy(kv.second);
+  if (x->st_ev) cudaEventDestroy(x->st_ev);
   if (x->d2h_last) cudaEventDestroy(x->d2h_last);
   if (x->h2d) cudaStreamDestroy(x->h2d);
   if (x->d2h) cudaStreamDestroy(x->d2h);
@@ -643,7 +651,16 @@ static cudaError_t xfer_quiesce(tpls_ctx *c) {
   if (!c->xf) return cudaSuccess;
   cudaError_t e = cudaStreamSynchronize(c->xf->h2d);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->xf->d2h);
+  if (e == cudaSuccess) c->xf->dl_pending = false;
   return e;
+}
+
+// Work enqueued on the context's stream after tpls_get_fields may overwrite
+// the fields those downloads read: it waits for them first.
+static cudaError_t xfer_fence(tpls_ctx *c) {
+  if (!c->xf || !c->xf->dl_pending) return cudaSuccess;
+  c->xf->dl_pending = false;
+  return cudaStreamWaitEvent(c->st, c->xf->d2h_last, 0);
 }
 
 int tpls_set_field(tpls_ctx *c, int f, const double *host) {
@@ -674,21 +691,23 @@ static cudaError_t xfer_init(tpls_ctx *c) {
   cudaError_t e = cudaStreamCreateWithFlags(&x->h2d, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&x->d2h, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&x->d2h_last, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&x->st_ev, cudaEventDisableTiming);
+  for (int f = 0; f < TPLS_F_COUNT && e == cudaSuccess; f++)
+    e = cudaEventCreateWithFlags(&x->field_dl[f], cudaEventDisableTiming);
   const size_t n = (size_t)(c->nx + 2) * (c->ny + 2) * (c->nz + 2);
-  x->slot[1][0] = c->stage;
-  for (int d = 0; d < 2 && e == cudaSuccess; d++)
-    for (int q = 0; q < Xfer::K && e == cudaSuccess; q++) {
-      if (!x->slot[d][q]) {
-        void *b = nullptr;
-        e = cudaMalloc(&b, n * sizeof(double));
-        if (e == cudaSuccess) {
-          c->allocs.push_back(b);
-          x->slot[d][q] = (double *)b;
-        }
+  x->slot[0] = c->stage;
+  for (int q = 0; q < Xfer::K && e == cudaSuccess; q++) {
+    if (!x->slot[q]) {
+      void *b = nullptr;
+      e = cudaMalloc(&b, n * sizeof(double));
+      if (e == cudaSuccess) {
+        c->allocs.push_back(b);
+        x->slot[q] = (double *)b;
       }
-      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&x->free_ev[d][q], cudaEventDisableTiming);
-      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&x->ready_ev[d][q], cudaEventDisableTiming);
     }
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&x->free_ev[q], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&x->ready_ev[q], cudaEventDisableTiming);
+  }
   if (e != cudaSuccess) {
     xfer_destroy(x);
     return e;
@@ -706,17 +725,18 @@ int tpls_set_fields(tpls_ctx *c, int n, const int *fields, const double *const *
   for (int i = 0; i < n; i++) {
     const int f = fields[i], nzp = nz_planes(field_kind(f), c->nz);
     const int w = c->nx + 2, rows = (c->ny + 2) * nzp;
-    const int q = x->next[0];
-    x->next[0] = (q + 1) % Xfer::K;
-    TCK(cudaStreamWaitEvent(x->h2d, x->free_ev[0][q], 0));
+    const int q = x->next;
+    x->next = (q + 1) % Xfer::K;
+    TCK(cudaStreamWaitEvent(x->h2d, x->free_ev[q], 0));
     auto hd = x->host_done.find(hosts[i]);  // a download into this array still in flight
     if (hd != x->host_done.end()) TCK(cudaStreamWaitEvent(x->h2d, hd->second, 0));
-    TCK(cudaMemcpyAsync(x->slot[0][q], hmap(c, hosts[i], (size_t)w * rows), sizeof(double) * (size_t)w * rows,
+    TCK(cudaMemcpyAsync(x->slot[q], hmap(c, hosts[i], (size_t)w * rows), sizeof(double) * (size_t)w * rows,
                         cudaMemcpyDefault, x->h2d));
-    TCK(cudaEventRecord(x->ready_ev[0][q], x->h2d));
-    TCK(cudaStreamWaitEvent(c->st, x->ready_ev[0][q], 0));
-    LCK(c, repack(x->slot[0][q], w, field_ptr(c, f), c->px, w, rows, c->st));
-    TCK(cudaEventRecord(x->free_ev[0][q], c->st));
+    TCK(cudaEventRecord(x->ready_ev[q], x->h2d));
+    TCK(cudaStreamWaitEvent(c->st, x->ready_ev[q], 0));
+    TCK(cudaStreamWaitEvent(c->st, x->field_dl[f], 0));  // a download from this field still in flight
+    LCK(c, repack(x->slot[q], w, field_ptr(c, f), c->px, w, rows, c->st));
+    TCK(cudaEventRecord(x->free_ev[q], c->st));
   }
   if (n > 0) c->need_exchange = true;
   return TPLS_OK;
@@ -733,23 +753,21 @@ int tpls_get_fields(tpls_ctx *c, int n, const int *fields, double *const *hosts)
     for (auto &kv : x->host_done) cudaEventDestroy(kv.second);
     x->host_done.clear();
   }
+  if (n == 0) return TPLS_OK;
+  TCK(cudaEventRecord(x->st_ev, c->st));  // the fields as of this call
+  TCK(cudaStreamWaitEvent(x->d2h, x->st_ev, 0));
   for (int i = 0; i < n; i++) {
     const int f = fields[i], nzp = nz_planes(field_kind(f), c->nz);
-    const int w = c->nx + 2, rows = (c->ny + 2) * nzp;
-    const int q = x->next[1];
-    x->next[1] = (q + 1) % Xfer::K;
-    TCK(cudaStreamWaitEvent(c->st, x->free_ev[1][q], 0));
-    LCK(c, repack(field_ptr(c, f), c->px, x->slot[1][q], w, w, rows, c->st));
-    TCK(cudaEventRecord(x->ready_ev[1][q], c->st));
-    TCK(cudaStreamWaitEvent(x->d2h, x->ready_ev[1][q], 0));
-    TCK(cudaMemcpyAsync(hmap(c, hosts[i], (size_t)w * rows), x->slot[1][q], sizeof(double) * (size_t)w * rows,
-                        cudaMemcpyDefault, x->d2h));
-    TCK(cudaEventRecord(x->free_ev[1][q], x->d2h));
+    const size_t w = (size_t)(c->nx + 2), rows = (size_t)(c->ny + 2) * nzp;
+    TCK(cudaMemcpy2DAsync(hmap(c, hosts[i], w * rows), sizeof(double) * w, field_ptr(c, f),
+                          sizeof(double) * (size_t)c->px, sizeof(double) * w, rows, cudaMemcpyDefault, x->d2h));
+    TCK(cudaEventRecord(x->field_dl[f], x->d2h));
     cudaEvent_t &ev = x->host_done[hosts[i]];
     if (!ev) TCK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
     TCK(cudaEventRecord(ev, x->d2h));
   }
-  if (n > 0) TCK(cudaEventRecord(x->d2h_last, x->d2h));
+  TCK(cudaEventRecord(x->d2h_last, x->d2h));
+  x->dl_pending = true;
   return TPLS_OK;
 }
 
@@ -783,6 +801,7 @@ int tpls_xfer_join(tpls_ctx *c) {
   if (!c) return TPLS_ERR_ARG;
   if (!c->xf) return TPLS_OK;
   TCK(cudaStreamWaitEvent(c->st, c->xf->d2h_last, 0));
+  c->xf->dl_pending = false;
   return TPLS_OK;
 }
 
@@ -955,6 +974,7 @@ static int momentum(tpls_ctx *c, int comp, CS coef, T **X, int max_iteration, co
 // (advect_phi.f90:317-322 / main_ns_hybrid.F90:728-733); later steps keep
 // them current in the kernels that write the state.
 static int prologue(tpls_ctx *c) {
+  TCK(xfer_fence(c));
   if (c->need_exchange) {
     LCK(c, launch_exchange(c->g, c->u2, c->nz, c->st));
     LCK(c, launch_exchange(c->g, c->v2, c->nz, c->st));
@@ -1396,6 +1416,7 @@ static void destroy_graphs(tpls_ctx *c) {
 
 int tpls_autotune(tpls_ctx *c, int reps) {
   if (!c || c->capturing || reps < 1) return TPLS_ERR_ARG;
+  TCK(xfer_fence(c));
   const bool f32 = c->mixed && !(c->prm.fp64_parts & TPLS_PART_MOMENTUM);
   const std::array<int, 4> key = {c->nx, c->ny, c->nz, f32 ? 1 : 0};
   {
