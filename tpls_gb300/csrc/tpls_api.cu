@@ -275,19 +275,26 @@ static P hmap(const tpls_ctx *c, P host, size_t count) {
   return host;
 }
 
+// A registered array's mirror already holds the host layout on the device:
+// the repack reads or writes it directly instead of through the staging
+// buffer.
 static cudaError_t h2d(tpls_ctx *c, double *dev0, const double *host, int nzp) {
   const int w = c->nx + 2, rows = (c->ny + 2) * nzp;
   const size_t n = (size_t)w * rows;
-  cudaError_t e = cudaMemcpyAsync(c->stage, hmap(c, host, n), sizeof(double) * n, cudaMemcpyDefault, c->st);
+  const double *src = hmap(c, host, n);
+  if (src != host) return repack(src, w, dev0, c->px, w, rows, c->st);
+  cudaError_t e = cudaMemcpyAsync(c->stage, host, sizeof(double) * n, cudaMemcpyHostToDevice, c->st);
   if (e != cudaSuccess) return e;
   return repack(c->stage, w, dev0, c->px, w, rows, c->st);
 }
 static cudaError_t d2h(tpls_ctx *c, double *host, const double *dev0, int nzp) {
   const int w = c->nx + 2, rows = (c->ny + 2) * nzp;
   const size_t n = (size_t)w * rows;
+  double *dst = hmap(c, host, n);
+  if (dst != host) return repack(dev0, c->px, dst, w, w, rows, c->st);
   cudaError_t e = repack(dev0, c->px, c->stage, w, w, rows, c->st);
   if (e != cudaSuccess) return e;
-  return cudaMemcpyAsync(hmap(c, host, n), c->stage, sizeof(double) * n, cudaMemcpyDefault, c->st);
+  return cudaMemcpyAsync(host, c->stage, sizeof(double) * n, cudaMemcpyDeviceToHost, c->st);
 }
 // viscosity_aug (-1:nx+2,-1:ny+2,0:nz+1) <-> device mu (x 0..nx+1, y -1..ny+2)
 static cudaError_t h2d_mu(tpls_ctx *c, double *mu0, const double *host) {
