@@ -229,6 +229,11 @@ def run_gpu(args, ws, rank, local) -> dict | None:
         buf[...] = a
         host[k] = buf
     bi = sum(a.nbytes for a in host.values())
+    # untimed round trip: the batched transfers' streams, events and staging
+    # buffer are created on first use (the state is set to itself)
+    g.get_fields_into(host)
+    g.set_fields(host)
+    g.sync()
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
