@@ -139,23 +139,24 @@ def _algorithmic_bytes(nx, ny, nz, mom, esz=8):
     return jac, sor_odd, 3 * outer, 6 * n_odd
 
 
-def _profile_figure(tag: str, kernel: str, workload: str) -> dict | None:
+def _profile_figure(tag: str, kernel: str, workload: str | None) -> dict | None:
     """A figure from the committed ncu summaries: lines
     '<tag> <kernel> <workload>: <number> build <digest>' (tag 'traffic' =
     DRAM bytes per launch, 'fp64pipe' = FP64 pipe active % of peak; digest =
-    tpls_gb300.build.source_digest() of the build the capture was taken of).
-    Returns {"value", "file", "build", "current"}: `current` says whether the
-    capture is of the sources this run was built from.  ncu figures are not
-    measured by this run; a figure whose build differs is reported only
-    under its capture record."""
+    tpls_gb300.build.source_digest() of the build the capture was taken of;
+    workload None: the first line of any workload).
+    Returns {"value", "file", "build", "current", "workload"}: `current`
+    says whether the capture is of the sources this run was built from.
+    ncu figures are not measured by this run; a figure whose build differs
+    is reported only under its capture record."""
     import re
     from tpls_gb300.build import source_digest
     for f in sorted((ROOT / "profiles").glob("*.md")):
         for line in f.read_text().splitlines():
             m = re.match(r"(\S+) (\S+) (\S+): ([0-9.]+) build ([0-9a-f]+)", line.strip())
-            if m and m.group(1) == tag and m.group(2) == kernel and m.group(3) == workload:
+            if m and m.group(1) == tag and m.group(2) == kernel and workload in (None, m.group(3)):
                 return {"value": float(m.group(4)), "file": f"profiles/{f.name}", "build": m.group(5),
-                        "current": m.group(5) == source_digest()}
+                        "current": m.group(5) == source_digest(), "workload": m.group(3)}
     return None
 
 
@@ -272,7 +273,9 @@ def run_gpu(args, ws, rank, local) -> dict | None:
     achieved = per_launch_b / (avg_ms / 1e3) / 1e9
     wl = f"{nx}x{ny}x{nz}-{'fp64' if precision == 0 else 'mixed'}"
     traffic_cap = _profile_figure("traffic", dominant, wl)
-    fp64_cap = _profile_figure("fp64pipe", dominant, wl)
+    # FP64 pipe utilisation from a --set full capture (a smaller case of the
+    # same kernel: a full set is not captured at this size)
+    fp64_cap = _profile_figure("fp64pipe", dominant, None) if precision == 0 else None
     traffic = traffic_cap["value"] if traffic_cap and traffic_cap["current"] else None
     cpu = None
     if ws == 1 and not args.no_cpu_baseline:
