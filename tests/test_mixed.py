@@ -122,9 +122,10 @@ def test_tma_staged_advection_is_bit_identical():
     """The FP32 advection with its phi tiles staged by TMA (the default)
     against the same kernel reading phi through the caches
     (TPLS_FLAG_NO_TMA): same arithmetic, so the states are bit-identical,
-    on the 64x32x48 channel and on ragged grids (partial tiles at the x, y
-    and z ends, ny below the tile height); no block's wait ran out."""
-    for size in ((NX, NY, NZ), (37, 5, 23), (70, 19, 9)):
+    on the 64x32x48 channel, on ragged grids (partial tiles at the x, y and
+    z ends, ny below the tile height) and on a wide one (12 tiles in x, the
+    row pitch of the largest served grids); no block's wait ran out."""
+    for size in ((NX, NY, NZ), (37, 5, 23), (70, 19, 9), (384, 16, 24)):
         a = _ctx(1, size, fp64_parts=2)
         b = _ctx(1, size, fp64_parts=2, flags=TPLS_FLAG_NO_TMA)
         assert a.step(3) == 0 and b.step(3) == 0
