@@ -75,6 +75,10 @@ typedef struct tpls_params {
  * read phi through the caches instead of staging its tiles with TMA
  * (bit-identical results). */
 #define TPLS_FLAG_NO_TMA 1
+/* tpls_params.flags: TPLS_FLAG_ODD_COLUMNS makes the odd half-sweep of the
+ * FP64 coefficient records walk each column in one block instead of one
+ * block per 64-level segment chained up the column (bit-identical). */
+#define TPLS_FLAG_ODD_COLUMNS 2
 
 /* Interface method (main_ns_hybrid.F90:595-612, option_names.F90:35-37). */
 #define TPLS_IDM_LSM 0

@@ -32,6 +32,7 @@ TPLS_PREC_FP64 = 0
 TPLS_PREC_FP32_MIXED = 1
 PART_ADVECT, PART_LEVELSET, PART_MOMENTUM, PART_MULTIGRID, PART_MOM_STENCIL = 1, 2, 4, 8, 16
 TPLS_FLAG_NO_TMA = 1  # tpls_params.flags: advection without TMA-staged tiles
+TPLS_FLAG_ODD_COLUMNS = 2  # tpls_params.flags: odd half-sweep one block per column, not per segment
 
 # field ids (enum tpls_field)
 TIMERS = ["advect", "levelset", "csf", "visc", "mom_rhs", "jacobi", "sor_even", "sor_odd", "pressure", "project",

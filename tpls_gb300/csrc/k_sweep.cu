@@ -157,8 +157,133 @@ __global__ void __launch_bounds__(SW_X *SW_Y)
 // few ulp.
 constexpr int SOC_W = 8, SOC_SC = 64;
 
-// One tile: 32 columns (x pairs from bx*32) of row j = by+1.  Every thread
-// of the block runs it (it synchronises the block).
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ double ld_acquire_f64(const double *p) {
+  double v;
+  asm volatile("ld.acquire.gpu.global.f64 %0, [%1];" : "=d"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_u32(unsigned *p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Phases 1 and 2 of one super-chunk (levels kc .. kc+n-1) of a tile: A and B
+// of every (level, column) pair into sA/sB, then each warp's chunk scanned
+// in place (y and P), its ends into ey/ep.  Synchronises the block.
+template <typename T, typename CS>
+__device__ __forceinline__ void odd_produce_scan(int comp, const Geo &g, const CS &coef, const T *__restrict__ x,
+                                                 int i, int j, bool act, int k0, int kc, int n,
+                                                 T (*sA)[32], T (*sB)[32], T (*ey)[32], T (*ep)[32]) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int sy_ = g.sy, sz = g.sz, nz = g.nz;
+  constexpr int PER = SOC_SC / SOC_W;
+#pragma unroll 4
+  for (int r = 0; r < PER; r++) {
+    const int lk = w + r * SOC_W, k = kc + lk;
+    if (lk < n) {
+      T A = 0, B = 0;
+      if (act) {
+        const int c = TPLS_IDX(g, i, j, k);
+        const Rec<T> q = get_rec(comp, g, coef, c, i, j, k, true);
+        const T xc = x[c];
+        T zp;
+        if (comp == 2) zp = x[c + sz];
+        else zp = (k == nz - 1) ? xc : x[c + sz];
+        T part = fma(q.xp, x[c + 1], q.b);
+        part = fma(q.xm, x[c - 1], part);
+        part = fma(q.yp, x[c + sy_], part);
+        part = fma(q.ym, x[c - sy_], part);
+        part = fma(q.zp, zp, part);
+        if (k == k0) {  // the point below is a wall value (w) or the point itself (u, v)
+          const T zm = (comp == 2) ? x[c - sz] : xc;
+          A = xc + (T)1.2 * (fma(q.zm, zm, part) - xc);
+        } else {
+          A = xc + (T)1.2 * (part - xc);
+          B = (T)1.2 * q.zm;
+        }
+      }
+      sA[lk][lane] = A;
+      sB[lk][lane] = B;
+    }
+  }
+  __syncthreads();
+  const int lb = w * PER, le = min(n, lb + PER);
+  T yv = 0, pv = 1;
+  for (int lk = lb; lk < le; lk++) {
+    const T B = sB[lk][lane];
+    yv = fma(B, yv, sA[lk][lane]);
+    pv = B * pv;
+    sA[lk][lane] = yv;
+    sB[lk][lane] = pv;
+  }
+  ey[w][lane] = yv;  // an empty chunk passes x_in through (y 0, P 1)
+  ep[w][lane] = pv;
+  __syncthreads();
+}
+
+// x at the super-chunk's last level given the value entering it (what phase
+// 3 writes there, by the same operations); 0 for a column outside the grid.
+template <typename T>
+__device__ __forceinline__ T odd_last_value(T xin, int n, bool col_in, T (*sA)[32], T (*sB)[32], T (*ey)[32],
+                                            T (*ep)[32]) {
+  const int lane = threadIdx.x & 31;
+  constexpr int PER = SOC_SC / SOC_W;
+  const int wl = (n - 1) / PER;
+  for (int v = 0; v < wl; v++) xin = fma(ep[v][lane], xin, ey[v][lane]);
+  return col_in ? fma(sB[n - 1][lane], xin, sA[n - 1][lane]) : (T)0;
+}
+
+// Phase 3: each warp folds the chunk ends below its own into the value
+// entering the super-chunk and writes x = y + P x_in, then the boundary rows
+// of its levels.  Returns x at the super-chunk's last level for the warp
+// that owns it (0 elsewhere).
+template <typename T>
+__device__ __forceinline__ T odd_write(int comp, const Geo &g, const Helm &h, T *__restrict__ x,
+                                       const double *__restrict__ X, const double *__restrict__ P, int bc,
+                                       int fuse, int i2, int i, int j, int iend, int npair, int kc, int n, T xin,
+                                       T (*sA)[32], T (*sB)[32], T (*ey)[32], T (*ep)[32]) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  constexpr int PER = SOC_SC / SOC_W;
+  const int lb = w * PER, le = min(n, lb + PER);
+  T last = 0;
+  for (int v = 0; v < w; v++) xin = fma(ep[v][lane], xin, ey[v][lane]);
+  if (i2 < npair) {
+    for (int lk = lb; lk < le; lk++) {
+      T v = 0;
+      if (i <= iend) {
+        v = fma(sB[lk][lane], xin, sA[lk][lane]);
+        put(g, x, i, j, kc + lk, v, fuse);
+      }
+      sA[lk][lane] = v;  // kept for the boundary rows below
+      if (lk == n - 1) last = v;
+    }
+    // boundary rows of these levels, by the owners of the first and last
+    // pairs, after the writes: the point each boundary copies (relaxed
+    // here, or of the other colour and final) is loaded for all levels at
+    // once instead of level by level.  Nothing in this sweep reads the
+    // boundary values of these levels.
+    if (bc && (i2 == 0 || i2 == (iend - 1) / 2)) {
+      const int ib = (i2 == 0) ? 1 : iend;
+      T src[PER];
+#pragma unroll
+      for (int l = 0; l < PER; l++)
+        src[l] = (lb + l < le) ? ((i != ib) ? x[TPLS_IDX(g, ib, j, kc + lb + l)] : sA[lb + l][lane]) : (T)0;
+#pragma unroll
+      for (int l = 0; l < PER; l++)
+        if (lb + l < le) sor_bc(comp, g, h, x, X, P, i2, ib, iend, src[l], j, kc + lb + l, fuse);
+    }
+  }
+  return last;
+}
+
+// One tile: 32 columns (x pairs from bx*32) of row j = by+1, the whole
+// column.  Every thread of the block runs it (it synchronises the block).
+// The segment kernel below runs the same phases by the helpers above, one
+// super-chunk per block.
 template <typename T, typename CS, int CC>
 __device__ __forceinline__ void sor_odd_c4_tile(int comp_, const Geo &g, const Helm &h, T *__restrict__ x,
                                                 const CS &coef, const double *__restrict__ P,
@@ -258,6 +383,81 @@ __device__ __forceinline__ void sor_odd_c4_tile(int comp_, const Geo &g, const H
   }
 }
 
+// Odd half-sweep of the FP64 form with one block per super-chunk of a
+// tile (segment), so a launch has nz/64 times the blocks of the
+// whole-column form and the blocks' load, scan and write phases overlap.
+// The value entering a segment is the last value of the segment below it:
+// segments are taken in ticket order, lowest segment of every tile first,
+// so the block a segment waits for took its ticket earlier and is running;
+// it publishes that value (the same operations as the whole-column form,
+// so the results are bit-identical to it) as soon as it has its own
+// entering value, before it writes.  The wait is bounded: if it runs out
+// the block counts it in *kto, takes NaN as its entering value (the step's
+// pressure solve then reports DIVERGED_NAN) and still publishes, so no
+// later segment waits on it.
+template <typename T, typename CS, int CC>
+__global__ void __launch_bounds__(SOC_W * 32, 5)  // 48 registers: 5 blocks per SM
+    k_sor_odd_seg(int comp_, Geo g, Helm h, T *__restrict__ x, const CS coef, const double *__restrict__ P,
+                  const double *__restrict__ X, int flg, int bc, int fuse, OddChain oc, int gx, int limit) {
+  const int comp = (CC >= 0) ? CC : comp_;
+  __shared__ T sA[SOC_SC][32], sB[SOC_SC][32];
+  __shared__ T ey[SOC_W][32], ep[SOC_W][32], sxin[32];
+  __shared__ unsigned s_t, s_ep;
+  if (threadIdx.x == 0) {
+    s_t = atomicAdd(&oc.ctr[0], 1u);
+    s_ep = ld_acquire_u32(&oc.ctr[2]);
+  }
+  __syncthreads();
+  const unsigned t = s_t, epoch = s_ep;
+  const int nct = gx * g.ny;
+  const int seg = (int)(t / (unsigned)nct), ct = (int)(t - (unsigned)seg * nct);
+  const int bx = ct % gx, j = ct / gx + 1;
+  const int iend = (comp == 0) ? g.nx - 1 : g.nx;
+  const int npair = (iend + 1) / 2;
+  const int par = (j + flg) & 1;
+  const int k0 = (comp == 2) ? 1 : 0, k1 = g.nz - 1;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int i2 = bx * 32 + lane, i = 2 * i2 + 1 + par;
+  const bool act = (i2 < npair) && (i <= iend);
+  const int kc = k0 + seg * SOC_SC, n = min(SOC_SC, k1 - kc + 1);
+  odd_produce_scan<T, CS>(comp, g, coef, x, i, j, act, k0, kc, n, sA, sB, ey, ep);
+  if (w == 0) {
+    T xin = 0;  // k0 has B = 0
+    if (seg > 0) {
+      // every lane acquires the flag itself (one transaction per poll for
+      // the warp) before reading its column's value
+      const unsigned pt = t - (unsigned)nct;  // the segment below, same columns
+      bool ok = true;
+      int it = 0;
+      while (ld_acquire_u32(&oc.flag[pt]) != epoch + 1u)
+        if (++it >= limit) {
+          ok = false;
+          break;
+        }
+      xin = ok ? (T)ld_acquire_f64(&oc.incl[(size_t)pt * 32 + lane]) : (T)__longlong_as_double(0x7ff8000000000000ll);
+      if (__any_sync(0xffffffffu, !ok) && lane == 0) atomicAdd(oc.kto, 1.0);
+    }
+    if (seg < (k1 - k0) / SOC_SC) {  // a segment above waits for this one
+      oc.incl[(size_t)t * 32 + lane] = (double)odd_last_value<T>(xin, n, i2 < npair && i <= iend, sA, sB, ey, ep);
+      __threadfence();
+      __syncwarp();
+      if (lane == 0) st_release_u32(&oc.flag[t], epoch + 1u);
+    }
+    sxin[lane] = xin;
+  }
+  __syncthreads();
+  odd_write<T>(comp, g, h, x, X, P, bc, fuse, i2, i, j, iend, npair, kc, n, sxin[lane], sA, sB, ey, ep);
+  if (threadIdx.x == 0) {  // the last block to leave resets the tickets and starts a new epoch
+    __threadfence();
+    if (atomicAdd(&oc.ctr[1], 1u) == gridDim.x - 1) {
+      oc.ctr[0] = 0u;
+      oc.ctr[1] = 0u;
+      __threadfence();
+      atomicAdd(&oc.ctr[2], 1u);
+    }
+  }
+}
+
 template <typename T, typename CS, int CC>
 __global__ void __launch_bounds__(SOC_W * 32)
     k_sor_odd_c4(int comp_, Geo g, Helm h, T *__restrict__ x, const CS coef,
@@ -350,10 +550,15 @@ static void even_v(int comp, const Geo &g, const Helm &h, T *x, CS coef, const d
   k_sor_even_c<T, CS, CC, BX, BY><<<grd, dim3(BX, BY), 0, st>>>(comp, g, h, x, coef, pres, X, flg, bc, fuse);
 }
 
+int odd_chain_segments(const Geo &g) {
+  const int gx = (((g.nx + 1) / 2) + 31) / 32;  // v and w have the most pairs
+  return ((g.nz - 1) / SOC_SC + 1) * gx * g.ny;
+}
+
 template <typename T, typename CS, int CC>
 static cudaError_t sor_c(int comp, const Geo &g, const Phys &ph, T *x, CS coef, const double *pres,
                          const double *X, int flg, int iteration_time, int bc, int fuse, int tile_even,
-                         int tile_odd, cudaStream_t st) {
+                         int tile_odd, cudaStream_t st, const OddChain *oc = nullptr) {
   const int iend = (comp == 0) ? g.nx - 1 : g.nx;
   const int npairs = (iend + 1) / 2;
   const Helm h = helm_of(ph);
@@ -365,10 +570,21 @@ static cudaError_t sor_c(int comp, const Geo &g, const Phys &ph, T *x, CS coef, 
       default: even_v<T, CS, CC, 32, 4>(comp, g, h, x, coef, pres, X, flg, bc, fuse, st); break;
     }
   } else {
-    // one block per 32 columns of a row, the column in super-chunks
     (void)tile_odd;
-    dim3 grd((npairs + 31) / 32, g.ny, 1);
-    k_sor_odd_c4<T, CS, CC><<<grd, SOC_W * 32, 0, st>>>(comp, g, h, x, coef, pres, X, flg, bc, fuse);
+    const int gx = (npairs + 31) / 32;
+    const int k0 = (comp == 2) ? 1 : 0, nseg = (g.nz - 1 - k0) / SOC_SC + 1;
+    bool chained = false;
+    if constexpr (sizeof(T) == sizeof(double)) {
+      if (oc && oc->cap >= nseg * gx * g.ny) {  // one block per segment, chained
+        k_sor_odd_seg<T, CS, CC><<<nseg * gx * g.ny, SOC_W * 32, 0, st>>>(comp, g, h, x, coef, pres, X, flg, bc,
+                                                                         fuse, *oc, gx, 1 << 20);
+        chained = true;
+      }
+    }
+    if (!chained) {  // one block per 32 columns of a row, the column in super-chunks
+      dim3 grd(gx, g.ny, 1);
+      k_sor_odd_c4<T, CS, CC><<<grd, SOC_W * 32, 0, st>>>(comp, g, h, x, coef, pres, X, flg, bc, fuse);
+    }
   }
   return cudaGetLastError();
 }
@@ -396,9 +612,9 @@ cudaError_t launch_jacobi_c(int comp, const Geo &g, const Phys &ph, const float 
 }
 cudaError_t launch_sor_c(int comp, const Geo &g, const Phys &ph, double *x, const double *coef,
                          const double *pres, int flg, int iteration_time, int bc, int fuse, cudaStream_t st,
-                         const SweepTiles &t) {
+                         const SweepTiles &t, const OddChain *oc) {
   return sor_c<double, const double *, -1>(comp, g, ph, x, coef, pres, nullptr, flg, iteration_time, bc, fuse, t.even,
-                                          t.odd, st);
+                                          t.odd, st, oc);
 }
 cudaError_t launch_sor_c(int comp, const Geo &g, const Phys &ph, float *x, const MuCoef &coef,
                          const double *pres, const double *X, int flg, int iteration_time, int bc, int fuse,

@@ -101,6 +101,7 @@ struct tpls_ctx {
   double *stage = nullptr; // host-layout staging of one field ((nx+2)(ny+2)(nz+2))
   struct Xfer *xf = nullptr;  // batched host transfers (tpls_set_fields / tpls_get_fields)
   std::map<const double *, HostReg> hreg;  // registered host arrays by base address
+  OddChain odd;  // FP64 form: state of the segment-chained odd half-sweep
   alignas(64) unsigned char advmap[128];  // FP32-mixed: tensor map of phi32 for the TMA advection
   bool adv_tma = false;
   size_t n_p, n_uv, n_w;  // elements of each allocation (incl. pitch and padding)
@@ -172,6 +173,12 @@ struct PhaseScope {
   PhaseScope(tpls_ctx *c_, int slot_);
   ~PhaseScope();
 };
+
+// The odd half-sweep state for launch_sor_c: null walks each column in one
+// block (TPLS_FLAG_ODD_COLUMNS; the same results).
+static const OddChain *odd_chain(const tpls_ctx *c) {
+  return (c->odd.cap > 0 && !(c->prm.flags & TPLS_FLAG_ODD_COLUMNS)) ? &c->odd : nullptr;
+}
 
 static int nz_planes(int kind, int nz) { return kind == 0 ? nz + 2 : (kind == 1 ? nz : nz + 1); }
 
@@ -561,6 +568,21 @@ static int create_impl(int nx, int ny, int nz, const tpls_params *prm, const dou
     TCK(cudaMallocHost(&b, sizeof(double) * SC_N));
     c->scal_host = (double *)b;
   }
+  {  // state of the segment-chained odd half-sweep (FP64 coefficient records), zeroed
+    const int cap = odd_chain_segments(c->g);
+    const size_t nu = 4 + (size_t)cap;
+    void *b = nullptr;
+    TCK(cudaMalloc(&b, sizeof(unsigned) * nu));
+    c->allocs.push_back(b);
+    TCK(cudaMemsetAsync(b, 0, sizeof(unsigned) * nu, c->st));
+    c->odd.ctr = (unsigned *)b;
+    c->odd.flag = (unsigned *)b + 4;
+    TCK(cudaMalloc(&b, sizeof(double) * 32 * (size_t)cap));
+    c->allocs.push_back(b);
+    c->odd.incl = (double *)b;
+    c->odd.kto = c->scal + SC_KTO;
+    c->odd.cap = cap;
+  }
   TCK(poisson_create(c->g, 1.0 / (prm->dy * prm->dy), 1.0 / (prm->dx * prm->dx), 1.0 / (prm->dz * prm->dz),
                      c->mixed ? !(prm->fp64_parts & TPLS_PART_MULTIGRID) : (prm->mg_fp32 != 0), &c->ps));
   memset(&c->stats, 0, sizeof(c->stats));
@@ -612,6 +634,8 @@ long long tpls_footprint_bytes(int nx, int ny, int nz, int precision) {
   const size_t d2 = (size_t)diff2_blocks(g, nz + 1);
   if (d2 > part) part = d2;
   t += round_alloc(D * (part + FS_TAIL)) + round_alloc(D * SC_N);
+  const size_t oseg = (size_t)odd_chain_segments(g);  // odd half-sweep chain state
+  t += round_alloc(sizeof(unsigned) * (4 + oseg)) + round_alloc(D * 32 * oseg);
   t += poisson_footprint(g, precision == TPLS_PREC_FP32_MIXED, round_alloc);
   return (long long)t;
 }
@@ -941,7 +965,7 @@ static int momentum(tpls_ctx *c, int comp, CS coef, T **X, int max_iteration, co
   auto sor = [&](T *x, int flg, int it, int bc) {
     if constexpr (sizeof(T) == sizeof(float)) return launch_sor_c(comp, g, c->ph, x, coef, c->pres, base, flg, it,
                                                                    bc, fuse, c->st, tl);
-    else return launch_sor_c(comp, g, c->ph, x, coef, c->pres, flg, it, bc, fuse, c->st, tl);
+    else return launch_sor_c(comp, g, c->ph, x, coef, c->pres, flg, it, bc, fuse, c->st, tl, odd_chain(c));
   };
   const int N = max_iteration / 2;
   for (int it = 1; it <= N; it++) {
@@ -1453,7 +1477,7 @@ int tpls_autotune(tpls_ctx *c, int reps) {
     }
     double *a = c->x3[0][0], *b = c->x3[0][1];
     if (kind == 0) return launch_jacobi_c(0, g, c->ph, a, c->coef[0], c->pres, b, fuse, c->st, t);
-    return launch_sor_c(0, g, c->ph, b, c->coef[0], c->pres, 0, kind == 1 ? 2 : 1, 1, fuse, c->st, t);
+    return launch_sor_c(0, g, c->ph, b, c->coef[0], c->pres, 0, kind == 1 ? 2 : 1, 1, fuse, c->st, t, odd_chain(c));
   };
   SweepTiles best = c->tiles;
   // The odd half-sweep's chunking changes its rounding, so it is not tuned:

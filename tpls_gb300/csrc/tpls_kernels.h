@@ -154,6 +154,21 @@ struct SweepTiles {
   int jac = 0, even = 0, odd = 0;
 };
 
+// State of the segment-chained odd half-sweep of the FP64 form, one per
+// context (its launches are ordered on the context's stream): ticket,
+// finished-block and epoch counters; per segment (64 levels of 32 columns
+// of one row) a ready flag (epoch + 1) and the 32 values entering the
+// segment above it.  Zeroed at allocation.
+struct OddChain {
+  unsigned *ctr = nullptr;   // [0] tickets, [1] blocks done, [2] epoch
+  unsigned *flag = nullptr;  // per segment
+  double *incl = nullptr;    // per segment, 32 values
+  double *kto = nullptr;     // waits that ran out (a context scalar)
+  int cap = 0;               // segments the arrays hold
+};
+// Segments of the largest component's odd half-sweep on grid g.
+int odd_chain_segments(const Geo &g);
+
 // Sweeps on the per-point coefficient records written by launch_mom_rhs
 // (coef != null there): same updates and boundary rows as launch_jacobi /
 // launch_sor with bc = 1.
@@ -161,10 +176,13 @@ cudaError_t launch_jacobi_c(int comp, const Geo &g, const Phys &ph,
                             const double *xo, const double *coef,
                             const double *pres, double *x, int fuse_ghosts,
                             cudaStream_t st, const SweepTiles &t = SweepTiles());
+// oc: the context's segment-chained odd half-sweep state (null: one block
+// walks each column, the same results).
 cudaError_t launch_sor_c(int comp, const Geo &g, const Phys &ph, double *x,
                          const double *coef, const double *pres, int flg,
                          int iteration_time, int bc, int fuse_ghosts,
-                         cudaStream_t st, const SweepTiles &t = SweepTiles());
+                         cudaStream_t st, const SweepTiles &t = SweepTiles(),
+                         const OddChain *oc = nullptr);
 // FP32 sweeps in defect form: x holds d = x - X for the FP64 base X (the
 // component's state).  Their coefficients are recomputed per point from the
 // FP32 viscosity field (face averages and Helmholtz diagonal: a few dozen
