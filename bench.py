@@ -162,7 +162,7 @@ def _profile_figure(tag: str, kernel: str, workload: str | None) -> dict | None:
 
 def run_gpu(args, ws, rank, local) -> dict | None:
     import torch
-    from tpls_gb300.api import TPLS_FLAG_NO_TMA, TplsGpu
+    from tpls_gb300.api import TPLS_FLAG_NO_TMA, TPLS_FLAG_ODD_COLUMNS, TplsGpu
     from tpls_gb300.channel import WORKLOADS, make_case
 
     torch.cuda.set_device(local)
@@ -176,7 +176,9 @@ def run_gpu(args, ws, rank, local) -> dict | None:
     nx, ny, nz = args.grid if args.grid else (w.nx, w.ny, w.nz)
     params, uin, st = make_case(args.config, nx=nx, ny=ny, nz=nz, p_rtol=args.p_rtol, precision=precision,
                                 fp64_parts=parts, mg_fp32=1 if (precision == 0 and args.mg_fp32) else 0,
-                                idm=args.idm, pe=args.dim_pe, flags=TPLS_FLAG_NO_TMA if args.no_tma else 0)
+                                idm=args.idm, pe=args.dim_pe,
+                                flags=(TPLS_FLAG_NO_TMA if args.no_tma else 0)
+                                | (TPLS_FLAG_ODD_COLUMNS if args.odd_columns else 0))
     cells = nx * ny * nz
     g = TplsGpu(nx, ny, nz, params, uin)
     g.set_state(st)
@@ -267,7 +269,7 @@ def run_gpu(args, ws, rank, local) -> dict | None:
     # (k_sor_odd_c4), its launches timed with CUDA events on the library's
     # stream in the phase pass
     sor_ms, sor_l = phases["sor_odd"]
-    dominant = "k_sor_odd_c4"
+    dominant = "k_sor_odd_c4" if args.odd_columns else "k_sor_odd_seg"
     per_launch_b = sor_b / sor_n
     avg_ms = sor_ms / max(sor_l, 1)
     achieved = per_launch_b / (avg_ms / 1e3) / 1e9
@@ -299,6 +301,8 @@ def run_gpu(args, ws, rank, local) -> dict | None:
                    "precision": "fp64" if precision == 0 else "fp32-mixed",
                    "fp64_parts": parts,
                    "mg_fp32": params.mg_fp32,
+                   "odd_half_sweep": ("one block per column" if args.odd_columns
+                                      else "one block per 64-level segment, chained up the column"),
                    "advect_phi": ("read through the caches" if (args.no_tma or precision == 0)
                                   else "tiles staged by TMA (cp.async.bulk.tensor)"),
                    "idm": args.idm,
@@ -814,6 +818,9 @@ def main():
                     help="per-routine entries' cost per timestep, host arrays vs registered arrays (not a "
                          "bench line)")
     ap.add_argument("--routine-reps", type=int, default=3)
+    ap.add_argument("--odd-columns", action="store_true",
+                    help="odd half-sweep: one block walks each whole column instead of one block per 64-level "
+                         "segment chained up the column (tpls_params.flags = TPLS_FLAG_ODD_COLUMNS; bit-identical)")
     ap.add_argument("--no-tma", action="store_true",
                     help="FP32-mixed form: advection reads phi through the caches instead of TMA-staged tiles "
                          "(tpls_params.flags = TPLS_FLAG_NO_TMA; bit-identical)")

@@ -573,15 +573,10 @@ static cudaError_t sor_c(int comp, const Geo &g, const Phys &ph, T *x, CS coef, 
     (void)tile_odd;
     const int gx = (npairs + 31) / 32;
     const int k0 = (comp == 2) ? 1 : 0, nseg = (g.nz - 1 - k0) / SOC_SC + 1;
-    bool chained = false;
-    if constexpr (sizeof(T) == sizeof(double)) {
-      if (oc && oc->cap >= nseg * gx * g.ny) {  // one block per segment, chained
-        k_sor_odd_seg<T, CS, CC><<<nseg * gx * g.ny, SOC_W * 32, 0, st>>>(comp, g, h, x, coef, pres, X, flg, bc,
-                                                                         fuse, *oc, gx, 1 << 20);
-        chained = true;
-      }
-    }
-    if (!chained) {  // one block per 32 columns of a row, the column in super-chunks
+    if (oc && oc->cap >= nseg * gx * g.ny) {  // one block per segment, chained
+      k_sor_odd_seg<T, CS, CC><<<nseg * gx * g.ny, SOC_W * 32, 0, st>>>(comp, g, h, x, coef, pres, X, flg, bc,
+                                                                       fuse, *oc, gx, 1 << 20);
+    } else {  // one block per 32 columns of a row, the column in super-chunks
       dim3 grd(gx, g.ny, 1);
       k_sor_odd_c4<T, CS, CC><<<grd, SOC_W * 32, 0, st>>>(comp, g, h, x, coef, pres, X, flg, bc, fuse);
     }
@@ -618,14 +613,14 @@ cudaError_t launch_sor_c(int comp, const Geo &g, const Phys &ph, double *x, cons
 }
 cudaError_t launch_sor_c(int comp, const Geo &g, const Phys &ph, float *x, const MuCoef &coef,
                          const double *pres, const double *X, int flg, int iteration_time, int bc, int fuse,
-                         cudaStream_t st, const SweepTiles &t) {
+                         cudaStream_t st, const SweepTiles &t, const OddChain *oc) {
   if (iteration_time % 2 == 0)  // checkerboard half-sweep: four x points per thread (k_sweep32.cu)
     return launch_sweep4(1, comp, g, helm_of(ph), x, x, coef, pres, X, flg, bc, fuse, t.even, st);
   if (comp == 0)
-    return sor_c<float, MuCoef, 0>(comp, g, ph, x, coef, pres, X, flg, iteration_time, bc, fuse, t.even, t.odd, st);
+    return sor_c<float, MuCoef, 0>(comp, g, ph, x, coef, pres, X, flg, iteration_time, bc, fuse, t.even, t.odd, st, oc);
   if (comp == 1)
-    return sor_c<float, MuCoef, 1>(comp, g, ph, x, coef, pres, X, flg, iteration_time, bc, fuse, t.even, t.odd, st);
-  return sor_c<float, MuCoef, 2>(comp, g, ph, x, coef, pres, X, flg, iteration_time, bc, fuse, t.even, t.odd, st);
+    return sor_c<float, MuCoef, 1>(comp, g, ph, x, coef, pres, X, flg, iteration_time, bc, fuse, t.even, t.odd, st, oc);
+  return sor_c<float, MuCoef, 2>(comp, g, ph, x, coef, pres, X, flg, iteration_time, bc, fuse, t.even, t.odd, st, oc);
 }
 
 // defect form: d = -X before the first sweep (the sweeps start from x = 0),

@@ -964,7 +964,7 @@ static int momentum(tpls_ctx *c, int comp, CS coef, T **X, int max_iteration, co
   };
   auto sor = [&](T *x, int flg, int it, int bc) {
     if constexpr (sizeof(T) == sizeof(float)) return launch_sor_c(comp, g, c->ph, x, coef, c->pres, base, flg, it,
-                                                                   bc, fuse, c->st, tl);
+                                                                   bc, fuse, c->st, tl, odd_chain(c));
     else return launch_sor_c(comp, g, c->ph, x, coef, c->pres, flg, it, bc, fuse, c->st, tl, odd_chain(c));
   };
   const int N = max_iteration / 2;

@@ -215,7 +215,8 @@ cudaError_t launch_sor_c(int comp, const Geo &g, const Phys &ph, float *x,
                          const MuCoef &coef, const double *pres,
                          const double *X, int flg, int iteration_time, int bc,
                          int fuse_ghosts, cudaStream_t st,
-                         const SweepTiles &t = SweepTiles());
+                         const SweepTiles &t = SweepTiles(),
+                         const OddChain *oc = nullptr);
 // d = -X (n elements) / x = X + d
 cudaError_t launch_defect_init(const double *X, float *d, size_t n, cudaStream_t st);
 cudaError_t launch_defect_apply(const double *X, const float *d, double *x, size_t n,
