@@ -430,14 +430,16 @@ def run_batch(args, ws, rank, local) -> dict | None:
     if ws > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from tpls_gb300.api import TPLS_FLAG_ODD_COLUMNS
     precision = _precision(args)
     insts = draw_instances(args.instances)
     cells = sum(i.cells for i in insts)
+    fl = TPLS_FLAG_ODD_COLUMNS if args.odd_columns else 0
     # e2e: states uploaded from host, the batch run, states downloaded
     hosts = []
     members = []
     for inst in insts:
-        g = open_instance(inst, precision, tune=True)  # sweep tile shapes per grid (cached per shape)
+        g = open_instance(inst, precision, tune=True, flags=fl)  # sweep tile shapes per grid (cached per shape)
         hosts.append(g.get_state())
         members.append(g)
     # the other launch form of the same members, timed first for comparison
@@ -460,7 +462,7 @@ def run_batch(args, ws, rank, local) -> dict | None:
     small = None
     if args.small_instances > 0:  # many small grids, where per-launch overhead dominates
         sm_insts = draw_instances(args.small_instances, max_dims=(64, 32, 32))
-        sm_mem = [open_instance(i, precision, tune=True) for i in sm_insts]
+        sm_mem = [open_instance(i, precision, tune=True, flags=fl) for i in sm_insts]
         sm_st = [g.get_state() for g in sm_mem]
         sm_cells = sum(i.cells for i in sm_insts)
         t_br, t_mu = timed(False, sm_mem, sm_st, args.steps), timed(True, sm_mem, sm_st, args.steps)

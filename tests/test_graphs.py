@@ -135,13 +135,13 @@ def test_download_is_not_overwritten_by_the_next_steps():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("size", [(64, 32, 48), (37, 19, 150), (8, 6, 400)])
+@pytest.mark.parametrize("size", [(64, 32, 200), (37, 19, 150), (8, 6, 400)])
 def test_segment_chained_odd_sweep_is_bit_identical(size):
     """The odd half-sweep with one block per 64-level segment, each segment
-    taking the value entering it from the segment below (the default), and
-    with one block walking each whole column (TPLS_FLAG_ODD_COLUMNS): the
-    same operations, so the states are bit-identical; 1, 3 and 7 segments
-    per column; no wait ran out."""
+    taking the value entering it from the segment below (the default for
+    columns of 3 or more segments), and with one block walking each whole
+    column (TPLS_FLAG_ODD_COLUMNS): the same operations, so the states are
+    bit-identical; 4, 3 and 7 segments per column; no wait ran out."""
     from tpls_gb300.api import TPLS_FLAG_ODD_COLUMNS
     nx, ny, nz = size
     out = []

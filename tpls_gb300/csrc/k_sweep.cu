@@ -573,7 +573,11 @@ static cudaError_t sor_c(int comp, const Geo &g, const Phys &ph, T *x, CS coef, 
     (void)tile_odd;
     const int gx = (npairs + 31) / 32;
     const int k0 = (comp == 2) ? 1 : 0, nseg = (g.nz - 1 - k0) / SOC_SC + 1;
-    if (oc && oc->cap >= nseg * gx * g.ny) {  // one block per segment, chained
+    // one block per segment, chained, for columns of 3 or more segments:
+    // with 2, half the blocks wait on the other half for a larger share of
+    // their time than the extra blocks save (measured slower on the batched
+    // workload's grids, nz <= 128; faster at nz = 192 and 256)
+    if (oc && nseg >= 3 && oc->cap >= nseg * gx * g.ny) {
       k_sor_odd_seg<T, CS, CC><<<nseg * gx * g.ny, SOC_W * 32, 0, st>>>(comp, g, h, x, coef, pres, X, flg, bc,
                                                                        fuse, *oc, gx, 1 << 20);
     } else {  // one block per 32 columns of a row, the column in super-chunks
