@@ -269,7 +269,8 @@ def run_gpu(args, ws, rank, local) -> dict | None:
     # (k_sor_odd_c4), its launches timed with CUDA events on the library's
     # stream in the phase pass
     sor_ms, sor_l = phases["sor_odd"]
-    dominant = "k_sor_odd_c4" if args.odd_columns else "k_sor_odd_seg"
+    # (one block per 64-level segment for columns of 3 or more segments)
+    dominant = "k_sor_odd_seg" if (not args.odd_columns and (nz - 1) // 64 + 1 >= 3) else "k_sor_odd_c4"
     per_launch_b = sor_b / sor_n
     avg_ms = sor_ms / max(sor_l, 1)
     achieved = per_launch_b / (avg_ms / 1e3) / 1e9
@@ -301,8 +302,8 @@ def run_gpu(args, ws, rank, local) -> dict | None:
                    "precision": "fp64" if precision == 0 else "fp32-mixed",
                    "fp64_parts": parts,
                    "mg_fp32": params.mg_fp32,
-                   "odd_half_sweep": ("one block per column" if args.odd_columns
-                                      else "one block per 64-level segment, chained up the column"),
+                   "odd_half_sweep": ("one block per 64-level segment, chained up the column"
+                                      if dominant == "k_sor_odd_seg" else "one block per column"),
                    "advect_phi": ("read through the caches" if (args.no_tma or precision == 0)
                                   else "tiles staged by TMA (cp.async.bulk.tensor)"),
                    "idm": args.idm,
