@@ -244,13 +244,14 @@ def run_gpu(args, ws, rank, local) -> dict | None:
     e0.record(ext)
     for _ in range(ke):
         g.set_fields(host)  # the whole state from pinned host memory
-        if g.step(1) != 0:
-            raise SystemExit("tpls_step failed in the end-to-end region")
+        g.step_async(1)
         g.get_fields_into(host)  # and back; the next upload waits for it on the device
     g.xfer_join()
     e1.record(ext)
     torch.cuda.synchronize()
     g.sync()
+    if g.stats()["p_worst"] != 0:
+        raise SystemExit("a pressure solve failed in the end-to-end region")
     ems = e0.elapsed_time(e1)
     ems = max_over_ranks([ems], dist, "cuda")[0]
     e2e = replica_throughput(ws, cells * ke, ems)
@@ -315,9 +316,9 @@ def run_gpu(args, ws, rank, local) -> dict | None:
                    "grid_geometry": "cubic cells dx=dy=dz=1/nz (the reference's initialisation grid)",
                    "headline_metric": HEADLINE_METRIC},
         "e2e": {"value": e2e, "unit": "cell-steps/s", "h2d_bytes_per_step": bi, "d2h_bytes_per_step": bi,
-                "steps": ke, "path": f"tpls_set_fields ({len(state_fields)} fields) -> tpls_step(1) -> "
+                "steps": ke, "path": f"tpls_set_fields ({len(state_fields)} fields) -> tpls_step_async(1) -> "
                                      f"tpls_get_fields ({len(state_fields)} fields) per step, pinned host "
-                                     f"arrays"},
+                                     f"arrays, one wait after the last step"},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "kernel": dominant, "bytes_per_launch": per_launch_b,
                      "avg_launch_ms": avg_ms,

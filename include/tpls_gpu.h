@@ -153,9 +153,13 @@ int tpls_get_dims(const tpls_ctx *ctx, int *nx, int *ny, int *nz);
  * arrays on the host): fields[i] to / from host[i], in the layouts of
  * tpls_set_field / tpls_get_field, without a host wait between fields.
  * Downloads are 2-D copies from the device fields on one copy stream;
- * uploads go through two staging buffers (one allocated on the first call)
- * on another and are repacked on the context's stream, so successive
- * fields overlap.  An upload of an array still being downloaded, or into a
+ * right after a graph-launched step, the fields that step no longer writes
+ * after its front half (the level set, the CSF and convection histories)
+ * are copied as soon as that half is done, while the rest of the step
+ * runs.  Uploads go through staging buffers on another stream (as many as
+ * the call's fields, allocated on first use and not counted by
+ * tpls_footprint_bytes) and are repacked on the context's stream, so
+ * successive fields overlap.  An upload of an array still being downloaded, or into a
  * field still being downloaded, waits for that download on the device: a
  * get of the state followed by a set of the same arrays runs both copy
  * directions at once.  Both calls return once the copies are enqueued:

@@ -155,3 +155,32 @@ def test_segment_chained_odd_sweep_is_bit_identical(size):
         g.close()
     for k in out[0]:
         assert np.array_equal(out[0][k], out[1][k]), (size, k)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [0, 1])
+def test_download_after_async_step_reads_that_step(precision):
+    """tpls_get_fields enqueued right after tpls_step_async: the fields final
+    after the step's front are copied while its back still runs, the others
+    after it; all equal the state after that step, although two more steps
+    are enqueued before the host waits."""
+    nx, ny, nz = 64, 32, 48
+    kw = {"precision": precision, "fp64_parts": 2 if precision else 0}
+    params, uin, st = make_case("A", nx=nx, ny=ny, nz=nz, **kw)
+    ref = TplsGpu(nx, ny, nz, params, uin)
+    ref.set_state(st)
+    assert ref.step(2) == 0
+    want = ref.get_state()
+    ref.close()
+    g = TplsGpu(nx, ny, nz, params, uin)
+    g.set_state(st)
+    assert g.step(1) == 0
+    bufs = {k: np.zeros_like(v, order="F") for k, v in want.items()}
+    g.step_async(1)
+    g.get_fields_into(bufs)
+    g.step_async(2)
+    g.sync()
+    for k in want:
+        assert np.array_equal(bufs[k], want[k]), k
+    assert g.stats()["p_worst"] == 0
+    g.close()

@@ -42,11 +42,13 @@ using DevLock = std::lock_guard<std::recursive_mutex>;
 // Later work on the context's stream waits for pending downloads lazily
 // (xfer_fence), so those uploads do not queue behind them.
 struct Xfer {
-  static constexpr int K = 2;  // upload staging slots
   cudaStream_t h2d = nullptr, d2h = nullptr;
-  double *slot[K] = {nullptr, nullptr};
-  cudaEvent_t free_ev[K] = {nullptr, nullptr};   // the slot may be refilled
-  cudaEvent_t ready_ev[K] = {nullptr, nullptr};  // the slot holds its data
+  // upload staging slots: two at first, as many as the largest call's fields
+  // once a call has more, so every upload of a call can run before the
+  // context's stream reaches its repack
+  std::vector<double *> slot;
+  std::vector<cudaEvent_t> free_ev;   // the slot may be refilled
+  std::vector<cudaEvent_t> ready_ev;  // the slot holds its data
   cudaEvent_t st_ev = nullptr;                   // the context's stream at a download call
   cudaEvent_t d2h_last = nullptr;                // the last download enqueued
   cudaEvent_t field_dl[TPLS_F_COUNT] = {};       // the last download from each field
@@ -116,8 +118,14 @@ struct tpls_ctx {
   bool use_graphs = true;
   bool capturing = false;
   bool graph_pending = false;  // graph steps launched since the last stats read
+  // a step is two graph launches per history phase: the front (viscosity to
+  // the momentum right-hand sides) and the back (sweeps, pressure,
+  // projection); front_ev is recorded between them
   cudaGraphExec_t gexec[3] = {nullptr, nullptr, nullptr};
-  long g_static[3] = {0, 0, 0};  // kernels per launch outside the CG loop body
+  cudaGraphExec_t gexec_back[3] = {nullptr, nullptr, nullptr};
+  long g_static[3] = {0, 0, 0};  // kernels per step outside the CG loop body
+  cudaEvent_t front_ev = nullptr;
+  bool front_ok = false;  // front_ev marks the front of the last work on the stream
   long g_body = 0;               // kernels per CG iteration
   double its_accounted = 0.0;    // pressure iterations already counted in `launches`
   SweepTiles tiles;              // sweep tile shapes (tpls_autotune)
@@ -178,6 +186,24 @@ struct PhaseScope {
 // block (TPLS_FLAG_ODD_COLUMNS; the same results).
 static const OddChain *odd_chain(const tpls_ctx *c) {
   return (c->odd.cap > 0 && !(c->prm.flags & TPLS_FLAG_ODD_COLUMNS)) ? &c->odd : nullptr;
+}
+
+// State fields a step no longer writes after its front (step_front /
+// mixed_front): the level set, its advection histories, the CSF and
+// convection histories.  u2, v2, w2, pres, pres_old and the intermediates
+// change in the back.
+static bool front_final(int f) {
+  switch (f) {
+    case TPLS_F_PHI2:
+    case TPLS_F_CONV0_PHI: case TPLS_F_CONV1_PHI:
+    case TPLS_F_CONV0_U: case TPLS_F_CONV1_U: case TPLS_F_CONV0_V: case TPLS_F_CONV1_V:
+    case TPLS_F_CONV0_W: case TPLS_F_CONV1_W:
+    case TPLS_F_CSF_U0: case TPLS_F_CSF_U1: case TPLS_F_CSF_V0: case TPLS_F_CSF_V1:
+    case TPLS_F_CSF_W0: case TPLS_F_CSF_W1:
+      return true;
+    default:
+      return false;
+  }
 }
 
 static int nz_planes(int kind, int nz) { return kind == 0 ? nz + 2 : (kind == 1 ? nz : nz + 1); }
@@ -392,10 +418,10 @@ static void xfer_destroy(Xfer *x) {
   if (!x) return;
   if (x->h2d) cudaStreamSynchronize(x->h2d);
   if (x->d2h) cudaStreamSynchronize(x->d2h);
-  for (int q = 0; q < Xfer::K; q++) {
-    if (x->free_ev[q]) cudaEventDestroy(x->free_ev[q]);
-    if (x->ready_ev[q]) cudaEventDestroy(x->ready_ev[q]);
-  }
+  for (cudaEvent_t e : x->free_ev)
+    if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : x->ready_ev)
+    if (e) cudaEventDestroy(e);
   for (cudaEvent_t e : x->field_dl)
     if (e) cudaEventDestroy(e);
   for (auto &kv : x->host_done) cudaEventDestroy(kv.second);
@@ -416,6 +442,9 @@ int tpls_gpu_destroy(tpls_ctx *c) {
   for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
   for (cudaGraphExec_t ge : c->gexec)
     if (ge) cudaGraphExecDestroy(ge);
+  for (cudaGraphExec_t ge : c->gexec_back)
+    if (ge) cudaGraphExecDestroy(ge);
+  if (c->front_ev) cudaEventDestroy(c->front_ev);
   poisson_destroy(c->ps);
   for (auto &kv : c->hreg) cudaFree(kv.second.mirror);
   for (void *p : c->allocs) cudaFree(p);
@@ -440,6 +469,7 @@ static int create_impl(int nx, int ny, int nz, const tpls_params *prm, const dou
   c->g.sz = c->px * (ny + 2);
   c->g.szm = c->px * (ny + 4);
   TCK(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
+  TCK(cudaEventCreateWithFlags(&c->front_ev, cudaEventDisableTiming));
   TCK(sweep_init());
   c->mixed = (prm->precision == TPLS_PREC_FP32_MIXED);
   c->n_p = (size_t)c->px * (ny + 2) * (nz + 2) + 8;
@@ -699,6 +729,7 @@ int tpls_set_field(tpls_ctx *c, int f, const double *host) {
   double *d = field_ptr(c, f);
   if (!d) return TPLS_ERR_ARG;
   TCK(xfer_quiesce(c));
+  c->front_ok = false;  // the fields change after the last step's front
   TCK(h2d(c, d, host, nz_planes(field_kind(f), c->nz)));
   TCK(cudaStreamSynchronize(c->st));
   c->need_exchange = true;
@@ -715,6 +746,38 @@ int tpls_get_field(tpls_ctx *c, int f, double *host) {
   return TPLS_OK;
 }
 
+// Adds upload staging slots until there are n (the first is the context's
+// own staging buffer).
+static cudaError_t xfer_slots(tpls_ctx *c, Xfer *x, int n) {
+  if ((int)x->slot.size() >= n) return cudaSuccess;
+  DevLock lk(g_dev_mu);
+  const size_t len = (size_t)(c->nx + 2) * (c->ny + 2) * (c->nz + 2);
+  cudaError_t e = cudaSuccess;
+  while ((int)x->slot.size() < n && e == cudaSuccess) {
+    double *b = nullptr;
+    if (x->slot.empty()) {
+      b = c->stage;
+    } else {
+      void *v = nullptr;
+      e = cudaMalloc(&v, len * sizeof(double));
+      if (e != cudaSuccess) break;
+      c->allocs.push_back(v);
+      b = (double *)v;
+    }
+    cudaEvent_t fe = nullptr, re = nullptr;
+    e = cudaEventCreateWithFlags(&fe, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&re, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+      if (fe) cudaEventDestroy(fe);
+      break;
+    }
+    x->slot.push_back(b);
+    x->free_ev.push_back(fe);
+    x->ready_ev.push_back(re);
+  }
+  return e;
+}
+
 static cudaError_t xfer_init(tpls_ctx *c) {
   if (c->xf) return cudaSuccess;
   DevLock lk(g_dev_mu);
@@ -725,20 +788,7 @@ static cudaError_t xfer_init(tpls_ctx *c) {
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&x->st_ev, cudaEventDisableTiming);
   for (int f = 0; f < TPLS_F_COUNT && e == cudaSuccess; f++)
     e = cudaEventCreateWithFlags(&x->field_dl[f], cudaEventDisableTiming);
-  const size_t n = (size_t)(c->nx + 2) * (c->ny + 2) * (c->nz + 2);
-  x->slot[0] = c->stage;
-  for (int q = 0; q < Xfer::K && e == cudaSuccess; q++) {
-    if (!x->slot[q]) {
-      void *b = nullptr;
-      e = cudaMalloc(&b, n * sizeof(double));
-      if (e == cudaSuccess) {
-        c->allocs.push_back(b);
-        x->slot[q] = (double *)b;
-      }
-    }
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&x->free_ev[q], cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&x->ready_ev[q], cudaEventDisableTiming);
-  }
+  if (e == cudaSuccess) e = xfer_slots(c, x, 2);
   if (e != cudaSuccess) {
     xfer_destroy(x);
     return e;
@@ -753,11 +803,14 @@ int tpls_set_fields(tpls_ctx *c, int n, const int *fields, const double *const *
     if (!hosts[i] || fields[i] < 0 || fields[i] >= TPLS_F_COUNT || !field_ptr(c, fields[i])) return TPLS_ERR_ARG;
   TCK(xfer_init(c));
   Xfer *x = c->xf;
+  if (n > 0) c->front_ok = false;  // the fields change after the last step's front
+  TCK(xfer_slots(c, x, n));
+  const int K = (int)x->slot.size();
   for (int i = 0; i < n; i++) {
     const int f = fields[i], nzp = nz_planes(field_kind(f), c->nz);
     const int w = c->nx + 2, rows = (c->ny + 2) * nzp;
-    const int q = x->next;
-    x->next = (q + 1) % Xfer::K;
+    const int q = x->next % K;
+    x->next = (q + 1) % K;
     TCK(cudaStreamWaitEvent(x->h2d, x->free_ev[q], 0));
     auto hd = x->host_done.find(hosts[i]);  // a download into this array still in flight
     if (hd != x->host_done.end()) TCK(cudaStreamWaitEvent(x->h2d, hd->second, 0));
@@ -786,8 +839,22 @@ int tpls_get_fields(tpls_ctx *c, int n, const int *fields, double *const *hosts)
   }
   if (n == 0) return TPLS_OK;
   TCK(cudaEventRecord(x->st_ev, c->st));  // the fields as of this call
-  TCK(cudaStreamWaitEvent(x->d2h, x->st_ev, 0));
-  for (int i = 0; i < n; i++) {
+  // Right after a graph-launched step, the fields final after its front are
+  // copied first, as soon as the front is done (while the back runs); the
+  // others after all of the step.
+  std::vector<int> order;
+  order.reserve(n);
+  if (c->front_ok) {
+    TCK(cudaStreamWaitEvent(x->d2h, c->front_ev, 0));
+    for (int i = 0; i < n; i++)
+      if (front_final(fields[i])) order.push_back(i);
+  }
+  const size_t n_front = order.size();
+  for (int i = 0; i < n; i++)
+    if (!(c->front_ok && front_final(fields[i]))) order.push_back(i);
+  for (size_t o = 0; o < order.size(); o++) {
+    const int i = order[o];
+    if (o == n_front) TCK(cudaStreamWaitEvent(x->d2h, x->st_ev, 0));
     const int f = fields[i], nzp = nz_planes(field_kind(f), c->nz);
     const size_t w = (size_t)(c->nx + 2), rows = (size_t)(c->ny + 2) * nzp;
     TCK(cudaMemcpy2DAsync(hmap(c, hosts[i], w * rows), sizeof(double) * w, field_ptr(c, f),
@@ -1075,7 +1142,10 @@ static int dim_stage(tpls_ctx *c, const double *conv2_phi) {
   return TPLS_OK;
 }
 
-static int step_once(tpls_ctx *c) {
+// The front of a step: viscosity, advection, level set, CSF and the
+// momentum right-hand sides.  Every state field but u2, v2, w2, pres and
+// pres_old is final after it (front_final).
+static int step_front(tpls_ctx *c) {
   const Geo &g = c->g;
   const Phys &ph = c->ph;
   cudaStream_t st = c->st;
@@ -1131,6 +1201,14 @@ static int step_once(tpls_ctx *c) {
                           c->csf_w[s1], c->csf_w[s0], c->conv_w[s2], c->csf_w[s2], nullptr, nullptr, c->coef[2],
                           st));
   }
+  return TPLS_OK;
+}
+
+// The back of a step: momentum sweeps, pressure solve, projection.
+static int step_back(tpls_ctx *c) {
+  const Geo &g = c->g;
+  const Phys &ph = c->ph;
+  cudaStream_t st = c->st;
   // momentum sweeps (:756-887)
   int s;
   if ((s = momentum<double, const double *>(c, 0, c->coef[0], c->x3[0], c->prm.mom_u))) return s;
@@ -1155,6 +1233,11 @@ static int step_once(tpls_ctx *c) {
   }
   if (c->capturing) return TPLS_OK;
   return finish_eager(c, its, rn, bn, reason);
+}
+
+static int step_once(tpls_ctx *c) {
+  const int s = step_front(c);
+  return s ? s : step_back(c);
 }
 
 // FP32-mixed timestep: the same sequence as step_once with the stencils,
@@ -1318,40 +1401,62 @@ static int mixed_back(tpls_ctx *c) {
   return finish_eager(c, its, rn, bn, reason);
 }
 
-static int step_once_mixed(tpls_ctx *c) {
-  int s = mixed_front(c);
-  if (s) return s;
+static int step_back_mixed(tpls_ctx *c) {
+  int s;
   if (mixed_fp32_sweeps(c) && (s = sweeps32(c))) return s;
   return mixed_back(c);
 }
 
-// One step as a CUDA-graph launch; the graph of this history phase is
-// captured from the eager sequence on first use.
+static int step_once_mixed(tpls_ctx *c) {
+  const int s = mixed_front(c);
+  return s ? s : step_back_mixed(c);
+}
+
+// Captures one part of a step into an executable graph; *n: the kernels it
+// launches outside the CG loop body.
+static int capture_part(tpls_ctx *c, int (*part)(tpls_ctx *), cudaGraphExec_t *out, long *n) {
+  const long l0 = c->launches;
+  TCK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
+  c->capturing = true;
+  const int s = part(c);
+  c->capturing = false;
+  cudaGraph_t gr = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(c->st, &gr);
+  *n = c->launches - l0;
+  c->launches = l0;
+  if (s != TPLS_OK || e != cudaSuccess) {
+    if (gr) cudaGraphDestroy(gr);
+    return s != TPLS_OK ? s : TPLS_ERR_CUDA_BASE + (int)e;
+  }
+  const cudaError_t ei = cudaGraphInstantiate(out, gr, 0);
+  cudaGraphDestroy(gr);
+  TCK(ei);
+  return TPLS_OK;
+}
+
+// One step as two CUDA-graph launches (front, back) with front_ev recorded
+// between them, so the fields final after the front can be downloaded while
+// the back runs; the graphs of this history phase are captured from the
+// eager sequence on first use.
 static int step_graph(tpls_ctx *c) {
   int s = prologue(c);
   if (s) return s;
   const int ph = c->phase;
-  if (!c->gexec[ph]) {
+  if (!c->gexec[ph] || !c->gexec_back[ph]) {
     DevLock lk(g_dev_mu);
-    const long l0 = c->launches;
-    TCK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
-    c->capturing = true;
-    s = c->mixed ? step_once_mixed(c) : step_once(c);
-    c->capturing = false;
-    cudaGraph_t gr = nullptr;
-    const cudaError_t e = cudaStreamEndCapture(c->st, &gr);
-    const long n = c->launches - l0;
-    c->launches = l0;
-    if (s != TPLS_OK || e != cudaSuccess) {
-      if (gr) cudaGraphDestroy(gr);
-      return s != TPLS_OK ? s : TPLS_ERR_CUDA_BASE + (int)e;
+    long nf = 0, nb = 0;
+    if (!c->gexec[ph] && (s = capture_part(c, c->mixed ? mixed_front : step_front, &c->gexec[ph], &nf))) return s;
+    if ((s = capture_part(c, c->mixed ? step_back_mixed : step_back, &c->gexec_back[ph], &nb))) {
+      cudaGraphExecDestroy(c->gexec[ph]);
+      c->gexec[ph] = nullptr;
+      return s;
     }
-    const cudaError_t ei = cudaGraphInstantiate(&c->gexec[ph], gr, 0);
-    cudaGraphDestroy(gr);
-    TCK(ei);
-    c->g_static[ph] = n;
+    c->g_static[ph] = nf + nb;
   }
   TCK(cudaGraphLaunch(c->gexec[ph], c->st));
+  TCK(cudaEventRecord(c->front_ev, c->st));
+  TCK(cudaGraphLaunch(c->gexec_back[ph], c->st));
+  c->front_ok = true;
   c->launches += c->g_static[ph];
   c->phase = (ph + 1) % 3;
   c->stats.steps_done++;
@@ -1400,6 +1505,7 @@ int tpls_step(tpls_ctx *c, int nsteps) {
     return worst < 0 ? worst : TPLS_OK;
   }
   int worst = TPLS_OK;
+  c->front_ok = false;
   for (int n = 0; n < nsteps; n++) {
     int s = prologue(c);
     if (s) return s;
@@ -1443,11 +1549,17 @@ static void destroy_graphs(tpls_ctx *c) {
       cudaGraphExecDestroy(ge);
       ge = nullptr;
     }
+  for (cudaGraphExec_t &ge : c->gexec_back)
+    if (ge) {
+      cudaGraphExecDestroy(ge);
+      ge = nullptr;
+    }
 }
 
 int tpls_autotune(tpls_ctx *c, int reps) {
   if (!c || c->capturing || reps < 1) return TPLS_ERR_ARG;
   TCK(xfer_fence(c));
+  c->front_ok = false;
   const bool f32 = c->mixed && !(c->prm.fp64_parts & TPLS_PART_MOMENTUM);
   const std::array<int, 4> key = {c->nx, c->ny, c->nz, f32 ? 1 : 0};
   {
@@ -1769,6 +1881,7 @@ int tpls_batch_step_async(tpls_batch *b, int nsteps) {
     }
     for (int q = 0; q < n; q++) {  // host uploads: ghost rows, then order the member streams before the batch
       tpls_ctx *c = b->m[q];
+      c->front_ok = false;
       int s = prologue(c);
       if (s) return s;
       TCK(cudaEventRecord(b->join[q], c->st));
