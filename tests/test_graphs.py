@@ -184,3 +184,32 @@ def test_download_after_async_step_reads_that_step(precision):
         assert np.array_equal(bufs[k], want[k]), k
     assert g.stats()["p_worst"] == 0
     g.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [0, 1])
+def test_upload_during_the_back_of_a_step(precision):
+    """tpls_set_fields enqueued right after tpls_step_async: the fields final
+    after the step's front are written while its back still runs (that back
+    reads none of them), the others after it; the next steps start from the
+    uploaded state exactly as when it is loaded after a wait."""
+    nx, ny, nz = 37, 19, 23
+    kw = {"precision": precision, "fp64_parts": 2 if precision else 0}
+    params, uin, st = make_case("A", nx=nx, ny=ny, nz=nz, **kw)
+    out = []
+    for early in (True, False):
+        g = TplsGpu(nx, ny, nz, params, uin)
+        g.set_state(st)
+        assert g.step(1) == 0
+        if early:
+            g.step_async(1)
+            g.set_fields(st)
+        else:
+            assert g.step(1) == 0
+            g.sync()
+            g.set_state(st)  # field by field after a wait
+        assert g.step(2) == 0
+        out.append(g.get_state())
+        g.close()
+    for k in out[0]:
+        assert np.array_equal(out[0][k], out[1][k]), k

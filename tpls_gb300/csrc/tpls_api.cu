@@ -50,6 +50,7 @@ struct Xfer {
   std::vector<cudaEvent_t> free_ev;   // the slot may be refilled
   std::vector<cudaEvent_t> ready_ev;  // the slot holds its data
   cudaEvent_t st_ev = nullptr;                   // the context's stream at a download call
+  cudaEvent_t up_ev = nullptr;                   // the last repack on the upload stream
   cudaEvent_t d2h_last = nullptr;                // the last download enqueued
   cudaEvent_t field_dl[TPLS_F_COUNT] = {};       // the last download from each field
   bool dl_pending = false;                       // downloads the context's stream has not waited for
@@ -426,6 +427,7 @@ static void xfer_destroy(Xfer *x) {
     if (e) cudaEventDestroy(e);
   for (auto &kv : x->host_done) cudaEventDestroy(kv.second);
   if (x->st_ev) cudaEventDestroy(x->st_ev);
+  if (x->up_ev) cudaEventDestroy(x->up_ev);
   if (x->d2h_last) cudaEventDestroy(x->d2h_last);
   if (x->h2d) cudaStreamDestroy(x->h2d);
   if (x->d2h) cudaStreamDestroy(x->d2h);
@@ -786,6 +788,7 @@ static cudaError_t xfer_init(tpls_ctx *c) {
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&x->d2h, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&x->d2h_last, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&x->st_ev, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&x->up_ev, cudaEventDisableTiming);
   for (int f = 0; f < TPLS_F_COUNT && e == cudaSuccess; f++)
     e = cudaEventCreateWithFlags(&x->field_dl[f], cudaEventDisableTiming);
   if (e == cudaSuccess) e = xfer_slots(c, x, 2);
@@ -803,10 +806,26 @@ int tpls_set_fields(tpls_ctx *c, int n, const int *fields, const double *const *
     if (!hosts[i] || fields[i] < 0 || fields[i] >= TPLS_F_COUNT || !field_ptr(c, fields[i])) return TPLS_ERR_ARG;
   TCK(xfer_init(c));
   Xfer *x = c->xf;
-  if (n > 0) c->front_ok = false;  // the fields change after the last step's front
+  if (n == 0) return TPLS_OK;
+  // Right after a graph-launched step, the work still pending on the
+  // context's stream (the back of that step) touches none of the fields
+  // final after its front: those are uploaded first and repacked on the
+  // copy stream as soon as the front is done, the others repacked on the
+  // context's stream after the step.
+  const bool early = c->front_ok;
+  c->front_ok = false;  // the fields change after the last step's front
   TCK(xfer_slots(c, x, n));
   const int K = (int)x->slot.size();
-  for (int i = 0; i < n; i++) {
+  std::vector<int> order;
+  order.reserve(n);
+  for (int i = 0; i < n; i++)
+    if (early && front_final(fields[i])) order.push_back(i);
+  const size_t n_early = order.size();
+  for (int i = 0; i < n; i++)
+    if (!(early && front_final(fields[i]))) order.push_back(i);
+  if (n_early > 0) TCK(cudaStreamWaitEvent(x->h2d, c->front_ev, 0));
+  for (size_t o = 0; o < order.size(); o++) {
+    const int i = order[o];
     const int f = fields[i], nzp = nz_planes(field_kind(f), c->nz);
     const int w = c->nx + 2, rows = (c->ny + 2) * nzp;
     const int q = x->next % K;
@@ -816,13 +835,23 @@ int tpls_set_fields(tpls_ctx *c, int n, const int *fields, const double *const *
     if (hd != x->host_done.end()) TCK(cudaStreamWaitEvent(x->h2d, hd->second, 0));
     TCK(cudaMemcpyAsync(x->slot[q], hmap(c, hosts[i], (size_t)w * rows), sizeof(double) * (size_t)w * rows,
                         cudaMemcpyDefault, x->h2d));
-    TCK(cudaEventRecord(x->ready_ev[q], x->h2d));
-    TCK(cudaStreamWaitEvent(c->st, x->ready_ev[q], 0));
-    TCK(cudaStreamWaitEvent(c->st, x->field_dl[f], 0));  // a download from this field still in flight
-    LCK(c, repack(x->slot[q], w, field_ptr(c, f), c->px, w, rows, c->st));
-    TCK(cudaEventRecord(x->free_ev[q], c->st));
+    if (o < n_early) {
+      TCK(cudaStreamWaitEvent(x->h2d, x->field_dl[f], 0));  // a download from this field still in flight
+      LCK(c, repack(x->slot[q], w, field_ptr(c, f), c->px, w, rows, x->h2d));
+      TCK(cudaEventRecord(x->free_ev[q], x->h2d));
+    } else {
+      TCK(cudaEventRecord(x->ready_ev[q], x->h2d));
+      TCK(cudaStreamWaitEvent(c->st, x->ready_ev[q], 0));
+      TCK(cudaStreamWaitEvent(c->st, x->field_dl[f], 0));  // a download from this field still in flight
+      LCK(c, repack(x->slot[q], w, field_ptr(c, f), c->px, w, rows, c->st));
+      TCK(cudaEventRecord(x->free_ev[q], c->st));
+    }
   }
-  if (n > 0) c->need_exchange = true;
+  if (n_early > 0) {  // later work on the context's stream reads the early fields
+    TCK(cudaEventRecord(x->up_ev, x->h2d));
+    TCK(cudaStreamWaitEvent(c->st, x->up_ev, 0));
+  }
+  c->need_exchange = true;
   return TPLS_OK;
 }
 
