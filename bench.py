@@ -312,7 +312,8 @@ def run_gpu(args, ws, rank, local) -> dict | None:
                    "sweep_tiles": tiles,
                    "parallelism": f"{ws} independent replica(s), no sharding",
                    "l2": f"working set ~{cells * 500 / 1e9:.0f} GB per step >> 129 MB L2 (no flush needed)",
-                   "launch": "one CUDA graph per step (device-side WHILE node for the pressure CG)",
+                   "launch": "two CUDA-graph launches per step, front and back (device-side WHILE node for the "
+                             "pressure CG)",
                    "grid_geometry": "cubic cells dx=dy=dz=1/nz (the reference's initialisation grid)",
                    "headline_metric": HEADLINE_METRIC},
         "e2e": {"value": e2e, "unit": "cell-steps/s", "h2d_bytes_per_step": bi, "d2h_bytes_per_step": bi,
