@@ -72,6 +72,29 @@ __device__ __forceinline__ Rec<float> get_rec(int comp, const Geo &g, const MuCo
   return q;
 }
 
+// The per-routine entries' coefficients (sor_iteration_allflux.f90 on host
+// arrays): face viscosities of the FP64 viscosity_aug and the right-hand
+// side, divided by the Helmholtz diagonal, the wall rule folded into the z
+// slots as in the records.
+__device__ __forceinline__ Rec<double> get_rec(int comp, const Geo &g, const RefCoef &s, int c, int i, int j, int k,
+                                               bool) {
+  const FcT<double> f = faces<double>(comp, g, s.mu, i, j, k);
+  const double diag = 1.0 + s.ax2 * (f.px + f.mx) + s.ay2 * (f.py + f.my) + s.az2 * (f.pz + f.mz);
+  const double r = 1.0 / diag;
+  double czp = s.az2 * f.pz * r, czm = s.az2 * f.mz * r;
+  if (comp != 2) {
+    if (k == 0) {
+      czp += czm * (1.0 / 3.0);
+      czm = -2.0 * czm;
+    } else if (k == g.nz - 1) {
+      czm += czp * (1.0 / 3.0);
+      czp = -2.0 * czp;
+    }
+  }
+  Rec<double> q = {s.ax2 * f.px * r, s.ax2 * f.mx * r, s.ay2 * f.py * r, s.ay2 * f.my * r, czp, czm, s.rhs[c] * r};
+  return q;
+}
+
 // Jacobi: x = J(xo) on the component's interior with its boundary rows.
 template <typename T, typename CS, int CC, int SW_X, int SW_Y>
 __global__ void __launch_bounds__(SW_X *SW_Y)
@@ -396,7 +419,7 @@ __device__ __forceinline__ void sor_odd_c4_tile(int comp_, const Geo &g, const H
 // pressure solve then reports DIVERGED_NAN) and still publishes, so no
 // later segment waits on it.
 template <typename T, typename CS, int CC>
-__global__ void __launch_bounds__(SOC_W * 32, 5)  // 48 registers: 5 blocks per SM
+__global__ void __launch_bounds__(SOC_W * 32, sizeof(T) == 4 ? 6 : 5)  // 40 / 48 registers: 6 / 5 blocks per SM
     k_sor_odd_seg(int comp_, Geo g, Helm h, T *__restrict__ x, const CS coef, const double *__restrict__ P,
                   const double *__restrict__ X, int flg, int bc, int fuse, OddChain oc, int gx, int limit) {
   const int comp = (CC >= 0) ? CC : comp_;
@@ -586,6 +609,18 @@ static cudaError_t sor_c(int comp, const Geo &g, const Phys &ph, T *x, CS coef, 
     }
   }
   return cudaGetLastError();
+}
+
+cudaError_t launch_sor_ref_odd(int comp, const Geo &g, const Phys &ph, double *x, const double *rhs,
+                               const double *mu, int flg, cudaStream_t st, const OddChain *oc) {
+  const Helm h = helm_of(ph);
+  RefCoef r;
+  r.mu = mu;
+  r.rhs = rhs;
+  r.ax2 = h.ax2;
+  r.ay2 = h.ay2;
+  r.az2 = h.az2;
+  return sor_c<double, RefCoef, -1>(comp, g, ph, x, r, nullptr, nullptr, flg, 1, 0, 0, 0, 0, st, oc);
 }
 
 MuCoef mu_coef(const Phys &ph, const float *mu, const float *b, const float4 *bco) {

@@ -2417,7 +2417,10 @@ static int sor_entry(tpls_ctx *c, int comp, double *x3, const double *rhs, const
   TCK(h2d(c, X, x3, nzp));
   TCK(h2d(c, R, rhs, nzp));
   TCK(h2d_mu(c, c->scr_mu, va));
-  LCK(c, launch_sor(comp, c->g, ph, X, R, c->scr_mu, nullptr, *flg, *iteration_time, 0, 0, c->st));
+  if (*iteration_time % 2 == 0)
+    LCK(c, launch_sor(comp, c->g, ph, X, R, c->scr_mu, nullptr, *flg, *iteration_time, 0, 0, c->st));
+  else  // the column recurrence in chunks (as the step's sweeps), not one thread per column
+    LCK(c, launch_sor_ref_odd(comp, c->g, ph, X, R, c->scr_mu, *flg, c->st, odd_chain(c)));
   TCK(d2h(c, x3, X, nzp));
   TCK(cudaStreamSynchronize(c->st));
   return TPLS_OK;

@@ -169,6 +169,19 @@ struct OddChain {
 // Segments of the largest component's odd half-sweep on grid g.
 int odd_chain_segments(const Geo &g);
 
+// Coefficient source of the per-routine sweep entries: the FP64
+// viscosity_aug (device mu layout) and right-hand side of host arrays.
+struct RefCoef {
+  const double *mu;
+  const double *rhs;
+  double ax2, ay2, az2;
+};
+// Odd-iteration half-sweep (iteration_time odd) of the per-routine entries
+// in the chunk-parallel column form, no boundary rows, no ghost fusing (the
+// reference's do_sor_u/v/w leave those to the driver).
+cudaError_t launch_sor_ref_odd(int comp, const Geo &g, const Phys &ph, double *x, const double *rhs,
+                               const double *mu, int flg, cudaStream_t st, const OddChain *oc);
+
 // Sweeps on the per-point coefficient records written by launch_mom_rhs
 // (coef != null there): same updates and boundary rows as launch_jacobi /
 // launch_sor with bc = 1.
