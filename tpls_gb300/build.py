@@ -46,15 +46,48 @@ def _run(cmd: list[str]) -> None:
         sys.stderr.write(r.stdout + r.stderr)
 
 
+def _code_only(text: str) -> str:
+    """C/C++ source with its comments removed (string and character
+    literals kept) and every run of white space outside literals made one
+    space, so a comment or layout edit does not change the digest."""
+    out, i, n = [], 0, len(text)
+    while i < n:
+        ch = text[i]
+        if ch in "\"'":
+            j = i + 1
+            while j < n and text[j] != ch:
+                j += 2 if text[j] == "\\" else 1
+            out.append(text[i:j + 1])
+            i = j + 1
+        elif text.startswith("//", i):
+            j = text.find("\n", i)
+            i = n if j < 0 else j
+        elif text.startswith("/*", i):
+            j = text.find("*/", i + 2)
+            i = n if j < 0 else j + 2
+        elif ch.isspace():
+            j = i
+            while j < n and text[j].isspace():
+                j += 1
+            if out and out[-1] != " ":
+                out.append(" ")
+            i = j
+        else:
+            out.append(ch)
+            i += 1
+    return "".join(out)
+
+
 def source_digest() -> str:
-    """12 hex digits of SHA-256 over the CUDA sources, headers and build
-    flags: names the build an ncu capture was taken of."""
+    """12 hex digits of SHA-256 over the CUDA sources and headers (their
+    code, comments removed) and the build flags: names the build an ncu
+    capture was taken of."""
     import hashlib
     h = hashlib.sha256(" ".join(ARCH + NVCC_FLAGS[:-1]).encode())
     files = sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.cuh"))
     for f in files + [ROOT / "include" / "tpls_gpu.h"]:
         h.update(f.name.encode())
-        h.update(f.read_bytes())
+        h.update(_code_only(f.read_text()).encode())
     return h.hexdigest()[:12]
 
 

@@ -406,9 +406,11 @@ __device__ __forceinline__ void sor_odd_c4_tile(int comp_, const Geo &g, const H
   }
 }
 
-// Odd half-sweep of the FP64 form with one block per super-chunk of a
-// tile (segment), so a launch has nz/64 times the blocks of the
-// whole-column form and the blocks' load, scan and write phases overlap.
+// Odd half-sweep with one block per super-chunk of a tile (segment), for
+// columns of 3 or more segments (FP64 records, the FP32 sweeps and the
+// per-routine entries alike), so a launch has nz/64 times the blocks of
+// the whole-column form and the blocks' load, scan and write phases
+// overlap.
 // The value entering a segment is the last value of the segment below it:
 // segments are taken in ticket order, lowest segment of every tile first,
 // so the block a segment waits for took its ticket earlier and is running;
