@@ -181,7 +181,7 @@ def test_contexts_created_on_a_thread_while_steps_are_captured():
     every step succeeds."""
     import threading
     from tpls_gb300.batch import Instance, open_instance
-    stop = threading.Event()
+    stop, first = threading.Event(), threading.Event()
     errors, churned = [], []
 
     def churn():
@@ -191,12 +191,15 @@ def test_contexts_created_on_a_thread_while_steps_are_captured():
                 g = open_instance(Instance(100 + q, 96, 64, 48, 2.0, 1.0, 100.0, 0.05, 50 + q), q % 2)
                 g.close()
                 q += 1
+                first.set()
             churned.append(q)
         except Exception as e:  # reported on the main thread
             errors.append(e)
+            first.set()
 
     t = threading.Thread(target=churn)
     t.start()
+    first.wait(timeout=120)  # the churn is under way before the captures start
     try:
         for q in range(12):
             g = open_instance(Instance(q, 64, 32, 32, 2.0, 1.0, 100.0, 0.05, 7 + q), q % 2)
