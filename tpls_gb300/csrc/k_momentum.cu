@@ -132,14 +132,15 @@ __device__ __forceinline__ bool cd_valid(int comp, const Geo &g, int i, int k) {
 // the wall ghost rule `-2 x(0) + x(1)/3` (and its top mirror) is folded in:
 // at k = 0 the czm slot multiplies the point itself and czp absorbs czm/3;
 // at k = nz-1 the czp slot multiplies the point itself and czm absorbs
-// czp/3.  One 64-byte record per point: (cxp, cxm, cyp, cym, czp, czm, b, 0).
+// czp/3.  One 64-byte record per point: (cxp, cxm, cyp, cym, czp, czm, b,
+// 1.2 czm), the last the factor of the odd half-sweep's column recurrence.
 __device__ __forceinline__ void store_rec(double *rec, double a0, double a1, double a2, double a3, double a4,
                                           double a5, double a6) {
   double2 *o = reinterpret_cast<double2 *>(rec);
   o[0] = make_double2(a0, a1);
   o[1] = make_double2(a2, a3);
   o[2] = make_double2(a4, a5);
-  o[3] = make_double2(a6, 0.0);
+  o[3] = make_double2(a6, 1.2 * a5);
 }
 
 // The record of one point of the FP64 sweeps.

@@ -5,7 +5,8 @@
 //
 // k_mom_rhs writes, once per timestep, one record per point of a velocity
 // component: the six neighbour coefficients and rhs/diag, already divided
-// by the Helmholtz diagonal (see write_coef in k_momentum.cu).  A sweep
+// by the Helmholtz diagonal, and the odd half-sweep's factor 1.2 czm (see
+// write_coef in k_momentum.cu).  A sweep
 // point is then x_new = sum(c_n x_n) + b: seven FMAs instead of the face
 // averages, diagonal and division of the reference's form, evaluated once
 // per step instead of once per sweep: on GB300's FP64 pipe the 64-byte
@@ -19,9 +20,13 @@
 
 namespace tpls {
 
+// bz = 1.2 zm, the factor of the odd half-sweep's column recurrence.  The
+// FP64 records carry it in their eighth slot (written by k_mom_rhs by the
+// same multiplication, so the values are identical), loaded with b instead
+// of computed in every odd half-sweep on the FP64 pipe.
 template <typename T>
 struct Rec {
-  T xp, xm, yp, ym, zp, zm, b;
+  T xp, xm, yp, ym, zp, zm, b, bz;
 };
 
 // record of point c of the FP64 sweeps (8 doubles; `stream` = evict-first loads)
@@ -29,7 +34,7 @@ __device__ __forceinline__ Rec<double> load_rec(const double *__restrict__ coef,
   const double2 *r = reinterpret_cast<const double2 *>(coef + 8 * (size_t)c);
   const double2 a = stream ? __ldcs(r) : __ldg(r), b = stream ? __ldcs(r + 1) : __ldg(r + 1);
   const double2 d = stream ? __ldcs(r + 2) : __ldg(r + 2), e = stream ? __ldcs(r + 3) : __ldg(r + 3);
-  Rec<double> q = {a.x, a.y, b.x, b.y, d.x, d.y, e.x};
+  Rec<double> q = {a.x, a.y, b.x, b.y, d.x, d.y, e.x, e.y};
   return q;
 }
 
@@ -68,7 +73,7 @@ __device__ __forceinline__ Rec<float> get_rec(int comp, const Geo &g, const MuCo
   }
   const float *bp = s.b + rec_slot(g, c, i);
   Rec<float> q = {s.ax2 * f.px * r, s.ax2 * f.mx * r, s.ay2 * f.py * r, s.ay2 * f.my * r, czp, czm,
-                  stream ? __ldcs(bp) : __ldg(bp)};
+                  stream ? __ldcs(bp) : __ldg(bp), 1.2f * czm};
   return q;
 }
 
@@ -91,7 +96,7 @@ __device__ __forceinline__ Rec<double> get_rec(int comp, const Geo &g, const Ref
       czp = -2.0 * czp;
     }
   }
-  Rec<double> q = {s.ax2 * f.px * r, s.ax2 * f.mx * r, s.ay2 * f.py * r, s.ay2 * f.my * r, czp, czm, s.rhs[c] * r};
+  Rec<double> q = {s.ax2 * f.px * r, s.ax2 * f.mx * r, s.ay2 * f.py * r, s.ay2 * f.my * r, czp, czm, s.rhs[c] * r, 1.2 * czm};
   return q;
 }
 
@@ -196,11 +201,14 @@ __device__ __forceinline__ void st_release_u32(unsigned *p, unsigned v) {
 
 // Phases 1 and 2 of one super-chunk (levels kc .. kc+n-1) of a tile: A and B
 // of every (level, column) pair into sA/sB, then each warp's chunk scanned
-// in place (y and P), its ends into ey/ep.  Synchronises the block.
+// in place (y and P), its ends into ey/ep.  Synchronises the block.  The
+// form of the FP32 sweeps (latency-bound): a warp per level, all (level,
+// column) pairs independent so that their loads overlap.
 template <typename T, typename CS>
-__device__ __forceinline__ void odd_produce_scan(int comp, const Geo &g, const CS &coef, const T *__restrict__ x,
-                                                 int i, int j, bool act, int k0, int kc, int n,
-                                                 T (*sA)[32], T (*sB)[32], T (*ey)[32], T (*ep)[32]) {
+__device__ __forceinline__ void odd_produce_scan_levels(int comp, const Geo &g, const CS &coef,
+                                                        const T *__restrict__ x, int i, int j, bool act, int k0,
+                                                        int kc, int n, T (*sA)[32], T (*sB)[32], T (*ey)[32],
+                                                        T (*ep)[32]) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int sy_ = g.sy, sz = g.sz, nz = g.nz;
   constexpr int PER = SOC_SC / SOC_W;
@@ -248,6 +256,66 @@ __device__ __forceinline__ void odd_produce_scan(int comp, const Geo &g, const C
   __syncthreads();
 }
 
+// The same for the FP64 sweeps (bound by the FP64 pipe): each warp marches
+// up its own PER consecutive levels and steps its chunk's recurrence as it
+// goes, B read from the record (bz), the point above a level becoming the
+// next level's centre value, no block barrier between production and scan.
+// The operations per level and their order are those above, so both forms
+// give the results of the whole-column form bit for bit.  With B from the
+// record and the segment kernel's once-per-block fold, this form measured
+// 10% faster than the level form for the FP64 sweeps at 256x128x192 and
+// 11% slower for the FP32 sweeps at 512x256x256.
+template <typename T, typename CS>
+__device__ __forceinline__ void odd_produce_scan(int comp, const Geo &g, const CS &coef, const T *__restrict__ x,
+                                                 int i, int j, bool act, int k0, int kc, int n,
+                                                 T (*sA)[32], T (*sB)[32], T (*ey)[32], T (*ep)[32]) {
+  if constexpr (sizeof(T) == 4) {
+    odd_produce_scan_levels<T, CS>(comp, g, coef, x, i, j, act, k0, kc, n, sA, sB, ey, ep);
+  } else {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int sy_ = g.sy, sz = g.sz, nz = g.nz;
+    constexpr int PER = SOC_SC / SOC_W;
+    const int lb = w * PER, le = min(n, lb + PER);
+    T yv = 0, pv = 1;
+    int c = act ? TPLS_IDX(g, i, j, kc + lb) : 0;
+    T xc = (act && lb < le) ? x[c] : (T)0;
+#pragma unroll
+    for (int l = 0; l < PER; l++) {
+      const int lk = lb + l, k = kc + lk;
+      if (lk < le) {
+        T A = 0, B = 0;
+        if (act) {
+          const Rec<T> q = get_rec(comp, g, coef, c, i, j, k, true);
+          T zp;
+          if (comp == 2) zp = x[c + sz];
+          else zp = (k == nz - 1) ? xc : x[c + sz];
+          T part = fma(q.xp, x[c + 1], q.b);
+          part = fma(q.xm, x[c - 1], part);
+          part = fma(q.yp, x[c + sy_], part);
+          part = fma(q.ym, x[c - sy_], part);
+          part = fma(q.zp, zp, part);
+          if (k == k0) {
+            const T zm = (comp == 2) ? x[c - sz] : xc;
+            A = xc + (T)1.2 * (fma(q.zm, zm, part) - xc);
+          } else {
+            A = xc + (T)1.2 * (part - xc);
+            B = q.bz;
+          }
+          xc = zp;  // x(k+1), the centre of the next level (unused after k = nz-1)
+          c += sz;
+        }
+        yv = fma(B, yv, A);
+        pv = B * pv;
+        sA[lk][lane] = yv;
+        sB[lk][lane] = pv;
+      }
+    }
+    ey[w][lane] = yv;  // an empty chunk passes x_in through (y 0, P 1)
+    ep[w][lane] = pv;
+    __syncthreads();
+  }
+}
+
 // x at the super-chunk's last level given the value entering it (what phase
 // 3 writes there, by the same operations); 0 for a column outside the grid.
 template <typename T>
@@ -260,10 +328,11 @@ __device__ __forceinline__ T odd_last_value(T xin, int n, bool col_in, T (*sA)[3
   return col_in ? fma(sB[n - 1][lane], xin, sA[n - 1][lane]) : (T)0;
 }
 
-// Phase 3: each warp folds the chunk ends below its own into the value
-// entering the super-chunk and writes x = y + P x_in, then the boundary rows
-// of its levels.  Returns x at the super-chunk's last level for the warp
-// that owns it (0 elsewhere).
+// Phase 3: each warp writes x = y + P x_in from the value entering its own
+// chunk (given in xin for FP64; for FP32 xin enters the super-chunk and the
+// warp folds the chunk ends below its own into it first), then the
+// boundary rows of its levels.  Returns x at the super-chunk's last level
+// for the warp that owns it (0 elsewhere).
 template <typename T>
 __device__ __forceinline__ T odd_write(int comp, const Geo &g, const Helm &h, T *__restrict__ x,
                                        const double *__restrict__ X, const double *__restrict__ P, int bc,
@@ -273,7 +342,8 @@ __device__ __forceinline__ T odd_write(int comp, const Geo &g, const Helm &h, T 
   constexpr int PER = SOC_SC / SOC_W;
   const int lb = w * PER, le = min(n, lb + PER);
   T last = 0;
-  for (int v = 0; v < w; v++) xin = fma(ep[v][lane], xin, ey[v][lane]);
+  if constexpr (sizeof(T) == 4)
+    for (int v = 0; v < w; v++) xin = fma(ep[v][lane], xin, ey[v][lane]);
   if (i2 < npair) {
     for (int lk = lb; lk < le; lk++) {
       T v = 0;
@@ -351,7 +421,7 @@ __device__ __forceinline__ void sor_odd_c4_tile(int comp_, const Geo &g, const H
             A = xc + (T)1.2 * (fma(q.zm, zm, part) - xc);
           } else {
             A = xc + (T)1.2 * (part - xc);
-            B = (T)1.2 * q.zm;
+            B = (sizeof(T) == 8) ? q.bz : (T)1.2 * q.zm;
           }
         }
         sA[lk][lane] = A;
@@ -426,7 +496,8 @@ __global__ void __launch_bounds__(SOC_W * 32, sizeof(T) == 4 ? 6 : 5)  // 40 / 4
                   const double *__restrict__ X, int flg, int bc, int fuse, OddChain oc, int gx, int limit) {
   const int comp = (CC >= 0) ? CC : comp_;
   __shared__ T sA[SOC_SC][32], sB[SOC_SC][32];
-  __shared__ T ey[SOC_W][32], ep[SOC_W][32], sxin[32];
+  // the value entering each warp's chunk (FP64), or the segment's (FP32)
+  __shared__ T ey[SOC_W][32], ep[SOC_W][32], sxin[sizeof(T) == 8 ? SOC_W : 1][32];
   __shared__ unsigned s_t, s_ep;
   if (threadIdx.x == 0) {
     s_t = atomicAdd(&oc.ctr[0], 1u);
@@ -445,6 +516,7 @@ __global__ void __launch_bounds__(SOC_W * 32, sizeof(T) == 4 ? 6 : 5)  // 40 / 4
   const int i2 = bx * 32 + lane, i = 2 * i2 + 1 + par;
   const bool act = (i2 < npair) && (i <= iend);
   const int kc = k0 + seg * SOC_SC, n = min(SOC_SC, k1 - kc + 1);
+  constexpr int PER = SOC_SC / SOC_W;
   odd_produce_scan<T, CS>(comp, g, coef, x, i, j, act, k0, kc, n, sA, sB, ey, ep);
   if (w == 0) {
     T xin = 0;  // k0 has B = 0
@@ -462,16 +534,35 @@ __global__ void __launch_bounds__(SOC_W * 32, sizeof(T) == 4 ? 6 : 5)  // 40 / 4
       xin = ok ? (T)ld_acquire_f64(&oc.incl[(size_t)pt * 32 + lane]) : (T)__longlong_as_double(0x7ff8000000000000ll);
       if (__any_sync(0xffffffffu, !ok) && lane == 0) atomicAdd(oc.kto, 1.0);
     }
-    if (seg < (k1 - k0) / SOC_SC) {  // a segment above waits for this one
-      oc.incl[(size_t)t * 32 + lane] = (double)odd_last_value<T>(xin, n, i2 < npair && i <= iend, sA, sB, ey, ep);
-      __threadfence();
-      __syncwarp();
-      if (lane == 0) st_release_u32(&oc.flag[t], epoch + 1u);
+    if constexpr (sizeof(T) == 8) {
+      // FP64: the value entering every warp's chunk, the chunk ends below
+      // it folded in order, once for the block instead of once per warp
+      T xw = xin;
+#pragma unroll
+      for (int v = 0; v < SOC_W; v++) {
+        sxin[v][lane] = xw;
+        if (v + 1 < SOC_W) xw = fma(ep[v][lane], xw, ey[v][lane]);
+      }
+      if (seg < (k1 - k0) / SOC_SC) {  // a segment above waits for this one
+        oc.incl[(size_t)t * 32 + lane] =
+            act ? fma(sB[n - 1][lane], sxin[(n - 1) / PER][lane], sA[n - 1][lane]) : (T)0;
+        __threadfence();
+        __syncwarp();
+        if (lane == 0) st_release_u32(&oc.flag[t], epoch + 1u);
+      }
+    } else {
+      if (seg < (k1 - k0) / SOC_SC) {  // a segment above waits for this one
+        oc.incl[(size_t)t * 32 + lane] = (double)odd_last_value<T>(xin, n, i2 < npair && i <= iend, sA, sB, ey, ep);
+        __threadfence();
+        __syncwarp();
+        if (lane == 0) st_release_u32(&oc.flag[t], epoch + 1u);
+      }
+      sxin[0][lane] = xin;
     }
-    sxin[lane] = xin;
   }
   __syncthreads();
-  odd_write<T>(comp, g, h, x, X, P, bc, fuse, i2, i, j, iend, npair, kc, n, sxin[lane], sA, sB, ey, ep);
+  odd_write<T>(comp, g, h, x, X, P, bc, fuse, i2, i, j, iend, npair, kc, n, sxin[sizeof(T) == 8 ? w : 0][lane], sA,
+               sB, ey, ep);
   if (threadIdx.x == 0) {  // the last block to leave resets the tickets and starts a new epoch
     __threadfence();
     if (atomicAdd(&oc.ctr[1], 1u) == gridDim.x - 1) {
