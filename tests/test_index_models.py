@@ -9,7 +9,9 @@ before the kernels first ran:
 * k_sor_odd_seg (csrc/k_sweep.cu): segments decode to valid (row, column
   tile, level range), every segment a block waits for exists, holds an
   earlier ticket and publishes its value, and the launch fits the context's
-  chain arrays (odd_chain_segments).
+  chain arrays (odd_chain_segments);
+* k_sor_odd_seg<double>'s marching production phase reads the same x
+  points and records as the level-per-warp form it replaced.
 
 The models restate the kernels' index arithmetic line by line."""
 import pytest
@@ -91,3 +93,60 @@ def test_segment_chain_waits_on_earlier_publishing_segments(size):
             if seg < (k1 - k0) // SOC_SC:
                 published.add(t)
         assert max(published, default=-1) < cap
+
+
+def _odd_reads(nx, ny, nz, comp, march):
+    """Global reads of one odd half-sweep's production phase over every
+    segment of every column tile: the x points (column, row, level) and the
+    record slots (level of a record read), for the level-per-warp form
+    (march False) or the FP64 marching form; also checks the shared-memory
+    rows each form writes stay inside the 64-level segment."""
+    SOC_W = 8
+    PER = SOC_SC // SOC_W
+    iend = nx - 1 if comp == 0 else nx
+    npair = (iend + 1) // 2
+    k0, k1 = (1 if comp == 2 else 0), nz - 1
+    xs, recs = set(), set()
+    for j in range(1, ny + 1):
+        par = (j + 1) & 1  # flg = 1; the other parity only shifts i
+        for i2 in range(npair):
+            i = 2 * i2 + 1 + par
+            if i > iend:
+                continue
+            for kc in range(k0, k1 + 1, SOC_SC):
+                n = min(SOC_SC, k1 - kc + 1)
+                for w in range(SOC_W):
+                    if march:
+                        lb, le = w * PER, min(n, w * PER + PER)
+                        levels = list(range(lb, le))
+                        if levels:
+                            xs.add((i, j, kc + lb))  # the first centre value
+                    else:
+                        levels = [w + r * SOC_W for r in range(PER) if w + r * SOC_W < n]
+                    for lk in levels:
+                        assert 0 <= lk < SOC_SC
+                        k = kc + lk
+                        recs.add((i, j, k))
+                        if not march:
+                            xs.add((i, j, k))
+                        if comp == 2 or k != nz - 1:
+                            xs.add((i, j, k + 1))
+                        xs.update({(i + 1, j, k), (i - 1, j, k), (i, j + 1, k), (i, j - 1, k)})
+                        if k == k0 and comp == 2:
+                            xs.add((i, j, k - 1))
+    return xs, recs
+
+
+@pytest.mark.parametrize("size", [(16, 6, 192), (13, 5, 150), (8, 3, 64), (9, 4, 200), (6, 3, 65)])
+@pytest.mark.parametrize("comp", [0, 1, 2])
+def test_fp64_marching_odd_sweep_reads_what_the_level_form_reads(size, comp):
+    """k_sor_odd_seg<double>'s marching production (each warp walks its own
+    8 levels, the point above a level reused as the next centre value)
+    reads exactly the x points and records of the level-per-warp form, so
+    it reads nothing the earlier form did not."""
+    nx, ny, nz = size
+    xs_l, recs_l = _odd_reads(nx, ny, nz, comp, False)
+    xs_m, recs_m = _odd_reads(nx, ny, nz, comp, True)
+    assert recs_m == recs_l
+    assert xs_m == xs_l
+    assert all(0 <= p[2] <= nz for p in xs_m)
